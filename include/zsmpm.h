@@ -1,0 +1,170 @@
+/*
+ * zsmpm -- GB300 (sm_103a) MLS-MPM substep behind a plain C ABI.
+ *
+ * Drop-in boundary for the CuLagrange MPM nodes of zenustech/zeno.  Every
+ * entry point takes plain pointers and sizes and returns an int32 status
+ * (mpm_status); mpm_last_error() gives the text of the last failure on the
+ * calling thread.  Host pointers are AoS as in zeno's PrimitiveObject / the
+ * reference TileVector channels: x, v are n x 3 floats, C and F are n x 3 x 3
+ * row-major floats (F[9*i + 3*r + c]).
+ *
+ * Stage entry points mirror the reference node sequence of one substep
+ * (paths relative to the zenustech/zeno tree):
+ *   mpm_partition       ZSPartitionForZSParticles  projects/CuLagrange/mpm/MPMPipeline.cu:21-112
+ *                       + ExpandZSPartition        projects/CuLagrange/mpm/MPMPipeline.cu:121-231
+ *   mpm_grid_clear      ZSGridFromZSPartition      projects/CuLagrange/mpm/MPMPipeline.cu:241-267
+ *   mpm_p2g             ZSParticleToZSGrid         projects/CuLagrange/mpm/Transfer.cu:985-1060
+ *   mpm_grid_update     UpdateZSGrid               projects/CuLagrange/mpm/MPMPipeline.cu:828-940
+ *   mpm_apply_boundary  ApplyBoundaryOnZSGrid      projects/CuLagrange/mpm/Boundary.cu:83-163
+ *   mpm_g2p             ZSGridToZSParticle         projects/CuLagrange/mpm/Transfer.cu:1069-1173
+ *   mpm_return_mapping  ZSReturnMapping            projects/CuLagrange/mpm/MPMPipeline.cu:953-1138
+ * and mpm_substep runs the whole sequence on the device (CUDA graph, no host
+ * synchronisation), the additive fused node ZSMPMSubstep.
+ *
+ * Threading: a context is used by one host thread at a time (the reference
+ * graph runs nodes serially, zeno/src/core/Graph.cpp:81-95).  All work is
+ * ordered on the context's stream.
+ */
+#ifndef ZSMPM_H
+#define ZSMPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZSMPM_ABI_VERSION 1
+
+typedef enum mpm_status {
+  MPM_OK = 0,
+  MPM_ERR_INVALID = 1,       /* bad argument or unsupported option */
+  MPM_ERR_CUDA = 2,          /* CUDA runtime error (text in mpm_last_error) */
+  MPM_ERR_CAPACITY = 3,      /* more particles / grid blocks than allocated */
+  MPM_ERR_OUT_OF_DOMAIN = 4, /* a particle left the block directory */
+  MPM_ERR_CFL = 5,           /* a particle moved too far in one substep */
+  MPM_ERR_NAN = 6,           /* non-finite state or inverted element */
+  MPM_ERR_TIMEOUT = 7,       /* a bounded device-side wait gave up */
+  MPM_ERR_NO_DEVICE = 8,     /* no CUDA device / wrong architecture */
+  MPM_ERR_STATE = 9          /* call out of order (e.g. p2g before partition) */
+} mpm_status;
+
+/* elastic models: ConfigConstitutiveModel "type" (Generation.cu:40-51), plus
+ * the equation-of-state fluid, which the reference nodes do not expose. */
+enum { MPM_FCR = 0, MPM_NHK = 1, MPM_STVK = 2, MPM_EOS = 3 };
+/* plasticity: ConfigConstitutiveModel "plasticity" (Generation.cu:66-84) */
+enum { MPM_PLASTIC_NONE = 0, MPM_PLASTIC_NADP = 1 };
+/* collider types: ToZSBoundary "type" (Generation.cu:1601-1611) */
+enum { MPM_BC_NONE = 0, MPM_BC_STICKY = 1, MPM_BC_SLIP = 2, MPM_BC_SEPARATE = 3 };
+
+/* Material of ConfigConstitutiveModel (Generation.cu:18-103): E, nu ->
+ * Lame parameters; Drucker-Prager friction angle in degrees; bulk modulus
+ * and exponent of the equation-of-state fluid. */
+typedef struct mpm_material {
+  int32_t type;
+  int32_t plasticity;
+  float E, nu, density;
+  float friction_angle_deg;
+  float bulk, gamma;
+} mpm_material;
+
+/* Analytic box collider standing in for ToZSBoundary's level set
+ * (Generation.cu:1597-1647): walls of `thickness` cells inside the node-index
+ * box [lo, hi] on every axis, static (collider velocity 0). */
+typedef struct mpm_boundary {
+  int32_t type;
+  int32_t thickness;
+  int32_t lo[3];
+  int32_t hi[3];
+} mpm_boundary;
+
+/* Context = MakeZSGrid + MakeZSPartition + the particle store
+ * (Generation.cu:1470-1512, Generation.cpp:690-1145).  The sparse grid of
+ * 4^3-cell blocks lives inside a block directory: block coordinates
+ * [block_lo, block_lo + block_dims) on each axis; particles must stay at
+ * least one block inside it. */
+typedef struct mpm_ctx_desc {
+  int32_t device;          /* CUDA device ordinal */
+  float dx;                /* MakeZSGrid "dx" */
+  int32_t block_lo[3];
+  int32_t block_dims[3];
+  int64_t max_particles;
+  int32_t max_grid_blocks; /* 0: derived from max_particles and the directory */
+  int32_t flags;           /* reserved, 0 */
+} mpm_ctx_desc;
+
+typedef struct mpm_stats {
+  int64_t n_particles;
+  int32_t n_particle_blocks; /* non-empty 4^3 particle blocks of the last partition */
+  int32_t n_grid_blocks;     /* grid blocks after the 1-ring halo */
+  float max_vel_sqr;         /* UpdateZSGrid "MaxVelSqr" of the last grid update */
+  int32_t status;            /* first device-side error (mpm_status) since the last clear */
+  int64_t substeps;          /* substeps run since the particles were uploaded */
+} mpm_stats;
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* version of this ABI (ZSMPM_ABI_VERSION) */
+int32_t mpm_abi_version(void);
+
+/* text of the last error on this thread ("" if none) */
+const char *mpm_last_error(void);
+
+int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out);
+int32_t mpm_ctx_destroy(mpm_ctx *ctx);
+
+/* Order the context's work after / before other work on `stream`
+ * (a cudaStream_t; NULL restores the context's own stream). */
+int32_t mpm_set_stream(mpm_ctx *ctx, void *stream);
+
+/* ConfigConstitutiveModel: material table indexed by the per-particle id. */
+int32_t mpm_set_materials(mpm_ctx *ctx, const mpm_material *mats, int32_t n);
+/* ToZSBoundary + ApplyBoundaryOnZSGrid collider */
+int32_t mpm_set_boundary(mpm_ctx *ctx, const mpm_boundary *bc);
+/* UpdateZSGrid "gravity" / "Accel" inputs (MPMPipeline.cu:838-846) */
+int32_t mpm_set_gravity(mpm_ctx *ctx, float gx, float gy, float gz);
+
+/* ToZSParticles (Generation.cpp:690-1145): host arrays -> device store.
+ * NULL optional arrays take the reference defaults: v = 0, C = 0, F = I,
+ * J = 1.  mu / lam are the per-particle overrides added by
+ * AdjustParticleMaterial (Temp.cu:16-56); both NULL or both set. */
+int32_t mpm_particles_upload(mpm_ctx *ctx, int64_t n, const float *x, const float *v,
+                             const float *C, const float *F, const float *J,
+                             const float *m, const float *vol, const int32_t *mat,
+                             const float *mu, const float *lam);
+/* UpdatePrimitiveFromZSParticles (Generation.cu:1088-1158): device store ->
+ * host arrays in the upload order; NULL skips a channel. */
+int32_t mpm_particles_download(mpm_ctx *ctx, float *x, float *v, float *C, float *F, float *J);
+
+/* Stage entry points (one reference node each). */
+int32_t mpm_partition(mpm_ctx *ctx);
+int32_t mpm_grid_clear(mpm_ctx *ctx);
+int32_t mpm_p2g(mpm_ctx *ctx, float dt);
+/* max_vel_sqr: host pointer that receives MaxVelSqr (synchronises), or NULL */
+int32_t mpm_grid_update(mpm_ctx *ctx, float dt, float *max_vel_sqr);
+int32_t mpm_apply_boundary(mpm_ctx *ctx);
+int32_t mpm_g2p(mpm_ctx *ctx, float dt);
+int32_t mpm_return_mapping(mpm_ctx *ctx);
+
+/* n_substeps full substeps (partition, clear, P2G, grid update + boundary,
+ * G2P + return mapping) without host synchronisation. */
+int32_t mpm_substep(mpm_ctx *ctx, float dt, int32_t n_substeps);
+
+/* Wait for the context's stream; returns the device status word. */
+int32_t mpm_sync(mpm_ctx *ctx);
+int32_t mpm_get_stats(mpm_ctx *ctx, mpm_stats *out);
+
+/* Inspection of the last partition (bit-exact tests): sorted directory
+ * index and particle count of every non-empty particle block, the particle
+ * permutation (sorted position -> index in upload order) and the sorted
+ * directory index of every grid block. */
+int32_t mpm_partition_download(mpm_ctx *ctx, int32_t *n_pb, int32_t *pb_dir, int32_t *pb_count,
+                               int64_t cap_pb, int32_t *perm, int32_t *n_gb, int32_t *gb_dir,
+                               int64_t cap_gb);
+/* Grid nodes of the last partition: n_grid_blocks x 64 x (m, v0, v1, v2). */
+int32_t mpm_grid_download(mpm_ctx *ctx, float *nodes, int64_t cap_floats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

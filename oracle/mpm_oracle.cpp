@@ -1,0 +1,650 @@
+// CPU oracle for the CuLagrange MLS-MPM substep -- TEST INFRASTRUCTURE ONLY.
+//
+// The GPU product never links or calls this file.  It is the checker used by
+// tests/, by the smoke check and by the CPU legs of bench.py.  Templated on
+// the real type: the double build is the physics oracle (order-stable
+// scatter: particle blocks are processed in 8 parity colours, so every grid
+// node receives its contributions in one fixed order whatever the thread
+// count); the float build with OpenMP is the timed CPU baseline.
+//
+// Reference node bodies restated here (file:line within zenustech/zeno):
+//   binning            projects/CuLagrange/mpm/MPMPipeline.cu:73-84
+//   halo expansion     projects/CuLagrange/mpm/MPMPipeline.cu:131-199
+//   grid clear         projects/CuLagrange/mpm/MPMPipeline.cu:256-262
+//   APIC P2G           projects/CuLagrange/mpm/Transfer.cu:849-889
+//   grid update        projects/CuLagrange/mpm/MPMPipeline.cu:852-877
+//   boundary           projects/CuLagrange/mpm/Boundary.cu:56-67,105-116
+//   APIC G2P           projects/CuLagrange/mpm/Transfer.cu:1139-1173
+//   return mapping     projects/CuLagrange/mpm/MPMPipeline.cu:958-971
+//   particle init      projects/CuLagrange/mpm/Generation.cpp:944-966
+// zpc (which holds the arithmetic) is absent; each restated formula below
+// names the published method it follows.
+#include "mpm_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <class R> struct Params {
+  R mu, lam, alpha, bulk, gamma;
+  int type, plastic;
+};
+
+template <class R> Params<R> material_params(const orc_material &m) {
+  // Lame parameters from (E, nu): the standard relations the reference
+  // obtains from zs::lame_parameters (projects/CuLagrange/mpm/Temp.cu:47).
+  Params<R> p;
+  const R E = R(m.E), nu = R(m.nu);
+  p.mu = E / (R(2) * (R(1) + nu));
+  p.lam = E * nu / ((R(1) + nu) * (R(1) - R(2) * nu));
+  // Drucker-Prager cone coefficient, Klar et al. 2016 "Drucker-Prager
+  // elastoplasticity for sand animation", sec. 7.3.
+  const R phi = R(m.friction_angle_deg) * R(3.14159265358979323846) / R(180);
+  const R s = std::sin(phi);
+  p.alpha = std::sqrt(R(2) / R(3)) * R(2) * s / (R(3) - s);
+  p.bulk = R(m.bulk);
+  p.gamma = R(m.gamma);
+  p.type = m.type;
+  p.plastic = m.plasticity;
+  return p;
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
+// Loan, Matrix Computations, 4th ed., Alg. 8.5.2 with sym.schur2).
+// A = Q diag(w) Q^T.
+template <class R> void sym_eig3(const R *A_, R *w, R *Q, int max_sweeps) {
+  R A[9];
+  for (int i = 0; i < 9; ++i) A[i] = A_[i];
+  for (int i = 0; i < 9; ++i) Q[i] = (i % 4 == 0) ? R(1) : R(0);
+  const int P[3] = {0, 0, 1}, Qi[3] = {1, 2, 2};
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    const R off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+    const R dia = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
+    if (off == R(0) || off <= dia * std::numeric_limits<R>::epsilon() *
+                                     std::numeric_limits<R>::epsilon() * R(1e-2))
+      break;
+    for (int r = 0; r < 3; ++r) {
+      const int p = P[r], q = Qi[r];
+      const R apq = A[p * 3 + q];
+      if (apq == R(0)) continue;
+      const R theta = (A[q * 3 + q] - A[p * 3 + p]) / (R(2) * apq);
+      const R t = (theta >= R(0) ? R(1) : R(-1)) /
+                  (std::fabs(theta) + std::sqrt(theta * theta + R(1)));
+      const R c = R(1) / std::sqrt(t * t + R(1)), s = t * c;
+      for (int k = 0; k < 3; ++k) {  // A <- A J
+        const R akp = A[k * 3 + p], akq = A[k * 3 + q];
+        A[k * 3 + p] = c * akp - s * akq;
+        A[k * 3 + q] = s * akp + c * akq;
+      }
+      for (int k = 0; k < 3; ++k) {  // A <- J^T A
+        const R apk = A[p * 3 + k], aqk = A[q * 3 + k];
+        A[p * 3 + k] = c * apk - s * aqk;
+        A[q * 3 + k] = s * apk + c * aqk;
+      }
+      for (int k = 0; k < 3; ++k) {  // Q <- Q J
+        const R qkp = Q[k * 3 + p], qkq = Q[k * 3 + q];
+        Q[k * 3 + p] = c * qkp - s * qkq;
+        Q[k * 3 + q] = s * qkp + c * qkq;
+      }
+    }
+  }
+  w[0] = A[0];
+  w[1] = A[4];
+  w[2] = A[8];
+}
+
+template <class R> inline R det3(const R *F) {
+  return F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+         F[2] * (F[3] * F[7] - F[4] * F[6]);
+}
+
+template <class R> inline void mul_ABt(const R *A, const R *B, R *out) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      R s = 0;
+      for (int k = 0; k < 3; ++k) s += A[i * 3 + k] * B[j * 3 + k];
+      out[i * 3 + j] = s;
+    }
+}
+
+template <class R> inline void mul_AB(const R *A, const R *B, R *out) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      R s = 0;
+      for (int k = 0; k < 3; ++k) s += A[i * 3 + k] * B[k * 3 + j];
+      out[i * 3 + j] = s;
+    }
+}
+
+// Q diag(d) Q^T
+template <class R> inline void qdqt(const R *Q, const R *d, R *out) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      R s = 0;
+      for (int k = 0; k < 3; ++k) s += Q[i * 3 + k] * d[k] * Q[j * 3 + k];
+      out[i * 3 + j] = s;
+    }
+}
+
+constexpr int kSweeps = 30;
+
+// Kirchhoff stress tau = P F^T.  The reference scatters
+// contrib = -dt * Dinv * vol * P * F^T (Transfer.cu:868); tau is that P F^T.
+//   fixed corotated (Stomakhin et al. 2012): P = 2mu(F-R) + lam(J-1)J F^-T,
+//     tau = 2mu(B - R F^T) + lam(J-1)J I with B = F F^T, R F^T = U S^ U^T
+//     (S^ = singular values with the smallest negated when J < 0).
+//   Neo-Hookean: P = mu(F - F^-T) + lam ln(J) F^-T, tau = mu(B - I) + lam ln(J) I.
+//   StVK with Hencky strain (Klar et al. 2016): tau = U(2mu ln S + lam tr(ln S))U^T.
+//   equation-of-state fluid (Tait, Becker & Teschner 2007):
+//     p = K(J^-gamma - 1), tau = -p J I.
+// U and S come from the eigen-decomposition of B = U S^2 U^T.
+template <class R>
+bool kirchhoff(const Params<R> &p, const R *F, R J, R *tau) {
+  for (int i = 0; i < 9; ++i) tau[i] = 0;
+  if (p.type == ORC_EOS) {
+    if (!(J > R(0))) return false;
+    const R t = p.bulk * (J - std::pow(J, R(1) - p.gamma));
+    tau[0] = tau[4] = tau[8] = t;
+    return true;
+  }
+  R B[9];
+  mul_ABt(F, F, B);
+  if (p.type == ORC_NHK) {
+    const R Jf = det3(F);
+    if (!(Jf > R(0))) return false;
+    for (int i = 0; i < 9; ++i) tau[i] = p.mu * B[i];
+    const R diag = -p.mu + p.lam * std::log(Jf);
+    tau[0] += diag;
+    tau[4] += diag;
+    tau[8] += diag;
+    return true;
+  }
+  R w[3], Q[9];
+  sym_eig3(B, w, Q, kSweeps);
+  if (p.type == ORC_FCR) {
+    const R Jf = det3(F);
+    R sig[3];
+    for (int k = 0; k < 3; ++k) sig[k] = std::sqrt(std::max(w[k], R(0)));
+    if (Jf < R(0)) {
+      int kmin = 0;
+      for (int k = 1; k < 3; ++k)
+        if (sig[k] < sig[kmin]) kmin = k;
+      sig[kmin] = -sig[kmin];
+    }
+    R S[9];
+    qdqt(Q, sig, S);
+    for (int i = 0; i < 9; ++i) tau[i] = R(2) * p.mu * (B[i] - S[i]);
+    const R diag = p.lam * (Jf - R(1)) * Jf;
+    tau[0] += diag;
+    tau[4] += diag;
+    tau[8] += diag;
+    return std::isfinite(tau[0]);
+  }
+  // StVK with Hencky strain
+  R eps[3];
+  for (int k = 0; k < 3; ++k) {
+    if (!(w[k] > R(0))) return false;
+    eps[k] = R(0.5) * std::log(w[k]);
+  }
+  const R tr = eps[0] + eps[1] + eps[2];
+  R d[3];
+  for (int k = 0; k < 3; ++k) d[k] = R(2) * p.mu * eps[k] + p.lam * tr;
+  qdqt(Q, d, tau);
+  return true;
+}
+
+// Non-associative Drucker-Prager return mapping in Hencky strain space
+// (Klar et al. 2016, Alg. 2 / sec. 7.3); applied by the reference's
+// ZSReturnMapping node after G2P (MPMPipeline.cu:958-971).  With
+// F = U S V^T and B = F F^T = U S^2 U^T, the projected F is
+// U S' V^T = U (S'/S) U^T F.
+template <class R> int project_dp(const Params<R> &p, R *F) {
+  R B[9], w[3], Q[9];
+  mul_ABt(F, F, B);
+  sym_eig3(B, w, Q, kSweeps);
+  R sig[3], eps[3];
+  for (int k = 0; k < 3; ++k) {
+    sig[k] = std::sqrt(std::max(w[k], R(0)));
+    if (!(sig[k] > R(0))) return -1;
+    eps[k] = std::log(sig[k]);
+  }
+  const R tr = eps[0] + eps[1] + eps[2];
+  R sig_new[3];
+  if (tr >= R(0)) {
+    sig_new[0] = sig_new[1] = sig_new[2] = R(1);
+  } else {
+    R ehat[3];
+    for (int k = 0; k < 3; ++k) ehat[k] = eps[k] - tr / R(3);
+    const R nrm = std::sqrt(ehat[0] * ehat[0] + ehat[1] * ehat[1] + ehat[2] * ehat[2]);
+    const R dg = nrm + (R(3) * p.lam + R(2) * p.mu) / (R(2) * p.mu) * tr * p.alpha;
+    if (dg <= R(0)) return 0;
+    for (int k = 0; k < 3; ++k) sig_new[k] = std::exp(eps[k] - dg / nrm * ehat[k]);
+  }
+  R ratio[3], Mr[9], Fn[9];
+  for (int k = 0; k < 3; ++k) ratio[k] = sig_new[k] / sig[k];
+  qdqt(Q, ratio, Mr);
+  mul_AB(Mr, F, Fn);
+  for (int i = 0; i < 9; ++i) F[i] = Fn[i];
+  return 1;
+}
+
+struct Partition {
+  std::vector<int32_t> pb_dir;   // directory index of each particle block (sorted)
+  std::vector<int64_t> pb_start; // offset of the block in perm
+  std::vector<int32_t> pb_count;
+  std::vector<int64_t> perm;     // sorted position -> particle index
+  std::vector<int32_t> gb_dir;   // directory index of each grid block (sorted)
+  std::vector<int32_t> dir2gb;   // directory index -> grid block or -1
+};
+
+struct Dir {
+  int32_t lo[3], dims[3];
+  int64_t size() const { return int64_t(dims[0]) * dims[1] * dims[2]; }
+  void coords(int64_t d, int32_t *c) const {
+    c[2] = int32_t(d % dims[2]);
+    c[1] = int32_t((d / dims[2]) % dims[1]);
+    c[0] = int32_t(d / (int64_t(dims[1]) * dims[2]));
+  }
+  int64_t index(const int32_t *c) const {
+    return (int64_t(c[0]) * dims[1] + c[1]) * dims[2] + c[2];
+  }
+};
+
+// Block of a particle: base = floor(x / dx - 0.5), key = base - (base & 3)
+// (MPMPipeline.cu:78-83).  Computed in the precision of R: one rounded
+// multiply by 1/dx, one rounded subtraction of 0.5, then floor.
+template <class R> inline void particle_base(const R *x, R inv_dx, int32_t *base) {
+  for (int d = 0; d < 3; ++d) {
+    R c = x[d] * inv_dx;
+    c = c - R(0.5);
+    base[d] = int32_t(std::floor(c));
+  }
+}
+
+// Partition + 1-ring expansion (ZSPartitionForZSParticles followed by one
+// iteration of ExpandZSPartition over all 26 neighbours).  Particle blocks
+// are sorted by directory index; inside a block particles are ordered by
+// (cell id, particle index), which is the stable order by (block, cell).
+template <class R>
+int build_partition(const orc_scene &sc, int64_t n, const R *x, Partition &P, int nthreads) {
+  Dir dir;
+  for (int d = 0; d < 3; ++d) {
+    dir.lo[d] = sc.block_lo[d];
+    dir.dims[d] = sc.block_dims[d];
+    if (dir.dims[d] < 3) return ORC_ERR_INVALID;
+  }
+  const int64_t D = dir.size();
+  if (D >= (int64_t(1) << 26)) return ORC_ERR_INVALID;
+  const R inv_dx = R(1) / R(sc.dx);
+  std::vector<int32_t> key(n);  // directory index * 64 + cell
+  int bad = 0;
+#pragma omp parallel for num_threads(nthreads) reduction(| : bad) schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t base[3], bc[3];
+    particle_base(x + 3 * i, inv_dx, base);
+    bool ok = true;
+    for (int d = 0; d < 3; ++d) {
+      bc[d] = (base[d] >> 2) - dir.lo[d];
+      if (bc[d] < 1 || bc[d] > dir.dims[d] - 2) ok = false;
+    }
+    if (!ok) {
+      bad |= 1;
+      key[i] = -1;
+      continue;
+    }
+    const int32_t cell = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3);
+    key[i] = int32_t(dir.index(bc) * 64 + cell);
+  }
+  if (bad) return ORC_ERR_OUT_OF_DOMAIN;
+
+  // counting sort by block, stable in particle index
+  std::vector<int64_t> count(D + 1, 0);
+  for (int64_t i = 0; i < n; ++i) count[key[i] >> 6]++;
+  std::vector<int64_t> start(D + 1, 0);
+  for (int64_t d = 0; d < D; ++d) start[d + 1] = start[d] + count[d];
+  std::vector<int64_t> tmp(n), fill(start.begin(), start.end());
+  for (int64_t i = 0; i < n; ++i) tmp[fill[key[i] >> 6]++] = i;
+
+  P.pb_dir.clear();
+  P.pb_start.clear();
+  P.pb_count.clear();
+  for (int64_t d = 0; d < D; ++d)
+    if (count[d]) {
+      P.pb_dir.push_back(int32_t(d));
+      P.pb_start.push_back(start[d]);
+      P.pb_count.push_back(int32_t(count[d]));
+    }
+  // inside each block: stable counting sort by cell id
+  P.perm.assign(n, 0);
+  const int64_t nb = int64_t(P.pb_dir.size());
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+  for (int64_t b = 0; b < nb; ++b) {
+    const int64_t s0 = P.pb_start[b], c = P.pb_count[b];
+    int64_t cc[65] = {0};
+    for (int64_t s = s0; s < s0 + c; ++s) cc[(key[tmp[s]] & 63) + 1]++;
+    for (int k = 0; k < 64; ++k) cc[k + 1] += cc[k];
+    for (int64_t s = s0; s < s0 + c; ++s) {
+      const int64_t i = tmp[s];
+      P.perm[s0 + cc[key[i] & 63]++] = i;
+    }
+  }
+
+  // halo: every particle block and its 26 neighbours
+  std::vector<uint8_t> mark(D, 0);
+  for (int64_t b = 0; b < nb; ++b) {
+    int32_t c[3];
+    dir.coords(P.pb_dir[b], c);
+    for (int i = -1; i <= 1; ++i)
+      for (int j = -1; j <= 1; ++j)
+        for (int k = -1; k <= 1; ++k) {
+          const int32_t cn[3] = {c[0] + i, c[1] + j, c[2] + k};
+          mark[dir.index(cn)] = 1;
+        }
+  }
+  P.gb_dir.clear();
+  P.dir2gb.assign(D, -1);
+  for (int64_t d = 0; d < D; ++d)
+    if (mark[d]) {
+      P.dir2gb[d] = int32_t(P.gb_dir.size());
+      P.gb_dir.push_back(int32_t(d));
+    }
+  return ORC_OK;
+}
+
+template <class R> struct Sim {
+  const orc_scene &sc;
+  Dir dir;
+  std::vector<Params<R>> mats;
+  int nthreads;
+  Partition P;
+  std::vector<R> grid;  // [gb][64][4] = m, mv (then v)
+  R max_vel_sqr = 0;
+
+  Sim(const orc_scene &s, int nt) : sc(s), nthreads(nt) {
+    for (int d = 0; d < 3; ++d) {
+      dir.lo[d] = s.block_lo[d];
+      dir.dims[d] = s.block_dims[d];
+    }
+    for (int i = 0; i < s.n_materials; ++i) mats.push_back(material_params<R>(s.materials[i]));
+  }
+
+  // Quadratic B-spline stencil (Hu et al. 2018 MLS-MPM; Jiang et al. 2016
+  // course notes): f = x/dx - base in [0.5, 1.5),
+  // w0 = (1.5-f)^2/2, w1 = 3/4 - (f-1)^2, w2 = (f-0.5)^2/2.
+  struct Stencil {
+    int32_t base[3];
+    R fx[3];
+    R w[3][3];
+  };
+  void stencil(const R *x, Stencil &st) const {
+    const R inv_dx = R(1) / R(sc.dx);
+    particle_base(x, inv_dx, st.base);
+    for (int d = 0; d < 3; ++d) {
+      const R f = x[d] * inv_dx - R(st.base[d]);
+      st.fx[d] = f;
+      st.w[d][0] = R(0.5) * (R(1.5) - f) * (R(1.5) - f);
+      st.w[d][1] = R(0.75) - (f - R(1)) * (f - R(1));
+      st.w[d][2] = R(0.5) * (f - R(0.5)) * (f - R(0.5));
+    }
+  }
+  R *node(const int32_t *I) {
+    int32_t bc[3];
+    for (int d = 0; d < 3; ++d) bc[d] = (I[d] >> 2) - dir.lo[d];
+    const int32_t gb = P.dir2gb[dir.index(bc)];
+    const int cell = ((I[0] & 3) << 4) | ((I[1] & 3) << 2) | (I[2] & 3);
+    return &grid[(int64_t(gb) * 64 + cell) * 4];
+  }
+
+  int substep(int64_t n, R *x, R *v, R *C, R *F, R *J, const R *m, const R *vol,
+              const int32_t *mat, const R *mu, const R *lam, R dt) {
+    int rc = build_partition<R>(sc, n, x, P, nthreads);
+    if (rc) return rc;
+    // ZSGridFromZSPartition: zero every channel of every block
+    grid.assign(P.gb_dir.size() * 64 * 4, R(0));
+
+    const R dx = R(sc.dx), inv_dx = R(1) / dx;
+    const R Dinv = R(4) * inv_dx * inv_dx;
+    int bad = 0;
+
+    // P2G in 8 parity colours of the particle-block coordinates: two blocks
+    // of one colour are >= 2 blocks apart on some axis, so their stencils
+    // (blocks K..K+1 per axis) never overlap.
+    const int64_t nb = int64_t(P.pb_dir.size());
+    for (int colour = 0; colour < 8; ++colour) {
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1) reduction(| : bad)
+      for (int64_t b = 0; b < nb; ++b) {
+        int32_t c[3];
+        dir.coords(P.pb_dir[b], c);
+        if ((((c[0] & 1) << 2) | ((c[1] & 1) << 1) | (c[2] & 1)) != colour) continue;
+        for (int64_t s = P.pb_start[b]; s < P.pb_start[b] + P.pb_count[b]; ++s) {
+          const int64_t p = P.perm[s];
+          Params<R> mp = mats[mat[p]];
+          if (mu && lam) {  // per-particle override (Transfer.cu:861-864)
+            mp.mu = mu[p];
+            mp.lam = lam[p];
+          }
+          R tau[9];
+          if (!kirchhoff(mp, F + 9 * p, J[p], tau)) bad |= 1;
+          R contrib[9];
+          for (int i = 0; i < 9; ++i) contrib[i] = -dt * Dinv * vol[p] * tau[i];
+          Stencil st;
+          stencil(x + 3 * p, st);
+          const R *Cp = C + 9 * p, *vp = v + 3 * p;
+          const R mass = m[p];
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+              for (int k = 0; k < 3; ++k) {
+                const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+                const R xixp[3] = {(R(i) - st.fx[0]) * dx, (R(j) - st.fx[1]) * dx,
+                                   (R(k) - st.fx[2]) * dx};
+                const R W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+                R *g = node(I);
+                g[0] += mass * W;
+                for (int d = 0; d < 3; ++d) {
+                  const R Cx = Cp[d * 3 + 0] * xixp[0] + Cp[d * 3 + 1] * xixp[1] +
+                               Cp[d * 3 + 2] * xixp[2];
+                  const R fdt = contrib[d * 3 + 0] * xixp[0] + contrib[d * 3 + 1] * xixp[1] +
+                                contrib[d * 3 + 2] * xixp[2];
+                  g[1 + d] += W * (mass * (vp[d] + Cx) + fdt);
+                }
+              }
+        }
+      }
+    }
+
+    // UpdateZSGrid (APIC branch) then ApplyBoundaryOnZSGrid, node-wise
+    const int64_t ng = int64_t(P.gb_dir.size());
+    R vmax = 0;
+    const R g[3] = {R(sc.gravity[0]), R(sc.gravity[1]), R(sc.gravity[2])};
+#pragma omp parallel for num_threads(nthreads) reduction(max : vmax) schedule(static)
+    for (int64_t gb = 0; gb < ng; ++gb) {
+      int32_t c[3];
+      dir.coords(P.gb_dir[gb], c);
+      for (int cell = 0; cell < 64; ++cell) {
+        R *nd = &grid[(gb * 64 + cell) * 4];
+        if (nd[0] == R(0)) continue;
+        const R rm = R(1) / nd[0];
+        R vel[3];
+        for (int d = 0; d < 3; ++d) vel[d] = nd[1 + d] * rm + g[d] * dt;
+        vmax = std::max(vmax, vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+        const int32_t I[3] = {(c[0] + dir.lo[0]) * 4 + (cell >> 4),
+                              (c[1] + dir.lo[1]) * 4 + ((cell >> 2) & 3),
+                              (c[2] + dir.lo[2]) * 4 + (cell & 3)};
+        apply_bc(I, vel);
+        for (int d = 0; d < 3; ++d) nd[1 + d] = vel[d];
+      }
+    }
+    max_vel_sqr = vmax;
+
+    // G2P (+ F update) and the Drucker-Prager return mapping
+#pragma omp parallel for num_threads(nthreads) schedule(static) reduction(| : bad)
+    for (int64_t p = 0; p < n; ++p) {
+      Stencil st;
+      stencil(x + 3 * p, st);
+      R vel[3] = {0, 0, 0}, Cn[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k) {
+            const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+            const R xixp[3] = {(R(i) - st.fx[0]) * dx, (R(j) - st.fx[1]) * dx,
+                               (R(k) - st.fx[2]) * dx};
+            const R W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+            const R *gv = node(I) + 1;
+            for (int a = 0; a < 3; ++a) {
+              vel[a] += gv[a] * W;
+              for (int bb = 0; bb < 3; ++bb) Cn[a * 3 + bb] += W * Dinv * gv[a] * xixp[bb];
+            }
+          }
+      for (int a = 0; a < 3; ++a) {
+        v[3 * p + a] = vel[a];
+        x[3 * p + a] += vel[a] * dt;
+      }
+      for (int i = 0; i < 9; ++i) C[9 * p + i] = Cn[i];
+      const Params<R> &mp = mats[mat[p]];
+      R *Fp = F + 9 * p;
+      if (mp.type == ORC_EOS) {
+        J[p] *= R(1) + dt * (Cn[0] + Cn[4] + Cn[8]);
+        const R s = std::cbrt(J[p]);
+        for (int i = 0; i < 9; ++i) Fp[i] = (i % 4 == 0) ? s : R(0);
+      } else {
+        R A[9], Fn[9];
+        for (int i = 0; i < 9; ++i) A[i] = dt * Cn[i] + ((i % 4 == 0) ? R(1) : R(0));
+        mul_AB(A, Fp, Fn);
+        for (int i = 0; i < 9; ++i) Fp[i] = Fn[i];
+        if (mp.plastic == ORC_PLASTIC_NADP) {
+          Params<R> pp = mp;
+          if (mu && lam) {
+            pp.mu = mu[p];
+            pp.lam = lam[p];
+          }
+          if (project_dp(pp, Fp) < 0) bad |= 1;
+        }
+        J[p] = det3(Fp);
+      }
+      for (int i = 0; i < 9; ++i)
+        if (!std::isfinite(Fp[i])) bad |= 1;
+      if (!std::isfinite(x[3 * p]) || !std::isfinite(x[3 * p + 1]) || !std::isfinite(x[3 * p + 2]))
+        bad |= 1;
+    }
+    return bad ? ORC_ERR_NAN : ORC_OK;
+  }
+
+  // Box walls of the analytic collider in node-index space: a node is in the
+  // lower wall of axis d when I_d < lo_d + thickness and in the upper wall
+  // when I_d > hi_d - thickness.  Collider semantics follow
+  // Boundary.cu:56-67 with a static wall (v_object = 0): sticky sets v to 0,
+  // slip removes the wall-normal component, separate removes it only when it
+  // points into the wall.
+  void apply_bc(const int32_t *I, R *vel) const {
+    if (sc.bc_type == ORC_BC_NONE) return;
+    const int t = sc.bc_thickness;
+    bool any = false;
+    for (int d = 0; d < 3; ++d) {
+      const bool lower = I[d] < sc.bc_lo[d] + t;
+      const bool upper = I[d] > sc.bc_hi[d] - t;
+      if (!(lower || upper)) continue;
+      any = true;
+      if (sc.bc_type == ORC_BC_SLIP) vel[d] = 0;
+      if (sc.bc_type == ORC_BC_SEPARATE) {
+        if (lower && vel[d] < 0) vel[d] = 0;
+        if (upper && vel[d] > 0) vel[d] = 0;
+      }
+    }
+    if (any && sc.bc_type == ORC_BC_STICKY) vel[0] = vel[1] = vel[2] = 0;
+  }
+};
+
+template <class R>
+int32_t run(const orc_scene *scene, int64_t n, R *x, R *v, R *C, R *F, R *J, const R *m,
+            const R *vol, const int32_t *mat, const R *mu, const R *lam, R dt, int32_t nsteps,
+            int32_t nthreads, orc_stats *stats) {
+  if (!scene || n < 0 || nsteps < 0) return ORC_ERR_INVALID;
+  for (int64_t p = 0; p < n; ++p)
+    if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  Sim<R> sim(*scene, nthreads);
+  int32_t rc = ORC_OK;
+  for (int32_t s = 0; s < nsteps && rc == ORC_OK; ++s)
+    rc = sim.substep(n, x, v, C, F, J, m, vol, mat, mu, lam, dt);
+  if (stats) {
+    stats->max_vel_sqr = double(sim.max_vel_sqr);
+    stats->n_pblocks = int64_t(sim.P.pb_dir.size());
+    stats->n_gblocks = int64_t(sim.P.gb_dir.size());
+    stats->status = rc;
+  }
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t orc_partition(const orc_scene *scene, int64_t n, const float *x, int64_t cap_pb,
+                      int32_t *n_pb, int32_t *pb_dir, int32_t *pb_count, int64_t *perm,
+                      int64_t cap_gb, int32_t *n_gb, int32_t *gb_dir) {
+  if (!scene || n < 0) return ORC_ERR_INVALID;
+  Partition P;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  const int rc = build_partition<float>(*scene, n, x, P, nt);
+  if (rc) return rc;
+  *n_pb = int32_t(P.pb_dir.size());
+  *n_gb = int32_t(P.gb_dir.size());
+  if (int64_t(P.pb_dir.size()) > cap_pb || int64_t(P.gb_dir.size()) > cap_gb)
+    return ORC_ERR_CAPACITY;
+  std::copy(P.pb_dir.begin(), P.pb_dir.end(), pb_dir);
+  std::copy(P.pb_count.begin(), P.pb_count.end(), pb_count);
+  std::copy(P.perm.begin(), P.perm.end(), perm);
+  std::copy(P.gb_dir.begin(), P.gb_dir.end(), gb_dir);
+  return ORC_OK;
+}
+
+int32_t orc_run_f64(const orc_scene *scene, int64_t n, double *x, double *v, double *C, double *F,
+                    double *J, const double *m, const double *vol, const int32_t *mat,
+                    const double *mu, const double *lam, double dt, int32_t nsteps,
+                    int32_t nthreads, orc_stats *stats) {
+  return run<double>(scene, n, x, v, C, F, J, m, vol, mat, mu, lam, dt, nsteps, nthreads, stats);
+}
+
+int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v, float *C, float *F,
+                    float *J, const float *m, const float *vol, const int32_t *mat,
+                    const float *mu, const float *lam, float dt, int32_t nsteps,
+                    int32_t nthreads, orc_stats *stats) {
+  return run<float>(scene, n, x, v, C, F, J, m, vol, mat, mu, lam, dt, nsteps, nthreads, stats);
+}
+
+void orc_sym_eig3(const double *A, double *w, double *Q) { sym_eig3<double>(A, w, Q, kSweeps); }
+
+int32_t orc_kirchhoff(const orc_material *mat, const double *F, double J, double *tau) {
+  const Params<double> p = material_params<double>(*mat);
+  return kirchhoff<double>(p, F, J, tau) ? 1 : 0;
+}
+
+int32_t orc_project_dp(const orc_material *mat, double *F) {
+  const Params<double> p = material_params<double>(*mat);
+  return project_dp<double>(p, F);
+}
+
+int32_t orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+/*
+ * CPU oracle for the CuLagrange MLS-MPM substep -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This library is the checker, never the product: only tests/, the smoke
+ * check in __graft_entry__.py and the cpu_baseline / reference legs of
+ * bench.py may load it.  The GPU product path never links or calls it.
+ *
+ * It restates, on the CPU, the node bodies of the reference substep:
+ *   ZSPartitionForZSParticles   projects/CuLagrange/mpm/MPMPipeline.cu:73-84
+ *   ExpandZSPartition           projects/CuLagrange/mpm/MPMPipeline.cu:131-199
+ *   ZSGridFromZSPartition       projects/CuLagrange/mpm/MPMPipeline.cu:256-262
+ *   ZSParticleToZSGrid (APIC)   projects/CuLagrange/mpm/Transfer.cu:843-890
+ *   UpdateZSGrid (APIC)         projects/CuLagrange/mpm/MPMPipeline.cu:852-877
+ *   ApplyBoundaryOnZSGrid       projects/CuLagrange/mpm/Boundary.cu:56-67,105-116
+ *   ZSGridToZSParticle (APIC)   projects/CuLagrange/mpm/Transfer.cu:1137-1173
+ *   ZSReturnMapping             projects/CuLagrange/mpm/MPMPipeline.cu:953-972
+ * The arithmetic the reference delegates to zpc (absent from the reference
+ * tree; submodule projects/CUDA/zpc, pinned commit unknown) is restated from
+ * the published methods named at each function in mpm_oracle.cpp.
+ *
+ * Parity status: the reference ships no MPM tests, golden vectors or
+ * fixtures and its substep cannot be compiled or run without zpc, so this
+ * oracle is pinned only by known-answer tests of its own (rigid motion,
+ * free fall, affine reproduction, zero stress at rest, lattice partitions):
+ * parity unpinned against reference outputs.
+ */
+#ifndef ZSMPM_ORACLE_H
+#define ZSMPM_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_FCR = 0, ORC_NHK = 1, ORC_STVK = 2, ORC_EOS = 3 };
+enum { ORC_PLASTIC_NONE = 0, ORC_PLASTIC_NADP = 1 };
+enum { ORC_BC_NONE = 0, ORC_BC_STICKY = 1, ORC_BC_SLIP = 2, ORC_BC_SEPARATE = 3 };
+
+enum {
+  ORC_OK = 0,
+  ORC_ERR_INVALID = 1,
+  ORC_ERR_OUT_OF_DOMAIN = 4,
+  ORC_ERR_NAN = 6,
+  ORC_ERR_CAPACITY = 3
+};
+
+typedef struct orc_material {
+  int32_t type;        /* ORC_FCR / ORC_NHK / ORC_STVK / ORC_EOS */
+  int32_t plasticity;  /* ORC_PLASTIC_NONE / ORC_PLASTIC_NADP */
+  float E, nu, density;
+  float friction_angle_deg; /* Drucker-Prager friction angle */
+  float bulk, gamma;        /* equation-of-state fluid */
+} orc_material;
+
+typedef struct orc_scene {
+  float dx;
+  float gravity[3];
+  int32_t block_lo[3];   /* block coordinates (units of 4 cells) of directory origin */
+  int32_t block_dims[3]; /* directory extent in blocks */
+  int32_t bc_type;       /* ORC_BC_* */
+  int32_t bc_thickness;  /* wall thickness in cells */
+  int32_t bc_lo[3];      /* node index of the lower domain face */
+  int32_t bc_hi[3];      /* node index of the upper domain face */
+  int32_t n_materials;
+  const orc_material *materials;
+} orc_scene;
+
+typedef struct orc_stats {
+  double max_vel_sqr;
+  int64_t n_pblocks;
+  int64_t n_gblocks;
+  int32_t status;
+} orc_stats;
+
+/* Partition of positions x (n x 3, float) into 4^3 blocks.
+ * Outputs (caller allocated, capacities given):
+ *   pb_dir[cap_pb]   sorted directory index of each non-empty particle block
+ *   pb_count[cap_pb] particles per block
+ *   perm[n]          stable sort of particle indices by (block, cell, index)
+ *   gb_dir[cap_gb]   sorted directory index of each grid block (1-ring halo)
+ */
+int32_t orc_partition(const orc_scene *scene, int64_t n, const float *x,
+                      int64_t cap_pb, int32_t *n_pb, int32_t *pb_dir,
+                      int32_t *pb_count, int64_t *perm, int64_t cap_gb,
+                      int32_t *n_gb, int32_t *gb_dir);
+
+/* nsteps substeps in double precision, order-stable scatter (the oracle). */
+int32_t orc_run_f64(const orc_scene *scene, int64_t n, double *x, double *v,
+                    double *C, double *F, double *J, const double *m,
+                    const double *vol, const int32_t *mat, const double *mu,
+                    const double *lam, double dt, int32_t nsteps,
+                    int32_t nthreads, orc_stats *stats);
+
+/* Same substeps in single precision with OpenMP (the CPU baseline). */
+int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v,
+                    float *C, float *F, float *J, const float *m,
+                    const float *vol, const int32_t *mat, const float *mu,
+                    const float *lam, float dt, int32_t nsteps,
+                    int32_t nthreads, orc_stats *stats);
+
+/* Symmetric 3x3 eigen-decomposition used by the constitutive models
+ * (exported for known-answer tests): A = Q diag(w) Q^T, Q column-major
+ * eigenvectors stored row-major as Q[i*3+j] = Q_ij. */
+void orc_sym_eig3(const double *A, double *w, double *Q);
+
+/* Kirchhoff stress tau = P F^T of one material at deformation F (or J for
+ * the equation-of-state fluid) -- exported for known-answer tests. */
+int32_t orc_kirchhoff(const orc_material *mat, const double *F, double J,
+                      double *tau);
+
+/* Drucker-Prager return mapping of F in place; returns 1 if projected. */
+int32_t orc_project_dp(const orc_material *mat, double *F);
+
+int32_t orc_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,166 @@
+"""ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, the smoke check and bench.py's CPU legs import this module; the
+product path (zeno_gb300/) never does.  The oracle restates the reference's
+CuLagrange MLS-MPM substep (see mpm_oracle.cpp for the file:line of every
+node body it follows).  Parity with reference outputs is unpinned: the
+reference ships no MPM golden vectors and its substep cannot run without the
+absent zpc submodule.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libzsmpm_oracle.so")
+
+
+class OrcMaterial(C.Structure):
+    _fields_ = [("type", C.c_int32), ("plasticity", C.c_int32), ("E", C.c_float),
+                ("nu", C.c_float), ("density", C.c_float), ("friction_angle_deg", C.c_float),
+                ("bulk", C.c_float), ("gamma", C.c_float)]
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("dx", C.c_float), ("gravity", C.c_float * 3), ("block_lo", C.c_int32 * 3),
+                ("block_dims", C.c_int32 * 3), ("bc_type", C.c_int32),
+                ("bc_thickness", C.c_int32), ("bc_lo", C.c_int32 * 3), ("bc_hi", C.c_int32 * 3),
+                ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial))]
+
+
+class OrcStats(C.Structure):
+    _fields_ = [("max_vel_sqr", C.c_double), ("n_pblocks", C.c_int64),
+                ("n_gblocks", C.c_int64), ("status", C.c_int32)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc + OpenMP)."""
+    if force or not os.path.exists(LIB_PATH) or \
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(os.path.join(HERE, f))
+                                             for f in ("mpm_oracle.cpp", "mpm_oracle.h")):
+        subprocess.run(["make", "-s", "-C", HERE, "-B"], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.orc_partition.argtypes = [C.POINTER(OrcScene), C.c_int64, P, C.c_int64, P, P, P, P,
+                                    C.c_int64, P, P]
+        L.orc_partition.restype = C.c_int32
+        for name, real in (("orc_run_f64", C.c_double), ("orc_run_f32", C.c_float)):
+            f = getattr(L, name)
+            f.argtypes = [C.POINTER(OrcScene), C.c_int64] + [P] * 10 + [real, C.c_int32,
+                                                                        C.c_int32,
+                                                                        C.POINTER(OrcStats)]
+            f.restype = C.c_int32
+        L.orc_sym_eig3.argtypes = [P, P, P]
+        L.orc_kirchhoff.argtypes = [C.POINTER(OrcMaterial), P, C.c_double, P]
+        L.orc_kirchhoff.restype = C.c_int32
+        L.orc_project_dp.argtypes = [C.POINTER(OrcMaterial), P]
+        L.orc_project_dp.restype = C.c_int32
+        L.orc_max_threads.restype = C.c_int32
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def make_material(m) -> OrcMaterial:
+    return OrcMaterial(int(m.type), int(m.plasticity), float(m.E), float(m.nu),
+                       float(m.density), float(m.friction_angle_deg), float(m.bulk),
+                       float(m.gamma))
+
+
+class _SceneHolder:
+    def __init__(self, scene):
+        mats = (OrcMaterial * max(1, len(scene.materials)))(
+            *[make_material(m) for m in scene.materials])
+        self.mats = mats
+        self.s = OrcScene(float(scene.dx), (C.c_float * 3)(*scene.gravity),
+                          (C.c_int32 * 3)(*scene.block_lo), (C.c_int32 * 3)(*scene.block_dims),
+                          int(scene.bc_type), int(scene.bc_thickness),
+                          (C.c_int32 * 3)(*scene.bc_lo), (C.c_int32 * 3)(*scene.bc_hi),
+                          len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)))
+
+
+def partition(scene, x: np.ndarray) -> dict:
+    """Bit-exact reference partition of float32 positions x (n, 3)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    n = x.shape[0]
+    h = _SceneHolder(scene)
+    D = int(np.prod(scene.block_dims))
+    cap_pb = min(D, max(n, 1))
+    cap_gb = D
+    n_pb = np.zeros(1, np.int32)
+    n_gb = np.zeros(1, np.int32)
+    pb_dir = np.zeros(cap_pb, np.int32)
+    pb_count = np.zeros(cap_pb, np.int32)
+    perm = np.zeros(max(n, 1), np.int64)
+    gb_dir = np.zeros(cap_gb, np.int32)
+    rc = lib().orc_partition(C.byref(h.s), n, _ptr(x), cap_pb, _ptr(n_pb), _ptr(pb_dir),
+                             _ptr(pb_count), _ptr(perm), cap_gb, _ptr(n_gb), _ptr(gb_dir))
+    if rc != 0:
+        raise RuntimeError(f"oracle partition failed with status {rc}")
+    return {"pb_dir": pb_dir[:n_pb[0]].copy(), "pb_count": pb_count[:n_pb[0]].copy(),
+            "perm": perm[:n].copy(), "gb_dir": gb_dir[:n_gb[0]].copy()}
+
+
+def run(scene, parts, nsteps: int, precision: str = "f64", nthreads: int = 0,
+        dt: float | None = None):
+    """Advance a copy of `parts` by nsteps substeps; returns (particles, stats)."""
+    dtype = np.float64 if precision == "f64" else np.float32
+    p = parts.copy(dtype=dtype)
+    for k in ("x", "v", "C", "F", "J", "m", "vol", "mu", "lam"):
+        a = getattr(p, k)
+        if a is not None:
+            setattr(p, k, np.ascontiguousarray(a, dtype=dtype))
+    p.mat = np.ascontiguousarray(p.mat, dtype=np.int32)
+    h = _SceneHolder(scene)
+    st = OrcStats()
+    fn = lib().orc_run_f64 if precision == "f64" else lib().orc_run_f32
+    rc = fn(C.byref(h.s), p.n, _ptr(p.x), _ptr(p.v), _ptr(p.C), _ptr(p.F), _ptr(p.J),
+            _ptr(p.m), _ptr(p.vol), _ptr(p.mat), _ptr(p.mu), _ptr(p.lam),
+            float(scene.dt if dt is None else dt), int(nsteps), int(nthreads), C.byref(st))
+    stats = {"status": rc, "max_vel_sqr": st.max_vel_sqr, "n_pblocks": st.n_pblocks,
+             "n_gblocks": st.n_gblocks}
+    return p, stats
+
+
+def sym_eig3(A: np.ndarray):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    w = np.zeros(3)
+    Q = np.zeros(9)
+    lib().orc_sym_eig3(_ptr(A), _ptr(w), _ptr(Q))
+    return w, Q.reshape(3, 3)
+
+
+def kirchhoff(material, F: np.ndarray, J: float = 1.0):
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    tau = np.zeros(9)
+    m = make_material(material)
+    ok = lib().orc_kirchhoff(C.byref(m), _ptr(F), float(J), _ptr(tau))
+    return bool(ok), tau.reshape(3, 3)
+
+
+def project_dp(material, F: np.ndarray):
+    F = np.array(F, dtype=np.float64, copy=True).reshape(9)
+    m = make_material(material)
+    rc = lib().orc_project_dp(C.byref(m), _ptr(F))
+    return rc, F.reshape(3, 3)
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())

@@ -1,0 +1,590 @@
+// C ABI of the GB300 MLS-MPM substep (declared in include/zsmpm.h).
+//
+// A context owns every device buffer of one scene (allocated once at
+// creation; no allocation on the substep path), one CUDA stream, and two
+// instantiated CUDA graphs of a whole substep, one per particle buffer
+// parity.  Kernel parameters that change between calls (dt, gravity,
+// boundary, material count) live in a small device struct that the host
+// refreshes with one copy before launching, so a captured graph stays valid
+// when dt changes (SubstepDt, zeno/src/nodes/ControlNodes.cpp:251-320).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "zsmpm_internal.cuh"
+
+using namespace zsmpm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int32_t fail(int32_t code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define ZS_CUDA(expr)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(MPM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+}  // namespace
+
+struct mpm_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  DevPtrs d{};
+  SimParams prm{};
+  bool prm_dirty = true;
+  int cur = 0;
+  bool partition_valid = false;
+  bool needs_full_clear = false;
+  int64_t substeps = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  Counters *h_cnt = nullptr;  // pinned
+  std::vector<void *> allocs;
+  float last_max_vel_sqr = 0.0f;
+};
+
+namespace {
+
+int32_t map_status(int bits) {
+  if (bits & ST_NAN) return MPM_ERR_NAN;
+  if (bits & ST_OUT_OF_DOMAIN) return MPM_ERR_OUT_OF_DOMAIN;
+  if (bits & ST_CAPACITY) return MPM_ERR_CAPACITY;
+  if (bits & ST_TIMEOUT) return MPM_ERR_TIMEOUT;
+  if (bits & ST_STENCIL) return MPM_ERR_CFL;
+  return MPM_OK;  // ST_BUCKET_OVERSIZE only affects the in-block order
+}
+
+const char *status_text(int32_t st) {
+  switch (st) {
+    case MPM_ERR_NAN: return "non-finite particle state or inverted element";
+    case MPM_ERR_OUT_OF_DOMAIN: return "a particle left the block directory";
+    case MPM_ERR_CAPACITY: return "more grid blocks than the context's capacity";
+    case MPM_ERR_TIMEOUT: return "a bounded device-side wait gave up";
+    case MPM_ERR_CFL: return "a particle moved out of its block's stencil window";
+    default: return "";
+  }
+}
+
+template <class T> int32_t dalloc(mpm_ctx *c, T **p, size_t count) {
+  void *q = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+  if (e != cudaSuccess)
+    return fail(MPM_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->allocs.push_back(q);
+  *p = static_cast<T *>(q);
+  return MPM_OK;
+}
+
+int32_t push_params(mpm_ctx *c) {
+  if (!c->prm_dirty) return MPM_OK;
+  ZS_CUDA(cudaMemcpyAsync(c->d.prm, &c->prm, sizeof(SimParams), cudaMemcpyHostToDevice,
+                          c->stream));
+  c->prm_dirty = false;
+  return MPM_OK;
+}
+
+int32_t set_dt(mpm_ctx *c, float dt) {
+  if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(MPM_ERR_INVALID, "dt must be positive");
+  if (c->prm.dt != dt) {
+    c->prm.dt = dt;
+    c->prm_dirty = true;
+  }
+  return push_params(c);
+}
+
+int32_t check(mpm_ctx *c) {
+  if (!c) return fail(MPM_ERR_INVALID, "null context");
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+int32_t launch_check(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+void enqueue_partition(mpm_ctx *c, int cur) {
+  launch_reset(c->d, c->stream);
+  launch_bin(c->d, cur, c->stream);
+  launch_scan(c->d, c->stream);
+  launch_scatter(c->d, c->stream);
+  launch_bucket_sort(c->d, c->stream);
+}
+
+void enqueue_substep(mpm_ctx *c, int cur) {
+  enqueue_partition(c, cur);
+  launch_grid_clear(c->d, c->stream);
+  launch_p2g(c->d, cur, c->stream);
+  launch_grid_update(c->d, 3, c->stream);
+  launch_g2p(c->d, cur, 1, c->stream);
+}
+
+bool graphs_enabled() {
+  const char *e = std::getenv("ZSMPM_NO_GRAPH");
+  return !(e && e[0] == '1');
+}
+
+int32_t ensure_graph(mpm_ctx *c, int cur) {
+  if (c->graph[cur]) return MPM_OK;
+  cudaGraph_t g = nullptr;
+  ZS_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_substep(c, cur);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&c->graph[cur], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess)
+    return fail(MPM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return MPM_OK;
+}
+
+int32_t prepare_partition(mpm_ctx *c) {
+  if (c->needs_full_clear) {
+    launch_full_dir_clear(c->d, c->stream);
+    c->needs_full_clear = false;
+  }
+  return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mpm_abi_version(void) { return ZSMPM_ABI_VERSION; }
+
+const char *mpm_last_error(void) { return g_last_error.c_str(); }
+
+int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
+  if (!desc || !out) return fail(MPM_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (!(desc->dx > 0.0f)) return fail(MPM_ERR_INVALID, "dx must be positive");
+  if (desc->max_particles <= 0 || desc->max_particles >= (int64_t(1) << 31))
+    return fail(MPM_ERR_INVALID, "max_particles must be in [1, 2^31)");
+  long long ndir = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (desc->block_dims[k] < 3) return fail(MPM_ERR_INVALID, "block_dims must be >= 3");
+    ndir *= desc->block_dims[k];
+  }
+  if (ndir >= (1ll << 25)) return fail(MPM_ERR_INVALID, "block directory larger than 2^25 blocks");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return fail(MPM_ERR_NO_DEVICE, "no CUDA device");
+  if (desc->device < 0 || desc->device >= ndev) return fail(MPM_ERR_INVALID, "bad device ordinal");
+  int major = 0, minor = 0, sms = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, desc->device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, desc->device);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
+  if (major * 10 + minor != 103)
+    return fail(MPM_ERR_NO_DEVICE, "zsmpm is built for sm_103a (GB300) only; device is sm_" +
+                                       std::to_string(major * 10 + minor));
+
+  mpm_ctx *c = new mpm_ctx();
+  c->device = desc->device;
+  int32_t rc = MPM_OK;
+  auto bail = [&](int32_t r) {
+    mpm_ctx_destroy(c);
+    return r;
+  };
+  if (cudaSetDevice(c->device) != cudaSuccess) return bail(fail(MPM_ERR_CUDA, "cudaSetDevice"));
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(MPM_ERR_CUDA, "cudaStreamCreate"));
+  c->stream = c->own_stream;
+
+  const long long cap = desc->max_particles;
+  long long capg = desc->max_grid_blocks > 0 ? desc->max_grid_blocks
+                                             : std::max<long long>(4096, cap / 16);
+  capg = std::min<long long>(capg, ndir);
+  DevPtrs &d = c->d;
+  d.cap = cap;
+  d.ndir = ndir;
+  d.cap_gblocks = (int)capg;
+  d.num_sms = sms;
+  d.ntiles = (int)((ndir + kScanTile - 1) / kScanTile);
+  for (int k = 0; k < 2; ++k) {
+    if ((rc = dalloc(c, &d.pbuf[k], (size_t)NCH * cap))) return bail(rc);
+    if ((rc = dalloc(c, &d.ibuf[k], (size_t)NICH * cap))) return bail(rc);
+  }
+  if ((rc = dalloc(c, &d.pkey, cap)) || (rc = dalloc(c, &d.perm, cap)) ||
+      (rc = dalloc(c, &d.dir_count, ndir)) || (rc = dalloc(c, &d.dir_fill, ndir)) ||
+      (rc = dalloc(c, &d.dir_gb, ndir)) || (rc = dalloc(c, &d.dir_flag, ndir)) ||
+      (rc = dalloc(c, &d.gb_dir, capg)) || (rc = dalloc(c, &d.bk_dir, capg)) ||
+      (rc = dalloc(c, &d.bk_start, capg)) || (rc = dalloc(c, &d.bk_count, capg)) ||
+      (rc = dalloc(c, &d.grid, (size_t)capg * 64)) ||
+      (rc = dalloc(c, &d.tile_sums, (size_t)3 * d.ntiles)) || (rc = dalloc(c, &d.cnt, 1)) ||
+      (rc = dalloc(c, &d.prm, 1)) || (rc = dalloc(c, &d.mats, kMaxMaterials)))
+    return bail(rc);
+  if (cudaMallocHost(&c->h_cnt, sizeof(Counters)) != cudaSuccess)
+    return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
+  cudaMemsetAsync(d.dir_count, 0, ndir * sizeof(int32_t), c->stream);
+  cudaMemsetAsync(d.dir_fill, 0, ndir * sizeof(int32_t), c->stream);
+  cudaMemsetAsync(d.dir_gb, 0xff, ndir * sizeof(int32_t), c->stream);
+  cudaMemsetAsync(d.dir_flag, 0, ndir, c->stream);
+  cudaMemsetAsync(d.cnt, 0, sizeof(Counters), c->stream);
+  cudaMemsetAsync(d.mats, 0, kMaxMaterials * sizeof(MatParams), c->stream);
+
+  SimParams &P = c->prm;
+  P.dt = 1e-4f;
+  P.dx = desc->dx;
+  P.inv_dx = 1.0f / desc->dx;
+  P.Dinv = 4.0f * P.inv_dx * P.inv_dx;
+  P.gravity[0] = 0.0f;
+  P.gravity[1] = -9.8f;
+  P.gravity[2] = 0.0f;
+  for (int k = 0; k < 3; ++k) {
+    P.block_lo[k] = desc->block_lo[k];
+    P.block_dims[k] = desc->block_dims[k];
+    P.bc_lo[k] = 0;
+    P.bc_hi[k] = 0;
+  }
+  P.bc_type = MPM_BC_NONE;
+  P.bc_thickness = 0;
+  P.n_materials = 0;
+  P.has_lame = 0;
+  P.n = 0;
+  c->prm_dirty = true;
+  if ((rc = push_params(c))) return bail(rc);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return bail(fail(MPM_ERR_CUDA, "context initialisation failed"));
+  *out = c;
+  return MPM_OK;
+}
+
+int32_t mpm_ctx_destroy(mpm_ctx *c) {
+  if (!c) return MPM_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int k = 0; k < 2; ++k)
+    if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->h_cnt) cudaFreeHost(c->h_cnt);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return MPM_OK;
+}
+
+int32_t mpm_set_stream(mpm_ctx *c, void *stream) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  c->prm_dirty = true;
+  return push_params(c);
+}
+
+int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!mats || n <= 0 || n > kMaxMaterials)
+    return fail(MPM_ERR_INVALID, "need 1.." + std::to_string(kMaxMaterials) + " materials");
+  std::vector<MatParams> h(kMaxMaterials);
+  for (int i = 0; i < n; ++i) {
+    const mpm_material &m = mats[i];
+    if (m.type < MPM_FCR || m.type > MPM_EOS) return fail(MPM_ERR_INVALID, "unknown material type");
+    if (m.plasticity != MPM_PLASTIC_NONE && m.plasticity != MPM_PLASTIC_NADP)
+      return fail(MPM_ERR_INVALID, "unknown plasticity");
+    if (m.plasticity == MPM_PLASTIC_NADP && m.type != MPM_STVK)
+      return fail(MPM_ERR_INVALID,
+                  "nadp plasticity runs on the StVK-Hencky model (Generation.cu:66-70)");
+    MatParams &p = h[i];
+    p.type = m.type;
+    p.plastic = m.plasticity;
+    // Lame parameters (standard relations, zs::lame_parameters at Temp.cu:47)
+    p.mu = m.E / (2.0f * (1.0f + m.nu));
+    p.lam = m.E * m.nu / ((1.0f + m.nu) * (1.0f - 2.0f * m.nu));
+    const double phi = (double)m.friction_angle_deg * 3.14159265358979323846 / 180.0;
+    const double s = std::sin(phi);
+    p.alpha = (float)(std::sqrt(2.0 / 3.0) * 2.0 * s / (3.0 - s));
+    p.bulk = m.bulk;
+    p.gamma = m.gamma;
+  }
+  ZS_CUDA(cudaMemcpyAsync(c->d.mats, h.data(), sizeof(MatParams) * kMaxMaterials,
+                          cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->prm.n_materials = n;
+  c->prm_dirty = true;
+  return push_params(c);
+}
+
+int32_t mpm_set_boundary(mpm_ctx *c, const mpm_boundary *bc) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!bc || bc->type < MPM_BC_NONE || bc->type > MPM_BC_SEPARATE || bc->thickness < 0)
+    return fail(MPM_ERR_INVALID, "bad boundary");
+  c->prm.bc_type = bc->type;
+  c->prm.bc_thickness = bc->thickness;
+  for (int k = 0; k < 3; ++k) {
+    c->prm.bc_lo[k] = bc->lo[k];
+    c->prm.bc_hi[k] = bc->hi[k];
+  }
+  c->prm_dirty = true;
+  return push_params(c);
+}
+
+int32_t mpm_set_gravity(mpm_ctx *c, float gx, float gy, float gz) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  c->prm.gravity[0] = gx;
+  c->prm.gravity[1] = gy;
+  c->prm.gravity[2] = gz;
+  c->prm_dirty = true;
+  return push_params(c);
+}
+
+int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float *v,
+                             const float *C, const float *F, const float *J, const float *m,
+                             const float *vol, const int32_t *mat, const float *mu,
+                             const float *lam) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (n < 0 || n > c->d.cap) return fail(MPM_ERR_CAPACITY, "particle count exceeds capacity");
+  if (n > 0 && (!x || !m || !vol)) return fail(MPM_ERR_INVALID, "x, m and vol are required");
+  if ((mu == nullptr) != (lam == nullptr)) return fail(MPM_ERR_INVALID, "mu and lam go together");
+  if (c->prm.n_materials <= 0) return fail(MPM_ERR_STATE, "set materials before uploading");
+  if (mat) {
+    for (int64_t i = 0; i < n; ++i)
+      if (mat[i] < 0 || mat[i] >= c->prm.n_materials)
+        return fail(MPM_ERR_INVALID, "material id out of range");
+  }
+  const int alt = 1 - c->cur;
+  float *st = c->d.pbuf[alt];
+  int32_t *ist = c->d.ibuf[alt];
+  IngestSrc src{};
+  auto put = [&](const float *h, size_t off, size_t count, const float **dst) -> int32_t {
+    if (!h) {
+      *dst = nullptr;
+      return MPM_OK;
+    }
+    ZS_CUDA(cudaMemcpyAsync(st + off, h, count * sizeof(float), cudaMemcpyHostToDevice,
+                            c->stream));
+    *dst = st + off;
+    return MPM_OK;
+  };
+  const size_t N = (size_t)n;
+  if ((rc = put(x, 0, 3 * N, &src.x)) || (rc = put(v, 3 * N, 3 * N, &src.v)) ||
+      (rc = put(C, 6 * N, 9 * N, &src.C)) || (rc = put(F, 15 * N, 9 * N, &src.F)) ||
+      (rc = put(J, 24 * N, N, &src.J)) || (rc = put(m, 25 * N, N, &src.m)) ||
+      (rc = put(vol, 26 * N, N, &src.vol)) || (rc = put(mu, 27 * N, N, &src.mu)) ||
+      (rc = put(lam, 28 * N, N, &src.lam)))
+    return rc;
+  src.mat = nullptr;
+  if (mat && n > 0) {
+    ZS_CUDA(cudaMemcpyAsync(ist, mat, N * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    src.mat = ist;
+  }
+  launch_ingest(c->d, c->cur, src, n, c->stream);
+  if ((rc = launch_check("ingest"))) return rc;
+  c->prm.n = n;
+  c->prm.has_lame = mu ? 1 : 0;
+  c->prm_dirty = true;
+  if ((rc = push_params(c))) return rc;
+  // a fresh store: clear the status word and the whole directory
+  ZS_CUDA(cudaMemsetAsync(&c->d.cnt->status, 0, sizeof(int), c->stream));
+  c->needs_full_clear = true;
+  c->partition_valid = false;
+  c->substeps = 0;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *F, float *J) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  const long long n = c->prm.n;
+  float *st = c->d.pbuf[1 - c->cur];
+  launch_egest(c->d, c->cur, st, n, c->stream);
+  if ((rc = launch_check("egest"))) return rc;
+  const size_t N = (size_t)n;
+  auto get = [&](float *h, size_t off, size_t count) -> int32_t {
+    if (!h || count == 0) return MPM_OK;
+    ZS_CUDA(cudaMemcpyAsync(h, st + off, count * sizeof(float), cudaMemcpyDeviceToHost,
+                            c->stream));
+    return MPM_OK;
+  };
+  if ((rc = get(x, 0, 3 * N)) || (rc = get(v, 3 * N, 3 * N)) || (rc = get(C, 6 * N, 9 * N)) ||
+      (rc = get(F, 15 * N, 9 * N)) || (rc = get(J, 24 * N, N)))
+    return rc;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_partition(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = push_params(c)) || (rc = prepare_partition(c))) return rc;
+  enqueue_partition(c, c->cur);
+  if ((rc = launch_check("partition"))) return rc;
+  c->partition_valid = true;
+  return MPM_OK;
+}
+
+int32_t mpm_grid_clear(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "grid clear needs a partition");
+  launch_grid_clear(c->d, c->stream);
+  return launch_check("grid clear");
+}
+
+int32_t mpm_p2g(mpm_ctx *c, float dt) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "p2g needs a partition of the current positions");
+  if ((rc = set_dt(c, dt))) return rc;
+  launch_p2g(c->d, c->cur, c->stream);
+  return launch_check("p2g");
+}
+
+int32_t mpm_grid_update(mpm_ctx *c, float dt, float *max_vel_sqr) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "grid update needs a partition");
+  if ((rc = set_dt(c, dt))) return rc;
+  ZS_CUDA(cudaMemsetAsync(&c->d.cnt->max_vel_sqr_bits, 0, sizeof(unsigned), c->stream));
+  launch_grid_update(c->d, 1, c->stream);
+  if ((rc = launch_check("grid update"))) return rc;
+  if (max_vel_sqr) {
+    ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
+                            c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    float f;
+    std::memcpy(&f, &c->h_cnt->max_vel_sqr_bits, sizeof(float));
+    *max_vel_sqr = f;
+  }
+  return MPM_OK;
+}
+
+int32_t mpm_apply_boundary(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "boundary needs a partition");
+  if ((rc = push_params(c))) return rc;
+  launch_grid_update(c->d, 2, c->stream);
+  return launch_check("boundary");
+}
+
+int32_t mpm_g2p(mpm_ctx *c, float dt) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "g2p needs the partition used by p2g");
+  if ((rc = set_dt(c, dt))) return rc;
+  launch_g2p(c->d, c->cur, 0, c->stream);
+  if ((rc = launch_check("g2p"))) return rc;
+  c->cur = 1 - c->cur;
+  c->partition_valid = false;
+  c->substeps += 1;
+  return MPM_OK;
+}
+
+int32_t mpm_return_mapping(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = push_params(c))) return rc;
+  launch_return_mapping(c->d, c->cur, c->stream);
+  return launch_check("return mapping");
+}
+
+int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (n_substeps < 0) return fail(MPM_ERR_INVALID, "negative substep count");
+  if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
+  const bool graphs = graphs_enabled();
+  for (int32_t k = 0; k < n_substeps; ++k) {
+    if (graphs) {
+      if ((rc = ensure_graph(c, c->cur))) return rc;
+      ZS_CUDA(cudaGraphLaunch(c->graph[c->cur], c->stream));
+    } else {
+      enqueue_substep(c, c->cur);
+      if ((rc = launch_check("substep"))) return rc;
+    }
+    c->cur = 1 - c->cur;
+  }
+  c->partition_valid = false;
+  c->substeps += n_substeps;
+  return MPM_OK;
+}
+
+int32_t mpm_sync(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
+                          c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  const int bits = c->h_cnt->status;
+  if (bits & (ST_CAPACITY | ST_OUT_OF_DOMAIN)) c->needs_full_clear = true;
+  const int32_t st = map_status(bits);
+  if (st != MPM_OK) return fail(st, status_text(st));
+  return MPM_OK;
+}
+
+int32_t mpm_get_stats(mpm_ctx *c, mpm_stats *out) {
+  if (!out) return fail(MPM_ERR_INVALID, "null stats");
+  int32_t rc = check(c);
+  if (rc) return rc;
+  const int32_t st = mpm_sync(c);
+  if (st == MPM_ERR_CUDA) return st;
+  out->n_particles = c->prm.n;
+  out->n_particle_blocks = c->h_cnt->n_buckets;
+  out->n_grid_blocks = c->h_cnt->n_gblocks;
+  float f;
+  std::memcpy(&f, &c->h_cnt->max_vel_sqr_bits, sizeof(float));
+  out->max_vel_sqr = f;
+  out->status = st;
+  out->substeps = c->substeps;
+  return MPM_OK;
+}
+
+int32_t mpm_partition_download(mpm_ctx *c, int32_t *n_pb, int32_t *pb_dir, int32_t *pb_count,
+                               int64_t cap_pb, int32_t *perm, int32_t *n_gb, int32_t *gb_dir,
+                               int64_t cap_gb) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "no partition of the current positions");
+  if ((rc = mpm_sync(c))) return rc;
+  const int nb = c->h_cnt->n_buckets, ng = c->h_cnt->n_gblocks;
+  if (n_pb) *n_pb = nb;
+  if (n_gb) *n_gb = ng;
+  if ((pb_dir || pb_count) && cap_pb < nb) return fail(MPM_ERR_CAPACITY, "cap_pb too small");
+  if (gb_dir && cap_gb < ng) return fail(MPM_ERR_CAPACITY, "cap_gb too small");
+  if (pb_dir) ZS_CUDA(cudaMemcpy(pb_dir, c->d.bk_dir, nb * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (pb_count)
+    ZS_CUDA(cudaMemcpy(pb_count, c->d.bk_count, nb * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (gb_dir) ZS_CUDA(cudaMemcpy(gb_dir, c->d.gb_dir, ng * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (perm) {
+    const long long n = c->prm.n;
+    std::vector<int32_t> p(n), id(n);
+    ZS_CUDA(cudaMemcpy(p.data(), c->d.perm, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    ZS_CUDA(cudaMemcpy(id.data(), c->d.ibuf[c->cur] + (size_t)IC_ID * c->d.cap,
+                       n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    const int binned = std::min<long long>(c->h_cnt->n_binned, n);
+    for (long long s = 0; s < n; ++s)
+      perm[s] = (s < binned && p[s] >= 0 && p[s] < n) ? id[p[s]] : -1;
+  }
+  return MPM_OK;
+}
+
+int32_t mpm_grid_download(mpm_ctx *c, float *nodes, int64_t cap_floats) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = mpm_sync(c))) return rc;
+  const long long ng = c->h_cnt->n_gblocks;
+  if (!nodes || cap_floats < ng * 256) return fail(MPM_ERR_CAPACITY, "node buffer too small");
+  ZS_CUDA(cudaMemcpy(nodes, c->d.grid, ng * 64 * sizeof(float4), cudaMemcpyDeviceToHost));
+  return MPM_OK;
+}
+
+}  // extern "C"

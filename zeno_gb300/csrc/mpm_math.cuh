@@ -1,0 +1,217 @@
+// Device math of the substep: quadratic B-spline stencil, symmetric 3x3
+// eigen-decomposition, Kirchhoff stresses and the Drucker-Prager return
+// mapping.  The reference takes these from zpc (absent from the reference
+// tree); each routine here is written from the published method it names.
+//
+// All strain measures are formed from G = F - I, which is exact in FP32 for
+// the diagonal (Sterbenz) and unchanged off the diagonal, so that
+// E = B - I = G G^T + G + G^T and J - 1 carry small strains without the
+// cancellation of forming B = F F^T and subtracting I.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "zsmpm_internal.cuh"
+
+namespace zsmpm {
+
+struct Sym3 {
+  float xx, yy, zz, xy, xz, yz;
+};
+
+// One Jacobi rotation on the (p, q) plane, r the third index (Golub & Van
+// Loan, Matrix Computations, sym.schur2: theta = (a_qq - a_pp) / (2 a_pq),
+// t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)), c = 1/sqrt(1+t^2), s = t c;
+// A <- J^T A J, Q <- Q J with J_pp = J_qq = c, J_pq = s, J_qp = -s).
+__device__ __forceinline__ void jacobi_rot(float &app, float &aqq, float &apq, float &arp,
+                                           float &arq, float (&Q)[9], int p, int q) {
+  if (fabsf(apq) <= 1e-30f) return;
+  const float theta = 0.5f * (aqq - app) / apq;
+  const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.0f)));
+  const float c = rsqrtf(fmaf(t, t, 1.0f));
+  const float s = t * c;
+  app = fmaf(-t, apq, app);
+  aqq = fmaf(t, apq, aqq);
+  apq = 0.0f;
+  const float rp = arp, rq = arq;
+  arp = c * rp - s * rq;
+  arq = s * rp + c * rq;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float qp = Q[k * 3 + p], qq = Q[k * 3 + q];
+    Q[k * 3 + p] = c * qp - s * qq;
+    Q[k * 3 + q] = s * qp + c * qq;
+  }
+}
+
+// Cyclic Jacobi on a symmetric 3x3 matrix: A = Q diag(w) Q^T.
+__device__ __forceinline__ void sym_eig3(Sym3 a, float (&w)[3], float (&Q)[9]) {
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Q[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+  float d0 = a.xx, d1 = a.yy, d2 = a.zz, o01 = a.xy, o02 = a.xz, o12 = a.yz;
+#pragma unroll 1
+  for (int sweep = 0; sweep < 6; ++sweep) {
+    const float off = o01 * o01 + o02 * o02 + o12 * o12;
+    const float dia = d0 * d0 + d1 * d1 + d2 * d2;
+    if (off <= 1e-14f * dia || off == 0.0f) break;
+    jacobi_rot(d0, d1, o01, o02, o12, Q, 0, 1);  // r = 2: a_r0 = o02, a_r1 = o12
+    jacobi_rot(d0, d2, o02, o01, o12, Q, 0, 2);  // r = 1: a_r0 = o01, a_r2 = o12
+    jacobi_rot(d1, d2, o12, o01, o02, Q, 1, 2);  // r = 0: a_r1 = o01, a_r2 = o02
+  }
+  w[0] = d0;
+  w[1] = d1;
+  w[2] = d2;
+}
+
+// Q diag(d) Q^T
+__device__ __forceinline__ Sym3 qdqt(const float (&Q)[9], float d0, float d1, float d2) {
+  Sym3 r;
+  r.xx = Q[0] * Q[0] * d0 + Q[1] * Q[1] * d1 + Q[2] * Q[2] * d2;
+  r.yy = Q[3] * Q[3] * d0 + Q[4] * Q[4] * d1 + Q[5] * Q[5] * d2;
+  r.zz = Q[6] * Q[6] * d0 + Q[7] * Q[7] * d1 + Q[8] * Q[8] * d2;
+  r.xy = Q[0] * Q[3] * d0 + Q[1] * Q[4] * d1 + Q[2] * Q[5] * d2;
+  r.xz = Q[0] * Q[6] * d0 + Q[1] * Q[7] * d1 + Q[2] * Q[8] * d2;
+  r.yz = Q[3] * Q[6] * d0 + Q[4] * Q[7] * d1 + Q[5] * Q[8] * d2;
+  return r;
+}
+
+// E = F F^T - I from G = F - I, and J - 1 = det(I + G) - 1 expanded in G.
+__device__ __forceinline__ void strain_of(const float (&F)[9], Sym3 &E, float &Jm1) {
+  const float g0 = F[0] - 1.0f, g1 = F[1], g2 = F[2];
+  const float g3 = F[3], g4 = F[4] - 1.0f, g5 = F[5];
+  const float g6 = F[6], g7 = F[7], g8 = F[8] - 1.0f;
+  E.xx = g0 * g0 + g1 * g1 + g2 * g2 + 2.0f * g0;
+  E.yy = g3 * g3 + g4 * g4 + g5 * g5 + 2.0f * g4;
+  E.zz = g6 * g6 + g7 * g7 + g8 * g8 + 2.0f * g8;
+  E.xy = g0 * g3 + g1 * g4 + g2 * g5 + g1 + g3;
+  E.xz = g0 * g6 + g1 * g7 + g2 * g8 + g2 + g6;
+  E.yz = g3 * g6 + g4 * g7 + g5 * g8 + g5 + g7;
+  const float m2 = (g0 * g4 - g1 * g3) + (g0 * g8 - g2 * g6) + (g4 * g8 - g5 * g7);
+  const float dg = g0 * (g4 * g8 - g5 * g7) - g1 * (g3 * g8 - g5 * g6) + g2 * (g3 * g7 - g4 * g6);
+  Jm1 = (g0 + g4 + g8) + m2 + dg;
+}
+
+// Kirchhoff stress tau = P F^T (the reference scatters -dt*Dinv*vol*P*F^T,
+// Transfer.cu:868):
+//  fixed corotated (Stomakhin et al. 2012): tau = 2mu U diag(s^2 - s^) U^T
+//      + lam (J-1) J I, with B = U S^2 U^T and s^ the singular values with the
+//      smallest negated when J < 0 (R F^T = U S^ U^T);
+//  Neo-Hookean: tau = mu (B - I) + lam ln(J) I;
+//  StVK-Hencky (Klar et al. 2016): tau = U diag(2mu e_i + lam sum e) U^T,
+//      e_i = ln s_i;
+//  equation-of-state fluid (Tait form, Becker & Teschner 2007):
+//      p = K (J^-gamma - 1), tau = -p J I.
+// Returns false for an inverted or degenerate state the model cannot take.
+__device__ __forceinline__ bool kirchhoff(int type, float mu, float lam, float bulk, float gam,
+                                          const float (&F)[9], float Jeos, Sym3 &tau) {
+  if (type == MPM_EOS) {
+    const float t = -bulk * Jeos * expm1f(-gam * logf(Jeos));
+    tau = Sym3{t, t, t, 0.f, 0.f, 0.f};
+    return Jeos > 0.0f;
+  }
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  const float J = 1.0f + Jm1;
+  if (type == MPM_NHK) {
+    const float diag = lam * log1pf(Jm1);
+    tau = Sym3{mu * E.xx + diag, mu * E.yy + diag, mu * E.zz + diag, mu * E.xy, mu * E.xz,
+               mu * E.yz};
+    return J > 0.0f;
+  }
+  float w[3], Q[9];
+  sym_eig3(E, w, Q);
+  if (type == MPM_FCR) {
+    float d[3], s[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float lamk = fmaxf(w[k], -1.0f);  // eigenvalue of B - I
+      s[k] = sqrtf(1.0f + lamk);
+      d[k] = s[k] * lamk / (s[k] + 1.0f);     // s^2 - s
+    }
+    if (J < 0.0f) {
+      const int kmin = (s[0] <= s[1] && s[0] <= s[2]) ? 0 : ((s[1] <= s[2]) ? 1 : 2);
+      d[kmin] = s[kmin] * s[kmin] + s[kmin];  // s^2 - (-s)
+    }
+    tau = qdqt(Q, 2.0f * mu * d[0], 2.0f * mu * d[1], 2.0f * mu * d[2]);
+    const float diag = lam * Jm1 * J;
+    tau.xx += diag;
+    tau.yy += diag;
+    tau.zz += diag;
+    return true;
+  }
+  // StVK with Hencky strain
+  const float e0 = 0.5f * log1pf(w[0]), e1 = 0.5f * log1pf(w[1]), e2 = 0.5f * log1pf(w[2]);
+  const float tr = e0 + e1 + e2;
+  tau = qdqt(Q, 2.0f * mu * e0 + lam * tr, 2.0f * mu * e1 + lam * tr, 2.0f * mu * e2 + lam * tr);
+  return w[0] > -1.0f && w[1] > -1.0f && w[2] > -1.0f;
+}
+
+// Non-associative Drucker-Prager return mapping in Hencky strain space
+// (Klar et al. 2016, sec. 7.3), the ZSReturnMapping node
+// (MPMPipeline.cu:958-971): with F = U S V^T and B = U S^2 U^T the projected
+// F is U S' V^T = F + U diag(S'/S - 1) U^T F.  Returns -1 on a degenerate F,
+// 1 if projected, 0 if inside the yield surface.
+__device__ __forceinline__ int project_dp(float mu, float lam, float alpha, float (&F)[9]) {
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  float w[3], Q[9];
+  sym_eig3(E, w, Q);
+  if (!(w[0] > -1.0f && w[1] > -1.0f && w[2] > -1.0f)) return -1;
+  const float e0 = 0.5f * log1pf(w[0]), e1 = 0.5f * log1pf(w[1]), e2 = 0.5f * log1pf(w[2]);
+  const float tr = e0 + e1 + e2;
+  float r0, r1, r2;  // S'/S - 1
+  if (tr >= 0.0f) {
+    r0 = expm1f(-e0);
+    r1 = expm1f(-e1);
+    r2 = expm1f(-e2);
+  } else {
+    const float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
+    const float nrm = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
+    const float dg = nrm + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * alpha;
+    if (dg <= 0.0f) return 0;
+    const float k = dg / nrm;
+    r0 = expm1f(-k * h0);
+    r1 = expm1f(-k * h1);
+    r2 = expm1f(-k * h2);
+  }
+  const Sym3 M = qdqt(Q, r0, r1, r2);
+  float Fn[9];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Fn[0 * 3 + j] = F[0 * 3 + j] + M.xx * F[j] + M.xy * F[3 + j] + M.xz * F[6 + j];
+    Fn[1 * 3 + j] = F[1 * 3 + j] + M.xy * F[j] + M.yy * F[3 + j] + M.yz * F[6 + j];
+    Fn[2 * 3 + j] = F[2 * 3 + j] + M.xz * F[j] + M.yz * F[3 + j] + M.zz * F[6 + j];
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) F[i] = Fn[i];
+  return 1;
+}
+
+__device__ __forceinline__ float det3(const float (&F)[9]) {
+  return F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+         F[2] * (F[3] * F[7] - F[4] * F[6]);
+}
+
+// Quadratic B-spline weights (Hu et al. 2018 MLS-MPM; Jiang et al. 2016
+// course notes): f = x/dx - base in [0.5, 1.5),
+// w0 = (1.5-f)^2/2, w1 = 3/4 - (f-1)^2, w2 = (f-0.5)^2/2.
+struct Stencil1 {
+  int base;
+  float f;
+  float w[3];
+};
+
+__device__ __forceinline__ Stencil1 stencil1(float x, float inv_dx) {
+  Stencil1 s;
+  s.base = __float2int_rd(__fsub_rn(__fmul_rn(x, inv_dx), 0.5f));
+  s.f = __fsub_rn(__fmul_rn(x, inv_dx), (float)s.base);
+  const float a = 1.5f - s.f, b = s.f - 1.0f, c = s.f - 0.5f;
+  s.w[0] = 0.5f * a * a;
+  s.w[1] = 0.75f - b * b;
+  s.w[2] = 0.5f * c * c;
+  return s;
+}
+
+}  // namespace zsmpm

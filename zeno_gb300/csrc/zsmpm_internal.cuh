@@ -1,0 +1,130 @@
+// Internal declarations shared by the zsmpm translation units.
+//
+// HBM layout (one context):
+//  * particles: two buffers (current / next substep), each `NCH` float planes
+//    of `cap` floats plus `NICH` int32 planes.  A plane holds one scalar
+//    channel for every particle, so a warp reads 32 consecutive particles of
+//    a channel as one 128-byte line.  The substep re-orders particles by
+//    (block, cell) as G2P writes the next buffer, so the next substep's
+//    reads through the sort permutation are near-sequential.
+//  * block directory: dense int32 arrays over every 4^3 block of the domain
+//    box (a perfect hash of block coordinates), holding particle counts,
+//    scatter cursors and the grid block index.
+//  * grid: `cap_gblocks` blocks x 64 nodes x float4 (m, mv / v), node cell id
+//    (i << 4) | (j << 2) | k inside the block.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/zsmpm.h"
+
+namespace zsmpm {
+
+// float particle channels (planes)
+enum : int {
+  CH_X = 0,     // 3
+  CH_V = 3,     // 3
+  CH_C = 6,     // 9, row-major
+  CH_F = 15,    // 9, row-major
+  CH_J = 24,    // 1
+  CH_M = 25,    // 1
+  CH_VOL = 26,  // 1
+  CH_MU = 27,   // 1, per-particle override (optional)
+  CH_LAM = 28,  // 1, per-particle override (optional)
+  NCH = 29
+};
+// int particle channels
+enum : int { IC_MAT = 0, IC_ID = 1, NICH = 2 };
+
+// device status bits (OR-ed into Counters::status)
+enum : int {
+  ST_OUT_OF_DOMAIN = 1,
+  ST_CAPACITY = 2,
+  ST_NAN = 4,
+  ST_BUCKET_OVERSIZE = 8,
+  ST_TIMEOUT = 16,
+  ST_STENCIL = 32
+};
+
+constexpr int kMaxMaterials = 64;
+constexpr int kScanTile = 4096;       // directory entries per scan tile
+constexpr int kScanThreads = 256;     // 16 entries per thread
+constexpr int kMaxSortBucket = 4096;  // particles per block sorted on chip
+
+struct MatParams {
+  int type, plastic;
+  float mu, lam, alpha, bulk, gamma, pad;
+};
+
+struct Counters {
+  int n_gblocks;  // grid blocks of the current partition (clamped to capacity)
+  int n_buckets;  // non-empty particle blocks
+  int status;
+  unsigned max_vel_sqr_bits;
+  int n_binned;
+  int pad[3];
+};
+
+// Device-resident parameters; the host updates them with one small copy
+// when they change, so captured graphs read the current values.
+struct SimParams {
+  float dt, dx, inv_dx, Dinv;
+  float gravity[3];
+  int block_lo[3];
+  int block_dims[3];
+  int bc_type, bc_thickness;
+  int bc_lo[3], bc_hi[3];
+  int n_materials;
+  int has_lame;
+  long long n;
+};
+
+struct DevPtrs {
+  float *pbuf[2];
+  int32_t *ibuf[2];
+  long long cap;  // particle plane stride
+  int32_t *pkey;  // (directory index << 6) | cell, per storage slot
+  int32_t *perm;  // sorted position -> storage slot
+  int32_t *dir_count, *dir_fill, *dir_gb;
+  uint8_t *dir_flag;
+  long long ndir;
+  int32_t *gb_dir;
+  int32_t *bk_dir, *bk_start, *bk_count;
+  int cap_gblocks;
+  float4 *grid;
+  int32_t *tile_sums;
+  int ntiles;
+  Counters *cnt;
+  SimParams *prm;
+  MatParams *mats;
+  int num_sms;
+};
+
+// partition.cu
+void launch_reset(const DevPtrs &d, cudaStream_t s);
+void launch_bin(const DevPtrs &d, int cur, cudaStream_t s);
+void launch_scan(const DevPtrs &d, cudaStream_t s);
+void launch_scatter(const DevPtrs &d, cudaStream_t s);
+void launch_bucket_sort(const DevPtrs &d, cudaStream_t s);
+void launch_grid_clear(const DevPtrs &d, cudaStream_t s);
+void launch_full_dir_clear(const DevPtrs &d, cudaStream_t s);
+
+// transfer.cu
+void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s);
+// mode bit 1: momentum -> velocity + gravity, bit 2: boundary
+void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s);
+void launch_g2p(const DevPtrs &d, int cur, int fuse_return_mapping, cudaStream_t s);
+void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s);
+
+// io.cu
+struct IngestSrc {
+  const float *x, *v, *C, *F, *J, *m, *vol, *mu, *lam;
+  const int32_t *mat;
+};
+void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s);
+// writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
+void launch_egest(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s);
+
+}  // namespace zsmpm

@@ -1,0 +1,284 @@
+"""Python binding of the zsmpm C ABI (include/zsmpm.h) over ctypes.
+
+This is a thin host-side mirror of the reference's MPM node sequence: a
+`Context` is the ZSGrid + ZSPartition + ZSParticles objects of one scene,
+and its methods are the nodes (`partition` = ZSPartitionForZSParticles +
+ExpandZSPartition, `p2g` = ZSParticleToZSGrid, ...).  Every call goes to the
+CUDA library; there is no CPU path.  Loading fails loudly when the library
+has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libzsmpm.so")
+
+MPM_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid", 2: "cuda", 3: "capacity", 4: "out_of_domain", 5: "cfl",
+                6: "nan", 7: "timeout", 8: "no_device", 9: "state"}
+
+
+class MPMError(RuntimeError):
+    def __init__(self, code: int, where: str, text: str):
+        self.code = code
+        super().__init__(f"{where}: {STATUS_NAMES.get(code, code)} ({code}): {text}")
+
+
+class CtxDesc(C.Structure):
+    _fields_ = [("device", C.c_int32), ("dx", C.c_float), ("block_lo", C.c_int32 * 3),
+                ("block_dims", C.c_int32 * 3), ("max_particles", C.c_int64),
+                ("max_grid_blocks", C.c_int32), ("flags", C.c_int32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("plasticity", C.c_int32), ("E", C.c_float),
+                ("nu", C.c_float), ("density", C.c_float), ("friction_angle_deg", C.c_float),
+                ("bulk", C.c_float), ("gamma", C.c_float)]
+
+
+class Boundary(C.Structure):
+    _fields_ = [("type", C.c_int32), ("thickness", C.c_int32), ("lo", C.c_int32 * 3),
+                ("hi", C.c_int32 * 3)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("n_particles", C.c_int64), ("n_particle_blocks", C.c_int32),
+                ("n_grid_blocks", C.c_int32), ("max_vel_sqr", C.c_float), ("status", C.c_int32),
+                ("substeps", C.c_int64)]
+
+
+EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destroy",
+           "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
+           "mpm_particles_upload", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
+           "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
+           "mpm_substep", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
+           "mpm_grid_download"]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libzsmpm.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    P = C.c_void_p
+    i32, i64, f32 = C.c_int32, C.c_int64, C.c_float
+    sig = {
+        "mpm_abi_version": ([], i32),
+        "mpm_last_error": ([], C.c_char_p),
+        "mpm_ctx_create": ([C.POINTER(CtxDesc), C.POINTER(C.c_void_p)], i32),
+        "mpm_ctx_destroy": ([P], i32),
+        "mpm_set_stream": ([P, P], i32),
+        "mpm_set_materials": ([P, C.POINTER(Material), i32], i32),
+        "mpm_set_boundary": ([P, C.POINTER(Boundary)], i32),
+        "mpm_set_gravity": ([P, f32, f32, f32], i32),
+        "mpm_particles_upload": ([P, i64] + [P] * 10, i32),
+        "mpm_particles_download": ([P] + [P] * 5, i32),
+        "mpm_partition": ([P], i32),
+        "mpm_grid_clear": ([P], i32),
+        "mpm_p2g": ([P, f32], i32),
+        "mpm_grid_update": ([P, f32, P], i32),
+        "mpm_apply_boundary": ([P], i32),
+        "mpm_g2p": ([P, f32], i32),
+        "mpm_return_mapping": ([P], i32),
+        "mpm_substep": ([P, f32, i32], i32),
+        "mpm_sync": ([P], i32),
+        "mpm_get_stats": ([P, C.POINTER(Stats)], i32),
+        "mpm_partition_download": ([P, P, P, P, i64, P, P, P, i64], i32),
+        "mpm_grid_download": ([P, P, i64], i32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a, shape):
+    if a is None:
+        return None
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(shape))
+
+
+class Context:
+    """One MPM scene on one GPU (ZSGrid + ZSPartition + ZSParticles)."""
+
+    def __init__(self, scene, max_particles: int, device: int = 0, max_grid_blocks: int = 0):
+        L = load()
+        self._L = L
+        desc = CtxDesc(device, float(scene.dx), (C.c_int32 * 3)(*scene.block_lo),
+                       (C.c_int32 * 3)(*scene.block_dims), int(max_particles),
+                       int(max_grid_blocks), 0)
+        h = C.c_void_p()
+        self._check(L.mpm_ctx_create(C.byref(desc), C.byref(h)), "mpm_ctx_create")
+        self.h = h
+        self.scene = scene
+        self.n = 0
+        self.set_materials(scene.materials)
+        self.set_boundary(scene.bc_type, scene.bc_thickness, scene.bc_lo, scene.bc_hi)
+        self.set_gravity(*scene.gravity)
+
+    def _check(self, rc: int, where: str):
+        if rc != MPM_OK:
+            raise MPMError(rc, where, self._L.mpm_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.mpm_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ConfigConstitutiveModel / ToZSBoundary / UpdateZSGrid inputs
+    def set_materials(self, mats):
+        arr = (Material * len(mats))(*[Material(int(m.type), int(m.plasticity), float(m.E),
+                                                float(m.nu), float(m.density),
+                                                float(m.friction_angle_deg), float(m.bulk),
+                                                float(m.gamma)) for m in mats])
+        self._check(self._L.mpm_set_materials(self.h, arr, len(mats)), "mpm_set_materials")
+
+    def set_boundary(self, bc_type, thickness, lo, hi):
+        b = Boundary(int(bc_type), int(thickness), (C.c_int32 * 3)(*lo), (C.c_int32 * 3)(*hi))
+        self._check(self._L.mpm_set_boundary(self.h, C.byref(b)), "mpm_set_boundary")
+
+    def set_gravity(self, gx, gy, gz):
+        self._check(self._L.mpm_set_gravity(self.h, gx, gy, gz), "mpm_set_gravity")
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._L.mpm_set_stream(self.h, C.c_void_p(stream_ptr or 0)), "mpm_set_stream")
+
+    # ToZSParticles / UpdatePrimitiveFromZSParticles
+    def upload(self, parts):
+        n = parts.n
+        x = _f32(parts.x, (n, 3))
+        v = _f32(parts.v, (n, 3))
+        Cm = _f32(parts.C, (n, 9))
+        F = _f32(parts.F, (n, 9))
+        J = _f32(parts.J, (n,))
+        m = _f32(parts.m, (n,))
+        vol = _f32(parts.vol, (n,))
+        mat = np.ascontiguousarray(parts.mat, dtype=np.int32)
+        mu = _f32(parts.mu, (n,))
+        lam = _f32(parts.lam, (n,))
+        self._keep = (x, v, Cm, F, J, m, vol, mat, mu, lam)
+        self._check(self._L.mpm_particles_upload(self.h, n, _p(x), _p(v), _p(Cm), _p(F), _p(J),
+                                                 _p(m), _p(vol), _p(mat), _p(mu), _p(lam)),
+                    "mpm_particles_upload")
+        self.n = n
+
+    def upload_raw(self, n, x, v=None, Cm=None, F=None, J=None, m=None, vol=None, mat=None,
+                   mu=None, lam=None):
+        """Upload from caller-owned contiguous float32 / int32 arrays (no copy)."""
+        self._check(self._L.mpm_particles_upload(self.h, n, _p(x), _p(v), _p(Cm), _p(F), _p(J),
+                                                 _p(m), _p(vol), _p(mat), _p(mu), _p(lam)),
+                    "mpm_particles_upload")
+        self.n = n
+
+    def download(self, channels=("x", "v", "C", "F", "J")) -> dict:
+        n = self.n
+        out = {}
+        shapes = {"x": (n, 3), "v": (n, 3), "C": (n, 3, 3), "F": (n, 3, 3), "J": (n,)}
+        for k in ("x", "v", "C", "F", "J"):
+            out[k] = np.empty(shapes[k], np.float32) if k in channels else None
+        self._check(self._L.mpm_particles_download(self.h, _p(out["x"]), _p(out["v"]),
+                                                   _p(out["C"]), _p(out["F"]), _p(out["J"])),
+                    "mpm_particles_download")
+        return {k: v for k, v in out.items() if v is not None}
+
+    def download_raw(self, x=None, v=None):
+        self._check(self._L.mpm_particles_download(self.h, _p(x), _p(v), None, None, None),
+                    "mpm_particles_download")
+
+    # the substep nodes
+    def partition(self):
+        self._check(self._L.mpm_partition(self.h), "mpm_partition")
+
+    def grid_clear(self):
+        self._check(self._L.mpm_grid_clear(self.h), "mpm_grid_clear")
+
+    def p2g(self, dt):
+        self._check(self._L.mpm_p2g(self.h, dt), "mpm_p2g")
+
+    def grid_update(self, dt, read_max: bool = True):
+        out = C.c_float(0.0)
+        self._check(self._L.mpm_grid_update(self.h, dt, C.byref(out) if read_max else None),
+                    "mpm_grid_update")
+        return out.value if read_max else None
+
+    def apply_boundary(self):
+        self._check(self._L.mpm_apply_boundary(self.h), "mpm_apply_boundary")
+
+    def g2p(self, dt):
+        self._check(self._L.mpm_g2p(self.h, dt), "mpm_g2p")
+
+    def return_mapping(self):
+        self._check(self._L.mpm_return_mapping(self.h), "mpm_return_mapping")
+
+    def staged_substep(self, dt):
+        """One substep through the node-by-node entry points."""
+        self.partition()
+        self.grid_clear()
+        self.p2g(dt)
+        vmax = self.grid_update(dt, read_max=False)
+        self.apply_boundary()
+        self.g2p(dt)
+        self.return_mapping()
+        return vmax
+
+    def substep(self, dt, n: int = 1):
+        self._check(self._L.mpm_substep(self.h, dt, int(n)), "mpm_substep")
+
+    def sync(self):
+        self._check(self._L.mpm_sync(self.h), "mpm_sync")
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self._L.mpm_get_stats(self.h, C.byref(s)), "mpm_get_stats")
+        return {"n_particles": s.n_particles, "n_particle_blocks": s.n_particle_blocks,
+                "n_grid_blocks": s.n_grid_blocks, "max_vel_sqr": s.max_vel_sqr,
+                "status": s.status, "substeps": s.substeps}
+
+    def partition_download(self) -> dict:
+        D = int(np.prod(self.scene.block_dims))
+        n_pb = np.zeros(1, np.int32)
+        n_gb = np.zeros(1, np.int32)
+        pb_dir = np.zeros(D, np.int32)
+        pb_count = np.zeros(D, np.int32)
+        gb_dir = np.zeros(D, np.int32)
+        perm = np.zeros(max(self.n, 1), np.int32)
+        self._check(self._L.mpm_partition_download(self.h, _p(n_pb), _p(pb_dir), _p(pb_count), D,
+                                                   _p(perm), _p(n_gb), _p(gb_dir), D),
+                    "mpm_partition_download")
+        return {"pb_dir": pb_dir[:n_pb[0]].copy(), "pb_count": pb_count[:n_pb[0]].copy(),
+                "perm": perm[:self.n].astype(np.int64), "gb_dir": gb_dir[:n_gb[0]].copy()}
+
+    def grid_download(self) -> np.ndarray:
+        st = self.stats()
+        ng = st["n_grid_blocks"]
+        out = np.zeros((max(ng, 1), 64, 4), np.float32)
+        self._check(self._L.mpm_grid_download(self.h, _p(out), out.size), "mpm_grid_download")
+        return out[:ng]
