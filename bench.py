@@ -1,0 +1,398 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 MLS-MPM substep, in particle-substeps/s.
+
+Workload: the plain four-material scene -- 2,097,152 FP32 particles at
+dx = 1/256 (fixed-corotated E=1e5, Neo-Hookean E=5e4, Drucker-Prager sand
+30 deg, equation-of-state fluid K=1e4 gamma=7; 8 ppc jittered; v ~ N(0, 0.5^2);
+slip walls 3 cells thick; dt = 1e-4).  One step = one full substep
+(partition + sort, grid clear, P2G, grid update + boundary, G2P + return
+mapping) of every particle, replayed as a CUDA graph.  The particle state
+(2 x 243 MB double buffer) is larger than L2, so no flush is needed between
+steps.
+
+Arms:
+  default           the CUDA library (zeno_gb300/libzsmpm.so) via its C ABI
+  --impl reference  the reference's CPU path: the reference substep cannot be
+                    built (its arithmetic lives in the absent zpc submodule and
+                    it has no CPU execution of the substep), so this times the
+                    FP32 OpenMP restatement of the node bodies in oracle/ on
+                    all host cores, a bounded sample per step.
+
+Multi-GPU: the substep of one scene does not shard here, so N GPUs run N
+independent replicas (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-substeps/s"
+KERNELS_PER_SUBSTEP = 10  # reset, bin, scan x2, scatter, sort, clear, p2g, grid update, g2p
+WORKLOAD = ("plain MLS-MPM substep, four-material scene (FCR E=1e5, NHK E=5e4, "
+            "Drucker-Prager sand 30deg, EOS fluid K=1e4 gamma=7), 2,097,152 FP32 particles, "
+            "dx=1/256, dt=1e-4, slip walls")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload():
+    from zeno_gb300 import scenes
+    return scenes.multi_material(seed=0)
+
+
+def algorithmic_bytes(parts, scene, n_gblocks):
+    """Algorithmic HBM bytes per substep and per kernel.
+
+    Per particle (FP32): P2G reads x, v, C, F, m, vol (104 B); G2P reads
+    x, F (48 B) and writes x, v, C, F (96 B): 248 B.  The fluid carries J
+    instead of F: P2G 72 B, G2P reads x, J (16 B) and writes x, v, C, J (64 B):
+    152 B.  Per grid node: clear 16 + accumulate 16 + update read 16 / write
+    12 + G2P read 12 = 72 B.  Partition and sort traffic is implementation
+    overhead: in the time, not in these bytes."""
+    from zeno_gb300 import scenes
+    eos_ids = [i for i, m in enumerate(scene.materials) if m.type == scenes.EOS]
+    n_eos = int(np.isin(parts.mat, eos_ids).sum())
+    n_f = parts.n - n_eos
+    nodes = 64 * n_gblocks
+    return {
+        "substep": 248 * n_f + 152 * n_eos + 72 * nodes,
+        "p2g": 104 * n_f + 72 * n_eos + 16 * nodes,
+        "g2p": 144 * n_f + 80 * n_eos + 12 * nodes,
+        "grid_update": 28 * nodes,
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append((time.perf_counter(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+
+    def summary(self, t0, t1):
+        sel = [r for (t, r) in self.rows if t0 - 0.06 <= t <= t1 + 0.06] or \
+              [r for (_, r) in self.rows]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in sel:
+            f = [x.strip() for x in r.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of each kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def cpu_baseline(parts, scene, target_s: float = 10.0):
+    """FP32 OpenMP restatement (oracle/) on all host cores, bounded sample."""
+    from oracle import oracle
+    oracle.build()
+    cores = oracle.max_threads()
+    t0 = time.perf_counter()
+    q, st = oracle.run(scene, parts, 1, "f32")
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(50, int(target_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    oracle.run(scene, q, steps, "f32", inplace=True)
+    dt = time.perf_counter() - t0
+    return {"value": parts.n * steps / dt, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{steps} substeps of the full {parts.n:,}-particle scene "
+                      f"(after 1 warm-up substep), FP32 OpenMP restatement of the node bodies"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle
+    oracle.build()
+    scene, parts = make_workload()
+    cores = oracle.max_threads()
+    # size each step so that W + K steps end within about two minutes
+    t0 = time.perf_counter()
+    q, _ = oracle.run(scene, parts, 1, "f32")
+    t_full = time.perf_counter() - t0
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    frac = min(1.0, budget / max(t_full, 1e-6))
+    n_sample = max(4096, int(parts.n * frac))
+    from zeno_gb300 import scenes as S
+    sub = S.Particles(*(None if a is None else np.ascontiguousarray(a[:n_sample]) for a in
+                        (q.x, q.v, q.C, q.F, q.J, q.m, q.vol, q.mat, q.mu, q.lam)))
+    for _ in range(args.warmup):
+        oracle.run(scene, sub, 1, "f32", inplace=True)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.run(scene, sub, 1, "f32", inplace=True)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sub.n * args.steps / total
+    sample = (f"each step: 1 substep of the first {sub.n:,} of {parts.n:,} particles "
+              f"of the scene (FP32 OpenMP restatement, {cores} threads)")
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded SplitMix64 scene)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "particles": parts.n, "form": "plain"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference MPM substep needs the absent zpc submodule and has no CPU "
+                    "execution; this arm times the oracle's FP32 OpenMP restatement"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    dev = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(dev)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    from zeno_gb300 import zsmpm
+    scene, parts = make_workload()
+    ctx = zsmpm.Context(scene, max_particles=parts.n, device=dev)
+    # a dedicated stream (a non-zero handle): the context's kernels and the
+    # timing events below are ordered on it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(parts)
+    dt = scene.dt
+
+    # warm-up (captures both graph parities)
+    ctx.substep(dt, max(args.warmup, 3))
+    ctx.sync()
+
+    sampler = ClockSampler(dev)
+    if not args.quick:
+        sampler.start()
+        # keep the GPU busy ~0.4 s so the sampler sees the loaded clock
+        t_busy = time.perf_counter()
+        while time.perf_counter() - t_busy < 0.4:
+            ctx.substep(dt, 20)
+            ctx.sync()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    c0 = time.perf_counter()
+    e0.record(stream)
+    ctx.substep(dt, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    c1 = time.perf_counter()
+    if pg:
+        pg.barrier()
+    sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    ctx.sync()
+    st = ctx.stats()
+    value = ws * parts.n * args.steps / (ms * 1e-3)
+
+    # live per-stage device times (CUDA events between the same kernels)
+    stage_runs = [ctx.substep_timed(dt) for _ in range(max(5, min(args.steps, 30)))]
+    stage_ms = {k: statistics.mean(r[k] for r in stage_runs) for k in stage_runs[0]}
+    ctx.sync()
+    st = ctx.stats()
+    ab = algorithmic_bytes(parts, scene, st["n_grid_blocks"])
+    peak, peak_kind = measured_peaks()
+    dom = max(("p2g", "g2p", "grid_update"), key=lambda k: stage_ms[k])
+    achieved = ab[dom] / (stage_ms[dom] * 1e-3) / 1e9
+    traffic = ncu_traffic().get(dom)
+    sub_ms = sum(stage_ms.values())
+    substep_achieved = ab["substep"] / (ms / args.steps * 1e-3) / 1e9
+
+    if args.quick:
+        ctx.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": METRIC, "quick": True,
+                              "ms_per_step": ms / args.steps, "stage_ms": stage_ms,
+                              "roofline_kernel": dom, "achieved_gbs": achieved,
+                              "status": st["status"]}))
+        if pg:
+            pg.barrier()
+            pg.destroy_process_group()
+        return 0
+
+    # end to end through the C ABI with pinned host buffers
+    n = parts.n
+    pin = lambda shape, dtp=torch.float32: torch.empty(shape, dtype=dtp, pin_memory=True).numpy()
+    hx, hv, hC, hF, hJ = pin((n, 3)), pin((n, 3)), pin((n, 9)), pin((n, 9)), pin((n,))
+    hm, hvol, hmat = pin((n,)), pin((n,)), pin((n,), torch.int32)
+    hx[:] = parts.x
+    hv[:] = parts.v
+    hC[:] = parts.C.reshape(n, 9)
+    hF[:] = parts.F.reshape(n, 9)
+    hJ[:] = parts.J
+    hm[:] = parts.m
+    hvol[:] = parts.vol
+    hmat[:] = parts.mat
+    ox, ov = pin((n, 3)), pin((n, 3))
+    e2e_steps = max(3, min(args.steps, 50))
+    ctx.set_stream(None)
+    for _ in range(2):
+        ctx.upload_raw(n, hx, hv, hC, hF, hJ, hm, hvol, hmat)
+        ctx.substep(dt, 1)
+        ctx.download_raw(ox, ov)
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.upload_raw(n, hx, hv, hC, hF, hJ, hm, hvol, hmat)
+        ctx.substep(dt, 1)
+        ctx.download_raw(ox, ov)
+    t_e2e = time.perf_counter() - t0
+    if pg:
+        t = torch.tensor([t_e2e], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    ctx.sync()
+    h2d = sum(a.nbytes for a in (hx, hv, hC, hF, hJ, hm, hvol, hmat))
+    d2h = ox.nbytes + ov.nbytes
+    ctx.close()
+
+    if rank != 0:
+        if pg:
+            pg.barrier()
+            pg.destroy_process_group()
+        return 0
+    cpu = None if args.no_cpu else cpu_baseline(parts, scene)
+    clocks = sampler.summary(c0, c1)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 scene)",
+        "config": {"workload": WORKLOAD, "particles": parts.n, "dx": "1/256", "dt": dt,
+                   "form": "plain", "particle_blocks": st["n_particle_blocks"],
+                   "grid_blocks": st["n_grid_blocks"],
+                   "l2": "inputs larger than L2 (2 x 243 MB particle buffers)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes": ab[dom], "peak_source": peak_kind,
+                     "launch_ms": stage_ms[dom]},
+        "substep_roofline": {"achieved": substep_achieved, "frac": substep_achieved / peak,
+                             "algorithmic_bytes": ab["substep"], "unit": "GB/s"},
+        "stage_ms": {k: round(v, 5) for k, v in stage_ms.items()},
+        "stage_sum_ms": sub_ms,
+        "cpu_baseline": cpu,
+        "e2e": {"value": ws * n * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "step": "upload full particle state from pinned host memory, 1 substep, "
+                        "download x and v"},
+        "clocks": clocks,
+        "gpu_launches": KERNELS_PER_SUBSTEP * args.steps,
+        "status": st["status"],
+    }
+    print(json.dumps(line))
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--quick", action="store_true",
+                    help="device timing only (no clock sampling, e2e or CPU legs): for ncu")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -150,6 +150,25 @@ int32_t mpm_return_mapping(mpm_ctx *ctx);
  * G2P + return mapping) without host synchronisation. */
 int32_t mpm_substep(mpm_ctx *ctx, float dt, int32_t n_substeps);
 
+/* One substep like mpm_substep, launched without the graph and with a CUDA
+ * event between kernels; stage_ms[i] receives the device time of stage i
+ * (MPM_STAGE_*).  The device-timed counterpart of the host timer zeno wraps
+ * around every node's apply() when ZENO_BENCHMARKING is on
+ * (zeno/src/core/INode.cpp:141-143). */
+enum {
+  MPM_STAGE_RESET = 0,
+  MPM_STAGE_BIN = 1,
+  MPM_STAGE_SCAN = 2,
+  MPM_STAGE_SCATTER = 3,
+  MPM_STAGE_SORT = 4,
+  MPM_STAGE_CLEAR = 5,
+  MPM_STAGE_P2G = 6,
+  MPM_STAGE_GRID_UPDATE = 7,
+  MPM_STAGE_G2P = 8,
+  MPM_NUM_STAGES = 9
+};
+int32_t mpm_substep_timed(mpm_ctx *ctx, float dt, float *stage_ms, int32_t n_stages);
+
 /* Wait for the context's stream; returns the device status word. */
 int32_t mpm_sync(mpm_ctx *ctx);
 int32_t mpm_get_stats(mpm_ctx *ctx, mpm_stats *out);

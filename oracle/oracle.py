@@ -119,13 +119,16 @@ def partition(scene, x: np.ndarray) -> dict:
 
 
 def run(scene, parts, nsteps: int, precision: str = "f64", nthreads: int = 0,
-        dt: float | None = None):
-    """Advance a copy of `parts` by nsteps substeps; returns (particles, stats)."""
+        dt: float | None = None, inplace: bool = False):
+    """Advance `parts` (a copy unless inplace) by nsteps substeps; returns
+    (particles, stats).  inplace needs contiguous arrays of the precision."""
     dtype = np.float64 if precision == "f64" else np.float32
-    p = parts.copy(dtype=dtype)
+    p = parts if inplace else parts.copy(dtype=dtype)
     for k in ("x", "v", "C", "F", "J", "m", "vol", "mu", "lam"):
         a = getattr(p, k)
         if a is not None:
+            if inplace and (a.dtype != dtype or not a.flags.c_contiguous):
+                raise ValueError(f"in-place run needs contiguous {dtype.__name__} '{k}'")
             setattr(p, k, np.ascontiguousarray(a, dtype=dtype))
     p.mat = np.ascontiguousarray(p.mat, dtype=np.int32)
     h = _SceneHolder(scene)

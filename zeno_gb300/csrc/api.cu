@@ -52,7 +52,7 @@ struct mpm_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   Counters *h_cnt = nullptr;  // pinned
   std::vector<void *> allocs;
-  float last_max_vel_sqr = 0.0f;
+  cudaEvent_t events[MPM_NUM_STAGES + 1] = {};
 };
 
 namespace {
@@ -126,12 +126,31 @@ void enqueue_partition(mpm_ctx *c, int cur) {
   launch_bucket_sort(c->d, c->stream);
 }
 
-void enqueue_substep(mpm_ctx *c, int cur) {
-  enqueue_partition(c, cur);
+// One substep; with `ev` set, event i is recorded before stage i and event
+// MPM_NUM_STAGES after the last one.
+void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
+  auto mark = [&](int i) {
+    if (ev) cudaEventRecord(ev[i], c->stream);
+  };
+  mark(MPM_STAGE_RESET);
+  launch_reset(c->d, c->stream);
+  mark(MPM_STAGE_BIN);
+  launch_bin(c->d, cur, c->stream);
+  mark(MPM_STAGE_SCAN);
+  launch_scan(c->d, c->stream);
+  mark(MPM_STAGE_SCATTER);
+  launch_scatter(c->d, c->stream);
+  mark(MPM_STAGE_SORT);
+  launch_bucket_sort(c->d, c->stream);
+  mark(MPM_STAGE_CLEAR);
   launch_grid_clear(c->d, c->stream);
+  mark(MPM_STAGE_P2G);
   launch_p2g(c->d, cur, c->stream);
+  mark(MPM_STAGE_GRID_UPDATE);
   launch_grid_update(c->d, 3, c->stream);
+  mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, c->stream);
+  mark(MPM_NUM_STAGES);
 }
 
 bool graphs_enabled() {
@@ -207,7 +226,7 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
 
   const long long cap = desc->max_particles;
   long long capg = desc->max_grid_blocks > 0 ? desc->max_grid_blocks
-                                             : std::max<long long>(4096, cap / 16);
+                                             : std::max<long long>(16384, cap / 4);
   capg = std::min<long long>(capg, ndir);
   DevPtrs &d = c->d;
   d.cap = cap;
@@ -230,6 +249,13 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
     return bail(rc);
   if (cudaMallocHost(&c->h_cnt, sizeof(Counters)) != cudaSuccess)
     return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
+  // every slot of the particle-indexed buffers starts as a valid index / id
+  for (int k = 0; k < 2; ++k) {
+    cudaMemsetAsync(d.pbuf[k], 0, (size_t)NCH * cap * sizeof(float), c->stream);
+    cudaMemsetAsync(d.ibuf[k], 0, (size_t)NICH * cap * sizeof(int32_t), c->stream);
+  }
+  cudaMemsetAsync(d.perm, 0, (size_t)cap * sizeof(int32_t), c->stream);
+  cudaMemsetAsync(d.pkey, 0, (size_t)cap * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_count, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_fill, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_gb, 0xff, ndir * sizeof(int32_t), c->stream);
@@ -270,6 +296,8 @@ int32_t mpm_ctx_destroy(mpm_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (int k = 0; k < 2; ++k)
     if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
+  for (cudaEvent_t e : c->events)
+    if (e) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
   if (c->h_cnt) cudaFreeHost(c->h_cnt);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -515,6 +543,29 @@ int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
   }
   c->partition_valid = false;
   c->substeps += n_substeps;
+  return MPM_OK;
+}
+
+int32_t mpm_substep_timed(mpm_ctx *c, float dt, float *stage_ms, int32_t n_stages) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!stage_ms || n_stages < MPM_NUM_STAGES)
+    return fail(MPM_ERR_INVALID, "stage_ms needs MPM_NUM_STAGES entries");
+  if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
+  if (!c->events[0]) {
+    for (int i = 0; i <= MPM_NUM_STAGES; ++i) ZS_CUDA(cudaEventCreate(&c->events[i]));
+  }
+  enqueue_substep(c, c->cur, c->events);
+  if ((rc = launch_check("timed substep"))) return rc;
+  ZS_CUDA(cudaEventSynchronize(c->events[MPM_NUM_STAGES]));
+  for (int i = 0; i < MPM_NUM_STAGES; ++i) {
+    float ms = 0.0f;
+    ZS_CUDA(cudaEventElapsedTime(&ms, c->events[i], c->events[i + 1]));
+    stage_ms[i] = ms;
+  }
+  c->cur = 1 - c->cur;
+  c->partition_valid = false;
+  c->substeps += 1;
   return MPM_OK;
 }
 

@@ -269,7 +269,13 @@ __global__ void k_scatter(DevPtrs d) {
     int base = 0;
     if (key >= 0 && lane == leader) base = atomicAdd(&d.dir_fill[dd], __popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (key >= 0) d.perm[base + __popc(peers & lanemask_lt())] = (int)i;
+    if (key >= 0) {
+      const long long pos = (long long)base + __popc(peers & lanemask_lt());
+      if (pos < n)
+        d.perm[pos] = (int)i;
+      else  // stale directory counts after an earlier overflow
+        atomicOr(&d.cnt->status, ST_CAPACITY);
+    }
   }
 }
 
@@ -281,7 +287,8 @@ __global__ void __launch_bounds__(kSortThreads) k_bucket_sort(DevPtrs d) {
   extern __shared__ unsigned long long skeys[];
   const int nb = d.cnt->n_buckets;
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    const int start = d.bk_start[b], cnt = d.bk_count[b];
+    const int start = d.bk_start[b];
+    const int cnt = (int)min((long long)d.bk_count[b], d.prm->n - start);
     if (cnt <= 1) continue;
     if (cnt > kMaxSortBucket) {
       if (threadIdx.x == 0) atomicOr(&d.cnt->status, ST_BUCKET_OVERSIZE);

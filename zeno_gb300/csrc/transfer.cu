@@ -54,10 +54,11 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__r
     int K[3];
     bucket_origin(P, dir, K);
     __syncthreads();
-    const int start = d.bk_start[b], cnt = d.bk_count[b];
+    const int start = d.bk_start[b];
+    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     for (int s = start + threadIdx.x; s < start + cnt; s += kP2GThreads) {
       const int p = d.perm[s];
-      const int mid = iin[IC_MAT * cap + p];
+      const int mid = min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1);
       const MatParams mp = d.mats[mid];
       float x[3], v[3], C[9], F[9];
 #pragma unroll
@@ -105,21 +106,38 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__r
         continue;
       }
       const float mv0 = mass * v[0], mv1 = mass * v[1], mv2 = mass * v[2];
+      // Particles are sorted by cell, so ~8 neighbouring lanes share one
+      // stencil.  Each lane walks the 27 nodes in its own rotated order
+      // (axis offsets shifted by the base-3 digits of lane % 27), so lanes of
+      // one cell update different nodes at every step instead of serialising
+      // on the same shared-memory word.
+      const int rot = (threadIdx.x & 31) % 27;
+      int o0[3], o1[3], o2[3];
+      float w0[3], w1[3], w2[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        o0[q] = (q + rot % 3) % 3;
+        o1[q] = (q + (rot / 3) % 3) % 3;
+        o2[q] = (q + rot / 9) % 3;
+        w0[q] = o0[q] == 0 ? s0.w[0] : (o0[q] == 1 ? s0.w[1] : s0.w[2]);
+        w1[q] = o1[q] == 0 ? s1.w[0] : (o1[q] == 1 ? s1.w[1] : s1.w[2]);
+        w2[q] = o2[q] == 0 ? s2.w[0] : (o2[q] == 1 ? s2.w[1] : s2.w[2]);
+      }
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        const float xi = ((float)i - s0.f) * dx;
+        const float xi = ((float)o0[i] - s0.f) * dx;
         const float a0 = mv0 + A[0] * xi, a1 = mv1 + A[3] * xi, a2 = mv2 + A[6] * xi;
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const float xj = ((float)j - s1.f) * dx;
+          const float xj = ((float)o1[j] - s1.f) * dx;
           const float b0 = a0 + A[1] * xj, b1 = a1 + A[4] * xj, b2 = a2 + A[7] * xj;
-          const float wij = s0.w[i] * s1.w[j];
-          const int row = ((l0 + i) * 6 + (l1 + j)) * 6 + l2;
+          const float wij = w0[i] * w1[j];
+          const int row = ((l0 + o0[i]) * 6 + (l1 + o1[j])) * 6 + l2;
 #pragma unroll
           for (int kk = 0; kk < 3; ++kk) {
-            const float xk = ((float)kk - s2.f) * dx;
-            const float W = wij * s2.w[kk];
-            const int nd = row + kk;
+            const float xk = ((float)o2[kk] - s2.f) * dx;
+            const float W = wij * w2[kk];
+            const int nd = row + o2[kk];
             atomicAdd(&sm[0][nd], W * mass);
             atomicAdd(&sm[1][nd], W * (b0 + A[2] * xk));
             atomicAdd(&sm[2][nd], W * (b1 + A[5] * xk));
@@ -225,10 +243,11 @@ __global__ void __launch_bounds__(kG2PThreads)
       sv[2][nd] = g.w;
     }
     __syncthreads();
-    const int start = d.bk_start[b], cnt = d.bk_count[b];
+    const int start = d.bk_start[b];
+    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     for (int s = start + threadIdx.x; s < start + cnt; s += kG2PThreads) {
       const int p = d.perm[s];
-      const int mid = iin[IC_MAT * cap + p];
+      const int mid = min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1);
       const MatParams mp = d.mats[mid];
       float x[3];
 #pragma unroll
@@ -339,7 +358,7 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
   const bool lame = P.has_lame != 0;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
-    const MatParams mp = d.mats[ibuf[IC_MAT * cap + p]];
+    const MatParams mp = d.mats[min(max(ibuf[IC_MAT * cap + p], 0), kMaxMaterials - 1)];
     if (mp.type == MPM_EOS || mp.plastic != MPM_PLASTIC_NADP) continue;
     float F[9];
 #pragma unroll

@@ -55,8 +55,10 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
            "mpm_particles_upload", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
-           "mpm_substep", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
+           "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download"]
+
+STAGES = ["reset", "bin", "scan", "scatter", "sort", "clear", "p2g", "grid_update", "g2p"]
 
 _lib = None
 
@@ -91,6 +93,7 @@ def load(path: str = LIB_PATH):
         "mpm_g2p": ([P, f32], i32),
         "mpm_return_mapping": ([P], i32),
         "mpm_substep": ([P, f32, i32], i32),
+        "mpm_substep_timed": ([P, f32, P, i32], i32),
         "mpm_sync": ([P], i32),
         "mpm_get_stats": ([P, C.POINTER(Stats)], i32),
         "mpm_partition_download": ([P, P, P, P, i64, P, P, P, i64], i32),
@@ -251,6 +254,13 @@ class Context:
 
     def substep(self, dt, n: int = 1):
         self._check(self._L.mpm_substep(self.h, dt, int(n)), "mpm_substep")
+
+    def substep_timed(self, dt) -> dict:
+        """One substep with CUDA events between stages: device ms per stage."""
+        ms = np.zeros(len(STAGES), np.float32)
+        self._check(self._L.mpm_substep_timed(self.h, dt, _p(ms), len(STAGES)),
+                    "mpm_substep_timed")
+        return dict(zip(STAGES, ms.tolist()))
 
     def sync(self):
         self._check(self._L.mpm_sync(self.h), "mpm_sync")
