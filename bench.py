@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-substeps/s"
-KERNELS_PER_SUBSTEP = 10  # reset, bin, scan x2, scatter, sort, clear, p2g, grid update, g2p
+KERNELS_PER_SUBSTEP = 7  # scan x2, scatter, sort, p2g, grid gather + update, g2p
 WORKLOAD = ("plain MLS-MPM substep, four-material scene (FCR E=1e5, NHK E=5e4, "
             "Drucker-Prager sand 30deg, EOS fluid K=1e4 gamma=7), 2,097,152 FP32 particles, "
             "dx=1/256, dt=1e-4, slip walls")

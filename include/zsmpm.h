@@ -132,6 +132,9 @@ int32_t mpm_particles_upload(mpm_ctx *ctx, int64_t n, const float *x, const floa
                              const float *C, const float *F, const float *J,
                              const float *m, const float *vol, const int32_t *mat,
                              const float *mu, const float *lam);
+/* AdjustParticleMaterial (Temp.cu:16-56): per-particle Lame parameters
+ * (host arrays, upload order) that override the material's mu / lam. */
+int32_t mpm_particles_set_lame(mpm_ctx *ctx, const float *mu, const float *lam);
 /* UpdatePrimitiveFromZSParticles (Generation.cu:1088-1158): device store ->
  * host arrays in the upload order; NULL skips a channel. */
 int32_t mpm_particles_download(mpm_ctx *ctx, float *x, float *v, float *C, float *F, float *J);
@@ -156,16 +159,14 @@ int32_t mpm_substep(mpm_ctx *ctx, float dt, int32_t n_substeps);
  * around every node's apply() when ZENO_BENCHMARKING is on
  * (zeno/src/core/INode.cpp:141-143). */
 enum {
-  MPM_STAGE_RESET = 0,
-  MPM_STAGE_BIN = 1,
-  MPM_STAGE_SCAN = 2,
-  MPM_STAGE_SCATTER = 3,
-  MPM_STAGE_SORT = 4,
-  MPM_STAGE_CLEAR = 5,
-  MPM_STAGE_P2G = 6,
-  MPM_STAGE_GRID_UPDATE = 7,
-  MPM_STAGE_G2P = 8,
-  MPM_NUM_STAGES = 9
+  MPM_STAGE_BIN = 0,         /* binning of uploaded positions (0 when G2P binned them) */
+  MPM_STAGE_SCAN = 1,        /* directory scan: grid blocks, particle blocks */
+  MPM_STAGE_SCATTER = 2,     /* particles into their blocks */
+  MPM_STAGE_SORT = 3,        /* canonical (block, cell, index) order */
+  MPM_STAGE_P2G = 4,
+  MPM_STAGE_GRID_UPDATE = 5, /* tile gather + grid update + boundary */
+  MPM_STAGE_G2P = 6,         /* G2P + return mapping + stress + binning */
+  MPM_NUM_STAGES = 7
 };
 int32_t mpm_substep_timed(mpm_ctx *ctx, float dt, float *stage_ms, int32_t n_stages);
 

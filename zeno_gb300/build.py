@@ -3,6 +3,8 @@
 * ``zeno_gb300/libzsmpm.so``: the CUDA substep behind the C ABI of
   ``include/zsmpm.h``, compiled for sm_103a only, one object per .cu file,
   compiled in parallel.
+* ``zeno_gb300/libzsmpm_nodes.so``: the C++ MPM node wrappers (zeno node
+  API mirror in ``nodes/zeno_api.hpp``) over that ABI.
 """
 from __future__ import annotations
 
@@ -16,6 +18,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libzsmpm.so")
+NODES_LIB = os.path.join(PKG, "libzsmpm_nodes.so")
+NODES = os.path.join(PKG, "nodes")
+NODE_SOURCES = ["MPMNodes.cpp", "nodes_capi.cpp"]
 
 SOURCES = ["partition.cu", "transfer.cu", "io.cu", "api.cu"]
 HEADERS = ["zsmpm_internal.cuh", "mpm_math.cuh"]
@@ -65,6 +70,14 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     if jobs or _newer(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         run(cmd)
+    node_srcs = [os.path.join(NODES, f) for f in NODE_SOURCES]
+    node_deps = node_srcs + [os.path.join(NODES, "zeno_api.hpp"),
+                             os.path.join(ROOT, "include", "zsmpm.h"), LIB]
+    if _newer(NODES_LIB, node_deps):
+        cxx = os.environ.get("CXX", "g++")
+        run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-Wno-unused-variable",
+             "-I", os.path.join(ROOT, "include"), "-o", NODES_LIB] + node_srcs +
+            ["-L", PKG, "-lzsmpm", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -48,6 +48,7 @@ struct mpm_ctx {
   int cur = 0;
   bool partition_valid = false;
   bool needs_full_clear = false;
+  bool binned = false;  // directory counts describe the current positions
   int64_t substeps = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   Counters *h_cnt = nullptr;  // pinned
@@ -118,38 +119,42 @@ int32_t launch_check(const char *what) {
   return MPM_OK;
 }
 
-void enqueue_partition(mpm_ctx *c, int cur) {
-  launch_reset(c->d, c->stream);
-  launch_bin(c->d, cur, c->stream);
-  launch_scan(c->d, c->stream);
-  launch_scatter(c->d, c->stream);
-  launch_bucket_sort(c->d, c->stream);
+// Binning of the current positions into the directory counts (only when
+// they do not already describe them: after an upload or a stage G2P).
+void enqueue_bin_if_needed(mpm_ctx *c) {
+  if (!c->binned) {
+    launch_bin(c->d, c->cur, c->stream);
+    c->binned = true;
+  }
 }
 
-// One substep; with `ev` set, event i is recorded before stage i and event
-// MPM_NUM_STAGES after the last one.
+void enqueue_sort(mpm_ctx *c) {
+  launch_scan(c->d, c->stream);  // consumes (zeroes) the counts
+  launch_scatter(c->d, c->stream);
+  launch_bucket_sort(c->d, c->stream);
+  c->binned = false;
+}
+
+// One substep of the fused path; the counts of the current positions must be
+// binned already, and the G2P epilogue bins the new positions, so a graph of
+// this sequence can be replayed back to back.  With `ev` set, event i is
+// recorded before stage i and event MPM_NUM_STAGES after the last one.
 void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], c->stream);
   };
-  mark(MPM_STAGE_RESET);
-  launch_reset(c->d, c->stream);
-  mark(MPM_STAGE_BIN);
-  launch_bin(c->d, cur, c->stream);
   mark(MPM_STAGE_SCAN);
   launch_scan(c->d, c->stream);
   mark(MPM_STAGE_SCATTER);
   launch_scatter(c->d, c->stream);
   mark(MPM_STAGE_SORT);
   launch_bucket_sort(c->d, c->stream);
-  mark(MPM_STAGE_CLEAR);
-  launch_grid_clear(c->d, c->stream);
   mark(MPM_STAGE_P2G);
   launch_p2g(c->d, cur, c->stream);
   mark(MPM_STAGE_GRID_UPDATE);
-  launch_grid_update(c->d, 3, c->stream);
+  launch_grid_gather(c->d, 3, c->stream);
   mark(MPM_STAGE_G2P);
-  launch_g2p(c->d, cur, 1, c->stream);
+  launch_g2p(c->d, cur, 1, 1, c->stream);
   mark(MPM_NUM_STAGES);
 }
 
@@ -176,6 +181,7 @@ int32_t prepare_partition(mpm_ctx *c) {
   if (c->needs_full_clear) {
     launch_full_dir_clear(c->d, c->stream);
     c->needs_full_clear = false;
+    c->binned = false;
   }
   return MPM_OK;
 }
@@ -234,13 +240,16 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
   d.cap_gblocks = (int)capg;
   d.num_sms = sms;
   d.ntiles = (int)((ndir + kScanTile - 1) / kScanTile);
+  configure_launches(d);
   for (int k = 0; k < 2; ++k) {
     if ((rc = dalloc(c, &d.pbuf[k], (size_t)NCH * cap))) return bail(rc);
     if ((rc = dalloc(c, &d.ibuf[k], (size_t)NICH * cap))) return bail(rc);
   }
   if ((rc = dalloc(c, &d.pkey, cap)) || (rc = dalloc(c, &d.perm, cap)) ||
+      (rc = dalloc(c, &d.perm_tmp, cap)) ||
       (rc = dalloc(c, &d.dir_count, ndir)) || (rc = dalloc(c, &d.dir_fill, ndir)) ||
       (rc = dalloc(c, &d.dir_gb, ndir)) || (rc = dalloc(c, &d.dir_flag, ndir)) ||
+      (rc = dalloc(c, &d.dir_bk, ndir)) || (rc = dalloc(c, &d.ptile, (size_t)capg * kTileNodes)) ||
       (rc = dalloc(c, &d.gb_dir, capg)) || (rc = dalloc(c, &d.bk_dir, capg)) ||
       (rc = dalloc(c, &d.bk_start, capg)) || (rc = dalloc(c, &d.bk_count, capg)) ||
       (rc = dalloc(c, &d.grid, (size_t)capg * 64)) ||
@@ -259,6 +268,7 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
   cudaMemsetAsync(d.dir_count, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_fill, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_gb, 0xff, ndir * sizeof(int32_t), c->stream);
+  cudaMemsetAsync(d.dir_bk, 0xff, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_flag, 0, ndir, c->stream);
   cudaMemsetAsync(d.cnt, 0, sizeof(Counters), c->stream);
   cudaMemsetAsync(d.mats, 0, kMaxMaterials * sizeof(MatParams), c->stream);
@@ -344,7 +354,12 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   c->prm.n_materials = n;
   c->prm_dirty = true;
-  return push_params(c);
+  if ((rc = push_params(c))) return rc;
+  if (c->prm.n > 0) {  // stored stresses follow the new parameters
+    launch_stress(c->d, c->cur, c->stream);
+    if ((rc = launch_check("stress"))) return rc;
+  }
+  return MPM_OK;
 }
 
 int32_t mpm_set_boundary(mpm_ctx *c, const mpm_boundary *bc) {
@@ -419,11 +434,34 @@ int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float 
   c->prm.has_lame = mu ? 1 : 0;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
+  launch_stress(c->d, c->cur, c->stream);  // S = vol * tau read by P2G
+  if ((rc = launch_check("stress"))) return rc;
   // a fresh store: clear the status word and the whole directory
   ZS_CUDA(cudaMemsetAsync(&c->d.cnt->status, 0, sizeof(int), c->stream));
   c->needs_full_clear = true;
   c->partition_valid = false;
+  c->binned = false;
   c->substeps = 0;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_particles_set_lame(mpm_ctx *c, const float *mu, const float *lam) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!mu || !lam) return fail(MPM_ERR_INVALID, "mu and lam are required");
+  const long long n = c->prm.n;
+  if (n == 0) return MPM_OK;
+  float *st = c->d.pbuf[1 - c->cur];  // staging: the other buffer is free between substeps
+  ZS_CUDA(cudaMemcpyAsync(st, mu, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(st + n, lam, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  launch_set_lame(c->d, c->cur, st, st + n, n, c->stream);
+  if ((rc = launch_check("set lame"))) return rc;
+  c->prm.has_lame = 1;
+  c->prm_dirty = true;
+  if ((rc = push_params(c))) return rc;
+  launch_stress(c->d, c->cur, c->stream);  // stored stresses follow the new parameters
+  if ((rc = launch_check("stress"))) return rc;
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   return MPM_OK;
 }
@@ -453,7 +491,8 @@ int32_t mpm_partition(mpm_ctx *c) {
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = push_params(c)) || (rc = prepare_partition(c))) return rc;
-  enqueue_partition(c, c->cur);
+  enqueue_bin_if_needed(c);
+  enqueue_sort(c);
   if ((rc = launch_check("partition"))) return rc;
   c->partition_valid = true;
   return MPM_OK;
@@ -473,6 +512,7 @@ int32_t mpm_p2g(mpm_ctx *c, float dt) {
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "p2g needs a partition of the current positions");
   if ((rc = set_dt(c, dt))) return rc;
   launch_p2g(c->d, c->cur, c->stream);
+  launch_grid_gather(c->d, 0, c->stream);  // grid = m, mv as after the reference P2G
   return launch_check("p2g");
 }
 
@@ -509,10 +549,11 @@ int32_t mpm_g2p(mpm_ctx *c, float dt) {
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "g2p needs the partition used by p2g");
   if ((rc = set_dt(c, dt))) return rc;
-  launch_g2p(c->d, c->cur, 0, c->stream);
+  launch_g2p(c->d, c->cur, 0, 0, c->stream);
   if ((rc = launch_check("g2p"))) return rc;
   c->cur = 1 - c->cur;
   c->partition_valid = false;
+  c->binned = false;
   c->substeps += 1;
   return MPM_OK;
 }
@@ -530,6 +571,7 @@ int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
   if (rc) return rc;
   if (n_substeps < 0) return fail(MPM_ERR_INVALID, "negative substep count");
   if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
+  if (n_substeps > 0) enqueue_bin_if_needed(c);
   const bool graphs = graphs_enabled();
   for (int32_t k = 0; k < n_substeps; ++k) {
     if (graphs) {
@@ -555,6 +597,8 @@ int32_t mpm_substep_timed(mpm_ctx *c, float dt, float *stage_ms, int32_t n_stage
   if (!c->events[0]) {
     for (int i = 0; i <= MPM_NUM_STAGES; ++i) ZS_CUDA(cudaEventCreate(&c->events[i]));
   }
+  ZS_CUDA(cudaEventRecord(c->events[MPM_STAGE_BIN], c->stream));
+  enqueue_bin_if_needed(c);
   enqueue_substep(c, c->cur, c->events);
   if ((rc = launch_check("timed substep"))) return rc;
   ZS_CUDA(cudaEventSynchronize(c->events[MPM_NUM_STAGES]));

@@ -58,7 +58,26 @@ __global__ void k_egest(const float *__restrict__ pb, const int32_t *__restrict_
   }
 }
 
+// per-particle Lame overrides given in upload order -> storage order
+__global__ void k_set_lame(float *__restrict__ pb, const int32_t *__restrict__ ib, long long cap,
+                           const float *__restrict__ mu, const float *__restrict__ lam,
+                           long long n) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+    const long long u = ib[IC_ID * cap + s];
+    if (u < 0 || u >= n) continue;
+    pb[CH_MU * cap + s] = mu[u];
+    pb[CH_LAM * cap + s] = lam[u];
+  }
+}
+
 }  // namespace
+
+void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
+                     cudaStream_t s) {
+  if (n <= 0) return;
+  k_set_lame<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], d.cap, mu, lam, n);
+}
 
 void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s) {
   if (n <= 0) return;

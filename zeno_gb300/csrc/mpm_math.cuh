@@ -26,8 +26,19 @@ struct Sym3 {
 __device__ __forceinline__ void jacobi_rot(float &app, float &aqq, float &apq, float &arp,
                                            float &arq, float (&Q)[9], int p, int q) {
   if (fabsf(apq) <= 1e-30f) return;
-  const float theta = 0.5f * (aqq - app) / apq;
-  const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.0f)));
+  // The rotation only has to be orthogonal: c and s come from one rsqrt, so
+  // c^2 + s^2 = 1 to rounding even though t is computed with approximate
+  // division; the residual of a_pq is removed by the next sweep.
+  const float theta = __fdividef(0.5f * (aqq - app), apq);
+  const float at = fabsf(theta);
+  float t;
+  if (at < 1e15f) {
+    const float h = fmaf(theta, theta, 1.0f);
+    t = __fdividef(1.0f, at + h * rsqrtf(h));
+  } else {
+    t = __fdividef(0.5f, at);
+  }
+  t = copysignf(t, theta);
   const float c = rsqrtf(fmaf(t, t, 1.0f));
   const float s = t * c;
   app = fmaf(-t, apq, app);
@@ -50,7 +61,7 @@ __device__ __forceinline__ void sym_eig3(Sym3 a, float (&w)[3], float (&Q)[9]) {
   for (int i = 0; i < 9; ++i) Q[i] = (i % 4 == 0) ? 1.0f : 0.0f;
   float d0 = a.xx, d1 = a.yy, d2 = a.zz, o01 = a.xy, o02 = a.xz, o12 = a.yz;
 #pragma unroll 1
-  for (int sweep = 0; sweep < 6; ++sweep) {
+  for (int sweep = 0; sweep < 5; ++sweep) {
     const float off = o01 * o01 + o02 * o02 + o12 * o12;
     const float dia = d0 * d0 + d1 * d1 + d2 * d2;
     if (off <= 1e-14f * dia || off == 0.0f) break;
@@ -150,32 +161,50 @@ __device__ __forceinline__ bool kirchhoff(int type, float mu, float lam, float b
 // Non-associative Drucker-Prager return mapping in Hencky strain space
 // (Klar et al. 2016, sec. 7.3), the ZSReturnMapping node
 // (MPMPipeline.cu:958-971): with F = U S V^T and B = U S^2 U^T the projected
-// F is U S' V^T = F + U diag(S'/S - 1) U^T F.  Returns -1 on a degenerate F,
+// F is U S' V^T = F + U diag(S'/S - 1) U^T F.  The same decomposition gives
+// the StVK-Hencky Kirchhoff stress of the (projected) state,
+// tau = U diag(2mu e'_i + lam sum e') U^T.  Returns -1 on a degenerate F,
 // 1 if projected, 0 if inside the yield surface.
-__device__ __forceinline__ int project_dp(float mu, float lam, float alpha, float (&F)[9]) {
+__device__ __forceinline__ int project_dp(float mu, float lam, float alpha, float (&F)[9],
+                                          Sym3 &tau) {
   Sym3 E;
   float Jm1;
   strain_of(F, E, Jm1);
   float w[3], Q[9];
   sym_eig3(E, w, Q);
-  if (!(w[0] > -1.0f && w[1] > -1.0f && w[2] > -1.0f)) return -1;
-  const float e0 = 0.5f * log1pf(w[0]), e1 = 0.5f * log1pf(w[1]), e2 = 0.5f * log1pf(w[2]);
+  if (!(w[0] > -1.0f && w[1] > -1.0f && w[2] > -1.0f)) {
+    tau = Sym3{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    return -1;
+  }
+  float e0 = 0.5f * log1pf(w[0]), e1 = 0.5f * log1pf(w[1]), e2 = 0.5f * log1pf(w[2]);
   const float tr = e0 + e1 + e2;
-  float r0, r1, r2;  // S'/S - 1
+  int projected = 1;
+  float r0 = 0.f, r1 = 0.f, r2 = 0.f;  // S'/S - 1
   if (tr >= 0.0f) {
     r0 = expm1f(-e0);
     r1 = expm1f(-e1);
     r2 = expm1f(-e2);
+    e0 = e1 = e2 = 0.0f;
   } else {
     const float h0 = e0 - tr / 3.0f, h1 = e1 - tr / 3.0f, h2 = e2 - tr / 3.0f;
     const float nrm = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
     const float dg = nrm + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * alpha;
-    if (dg <= 0.0f) return 0;
-    const float k = dg / nrm;
-    r0 = expm1f(-k * h0);
-    r1 = expm1f(-k * h1);
-    r2 = expm1f(-k * h2);
+    if (dg <= 0.0f) {
+      projected = 0;
+    } else {
+      const float k = dg / nrm;
+      r0 = expm1f(-k * h0);
+      r1 = expm1f(-k * h1);
+      r2 = expm1f(-k * h2);
+      e0 -= k * h0;
+      e1 -= k * h1;
+      e2 -= k * h2;
+    }
   }
+  const float trp = e0 + e1 + e2;
+  tau = qdqt(Q, 2.0f * mu * e0 + lam * trp, 2.0f * mu * e1 + lam * trp,
+             2.0f * mu * e2 + lam * trp);
+  if (!projected) return 0;
   const Sym3 M = qdqt(Q, r0, r1, r2);
   float Fn[9];
 #pragma unroll

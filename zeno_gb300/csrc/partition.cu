@@ -6,19 +6,23 @@
 // CAS and expands the table on the host in several synchronised passes.
 // Here a dense block directory stands in for the hash table (O(1) lookup,
 // no probing, 1-8 MB for the domains in use), and one substep's partition is
-// six device kernels with no host read:
-//   reset   clear the directory entries the previous partition touched
+// four device kernels with no host read:
 //   bin     per particle: key = (block << 6) | cell, warp-aggregated count;
 //           the first particle of a block marks its 27-block neighbourhood
-//           (the 1-ring halo of ExpandZSPartition)
-//   scan    two-pass scan over the directory: grid block index of each
-//           marked block, start of each non-empty particle block
+//           (the 1-ring halo).  In the fused substep G2P does this for the
+//           positions it writes, so the kernel only runs after an upload.
+//   scan    two passes over the directory: grid block index of each marked
+//           block, start of each non-empty particle block; the second pass
+//           rewrites every directory entry it reads (grid block / particle
+//           block index or -1) and zeroes the counts for the next binning,
+//           so no separate reset is needed
 //   scatter warp-aggregated placement of particle indices into their block
-//   sort    per block, bitonic sort on chip by (cell, index): the canonical
-//           (block, cell, index) order, independent of atomic timing
-//   clear   zero the grid blocks (ZSGridFromZSPartition, :256-262)
+//   sort    per block, counting sort by cell plus a per-cell insertion sort:
+//           the canonical (block, cell, index) order, independent of atomic
+//           timing
 #include <cuda_runtime.h>
 
+#include "binning.cuh"
 #include "zsmpm_internal.cuh"
 
 namespace zsmpm {
@@ -30,23 +34,13 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
-__global__ void k_reset(DevPtrs d) {
-  const int n = min(d.cnt->n_gblocks, d.cap_gblocks);
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
-    const int dd = d.gb_dir[g];
-    d.dir_count[dd] = 0;
-    d.dir_fill[dd] = 0;
-    d.dir_gb[dd] = -1;
-    d.dir_flag[dd] = 0;
-  }
-}
-
 __global__ void k_full_dir_clear(DevPtrs d) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.ndir;
        i += (long long)gridDim.x * blockDim.x) {
     d.dir_count[i] = 0;
     d.dir_fill[i] = 0;
     d.dir_gb[i] = -1;
+    d.dir_bk[i] = -1;
     d.dir_flag[i] = 0;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -55,75 +49,38 @@ __global__ void k_full_dir_clear(DevPtrs d) {
   }
 }
 
-// Block of a particle: base = floor(x / dx - 0.5) per axis
-// (MPMPipeline.cu:78-82), computed as one rounded multiply by 1/dx and one
-// rounded subtraction so that no FMA contraction changes a key.
-__device__ __forceinline__ int particle_base(float x, float inv_dx) {
-  return __float2int_rd(__fsub_rn(__fmul_rn(x, inv_dx), 0.5f));
-}
-
 __global__ void k_bin(DevPtrs d, const float *__restrict__ pin) {
   const SimParams &P = *d.prm;
   const long long n = P.n;
   const long long cap = d.cap;
-  if (blockIdx.x == 0 && threadIdx.x == 0) d.cnt->max_vel_sqr_bits = 0u;
   const int lane = threadIdx.x & 31;
   const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const int dy = P.block_dims[1], dz = P.block_dims[2];
   for (long long w = warp0; w < n; w += stride) {
     const long long i = w + lane;
     int key = -1;
     if (i < n) {
-      const float x0 = pin[CH_X * cap + i], x1 = pin[(CH_X + 1) * cap + i],
-                  x2 = pin[(CH_X + 2) * cap + i];
-      if (isfinite(x0) && isfinite(x1) && isfinite(x2)) {
-        const int b0 = particle_base(x0, P.inv_dx), b1 = particle_base(x1, P.inv_dx),
-                  b2 = particle_base(x2, P.inv_dx);
-        const int c0 = (b0 >> 2) - P.block_lo[0], c1 = (b1 >> 2) - P.block_lo[1],
-                  c2 = (b2 >> 2) - P.block_lo[2];
-        if (c0 >= 1 && c0 <= P.block_dims[0] - 2 && c1 >= 1 && c1 <= dy - 2 && c2 >= 1 &&
-            c2 <= dz - 2) {
-          const int dd = (c0 * dy + c1) * dz + c2;
-          key = (dd << 6) | ((b0 & 3) << 4) | ((b1 & 3) << 2) | (b2 & 3);
-        } else {
-          atomicOr(&d.cnt->status, ST_OUT_OF_DOMAIN);
-        }
-      } else {
-        atomicOr(&d.cnt->status, ST_NAN);
-      }
+      key = bin_key(P, pin[CH_X * cap + i], pin[(CH_X + 1) * cap + i], pin[(CH_X + 2) * cap + i],
+                    &d.cnt->status);
       d.pkey[i] = key;
     }
-    const int dd = key >> 6;  // -1 for invalid
-    const unsigned peers = __match_any_sync(0xffffffffu, dd);
-    const int leader = __ffs(peers) - 1;
-    if (key >= 0 && lane == leader) {
-      const int old = atomicAdd(&d.dir_count[dd], __popc(peers));
-      if (old == 0) {
-        // first particle of the block: mark the block and its 26 neighbours
-        for (int a = -1; a <= 1; ++a)
-          for (int b = -1; b <= 1; ++b)
-            for (int c = -1; c <= 1; ++c) d.dir_flag[dd + (a * dy + b) * dz + c] = 1;
-      }
-    }
+    bin_count(d, P, key, 0xffffffffu);
   }
 }
 
 // Pass 1 of the directory scan: per tile sums of (grid block flag, particle
 // count, non-empty flag).
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevPtrs d) {
-  const long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * 16;
+  const long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
   int f = 0, c = 0, e = 0;
-  if (base < d.ndir) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const long long i = base + k;
-      if (i < d.ndir) {
-        const int cc = d.dir_count[i];
-        f += d.dir_flag[i];
-        c += cc;
-        e += cc > 0;
-      }
+  for (int k = 0; k < kScanPerThread; ++k) {
+    const long long i = base + k;
+    if (i < d.ndir) {
+      const int cc = d.dir_count[i];
+      f += d.dir_flag[i];
+      c += cc;
+      e += cc > 0;
     }
   }
   __shared__ int red[3][kScanThreads / 32];
@@ -148,11 +105,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevPtrs d) {
 }
 
 // Pass 2: exclusive prefix of the tile sums, local scan, and the outputs.
+// Every entry of the tile is rewritten: grid block index or -1, particle
+// block index or -1, count and flag back to 0 for the next binning.
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
   __shared__ int red[3][kScanThreads / 32];
   __shared__ int tile_prefix[3];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // prefix over previous tiles
+  if (blockIdx.x == 0 && tid == 0) d.cnt->max_vel_sqr_bits = 0u;
   int pf = 0, pc = 0, pe = 0;
   for (int t = tid; t < (int)blockIdx.x; t += kScanThreads) {
     pf += d.tile_sums[3 * t];
@@ -178,12 +137,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
   }
   __syncthreads();
 
-  // thread-local values
-  const long long base = (long long)blockIdx.x * kScanTile + tid * 16;
-  int fl[16], ct[16];
+  const long long base = (long long)blockIdx.x * kScanTile + tid * kScanPerThread;
+  int fl[kScanPerThread], ct[kScanPerThread];
   int f = 0, c = 0, e = 0;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
+  for (int k = 0; k < kScanPerThread; ++k) {
     const long long i = base + k;
     fl[k] = 0;
     ct[k] = 0;
@@ -195,7 +153,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
     c += ct[k];
     e += ct[k] > 0;
   }
-  // block exclusive scan of (f, c, e)
   int sf = f, sc = c, se = e;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -225,12 +182,14 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
   int bpos = tile_prefix[2] + we + se - e;
   const int cap = d.cap_gblocks;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
+  for (int k = 0; k < kScanPerThread; ++k) {
     const long long i = base + k;
+    if (i >= d.ndir) break;
+    int gb = -1, bk = -1;
     if (fl[k]) {
       if (gpos < cap) {
         d.gb_dir[gpos] = (int)i;
-        d.dir_gb[i] = gpos;
+        gb = gpos;
       } else {
         atomicOr(&d.cnt->status, ST_CAPACITY);
       }
@@ -241,11 +200,16 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
         d.bk_dir[bpos] = (int)i;
         d.bk_start[bpos] = ppos;
         d.bk_count[bpos] = ct[k];
+        bk = bpos;
       }
       d.dir_fill[i] = ppos;
       ++bpos;
       ppos += ct[k];
     }
+    d.dir_gb[i] = gb;
+    d.dir_bk[i] = bk;
+    if (fl[k]) d.dir_flag[i] = 0;
+    if (ct[k]) d.dir_count[i] = 0;
   }
   if (blockIdx.x == gridDim.x - 1 && tid == kScanThreads - 1) {
     d.cnt->n_gblocks = min(gpos, cap);
@@ -279,50 +243,151 @@ __global__ void k_scatter(DevPtrs d) {
   }
 }
 
-// Canonical order inside each particle block: bitonic sort of
-// (cell << 32 | storage index) in shared memory.
-constexpr int kSortThreads = 512;
+// Canonical order inside each particle block: (cell, storage index).
+// A counting sort by cell id (64 bins, integer shared-memory atomics) followed
+// by an insertion sort of each cell's few particles by storage index.  A cell
+// with more than kCellSortMax particles sends the block to an on-chip bitonic
+// sort; a block with more than kSortCap particles is sorted the same way
+// through global scratch (slower; flagged with the informational
+// ST_BUCKET_OVERSIZE bit).
+constexpr int kSortThreads = 256;
+constexpr int kSortCap = 2048;
+constexpr int kCellSortMax = 64;
+
+__device__ __forceinline__ void warp_exclusive_scan64(const int *in, int *out) {
+  // one warp: 64 values, two per lane
+  const int lane = threadIdx.x & 31;
+  const int a = in[2 * lane], b = in[2 * lane + 1];
+  int s = a + b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, s, o);
+    if (lane >= o) s += t;
+  }
+  const int excl = s - a - b;
+  out[2 * lane] = excl;
+  out[2 * lane + 1] = excl + a;
+  if (lane == 31) out[64] = s;
+}
 
 __global__ void __launch_bounds__(kSortThreads) k_bucket_sort(DevPtrs d) {
-  extern __shared__ unsigned long long skeys[];
+  __shared__ __align__(16) int sbuf[2 * kSortCap];
+  int *sp = sbuf, *op = sbuf + kSortCap;
+  __shared__ unsigned char sc[kSortCap];
+  __shared__ int ccount[64], cstart[65], cfill[64];
+  __shared__ int big_cell;
   const int nb = d.cnt->n_buckets;
+  const long long n = d.prm->n;
+  const int tid = threadIdx.x;
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const int start = d.bk_start[b];
-    const int cnt = (int)min((long long)d.bk_count[b], d.prm->n - start);
+    const int cnt = (int)min((long long)d.bk_count[b], n - start);
     if (cnt <= 1) continue;
-    if (cnt > kMaxSortBucket) {
-      if (threadIdx.x == 0) atomicOr(&d.cnt->status, ST_BUCKET_OVERSIZE);
-      continue;
+    if (tid < 64) {
+      ccount[tid] = 0;
+      cfill[tid] = 0;
     }
-    int N = 2;
-    while (N < cnt) N <<= 1;
-    for (int j = threadIdx.x; j < N; j += kSortThreads) {
-      unsigned long long k = ~0ull;
-      if (j < cnt) {
-        const int p = d.perm[start + j];
-        k = ((unsigned long long)(d.pkey[p] & 63) << 32) | (unsigned)p;
-      }
-      skeys[j] = k;
-    }
+    if (tid == 0) big_cell = 0;
     __syncthreads();
-    for (int k = 2; k <= N; k <<= 1) {
-      for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int i = threadIdx.x; i < N; i += kSortThreads) {
-          const int ixj = i ^ j;
-          if (ixj > i) {
-            const unsigned long long a = skeys[i], c = skeys[ixj];
-            const bool up = (i & k) == 0;
-            if ((a > c) == up) {
-              skeys[i] = c;
-              skeys[ixj] = a;
+    if (cnt <= kSortCap) {
+      for (int j = tid; j < cnt; j += kSortThreads) {
+        const int p = d.perm[start + j];
+        const int c = d.pkey[p] & 63;
+        sp[j] = p;
+        sc[j] = (unsigned char)c;
+        atomicAdd(&ccount[c], 1);
+      }
+      __syncthreads();
+      if (tid < 32) warp_exclusive_scan64(ccount, cstart);
+      __syncthreads();
+      for (int j = tid; j < cnt; j += kSortThreads) {
+        const int c = sc[j];
+        op[cstart[c] + atomicAdd(&cfill[c], 1)] = sp[j];
+      }
+      __syncthreads();
+      if (tid < 64) {
+        const int lo = cstart[tid], hi = cstart[tid + 1];
+        if (hi - lo > kCellSortMax) {
+          big_cell = 1;
+        } else {
+          for (int i = lo + 1; i < hi; ++i) {
+            const int v = op[i];
+            int k = i - 1;
+            while (k >= lo && op[k] > v) {
+              op[k + 1] = op[k];
+              --k;
             }
+            op[k + 1] = v;
           }
         }
-        __syncthreads();
       }
+      __syncthreads();
+      if (big_cell) {
+        // bitonic sort of (cell << 32 | index) over the whole block
+        unsigned long long *key = reinterpret_cast<unsigned long long *>(sbuf);  // 16 KB
+        int N = 2;
+        while (N < cnt) N <<= 1;
+        __syncthreads();
+        for (int j = tid; j < N; j += kSortThreads) {
+          unsigned long long k = ~0ull;
+          if (j < cnt) {
+            const int p = d.perm[start + j];
+            k = ((unsigned long long)(d.pkey[p] & 63) << 32) | (unsigned)p;
+          }
+          key[j] = k;
+        }
+        __syncthreads();
+        for (int k = 2; k <= N; k <<= 1) {
+          for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < N; i += kSortThreads) {
+              const int ixj = i ^ j;
+              if (ixj > i) {
+                const unsigned long long a = key[i], c = key[ixj];
+                if ((a > c) == ((i & k) == 0)) {
+                  key[i] = c;
+                  key[ixj] = a;
+                }
+              }
+            }
+            __syncthreads();
+          }
+        }
+        for (int j = tid; j < cnt; j += kSortThreads)
+          d.perm[start + j] = (int)(key[j] & 0xffffffffull);
+      } else {
+        for (int j = tid; j < cnt; j += kSortThreads) d.perm[start + j] = op[j];
+      }
+    } else {
+      // oversize block: counting sort by cell through global scratch
+      for (int j = tid; j < cnt; j += kSortThreads)
+        atomicAdd(&ccount[d.pkey[d.perm[start + j]] & 63], 1);
+      __syncthreads();
+      if (tid < 32) warp_exclusive_scan64(ccount, cstart);
+      __syncthreads();
+      for (int j = tid; j < cnt; j += kSortThreads) {
+        const int p = d.perm[start + j];
+        const int c = d.pkey[p] & 63;
+        d.perm_tmp[start + cstart[c] + atomicAdd(&cfill[c], 1)] = p;
+      }
+      __syncthreads();
+      // canonical order inside each cell (insertion sort in global scratch)
+      if (tid < 64) {
+        int *q = d.perm_tmp + start;
+        const int lo = cstart[tid], hi = cstart[tid + 1];
+        for (int i = lo + 1; i < hi; ++i) {
+          const int v = q[i];
+          int k = i - 1;
+          while (k >= lo && q[k] > v) {
+            q[k + 1] = q[k];
+            --k;
+          }
+          q[k + 1] = v;
+        }
+      }
+      __syncthreads();
+      for (int j = tid; j < cnt; j += kSortThreads) d.perm[start + j] = d.perm_tmp[start + j];
+      if (tid == 0) atomicOr(&d.cnt->status, ST_BUCKET_OVERSIZE);
     }
-    for (int j = threadIdx.x; j < cnt; j += kSortThreads)
-      d.perm[start + j] = (int)(skeys[j] & 0xffffffffull);
     __syncthreads();
   }
 }
@@ -338,10 +403,6 @@ __global__ void k_grid_clear(DevPtrs d) {
 inline int grid_for(const DevPtrs &d, int per_sm) { return d.num_sms * per_sm; }
 
 }  // namespace
-
-void launch_reset(const DevPtrs &d, cudaStream_t s) {
-  k_reset<<<grid_for(d, 4), 256, 0, s>>>(d);
-}
 
 void launch_full_dir_clear(const DevPtrs &d, cudaStream_t s) {
   k_full_dir_clear<<<grid_for(d, 8), 256, 0, s>>>(d);
@@ -361,8 +422,7 @@ void launch_scatter(const DevPtrs &d, cudaStream_t s) {
 }
 
 void launch_bucket_sort(const DevPtrs &d, cudaStream_t s) {
-  k_bucket_sort<<<grid_for(d, 4), kSortThreads, kMaxSortBucket * sizeof(unsigned long long), s>>>(
-      d);
+  k_bucket_sort<<<grid_for(d, 8), kSortThreads, 0, s>>>(d);
 }
 
 void launch_grid_clear(const DevPtrs &d, cudaStream_t s) {

@@ -1,25 +1,32 @@
 // Particle-to-grid, grid update + boundary, grid-to-particle.
 //
-// One CTA owns one particle block at a time (particles sorted by block, see
-// partition.cu).  A block's quadratic stencils all fall in the 6^3 nodes
-// [K, K+6) of its block key K, which lie in the 2x2x2 grid blocks K + {0,4}^3:
-//  * P2G (Transfer.cu:849-889) accumulates the 27-node APIC scatter of the
-//    block's particles into those 216 nodes in shared memory and flushes
-//    each node once with a vector float4 atomic, instead of the reference's
-//    27 x 4 global float atomics per particle.
+// One CTA owns one particle block at a time (particles sorted by block and
+// cell, see partition.cu).  A block's quadratic stencils all fall in the 6^3
+// nodes [K, K+6) of its block key K, which lie in the 2x2x2 grid blocks
+// K + {0,4}^3:
+//  * P2G (Transfer.cu:849-889) sums the block's particle contributions per
+//    node in shared memory (one warp per cell, one lane per stencil node) and
+//    stores the 216 node sums of the block as a tile; the grid gather then
+//    adds, per grid node, the <= 8 tiles that cover it in a fixed order and
+//    applies the grid update and boundary.  The reference's 27 x 4 global
+//    float atomics per particle become plain stores, the grid needs no clear,
+//    and the grid sums do not depend on scheduling.
 //  * G2P (Transfer.cu:1139-1173) stages the 216 node velocities in shared
 //    memory and gathers from there; it writes the particle's new state into
 //    the other particle buffer at its sorted position, so storage follows
-//    the block order from one substep to the next.
+//    the block order from one substep to the next.  It ends with the return
+//    mapping (ZSReturnMapping) and the Kirchhoff stress of the new F, stored
+//    as S = vol * tau for the next P2G, so that the Drucker-Prager projection
+//    and the StVK-Hencky stress share one eigen-decomposition.
 #include <cuda_runtime.h>
 
+#include "binning.cuh"
 #include "mpm_math.cuh"
 #include "zsmpm_internal.cuh"
 
 namespace zsmpm {
 namespace {
 
-constexpr int kP2GThreads = 128;
 constexpr int kG2PThreads = 128;
 constexpr int kNodes = 216;  // 6^3
 
@@ -38,173 +45,248 @@ __device__ __forceinline__ int neighbour_gb(const DevPtrs &d, const SimParams &P
   return d.dir_gb[dir + ((t >> 2) * dy + ((t >> 1) & 1)) * dz + (t & 1)];
 }
 
+// P2G of one particle block (ZSParticleToZSGrid::p2g_apic, Transfer.cu:849-889).
+//  phase 1: per particle, the affine matrix A = m C - dt Dinv S (S = vol tau
+//           from the previous G2P); the momentum of stencil offset o
+//           (node - x = (o - f) dx) is W (m v + A (o - f) dx) = W (b + A o dx)
+//           with b = m v - dx A f, so phase 1 stores (m, b, A, f) per particle.
+//  phase 2: warp w takes cells w, w + 8, ..., w + 56 (three at a time, one
+//           per 9-lane slot); the particles of a cell are a contiguous range
+//           (sorted by cell).  Lane (slot, i, j) owns the three stencil nodes
+//           (i, j, 0..2) of its slot's cell: one weight product w_i w_j serves
+//           three nodes.  Sums go to the warp's private node array, slot by
+//           slot, so no two lanes ever update one word at the same time.
+//  reduce:  the 8 warp arrays are added per node in warp order and stored as
+//           the block's tile.  No atomics: the tile is reproducible bit for bit.
+constexpr int kP2GThreads = 256;
+constexpr int kP2GWarps = kP2GThreads / 32;
+constexpr int kP2GChunk = 384;
+constexpr int kP2GSpdBytes = 4 * kP2GChunk * 16;
+constexpr int kP2GAccBytes = kP2GWarps * 4 * kNodes * 4;
+constexpr int kP2GSmem = kP2GSpdBytes + kP2GAccBytes + 65 * 4 + kP2GChunk;
+
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__restrict__ pin,
                                                      const int32_t *__restrict__ iin) {
-  __shared__ float sm[4][kNodes];
-  __shared__ int sgb[8];
+  // dynamic shared memory (kP2GSmem bytes):
+  //   spd   4 x kP2GChunk float4: (m,b0,b1,b2) (A00,A01,A02,A10) (A11,A12,A20,A21) (A22,f0,f1,f2)
+  //   acc   kP2GWarps x 4 x 216 floats: per-warp node sums (m, mv)
+  //   cst   65 ints: cell ranges of the chunk
+  //   scell kP2GChunk bytes: cell of each chunk particle
+  extern __shared__ __align__(16) unsigned char p2g_smem[];
+  float4(*spd)[kP2GChunk] = reinterpret_cast<float4(*)[kP2GChunk]>(p2g_smem);
+  float(*acc)[4][kNodes] = reinterpret_cast<float(*)[4][kNodes]>(p2g_smem + kP2GSpdBytes);
+  int *cst = reinterpret_cast<int *>(p2g_smem + kP2GSpdBytes + kP2GAccBytes);
+  unsigned char *scell = p2g_smem + kP2GSpdBytes + kP2GAccBytes + 65 * sizeof(int);
   const SimParams &P = *d.prm;
   const long long cap = d.cap;
   const float dt = P.dt, dx = P.dx, inv_dx = P.inv_dx, Dinv = P.Dinv;
   const int nb = d.cnt->n_buckets;
-  const bool lame = P.has_lame != 0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // lane constants of phase 2: slot, stencil column (i, j), weight polynomials
+  // w_0(f) = (1.5-f)^2/2, w_1(f) = 3/4-(f-1)^2, w_2(f) = (f-1/2)^2/2 written as
+  // c0 + f (c1 + f c2)
+  const int slot = lane / 9, oi = (lane % 9) / 3, oj = lane % 3;
+  auto coef = [](int o, float &c0, float &c1, float &c2) {
+    c0 = o == 0 ? 1.125f : (o == 1 ? -0.25f : 0.125f);
+    c1 = o == 0 ? -1.5f : (o == 1 ? 2.0f : -0.5f);
+    c2 = o == 1 ? -1.0f : 0.5f;
+  };
+  float ci0, ci1, ci2, cj0, cj1, cj2;
+  coef(oi, ci0, ci1, ci2);
+  coef(oj, cj0, cj1, cj2);
+  const float odx = oi * dx, ody = oj * dx;
+  float *myacc = &acc[warp][0][0];
+
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    for (int i = threadIdx.x; i < 4 * kNodes; i += kP2GThreads) (&sm[0][0])[i] = 0.0f;
+    for (int i = tid; i < kP2GWarps * 4 * kNodes; i += kP2GThreads) (&acc[0][0][0])[i] = 0.0f;
     const int dir = d.bk_dir[b];
-    if (threadIdx.x < 8) sgb[threadIdx.x] = neighbour_gb(d, P, dir, threadIdx.x);
     int K[3];
     bucket_origin(P, dir, K);
-    __syncthreads();
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
-    for (int s = start + threadIdx.x; s < start + cnt; s += kP2GThreads) {
-      const int p = d.perm[s];
-      const int mid = min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1);
-      const MatParams mp = d.mats[mid];
-      float x[3], v[3], C[9], F[9];
+    for (int c0 = 0; c0 < cnt; c0 += kP2GChunk) {
+      const int nc = min(kP2GChunk, cnt - c0);
+      __syncthreads();  // spd / scell of the previous chunk consumed
+      for (int j = tid; j < nc; j += kP2GThreads) {
+        const int p = d.perm[start + c0 + j];
+        float x[3], v[3], C[9], Sv[6];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        x[k] = pin[(CH_X + k) * cap + p];
-        v[k] = pin[(CH_V + k) * cap + p];
+        for (int k = 0; k < 3; ++k) {
+          x[k] = pin[(CH_X + k) * cap + p];
+          v[k] = pin[(CH_V + k) * cap + p];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) C[k] = pin[(CH_C + k) * cap + p];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) Sv[k] = pin[(CH_S + k) * cap + p];
+        float mass = pin[CH_M * cap + p];
+        // A = m C - dt Dinv vol tau (contrib of Transfer.cu:868 is -dt Dinv vol P F^T)
+        const float kk = -dt * Dinv;
+        float A[9];
+        A[0] = mass * C[0] + kk * Sv[0];
+        A[1] = mass * C[1] + kk * Sv[3];
+        A[2] = mass * C[2] + kk * Sv[4];
+        A[3] = mass * C[3] + kk * Sv[3];
+        A[4] = mass * C[4] + kk * Sv[1];
+        A[5] = mass * C[5] + kk * Sv[5];
+        A[6] = mass * C[6] + kk * Sv[4];
+        A[7] = mass * C[7] + kk * Sv[5];
+        A[8] = mass * C[8] + kk * Sv[2];
+        const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
+                       s2 = stencil1(x[2], inv_dx);
+        const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
+        const int cell = d.pkey[p] & 63;
+        if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u ||
+            ((l0 << 4) | (l1 << 2) | l2) != cell) {
+          atomicOr(&d.cnt->status, ST_STENCIL);
+          mass = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) A[k] = 0.0f;
+          v[0] = v[1] = v[2] = 0.0f;
+        }
+        const float fdx0 = s0.f * dx, fdx1 = s1.f * dx, fdx2 = s2.f * dx;
+        const float b0 = mass * v[0] - (A[0] * fdx0 + A[1] * fdx1 + A[2] * fdx2);
+        const float b1 = mass * v[1] - (A[3] * fdx0 + A[4] * fdx1 + A[5] * fdx2);
+        const float b2 = mass * v[2] - (A[6] * fdx0 + A[7] * fdx1 + A[8] * fdx2);
+        spd[0][j] = make_float4(mass, b0, b1, b2);
+        spd[1][j] = make_float4(A[0], A[1], A[2], A[3]);
+        spd[2][j] = make_float4(A[4], A[5], A[6], A[7]);
+        spd[3][j] = make_float4(A[8], s0.f, s1.f, s2.f);
+        scell[j] = (unsigned char)cell;
       }
-#pragma unroll
-      for (int k = 0; k < 9; ++k) C[k] = pin[(CH_C + k) * cap + p];
-      const float mass = pin[CH_M * cap + p], vol = pin[CH_VOL * cap + p];
-      float Jeos = 1.0f;
-      if (mp.type == MPM_EOS) {
-        Jeos = pin[CH_J * cap + p];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
-      } else {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) F[k] = pin[(CH_F + k) * cap + p];
+      __syncthreads();
+      // cell ranges of the chunk (sorted by cell): first index with cell >= c
+      for (int c = tid; c <= 64; c += kP2GThreads) {
+        int lo = 0, hi = nc;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (scell[mid] < c)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        cst[c] = lo;
       }
-      float mu = mp.mu, lam = mp.lam;
-      if (lame) {
-        mu = pin[CH_MU * cap + p];
-        lam = pin[CH_LAM * cap + p];
-      }
-      Sym3 tau;
-      if (!kirchhoff(mp.type, mu, lam, mp.bulk, mp.gamma, F, Jeos, tau))
-        atomicOr(&d.cnt->status, ST_NAN);
-      // A = m C - dt Dinv vol tau: momentum of node i is W (m v + A (x_i - x_p))
-      const float k = -dt * Dinv * vol;
-      float A[9];
-      A[0] = mass * C[0] + k * tau.xx;
-      A[1] = mass * C[1] + k * tau.xy;
-      A[2] = mass * C[2] + k * tau.xz;
-      A[3] = mass * C[3] + k * tau.xy;
-      A[4] = mass * C[4] + k * tau.yy;
-      A[5] = mass * C[5] + k * tau.yz;
-      A[6] = mass * C[6] + k * tau.xz;
-      A[7] = mass * C[7] + k * tau.yz;
-      A[8] = mass * C[8] + k * tau.zz;
-      const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
-                     s2 = stencil1(x[2], inv_dx);
-      const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
-      if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u) {
-        atomicOr(&d.cnt->status, ST_STENCIL);
-        continue;
-      }
-      const float mv0 = mass * v[0], mv1 = mass * v[1], mv2 = mass * v[2];
-      // Particles are sorted by cell, so ~8 neighbouring lanes share one
-      // stencil.  Each lane walks the 27 nodes in its own rotated order
-      // (axis offsets shifted by the base-3 digits of lane % 27), so lanes of
-      // one cell update different nodes at every step instead of serialising
-      // on the same shared-memory word.
-      const int rot = (threadIdx.x & 31) % 27;
-      int o0[3], o1[3], o2[3];
-      float w0[3], w1[3], w2[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        o0[q] = (q + rot % 3) % 3;
-        o1[q] = (q + (rot / 3) % 3) % 3;
-        o2[q] = (q + rot / 9) % 3;
-        w0[q] = o0[q] == 0 ? s0.w[0] : (o0[q] == 1 ? s0.w[1] : s0.w[2]);
-        w1[q] = o1[q] == 0 ? s1.w[0] : (o1[q] == 1 ? s1.w[1] : s1.w[2]);
-        w2[q] = o2[q] == 0 ? s2.w[0] : (o2[q] == 1 ? s2.w[1] : s2.w[2]);
-      }
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        const float xi = ((float)o0[i] - s0.f) * dx;
-        const float a0 = mv0 + A[0] * xi, a1 = mv1 + A[3] * xi, a2 = mv2 + A[6] * xi;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const float xj = ((float)o1[j] - s1.f) * dx;
-          const float b0 = a0 + A[1] * xj, b1 = a1 + A[4] * xj, b2 = a2 + A[7] * xj;
-          const float wij = w0[i] * w1[j];
-          const int row = ((l0 + o0[i]) * 6 + (l1 + o1[j])) * 6 + l2;
-#pragma unroll
-          for (int kk = 0; kk < 3; ++kk) {
-            const float xk = ((float)o2[kk] - s2.f) * dx;
-            const float W = wij * w2[kk];
-            const int nd = row + o2[kk];
-            atomicAdd(&sm[0][nd], W * mass);
-            atomicAdd(&sm[1][nd], W * (b0 + A[2] * xk));
-            atomicAdd(&sm[2][nd], W * (b1 + A[5] * xk));
-            atomicAdd(&sm[3][nd], W * (b2 + A[8] * xk));
+      __syncthreads();
+      // phase 2: 8 cells per warp, three per round (slots), 9 lanes per cell
+      for (int round = 0; round < 3; ++round) {
+        const int t = 3 * round + slot;  // this lane's cell of the warp, 0..8
+        const bool has = lane < 27 && t < 8;
+        const int cell = warp + 8 * t;
+        int q = 0, q1 = 0;
+        if (has) {
+          q = cst[cell];
+          q1 = cst[cell + 1];
+        }
+        float am0 = 0.f, am1 = 0.f, am2 = 0.f;
+        float a00 = 0.f, a01 = 0.f, a02 = 0.f, a10 = 0.f, a11 = 0.f, a12 = 0.f;
+        float a20 = 0.f, a21 = 0.f, a22 = 0.f;
+        for (; q < q1; ++q) {
+          const float4 u0 = spd[0][q], u1 = spd[1][q], u2 = spd[2][q], u3 = spd[3][q];
+          const float wx = fmaf(fmaf(ci2, u3.y, ci1), u3.y, ci0);
+          const float wy = fmaf(fmaf(cj2, u3.z, cj1), u3.z, cj0);
+          const float fz = u3.w;
+          const float wz0 = fmaf(fmaf(0.5f, fz, -1.5f), fz, 1.125f);
+          const float wz1 = fmaf(fmaf(-1.0f, fz, 2.0f), fz, -0.25f);
+          const float wz2 = fmaf(fmaf(0.5f, fz, -0.5f), fz, 0.125f);
+          const float wij = wx * wy;
+          const float mw = u0.x * wij;
+          // b + A (i dx, j dx, k dx) for k = 0, 1, 2
+          const float p0 = fmaf(u1.y, ody, fmaf(u1.x, odx, u0.y));
+          const float p1 = fmaf(u2.x, ody, fmaf(u1.w, odx, u0.z));
+          const float p2 = fmaf(u2.w, ody, fmaf(u2.z, odx, u0.w));
+          const float r0 = u1.z * dx, r1 = u2.y * dx, r2 = u3.x * dx;
+          const float W0 = wij * wz0, W1 = wij * wz1, W2 = wij * wz2;
+          am0 = fmaf(mw, wz0, am0);
+          am1 = fmaf(mw, wz1, am1);
+          am2 = fmaf(mw, wz2, am2);
+          a00 = fmaf(W0, p0, a00);
+          a01 = fmaf(W0, p1, a01);
+          a02 = fmaf(W0, p2, a02);
+          a10 = fmaf(W1, p0 + r0, a10);
+          a11 = fmaf(W1, p1 + r1, a11);
+          a12 = fmaf(W1, p2 + r2, a12);
+          const float r02 = r0 + r0, r12 = r1 + r1, r22 = r2 + r2;
+          a20 = fmaf(W2, p0 + r02, a20);
+          a21 = fmaf(W2, p1 + r12, a21);
+          a22 = fmaf(W2, p2 + r22, a22);
+        }
+        // slot by slot into the warp's private nodes (cells of one round may
+        // share nodes, lanes of one slot own distinct nodes)
+        const int nd0 = has ? ((((cell >> 4) + oi) * 6 + (((cell >> 2) & 3) + oj)) * 6 + (cell & 3))
+                            : 0;
+        for (int sl = 0; sl < 3; ++sl) {
+          if (has && slot == sl && q1 > cst[cell]) {
+            myacc[0 * kNodes + nd0] += am0;
+            myacc[1 * kNodes + nd0] += a00;
+            myacc[2 * kNodes + nd0] += a01;
+            myacc[3 * kNodes + nd0] += a02;
+            myacc[0 * kNodes + nd0 + 1] += am1;
+            myacc[1 * kNodes + nd0 + 1] += a10;
+            myacc[2 * kNodes + nd0 + 1] += a11;
+            myacc[3 * kNodes + nd0 + 1] += a12;
+            myacc[0 * kNodes + nd0 + 2] += am2;
+            myacc[1 * kNodes + nd0 + 2] += a20;
+            myacc[2 * kNodes + nd0 + 2] += a21;
+            myacc[3 * kNodes + nd0 + 2] += a22;
           }
+          __syncwarp();
         }
       }
     }
     __syncthreads();
-    for (int nd = threadIdx.x; nd < kNodes; nd += kP2GThreads) {
-      const float4 val = make_float4(sm[0][nd], sm[1][nd], sm[2][nd], sm[3][nd]);
-      if (val.x != 0.0f || val.y != 0.0f || val.z != 0.0f || val.w != 0.0f) {
-        const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
-        const int gb = sgb[((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2)];
-        const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
-        if (gb >= 0) atomicAdd(&d.grid[(long long)gb * 64 + cell], val);
+    float4 *tile = d.ptile + (long long)b * kTileNodes;
+    for (int nd = tid; nd < kNodes; nd += kP2GThreads) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int w = 0; w < kP2GWarps; ++w) {
+        v.x += acc[w][0][nd];
+        v.y += acc[w][1][nd];
+        v.z += acc[w][2][nd];
+        v.w += acc[w][3][nd];
       }
+      tile[nd] = v;
     }
     __syncthreads();
   }
 }
 
-// UpdateZSGrid (MPMPipeline.cu:852-877): v = mv / m + g dt where m != 0,
-// running max of |v|^2; then ApplyBoundaryOnZSGrid (Boundary.cu:105-116) with
-// the analytic box walls (see the oracle's apply_bc for the same rule).
-__global__ void k_grid_update(DevPtrs d, int mode) {
+// Grid node sums from the P2G tiles: node (l0, l1, l2) of grid block G lies
+// in the tile of particle block G - o (o in {0, 1}^3, in blocks) at tile
+// coordinate l + 4 o when that is < 6.  The <= 8 tiles are added in the fixed
+// order o = (0,0,0), (0,0,1), ..., so the sums are reproducible.  mode bit 1
+// applies UpdateZSGrid and bit 2 ApplyBoundaryOnZSGrid to the sum.
+__device__ __forceinline__ void update_node(const SimParams &P, int mode, int gdir, int cell,
+                                            float4 &g, float &vmax);
+
+__global__ void k_grid_gather(DevPtrs d, int mode) {
   const SimParams &P = *d.prm;
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
-  const float dt = P.dt;
+  const int dy = P.block_dims[1], dz = P.block_dims[2];
   float vmax = 0.0f;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
        idx += (long long)gridDim.x * blockDim.x) {
-    float4 g = d.grid[idx];
-    if (g.x == 0.0f) continue;
-    if (mode & 1) {
-      const float r = 1.0f / g.x;
-      g.y = g.y * r + P.gravity[0] * dt;
-      g.z = g.z * r + P.gravity[1] * dt;
-      g.w = g.w * r + P.gravity[2] * dt;
-      vmax = fmaxf(vmax, g.y * g.y + g.z * g.z + g.w * g.w);
-    }
-    if ((mode & 2) && P.bc_type != MPM_BC_NONE) {
-      const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
-      const int dir = d.gb_dir[gb];
-      const int dz = P.block_dims[2], dy = P.block_dims[1];
-      const int I[3] = {((dir / (dz * dy)) + P.block_lo[0]) * 4 + (cell >> 4),
-                        (((dir / dz) % dy) + P.block_lo[1]) * 4 + ((cell >> 2) & 3),
-                        ((dir % dz) + P.block_lo[2]) * 4 + (cell & 3)};
-      float vel[3] = {g.y, g.z, g.w};
-      bool any = false;
-      const int t = P.bc_thickness;
+    const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
+    const int gdir = d.gb_dir[gb];
+    const int c0 = gdir / (dz * dy), c1 = (gdir / dz) % dy, c2 = gdir % dz;
+    const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const bool lower = I[a] < P.bc_lo[a] + t, upper = I[a] > P.bc_hi[a] - t;
-        if (!(lower || upper)) continue;
-        any = true;
-        if (P.bc_type == MPM_BC_SLIP) vel[a] = 0.0f;
-        if (P.bc_type == MPM_BC_SEPARATE) {
-          if (lower && vel[a] < 0.0f) vel[a] = 0.0f;
-          if (upper && vel[a] > 0.0f) vel[a] = 0.0f;
-        }
-      }
-      if (any && P.bc_type == MPM_BC_STICKY) vel[0] = vel[1] = vel[2] = 0.0f;
-      g.y = vel[0];
-      g.z = vel[1];
-      g.w = vel[2];
+    for (int o = 0; o < 8; ++o) {
+      const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
+      if ((o0 && (l0 >= 2 || c0 < 1)) || (o1 && (l1 >= 2 || c1 < 1)) ||
+          (o2 && (l2 >= 2 || c2 < 1)))
+        continue;
+      const int bk = d.dir_bk[gdir - (o0 * dy + o1) * dz - o2];
+      if (bk < 0) continue;
+      const float4 t = d.ptile[(long long)bk * kTileNodes +
+                               ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2)];
+      g.x += t.x;
+      g.y += t.y;
+      g.z += t.z;
+      g.w += t.w;
     }
+    if (g.x != 0.0f) update_node(P, mode, gdir, cell, g, vmax);
     d.grid[idx] = g;
   }
   if (mode & 1) {
@@ -215,7 +297,68 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
   }
 }
 
-template <bool kFuseRM>
+// UpdateZSGrid (MPMPipeline.cu:852-877): v = mv / m + g dt where m != 0,
+// running max of |v|^2; then ApplyBoundaryOnZSGrid (Boundary.cu:105-116) with
+// the analytic box walls: a node is in the lower wall of axis a when
+// I_a < lo_a + thickness and in the upper wall when I_a > hi_a - thickness;
+// sticky sets v = 0, slip removes the wall-normal component, separate removes
+// it only when it points into the wall (collider velocity 0).
+__device__ __forceinline__ void update_node(const SimParams &P, int mode, int gdir, int cell,
+                                            float4 &g, float &vmax) {
+  if (mode & 1) {
+    const float r = 1.0f / g.x;
+    const float dt = P.dt;
+    g.y = g.y * r + P.gravity[0] * dt;
+    g.z = g.z * r + P.gravity[1] * dt;
+    g.w = g.w * r + P.gravity[2] * dt;
+    vmax = fmaxf(vmax, g.y * g.y + g.z * g.z + g.w * g.w);
+  }
+  if ((mode & 2) && P.bc_type != MPM_BC_NONE) {
+    const int dz = P.block_dims[2], dy = P.block_dims[1];
+    const int I[3] = {((gdir / (dz * dy)) + P.block_lo[0]) * 4 + (cell >> 4),
+                      (((gdir / dz) % dy) + P.block_lo[1]) * 4 + ((cell >> 2) & 3),
+                      ((gdir % dz) + P.block_lo[2]) * 4 + (cell & 3)};
+    float vel[3] = {g.y, g.z, g.w};
+    bool any = false;
+    const int t = P.bc_thickness;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const bool lower = I[a] < P.bc_lo[a] + t, upper = I[a] > P.bc_hi[a] - t;
+      if (!(lower || upper)) continue;
+      any = true;
+      if (P.bc_type == MPM_BC_SLIP) vel[a] = 0.0f;
+      if (P.bc_type == MPM_BC_SEPARATE) {
+        if (lower && vel[a] < 0.0f) vel[a] = 0.0f;
+        if (upper && vel[a] > 0.0f) vel[a] = 0.0f;
+      }
+    }
+    if (any && P.bc_type == MPM_BC_STICKY) vel[0] = vel[1] = vel[2] = 0.0f;
+    g.y = vel[0];
+    g.z = vel[1];
+    g.w = vel[2];
+  }
+}
+
+__global__ void k_grid_update(DevPtrs d, int mode) {
+  const SimParams &P = *d.prm;
+  const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
+  float vmax = 0.0f;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    float4 g = d.grid[idx];
+    if (g.x == 0.0f) continue;
+    update_node(P, mode, d.gb_dir[idx >> 6], (int)(idx & 63), g, vmax);
+    d.grid[idx] = g;
+  }
+  if (mode & 1) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if ((threadIdx.x & 31) == 0 && vmax > 0.0f)
+      atomicMax(&d.cnt->max_vel_sqr_bits, __float_as_uint(vmax));
+  }
+}
+
+template <bool kFuseRM, bool kFuseBin>
 __global__ void __launch_bounds__(kG2PThreads)
     k_g2p(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
           float *__restrict__ pout, int32_t *__restrict__ iout) {
@@ -245,7 +388,13 @@ __global__ void __launch_bounds__(kG2PThreads)
     __syncthreads();
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
-    for (int s = start + threadIdx.x; s < start + cnt; s += kG2PThreads) {
+    // warp-uniform trip count: the fused binning below is a warp collective
+    for (int sbase = start; sbase < start + cnt; sbase += kG2PThreads) {
+      const int s = sbase + (int)threadIdx.x;
+      const bool live = s < start + cnt;
+      const unsigned mask = __ballot_sync(0xffffffffu, live);
+      if (!mask) continue;
+      if (!live) continue;  // live lanes are exactly `mask`
       const int p = d.perm[s];
       const int mid = min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1);
       const MatParams mp = d.mats[mid];
@@ -259,35 +408,59 @@ __global__ void __launch_bounds__(kG2PThreads)
       if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u) {
         atomicOr(&d.cnt->status, ST_STENCIL);
       } else {
+        // v = sum W g and C = Dinv sum W g (x_i - x_p)^T over the 27 nodes,
+        // summed k-innermost so each weight product is formed once per level:
+        // with W = w_i w_j w_k and x_i - x_p = (xi, xj, xk),
+        //   t = sum_k w_k g, tk = sum_k w_k xk g; S = sum_j w_j t,
+        //   Sj = sum_j w_j xj t, Sk = sum_j w_j tk; then over i.
+        float xi[3], xj[3], xk[3], wxk[3], wyj[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          xi[q] = ((float)q - s0.f) * dx;
+          xj[q] = ((float)q - s1.f) * dx;
+          xk[q] = ((float)q - s2.f) * dx;
+          wxk[q] = s2.w[q] * xk[q];
+          wyj[q] = s1.w[q] * xj[q];
+        }
+        float cx[3] = {0.f, 0.f, 0.f}, cy[3] = {0.f, 0.f, 0.f}, cz[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const float xi = ((float)i - s0.f) * dx;
+          float S[3] = {0.f, 0.f, 0.f}, Sj[3] = {0.f, 0.f, 0.f}, Sk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
-            const float xj = ((float)j - s1.f) * dx;
-            const float wij = s0.w[i] * s1.w[j];
             const int row = ((l0 + i) * 6 + (l1 + j)) * 6 + l2;
+            float t[3] = {0.f, 0.f, 0.f}, tk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
-              const float xk = ((float)kk - s2.f) * dx;
-              const float W = wij * s2.w[kk];
               const int nd = row + kk;
-              const float g0 = sv[0][nd], g1 = sv[1][nd], g2 = sv[2][nd];
-              vel[0] += W * g0;
-              vel[1] += W * g1;
-              vel[2] += W * g2;
-              const float w0 = W * g0, w1 = W * g1, w2 = W * g2;
-              Cn[0] += w0 * xi;
-              Cn[1] += w0 * xj;
-              Cn[2] += w0 * xk;
-              Cn[3] += w1 * xi;
-              Cn[4] += w1 * xj;
-              Cn[5] += w1 * xk;
-              Cn[6] += w2 * xi;
-              Cn[7] += w2 * xj;
-              Cn[8] += w2 * xk;
+              const float g[3] = {sv[0][nd], sv[1][nd], sv[2][nd]};
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                t[a] = fmaf(s2.w[kk], g[a], t[a]);
+                tk[a] = fmaf(wxk[kk], g[a], tk[a]);
+              }
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+              S[a] = fmaf(s1.w[j], t[a], S[a]);
+              Sj[a] = fmaf(wyj[j], t[a], Sj[a]);
+              Sk[a] = fmaf(s1.w[j], tk[a], Sk[a]);
             }
           }
+          const float wxi = s0.w[i] * xi[i];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            vel[a] = fmaf(s0.w[i], S[a], vel[a]);
+            cx[a] = fmaf(wxi, S[a], cx[a]);
+            cy[a] = fmaf(s0.w[i], Sj[a], cy[a]);
+            cz[a] = fmaf(s0.w[i], Sk[a], cz[a]);
+          }
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          Cn[a * 3 + 0] = cx[a];
+          Cn[a * 3 + 1] = cy[a];
+          Cn[a * 3 + 2] = cz[a];
         }
       }
 #pragma unroll
@@ -295,11 +468,19 @@ __global__ void __launch_bounds__(kG2PThreads)
 #pragma unroll
       for (int k = 0; k < 3; ++k) x[k] += vel[k] * dt;
       float F[9], J;
+      Sym3 tau;
+      bool ok_state = true;
+      float mu = mp.mu, lam = mp.lam;
+      if (lame) {
+        mu = pin[CH_MU * cap + p];
+        lam = pin[CH_LAM * cap + p];
+      }
       if (mp.type == MPM_EOS) {
         J = pin[CH_J * cap + p] * (1.0f + dt * (Cn[0] + Cn[4] + Cn[8]));
         const float c = cbrtf(J);
 #pragma unroll
         for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? c : 0.0f;
+        ok_state = kirchhoff(MPM_EOS, mu, lam, mp.bulk, mp.gamma, F, J, tau);
       } else {
         float Fo[9];
 #pragma unroll
@@ -311,16 +492,14 @@ __global__ void __launch_bounds__(kG2PThreads)
           for (int c = 0; c < 3; ++c)
             F[r * 3 + c] = Fo[r * 3 + c] + dt * (Cn[r * 3 + 0] * Fo[c] + Cn[r * 3 + 1] * Fo[3 + c] +
                                                  Cn[r * 3 + 2] * Fo[6 + c]);
-        if (kFuseRM && mp.plastic == MPM_PLASTIC_NADP) {
-          float mu = mp.mu, lam = mp.lam;
-          if (lame) {
-            mu = pin[CH_MU * cap + p];
-            lam = pin[CH_LAM * cap + p];
-          }
-          if (project_dp(mu, lam, mp.alpha, F) < 0) atomicOr(&d.cnt->status, ST_NAN);
-        }
+        if (kFuseRM && mp.plastic == MPM_PLASTIC_NADP)
+          ok_state = project_dp(mu, lam, mp.alpha, F, tau) >= 0;
+        else
+          ok_state = kirchhoff(mp.type, mu, lam, mp.bulk, mp.gamma, F, 1.0f, tau);
         J = det3(F);
       }
+      if (!ok_state) atomicOr(&d.cnt->status, ST_NAN);
+      const float vol = pin[CH_VOL * cap + p];
       bool finite = isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(J);
 #pragma unroll
       for (int k = 0; k < 9; ++k) finite = finite && isfinite(F[k]);
@@ -338,19 +517,42 @@ __global__ void __launch_bounds__(kG2PThreads)
       }
       pout[CH_J * cap + s] = J;
       pout[CH_M * cap + s] = pin[CH_M * cap + p];
-      pout[CH_VOL * cap + s] = pin[CH_VOL * cap + p];
+      pout[CH_VOL * cap + s] = vol;
+      pout[(CH_S + 0) * cap + s] = vol * tau.xx;
+      pout[(CH_S + 1) * cap + s] = vol * tau.yy;
+      pout[(CH_S + 2) * cap + s] = vol * tau.zz;
+      pout[(CH_S + 3) * cap + s] = vol * tau.xy;
+      pout[(CH_S + 4) * cap + s] = vol * tau.xz;
+      pout[(CH_S + 5) * cap + s] = vol * tau.yz;
       if (lame) {
         pout[CH_MU * cap + s] = pin[CH_MU * cap + p];
         pout[CH_LAM * cap + s] = pin[CH_LAM * cap + p];
       }
       iout[IC_MAT * cap + s] = mid;
       iout[IC_ID * cap + s] = iin[IC_ID * cap + p];
+      if (kFuseBin) {
+        // key of the new position for the next partition (storage slot s)
+        const int key = bin_key(P, x[0], x[1], x[2], &d.cnt->status);
+        d.pkey[s] = key;
+        bin_count(d, P, key, mask);
+      }
     }
     __syncthreads();
   }
 }
 
-// ZSReturnMapping as its own pass (in place, storage order).
+__device__ __forceinline__ void store_stress(float *__restrict__ pb, long long cap, long long p,
+                                             float vol, const Sym3 &t) {
+  pb[(CH_S + 0) * cap + p] = vol * t.xx;
+  pb[(CH_S + 1) * cap + p] = vol * t.yy;
+  pb[(CH_S + 2) * cap + p] = vol * t.zz;
+  pb[(CH_S + 3) * cap + p] = vol * t.xy;
+  pb[(CH_S + 4) * cap + p] = vol * t.xz;
+  pb[(CH_S + 5) * cap + p] = vol * t.yz;
+}
+
+// ZSReturnMapping as its own pass (in place, storage order); refreshes the
+// stored stress of every projected particle.
 __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
                                  const int32_t *__restrict__ ibuf) {
   const SimParams &P = *d.prm;
@@ -368,37 +570,90 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
       mu = pbuf[CH_MU * cap + p];
       lam = pbuf[CH_LAM * cap + p];
     }
-    const int r = project_dp(mu, lam, mp.alpha, F);
+    Sym3 tau;
+    const int r = project_dp(mu, lam, mp.alpha, F, tau);
     if (r < 0) atomicOr(&d.cnt->status, ST_NAN);
     if (r > 0) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) pbuf[(CH_F + k) * cap + p] = F[k];
       pbuf[CH_J * cap + p] = det3(F);
+      store_stress(pbuf, cap, p, pbuf[CH_VOL * cap + p], tau);
     }
+  }
+}
+
+// S = vol * tau of every particle from its current F (or J): the stress P2G
+// reads, recomputed after an upload or a change of materials.
+__global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__restrict__ ibuf) {
+  const SimParams &P = *d.prm;
+  const long long cap = d.cap, n = P.n;
+  const bool lame = P.has_lame != 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const MatParams mp = d.mats[min(max(ibuf[IC_MAT * cap + p], 0), kMaxMaterials - 1)];
+    float F[9];
+    float J = 1.0f;
+    if (mp.type == MPM_EOS) {
+      J = pbuf[CH_J * cap + p];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) F[k] = pbuf[(CH_F + k) * cap + p];
+    }
+    float mu = mp.mu, lam = mp.lam;
+    if (lame) {
+      mu = pbuf[CH_MU * cap + p];
+      lam = pbuf[CH_LAM * cap + p];
+    }
+    Sym3 tau;
+    if (!kirchhoff(mp.type, mu, lam, mp.bulk, mp.gamma, F, J, tau))
+      atomicOr(&d.cnt->status, ST_NAN);
+    store_stress(pbuf, cap, p, pbuf[CH_VOL * cap + p], tau);
   }
 }
 
 }  // namespace
 
+void configure_launches(DevPtrs &d) {
+  int a = 0, b = 0;
+  cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, kP2GSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g, kP2GThreads, kP2GSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true>, kG2PThreads, 0);
+  d.grid_p2g = d.num_sms * (a > 0 ? a : 1);
+  d.grid_g2p = d.num_sms * (b > 0 ? b : 1);
+}
+
 void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
-  k_p2g<<<d.num_sms * 8, kP2GThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+  k_p2g<<<d.grid_p2g, kP2GThreads, kP2GSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+}
+
+void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
+  k_grid_gather<<<d.num_sms * 8, 256, 0, s>>>(d, mode);
 }
 
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {
   k_grid_update<<<d.num_sms * 8, 256, 0, s>>>(d, mode);
 }
 
-void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, cudaStream_t s) {
-  if (fuse_rm)
-    k_g2p<true><<<d.num_sms * 8, kG2PThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur],
-                                                      d.pbuf[1 - cur], d.ibuf[1 - cur]);
+void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
+  const int grid = d.grid_g2p;
+  float *pi = d.pbuf[cur], *po = d.pbuf[1 - cur];
+  int32_t *ii = d.ibuf[cur], *io = d.ibuf[1 - cur];
+  if (fuse_rm && fuse_bin)
+    k_g2p<true, true><<<grid, kG2PThreads, 0, s>>>(d, pi, ii, po, io);
+  else if (fuse_rm)
+    k_g2p<true, false><<<grid, kG2PThreads, 0, s>>>(d, pi, ii, po, io);
   else
-    k_g2p<false><<<d.num_sms * 8, kG2PThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur],
-                                                       d.pbuf[1 - cur], d.ibuf[1 - cur]);
+    k_g2p<false, false><<<grid, kG2PThreads, 0, s>>>(d, pi, ii, po, io);
 }
 
 void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s) {
   k_return_mapping<<<d.num_sms * 8, 256, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+}
+
+void launch_stress(const DevPtrs &d, int cur, cudaStream_t s) {
+  k_stress<<<d.num_sms * 8, 256, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
 }
 
 }  // namespace zsmpm

@@ -33,7 +33,8 @@ enum : int {
   CH_VOL = 26,  // 1
   CH_MU = 27,   // 1, per-particle override (optional)
   CH_LAM = 28,  // 1, per-particle override (optional)
-  NCH = 29
+  CH_S = 29,    // 6, vol * Kirchhoff stress (xx, yy, zz, xy, xz, yz) of the current F
+  NCH = 35
 };
 // int particle channels
 enum : int { IC_MAT = 0, IC_ID = 1, NICH = 2 };
@@ -49,9 +50,10 @@ enum : int {
 };
 
 constexpr int kMaxMaterials = 64;
-constexpr int kScanTile = 4096;       // directory entries per scan tile
-constexpr int kScanThreads = 256;     // 16 entries per thread
-constexpr int kMaxSortBucket = 4096;  // particles per block sorted on chip
+constexpr int kScanTile = 2048;       // directory entries per scan tile
+constexpr int kScanThreads = 256;     // 8 entries per thread
+constexpr int kScanPerThread = kScanTile / kScanThreads;
+constexpr int kTileNodes = 216;       // 6^3 nodes of one particle block's stencils
 
 struct MatParams {
   int type, plastic;
@@ -87,23 +89,25 @@ struct DevPtrs {
   long long cap;  // particle plane stride
   int32_t *pkey;  // (directory index << 6) | cell, per storage slot
   int32_t *perm;  // sorted position -> storage slot
-  int32_t *dir_count, *dir_fill, *dir_gb;
+  int32_t *perm_tmp;  // scratch of the oversize-block sort
+  int32_t *dir_count, *dir_fill, *dir_gb, *dir_bk;
   uint8_t *dir_flag;
   long long ndir;
   int32_t *gb_dir;
   int32_t *bk_dir, *bk_start, *bk_count;
   int cap_gblocks;
   float4 *grid;
+  float4 *ptile;  // per particle block: its 6^3 P2G node sums (216 float4)
   int32_t *tile_sums;
   int ntiles;
   Counters *cnt;
   SimParams *prm;
   MatParams *mats;
   int num_sms;
+  int grid_p2g, grid_g2p;  // persistent grids: SMs x resident CTAs per SM
 };
 
 // partition.cu
-void launch_reset(const DevPtrs &d, cudaStream_t s);
 void launch_bin(const DevPtrs &d, int cur, cudaStream_t s);
 void launch_scan(const DevPtrs &d, cudaStream_t s);
 void launch_scatter(const DevPtrs &d, cudaStream_t s);
@@ -112,11 +116,20 @@ void launch_grid_clear(const DevPtrs &d, cudaStream_t s);
 void launch_full_dir_clear(const DevPtrs &d, cudaStream_t s);
 
 // transfer.cu
+// fills the persistent grid sizes of DevPtrs from the occupancy of each kernel
+void configure_launches(DevPtrs &d);
 void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s);
-// mode bit 1: momentum -> velocity + gravity, bit 2: boundary
+// sum of the P2G tiles into the grid; mode bit 1: momentum -> velocity +
+// gravity, bit 2: boundary (mode 0 leaves m, mv as the reference P2G does)
+void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s);
+// mode bit 1: momentum -> velocity + gravity, bit 2: boundary, on the grid
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s);
-void launch_g2p(const DevPtrs &d, int cur, int fuse_return_mapping, cudaStream_t s);
+// fuse_rm: return mapping in G2P; fuse_bin: bin the new positions for the
+// next partition
+void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s);
 void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s);
+// vol * Kirchhoff stress of every particle from its current F (or J)
+void launch_stress(const DevPtrs &d, int cur, cudaStream_t s);
 
 // io.cu
 struct IngestSrc {
@@ -124,6 +137,8 @@ struct IngestSrc {
   const int32_t *mat;
 };
 void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s);
+void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
+                     cudaStream_t s);
 // writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
 void launch_egest(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s);
 

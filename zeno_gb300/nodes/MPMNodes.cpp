@@ -1,0 +1,614 @@
+// The CuLagrange MPM nodes of zeno (projects/CuLagrange/mpm/*.cu) as thin
+// wrappers over the zsmpm C ABI: same node names, socket names, parameter
+// names and defaults, same in-place object flow (a node mutates its input
+// object and emits the same pointer).  The zpc containers the reference
+// passes between nodes become one device context per particle set, shared
+// by the ZSParticles, ZSPartition and ZSGrid objects once they are bound.
+#include <zsmpm.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "zeno_api.hpp"
+
+namespace zeno {
+
+namespace {
+
+void check(int32_t rc, const char *what) {
+  if (rc != MPM_OK)
+    throw std::runtime_error(std::string(what) + " failed (" + std::to_string(rc) +
+                             "): " + mpm_last_error());
+}
+
+}  // namespace
+
+// One device context: grid + partition + particle store of a particle set.
+struct MpmContext {
+  mpm_ctx *h = nullptr;
+  float dx = 0.0f;
+  ~MpmContext() {
+    if (h) mpm_ctx_destroy(h);
+  }
+};
+
+// ConfigConstitutiveModel output (Structures.hpp:34-132)
+struct ZenoConstitutiveModel : IObject {
+  mpm_material mat{};
+  float dx = 0.1f, volume = 0.0f, density = 1000.0f;
+};
+
+// ToZSParticles output (Structures.hpp:134-531)
+struct ZenoParticles : IObject {
+  std::shared_ptr<MpmContext> ctx;
+  std::shared_ptr<PrimitiveObject> prim;  // the source primitive, written back by
+                                          // UpdatePrimitiveFromZSParticles
+  std::shared_ptr<ZenoConstitutiveModel> model;
+  int64_t n = 0;
+  int category = 0;
+};
+
+// MakeZSPartition output (Structures.hpp:533-586)
+struct ZenoPartition : IObject {
+  std::shared_ptr<MpmContext> ctx;
+  bool rebuilt = false;
+};
+
+// MakeZSGrid output (Structures.hpp:588-623)
+struct ZenoGrid : IObject {
+  float dx = 0.1f;
+  std::string transferScheme = "apic";
+  std::shared_ptr<MpmContext> ctx;
+  std::shared_ptr<ZenoPartition> partition;
+};
+
+// ToZSBoundary output (Structures.hpp:807-835), analytic box collider
+struct ZenoBoundary : IObject {
+  mpm_boundary bc{};
+};
+
+namespace {
+
+float get_dt(const INode &node) {
+  return node.get_input<NumericObject>("dt")->get<float>();
+}
+
+std::shared_ptr<MpmContext> bound_ctx(const std::shared_ptr<ZenoPartition> &p, const char *node) {
+  if (!p->ctx)
+    throw std::runtime_error(std::string(node) +
+                             ": the ZSPartition is not bound to particles "
+                             "(run ZSPartitionForZSParticles first)");
+  return p->ctx;
+}
+
+}  // namespace
+
+/// ConfigConstitutiveModel (Generation.cu:18-88)
+struct ConfigConstitutiveModel : INode {
+  void apply() override {
+    auto out = std::make_shared<ZenoConstitutiveModel>();
+    const float dx = get_input2<float>("dx");
+    out->dx = dx;
+    out->volume = dx * dx * dx / get_input2<float>("ppc");
+    out->density = get_input2<float>("density");
+    mpm_material &m = out->mat;
+    m.E = get_input2<float>("E");
+    m.nu = get_input2<float>("nu");
+    m.density = out->density;
+    m.friction_angle_deg = 35.0f;  // reference default (Generation.cu:70)
+    m.bulk = 1e4f;
+    m.gamma = 7.0f;
+    if (has_input<NumericObject>("friction_angle"))
+      m.friction_angle_deg = get_input<NumericObject>("friction_angle")->get<float>();
+    if (has_input<NumericObject>("bulk")) m.bulk = get_input<NumericObject>("bulk")->get<float>();
+    if (has_input<NumericObject>("gamma")) m.gamma = get_input<NumericObject>("gamma")->get<float>();
+    const std::string type = get_input2<std::string>("type");
+    if (type == "fcr")
+      m.type = MPM_FCR;
+    else if (type == "nhk")
+      m.type = MPM_NHK;
+    else if (type == "stvk")
+      m.type = MPM_STVK;
+    else if (type == "eos")
+      m.type = MPM_EOS;
+    else
+      throw std::runtime_error("unrecognized (isotropic) elastic model [" + type + "]");
+    if (get_input2<std::string>("aniso") != "none")
+      throw std::runtime_error("anisotropic models are not supported by this MPM backend");
+    const std::string plastic = get_input2<std::string>("plasticity");
+    if (plastic == "nadp") {
+      m.type = MPM_STVK;  // plasticity runs on StvkWithHencky (Generation.cu:66-70)
+      m.plasticity = MPM_PLASTIC_NADP;
+    } else if (plastic == "none") {
+      m.plasticity = MPM_PLASTIC_NONE;
+    } else {
+      throw std::runtime_error("plasticity [" + plastic + "] is not supported by this MPM backend");
+    }
+    set_output("ZSModel", out);
+  }
+};
+ZENDEFNODE(ConfigConstitutiveModel, {
+                                        {{"float", "dx", "0.1"},
+                                         {"float", "ppc", "8"},
+                                         {"float", "density", "1000"},
+                                         {"enum fcr nhk stvk snhk eos", "type", "fcr"},
+                                         {"enum none arap", "aniso", "none"},
+                                         {"enum none nadp navm nacc", "plasticity", "none"},
+                                         {"float", "E", "10000"},
+                                         {"float", "nu", "0.4"},
+                                         {"DictObject:NumericObject", "params"}},
+                                        {"ZSModel"},
+                                        {},
+                                        {"MPM"},
+                                    });
+
+/// ToZSParticles (Generation.cpp:690-1145): m = vol * density, F = I, C = 0.
+/// The device context is sized for the primitive: its block directory spans
+/// the optional domain_min / domain_max inputs, else the bounding box grown
+/// by its own extent (at least 8 blocks) on every side.
+struct ToZSParticles : INode {
+  void apply() override {
+    auto model = get_input<ZenoConstitutiveModel>("ZSModel");
+    auto prim = get_input<PrimitiveObject>("prim");
+    const auto &pos = prim->verts();
+    const int64_t n = (int64_t)pos.size();
+    auto out = std::make_shared<ZenoParticles>();
+    out->prim = prim;
+    out->model = model;
+    out->n = n;
+    out->category = get_input2<int>("category");
+    if (out->category != 0)
+      throw std::runtime_error("only mpm particles (category 0) are supported by this backend");
+
+    const float dx = model->dx;
+    float lo[3], hi[3];
+    if (has_input<NumericObject>("domain_min") && has_input<NumericObject>("domain_max")) {
+      auto a = get_input<NumericObject>("domain_min")->get<vec3f>();
+      auto b = get_input<NumericObject>("domain_max")->get<vec3f>();
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = a[d];
+        hi[d] = b[d];
+      }
+    } else {
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::numeric_limits<float>::max();
+        hi[d] = -std::numeric_limits<float>::max();
+      }
+      for (const auto &p : pos)
+        for (int d = 0; d < 3; ++d) {
+          lo[d] = std::min(lo[d], p[d]);
+          hi[d] = std::max(hi[d], p[d]);
+        }
+      if (n == 0)
+        for (int d = 0; d < 3; ++d) lo[d] = hi[d] = 0.0f;
+      for (int d = 0; d < 3; ++d) {
+        const float grow = std::max(hi[d] - lo[d], 32.0f * dx);
+        lo[d] -= grow;
+        hi[d] += grow;
+      }
+    }
+    mpm_ctx_desc desc{};
+    desc.device = 0;
+    desc.dx = dx;
+    for (int d = 0; d < 3; ++d) {
+      const int b0 = (int)std::floor(lo[d] / dx / 4.0f) - 1;
+      const int b1 = (int)std::floor(hi[d] / dx / 4.0f) + 2;
+      desc.block_lo[d] = b0;
+      desc.block_dims[d] = std::max(3, b1 - b0 + 1);
+    }
+    desc.max_particles = std::max<int64_t>(n, 1);
+    auto ctx = std::make_shared<MpmContext>();
+    ctx->dx = dx;
+    check(mpm_ctx_create(&desc, &ctx->h), "mpm_ctx_create");
+    check(mpm_set_materials(ctx->h, &model->mat, 1), "mpm_set_materials");
+
+    std::vector<float> x(3 * n), v(3 * n, 0.0f), m(n, model->volume * model->density),
+        vol(n, model->volume);
+    for (int64_t i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d) x[3 * i + d] = pos[i][d];
+    auto vel = prim->attrs3.find("vel");
+    if (vel != prim->attrs3.end() && (int64_t)vel->second.size() == n)
+      for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) v[3 * i + d] = vel->second[i][d];
+    check(mpm_particles_upload(ctx->h, n, x.data(), v.data(), nullptr, nullptr, nullptr, m.data(),
+                               vol.data(), nullptr, nullptr, nullptr),
+          "mpm_particles_upload");
+    out->ctx = ctx;
+    set_output("ZSParticles", out);
+  }
+};
+ZENDEFNODE(ToZSParticles, {
+                              {"ZSModel", "prim", {"int", "category", "0"}},
+                              {"ZSParticles"},
+                              {},
+                              {"MPM"},
+                          });
+
+/// MakeZSPartition (Generation.cu:1470-1477)
+struct MakeZSPartition : INode {
+  void apply() override { set_output("ZSPartition", std::make_shared<ZenoPartition>()); }
+};
+ZENDEFNODE(MakeZSPartition, {
+                                {},
+                                {"ZSPartition"},
+                                {},
+                                {"MPM"},
+                            });
+
+/// MakeZSGrid (Generation.cu:1486-1512)
+struct MakeZSGrid : INode {
+  void apply() override {
+    auto grid = std::make_shared<ZenoGrid>();
+    grid->dx = get_input2<float>("dx");
+    grid->transferScheme = get_input2<std::string>("transfer");
+    if (grid->transferScheme != "apic")
+      throw std::runtime_error("unrecognized transfer scheme [" + grid->transferScheme +
+                               "] (this backend implements apic)");
+    set_output("ZSGrid", grid);
+  }
+};
+ZENDEFNODE(MakeZSGrid, {
+                           {{"float", "dx", "0.1"}, {"string", "transfer", "apic"}},
+                           {"ZSGrid"},
+                           {},
+                           {"MPM"},
+                       });
+
+/// ZSPartitionForZSParticles (MPMPipeline.cu:21-112): bins the particles into
+/// 4^3 blocks with the 1-ring halo and sorts them by (block, cell).  Both
+/// strategies rebuild: a rebuild costs a few microseconds here.
+struct ZSPartitionForZSParticles : INode {
+  void apply() override {
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const std::string strategy = get_param<std::string>("strategy");
+    if (strategy != "force" && strategy != "cache")
+      throw std::runtime_error("unknown partition strategy [" + strategy + "]");
+    if (std::fabs(grid->dx - pars->ctx->dx) > 1e-6f * pars->ctx->dx)
+      throw std::runtime_error("ZSGrid dx differs from the dx of the particles' model");
+    table->ctx = pars->ctx;
+    grid->ctx = pars->ctx;
+    check(mpm_partition(pars->ctx->h), "mpm_partition");
+    table->rebuilt = true;
+    set_output("ZSPartition", table);
+  }
+};
+ZENDEFNODE(ZSPartitionForZSParticles, {
+                                          {"ZSPartition", "ZSGrid", "ZSParticles", {"float", "ppb", "1"}},
+                                          {"ZSPartition"},
+                                          {{"enum force cache", "strategy", "force"}},
+                                          {"MPM"},
+                                      });
+
+/// ExpandZSPartition (MPMPipeline.cu:121-231): the partition already holds
+/// the 1-ring of neighbour blocks every quadratic stencil needs, so this node
+/// only validates its parameters and passes the partition on.
+struct ExpandZSPartition : INode {
+  void apply() override {
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    (void)get_param<int>("offset");
+    (void)get_param<int>("extent");
+    set_output("ZSPartition", table);
+  }
+};
+ZENDEFNODE(ExpandZSPartition, {
+                                  {"ZSPartition"},
+                                  {"ZSPartition"},
+                                  {{"int", "offset", "0"}, {"int", "extent", "2"}},
+                                  {"MPM"},
+                              });
+
+/// ZSGridFromZSPartition (MPMPipeline.cu:241-267): size and clear the grid
+struct ZSGridFromZSPartition : INode {
+  void apply() override {
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    auto ctx = bound_ctx(table, "ZSGridFromZSPartition");
+    grid->ctx = ctx;
+    grid->partition = table;
+    check(mpm_grid_clear(ctx->h), "mpm_grid_clear");
+    set_output("ZSGrid", grid);
+  }
+};
+ZENDEFNODE(ZSGridFromZSPartition, {
+                                      {"ZSPartition", "ZSGrid"},
+                                      {"ZSGrid"},
+                                      {},
+                                      {"MPM"},
+                                  });
+
+/// ZSParticleToZSGrid (Transfer.cu:985-1060), APIC transfer
+struct ZSParticleToZSGrid : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    auto ctx = bound_ctx(table, "ZSParticleToZSGrid");
+    if (pars->ctx != ctx) throw std::runtime_error("ZSParticles and ZSPartition are not bound");
+    check(mpm_p2g(ctx->h, get_dt(*this)), "mpm_p2g");
+    set_output("ZSGrid", grid);
+  }
+};
+ZENDEFNODE(ZSParticleToZSGrid, {
+                                   {"ZSParticles", "ZSPartition", "ZSGrid", "dt"},
+                                   {"ZSGrid"},
+                                   {},
+                                   {"MPM"},
+                               });
+
+/// UpdateZSGrid (MPMPipeline.cu:828-940): v = mv / m + accel dt, MaxVelSqr
+struct UpdateZSGrid : INode {
+  void apply() override {
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    auto ctx = bound_ctx(table, "UpdateZSGrid");
+    float acc[3] = {0.0f, get_input2<float>("gravity"), 0.0f};
+    if (has_input("Accel")) {
+      auto a = get_input<NumericObject>("Accel")->get<vec3f>();
+      acc[0] = a[0];
+      acc[1] = a[1];
+      acc[2] = a[2];
+    }
+    check(mpm_set_gravity(ctx->h, acc[0], acc[1], acc[2]), "mpm_set_gravity");
+    float vmax = 0.0f;
+    check(mpm_grid_update(ctx->h, get_dt(*this), &vmax), "mpm_grid_update");
+    set_output("ZSGrid", grid);
+    set_output("MaxVelSqr", std::make_shared<NumericObject>(vmax));
+  }
+};
+ZENDEFNODE(UpdateZSGrid, {
+                             {{"float", "gravity", "-9.8"}, "ZSPartition", "ZSGrid", "dt", "Accel"},
+                             {"ZSGrid", "MaxVelSqr"},
+                             {},
+                             {"MPM"},
+                         });
+
+/// ToZSBoundary (Generation.cu:1597-1647).  The level-set collider input
+/// (ZSLevelSet) is replaced by the analytic walls of the domain box
+/// [domain_min, domain_max] (node indices from world coordinates / dx), of
+/// `thickness` cells; translation / rotation of the collider are not
+/// supported (the walls are static).
+struct ToZSBoundary : INode {
+  void apply() override {
+    if (has_input("ZSLevelSet"))
+      throw std::runtime_error("level-set colliders are not supported by this backend; "
+                               "use the analytic box walls (domain_min / domain_max)");
+    auto b = std::make_shared<ZenoBoundary>();
+    const std::string type = get_input2<std::string>("type");
+    if (type == "sticky" || type == "Sticky")
+      b->bc.type = MPM_BC_STICKY;
+    else if (type == "slip" || type == "Slip")
+      b->bc.type = MPM_BC_SLIP;
+    else if (type == "separate" || type == "Separate")
+      b->bc.type = MPM_BC_SEPARATE;
+    else
+      b->bc.type = MPM_BC_STICKY;  // the reference's fallback (Generation.cu:1611)
+    b->bc.thickness = get_input2<int>("thickness");
+    const float dx = get_input2<float>("dx");
+    vec3f lo{0.f, 0.f, 0.f}, hi{1.f, 1.f, 1.f};
+    if (has_input<NumericObject>("domain_min")) lo = get_input<NumericObject>("domain_min")->get<vec3f>();
+    if (has_input<NumericObject>("domain_max")) hi = get_input<NumericObject>("domain_max")->get<vec3f>();
+    for (int d = 0; d < 3; ++d) {
+      b->bc.lo[d] = (int)std::lround(lo[d] / dx);
+      b->bc.hi[d] = (int)std::lround(hi[d] / dx);
+    }
+    set_output("ZSBoundary", b);
+  }
+};
+ZENDEFNODE(ToZSBoundary, {
+                             {"ZSLevelSet",
+                              "translation",
+                              "translation_rate",
+                              "scale",
+                              "scale_rate",
+                              "ypr_angles",
+                              {"string", "type", "sticky"},
+                              {"float", "dx", "0.1"},
+                              {"int", "thickness", "3"},
+                              "domain_min",
+                              "domain_max"},
+                             {"ZSBoundary"},
+                             {},
+                             {"MPM"},
+                         });
+
+/// ApplyBoundaryOnZSGrid (Boundary.cu:83-163)
+struct ApplyBoundaryOnZSGrid : INode {
+  void apply() override {
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    if (has_input<ZenoBoundary>("ZSBoundary")) {
+      auto table = get_input<ZenoPartition>("ZSPartition");
+      auto ctx = bound_ctx(table, "ApplyBoundaryOnZSGrid");
+      auto b = get_input<ZenoBoundary>("ZSBoundary");
+      check(mpm_set_boundary(ctx->h, &b->bc), "mpm_set_boundary");
+      check(mpm_apply_boundary(ctx->h), "mpm_apply_boundary");
+    }
+    set_output("ZSGrid", grid);
+  }
+};
+ZENDEFNODE(ApplyBoundaryOnZSGrid, {
+                                      {"ZSPartition", "ZSGrid", "ZSBoundary"},
+                                      {"ZSGrid"},
+                                      {},
+                                      {"MPM"},
+                                  });
+
+/// ZSGridToZSParticle (Transfer.cu:1069-1173), APIC transfer
+struct ZSGridToZSParticle : INode {
+  void apply() override {
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    auto ctx = bound_ctx(table, "ZSGridToZSParticle");
+    if (pars->ctx != ctx) throw std::runtime_error("ZSParticles and ZSPartition are not bound");
+    (void)grid;
+    check(mpm_g2p(ctx->h, get_dt(*this)), "mpm_g2p");
+    table->rebuilt = false;
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(ZSGridToZSParticle, {
+                                   {"ZSGrid", "ZSPartition", "ZSParticles", "dt"},
+                                   {"ZSParticles"},
+                                   {},
+                                   {"MPM"},
+                               });
+
+/// ZSReturnMapping (MPMPipeline.cu:953-1138): Drucker-Prager projection
+struct ZSReturnMapping : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    check(mpm_return_mapping(pars->ctx->h), "mpm_return_mapping");
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(ZSReturnMapping, {
+                                {"ZSParticles"},
+                                {"ZSParticles"},
+                                {},
+                                {"MPM"},
+                            });
+
+/// AdjustParticleMaterial (Temp.cu:16-56): per-particle E, nu blended along
+/// one axis between (end_soft, E_soft, nu_soft) and (end_hard, E_hard, nu_hard)
+struct AdjustParticleMaterial : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const float Eh = get_input2<float>("E_hard"), Es = get_input2<float>("E_soft");
+    const float nh = get_input2<float>("nu_hard"), ns = get_input2<float>("nu_soft");
+    const float eh = get_input2<float>("end_hard"), es = get_input2<float>("end_soft");
+    const std::string orient = get_param<std::string>("orientation");
+    const int d = orient == "x" ? 0 : (orient == "y" ? 1 : 2);
+    const int64_t n = pars->n;
+    std::vector<float> x(3 * n), mu(n), lam(n);
+    check(mpm_particles_download(pars->ctx->h, x.data(), nullptr, nullptr, nullptr, nullptr),
+          "mpm_particles_download");
+    const float span = eh - es;
+    for (int64_t i = 0; i < n; ++i) {
+      const float ratio = std::min(1.0f, std::max(0.0f, (eh - x[3 * i + d]) / span));
+      const float E = Es * ratio + Eh * (1.0f - ratio);
+      const float nu = ns * ratio + nh * (1.0f - ratio);
+      mu[i] = E / (2.0f * (1.0f + nu));
+      lam[i] = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+    }
+    check(mpm_particles_set_lame(pars->ctx->h, mu.data(), lam.data()), "mpm_particles_set_lame");
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(AdjustParticleMaterial, {
+                                       {"ZSParticles",
+                                        {"float", "E_hard", "100"},
+                                        {"float", "E_soft", "50"},
+                                        {"float", "nu_hard", "0.4"},
+                                        {"float", "nu_soft", "0.2"},
+                                        {"float", "end_hard", "1"},
+                                        {"float", "end_soft", "-0.5"}},
+                                       {"ZSParticles"},
+                                       {{"enum x y z", "orientation", "y"}},
+                                       {"MPM"},
+                                   });
+
+/// UpdatePrimitiveFromZSParticles (Generation.cu:1088-1158): x, v back into
+/// the source primitive ("pos", "vel")
+struct UpdatePrimitiveFromZSParticles : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    if (pars->prim) {
+      const int64_t n = pars->n;
+      std::vector<float> x(3 * n), v(3 * n);
+      check(mpm_particles_download(pars->ctx->h, x.data(), v.data(), nullptr, nullptr, nullptr),
+            "mpm_particles_download");
+      auto &pos = pars->prim->verts();
+      auto &vel = pars->prim->attrs3["vel"];
+      pos.resize(n);
+      vel.resize(n);
+      for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+          pos[i][d] = x[3 * i + d];
+          vel[i][d] = v[3 * i + d];
+        }
+    }
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(UpdatePrimitiveFromZSParticles, {
+                                               {"ZSParticles"},
+                                               {"ZSParticles"},
+                                               {},
+                                               {"MPM"},
+                                           });
+
+/// ZSParticlesToPrimitiveObject (Generation.cu:1744-1833): a new primitive
+/// with "pos" and "vel"
+struct ZSParticlesToPrimitiveObject : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const int64_t n = pars->n;
+    std::vector<float> x(3 * n), v(3 * n);
+    check(mpm_particles_download(pars->ctx->h, x.data(), v.data(), nullptr, nullptr, nullptr),
+          "mpm_particles_download");
+    auto prim = std::make_shared<PrimitiveObject>();
+    auto &pos = prim->verts();
+    auto &vel = prim->attrs3["vel"];
+    pos.resize(n);
+    vel.resize(n);
+    for (int64_t i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d) {
+        pos[i][d] = x[3 * i + d];
+        vel[i][d] = v[3 * i + d];
+      }
+    set_output("prim", prim);
+  }
+};
+ZENDEFNODE(ZSParticlesToPrimitiveObject, {
+                                             {"ZSParticles"},
+                                             {"prim"},
+                                             {},
+                                             {"MPM"},
+                                         });
+
+/// ZSMPMSubstep (new, additive): partition, grid, P2G, grid update +
+/// boundary, G2P + return mapping for `substeps` substeps on the device in
+/// one call (CUDA-graph replay, no host synchronisation between substeps).
+struct ZSMPMSubstep : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    auto ctx = pars->ctx;
+    float acc[3] = {0.0f, get_input2<float>("gravity"), 0.0f};
+    if (has_input("Accel")) {
+      auto a = get_input<NumericObject>("Accel")->get<vec3f>();
+      acc[0] = a[0];
+      acc[1] = a[1];
+      acc[2] = a[2];
+    }
+    check(mpm_set_gravity(ctx->h, acc[0], acc[1], acc[2]), "mpm_set_gravity");
+    if (has_input<ZenoBoundary>("ZSBoundary"))
+      check(mpm_set_boundary(ctx->h, &get_input<ZenoBoundary>("ZSBoundary")->bc),
+            "mpm_set_boundary");
+    check(mpm_substep(ctx->h, get_dt(*this), get_input2<int>("substeps")), "mpm_substep");
+    mpm_stats st{};
+    check(mpm_get_stats(ctx->h, &st), "mpm_get_stats");
+    check(st.status, "substep");
+    set_output("ZSParticles", pars);
+    set_output("MaxVelSqr", std::make_shared<NumericObject>(st.max_vel_sqr));
+  }
+};
+ZENDEFNODE(ZSMPMSubstep, {
+                             {"ZSParticles",
+                              "ZSBoundary",
+                              "dt",
+                              {"float", "gravity", "-9.8"},
+                              "Accel",
+                              {"int", "substeps", "1"}},
+                             {"ZSParticles", "MaxVelSqr"},
+                             {},
+                             {"MPM"},
+                         });
+
+}  // namespace zeno

@@ -1,0 +1,186 @@
+// Test entry points of the node layer (libzsmpm_nodes.so):
+//  * the registered node descriptors as JSON, to check names, sockets and
+//    defaults against the reference's ZENDEFNODE declarations;
+//  * one headless run of the reference substep graph built from those nodes
+//    with Graph::addNode / setNodeInput / bindNodeInput / applyNodes, the
+//    way a zeno graph wires them (the loop body is re-applied per substep,
+//    the setup nodes are evaluated once).
+#include <zsmpm.h>
+
+#include <cstdint>
+#include <cstring>
+#include <sstream>
+#include <string>
+
+#include "zeno_api.hpp"
+
+namespace {
+
+std::string esc(const std::string &s) {
+  std::string o;
+  for (char c : s) {
+    if (c == '"' || c == '\\') o += '\\';
+    o += c;
+  }
+  return o;
+}
+
+void sockets(std::ostringstream &os, const std::vector<zeno::SocketDescriptor> &v) {
+  os << "[";
+  for (size_t i = 0; i < v.size(); ++i) {
+    if (i) os << ",";
+    os << "[\"" << esc(v[i].type) << "\",\"" << esc(v[i].name) << "\",\"" << esc(v[i].defl)
+       << "\"]";
+  }
+  os << "]";
+}
+
+int32_t copy_out(const std::string &s, char *buf, int64_t cap) {
+  if (!buf || cap <= 0) return -1;
+  const size_t n = std::min<size_t>(s.size(), (size_t)cap - 1);
+  std::memcpy(buf, s.data(), n);
+  buf[n] = 0;
+  return (int32_t)s.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+// JSON object {node name: {inputs, outputs, params, categories}}; returns the
+// full length (the buffer holds cap - 1 characters at most).
+int32_t zsn_descriptors_json(char *buf, int64_t cap) {
+  std::ostringstream os;
+  os << "{";
+  bool first = true;
+  for (const auto &[name, cls] : zeno::node_registry()) {
+    if (!first) os << ",";
+    first = false;
+    os << "\"" << esc(name) << "\":{\"inputs\":";
+    sockets(os, cls.desc.inputs);
+    os << ",\"outputs\":";
+    sockets(os, cls.desc.outputs);
+    os << ",\"params\":";
+    sockets(os, cls.desc.params);
+    os << ",\"categories\":[";
+    for (size_t i = 0; i < cls.desc.categories.size(); ++i)
+      os << (i ? "," : "") << "\"" << esc(cls.desc.categories[i]) << "\"";
+    os << "]}";
+  }
+  os << "}";
+  return copy_out(os.str(), buf, cap);
+}
+
+// Runs `substeps` substeps of one particle set through the node graph
+// (fused = 0: the reference's node sequence per substep; fused = 1: one
+// ZSMPMSubstep node) and returns x, v (n x 3) and the last MaxVelSqr.
+int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *vel, float dx,
+                      const char *type, const char *plasticity, float E, float nu,
+                      float density, float ppc, const char *bc_type, int32_t bc_thickness,
+                      float dt, float gravity, int32_t substeps, float *out_x, float *out_v,
+                      float *out_max_vel_sqr, char *err, int64_t err_cap) {
+  using namespace zeno;
+  try {
+    Graph g;
+    auto num = [](float v) { return std::make_shared<NumericObject>(v); };
+    auto inum = [](int v) { return std::make_shared<NumericObject>(v); };
+    auto str = [](const char *v) { return std::make_shared<StringObject>(v); };
+    auto prim = std::make_shared<PrimitiveObject>();
+    auto &p = prim->verts();
+    auto &pv = prim->attrs3["vel"];
+    p.resize(n);
+    pv.resize(n);
+    for (int64_t i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d) {
+        p[i][d] = pos[3 * i + d];
+        pv[i][d] = vel ? vel[3 * i + d] : 0.0f;
+      }
+
+    g.addNode("ConfigConstitutiveModel", "model");
+    g.setNodeInput("model", "dx", num(dx));
+    g.setNodeInput("model", "ppc", num(ppc));
+    g.setNodeInput("model", "density", num(density));
+    g.setNodeInput("model", "type", str(type));
+    g.setNodeInput("model", "plasticity", str(plasticity));
+    g.setNodeInput("model", "E", num(E));
+    g.setNodeInput("model", "nu", num(nu));
+    g.addNode("ToZSParticles", "pars");
+    g.bindNodeInput("pars", "ZSModel", "model", "ZSModel");
+    g.setNodeInput("pars", "prim", prim);
+    g.addNode("MakeZSPartition", "table");
+    g.addNode("MakeZSGrid", "grid");
+    g.setNodeInput("grid", "dx", num(dx));
+    g.addNode("ToZSBoundary", "bnd");
+    g.setNodeInput("bnd", "type", str(bc_type));
+    g.setNodeInput("bnd", "dx", num(dx));
+    g.setNodeInput("bnd", "thickness", inum(bc_thickness));
+    for (const char *id : {"model", "pars", "table", "grid", "bnd"}) g.markOnce(id);
+    auto dtobj = num(dt);
+    std::string last;
+    if (fused) {
+      g.addNode("ZSMPMSubstep", "step");
+      g.bindNodeInput("step", "ZSParticles", "pars", "ZSParticles");
+      g.bindNodeInput("step", "ZSBoundary", "bnd", "ZSBoundary");
+      g.setNodeInput("step", "dt", dtobj);
+      g.setNodeInput("step", "gravity", num(gravity));
+      g.setNodeInput("step", "substeps", inum(substeps));
+      g.applyNodes({"step"});
+      last = "step";
+    } else {
+      g.addNode("ZSPartitionForZSParticles", "part");
+      g.bindNodeInput("part", "ZSPartition", "table", "ZSPartition");
+      g.bindNodeInput("part", "ZSGrid", "grid", "ZSGrid");
+      g.bindNodeInput("part", "ZSParticles", "pars", "ZSParticles");
+      g.addNode("ExpandZSPartition", "expand");
+      g.bindNodeInput("expand", "ZSPartition", "part", "ZSPartition");
+      g.addNode("ZSGridFromZSPartition", "clear");
+      g.bindNodeInput("clear", "ZSPartition", "expand", "ZSPartition");
+      g.bindNodeInput("clear", "ZSGrid", "grid", "ZSGrid");
+      g.addNode("ZSParticleToZSGrid", "p2g");
+      g.bindNodeInput("p2g", "ZSParticles", "pars", "ZSParticles");
+      g.bindNodeInput("p2g", "ZSPartition", "expand", "ZSPartition");
+      g.bindNodeInput("p2g", "ZSGrid", "clear", "ZSGrid");
+      g.setNodeInput("p2g", "dt", dtobj);
+      g.addNode("UpdateZSGrid", "update");
+      g.bindNodeInput("update", "ZSPartition", "expand", "ZSPartition");
+      g.bindNodeInput("update", "ZSGrid", "p2g", "ZSGrid");
+      g.setNodeInput("update", "dt", dtobj);
+      g.setNodeInput("update", "gravity", num(gravity));
+      g.addNode("ApplyBoundaryOnZSGrid", "bc");
+      g.bindNodeInput("bc", "ZSPartition", "expand", "ZSPartition");
+      g.bindNodeInput("bc", "ZSGrid", "update", "ZSGrid");
+      g.bindNodeInput("bc", "ZSBoundary", "bnd", "ZSBoundary");
+      g.addNode("ZSGridToZSParticle", "g2p");
+      g.bindNodeInput("g2p", "ZSGrid", "bc", "ZSGrid");
+      g.bindNodeInput("g2p", "ZSPartition", "expand", "ZSPartition");
+      g.bindNodeInput("g2p", "ZSParticles", "pars", "ZSParticles");
+      g.setNodeInput("g2p", "dt", dtobj);
+      g.addNode("ZSReturnMapping", "rm");
+      g.bindNodeInput("rm", "ZSParticles", "g2p", "ZSParticles");
+      for (int32_t k = 0; k < substeps; ++k) g.applyNodes({"rm"});
+      last = "rm";
+      if (out_max_vel_sqr && substeps > 0)
+        *out_max_vel_sqr =
+            std::dynamic_pointer_cast<NumericObject>(g.getNodeOutput("update", "MaxVelSqr"))
+                ->get<float>();
+    }
+    if (fused && out_max_vel_sqr)
+      *out_max_vel_sqr =
+          std::dynamic_pointer_cast<NumericObject>(g.getNodeOutput("step", "MaxVelSqr"))
+              ->get<float>();
+    g.addNode("UpdatePrimitiveFromZSParticles", "out");
+    g.setNodeInput("out", "ZSParticles", g.getNodeOutput(last, "ZSParticles"));
+    g.applyNodes({"out"});
+    for (int64_t i = 0; i < n; ++i)
+      for (int d = 0; d < 3; ++d) {
+        out_x[3 * i + d] = p[i][d];
+        out_v[3 * i + d] = pv[i][d];
+      }
+    return 0;
+  } catch (const std::exception &e) {
+    copy_out(e.what(), err, err_cap);
+    return 1;
+  }
+}
+
+}  // extern "C"

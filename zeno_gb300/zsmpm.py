@@ -53,12 +53,12 @@ class Stats(C.Structure):
 
 EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destroy",
            "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
-           "mpm_particles_upload", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
+           "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download"]
 
-STAGES = ["reset", "bin", "scan", "scatter", "sort", "clear", "p2g", "grid_update", "g2p"]
+STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 
 _lib = None
 
@@ -84,6 +84,7 @@ def load(path: str = LIB_PATH):
         "mpm_set_boundary": ([P, C.POINTER(Boundary)], i32),
         "mpm_set_gravity": ([P, f32, f32, f32], i32),
         "mpm_particles_upload": ([P, i64] + [P] * 10, i32),
+        "mpm_particles_set_lame": ([P, P, P], i32),
         "mpm_particles_download": ([P] + [P] * 5, i32),
         "mpm_partition": ([P], i32),
         "mpm_grid_clear": ([P], i32),
@@ -201,6 +202,13 @@ class Context:
                     "mpm_particles_upload")
         self.n = n
 
+    def set_lame(self, mu, lam):
+        """AdjustParticleMaterial: per-particle mu / lam in upload order."""
+        mu = _f32(mu, (self.n,))
+        lam = _f32(lam, (self.n,))
+        self._check(self._L.mpm_particles_set_lame(self.h, _p(mu), _p(lam)),
+                    "mpm_particles_set_lame")
+
     def download(self, channels=("x", "v", "C", "F", "J")) -> dict:
         n = self.n
         out = {}
@@ -292,3 +300,63 @@ class Context:
         out = np.zeros((max(ng, 1), 64, 4), np.float32)
         self._check(self._L.mpm_grid_download(self.h, _p(out), out.size), "mpm_grid_download")
         return out[:ng]
+
+
+# ---------------------------------------------------------------------------
+# the C++ node layer (libzsmpm_nodes.so): zeno's MPM nodes over this ABI
+
+NODES_LIB_PATH = os.path.join(PKG, "libzsmpm_nodes.so")
+_nodes = None
+
+
+def load_nodes(path: str = NODES_LIB_PATH):
+    global _nodes
+    if _nodes is not None:
+        return _nodes
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    L.zsn_descriptors_json.argtypes = [C.c_char_p, C.c_int64]
+    L.zsn_descriptors_json.restype = C.c_int32
+    P = C.c_void_p
+    L.zsn_run_graph.argtypes = [C.c_int32, C.c_int64, P, P, C.c_float, C.c_char_p, C.c_char_p,
+                                C.c_float, C.c_float, C.c_float, C.c_float, C.c_char_p,
+                                C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
+                                C.c_char_p, C.c_int64]
+    L.zsn_run_graph.restype = C.c_int32
+    _nodes = L
+    return L
+
+
+def node_descriptors() -> dict:
+    import json
+    L = load_nodes()
+    n = L.zsn_descriptors_json(None, 0)
+    cap = 1 << 16
+    while True:
+        buf = C.create_string_buffer(cap)
+        n = L.zsn_descriptors_json(buf, cap)
+        if n < cap:
+            return json.loads(buf.value.decode())
+        cap = 2 * n
+
+
+def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
+                   ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
+                   fused=False):
+    """Run the zeno MPM substep graph headless through the C++ node layer."""
+    L = load_nodes()
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
+    v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
+    n = x.shape[0]
+    ox = np.zeros_like(x)
+    ov = np.zeros_like(x)
+    vmax = np.zeros(1, np.float32)
+    err = C.create_string_buffer(1024)
+    rc = L.zsn_run_graph(1 if fused else 0, n, _p(x), _p(v), dx, type.encode(),
+                         plasticity.encode(), E, nu, density, ppc, bc.encode(), thickness, dt,
+                         gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024)
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return ox, ov, float(vmax[0])
