@@ -7,7 +7,7 @@ dx = 1/256 (fixed-corotated E=1e5, Neo-Hookean E=5e4, Drucker-Prager sand
 slip walls 3 cells thick; dt = 1e-4).  One step = one full substep
 (partition + sort, grid clear, P2G, grid update + boundary, G2P + return
 mapping) of every particle, replayed as a CUDA graph.  The particle state
-(2 x 243 MB double buffer) is larger than L2, so no flush is needed between
+(2 x 294 MB double buffer) is larger than L2, so no flush is needed between
 steps.
 
 Arms:
@@ -351,7 +351,8 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "particles": parts.n, "dx": "1/256", "dt": dt,
                    "form": "plain", "particle_blocks": st["n_particle_blocks"],
                    "grid_blocks": st["n_grid_blocks"],
-                   "l2": "inputs larger than L2 (2 x 243 MB particle buffers)",
+                   "l2": f"inputs larger than L2 (2 x {parts.n * 35 * 4 / 1e6:.0f} MB particle "
+                         "buffers, 126 MB L2): no flush needed",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

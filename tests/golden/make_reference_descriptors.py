@@ -11,7 +11,8 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF_DEFAULT = "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else REF_DEFAULT
 FILES = ["projects/CuLagrange/mpm/Generation.cu", "projects/CuLagrange/mpm/Generation.cpp",
          "projects/CuLagrange/mpm/MPMPipeline.cu", "projects/CuLagrange/mpm/Transfer.cu",
          "projects/CuLagrange/mpm/Boundary.cu", "projects/CuLagrange/mpm/Temp.cu"]

@@ -53,3 +53,21 @@ def test_sockets_match_reference(descriptors, reference, kind):
 def test_fused_substep_node_registered(descriptors):
     d = descriptors["ZSMPMSubstep"]
     assert [s[1] for s in d["outputs"]] == ["ZSParticles", "MaxVelSqr"]
+
+
+def test_node_file_compiles_against_zeno_headers():
+    """The same MPMNodes.cpp compiles against zeno's own node API headers
+    (inside zeno, ZSMPM_WITH_ZENO selects them instead of the mirror)."""
+    import shutil
+    import subprocess
+    from .golden.make_reference_descriptors import REF_DEFAULT
+    zeno_inc = os.environ.get("ZENO_INCLUDE", os.path.join(REF_DEFAULT, "zeno", "include"))
+    if not os.path.isdir(zeno_inc):
+        pytest.skip("zeno headers not present")
+    root = os.path.dirname(HERE)
+    cxx = shutil.which("g++") or "g++"
+    r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-DZSMPM_WITH_ZENO", "-I", zeno_inc,
+                        "-I", os.path.join(root, "include"),
+                        os.path.join(root, "zeno_gb300", "nodes", "MPMNodes.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]

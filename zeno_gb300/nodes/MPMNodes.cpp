@@ -11,10 +11,46 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
+#ifdef ZSMPM_WITH_ZENO
+// inside zeno: the real node API (projects/CuLagrange/CMakeLists.txt adds
+// this file to the zeno target)
+#include <zeno/types/NumericObject.h>
+#include <zeno/types/PrimitiveObject.h>
+#include <zeno/types/StringObject.h>
+#include <zeno/zeno.h>
+namespace zeno {
+namespace prim_access {
+inline std::vector<vec3f> &pos(PrimitiveObject &p) { return p.verts.values; }
+inline std::vector<vec3f> *vel(PrimitiveObject &p, bool create) {
+  if (!p.verts.has_attr("vel")) {
+    if (!create) return nullptr;
+    p.verts.add_attr<vec3f>("vel");
+  }
+  return &p.verts.attr<vec3f>("vel");
+}
+}  // namespace prim_access
+}  // namespace zeno
+#else
+// headless: the mirror of the node API
 #include "zeno_api.hpp"
+namespace zeno {
+namespace prim_access {
+inline std::vector<vec3f> &pos(PrimitiveObject &p) { return p.verts(); }
+inline std::vector<vec3f> *vel(PrimitiveObject &p, bool create) {
+  auto it = p.attrs3.find("vel");
+  if (it == p.attrs3.end()) {
+    if (!create) return nullptr;
+    return &p.attrs3["vel"];
+  }
+  return &it->second;
+}
+}  // namespace prim_access
+}  // namespace zeno
+#endif
 
 namespace zeno {
 
@@ -155,7 +191,7 @@ struct ToZSParticles : INode {
   void apply() override {
     auto model = get_input<ZenoConstitutiveModel>("ZSModel");
     auto prim = get_input<PrimitiveObject>("prim");
-    const auto &pos = prim->verts();
+    const auto &pos = prim_access::pos(*prim);
     const int64_t n = (int64_t)pos.size();
     auto out = std::make_shared<ZenoParticles>();
     out->prim = prim;
@@ -211,10 +247,9 @@ struct ToZSParticles : INode {
         vol(n, model->volume);
     for (int64_t i = 0; i < n; ++i)
       for (int d = 0; d < 3; ++d) x[3 * i + d] = pos[i][d];
-    auto vel = prim->attrs3.find("vel");
-    if (vel != prim->attrs3.end() && (int64_t)vel->second.size() == n)
+    if (auto *vel = prim_access::vel(*prim, false); vel && (int64_t)vel->size() == n)
       for (int64_t i = 0; i < n; ++i)
-        for (int d = 0; d < 3; ++d) v[3 * i + d] = vel->second[i][d];
+        for (int d = 0; d < 3; ++d) v[3 * i + d] = (*vel)[i][d];
     check(mpm_particles_upload(ctx->h, n, x.data(), v.data(), nullptr, nullptr, nullptr, m.data(),
                                vol.data(), nullptr, nullptr, nullptr),
           "mpm_particles_upload");
@@ -524,9 +559,9 @@ struct UpdatePrimitiveFromZSParticles : INode {
       std::vector<float> x(3 * n), v(3 * n);
       check(mpm_particles_download(pars->ctx->h, x.data(), v.data(), nullptr, nullptr, nullptr),
             "mpm_particles_download");
-      auto &pos = pars->prim->verts();
-      auto &vel = pars->prim->attrs3["vel"];
-      pos.resize(n);
+      auto &pos = prim_access::pos(*pars->prim);
+      if ((int64_t)pos.size() != n) pos.resize(n);
+      auto &vel = *prim_access::vel(*pars->prim, true);
       vel.resize(n);
       for (int64_t i = 0; i < n; ++i)
         for (int d = 0; d < 3; ++d) {
@@ -554,9 +589,9 @@ struct ZSParticlesToPrimitiveObject : INode {
     check(mpm_particles_download(pars->ctx->h, x.data(), v.data(), nullptr, nullptr, nullptr),
           "mpm_particles_download");
     auto prim = std::make_shared<PrimitiveObject>();
-    auto &pos = prim->verts();
-    auto &vel = prim->attrs3["vel"];
+    auto &pos = prim_access::pos(*prim);
     pos.resize(n);
+    auto &vel = *prim_access::vel(*prim, true);
     vel.resize(n);
     for (int64_t i = 0; i < n; ++i)
       for (int d = 0; d < 3; ++d) {
