@@ -184,6 +184,33 @@ int32_t mpm_partition_download(mpm_ctx *ctx, int32_t *n_pb, int32_t *pb_dir, int
 /* Grid nodes of the last partition: n_grid_blocks x 64 x (m, v0, v1, v2). */
 int32_t mpm_grid_download(mpm_ctx *ctx, float *nodes, int64_t cap_floats);
 
+/* Partition without device allocation.  No counterpart in the reference:
+ * it serves callers that cannot call cudaMalloc -- hosts that own all device
+ * memory through their own allocator or a fixed budget (an engine or
+ * renderer plugin, a framework whose caching allocator a stray cudaMalloc
+ * would fragment), or code in a real-time loop where cudaMalloc / cudaFree
+ * would synchronise the device.  It bins n particles into 4^3 blocks of the
+ * block directory (dx, block_lo, block_dims) and sorts them by
+ * (block, cell, index), exactly like mpm_partition.
+ *   x_planes  device, 3 * n floats: all x, then all y, then all z
+ *   perm      device, n ints: sorted position -> particle index
+ *   pb_dir, pb_count  device, cap_pb ints: directory index and particle
+ *             count of each non-empty block, in sorted order
+ *   n_pb      host: number of non-empty blocks
+ *   stream    cudaStream_t (NULL: the default stream); the call waits for it.
+ * Its scratch is one file-scope device array of 32 MiB that every GPU loading
+ * the library holds until the process exits; sizes above
+ * ZSMPM_NOALLOC_MAX_PARTICLES particles or ZSMPM_NOALLOC_MAX_BLOCKS directory
+ * blocks are rejected with MPM_ERR_CAPACITY.  The first call on a device sets
+ * up that device's scratch address (make it before any stream capture).
+ * Calls share the scratch: calls that overlap on the GPU race. */
+#define ZSMPM_NOALLOC_MAX_PARTICLES (1 << 20)
+#define ZSMPM_NOALLOC_MAX_BLOCKS (1 << 19)
+int32_t mpm_partition_noalloc(const float *x_planes, int64_t n, float dx,
+                              const int32_t block_lo[3], const int32_t block_dims[3],
+                              int32_t *perm, int32_t *pb_dir, int32_t *pb_count,
+                              int64_t cap_pb, int32_t *n_pb, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

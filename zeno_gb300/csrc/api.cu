@@ -38,6 +38,8 @@ int32_t fail(int32_t code, const std::string &msg) {
 
 }  // namespace
 
+void zsmpm::set_last_error(const std::string &msg) { g_last_error = msg; }
+
 struct mpm_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 #include "../../include/zsmpm.h"
 
@@ -130,6 +131,9 @@ void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream
 void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s);
 // vol * Kirchhoff stress of every particle from its current F (or J)
 void launch_stress(const DevPtrs &d, int cur, cudaStream_t s);
+
+// api.cu: the text mpm_last_error() returns on this thread
+void set_last_error(const std::string &msg);
 
 // io.cu
 struct IngestSrc {

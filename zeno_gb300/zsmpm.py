@@ -56,7 +56,7 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
-           "mpm_grid_download"]
+           "mpm_grid_download", "mpm_partition_noalloc"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 
@@ -99,6 +99,7 @@ def load(path: str = LIB_PATH):
         "mpm_get_stats": ([P, C.POINTER(Stats)], i32),
         "mpm_partition_download": ([P, P, P, P, i64, P, P, P, i64], i32),
         "mpm_grid_download": ([P, P, i64], i32),
+        "mpm_partition_noalloc": ([P, i64, f32, P, P, P, P, P, i64, P, P], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
