@@ -157,6 +157,60 @@ def ncu_traffic():
     return {}
 
 
+def batched_form(zsmpm, steps: int, dev: int):
+    """The batched form: 256 independent scenes (log-uniform counts in
+    [2,048, 200,000], seed 1, dx = 1/128, four materials) in one context, one
+    persistent launch per stage, against the same scenes advanced one after
+    another by the plain path (one context each)."""
+    import torch
+    from zeno_gb300 import scenes
+    pairs = scenes.batched_workload()
+    scns, mats, parts, offs = zsmpm.concat_scenes(pairs)
+    dt = pairs[0][0].dt
+    stream = torch.cuda.current_stream()
+    ctx = zsmpm.BatchContext(scns, mats, max_particles=parts.n, device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_batch(parts, offs)
+    ctx.substep(dt, 5)
+    ctx.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.substep(dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_b = e0.elapsed_time(e1)
+    ctx.sync()
+    st = ctx.stats()
+    ctx.close()
+    # the same scenes, each on its own plain context, one after another
+    ctxs = []
+    for scene, p in pairs:
+        c = zsmpm.Context(scene, max_particles=max(p.n, 1), device=dev)
+        c.set_stream(stream.cuda_stream)
+        c.upload(p)
+        c.substep(dt, 5)
+        ctxs.append(c)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for c in ctxs:
+        c.substep(dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_p = e0.elapsed_time(e1)
+    for c in ctxs:
+        c.sync()
+        c.close()
+    n = parts.n
+    return {"workload": f"{len(pairs)} scenes, {n:,} particles (log-uniform 2,048-200,000 per "
+                        "scene, seed 1), dx=1/128 each, four materials, slip walls",
+            "value": n * steps / (ms_b * 1e-3), "unit": METRIC, "steps": steps,
+            "ms_per_step": ms_b / steps, "status": st["status"],
+            "plain_sequential": n * steps / (ms_p * 1e-3),
+            "speedup_over_plain": ms_p / ms_b,
+            "kernel_launches_per_step": KERNELS_PER_SUBSTEP}
+
+
 def cpu_baseline(parts, scene, target_s: float = 10.0):
     """FP32 OpenMP restatement (oracle/) on all host cores, bounded sample."""
     from oracle import oracle
@@ -336,6 +390,9 @@ def run_gpu(args):
     d2h = ox.nbytes + ov.nbytes
     ctx.close()
 
+    forms = {}
+    if not args.no_forms:
+        forms["batched"] = batched_form(zsmpm, max(10, min(args.steps, 100)), dev)
     if rank != 0:
         if pg:
             pg.barrier()
@@ -370,6 +427,7 @@ def run_gpu(args):
         "clocks": clocks,
         "gpu_launches": KERNELS_PER_SUBSTEP * args.steps,
         "status": st["status"],
+        "forms": forms,
     }
     print(json.dumps(line))
     if pg:
@@ -385,6 +443,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched / differentiable forms reported beside the headline")
     ap.add_argument("--quick", action="store_true",
                     help="device timing only (no clock sampling, e2e or CPU legs): for ncu")
     args = ap.parse_args()

@@ -93,6 +93,19 @@ typedef struct mpm_ctx_desc {
   int32_t flags;           /* reserved, 0 */
 } mpm_ctx_desc;
 
+/* One scene of a batched context: many independent scenes (each its own
+ * grid spacing, block directory, boundary and gravity) advanced together,
+ * every stage one persistent launch over the blocks of all scenes.  The
+ * reference has no batching; a scene is what one ZSGrid + ZSPartition +
+ * ZSParticles triple holds there. */
+typedef struct mpm_scene_desc {
+  float dx;
+  int32_t block_lo[3];
+  int32_t block_dims[3];
+  float gravity[3];
+  mpm_boundary boundary;
+} mpm_scene_desc;
+
 typedef struct mpm_stats {
   int64_t n_particles;
   int32_t n_particle_blocks; /* non-empty 4^3 particle blocks of the last partition */
@@ -112,6 +125,10 @@ const char *mpm_last_error(void);
 
 int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out);
 int32_t mpm_ctx_destroy(mpm_ctx *ctx);
+/* A context of n_scenes independent scenes (mpm_set_boundary and
+ * mpm_set_gravity then apply to every scene). */
+int32_t mpm_batch_create(int32_t device, const mpm_scene_desc *scenes, int32_t n_scenes,
+                         int64_t max_particles, int32_t max_grid_blocks, mpm_ctx **out);
 
 /* Order the context's work after / before other work on `stream`
  * (a cudaStream_t; NULL restores the context's own stream). */
@@ -132,6 +149,13 @@ int32_t mpm_particles_upload(mpm_ctx *ctx, int64_t n, const float *x, const floa
                              const float *C, const float *F, const float *J,
                              const float *m, const float *vol, const int32_t *mat,
                              const float *mu, const float *lam);
+/* Upload of all scenes of a batched context: scene s owns particles
+ * [scene_offsets[s], scene_offsets[s+1]) of the arrays (n_scenes + 1 offsets,
+ * from 0 to n); arrays as in mpm_particles_upload. */
+int32_t mpm_batch_upload(mpm_ctx *ctx, const int64_t *scene_offsets, int64_t n, const float *x,
+                         const float *v, const float *C, const float *F, const float *J,
+                         const float *m, const float *vol, const int32_t *mat, const float *mu,
+                         const float *lam);
 /* AdjustParticleMaterial (Temp.cu:16-56): per-particle Lame parameters
  * (host arrays, upload order) that override the material's mu / lam. */
 int32_t mpm_particles_set_lame(mpm_ctx *ctx, const float *mu, const float *lam);

@@ -56,6 +56,8 @@ struct mpm_ctx {
   Counters *h_cnt = nullptr;  // pinned
   std::vector<void *> allocs;
   cudaEvent_t events[MPM_NUM_STAGES + 1] = {};
+  std::vector<SceneParams> scenes;
+  int n_materials = 0;
 };
 
 namespace {
@@ -95,6 +97,8 @@ int32_t push_params(mpm_ctx *c) {
   if (!c->prm_dirty) return MPM_OK;
   ZS_CUDA(cudaMemcpyAsync(c->d.prm, &c->prm, sizeof(SimParams), cudaMemcpyHostToDevice,
                           c->stream));
+  ZS_CUDA(cudaMemcpyAsync(c->d.scn, c->scenes.data(), sizeof(SceneParams) * c->scenes.size(),
+                          cudaMemcpyHostToDevice, c->stream));
   c->prm_dirty = false;
   return MPM_OK;
 }
@@ -196,32 +200,67 @@ int32_t mpm_abi_version(void) { return ZSMPM_ABI_VERSION; }
 
 const char *mpm_last_error(void) { return g_last_error.c_str(); }
 
-int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
-  if (!desc || !out) return fail(MPM_ERR_INVALID, "null argument");
-  *out = nullptr;
-  if (!(desc->dx > 0.0f)) return fail(MPM_ERR_INVALID, "dx must be positive");
-  if (desc->max_particles <= 0 || desc->max_particles >= (int64_t(1) << 31))
-    return fail(MPM_ERR_INVALID, "max_particles must be in [1, 2^31)");
-  long long ndir = 1;
+}  // extern "C"
+
+namespace {
+
+SceneParams scene_from(const mpm_scene_desc &sd) {
+  SceneParams S{};
+  S.dx = sd.dx;
+  S.inv_dx = 1.0f / sd.dx;
+  S.Dinv = 4.0f * S.inv_dx * S.inv_dx;
   for (int k = 0; k < 3; ++k) {
-    if (desc->block_dims[k] < 3) return fail(MPM_ERR_INVALID, "block_dims must be >= 3");
-    ndir *= desc->block_dims[k];
+    S.gravity[k] = sd.gravity[k];
+    S.block_lo[k] = sd.block_lo[k];
+    S.block_dims[k] = sd.block_dims[k];
+    S.bc_lo[k] = sd.boundary.lo[k];
+    S.bc_hi[k] = sd.boundary.hi[k];
+  }
+  S.bc_type = sd.boundary.type;
+  S.bc_thickness = sd.boundary.thickness;
+  return S;
+}
+
+int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_scenes,
+                       int64_t max_particles, int32_t max_grid_blocks, mpm_ctx **out) {
+  if (!scenes || !out || n_scenes <= 0) return fail(MPM_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (n_scenes > kMaxScenes)
+    return fail(MPM_ERR_INVALID, "at most " + std::to_string(kMaxScenes) + " scenes");
+  if (max_particles <= 0 || max_particles >= (int64_t(1) << 31))
+    return fail(MPM_ERR_INVALID, "max_particles must be in [1, 2^31)");
+  long long ndir = 0;
+  std::vector<SceneParams> sp(n_scenes);
+  for (int s = 0; s < n_scenes; ++s) {
+    const mpm_scene_desc &sd = scenes[s];
+    if (!(sd.dx > 0.0f)) return fail(MPM_ERR_INVALID, "dx must be positive");
+    if (sd.boundary.type < MPM_BC_NONE || sd.boundary.type > MPM_BC_SEPARATE ||
+        sd.boundary.thickness < 0)
+      return fail(MPM_ERR_INVALID, "bad boundary");
+    long long nd = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (sd.block_dims[k] < 3) return fail(MPM_ERR_INVALID, "block_dims must be >= 3");
+      nd *= sd.block_dims[k];
+    }
+    sp[s] = scene_from(sd);
+    sp[s].dir_off = (int)std::min<long long>(ndir, 1ll << 30);
+    ndir += nd;
   }
   if (ndir >= (1ll << 25)) return fail(MPM_ERR_INVALID, "block directory larger than 2^25 blocks");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
     return fail(MPM_ERR_NO_DEVICE, "no CUDA device");
-  if (desc->device < 0 || desc->device >= ndev) return fail(MPM_ERR_INVALID, "bad device ordinal");
+  if (device < 0 || device >= ndev) return fail(MPM_ERR_INVALID, "bad device ordinal");
   int major = 0, minor = 0, sms = 0;
-  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, desc->device);
-  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, desc->device);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, desc->device);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (major * 10 + minor != 103)
     return fail(MPM_ERR_NO_DEVICE, "zsmpm is built for sm_103a (GB300) only; device is sm_" +
                                        std::to_string(major * 10 + minor));
 
   mpm_ctx *c = new mpm_ctx();
-  c->device = desc->device;
+  c->device = device;
   int32_t rc = MPM_OK;
   auto bail = [&](int32_t r) {
     mpm_ctx_destroy(c);
@@ -232,9 +271,8 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
     return bail(fail(MPM_ERR_CUDA, "cudaStreamCreate"));
   c->stream = c->own_stream;
 
-  const long long cap = desc->max_particles;
-  long long capg = desc->max_grid_blocks > 0 ? desc->max_grid_blocks
-                                             : std::max<long long>(16384, cap / 4);
+  const long long cap = max_particles;
+  long long capg = max_grid_blocks > 0 ? max_grid_blocks : std::max<long long>(16384, cap / 4);
   capg = std::min<long long>(capg, ndir);
   DevPtrs &d = c->d;
   d.cap = cap;
@@ -242,6 +280,7 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
   d.cap_gblocks = (int)capg;
   d.num_sms = sms;
   d.ntiles = (int)((ndir + kScanTile - 1) / kScanTile);
+  d.n_scenes = n_scenes;
   configure_launches(d);
   for (int k = 0; k < 2; ++k) {
     if ((rc = dalloc(c, &d.pbuf[k], (size_t)NCH * cap))) return bail(rc);
@@ -256,7 +295,8 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
       (rc = dalloc(c, &d.bk_start, capg)) || (rc = dalloc(c, &d.bk_count, capg)) ||
       (rc = dalloc(c, &d.grid, (size_t)capg * 64)) ||
       (rc = dalloc(c, &d.tile_sums, (size_t)3 * d.ntiles)) || (rc = dalloc(c, &d.cnt, 1)) ||
-      (rc = dalloc(c, &d.prm, 1)) || (rc = dalloc(c, &d.mats, kMaxMaterials)))
+      (rc = dalloc(c, &d.prm, 1)) || (rc = dalloc(c, &d.scn, n_scenes)) ||
+      (rc = dalloc(c, &d.mats, kMaxMaterials)))
     return bail(rc);
   if (cudaMallocHost(&c->h_cnt, sizeof(Counters)) != cudaSuccess)
     return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
@@ -275,23 +315,9 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
   cudaMemsetAsync(d.cnt, 0, sizeof(Counters), c->stream);
   cudaMemsetAsync(d.mats, 0, kMaxMaterials * sizeof(MatParams), c->stream);
 
+  c->scenes = sp;
   SimParams &P = c->prm;
   P.dt = 1e-4f;
-  P.dx = desc->dx;
-  P.inv_dx = 1.0f / desc->dx;
-  P.Dinv = 4.0f * P.inv_dx * P.inv_dx;
-  P.gravity[0] = 0.0f;
-  P.gravity[1] = -9.8f;
-  P.gravity[2] = 0.0f;
-  for (int k = 0; k < 3; ++k) {
-    P.block_lo[k] = desc->block_lo[k];
-    P.block_dims[k] = desc->block_dims[k];
-    P.bc_lo[k] = 0;
-    P.bc_hi[k] = 0;
-  }
-  P.bc_type = MPM_BC_NONE;
-  P.bc_thickness = 0;
-  P.n_materials = 0;
   P.has_lame = 0;
   P.n = 0;
   c->prm_dirty = true;
@@ -300,6 +326,28 @@ int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
     return bail(fail(MPM_ERR_CUDA, "context initialisation failed"));
   *out = c;
   return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mpm_ctx_create(const mpm_ctx_desc *desc, mpm_ctx **out) {
+  if (!desc || !out) return fail(MPM_ERR_INVALID, "null argument");
+  mpm_scene_desc sd{};
+  sd.dx = desc->dx;
+  for (int k = 0; k < 3; ++k) {
+    sd.block_lo[k] = desc->block_lo[k];
+    sd.block_dims[k] = desc->block_dims[k];
+  }
+  sd.gravity[1] = -9.8f;  // UpdateZSGrid "gravity" default (MPMPipeline.cu:946-951)
+  sd.boundary.type = MPM_BC_NONE;
+  return create_context(desc->device, &sd, 1, desc->max_particles, desc->max_grid_blocks, out);
+}
+
+int32_t mpm_batch_create(int32_t device, const mpm_scene_desc *scenes, int32_t n_scenes,
+                         int64_t max_particles, int32_t max_grid_blocks, mpm_ctx **out) {
+  return create_context(device, scenes, n_scenes, max_particles, max_grid_blocks, out);
 }
 
 int32_t mpm_ctx_destroy(mpm_ctx *c) {
@@ -354,7 +402,7 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
   ZS_CUDA(cudaMemcpyAsync(c->d.mats, h.data(), sizeof(MatParams) * kMaxMaterials,
                           cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
-  c->prm.n_materials = n;
+  c->n_materials = n;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
   if (c->prm.n > 0) {  // stored stresses follow the new parameters
@@ -369,11 +417,13 @@ int32_t mpm_set_boundary(mpm_ctx *c, const mpm_boundary *bc) {
   if (rc) return rc;
   if (!bc || bc->type < MPM_BC_NONE || bc->type > MPM_BC_SEPARATE || bc->thickness < 0)
     return fail(MPM_ERR_INVALID, "bad boundary");
-  c->prm.bc_type = bc->type;
-  c->prm.bc_thickness = bc->thickness;
-  for (int k = 0; k < 3; ++k) {
-    c->prm.bc_lo[k] = bc->lo[k];
-    c->prm.bc_hi[k] = bc->hi[k];
+  for (SceneParams &S : c->scenes) {
+    S.bc_type = bc->type;
+    S.bc_thickness = bc->thickness;
+    for (int k = 0; k < 3; ++k) {
+      S.bc_lo[k] = bc->lo[k];
+      S.bc_hi[k] = bc->hi[k];
+    }
   }
   c->prm_dirty = true;
   return push_params(c);
@@ -382,26 +432,42 @@ int32_t mpm_set_boundary(mpm_ctx *c, const mpm_boundary *bc) {
 int32_t mpm_set_gravity(mpm_ctx *c, float gx, float gy, float gz) {
   int32_t rc = check(c);
   if (rc) return rc;
-  c->prm.gravity[0] = gx;
-  c->prm.gravity[1] = gy;
-  c->prm.gravity[2] = gz;
+  for (SceneParams &S : c->scenes) {
+    S.gravity[0] = gx;
+    S.gravity[1] = gy;
+    S.gravity[2] = gz;
+  }
   c->prm_dirty = true;
   return push_params(c);
 }
 
-int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float *v,
-                             const float *C, const float *F, const float *J, const float *m,
-                             const float *vol, const int32_t *mat, const float *mu,
-                             const float *lam) {
+}  // extern "C"
+
+namespace {
+
+int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const float *x,
+                    const float *v, const float *C, const float *F, const float *J,
+                    const float *m, const float *vol, const int32_t *mat, const float *mu,
+                    const float *lam) {
   int32_t rc = check(c);
   if (rc) return rc;
+  const int ns = (int)c->scenes.size();
+  if (scene_offsets) {
+    if (scene_offsets[0] != 0 || scene_offsets[ns] != n)
+      return fail(MPM_ERR_INVALID, "scene offsets must run from 0 to n");
+    for (int s = 0; s < ns; ++s)
+      if (scene_offsets[s + 1] < scene_offsets[s])
+        return fail(MPM_ERR_INVALID, "scene offsets must not decrease");
+  } else if (ns != 1) {
+    return fail(MPM_ERR_INVALID, "a batched context takes mpm_batch_upload");
+  }
   if (n < 0 || n > c->d.cap) return fail(MPM_ERR_CAPACITY, "particle count exceeds capacity");
   if (n > 0 && (!x || !m || !vol)) return fail(MPM_ERR_INVALID, "x, m and vol are required");
   if ((mu == nullptr) != (lam == nullptr)) return fail(MPM_ERR_INVALID, "mu and lam go together");
-  if (c->prm.n_materials <= 0) return fail(MPM_ERR_STATE, "set materials before uploading");
+  if (c->n_materials <= 0) return fail(MPM_ERR_STATE, "set materials before uploading");
   if (mat) {
     for (int64_t i = 0; i < n; ++i)
-      if (mat[i] < 0 || mat[i] >= c->prm.n_materials)
+      if (mat[i] < 0 || mat[i] >= c->n_materials)
         return fail(MPM_ERR_INVALID, "material id out of range");
   }
   const int alt = 1 - c->cur;
@@ -434,6 +500,7 @@ int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float 
   if ((rc = launch_check("ingest"))) return rc;
   c->prm.n = n;
   c->prm.has_lame = mu ? 1 : 0;
+  for (int s = 0; s < ns; ++s) c->scenes[s].p_off = scene_offsets ? scene_offsets[s] : 0;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
   launch_stress(c->d, c->cur, c->stream);  // S = vol * tau read by P2G
@@ -446,6 +513,25 @@ int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float 
   c->substeps = 0;
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float *v,
+                             const float *C, const float *F, const float *J, const float *m,
+                             const float *vol, const int32_t *mat, const float *mu,
+                             const float *lam) {
+  return upload_impl(c, nullptr, n, x, v, C, F, J, m, vol, mat, mu, lam);
+}
+
+int32_t mpm_batch_upload(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const float *x,
+                         const float *v, const float *C, const float *F, const float *J,
+                         const float *m, const float *vol, const int32_t *mat, const float *mu,
+                         const float *lam) {
+  if (!scene_offsets) return fail(MPM_ERR_INVALID, "scene offsets are required");
+  return upload_impl(c, scene_offsets, n, x, v, C, F, J, m, vol, mat, mu, lam);
 }
 
 int32_t mpm_particles_set_lame(mpm_ctx *c, const float *mu, const float *lam) {

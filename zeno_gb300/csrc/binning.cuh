@@ -16,32 +16,33 @@ __device__ __forceinline__ int particle_base(float x, float inv_dx) {
   return __float2int_rd(__fsub_rn(__fmul_rn(x, inv_dx), 0.5f));
 }
 
-// key = (directory index << 6) | cell, or -1 (status bit set) for a
-// non-finite position or one outside the directory's interior
-__device__ __forceinline__ int bin_key(const SimParams &P, float x0, float x1, float x2,
+// key = (global directory index << 6) | cell, or -1 (status bit set) for a
+// non-finite position or one outside the interior of the scene's directory
+__device__ __forceinline__ int bin_key(const SceneParams &S, float x0, float x1, float x2,
                                        int *status) {
   if (!(isfinite(x0) && isfinite(x1) && isfinite(x2))) {
     atomicOr(status, ST_NAN);
     return -1;
   }
-  const int b0 = particle_base(x0, P.inv_dx), b1 = particle_base(x1, P.inv_dx),
-            b2 = particle_base(x2, P.inv_dx);
-  const int c0 = (b0 >> 2) - P.block_lo[0], c1 = (b1 >> 2) - P.block_lo[1],
-            c2 = (b2 >> 2) - P.block_lo[2];
-  const int dy = P.block_dims[1], dz = P.block_dims[2];
-  if (c0 < 1 || c0 > P.block_dims[0] - 2 || c1 < 1 || c1 > dy - 2 || c2 < 1 || c2 > dz - 2) {
+  const int b0 = particle_base(x0, S.inv_dx), b1 = particle_base(x1, S.inv_dx),
+            b2 = particle_base(x2, S.inv_dx);
+  const int c0 = (b0 >> 2) - S.block_lo[0], c1 = (b1 >> 2) - S.block_lo[1],
+            c2 = (b2 >> 2) - S.block_lo[2];
+  const int dy = S.block_dims[1], dz = S.block_dims[2];
+  if (c0 < 1 || c0 > S.block_dims[0] - 2 || c1 < 1 || c1 > dy - 2 || c2 < 1 || c2 > dz - 2) {
     atomicOr(status, ST_OUT_OF_DOMAIN);
     return -1;
   }
-  const int dd = (c0 * dy + c1) * dz + c2;
+  const int dd = S.dir_off + (c0 * dy + c1) * dz + c2;
   return (dd << 6) | ((b0 & 3) << 4) | ((b1 & 3) << 2) | (b2 & 3);
 }
 
 // Warp-aggregated count of `key` into its block; the first particle of a
 // block marks the block and its 26 neighbours as grid blocks (the 1-ring
 // halo of ExpandZSPartition, MPMPipeline.cu:131-199).  Every lane of `mask`
-// must call this together.
-__device__ __forceinline__ void bin_count(const DevPtrs &d, const SimParams &P, int key,
+// must call this together; lanes of one call may belong to different scenes
+// (the leader of a block marks with its own scene's strides).
+__device__ __forceinline__ void bin_count(const DevPtrs &d, const SceneParams &S, int key,
                                           unsigned mask) {
   const int dd = key >> 6;  // -1 for invalid
   const unsigned peers = __match_any_sync(mask, dd);
@@ -49,7 +50,7 @@ __device__ __forceinline__ void bin_count(const DevPtrs &d, const SimParams &P, 
   if (key >= 0 && (int)(threadIdx.x & 31) == leader) {
     const int old = atomicAdd(&d.dir_count[dd], __popc(peers));
     if (old == 0) {
-      const int dy = P.block_dims[1], dz = P.block_dims[2];
+      const int dy = S.block_dims[1], dz = S.block_dims[2];
       for (int a = -1; a <= 1; ++a)
         for (int b = -1; b <= 1; ++b)
           for (int c = -1; c <= 1; ++c) d.dir_flag[dd + (a * dy + b) * dz + c] = 1;

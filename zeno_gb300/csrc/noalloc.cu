@@ -37,7 +37,8 @@ constexpr int kNoAllocMaxTiles = (int)((kNoAllocMaxBlocks + kScanTile - 1) / kSc
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kOffCounters = 0;
 constexpr size_t kOffParams = align256(kOffCounters + sizeof(Counters));
-constexpr size_t kOffKeys = align256(kOffParams + sizeof(SimParams));
+constexpr size_t kOffScene = align256(kOffParams + sizeof(SimParams));
+constexpr size_t kOffKeys = align256(kOffScene + sizeof(SceneParams));
 constexpr size_t kOffPermTmp = align256(kOffKeys + 4 * kNoAllocMaxParticles);
 constexpr size_t kOffDirCount = align256(kOffPermTmp + 4 * kNoAllocMaxParticles);
 constexpr size_t kOffDirFill = align256(kOffDirCount + 4 * kNoAllocMaxBlocks);
@@ -146,14 +147,15 @@ extern "C" int32_t mpm_partition_noalloc(const float *x_planes, int64_t n, float
 
   SimParams P{};
   P.dt = 1.0f;
-  P.dx = dx;
-  P.inv_dx = 1.0f / dx;
-  P.Dinv = 4.0f * P.inv_dx * P.inv_dx;
-  for (int k = 0; k < 3; ++k) {
-    P.block_lo[k] = block_lo[k];
-    P.block_dims[k] = block_dims[k];
-  }
   P.n = n;
+  SceneParams S{};
+  S.dx = dx;
+  S.inv_dx = 1.0f / dx;
+  S.Dinv = 4.0f * S.inv_dx * S.inv_dx;
+  for (int k = 0; k < 3; ++k) {
+    S.block_lo[k] = block_lo[k];
+    S.block_dims[k] = block_dims[k];
+  }
 
   DevPtrs d{};
   d.pbuf[0] = const_cast<float *>(x_planes);  // planes x[0..n), y[n..2n), z[2n..3n)
@@ -176,9 +178,13 @@ extern "C" int32_t mpm_partition_noalloc(const float *x_planes, int64_t n, float
   d.ntiles = (int)((ndir + kScanTile - 1) / kScanTile);
   d.cnt = reinterpret_cast<Counters *>(base + kOffCounters);
   d.prm = reinterpret_cast<SimParams *>(base + kOffParams);
+  d.scn = reinterpret_cast<SceneParams *>(base + kOffScene);
+  d.n_scenes = 1;
   d.num_sms = sc.num_sms;
 
   cudaError_t e = cudaMemcpyAsync(d.prm, &P, sizeof(SimParams), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d.scn, &S, sizeof(SceneParams), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("parameters: ") + cudaGetErrorString(e));
   k_noalloc_clear<<<sc.num_sms * 4, 256, 0, s>>>(base, ndir);
   launch_bin(d, 0, s);

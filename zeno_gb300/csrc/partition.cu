@@ -49,6 +49,8 @@ __global__ void k_full_dir_clear(DevPtrs d) {
   }
 }
 
+// Binning of particles in upload order (after an upload the storage slot is
+// the upload index, which gives the scene).
 __global__ void k_bin(DevPtrs d, const float *__restrict__ pin) {
   const SimParams &P = *d.prm;
   const long long n = P.n;
@@ -59,12 +61,14 @@ __global__ void k_bin(DevPtrs d, const float *__restrict__ pin) {
   for (long long w = warp0; w < n; w += stride) {
     const long long i = w + lane;
     int key = -1;
+    int scene = 0;
     if (i < n) {
-      key = bin_key(P, pin[CH_X * cap + i], pin[(CH_X + 1) * cap + i], pin[(CH_X + 2) * cap + i],
-                    &d.cnt->status);
+      scene = scene_of_particle(d, i);
+      key = bin_key(d.scn[scene], pin[CH_X * cap + i], pin[(CH_X + 1) * cap + i],
+                    pin[(CH_X + 2) * cap + i], &d.cnt->status);
       d.pkey[i] = key;
     }
-    bin_count(d, P, key, 0xffffffffu);
+    bin_count(d, d.scn[scene], key, 0xffffffffu);
   }
 }
 

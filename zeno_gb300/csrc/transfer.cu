@@ -30,18 +30,21 @@ namespace {
 constexpr int kG2PThreads = 128;
 constexpr int kNodes = 216;  // 6^3
 
-__device__ __forceinline__ void bucket_origin(const SimParams &P, int dir, int (&K)[3]) {
-  const int dz = P.block_dims[2], dy = P.block_dims[1];
-  const int c2 = dir % dz, c1 = (dir / dz) % dy, c0 = dir / (dz * dy);
-  K[0] = (c0 + P.block_lo[0]) * 4;
-  K[1] = (c1 + P.block_lo[1]) * 4;
-  K[2] = (c2 + P.block_lo[2]) * 4;
+// node index of the first node of the particle block at (scene-local)
+// directory index `ldir`
+__device__ __forceinline__ void bucket_origin(const SceneParams &S, int ldir, int (&K)[3]) {
+  const int dz = S.block_dims[2], dy = S.block_dims[1];
+  const int c2 = ldir % dz, c1 = (ldir / dz) % dy, c0 = ldir / (dz * dy);
+  K[0] = (c0 + S.block_lo[0]) * 4;
+  K[1] = (c1 + S.block_lo[1]) * 4;
+  K[2] = (c2 + S.block_lo[2]) * 4;
 }
 
-// grid block of each of the 2x2x2 blocks around particle block `dir`
-__device__ __forceinline__ int neighbour_gb(const DevPtrs &d, const SimParams &P, int dir,
+// grid block of each of the 2x2x2 blocks around the particle block at
+// (global) directory index `dir`
+__device__ __forceinline__ int neighbour_gb(const DevPtrs &d, const SceneParams &S, int dir,
                                             int t) {
-  const int dz = P.block_dims[2], dy = P.block_dims[1];
+  const int dz = S.block_dims[2], dy = S.block_dims[1];
   return d.dir_gb[dir + ((t >> 2) * dy + ((t >> 1) & 1)) * dz + (t & 1)];
 }
 
@@ -79,7 +82,7 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__r
   unsigned char *scell = p2g_smem + kP2GSpdBytes + kP2GAccBytes + 65 * sizeof(int);
   const SimParams &P = *d.prm;
   const long long cap = d.cap;
-  const float dt = P.dt, dx = P.dx, inv_dx = P.inv_dx, Dinv = P.Dinv;
+  const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // lane constants of phase 2: slot, stencil column (i, j), weight polynomials
@@ -94,14 +97,16 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__r
   float ci0, ci1, ci2, cj0, cj1, cj2;
   coef(oi, ci0, ci1, ci2);
   coef(oj, cj0, cj1, cj2);
-  const float odx = oi * dx, ody = oj * dx;
   float *myacc = &acc[warp][0][0];
 
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     for (int i = tid; i < kP2GWarps * 4 * kNodes; i += kP2GThreads) (&acc[0][0][0])[i] = 0.0f;
     const int dir = d.bk_dir[b];
+    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
+    const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
+    const float odx = oi * dx, ody = oj * dx;
     int K[3];
-    bucket_origin(P, dir, K);
+    bucket_origin(S, dir - S.dir_off, K);
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     for (int c0 = 0; c0 < cnt; c0 += kP2GChunk) {
@@ -256,19 +261,21 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__r
 // coordinate l + 4 o when that is < 6.  The <= 8 tiles are added in the fixed
 // order o = (0,0,0), (0,0,1), ..., so the sums are reproducible.  mode bit 1
 // applies UpdateZSGrid and bit 2 ApplyBoundaryOnZSGrid to the sum.
-__device__ __forceinline__ void update_node(const SimParams &P, int mode, int gdir, int cell,
-                                            float4 &g, float &vmax);
+__device__ __forceinline__ void update_node(const SceneParams &S, float dt, int mode, int ldir,
+                                            int cell, float4 &g, float &vmax);
 
 __global__ void k_grid_gather(DevPtrs d, int mode) {
   const SimParams &P = *d.prm;
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
-  const int dy = P.block_dims[1], dz = P.block_dims[2];
   float vmax = 0.0f;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
        idx += (long long)gridDim.x * blockDim.x) {
     const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
     const int gdir = d.gb_dir[gb];
-    const int c0 = gdir / (dz * dy), c1 = (gdir / dz) % dy, c2 = gdir % dz;
+    const SceneParams &S = d.scn[scene_of_dir(d, gdir)];
+    const int dy = S.block_dims[1], dz = S.block_dims[2];
+    const int ldir = gdir - S.dir_off;
+    const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
     const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
     float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -286,7 +293,7 @@ __global__ void k_grid_gather(DevPtrs d, int mode) {
       g.z += t.z;
       g.w += t.w;
     }
-    if (g.x != 0.0f) update_node(P, mode, gdir, cell, g, vmax);
+    if (g.x != 0.0f) update_node(S, P.dt, mode, ldir, cell, g, vmax);
     d.grid[idx] = g;
   }
   if (mode & 1) {
@@ -303,36 +310,35 @@ __global__ void k_grid_gather(DevPtrs d, int mode) {
 // I_a < lo_a + thickness and in the upper wall when I_a > hi_a - thickness;
 // sticky sets v = 0, slip removes the wall-normal component, separate removes
 // it only when it points into the wall (collider velocity 0).
-__device__ __forceinline__ void update_node(const SimParams &P, int mode, int gdir, int cell,
-                                            float4 &g, float &vmax) {
+__device__ __forceinline__ void update_node(const SceneParams &S, float dt, int mode, int ldir,
+                                            int cell, float4 &g, float &vmax) {
   if (mode & 1) {
     const float r = 1.0f / g.x;
-    const float dt = P.dt;
-    g.y = g.y * r + P.gravity[0] * dt;
-    g.z = g.z * r + P.gravity[1] * dt;
-    g.w = g.w * r + P.gravity[2] * dt;
+    g.y = g.y * r + S.gravity[0] * dt;
+    g.z = g.z * r + S.gravity[1] * dt;
+    g.w = g.w * r + S.gravity[2] * dt;
     vmax = fmaxf(vmax, g.y * g.y + g.z * g.z + g.w * g.w);
   }
-  if ((mode & 2) && P.bc_type != MPM_BC_NONE) {
-    const int dz = P.block_dims[2], dy = P.block_dims[1];
-    const int I[3] = {((gdir / (dz * dy)) + P.block_lo[0]) * 4 + (cell >> 4),
-                      (((gdir / dz) % dy) + P.block_lo[1]) * 4 + ((cell >> 2) & 3),
-                      ((gdir % dz) + P.block_lo[2]) * 4 + (cell & 3)};
+  if ((mode & 2) && S.bc_type != MPM_BC_NONE) {
+    const int dz = S.block_dims[2], dy = S.block_dims[1];
+    const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
+                      (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
+                      ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
     float vel[3] = {g.y, g.z, g.w};
     bool any = false;
-    const int t = P.bc_thickness;
+    const int t = S.bc_thickness;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      const bool lower = I[a] < P.bc_lo[a] + t, upper = I[a] > P.bc_hi[a] - t;
+      const bool lower = I[a] < S.bc_lo[a] + t, upper = I[a] > S.bc_hi[a] - t;
       if (!(lower || upper)) continue;
       any = true;
-      if (P.bc_type == MPM_BC_SLIP) vel[a] = 0.0f;
-      if (P.bc_type == MPM_BC_SEPARATE) {
+      if (S.bc_type == MPM_BC_SLIP) vel[a] = 0.0f;
+      if (S.bc_type == MPM_BC_SEPARATE) {
         if (lower && vel[a] < 0.0f) vel[a] = 0.0f;
         if (upper && vel[a] > 0.0f) vel[a] = 0.0f;
       }
     }
-    if (any && P.bc_type == MPM_BC_STICKY) vel[0] = vel[1] = vel[2] = 0.0f;
+    if (any && S.bc_type == MPM_BC_STICKY) vel[0] = vel[1] = vel[2] = 0.0f;
     g.y = vel[0];
     g.z = vel[1];
     g.w = vel[2];
@@ -347,7 +353,9 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
        idx += (long long)gridDim.x * blockDim.x) {
     float4 g = d.grid[idx];
     if (g.x == 0.0f) continue;
-    update_node(P, mode, d.gb_dir[idx >> 6], (int)(idx & 63), g, vmax);
+    const int gdir = d.gb_dir[idx >> 6];
+    const SceneParams &S = d.scn[scene_of_dir(d, gdir)];
+    update_node(S, P.dt, mode, gdir - S.dir_off, (int)(idx & 63), g, vmax);
     d.grid[idx] = g;
   }
   if (mode & 1) {
@@ -366,14 +374,16 @@ __global__ void __launch_bounds__(kG2PThreads)
   __shared__ int sgb[8];
   const SimParams &P = *d.prm;
   const long long cap = d.cap;
-  const float dt = P.dt, dx = P.dx, inv_dx = P.inv_dx, Dinv = P.Dinv;
+  const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const bool lame = P.has_lame != 0;
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const int dir = d.bk_dir[b];
-    if (threadIdx.x < 8) sgb[threadIdx.x] = neighbour_gb(d, P, dir, threadIdx.x);
+    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
+    const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
+    if (threadIdx.x < 8) sgb[threadIdx.x] = neighbour_gb(d, S, dir, threadIdx.x);
     int K[3];
-    bucket_origin(P, dir, K);
+    bucket_origin(S, dir - S.dir_off, K);
     __syncthreads();
     for (int nd = threadIdx.x; nd < kNodes; nd += kG2PThreads) {
       const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
@@ -532,9 +542,9 @@ __global__ void __launch_bounds__(kG2PThreads)
       iout[IC_ID * cap + s] = iin[IC_ID * cap + p];
       if (kFuseBin) {
         // key of the new position for the next partition (storage slot s)
-        const int key = bin_key(P, x[0], x[1], x[2], &d.cnt->status);
+        const int key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
         d.pkey[s] = key;
-        bin_count(d, P, key, mask);
+        bin_count(d, S, key, mask);
       }
     }
     __syncthreads();

@@ -50,7 +50,8 @@ enum : int {
   ST_STENCIL = 32
 };
 
-constexpr int kMaxMaterials = 64;
+constexpr int kMaxMaterials = 256;
+constexpr int kMaxScenes = 4096;
 constexpr int kScanTile = 2048;       // directory entries per scan tile
 constexpr int kScanThreads = 256;     // 8 entries per thread
 constexpr int kScanPerThread = kScanTile / kScanThreads;
@@ -73,15 +74,23 @@ struct Counters {
 // Device-resident parameters; the host updates them with one small copy
 // when they change, so captured graphs read the current values.
 struct SimParams {
-  float dt, dx, inv_dx, Dinv;
+  float dt;
+  int has_lame;
+  long long n;  // particles of all scenes
+};
+
+// One scene of a context: its grid spacing, its slice of the concatenated
+// block directory, its boundary and gravity.  A context holds one scene
+// (the plain substep) or many independent scenes (the batched substep).
+struct SceneParams {
+  float dx, inv_dx, Dinv;
   float gravity[3];
   int block_lo[3];
   int block_dims[3];
+  int dir_off;     // first directory entry of the scene
   int bc_type, bc_thickness;
   int bc_lo[3], bc_hi[3];
-  int n_materials;
-  int has_lame;
-  long long n;
+  long long p_off;  // first particle of the scene in upload order
 };
 
 struct DevPtrs {
@@ -103,6 +112,8 @@ struct DevPtrs {
   int ntiles;
   Counters *cnt;
   SimParams *prm;
+  SceneParams *scn;  // n_scenes entries
+  int n_scenes;
   MatParams *mats;
   int num_sms;
   int grid_p2g, grid_g2p;  // persistent grids: SMs x resident CTAs per SM
@@ -145,5 +156,34 @@ void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *la
                      cudaStream_t s);
 // writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
 void launch_egest(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s);
+
+#ifdef __CUDACC__
+// scene of a (global) directory index: the last scene whose slice starts at
+// or before it
+__device__ __forceinline__ int scene_of_dir(const DevPtrs &d, int dir) {
+  int lo = 0, hi = d.n_scenes - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d.scn[mid].dir_off <= dir)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// scene of a particle in upload order
+__device__ __forceinline__ int scene_of_particle(const DevPtrs &d, long long i) {
+  int lo = 0, hi = d.n_scenes - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d.scn[mid].p_off <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+#endif
 
 }  // namespace zsmpm

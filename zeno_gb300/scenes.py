@@ -250,3 +250,12 @@ def batched_scene(index: int, count: int, seed: int = 1, dx: float = 1.0 / 128):
     v = 0.5 * normal(seed, 3000 + index, count * 3).reshape(-1, 3)
     parts = make_particles(x, dx, 8, scene.materials, np.zeros(count, np.int32), v=v)
     return scene, parts
+
+
+def batched_workload(n_scenes: int = 256, lo: int = 2048, hi: int = 200000, seed: int = 1,
+                     dx: float = 1.0 / 128):
+    """The batched workload: n_scenes independent scenes with log-uniform
+    particle counts in [lo, hi] (seed 1), each its own dx = 1/128 grid over
+    [0,1]^3 with slip walls and one material drawn uniformly from the four."""
+    counts = batched_counts(n_scenes, lo, hi, seed)
+    return [batched_scene(i, int(c), seed=seed, dx=dx) for i, c in enumerate(counts)]

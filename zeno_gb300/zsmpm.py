@@ -45,6 +45,11 @@ class Boundary(C.Structure):
                 ("hi", C.c_int32 * 3)]
 
 
+class SceneDesc(C.Structure):
+    _fields_ = [("dx", C.c_float), ("block_lo", C.c_int32 * 3), ("block_dims", C.c_int32 * 3),
+                ("gravity", C.c_float * 3), ("boundary", Boundary)]
+
+
 class Stats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_particle_blocks", C.c_int32),
                 ("n_grid_blocks", C.c_int32), ("max_vel_sqr", C.c_float), ("status", C.c_int32),
@@ -52,6 +57,7 @@ class Stats(C.Structure):
 
 
 EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destroy",
+           "mpm_batch_create", "mpm_batch_upload",
            "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
            "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
@@ -79,6 +85,9 @@ def load(path: str = LIB_PATH):
         "mpm_last_error": ([], C.c_char_p),
         "mpm_ctx_create": ([C.POINTER(CtxDesc), C.POINTER(C.c_void_p)], i32),
         "mpm_ctx_destroy": ([P], i32),
+        "mpm_batch_create": ([i32, C.POINTER(SceneDesc), i32, i64, i32, C.POINTER(C.c_void_p)],
+                             i32),
+        "mpm_batch_upload": ([P, P, i64] + [P] * 10, i32),
         "mpm_set_stream": ([P, P], i32),
         "mpm_set_materials": ([P, C.POINTER(Material), i32], i32),
         "mpm_set_boundary": ([P, C.POINTER(Boundary)], i32),
@@ -136,6 +145,10 @@ class Context:
         self.set_materials(scene.materials)
         self.set_boundary(scene.bc_type, scene.bc_thickness, scene.bc_lo, scene.bc_hi)
         self.set_gravity(*scene.gravity)
+
+    @property
+    def dir_size(self) -> int:
+        return int(np.prod(self.scene.block_dims))
 
     def _check(self, rc: int, where: str):
         if rc != MPM_OK:
@@ -282,7 +295,7 @@ class Context:
                 "status": s.status, "substeps": s.substeps}
 
     def partition_download(self) -> dict:
-        D = int(np.prod(self.scene.block_dims))
+        D = self.dir_size
         n_pb = np.zeros(1, np.int32)
         n_gb = np.zeros(1, np.int32)
         pb_dir = np.zeros(D, np.int32)
@@ -301,6 +314,81 @@ class Context:
         out = np.zeros((max(ng, 1), 64, 4), np.float32)
         self._check(self._L.mpm_grid_download(self.h, _p(out), out.size), "mpm_grid_download")
         return out[:ng]
+
+
+class BatchContext(Context):
+    """Many independent scenes in one context: every stage of a substep is one
+    persistent launch over the blocks of all scenes.  Materials of all scenes
+    share one table; each particle carries its material id."""
+
+    def __init__(self, scenes, materials, max_particles: int, device: int = 0,
+                 max_grid_blocks: int = 0):
+        L = load()
+        self._L = L
+        arr = (SceneDesc * len(scenes))(*[
+            SceneDesc(float(sc.dx), (C.c_int32 * 3)(*sc.block_lo),
+                      (C.c_int32 * 3)(*sc.block_dims), (C.c_float * 3)(*sc.gravity),
+                      Boundary(int(sc.bc_type), int(sc.bc_thickness),
+                               (C.c_int32 * 3)(*sc.bc_lo), (C.c_int32 * 3)(*sc.bc_hi)))
+            for sc in scenes])
+        h = C.c_void_p()
+        self._check(L.mpm_batch_create(device, arr, len(scenes), int(max_particles),
+                                       int(max_grid_blocks), C.byref(h)), "mpm_batch_create")
+        self.h = h
+        self.scenes = scenes
+        self.scene = scenes[0]
+        self.n = 0
+        self.set_materials(materials)
+
+    @property
+    def dir_size(self) -> int:
+        return int(sum(int(np.prod(sc.block_dims)) for sc in self.scenes))
+
+    def upload_batch(self, parts, offsets):
+        n = parts.n
+        offs = np.ascontiguousarray(offsets, dtype=np.int64)
+        x = _f32(parts.x, (n, 3))
+        v = _f32(parts.v, (n, 3))
+        Cm = _f32(parts.C, (n, 9))
+        F = _f32(parts.F, (n, 9))
+        J = _f32(parts.J, (n,))
+        m = _f32(parts.m, (n,))
+        vol = _f32(parts.vol, (n,))
+        mat = np.ascontiguousarray(parts.mat, dtype=np.int32)
+        mu = _f32(parts.mu, (n,))
+        lam = _f32(parts.lam, (n,))
+        self._keep = (offs, x, v, Cm, F, J, m, vol, mat, mu, lam)
+        self._check(self._L.mpm_batch_upload(self.h, _p(offs), n, _p(x), _p(v), _p(Cm), _p(F),
+                                             _p(J), _p(m), _p(vol), _p(mat), _p(mu), _p(lam)),
+                    "mpm_batch_upload")
+        self.n = n
+
+
+def concat_scenes(pairs):
+    """(scene, particles) pairs -> (scenes, shared material table, particles
+    with remapped material ids, scene offsets)."""
+    from . import scenes as S
+    mats, scenes_out, chunks, offsets = [], [], [], [0]
+    for scene, p in pairs:
+        ids = []
+        for m in scene.materials:  # identical materials share one table entry
+            if m not in mats:
+                mats.append(m)
+            ids.append(mats.index(m))
+        scenes_out.append(scene)
+        q = p.copy()
+        q.mat = np.asarray(ids, dtype=np.int32)[q.mat] if q.n else q.mat.astype(np.int32)
+        chunks.append(q)
+        offsets.append(offsets[-1] + q.n)
+
+    def cat(k):
+        arrs = [getattr(c, k) for c in chunks]
+        if any(a is None for a in arrs):
+            return None
+        return np.concatenate(arrs)
+    parts = S.Particles(*(cat(k) for k in ("x", "v", "C", "F", "J", "m", "vol", "mat", "mu",
+                                            "lam")))
+    return scenes_out, mats, parts, np.array(offsets, dtype=np.int64)
 
 
 # ---------------------------------------------------------------------------
