@@ -171,6 +171,8 @@ def batched_form(zsmpm, steps: int, dev: int):
     ctx = zsmpm.BatchContext(scns, mats, max_particles=parts.n, device=dev)
     ctx.set_stream(stream.cuda_stream)
     ctx.upload_batch(parts, offs)
+    from zeno_gb300 import autotune
+    tuned = autotune.tune(ctx, dt, state=lambda: ctx.upload_batch(parts, offs))
     ctx.substep(dt, 5)
     ctx.sync()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -208,7 +210,10 @@ def batched_form(zsmpm, steps: int, dev: int):
             "ms_per_step": ms_b / steps, "status": st["status"],
             "plain_sequential": n * steps / (ms_p * 1e-3),
             "speedup_over_plain": ms_p / ms_b,
-            "kernel_launches_per_step": KERNELS_PER_SUBSTEP}
+            "kernel_launches_per_step": KERNELS_PER_SUBSTEP,
+            "launch_config": tuned["config"],
+            "note": "plain_sequential: the same scenes, one plain context each, default launch "
+                    "shapes; batched: autotuned launch shapes"}
 
 
 def cpu_baseline(parts, scene, target_s: float = 10.0):
@@ -292,6 +297,8 @@ def run_gpu(args):
     ctx.set_stream(stream.cuda_stream)
     ctx.upload(parts)
     dt = scene.dt
+    from zeno_gb300 import autotune
+    tuned = autotune.tune(ctx, dt, state=lambda: ctx.upload(parts))
 
     # warm-up (captures both graph parities)
     ctx.substep(dt, max(args.warmup, 3))
@@ -427,6 +434,7 @@ def run_gpu(args):
         "clocks": clocks,
         "gpu_launches": KERNELS_PER_SUBSTEP * args.steps,
         "status": st["status"],
+        "launch_config": tuned["config"],
         "forms": forms,
     }
     print(json.dumps(line))

@@ -194,6 +194,20 @@ enum {
 };
 int32_t mpm_substep_timed(mpm_ctx *ctx, float dt, float *stage_ms, int32_t n_stages);
 
+/* Launch shape of the persistent kernels, chosen by the autotuner
+ * (zeno_gb300/autotune.py); 0 fields take the defaults (occupancy maximum for
+ * P2G / G2P, 8 CTAs per SM for the sort and the streaming kernels).  The
+ * reference launches one thread per particle or node (zpc's cuda policy). */
+typedef struct mpm_launch_config {
+  int32_t p2g_ctas_per_sm;
+  int32_t g2p_ctas_per_sm;
+  int32_t sort_ctas_per_sm;
+  int32_t stream_ctas_per_sm; /* binning, scatter, grid gather */
+  int32_t g2p_threads;        /* 128 or 256 */
+} mpm_launch_config;
+int32_t mpm_set_launch_config(mpm_ctx *ctx, const mpm_launch_config *cfg);
+int32_t mpm_get_launch_config(mpm_ctx *ctx, mpm_launch_config *cfg);
+
 /* Wait for the context's stream; returns the device status word. */
 int32_t mpm_sync(mpm_ctx *ctx);
 int32_t mpm_get_stats(mpm_ctx *ctx, mpm_stats *out);

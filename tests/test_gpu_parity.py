@@ -176,3 +176,34 @@ def test_full_size_substeps_against_oracle(zsmpm_mod, oracle_mod):
     assert st["status"] == 0 and ost["status"] == 0
     assert st["n_grid_blocks"] == ost["n_gblocks"]
     _compare(out, ref)
+
+
+def test_launch_shapes_do_not_change_results(zsmpm_mod):
+    """Every launch configuration the autotuner may pick gives the same bits."""
+    scene, parts = S.multi_material(dx=1.0 / 128, region_cells=(32, 16, 16))
+    outs = []
+    for cfg in ({}, {"g2p_threads": 256, "g2p_ctas_per_sm": 2, "p2g_ctas_per_sm": 1},
+                {"sort_ctas_per_sm": 16, "stream_ctas_per_sm": 4, "g2p_ctas_per_sm": 3}):
+        with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+            ctx.set_launch_config(cfg)
+            ctx.upload(parts)
+            ctx.substep(scene.dt, 15)
+            ctx.sync()
+            outs.append(ctx.download())
+    for o in outs[1:]:
+        for k in ("x", "v", "F"):
+            np.testing.assert_array_equal(o[k], outs[0][k], err_msg=k)
+
+
+def test_autotuner_restores_state(zsmpm_mod, tmp_path, monkeypatch):
+    from zeno_gb300 import autotune
+    monkeypatch.setenv("ZSMPM_TUNE_CACHE", str(tmp_path / "launch.json"))
+    scene, parts = S.jelly_cube(cells=8)
+    with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+        ctx.upload(parts)
+        res = autotune.tune(ctx, scene.dt, reps=2)
+        out = ctx.download()
+        np.testing.assert_array_equal(out["x"], parts.x)
+        assert set(res["config"]) == set(autotune.KNOBS)
+        again = autotune.tune(ctx, scene.dt, reps=2)  # from the cache
+        assert again["config"] == res["config"]

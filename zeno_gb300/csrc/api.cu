@@ -701,6 +701,39 @@ int32_t mpm_substep_timed(mpm_ctx *c, float dt, float *stage_ms, int32_t n_stage
   return MPM_OK;
 }
 
+int32_t mpm_set_launch_config(mpm_ctx *c, const mpm_launch_config *cfg) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!cfg || cfg->p2g_ctas_per_sm < 0 || cfg->g2p_ctas_per_sm < 0 || cfg->sort_ctas_per_sm < 0 ||
+      cfg->stream_ctas_per_sm < 0 || cfg->p2g_ctas_per_sm > 64 || cfg->g2p_ctas_per_sm > 64 ||
+      cfg->sort_ctas_per_sm > 64 || cfg->stream_ctas_per_sm > 64 ||
+      (cfg->g2p_threads != 0 && cfg->g2p_threads != 128 && cfg->g2p_threads != 256))
+    return fail(MPM_ERR_INVALID, "bad launch configuration");
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->d.launch = LaunchConfig{cfg->p2g_ctas_per_sm, cfg->g2p_ctas_per_sm, cfg->sort_ctas_per_sm,
+                             cfg->stream_ctas_per_sm, cfg->g2p_threads};
+  configure_launches(c->d);
+  for (int k = 0; k < 2; ++k)  // the captured graphs hold the old shapes
+    if (c->graph[k]) {
+      cudaGraphExecDestroy(c->graph[k]);
+      c->graph[k] = nullptr;
+    }
+  return MPM_OK;
+}
+
+int32_t mpm_get_launch_config(mpm_ctx *c, mpm_launch_config *cfg) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!cfg) return fail(MPM_ERR_INVALID, "null config");
+  const DevPtrs &d = c->d;
+  cfg->p2g_ctas_per_sm = d.grid_p2g / d.num_sms;
+  cfg->g2p_ctas_per_sm = d.grid_g2p / d.num_sms;
+  cfg->sort_ctas_per_sm = d.grid_sort / d.num_sms;
+  cfg->stream_ctas_per_sm = d.grid_stream / d.num_sms;
+  cfg->g2p_threads = d.g2p_threads;
+  return MPM_OK;
+}
+
 int32_t mpm_sync(mpm_ctx *c) {
   int32_t rc = check(c);
   if (rc) return rc;

@@ -413,7 +413,7 @@ void launch_full_dir_clear(const DevPtrs &d, cudaStream_t s) {
 }
 
 void launch_bin(const DevPtrs &d, int cur, cudaStream_t s) {
-  k_bin<<<grid_for(d, 8), 256, 0, s>>>(d, d.pbuf[cur]);
+  k_bin<<<d.grid_stream > 0 ? d.grid_stream : grid_for(d, 8), 256, 0, s>>>(d, d.pbuf[cur]);
 }
 
 void launch_scan(const DevPtrs &d, cudaStream_t s) {
@@ -422,11 +422,11 @@ void launch_scan(const DevPtrs &d, cudaStream_t s) {
 }
 
 void launch_scatter(const DevPtrs &d, cudaStream_t s) {
-  k_scatter<<<grid_for(d, 8), 256, 0, s>>>(d);
+  k_scatter<<<d.grid_stream > 0 ? d.grid_stream : grid_for(d, 8), 256, 0, s>>>(d);
 }
 
 void launch_bucket_sort(const DevPtrs &d, cudaStream_t s) {
-  k_bucket_sort<<<grid_for(d, 8), kSortThreads, 0, s>>>(d);
+  k_bucket_sort<<<d.grid_sort > 0 ? d.grid_sort : grid_for(d, 8), kSortThreads, 0, s>>>(d);
 }
 
 void launch_grid_clear(const DevPtrs &d, cudaStream_t s) {

@@ -20,6 +20,8 @@
 //    and the StVK-Hencky stress share one eigen-decomposition.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "binning.cuh"
 #include "mpm_math.cuh"
 #include "zsmpm_internal.cuh"
@@ -27,7 +29,6 @@
 namespace zsmpm {
 namespace {
 
-constexpr int kG2PThreads = 128;
 constexpr int kNodes = 216;  // 6^3
 
 // node index of the first node of the particle block at (scene-local)
@@ -366,8 +367,8 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
   }
 }
 
-template <bool kFuseRM, bool kFuseBin>
-__global__ void __launch_bounds__(kG2PThreads)
+template <bool kFuseRM, bool kFuseBin, int NT>
+__global__ void __launch_bounds__(NT)
     k_g2p(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
           float *__restrict__ pout, int32_t *__restrict__ iout) {
   __shared__ float sv[3][kNodes];
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(kG2PThreads)
     int K[3];
     bucket_origin(S, dir - S.dir_off, K);
     __syncthreads();
-    for (int nd = threadIdx.x; nd < kNodes; nd += kG2PThreads) {
+    for (int nd = threadIdx.x; nd < kNodes; nd += NT) {
       const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
       const int gb = sgb[((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2)];
       const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
@@ -399,7 +400,7 @@ __global__ void __launch_bounds__(kG2PThreads)
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     // warp-uniform trip count: the fused binning below is a warp collective
-    for (int sbase = start; sbase < start + cnt; sbase += kG2PThreads) {
+    for (int sbase = start; sbase < start + cnt; sbase += NT) {
       const int s = sbase + (int)threadIdx.x;
       const bool live = s < start + cnt;
       const unsigned mask = __ballot_sync(0xffffffffu, live);
@@ -625,13 +626,25 @@ __global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__r
 
 }  // namespace
 
+template <int NT> int g2p_occupancy() {
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true, NT>, NT, 0);
+  return b > 0 ? b : 1;
+}
+
 void configure_launches(DevPtrs &d) {
-  int a = 0, b = 0;
+  int a = 0;
   cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, kP2GSmem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g, kP2GThreads, kP2GSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true>, kG2PThreads, 0);
-  d.grid_p2g = d.num_sms * (a > 0 ? a : 1);
-  d.grid_g2p = d.num_sms * (b > 0 ? b : 1);
+  a = a > 0 ? a : 1;
+  const LaunchConfig &L = d.launch;
+  const int gt = L.g2p_threads == 256 ? 256 : 128;
+  const int g = gt == 256 ? g2p_occupancy<256>() : g2p_occupancy<128>();
+  d.grid_p2g = d.num_sms * (L.p2g_ctas_per_sm > 0 ? std::min(L.p2g_ctas_per_sm, a) : a);
+  d.grid_g2p = d.num_sms * (L.g2p_ctas_per_sm > 0 ? std::min(L.g2p_ctas_per_sm, g) : g);
+  d.grid_sort = d.num_sms * (L.sort_ctas_per_sm > 0 ? L.sort_ctas_per_sm : 8);
+  d.grid_stream = d.num_sms * (L.stream_ctas_per_sm > 0 ? L.stream_ctas_per_sm : 8);
+  d.g2p_threads = gt;
 }
 
 void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
@@ -639,23 +652,31 @@ void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
 }
 
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
-  k_grid_gather<<<d.num_sms * 8, 256, 0, s>>>(d, mode);
+  k_grid_gather<<<d.grid_stream, 256, 0, s>>>(d, mode);
 }
 
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {
   k_grid_update<<<d.num_sms * 8, 256, 0, s>>>(d, mode);
 }
 
-void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
+template <int NT>
+void launch_g2p_nt(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
   const int grid = d.grid_g2p;
   float *pi = d.pbuf[cur], *po = d.pbuf[1 - cur];
   int32_t *ii = d.ibuf[cur], *io = d.ibuf[1 - cur];
   if (fuse_rm && fuse_bin)
-    k_g2p<true, true><<<grid, kG2PThreads, 0, s>>>(d, pi, ii, po, io);
+    k_g2p<true, true, NT><<<grid, NT, 0, s>>>(d, pi, ii, po, io);
   else if (fuse_rm)
-    k_g2p<true, false><<<grid, kG2PThreads, 0, s>>>(d, pi, ii, po, io);
+    k_g2p<true, false, NT><<<grid, NT, 0, s>>>(d, pi, ii, po, io);
   else
-    k_g2p<false, false><<<grid, kG2PThreads, 0, s>>>(d, pi, ii, po, io);
+    k_g2p<false, false, NT><<<grid, NT, 0, s>>>(d, pi, ii, po, io);
+}
+
+void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
+  if (d.g2p_threads == 256)
+    launch_g2p_nt<256>(d, cur, fuse_rm, fuse_bin, s);
+  else
+    launch_g2p_nt<128>(d, cur, fuse_rm, fuse_bin, s);
 }
 
 void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s) {

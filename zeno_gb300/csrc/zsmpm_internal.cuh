@@ -93,6 +93,12 @@ struct SceneParams {
   long long p_off;  // first particle of the scene in upload order
 };
 
+// Launch shape of the persistent kernels (0 = default); picked by the
+// autotuner through mpm_set_launch_config.
+struct LaunchConfig {
+  int p2g_ctas_per_sm, g2p_ctas_per_sm, sort_ctas_per_sm, stream_ctas_per_sm, g2p_threads;
+};
+
 struct DevPtrs {
   float *pbuf[2];
   int32_t *ibuf[2];
@@ -117,6 +123,8 @@ struct DevPtrs {
   MatParams *mats;
   int num_sms;
   int grid_p2g, grid_g2p;  // persistent grids: SMs x resident CTAs per SM
+  int grid_sort, grid_stream, g2p_threads;
+  LaunchConfig launch;
 };
 
 // partition.cu

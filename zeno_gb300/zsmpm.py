@@ -50,6 +50,12 @@ class SceneDesc(C.Structure):
                 ("gravity", C.c_float * 3), ("boundary", Boundary)]
 
 
+class LaunchConfig(C.Structure):
+    _fields_ = [("p2g_ctas_per_sm", C.c_int32), ("g2p_ctas_per_sm", C.c_int32),
+                ("sort_ctas_per_sm", C.c_int32), ("stream_ctas_per_sm", C.c_int32),
+                ("g2p_threads", C.c_int32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_particle_blocks", C.c_int32),
                 ("n_grid_blocks", C.c_int32), ("max_vel_sqr", C.c_float), ("status", C.c_int32),
@@ -62,7 +68,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
-           "mpm_grid_download", "mpm_partition_noalloc"]
+           "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
+           "mpm_get_launch_config"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 
@@ -109,6 +116,8 @@ def load(path: str = LIB_PATH):
         "mpm_partition_download": ([P, P, P, P, i64, P, P, P, i64], i32),
         "mpm_grid_download": ([P, P, i64], i32),
         "mpm_partition_noalloc": ([P, i64, f32, P, P, P, P, P, i64, P, P], i32),
+        "mpm_set_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
+        "mpm_get_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -286,6 +295,15 @@ class Context:
 
     def sync(self):
         self._check(self._L.mpm_sync(self.h), "mpm_sync")
+
+    def set_launch_config(self, cfg: dict):
+        lc = LaunchConfig(*(int(cfg.get(k, 0)) for k, _ in LaunchConfig._fields_))
+        self._check(self._L.mpm_set_launch_config(self.h, C.byref(lc)), "mpm_set_launch_config")
+
+    def get_launch_config(self) -> dict:
+        lc = LaunchConfig()
+        self._check(self._L.mpm_get_launch_config(self.h, C.byref(lc)), "mpm_get_launch_config")
+        return {k: getattr(lc, k) for k, _ in LaunchConfig._fields_}
 
     def stats(self) -> dict:
         s = Stats()
