@@ -194,6 +194,25 @@ enum {
 };
 int32_t mpm_substep_timed(mpm_ctx *ctx, float dt, float *stage_ms, int32_t n_stages);
 
+/* ---- differentiable form (no counterpart in the reference) ----
+ * State / adjoint planes: 25 device float planes of n particles each, in
+ * upload order: x (3), v (3), C (9), F (9), J (1). */
+#define MPM_STATE_PLANES 25
+/* keep = 1: G2P writes every particle back to its own slot, so the particle
+ * store keeps the upload order and saved states / adjoints share it
+ * (required by the calls below). */
+int32_t mpm_set_order_mode(mpm_ctx *ctx, int32_t keep_upload_order);
+/* copy the current state to / from caller device memory (checkpoints) */
+int32_t mpm_state_save(mpm_ctx *ctx, float *dst_planes);
+int32_t mpm_state_load(mpm_ctx *ctx, const float *src_planes);
+/* Adjoint of the substep that advances the current state n with dt: given
+ * adj_next, the adjoint planes of state n+1, writes adj_prev, the adjoint
+ * planes of state n, and adds the gradients with respect to every
+ * particle's mu and lam to grad_mu / grad_lam (n floats each, device).  The
+ * state is not advanced.  Fixed-corotated and Neo-Hookean materials. */
+int32_t mpm_adjoint_substep(mpm_ctx *ctx, float dt, const float *adj_next, float *adj_prev,
+                            float *grad_mu, float *grad_lam);
+
 /* Launch shape of the persistent kernels, chosen by the autotuner
  * (zeno_gb300/autotune.py); 0 fields take the defaults (occupancy maximum for
  * P2G / G2P, 8 CTAs per SM for the sort and the streaming kernels).  The

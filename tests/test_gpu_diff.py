@@ -1,0 +1,113 @@
+"""Gradients of the differentiable rollout (hand-written adjoint with
+checkpointing and recomputation) against central finite differences: of the
+same GPU forward in FP32 (h = 1e-3) and of the FP64 oracle (h = 1e-6, the
+FP64 reference gradient).  Loss: squared distance of the final centre of mass
+to (0.7, 0.5, 0.5); parameters: per-particle initial velocity v0 and Young's
+modulus E (perturbed relatively: E (1 + h r), r in [0.5, 1.5]).  The block is
+thrown at the floor: 64 substeps take it into contact, where its stiffness
+moves the centre of mass (a free block's centre of mass does not depend on E)."""
+import numpy as np
+import pytest
+
+from zeno_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+TARGET = np.array([0.7, 0.5, 0.5])
+
+
+def _problem(cells=(16, 8, 8)):
+    scene, parts = S.diff_scene(cells=cells)
+    nu = scene.materials[0].nu
+    E = parts.mu.astype(np.float64) * 2.0 * (1.0 + nu)
+    v0 = np.tile([[0.3, -3.0, 0.1]], (parts.n, 1)) + 0.2 * S.normal(4, 0, parts.n * 3).reshape(-1, 3)
+    dv = np.tile([[1.0, 0.5, -0.3]], (parts.n, 1)) + 0.5 * S.normal(5, 0, parts.n * 3).reshape(-1, 3)
+    rE = 0.5 + S.uniform(6, 0, parts.n)
+    return scene, parts, E, v0, dv, rE
+
+
+def _gpu_grads(scene, parts, E, v0, steps, ckpt):
+    import torch
+    from zeno_gb300 import diff
+    sim = diff.Rollout(scene, parts, steps, ckpt)
+    v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+    e = torch.tensor(E, dtype=torch.float64, device="cuda", requires_grad=True)
+    L = diff.com_loss(sim.rollout(v, e), TARGET)
+    L.backward()
+    return sim, float(L.detach()), v.grad.double().cpu().numpy(), e.grad.double().cpu().numpy()
+
+
+def _gpu_loss(sim, v0, E):
+    import torch
+    from zeno_gb300 import diff
+    with torch.no_grad():
+        x = sim.rollout(torch.tensor(v0, dtype=torch.float32, device="cuda"),
+                        torch.tensor(E, dtype=torch.float64, device="cuda"))
+        return float(diff.com_loss(x, TARGET))
+
+
+def _oracle_loss(oracle_mod, scene, parts, v0, E, steps):
+    p = parts.copy(dtype=np.float64)
+    p.v = np.asarray(v0, np.float64)
+    mu, lam = S.lame(np.asarray(E, np.float64), scene.materials[0].nu)
+    p.mu, p.lam = mu, lam
+    out, st = oracle_mod.run(scene, p, steps, "f64")
+    assert st["status"] == 0
+    return float(((out.x.mean(axis=0) - TARGET) ** 2).sum())
+
+
+def test_gradients_against_fp32_finite_differences(zsmpm_mod):
+    scene, parts, E, v0, dv, rE = _problem()
+    steps = 64
+    sim, L, gv, gE = _gpu_grads(scene, parts, E, v0, steps, 16)
+    h = 1e-3
+    fd_v = (_gpu_loss(sim, v0 + h * dv, E) - _gpu_loss(sim, v0 - h * dv, E)) / (2 * h)
+    ad_v = float((gv * dv).sum())
+    assert abs(ad_v - fd_v) <= 2e-3 * abs(fd_v), (ad_v, fd_v)
+    h = 1e-2  # the loss moves by ~1e-6 per percent of E: a larger step than for v0
+    fd_E = (_gpu_loss(sim, v0, E * (1 + h * rE)) - _gpu_loss(sim, v0, E * (1 - h * rE))) / (2 * h)
+    ad_E = float((gE * E * rE).sum())
+    assert abs(ad_E - fd_E) <= 5e-2 * abs(fd_E) + 1e-12, (ad_E, fd_E)
+
+
+def test_gradients_against_fp64_reference(zsmpm_mod, oracle_mod):
+    scene, parts, E, v0, dv, rE = _problem()
+    steps = 64
+    _, L, gv, gE = _gpu_grads(scene, parts, E, v0, steps, 16)
+    h = 1e-6
+    ref_v = (_oracle_loss(oracle_mod, scene, parts, v0 + h * dv, E, steps) -
+             _oracle_loss(oracle_mod, scene, parts, v0 - h * dv, E, steps)) / (2 * h)
+    ad_v = float((gv * dv).sum())
+    assert abs(ad_v - ref_v) <= 1e-3 * abs(ref_v), (ad_v, ref_v)
+    ref_E = (_oracle_loss(oracle_mod, scene, parts, v0, E * (1 + h * rE), steps) -
+             _oracle_loss(oracle_mod, scene, parts, v0, E * (1 - h * rE), steps)) / (2 * h)
+    ad_E = float((gE * E * rE).sum())
+    assert abs(ad_E - ref_E) <= 1e-2 * abs(ref_E) + 1e-12, (ad_E, ref_E)
+
+
+def test_checkpoint_interval_does_not_change_gradients(zsmpm_mod):
+    scene, parts, E, v0, _, _ = _problem(cells=(8, 8, 8))
+    a = _gpu_grads(scene, parts, E, v0, 24, 4)
+    b = _gpu_grads(scene, parts, E, v0, 24, 24)
+    np.testing.assert_array_equal(a[2], b[2])
+    np.testing.assert_array_equal(a[3], b[3])
+
+
+def test_forward_matches_plain_substeps(zsmpm_mod):
+    """The rollout's forward (upload-order mode) equals the plain substep."""
+    import torch
+    from zeno_gb300 import diff
+    scene, parts, E, v0, _, _ = _problem(cells=(8, 8, 8))
+    sim = diff.Rollout(scene, parts, 20, 5)
+    with torch.no_grad():
+        x = sim.rollout(torch.tensor(v0, dtype=torch.float32, device="cuda"),
+                        torch.tensor(E, device="cuda")).cpu().numpy()
+    p = parts.copy()
+    p.v = v0.astype(np.float32)
+    mu, lam = S.lame(E, scene.materials[0].nu)
+    p.mu, p.lam = mu.astype(np.float32), lam.astype(np.float32)
+    with zsmpm_mod.Context(scene, max_particles=p.n) as ctx:
+        ctx.upload(p)
+        ctx.substep(scene.dt, 20)
+        ref = ctx.download()["x"]
+    np.testing.assert_allclose(x, ref, rtol=0, atol=2e-6)

@@ -1,0 +1,402 @@
+// Adjoint of one substep (the differentiable form; the reference has none).
+//
+// Forward substep n (particles x, v, C, F; grid nodes i):
+//   P2G   m_i = sum_p W m_p,  mv_i = sum_p W (m_p v_p + A_p (x_i - x_p)),
+//         A_p = m_p C_p - dt Dinv vol_p tau(F_p)
+//   grid  v_i = BC(mv_i / m_i + g dt)
+//   G2P   v' = sum_i W v_i,  C' = Dinv sum_i W v_i (x_i - x_p)^T,
+//         x' = x + dt v',  F' = (I + dt C') F
+// Given the adjoints (x', v', C', F')-bar of the next state, the three
+// kernels here produce the adjoints of this state and of mu, lam:
+//   k_g2p_adjoint   per particle block: recomputes G2P, forms
+//                   Cb = C'b + dt F'b F^T, vb = v'b + dt x'b, F-bar = (I + dt C')^T F'b,
+//                   x-bar through the weights, and scatters the node adjoint
+//                   v_i-bar += W (vb + Dinv Cb (x_i - x_p)) into tiles
+//                   (tile_scatter: deterministic, no atomics)
+//   k_grid_adjoint  per node: the tiles' sum, the boundary's transpose, then
+//                   mv_i-bar = v-bar / m_i, m_i-bar = -v-bar . mv_i / m_i^2
+//   k_p2g_adjoint   per particle block: gathers (m-bar, mv-bar) of the 216
+//                   nodes: v-bar = m sum W mv-bar, A-bar = sum W mv-bar (x_i - x_p)^T,
+//                   C-bar = m A-bar, tau-bar = -dt Dinv vol A-bar through the
+//                   stress adjoint, x-bar through the weights and (x_i - x_p)
+// The particles stay in upload order in the differentiable mode, so every
+// state and adjoint array shares one indexing.
+#include <cuda_runtime.h>
+
+#include "binning.cuh"
+#include "mpm_math.cuh"
+#include "tile_scatter.cuh"
+#include "zsmpm_internal.cuh"
+
+namespace zsmpm {
+namespace {
+
+// adjoint planes (n each): x 3, v 3, C 9, F 9, J 1
+enum : int { AJ_X = 0, AJ_V = 3, AJ_C = 6, AJ_F = 15, AJ_J = 24, NAJ = 25 };
+
+__device__ __forceinline__ void origin_of(const SceneParams &S, int ldir, int (&K)[3]) {
+  const int dz = S.block_dims[2], dy = S.block_dims[1];
+  K[0] = ((ldir / (dz * dy)) + S.block_lo[0]) * 4;
+  K[1] = (((ldir / dz) % dy) + S.block_lo[1]) * 4;
+  K[2] = ((ldir % dz) + S.block_lo[2]) * 4;
+}
+
+__device__ __forceinline__ int gb_of(const DevPtrs &d, const SceneParams &S, int dir, int t) {
+  const int dz = S.block_dims[2], dy = S.block_dims[1];
+  return d.dir_gb[dir + ((t >> 2) * dy + ((t >> 1) & 1)) * dz + (t & 1)];
+}
+
+// 216 node float4 staged after the tile smem, at a 16-byte boundary
+constexpr int kAdjSgOffset = (kP2GSmem + 15) & ~15;
+constexpr int kAdjSmem = kAdjSgOffset + kNodes * 16;
+static_assert(kAdjSgOffset % 16 == 0, "float4 staging must be 16-byte aligned");
+
+__global__ void __launch_bounds__(kP2GThreads)
+    k_g2p_adjoint(DevPtrs d, const float *__restrict__ pin, const float *__restrict__ an,
+                  float *__restrict__ ap, long long n) {
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  const TileSmem ts = tile_smem(adj_smem);
+  float4 *sg = reinterpret_cast<float4 *>(adj_smem + kAdjSgOffset);
+  __shared__ int sgb[8];
+  const SimParams &P = *d.prm;
+  const long long cap = d.cap;
+  const float dt = P.dt;
+  const int nb = d.cnt->n_buckets;
+  const int tid = threadIdx.x;
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    tile_zero(ts);
+    const int dir = d.bk_dir[b];
+    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
+    const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
+    if (tid < 8) sgb[tid] = gb_of(d, S, dir, tid);
+    int K[3];
+    origin_of(S, dir - S.dir_off, K);
+    __syncthreads();
+    for (int nd = tid; nd < kNodes; nd += kP2GThreads) {
+      const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
+      const int gb = sgb[((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2)];
+      const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
+      sg[nd] = gb >= 0 ? d.grid[(long long)gb * 64 + cell] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const int start = d.bk_start[b];
+    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
+    for (int c0 = 0; c0 < cnt; c0 += kP2GChunk) {
+      const int nc = min(kP2GChunk, cnt - c0);
+      __syncthreads();
+      for (int j = tid; j < nc; j += kP2GThreads) {
+        const int p = d.perm[start + c0 + j];
+        float x[3], F[9], xb[3], vb[3], Cb[9], Fb[9];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          x[k] = pin[(CH_X + k) * cap + p];
+          xb[k] = an[(AJ_X + k) * n + p];
+          vb[k] = an[(AJ_V + k) * n + p] + dt * xb[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          F[k] = pin[(CH_F + k) * cap + p];
+          Fb[k] = an[(AJ_F + k) * n + p];
+          Cb[k] = an[(AJ_C + k) * n + p];
+        }
+        // C'b += dt F'b F^T
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Cb[r * 3 + c] += dt * (Fb[r * 3] * F[c * 3] + Fb[r * 3 + 1] * F[c * 3 + 1] +
+                                   Fb[r * 3 + 2] * F[c * 3 + 2]);
+        const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
+                       s2 = stencil1(x[2], inv_dx);
+        const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
+        float dw0[3], dw1[3], dw2[3];
+        stencil_dw(s0.f, dw0);
+        stencil_dw(s1.f, dw1);
+        stencil_dw(s2.f, dw2);
+        float Cn[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float gx[3] = {0.f, 0.f, 0.f};
+        const bool inside = (unsigned)l0 <= 3u && (unsigned)l1 <= 3u && (unsigned)l2 <= 3u;
+        if (!inside) atomicOr(&d.cnt->status, ST_STENCIL);
+        if (inside) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk) {
+                const float4 g4 = sg[((l0 + i) * 6 + (l1 + jj)) * 6 + (l2 + kk)];
+                const float g[3] = {g4.y, g4.z, g4.w};
+                const float W = s0.w[i] * s1.w[jj] * s2.w[kk];
+                const float dW[3] = {dw0[i] * s1.w[jj] * s2.w[kk] * inv_dx,
+                                     s0.w[i] * dw1[jj] * s2.w[kk] * inv_dx,
+                                     s0.w[i] * s1.w[jj] * dw2[kk] * inv_dx};
+                const float xx[3] = {((float)i - s0.f) * dx, ((float)jj - s1.f) * dx,
+                                     ((float)kk - s2.f) * dx};
+                float Cx[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                  Cx[a] = Cb[a * 3] * xx[0] + Cb[a * 3 + 1] * xx[1] + Cb[a * 3 + 2] * xx[2];
+                const float s = g[0] * vb[0] + g[1] * vb[1] + g[2] * vb[2] +
+                                Dinv * (g[0] * Cx[0] + g[1] * Cx[1] + g[2] * Cx[2]);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                  // forward C', then x-bar via dW and via (x_i - x_p)
+                  Cn[a * 3 + 0] += W * g[a] * xx[0];
+                  Cn[a * 3 + 1] += W * g[a] * xx[1];
+                  Cn[a * 3 + 2] += W * g[a] * xx[2];
+                  const float CTg = Cb[0 * 3 + a] * g[0] + Cb[1 * 3 + a] * g[1] + Cb[2 * 3 + a] * g[2];
+                  gx[a] += dW[a] * s - Dinv * W * CTg;
+                }
+              }
+        }
+        // F-bar = (I + dt C')^T F'b
+        float Fbn[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Fbn[r * 3 + c] = Fb[r * 3 + c] + dt * Dinv *
+                                                 (Cn[0 * 3 + r] * Fb[0 * 3 + c] +
+                                                  Cn[1 * 3 + r] * Fb[1 * 3 + c] +
+                                                  Cn[2 * 3 + r] * Fb[2 * 3 + c]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ap[(AJ_X + k) * n + p] = xb[k] + gx[k];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) ap[(AJ_F + k) * n + p] = Fbn[k];
+        // node scatter of W (vb + Dinv Cb (x_i - x_p)): b = vb - dx A f, A = Dinv Cb
+        float A[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] = inside ? Dinv * Cb[k] : 0.0f;
+        const float f[3] = {s0.f, s1.f, s2.f};
+        float bv[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          bv[a] = inside ? vb[a] - dx * (A[a * 3] * f[0] + A[a * 3 + 1] * f[1] + A[a * 3 + 2] * f[2])
+                         : 0.0f;
+        tile_stage(ts, j, 0.0f, bv, A, f, d.pkey[p] & 63);
+      }
+      __syncthreads();
+      tile_cell_ranges(ts, nc);
+      __syncthreads();
+      tile_scatter(ts, dx);
+    }
+    __syncthreads();
+    tile_store(ts, d.ptile_adj + (long long)b * kTileNodes);
+    __syncthreads();
+  }
+}
+
+// per grid node: v-bar from the adjoint tiles; m, mv from the forward tiles
+__global__ void k_grid_adjoint(DevPtrs d) {
+  const SimParams &P = *d.prm;
+  const long long nn = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nn;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
+    const int gdir = d.gb_dir[gb];
+    const SceneParams &S = d.scn[scene_of_dir(d, gdir)];
+    const int dy = S.block_dims[1], dz = S.block_dims[2];
+    const int ldir = gdir - S.dir_off;
+    const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
+    const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
+    float4 fw = make_float4(0.f, 0.f, 0.f, 0.f), ad = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
+      if ((o0 && (l0 >= 2 || c0 < 1)) || (o1 && (l1 >= 2 || c1 < 1)) ||
+          (o2 && (l2 >= 2 || c2 < 1)))
+        continue;
+      const int bk = d.dir_bk[gdir - (o0 * dy + o1) * dz - o2];
+      if (bk < 0) continue;
+      const long long t = (long long)bk * kTileNodes +
+                          ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2);
+      const float4 a = d.ptile[t], c = d.ptile_adj[t];
+      fw.x += a.x;
+      fw.y += a.y;
+      fw.z += a.z;
+      fw.w += a.w;
+      ad.y += c.y;
+      ad.z += c.z;
+      ad.w += c.w;
+    }
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (fw.x != 0.0f) {
+      const float r = 1.0f / fw.x;
+      const float vp[3] = {fw.y * r + S.gravity[0] * P.dt, fw.z * r + S.gravity[1] * P.dt,
+                           fw.w * r + S.gravity[2] * P.dt};
+      float vb[3] = {ad.y, ad.z, ad.w};
+      if (S.bc_type != MPM_BC_NONE) {
+        const int I[3] = {(c0 + S.block_lo[0]) * 4 + l0, (c1 + S.block_lo[1]) * 4 + l1,
+                          (c2 + S.block_lo[2]) * 4 + l2};
+        bool any = false;
+        const int th = S.bc_thickness;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const bool lower = I[a] < S.bc_lo[a] + th, upper = I[a] > S.bc_hi[a] - th;
+          if (!(lower || upper)) continue;
+          any = true;
+          if (S.bc_type == MPM_BC_SLIP) vb[a] = 0.0f;
+          if (S.bc_type == MPM_BC_SEPARATE && ((lower && vp[a] < 0.0f) || (upper && vp[a] > 0.0f)))
+            vb[a] = 0.0f;
+        }
+        if (any && S.bc_type == MPM_BC_STICKY) vb[0] = vb[1] = vb[2] = 0.0f;
+      }
+      out.y = vb[0] * r;
+      out.z = vb[1] * r;
+      out.w = vb[2] * r;
+      out.x = -(vb[0] * fw.y + vb[1] * fw.z + vb[2] * fw.w) * r * r;
+    }
+    d.grid[idx] = out;  // (m-bar, mv-bar)
+  }
+}
+
+constexpr int kP2GAdjThreads = 128;
+
+__global__ void __launch_bounds__(kP2GAdjThreads)
+    k_p2g_adjoint(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
+                  float *__restrict__ ap, float *__restrict__ gmu, float *__restrict__ glam,
+                  long long n) {
+  __shared__ float4 sg[kNodes];
+  __shared__ int sgb[8];
+  const SimParams &P = *d.prm;
+  const long long cap = d.cap;
+  const float dt = P.dt;
+  const int nb = d.cnt->n_buckets;
+  const bool lame = P.has_lame != 0;
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const int dir = d.bk_dir[b];
+    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
+    const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
+    if (threadIdx.x < 8) sgb[threadIdx.x] = gb_of(d, S, dir, threadIdx.x);
+    int K[3];
+    origin_of(S, dir - S.dir_off, K);
+    __syncthreads();
+    for (int nd = threadIdx.x; nd < kNodes; nd += kP2GAdjThreads) {
+      const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
+      const int gb = sgb[((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2)];
+      const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
+      sg[nd] = gb >= 0 ? d.grid[(long long)gb * 64 + cell] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const int start = d.bk_start[b];
+    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
+    for (int s = start + threadIdx.x; s < start + cnt; s += kP2GAdjThreads) {
+      const int p = d.perm[s];
+      const MatParams mp = d.mats[min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1)];
+      float x[3], v[3], C[9], F[9], Sv[6];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        x[k] = pin[(CH_X + k) * cap + p];
+        v[k] = pin[(CH_V + k) * cap + p];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        C[k] = pin[(CH_C + k) * cap + p];
+        F[k] = pin[(CH_F + k) * cap + p];
+      }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Sv[k] = pin[(CH_S + k) * cap + p];
+      const float mass = pin[CH_M * cap + p], vol = pin[CH_VOL * cap + p];
+      float mu = mp.mu, lam = mp.lam;
+      if (lame) {
+        mu = pin[CH_MU * cap + p];
+        lam = pin[CH_LAM * cap + p];
+      }
+      const float kk = -dt * Dinv;
+      const float A[9] = {mass * C[0] + kk * Sv[0], mass * C[1] + kk * Sv[3],
+                          mass * C[2] + kk * Sv[4], mass * C[3] + kk * Sv[3],
+                          mass * C[4] + kk * Sv[1], mass * C[5] + kk * Sv[5],
+                          mass * C[6] + kk * Sv[4], mass * C[7] + kk * Sv[5],
+                          mass * C[8] + kk * Sv[2]};
+      const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
+                     s2 = stencil1(x[2], inv_dx);
+      const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
+      float dw0[3], dw1[3], dw2[3];
+      stencil_dw(s0.f, dw0);
+      stencil_dw(s1.f, dw1);
+      stencil_dw(s2.f, dw2);
+      float vbar[3] = {0.f, 0.f, 0.f}, Ab[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float gx[3] = {0.f, 0.f, 0.f};
+      if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u) {
+        atomicOr(&d.cnt->status, ST_STENCIL);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const float4 g4 = sg[((l0 + i) * 6 + (l1 + jj)) * 6 + (l2 + q)];
+              const float mb = g4.x, gb3[3] = {g4.y, g4.z, g4.w};
+              const float W = s0.w[i] * s1.w[jj] * s2.w[q];
+              const float dW[3] = {dw0[i] * s1.w[jj] * s2.w[q] * inv_dx,
+                                   s0.w[i] * dw1[jj] * s2.w[q] * inv_dx,
+                                   s0.w[i] * s1.w[jj] * dw2[q] * inv_dx};
+              const float xx[3] = {((float)i - s0.f) * dx, ((float)jj - s1.f) * dx,
+                                   ((float)q - s2.f) * dx};
+              float u = mb * mass;  // d(m_i)/dW m-bar + mv-bar . (m v + A xx)
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                const float val = mass * v[a] + A[a * 3] * xx[0] + A[a * 3 + 1] * xx[1] +
+                                  A[a * 3 + 2] * xx[2];
+                u += gb3[a] * val;
+                vbar[a] += W * gb3[a];
+                Ab[a * 3 + 0] += W * gb3[a] * xx[0];
+                Ab[a * 3 + 1] += W * gb3[a] * xx[1];
+                Ab[a * 3 + 2] += W * gb3[a] * xx[2];
+              }
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                const float ATg = A[0 * 3 + a] * gb3[0] + A[1 * 3 + a] * gb3[1] + A[2 * 3 + a] * gb3[2];
+                gx[a] += dW[a] * u - W * ATg;
+              }
+            }
+      }
+      // tau-bar = -dt Dinv vol A-bar; stress adjoint
+      float tb[9], Fb[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        tb[k] = -dt * Dinv * vol * Ab[k];
+        Fb[k] = ap[(AJ_F + k) * n + p];
+      }
+      float mub = 0.f, lamb = 0.f;
+      if (mp.type == MPM_FCR)
+        fcr_vjp(mu, lam, F, tb, Fb, mub, lamb);
+      else if (mp.type == MPM_NHK)
+        nhk_vjp(mu, lam, F, tb, Fb, mub, lamb);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ap[(AJ_X + k) * n + p] += gx[k];
+        ap[(AJ_V + k) * n + p] = mass * vbar[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        ap[(AJ_C + k) * n + p] = mass * Ab[k];
+        ap[(AJ_F + k) * n + p] = Fb[k];
+      }
+      ap[AJ_J * n + p] = 0.0f;
+      gmu[p] += mub;
+      glam[p] += lamb;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, long long n,
+                        cudaStream_t s) {
+  cudaFuncSetAttribute(k_g2p_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmem);
+  k_g2p_adjoint<<<d.num_sms * 2, kP2GThreads, kAdjSmem, s>>>(d, d.pbuf[cur], an, ap, n);
+}
+
+void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s) {
+  k_grid_adjoint<<<d.num_sms * 8, 256, 0, s>>>(d);
+}
+
+void launch_p2g_adjoint(const DevPtrs &d, int cur, float *ap, float *gmu, float *glam, long long n,
+                        cudaStream_t s) {
+  k_p2g_adjoint<<<d.num_sms * 4, kP2GAdjThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur], ap, gmu,
+                                                        glam, n);
+}
+
+}  // namespace zsmpm

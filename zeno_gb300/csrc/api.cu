@@ -58,6 +58,7 @@ struct mpm_ctx {
   cudaEvent_t events[MPM_NUM_STAGES + 1] = {};
   std::vector<SceneParams> scenes;
   int n_materials = 0;
+  bool differentiable = false;  // every material has an adjoint
 };
 
 namespace {
@@ -403,6 +404,11 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
                           cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   c->n_materials = n;
+  c->differentiable = true;
+  for (int i = 0; i < n; ++i)
+    if (!((mats[i].type == MPM_FCR || mats[i].type == MPM_NHK) &&
+          mats[i].plasticity == MPM_PLASTIC_NONE))
+      c->differentiable = false;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
   if (c->prm.n > 0) {  // stored stresses follow the new parameters
@@ -731,6 +737,77 @@ int32_t mpm_get_launch_config(mpm_ctx *c, mpm_launch_config *cfg) {
   cfg->sort_ctas_per_sm = d.grid_sort / d.num_sms;
   cfg->stream_ctas_per_sm = d.grid_stream / d.num_sms;
   cfg->g2p_threads = d.g2p_threads;
+  return MPM_OK;
+}
+
+int32_t mpm_set_order_mode(mpm_ctx *c, int32_t keep) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (keep && !c->d.ptile_adj && (rc = dalloc(c, &c->d.ptile_adj, (size_t)c->d.cap_gblocks * kTileNodes)))
+    return rc;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->d.keep_order = keep ? 1 : 0;
+  for (int k = 0; k < 2; ++k)  // the graphs hold the old G2P output indexing
+    if (c->graph[k]) {
+      cudaGraphExecDestroy(c->graph[k]);
+      c->graph[k] = nullptr;
+    }
+  return MPM_OK;
+}
+
+int32_t mpm_state_save(mpm_ctx *c, float *dst) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->d.keep_order) return fail(MPM_ERR_STATE, "state copies need mpm_set_order_mode(ctx, 1)");
+  if (!dst) return fail(MPM_ERR_INVALID, "null destination");
+  const size_t n = (size_t)c->prm.n;
+  if (n == 0) return MPM_OK;
+  ZS_CUDA(cudaMemcpy2DAsync(dst, n * sizeof(float), c->d.pbuf[c->cur], c->d.cap * sizeof(float),
+                            n * sizeof(float), MPM_STATE_PLANES, cudaMemcpyDeviceToDevice,
+                            c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_state_load(mpm_ctx *c, const float *src) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->d.keep_order) return fail(MPM_ERR_STATE, "state copies need mpm_set_order_mode(ctx, 1)");
+  if (!src) return fail(MPM_ERR_INVALID, "null source");
+  const size_t n = (size_t)c->prm.n;
+  if (n == 0) return MPM_OK;
+  ZS_CUDA(cudaMemcpy2DAsync(c->d.pbuf[c->cur], c->d.cap * sizeof(float), src, n * sizeof(float),
+                            n * sizeof(float), MPM_STATE_PLANES, cudaMemcpyDeviceToDevice,
+                            c->stream));
+  if ((rc = push_params(c))) return rc;
+  launch_stress(c->d, c->cur, c->stream);
+  if ((rc = launch_check("state load"))) return rc;
+  c->needs_full_clear = true;  // the directory counts described the old positions
+  c->binned = false;
+  c->partition_valid = false;
+  return MPM_OK;
+}
+
+int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *adj_prev,
+                            float *grad_mu, float *grad_lam) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->d.keep_order) return fail(MPM_ERR_STATE, "the adjoint needs mpm_set_order_mode(ctx, 1)");
+  if (!adj_next || !adj_prev || !grad_mu || !grad_lam)
+    return fail(MPM_ERR_INVALID, "null adjoint buffer");
+  if (!c->differentiable)
+    return fail(MPM_ERR_INVALID,
+                "the adjoint covers fixed-corotated and Neo-Hookean materials without plasticity");
+  if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
+  enqueue_bin_if_needed(c);
+  enqueue_sort(c);
+  launch_p2g(c->d, c->cur, c->stream);
+  launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
+  const long long n = c->prm.n;
+  launch_g2p_adjoint(c->d, c->cur, adj_next, adj_prev, n, c->stream);
+  launch_grid_adjoint(c->d, c->stream);
+  launch_p2g_adjoint(c->d, c->cur, adj_prev, grad_mu, grad_lam, n, c->stream);
+  if ((rc = launch_check("adjoint substep"))) return rc;
+  c->partition_valid = true;
   return MPM_OK;
 }
 

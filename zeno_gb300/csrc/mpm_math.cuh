@@ -244,3 +244,148 @@ __device__ __forceinline__ Stencil1 stencil1(float x, float inv_dx) {
 }
 
 }  // namespace zsmpm
+
+namespace zsmpm {
+
+// ---------------------------------------------------------------------------
+// Adjoints (vector-Jacobian products) of the Kirchhoff stresses.
+
+__device__ __forceinline__ void cofactor3(const float (&F)[9], float (&c)[9]) {
+  c[0] = F[4] * F[8] - F[5] * F[7];
+  c[1] = F[5] * F[6] - F[3] * F[8];
+  c[2] = F[3] * F[7] - F[4] * F[6];
+  c[3] = F[2] * F[7] - F[1] * F[8];
+  c[4] = F[0] * F[8] - F[2] * F[6];
+  c[5] = F[1] * F[6] - F[0] * F[7];
+  c[6] = F[1] * F[5] - F[2] * F[4];
+  c[7] = F[2] * F[3] - F[0] * F[5];
+  c[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// Fixed corotated, tau = 2mu (F F^T - R F^T) + lam (J^2 - J) I.  Given the
+// adjoint tb of tau (3x3), adds to Fb, mub, lamb:
+//   Fb += 2mu (tb F + tb^T F - tb^T R - dR^T[tb F]) + lam (2J - 1) tr(tb) cof(F)
+//   mub += 2 <tb, F F^T - R F^T>,  lamb += tr(tb) (J^2 - J)
+// where dR^T[G] = [K ax(G R^T)]x R is the adjoint of the derivative of the
+// polar rotation (F = R S: R^T dR = [w]x with (tr(S) I - S) w = ax(R^T dF),
+// ax(M) = (M21 - M12, M02 - M20, M10 - M01)), and K = U diag(1 / (tr s^ - s^_i))
+// U^T in the frame of B = F F^T = U S^2 U^T, s^ the sign-fixed singular values.
+__device__ __forceinline__ void fcr_vjp(float mu, float lam, const float (&F)[9],
+                                        const float (&tb)[9], float (&Fb)[9], float &mub,
+                                        float &lamb) {
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  const float J = 1.0f + Jm1;
+  float w[3], Q[9];
+  sym_eig3(E, w, Q);
+  float s[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) s[k] = sqrtf(1.0f + fmaxf(w[k], -1.0f));
+  if (J < 0.0f) {
+    const int kmin = (s[0] <= s[1] && s[0] <= s[2]) ? 0 : ((s[1] <= s[2]) ? 1 : 2);
+    s[kmin] = -s[kmin];
+  }
+  // R = U diag(1/s^) U^T F,  R F^T = U diag(s^) U^T
+  const Sym3 Ui = qdqt(Q, 1.0f / s[0], 1.0f / s[1], 1.0f / s[2]);
+  const float Uim[9] = {Ui.xx, Ui.xy, Ui.xz, Ui.xy, Ui.yy, Ui.yz, Ui.xz, Ui.yz, Ui.zz};
+  float R[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      R[i * 3 + j] = Uim[i * 3] * F[j] + Uim[i * 3 + 1] * F[3 + j] + Uim[i * 3 + 2] * F[6 + j];
+  const Sym3 RFt = qdqt(Q, s[0], s[1], s[2]);
+  const float ts = s[0] + s[1] + s[2];
+  const Sym3 Kl = qdqt(Q, 1.0f / (ts - s[0]), 1.0f / (ts - s[1]), 1.0f / (ts - s[2]));
+  // G = tb F, M = G R^T
+  float G[9], M[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      G[i * 3 + j] = tb[i * 3] * F[j] + tb[i * 3 + 1] * F[3 + j] + tb[i * 3 + 2] * F[6 + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      M[i * 3 + j] = G[i * 3] * R[j * 3] + G[i * 3 + 1] * R[j * 3 + 1] + G[i * 3 + 2] * R[j * 3 + 2];
+  const float a0 = M[7] - M[5], a1 = M[2] - M[6], a2 = M[3] - M[1];
+  const float g0 = Kl.xx * a0 + Kl.xy * a1 + Kl.xz * a2;
+  const float g1 = Kl.xy * a0 + Kl.yy * a1 + Kl.yz * a2;
+  const float g2 = Kl.xz * a0 + Kl.yz * a1 + Kl.zz * a2;
+  // [g]x R
+  float gR[9];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    gR[0 * 3 + j] = -g2 * R[3 + j] + g1 * R[6 + j];
+    gR[1 * 3 + j] = g2 * R[j] - g0 * R[6 + j];
+    gR[2 * 3 + j] = -g1 * R[j] + g0 * R[3 + j];
+  }
+  float cof[9];
+  cofactor3(F, cof);
+  const float trtb = tb[0] + tb[4] + tb[8];
+  const float cj = lam * (2.0f * J - 1.0f) * trtb;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float tTF = 0.f, tTR = 0.f;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        tTF += tb[k * 3 + i] * F[k * 3 + j];
+        tTR += tb[k * 3 + i] * R[k * 3 + j];
+      }
+      Fb[i * 3 + j] += 2.0f * mu * (G[i * 3 + j] + tTF - tTR - gR[i * 3 + j]) + cj * cof[i * 3 + j];
+    }
+  // B - R F^T with B = F F^T = I + E
+  const float D[9] = {E.xx + 1.0f - RFt.xx, E.xy - RFt.xy, E.xz - RFt.xz,
+                      E.xy - RFt.xy, E.yy + 1.0f - RFt.yy, E.yz - RFt.yz,
+                      E.xz - RFt.xz, E.yz - RFt.yz, E.zz + 1.0f - RFt.zz};
+  float dot = 0.f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) dot += tb[k] * D[k];
+  mub += 2.0f * dot;
+  lamb += trtb * Jm1 * J;
+}
+
+// Neo-Hookean, tau = mu (F F^T - I) + lam ln(J) I:
+//   Fb += mu (tb + tb^T) F + lam tr(tb) F^-T,  mub += <tb, B - I>,
+//   lamb += tr(tb) ln J
+__device__ __forceinline__ void nhk_vjp(float mu, float lam, const float (&F)[9],
+                                        const float (&tb)[9], float (&Fb)[9], float &mub,
+                                        float &lamb) {
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  const float J = 1.0f + Jm1;
+  float cof[9];
+  cofactor3(F, cof);
+  const float trtb = tb[0] + tb[4] + tb[8];
+  const float cj = lam * trtb / J;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float v = 0.f;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) v += (tb[i * 3 + k] + tb[k * 3 + i]) * F[k * 3 + j];
+      Fb[i * 3 + j] += mu * v + cj * cof[i * 3 + j];
+    }
+  const float Em[9] = {E.xx, E.xy, E.xz, E.xy, E.yy, E.yz, E.xz, E.yz, E.zz};
+  float dot = 0.f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) dot += tb[k] * Em[k];
+  mub += dot;
+  lamb += trtb * log1pf(Jm1);
+}
+
+// dw/df of the quadratic B-spline weights (per axis): w0' = f - 1.5,
+// w1' = -2 (f - 1), w2' = f - 0.5
+__device__ __forceinline__ void stencil_dw(float f, float (&dw)[3]) {
+  dw[0] = f - 1.5f;
+  dw[1] = -2.0f * (f - 1.0f);
+  dw[2] = f - 0.5f;
+}
+
+}  // namespace zsmpm

@@ -24,12 +24,12 @@
 
 #include "binning.cuh"
 #include "mpm_math.cuh"
+#include "tile_scatter.cuh"
 #include "zsmpm_internal.cuh"
 
 namespace zsmpm {
 namespace {
 
-constexpr int kNodes = 216;  // 6^3
 
 // node index of the first node of the particle block at (scene-local)
 // directory index `ldir`
@@ -49,70 +49,33 @@ __device__ __forceinline__ int neighbour_gb(const DevPtrs &d, const SceneParams 
   return d.dir_gb[dir + ((t >> 2) * dy + ((t >> 1) & 1)) * dz + (t & 1)];
 }
 
-// P2G of one particle block (ZSParticleToZSGrid::p2g_apic, Transfer.cu:849-889).
-//  phase 1: per particle, the affine matrix A = m C - dt Dinv S (S = vol tau
-//           from the previous G2P); the momentum of stencil offset o
-//           (node - x = (o - f) dx) is W (m v + A (o - f) dx) = W (b + A o dx)
-//           with b = m v - dx A f, so phase 1 stores (m, b, A, f) per particle.
-//  phase 2: warp w takes cells w, w + 8, ..., w + 56 (three at a time, one
-//           per 9-lane slot); the particles of a cell are a contiguous range
-//           (sorted by cell).  Lane (slot, i, j) owns the three stencil nodes
-//           (i, j, 0..2) of its slot's cell: one weight product w_i w_j serves
-//           three nodes.  Sums go to the warp's private node array, slot by
-//           slot, so no two lanes ever update one word at the same time.
-//  reduce:  the 8 warp arrays are added per node in warp order and stored as
-//           the block's tile.  No atomics: the tile is reproducible bit for bit.
-constexpr int kP2GThreads = 256;
-constexpr int kP2GWarps = kP2GThreads / 32;
-constexpr int kP2GChunk = 384;
-constexpr int kP2GSpdBytes = 4 * kP2GChunk * 16;
-constexpr int kP2GAccBytes = kP2GWarps * 4 * kNodes * 4;
-constexpr int kP2GSmem = kP2GSpdBytes + kP2GAccBytes + 65 * 4 + kP2GChunk;
-
+// P2G of one particle block (ZSParticleToZSGrid::p2g_apic, Transfer.cu:849-889):
+// per particle the affine matrix A = m C - dt Dinv S (S = vol tau from the
+// previous G2P); the momentum of stencil node o is W (m v + A (o - f) dx) =
+// W (b + A o dx) with b = m v - dx A f.  The block's particles are staged and
+// scattered into its 216-node tile by tile_scatter (tile_scatter.cuh).
 __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__restrict__ pin,
                                                      const int32_t *__restrict__ iin) {
-  // dynamic shared memory (kP2GSmem bytes):
-  //   spd   4 x kP2GChunk float4: (m,b0,b1,b2) (A00,A01,A02,A10) (A11,A12,A20,A21) (A22,f0,f1,f2)
-  //   acc   kP2GWarps x 4 x 216 floats: per-warp node sums (m, mv)
-  //   cst   65 ints: cell ranges of the chunk
-  //   scell kP2GChunk bytes: cell of each chunk particle
   extern __shared__ __align__(16) unsigned char p2g_smem[];
-  float4(*spd)[kP2GChunk] = reinterpret_cast<float4(*)[kP2GChunk]>(p2g_smem);
-  float(*acc)[4][kNodes] = reinterpret_cast<float(*)[4][kNodes]>(p2g_smem + kP2GSpdBytes);
-  int *cst = reinterpret_cast<int *>(p2g_smem + kP2GSpdBytes + kP2GAccBytes);
-  unsigned char *scell = p2g_smem + kP2GSpdBytes + kP2GAccBytes + 65 * sizeof(int);
+  const TileSmem ts = tile_smem(p2g_smem);
   const SimParams &P = *d.prm;
   const long long cap = d.cap;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // lane constants of phase 2: slot, stencil column (i, j), weight polynomials
-  // w_0(f) = (1.5-f)^2/2, w_1(f) = 3/4-(f-1)^2, w_2(f) = (f-1/2)^2/2 written as
-  // c0 + f (c1 + f c2)
-  const int slot = lane / 9, oi = (lane % 9) / 3, oj = lane % 3;
-  auto coef = [](int o, float &c0, float &c1, float &c2) {
-    c0 = o == 0 ? 1.125f : (o == 1 ? -0.25f : 0.125f);
-    c1 = o == 0 ? -1.5f : (o == 1 ? 2.0f : -0.5f);
-    c2 = o == 1 ? -1.0f : 0.5f;
-  };
-  float ci0, ci1, ci2, cj0, cj1, cj2;
-  coef(oi, ci0, ci1, ci2);
-  coef(oj, cj0, cj1, cj2);
-  float *myacc = &acc[warp][0][0];
+  const int tid = threadIdx.x;
 
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    for (int i = tid; i < kP2GWarps * 4 * kNodes; i += kP2GThreads) (&acc[0][0][0])[i] = 0.0f;
+    tile_zero(ts);
     const int dir = d.bk_dir[b];
     const SceneParams &S = d.scn[scene_of_dir(d, dir)];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
-    const float odx = oi * dx, ody = oj * dx;
     int K[3];
     bucket_origin(S, dir - S.dir_off, K);
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     for (int c0 = 0; c0 < cnt; c0 += kP2GChunk) {
       const int nc = min(kP2GChunk, cnt - c0);
-      __syncthreads();  // spd / scell of the previous chunk consumed
+      __syncthreads();  // the previous chunk consumed
       for (int j = tid; j < nc; j += kP2GThreads) {
         const int p = d.perm[start + c0 + j];
         float x[3], v[3], C[9], Sv[6];
@@ -150,109 +113,20 @@ __global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__r
           for (int k = 0; k < 9; ++k) A[k] = 0.0f;
           v[0] = v[1] = v[2] = 0.0f;
         }
+        const float f[3] = {s0.f, s1.f, s2.f};
         const float fdx0 = s0.f * dx, fdx1 = s1.f * dx, fdx2 = s2.f * dx;
-        const float b0 = mass * v[0] - (A[0] * fdx0 + A[1] * fdx1 + A[2] * fdx2);
-        const float b1 = mass * v[1] - (A[3] * fdx0 + A[4] * fdx1 + A[5] * fdx2);
-        const float b2 = mass * v[2] - (A[6] * fdx0 + A[7] * fdx1 + A[8] * fdx2);
-        spd[0][j] = make_float4(mass, b0, b1, b2);
-        spd[1][j] = make_float4(A[0], A[1], A[2], A[3]);
-        spd[2][j] = make_float4(A[4], A[5], A[6], A[7]);
-        spd[3][j] = make_float4(A[8], s0.f, s1.f, s2.f);
-        scell[j] = (unsigned char)cell;
+        const float bv[3] = {mass * v[0] - (A[0] * fdx0 + A[1] * fdx1 + A[2] * fdx2),
+                             mass * v[1] - (A[3] * fdx0 + A[4] * fdx1 + A[5] * fdx2),
+                             mass * v[2] - (A[6] * fdx0 + A[7] * fdx1 + A[8] * fdx2)};
+        tile_stage(ts, j, mass, bv, A, f, cell);
       }
       __syncthreads();
-      // cell ranges of the chunk (sorted by cell): first index with cell >= c
-      for (int c = tid; c <= 64; c += kP2GThreads) {
-        int lo = 0, hi = nc;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (scell[mid] < c)
-            lo = mid + 1;
-          else
-            hi = mid;
-        }
-        cst[c] = lo;
-      }
+      tile_cell_ranges(ts, nc);
       __syncthreads();
-      // phase 2: 8 cells per warp, three per round (slots), 9 lanes per cell
-      for (int round = 0; round < 3; ++round) {
-        const int t = 3 * round + slot;  // this lane's cell of the warp, 0..8
-        const bool has = lane < 27 && t < 8;
-        const int cell = warp + 8 * t;
-        int q = 0, q1 = 0;
-        if (has) {
-          q = cst[cell];
-          q1 = cst[cell + 1];
-        }
-        float am0 = 0.f, am1 = 0.f, am2 = 0.f;
-        float a00 = 0.f, a01 = 0.f, a02 = 0.f, a10 = 0.f, a11 = 0.f, a12 = 0.f;
-        float a20 = 0.f, a21 = 0.f, a22 = 0.f;
-        for (; q < q1; ++q) {
-          const float4 u0 = spd[0][q], u1 = spd[1][q], u2 = spd[2][q], u3 = spd[3][q];
-          const float wx = fmaf(fmaf(ci2, u3.y, ci1), u3.y, ci0);
-          const float wy = fmaf(fmaf(cj2, u3.z, cj1), u3.z, cj0);
-          const float fz = u3.w;
-          const float wz0 = fmaf(fmaf(0.5f, fz, -1.5f), fz, 1.125f);
-          const float wz1 = fmaf(fmaf(-1.0f, fz, 2.0f), fz, -0.25f);
-          const float wz2 = fmaf(fmaf(0.5f, fz, -0.5f), fz, 0.125f);
-          const float wij = wx * wy;
-          const float mw = u0.x * wij;
-          // b + A (i dx, j dx, k dx) for k = 0, 1, 2
-          const float p0 = fmaf(u1.y, ody, fmaf(u1.x, odx, u0.y));
-          const float p1 = fmaf(u2.x, ody, fmaf(u1.w, odx, u0.z));
-          const float p2 = fmaf(u2.w, ody, fmaf(u2.z, odx, u0.w));
-          const float r0 = u1.z * dx, r1 = u2.y * dx, r2 = u3.x * dx;
-          const float W0 = wij * wz0, W1 = wij * wz1, W2 = wij * wz2;
-          am0 = fmaf(mw, wz0, am0);
-          am1 = fmaf(mw, wz1, am1);
-          am2 = fmaf(mw, wz2, am2);
-          a00 = fmaf(W0, p0, a00);
-          a01 = fmaf(W0, p1, a01);
-          a02 = fmaf(W0, p2, a02);
-          a10 = fmaf(W1, p0 + r0, a10);
-          a11 = fmaf(W1, p1 + r1, a11);
-          a12 = fmaf(W1, p2 + r2, a12);
-          const float r02 = r0 + r0, r12 = r1 + r1, r22 = r2 + r2;
-          a20 = fmaf(W2, p0 + r02, a20);
-          a21 = fmaf(W2, p1 + r12, a21);
-          a22 = fmaf(W2, p2 + r22, a22);
-        }
-        // slot by slot into the warp's private nodes (cells of one round may
-        // share nodes, lanes of one slot own distinct nodes)
-        const int nd0 = has ? ((((cell >> 4) + oi) * 6 + (((cell >> 2) & 3) + oj)) * 6 + (cell & 3))
-                            : 0;
-        for (int sl = 0; sl < 3; ++sl) {
-          if (has && slot == sl && q1 > cst[cell]) {
-            myacc[0 * kNodes + nd0] += am0;
-            myacc[1 * kNodes + nd0] += a00;
-            myacc[2 * kNodes + nd0] += a01;
-            myacc[3 * kNodes + nd0] += a02;
-            myacc[0 * kNodes + nd0 + 1] += am1;
-            myacc[1 * kNodes + nd0 + 1] += a10;
-            myacc[2 * kNodes + nd0 + 1] += a11;
-            myacc[3 * kNodes + nd0 + 1] += a12;
-            myacc[0 * kNodes + nd0 + 2] += am2;
-            myacc[1 * kNodes + nd0 + 2] += a20;
-            myacc[2 * kNodes + nd0 + 2] += a21;
-            myacc[3 * kNodes + nd0 + 2] += a22;
-          }
-          __syncwarp();
-        }
-      }
+      tile_scatter(ts, dx);
     }
     __syncthreads();
-    float4 *tile = d.ptile + (long long)b * kTileNodes;
-    for (int nd = tid; nd < kNodes; nd += kP2GThreads) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int w = 0; w < kP2GWarps; ++w) {
-        v.x += acc[w][0][nd];
-        v.y += acc[w][1][nd];
-        v.z += acc[w][2][nd];
-        v.w += acc[w][3][nd];
-      }
-      tile[nd] = v;
-    }
+    tile_store(ts, d.ptile + (long long)b * kTileNodes);
     __syncthreads();
   }
 }
@@ -515,36 +389,38 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
       for (int k = 0; k < 9; ++k) finite = finite && isfinite(F[k]);
       if (!finite) atomicOr(&d.cnt->status, ST_NAN);
-      // next buffer, sorted position s
+      // next buffer: sorted position s, or the particle's own slot p in the
+      // differentiable mode (every state then shares the upload order)
+      const int so = d.keep_order ? p : s;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        pout[(CH_X + k) * cap + s] = x[k];
-        pout[(CH_V + k) * cap + s] = vel[k];
+        pout[(CH_X + k) * cap + so] = x[k];
+        pout[(CH_V + k) * cap + so] = vel[k];
       }
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
-        pout[(CH_C + k) * cap + s] = Cn[k];
-        pout[(CH_F + k) * cap + s] = F[k];
+        pout[(CH_C + k) * cap + so] = Cn[k];
+        pout[(CH_F + k) * cap + so] = F[k];
       }
-      pout[CH_J * cap + s] = J;
-      pout[CH_M * cap + s] = pin[CH_M * cap + p];
-      pout[CH_VOL * cap + s] = vol;
-      pout[(CH_S + 0) * cap + s] = vol * tau.xx;
-      pout[(CH_S + 1) * cap + s] = vol * tau.yy;
-      pout[(CH_S + 2) * cap + s] = vol * tau.zz;
-      pout[(CH_S + 3) * cap + s] = vol * tau.xy;
-      pout[(CH_S + 4) * cap + s] = vol * tau.xz;
-      pout[(CH_S + 5) * cap + s] = vol * tau.yz;
+      pout[CH_J * cap + so] = J;
+      pout[CH_M * cap + so] = pin[CH_M * cap + p];
+      pout[CH_VOL * cap + so] = vol;
+      pout[(CH_S + 0) * cap + so] = vol * tau.xx;
+      pout[(CH_S + 1) * cap + so] = vol * tau.yy;
+      pout[(CH_S + 2) * cap + so] = vol * tau.zz;
+      pout[(CH_S + 3) * cap + so] = vol * tau.xy;
+      pout[(CH_S + 4) * cap + so] = vol * tau.xz;
+      pout[(CH_S + 5) * cap + so] = vol * tau.yz;
       if (lame) {
-        pout[CH_MU * cap + s] = pin[CH_MU * cap + p];
-        pout[CH_LAM * cap + s] = pin[CH_LAM * cap + p];
+        pout[CH_MU * cap + so] = pin[CH_MU * cap + p];
+        pout[CH_LAM * cap + so] = pin[CH_LAM * cap + p];
       }
-      iout[IC_MAT * cap + s] = mid;
-      iout[IC_ID * cap + s] = iin[IC_ID * cap + p];
+      iout[IC_MAT * cap + so] = mid;
+      iout[IC_ID * cap + so] = iin[IC_ID * cap + p];
       if (kFuseBin) {
         // key of the new position for the next partition (storage slot s)
         const int key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
-        d.pkey[s] = key;
+        d.pkey[so] = key;
         bin_count(d, S, key, mask);
       }
     }

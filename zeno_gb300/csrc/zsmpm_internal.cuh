@@ -113,7 +113,9 @@ struct DevPtrs {
   int32_t *bk_dir, *bk_start, *bk_count;
   int cap_gblocks;
   float4 *grid;
-  float4 *ptile;  // per particle block: its 6^3 P2G node sums (216 float4)
+  float4 *ptile;      // per particle block: its 6^3 P2G node sums (216 float4)
+  float4 *ptile_adj;  // the same for the G2P adjoint (differentiable mode)
+  int keep_order;     // differentiable mode: G2P writes each particle to its own slot
   int32_t *tile_sums;
   int ntiles;
   Counters *cnt;
@@ -153,6 +155,14 @@ void launch_stress(const DevPtrs &d, int cur, cudaStream_t s);
 
 // api.cu: the text mpm_last_error() returns on this thread
 void set_last_error(const std::string &msg);
+
+// adjoint.cu: the three adjoint kernels of one substep (an / ap: adjoint
+// planes of the next / this state, n particles each)
+void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, long long n,
+                        cudaStream_t s);
+void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s);
+void launch_p2g_adjoint(const DevPtrs &d, int cur, float *ap, float *gmu, float *glam, long long n,
+                        cudaStream_t s);
 
 // io.cu
 struct IngestSrc {

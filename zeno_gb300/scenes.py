@@ -210,10 +210,14 @@ def multi_material(seed: int = 0, dx: float = 1.0 / 256, region_cells=(64, 32, 3
 def diff_scene(seed: int = 0, dx: float = 1.0 / 128, cells=(32, 16, 16)):
     """Differentiable-rollout scene: fixed-corotated block of 32x16x16 cells x
     8 ppc = 65,536 particles at dx = 1/128, per-particle Young's modulus
-    E ~ U[3e4, 1e5] (nu = 0.3) carried as per-particle mu / lam, sticky walls."""
+    E ~ U[3e4, 1e5] (nu = 0.3) carried as per-particle mu / lam, sticky walls.
+    The block rests one cell above the floor's wall band, so that a downward
+    initial velocity makes it hit the floor inside the rollout: a free block's
+    centre of mass does not depend on its stiffness (internal forces sum to
+    zero), a block in contact does."""
     mats = [Material(FCR, E=5e4, nu=0.3)]
     scene = Scene.unit_box(dx, bc_type=BC_STICKY, bc_thickness=3, dt=1e-4, materials=mats)
-    x = box_particles((0.3, 0.4, 0.4), cells, dx, 8, seed, 0)
+    x = box_particles((0.3, 4 * dx, 0.4), cells, dx, 8, seed, 0)
     parts = make_particles(x, dx, 8, mats, np.zeros(x.shape[0], np.int32))
     E = 3e4 + (1e5 - 3e4) * uniform(seed, 300, x.shape[0])
     mu, lam = lame(E, 0.3)

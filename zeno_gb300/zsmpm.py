@@ -69,7 +69,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
-           "mpm_get_launch_config"]
+           "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
+           "mpm_adjoint_substep"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 
@@ -118,6 +119,10 @@ def load(path: str = LIB_PATH):
         "mpm_partition_noalloc": ([P, i64, f32, P, P, P, P, P, i64, P, P], i32),
         "mpm_set_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
         "mpm_get_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
+        "mpm_set_order_mode": ([P, i32], i32),
+        "mpm_state_save": ([P, P], i32),
+        "mpm_state_load": ([P, P], i32),
+        "mpm_adjoint_substep": ([P, f32, P, P, P, P], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -295,6 +300,21 @@ class Context:
 
     def sync(self):
         self._check(self._L.mpm_sync(self.h), "mpm_sync")
+
+    # differentiable form: device pointers (ints), 25 planes of n floats
+    def set_order_mode(self, keep: bool):
+        self._check(self._L.mpm_set_order_mode(self.h, 1 if keep else 0), "mpm_set_order_mode")
+
+    def state_save(self, dst_ptr: int):
+        self._check(self._L.mpm_state_save(self.h, C.c_void_p(dst_ptr)), "mpm_state_save")
+
+    def state_load(self, src_ptr: int):
+        self._check(self._L.mpm_state_load(self.h, C.c_void_p(src_ptr)), "mpm_state_load")
+
+    def adjoint_substep(self, dt, adj_next: int, adj_prev: int, grad_mu: int, grad_lam: int):
+        self._check(self._L.mpm_adjoint_substep(self.h, dt, C.c_void_p(adj_next),
+                                                C.c_void_p(adj_prev), C.c_void_p(grad_mu),
+                                                C.c_void_p(grad_lam)), "mpm_adjoint_substep")
 
     def set_launch_config(self, cfg: dict):
         lc = LaunchConfig(*(int(cfg.get(k, 0)) for k, _ in LaunchConfig._fields_))
