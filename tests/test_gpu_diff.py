@@ -20,7 +20,7 @@ def _problem(cells=(16, 8, 8)):
     scene, parts = S.diff_scene(cells=cells)
     nu = scene.materials[0].nu
     E = parts.mu.astype(np.float64) * 2.0 * (1.0 + nu)
-    v0 = np.tile([[0.3, -3.0, 0.1]], (parts.n, 1)) + 0.2 * S.normal(4, 0, parts.n * 3).reshape(-1, 3)
+    v0 = S.diff_velocity(parts.n)
     dv = np.tile([[1.0, 0.5, -0.3]], (parts.n, 1)) + 0.5 * S.normal(5, 0, parts.n * 3).reshape(-1, 3)
     rE = 0.5 + S.uniform(6, 0, parts.n)
     return scene, parts, E, v0, dv, rE

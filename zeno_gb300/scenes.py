@@ -226,6 +226,12 @@ def diff_scene(seed: int = 0, dx: float = 1.0 / 128, cells=(32, 16, 16)):
     return scene, parts
 
 
+def diff_velocity(n: int, seed: int = 4):
+    """Initial velocity of the differentiable rollout: the block is thrown at
+    the floor, (0.3, -3, 0.1) m/s plus N(0, 0.2^2) per component."""
+    return np.tile([[0.3, -3.0, 0.1]], (n, 1)) + 0.2 * normal(seed, 0, n * 3).reshape(-1, 3)
+
+
 def batched_counts(n_scenes: int = 256, lo: int = 2048, hi: int = 200000, seed: int = 1):
     """Per-scene particle counts drawn log-uniform in [lo, hi]."""
     u = uniform(seed, 0, n_scenes)
