@@ -300,7 +300,8 @@ int build_partition(const orc_scene &sc, int64_t n, const R *x, Partition &P, in
       key[i] = -1;
       continue;
     }
-    const int32_t cell = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3);
+    // z-major cell id inside the block, (z << 4) | (x << 2) | y
+    const int32_t cell = ((base[2] & 3) << 4) | ((base[0] & 3) << 2) | (base[1] & 3);
     key[i] = int32_t(dir.index(bc) * 64 + cell);
   }
   if (bad) return ORC_ERR_OUT_OF_DOMAIN;

@@ -173,7 +173,8 @@ def test_partition_lattice_restatement(oracle_mod):
         base = [int(math.floor(np.float32(np.float32(c) * inv) - np.float32(0.5))) for c in p]
         bc = [(b >> 2) - lo for b, lo in zip(base, scene.block_lo)]
         d = (bc[0] * dims[1] + bc[1]) * dims[2] + bc[2]
-        cell = ((base[0] & 3) << 4) | ((base[1] & 3) << 2) | (base[2] & 3)
+        # z-major cell id inside the block: (z, x, y)
+        cell = ((base[2] & 3) << 4) | ((base[0] & 3) << 2) | (base[1] & 3)
         keys.append((d, cell, i))
     keys.sort()
     perm = [k[2] for k in keys]

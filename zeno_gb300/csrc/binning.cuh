@@ -16,6 +16,14 @@ __device__ __forceinline__ int particle_base(float x, float inv_dx) {
   return __float2int_rd(__fsub_rn(__fmul_rn(x, inv_dx), 0.5f));
 }
 
+// Cell id of a particle inside its 4^3 block, the order of particles within
+// a block: z-major, (l2 << 4) | (l0 << 2) | l1, so that the block's 16 cell
+// columns (l0, l1) interleave along the sorted order and every contiguous
+// chunk of a block's particles spans all 16 columns.
+__device__ __forceinline__ int sort_cell(int l0, int l1, int l2) {
+  return (l2 << 4) | (l0 << 2) | l1;
+}
+
 // key = (global directory index << 6) | cell, or -1 (status bit set) for a
 // non-finite position or one outside the interior of the scene's directory
 __device__ __forceinline__ int bin_key(const SceneParams &S, float x0, float x1, float x2,
@@ -34,7 +42,7 @@ __device__ __forceinline__ int bin_key(const SceneParams &S, float x0, float x1,
     return -1;
   }
   const int dd = S.dir_off + (c0 * dy + c1) * dz + c2;
-  return (dd << 6) | ((b0 & 3) << 4) | ((b1 & 3) << 2) | (b2 & 3);
+  return (dd << 6) | sort_cell(b0 & 3, b1 & 3, b2 & 3);
 }
 
 // Warp-aggregated count of `key` into its block; the first particle of a

@@ -74,6 +74,80 @@ __device__ __forceinline__ void sym_eig3(Sym3 a, float (&w)[3], float (&Q)[9]) {
   w[2] = d2;
 }
 
+// Eigenvalues of a symmetric 3x3 matrix from its characteristic cubic in
+// trigonometric form (O. K. Smith, "Eigenvalues of a symmetric 3x3 matrix",
+// Comm. ACM 4(4):168, 1961): with q = tr(A)/3, p^2 = tr((A - qI)^2)/6 and
+// r = det((A - qI)/p)/2, the roots are q + 2p cos(phi + 2 pi k/3),
+// phi = acos(r)/3.  Each eigenvalue is accurate to rounding of p, which is all
+// the symmetric functions of the eigenvalues below need.
+__device__ __forceinline__ void sym_eigvals3(const Sym3 &a, float (&w)[3]) {
+  const float q = (a.xx + a.yy + a.zz) * (1.0f / 3.0f);
+  const float b0 = a.xx - q, b1 = a.yy - q, b2 = a.zz - q;
+  const float off = a.xy * a.xy + a.xz * a.xz + a.yz * a.yz;
+  const float p2 = (b0 * b0 + b1 * b1 + b2 * b2 + 2.0f * off) * (1.0f / 6.0f);
+  if (!(p2 > 0.0f)) {
+    w[0] = w[1] = w[2] = q;
+    return;
+  }
+  const float p = sqrtf(p2);
+  const float det = b0 * (b1 * b2 - a.yz * a.yz) - a.xy * (a.xy * b2 - a.yz * a.xz) +
+                    a.xz * (a.xy * a.yz - b1 * a.xz);
+  const float r = fminf(fmaxf(det / (2.0f * p2 * p), -1.0f), 1.0f);
+  const float phi = acosf(r) * (1.0f / 3.0f);
+  float sn, cs;
+  __sincosf(phi, &sn, &cs);  // phi in [0, pi/3]
+  w[0] = fmaf(2.0f * p, cs, q);
+  w[2] = fmaf(2.0f * p, -0.5f * cs - 0.8660254037844386f * sn, q);  // cos(phi + 2pi/3)
+  w[1] = 3.0f * q - w[0] - w[2];
+}
+
+// Fixed-corotated Kirchhoff stress from the stretch invariants, for J > 0:
+// tau = 2mu (B - V) + lam (J-1) J I with V = R F^T = sqrt(B).  Cayley-Hamilton
+// for V (invariants I1, I2, I3 of V, V^2 = B) gives
+//   V = (-B^2 + (I1^2 - I2) B + I1 I3 I) / (I1 I2 - I3)
+// (Hoger & Carlson, "Determination of the stretch and rotation in the polar
+// decomposition of the deformation gradient", Q. Appl. Math. 42, 1984).  In
+// strain variables, B = I + E and s_i = 1 + t_i with t_i = e_i / (1 +
+// sqrt(1 + e_i)) (e_i the eigenvalues of E) and e1, e2, e3 the elementary
+// symmetric polynomials of the t_i, this is
+//   V - I = (e3 (4 + e1) I + (4 + 4 e1 + e1^2 - e2) E - E^2) / D,
+//   D = (s1 + s2)(s1 + s3)(s2 + s3) = 8 + 8 e1 + 2 e2 + 2 e1^2 + e1 e2 - e3,
+// which keeps small strains free of cancellation and needs no eigenvectors.
+__device__ __forceinline__ void fcr_tau_invariant(float mu, float lam, const Sym3 &E, float Jm1,
+                                                  Sym3 &tau) {
+  float w[3];
+  sym_eigvals3(E, w);
+  float t[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float e = fmaxf(w[k], -1.0f);
+    t[k] = e / (1.0f + sqrtf(1.0f + e));
+  }
+  const float e1 = t[0] + t[1] + t[2];
+  const float e2 = t[0] * t[1] + t[0] * t[2] + t[1] * t[2];
+  const float e3 = t[0] * t[1] * t[2];
+  const float D = 8.0f + 8.0f * e1 + 2.0f * e2 + 2.0f * e1 * e1 + e1 * e2 - e3;
+  const float rD = 1.0f / D;
+  const float c0 = e3 * (4.0f + e1) * rD, c1 = (4.0f + 4.0f * e1 + e1 * e1 - e2) * rD;
+  // E^2 (symmetric)
+  const float qxx = E.xx * E.xx + E.xy * E.xy + E.xz * E.xz;
+  const float qyy = E.xy * E.xy + E.yy * E.yy + E.yz * E.yz;
+  const float qzz = E.xz * E.xz + E.yz * E.yz + E.zz * E.zz;
+  const float qxy = E.xx * E.xy + E.xy * E.yy + E.xz * E.yz;
+  const float qxz = E.xx * E.xz + E.xy * E.yz + E.xz * E.zz;
+  const float qyz = E.xy * E.xz + E.yy * E.yz + E.yz * E.zz;
+  // B - V = E - (V - I)
+  const float m2 = 2.0f * mu, k1 = 1.0f - c1;
+  const float J = 1.0f + Jm1;
+  const float diag = lam * Jm1 * J - m2 * c0;
+  tau.xx = m2 * fmaf(qxx, rD, k1 * E.xx) + diag;
+  tau.yy = m2 * fmaf(qyy, rD, k1 * E.yy) + diag;
+  tau.zz = m2 * fmaf(qzz, rD, k1 * E.zz) + diag;
+  tau.xy = m2 * fmaf(qxy, rD, k1 * E.xy);
+  tau.xz = m2 * fmaf(qxz, rD, k1 * E.xz);
+  tau.yz = m2 * fmaf(qyz, rD, k1 * E.yz);
+}
+
 // Q diag(d) Q^T
 __device__ __forceinline__ Sym3 qdqt(const float (&Q)[9], float d0, float d1, float d2) {
   Sym3 r;
@@ -130,9 +204,13 @@ __device__ __forceinline__ bool kirchhoff(int type, float mu, float lam, float b
                mu * E.yz};
     return J > 0.0f;
   }
+  if (type == MPM_FCR && J > 0.0f) {
+    fcr_tau_invariant(mu, lam, E, Jm1, tau);
+    return true;
+  }
   float w[3], Q[9];
   sym_eig3(E, w, Q);
-  if (type == MPM_FCR) {
+  if (type == MPM_FCR) {  // inverted (J <= 0): sign-fixed singular values
     float d[3], s[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -142,7 +220,9 @@ __device__ __forceinline__ bool kirchhoff(int type, float mu, float lam, float b
     }
     if (J < 0.0f) {
       const int kmin = (s[0] <= s[1] && s[0] <= s[2]) ? 0 : ((s[1] <= s[2]) ? 1 : 2);
-      d[kmin] = s[kmin] * s[kmin] + s[kmin];  // s^2 - (-s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k == kmin) d[k] = s[k] * s[k] + s[k];  // s^2 - (-s)
     }
     tau = qdqt(Q, 2.0f * mu * d[0], 2.0f * mu * d[1], 2.0f * mu * d[2]);
     const float diag = lam * Jm1 * J;
@@ -284,7 +364,9 @@ __device__ __forceinline__ void fcr_vjp(float mu, float lam, const float (&F)[9]
   for (int k = 0; k < 3; ++k) s[k] = sqrtf(1.0f + fmaxf(w[k], -1.0f));
   if (J < 0.0f) {
     const int kmin = (s[0] <= s[1] && s[0] <= s[2]) ? 0 : ((s[1] <= s[2]) ? 1 : 2);
-    s[kmin] = -s[kmin];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (k == kmin) s[k] = -s[k];
   }
   // R = U diag(1/s^) U^T F,  R F^T = U diag(s^) U^T
   const Sym3 Ui = qdqt(Q, 1.0f / s[0], 1.0f / s[1], 1.0f / s[2]);

@@ -145,7 +145,8 @@ __device__ __forceinline__ void tile_scatter(const TileSmem &t, float dx) {
     }
     // slot by slot into the warp's private nodes (cells of one round may
     // share nodes, lanes of one slot own distinct nodes)
-    const int nd0 = has ? ((((cell >> 4) + oi) * 6 + (((cell >> 2) & 3) + oj)) * 6 + (cell & 3))
+    // cell = sort_cell(l0, l1, l2) = (l2 << 4) | (l0 << 2) | l1
+    const int nd0 = has ? (((((cell >> 2) & 3) + oi) * 6 + ((cell & 3) + oj)) * 6 + (cell >> 4))
                         : 0;
     for (int sl = 0; sl < 3; ++sl) {
       if (has && slot == sl && q1 > cst[cell]) {

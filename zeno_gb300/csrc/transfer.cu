@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "binning.cuh"
+#include "cp_async.cuh"
 #include "mpm_math.cuh"
 #include "tile_scatter.cuh"
 #include "zsmpm_internal.cuh"
@@ -52,83 +53,277 @@ __device__ __forceinline__ int neighbour_gb(const DevPtrs &d, const SceneParams 
 // P2G of one particle block (ZSParticleToZSGrid::p2g_apic, Transfer.cu:849-889):
 // per particle the affine matrix A = m C - dt Dinv S (S = vol tau from the
 // previous G2P); the momentum of stencil node o is W (m v + A (o - f) dx) =
-// W (b + A o dx) with b = m v - dx A f.  The block's particles are staged and
-// scattered into its 216-node tile by tile_scatter (tile_scatter.cuh).
-__global__ void __launch_bounds__(kP2GThreads) k_p2g(DevPtrs d, const float *__restrict__ pin,
+// W (b + a o) with a = dx A and b = m v - dx A f.
+//
+// Column scatter: the block's 16 cell columns (cx, cy) each belong to one
+// 9-lane slot of a warp (6 warps, 3 slots each); lane (oi, oj) of the slot
+// keeps the 6 nodes (cx + oi, cy + oj, 0..5) of its column in registers and
+// adds, cell by cell (cz = 0..3, nodes cz..cz+2), every particle of the
+// column in sorted order, over all chunks of the block.  At the end each
+// lane writes its 6 node sums as a record, and the 216 tile nodes are the
+// sums of the <= 9 records that cover them, added in a fixed (oi, oj) order:
+// no atomics, no shared-memory read-modify-write, and a reproducible tile.
+//
+// Particles of a block are sorted by the z-major cell id (l2, l0, l1), so a
+// chunk of the block holds cells of every column.  A CTA walks its blocks in
+// chunks of kColChunk particles (thread j <-> particle j): each thread
+// converts its own particle's raw channels into a scatter record, and as
+// soon as the records are published it issues the cp.async copies of its
+// particle of the next chunk into the raw buffer, so that those loads are in
+// flight while the current chunk scatters; the permutation entries of the
+// chunk after that load into registers.
+constexpr int kColThreads = 192;
+constexpr int kColChunk = kColThreads;
+constexpr int kColRaw = 23;            // x3 v3 C9 S6 m key
+constexpr int kColRecs = 16 * 9 * 6;  // float4 records: (column, oi oj, z)
+constexpr int kColMeta = 128;          // blocks per CTA whose metadata is staged
+// shared memory: raw[23][chunk] floats; spd[4][chunk] float4 (m b),
+// (a00 a10 a20 a01), (a11 a21 a02 a12), (a22 wz0 wz1 wz2); sw[chunk][6]
+// wx0..2 wy0..2; the records; the chunk's cells; block metadata
+constexpr int kColOffSpd = kColRaw * kColChunk * 4;
+constexpr int kColOffW = kColOffSpd + 4 * kColChunk * 16;
+constexpr int kColOffRec = kColOffW + kColChunk * 6 * 4;
+constexpr int kColOffCell = kColOffRec + kColRecs * 16;
+constexpr int kColOffMeta = kColOffCell + ((kColChunk + 15) & ~15);
+constexpr int kColSmem = kColOffMeta + kColMeta * 16;
+static_assert(kColOffSpd % 16 == 0 && kColOffRec % 16 == 0 && kColOffMeta % 16 == 0,
+              "float4 / int4 regions must be 16-byte aligned");
+// raw channel slots
+constexpr int RC_X = 0, RC_V = 3, RC_C = 6, RC_S = 15, RC_M = 21, RC_KEY = 22;
+
+__global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__restrict__ pin,
                                                      const int32_t *__restrict__ iin) {
   extern __shared__ __align__(16) unsigned char p2g_smem[];
-  const TileSmem ts = tile_smem(p2g_smem);
+  float(*raw)[kColChunk] = reinterpret_cast<float(*)[kColChunk]>(p2g_smem);
+  float4(*spd)[kColChunk] = reinterpret_cast<float4(*)[kColChunk]>(p2g_smem + kColOffSpd);
+  float(*sw)[6] = reinterpret_cast<float(*)[6]>(p2g_smem + kColOffW);
+  float4 *rec = reinterpret_cast<float4 *>(p2g_smem + kColOffRec);
+  unsigned char *scell = p2g_smem + kColOffCell;
+  int4 *meta = reinterpret_cast<int4 *>(p2g_smem + kColOffMeta);  // (start, cnt, dir, scene)
   const SimParams &P = *d.prm;
-  const long long cap = d.cap;
+  const long long cap = d.cap, n = P.n;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // lane constants: slot, column, stencil offsets (oi, oj)
+  const int slot = lane / 9, oij = lane % 9;
+  const int col = 3 * warp + slot;
+  const bool has_col = lane < 27 && col < 16;
+  const float foi = (float)(oij / 3), foj = (float)(oij % 3);
+  const int wxo = oij / 3, wyo = 3 + oij % 3;
 
-  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    tile_zero(ts);
-    const int dir = d.bk_dir[b];
-    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
+  const int nblk = nb > (int)blockIdx.x ? (nb - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  auto load_meta = [&](int k) {
+    const int b = blockIdx.x + k * gridDim.x;
+    const int dir = d.bk_dir[b], start = d.bk_start[b];
+    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], n - start));
+    return make_int4(start, cnt, dir, scene_of_dir(d, dir));
+  };
+  for (int k = tid; k < min(nblk, kColMeta); k += kColThreads) meta[k] = load_meta(k);
+  __syncthreads();
+  auto meta_of = [&](int k) { return k < kColMeta ? meta[k] : load_meta(k); };
+
+  struct Item {
+    int k, c0;
+  };
+  auto skip_empty = [&](Item it) {
+    while (it.k < nblk && meta_of(it.k).y == 0) ++it.k;
+    return it;
+  };
+  auto advance = [&](Item it) {
+    if (it.k >= nblk) return it;
+    it.c0 += kColChunk;
+    if (it.c0 >= meta_of(it.k).y) {
+      ++it.k;
+      it.c0 = 0;
+      it = skip_empty(it);
+    }
+    return it;
+  };
+  auto perm_of = [&](const Item &it) {
+    if (it.k >= nblk) return -1;
+    const int4 m = meta_of(it.k);
+    return tid < m.y - it.c0 ? d.perm[m.x + it.c0 + tid] : -1;
+  };
+  auto issue = [&](int p) {
+    if (p < 0) return;
+    float(*q)[kColChunk] = raw;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      cp_async4(&q[RC_X + c][tid], &pin[(CH_X + c) * cap + p]);
+      cp_async4(&q[RC_V + c][tid], &pin[(CH_V + c) * cap + p]);
+    }
+#pragma unroll
+    for (int c = 0; c < 9; ++c) cp_async4(&q[RC_C + c][tid], &pin[(CH_C + c) * cap + p]);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) cp_async4(&q[RC_S + c][tid], &pin[(CH_S + c) * cap + p]);
+    cp_async4(&q[RC_M][tid], &pin[CH_M * cap + p]);
+    cp_async4(&q[RC_KEY][tid], &d.pkey[p]);
+  };
+
+  float4 acc[6];
+#pragma unroll
+  for (int z = 0; z < 6; ++z) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+  Item cur = skip_empty(Item{0, 0});
+  Item nxt = advance(cur);
+  Item nn = advance(nxt);
+  int p_nxt = perm_of(nxt);
+  issue(perm_of(cur));
+  cp_async_commit();
+  while (cur.k < nblk) {
+    const int p_nn = perm_of(nn);
+    const int4 m = meta_of(cur.k);
+    const SceneParams &S = d.scn[m.w];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
     int K[3];
-    bucket_origin(S, dir - S.dir_off, K);
-    const int start = d.bk_start[b];
-    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
-    for (int c0 = 0; c0 < cnt; c0 += kP2GChunk) {
-      const int nc = min(kP2GChunk, cnt - c0);
-      __syncthreads();  // the previous chunk consumed
-      for (int j = tid; j < nc; j += kP2GThreads) {
-        const int p = d.perm[start + c0 + j];
-        float x[3], v[3], C[9], Sv[6];
+    bucket_origin(S, m.z - S.dir_off, K);
+    const int nc = min(kColChunk, m.y - cur.c0);
+    cp_async_wait<0>();  // this thread's particle of chunk `cur` has landed
+    // convert particle tid of the chunk into its scatter record
+    if (tid < nc) {
+      const float(*q)[kColChunk] = raw;
+      float x[3], v[3], C[9], Sv[6];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          x[k] = pin[(CH_X + k) * cap + p];
-          v[k] = pin[(CH_V + k) * cap + p];
-        }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) C[k] = pin[(CH_C + k) * cap + p];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) Sv[k] = pin[(CH_S + k) * cap + p];
-        float mass = pin[CH_M * cap + p];
-        // A = m C - dt Dinv vol tau (contrib of Transfer.cu:868 is -dt Dinv vol P F^T)
-        const float kk = -dt * Dinv;
-        float A[9];
-        A[0] = mass * C[0] + kk * Sv[0];
-        A[1] = mass * C[1] + kk * Sv[3];
-        A[2] = mass * C[2] + kk * Sv[4];
-        A[3] = mass * C[3] + kk * Sv[3];
-        A[4] = mass * C[4] + kk * Sv[1];
-        A[5] = mass * C[5] + kk * Sv[5];
-        A[6] = mass * C[6] + kk * Sv[4];
-        A[7] = mass * C[7] + kk * Sv[5];
-        A[8] = mass * C[8] + kk * Sv[2];
-        const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
-                       s2 = stencil1(x[2], inv_dx);
-        const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
-        const int cell = d.pkey[p] & 63;
-        if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u ||
-            ((l0 << 4) | (l1 << 2) | l2) != cell) {
-          atomicOr(&d.cnt->status, ST_STENCIL);
-          mass = 0.0f;
-#pragma unroll
-          for (int k = 0; k < 9; ++k) A[k] = 0.0f;
-          v[0] = v[1] = v[2] = 0.0f;
-        }
-        const float f[3] = {s0.f, s1.f, s2.f};
-        const float fdx0 = s0.f * dx, fdx1 = s1.f * dx, fdx2 = s2.f * dx;
-        const float bv[3] = {mass * v[0] - (A[0] * fdx0 + A[1] * fdx1 + A[2] * fdx2),
-                             mass * v[1] - (A[3] * fdx0 + A[4] * fdx1 + A[5] * fdx2),
-                             mass * v[2] - (A[6] * fdx0 + A[7] * fdx1 + A[8] * fdx2)};
-        tile_stage(ts, j, mass, bv, A, f, cell);
+      for (int k = 0; k < 3; ++k) {
+        x[k] = q[RC_X + k][tid];
+        v[k] = q[RC_V + k][tid];
       }
-      __syncthreads();
-      tile_cell_ranges(ts, nc);
-      __syncthreads();
-      tile_scatter(ts, dx);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) C[k] = q[RC_C + k][tid];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Sv[k] = q[RC_S + k][tid];
+      float mass = q[RC_M][tid];
+      const int cell = __float_as_int(q[RC_KEY][tid]) & 63;
+      // A = m C - dt Dinv vol tau (contrib of Transfer.cu:868 is -dt Dinv vol P F^T)
+      const float kk = -dt * Dinv;
+      float A[9];
+      A[0] = mass * C[0] + kk * Sv[0];
+      A[1] = mass * C[1] + kk * Sv[3];
+      A[2] = mass * C[2] + kk * Sv[4];
+      A[3] = mass * C[3] + kk * Sv[3];
+      A[4] = mass * C[4] + kk * Sv[1];
+      A[5] = mass * C[5] + kk * Sv[5];
+      A[6] = mass * C[6] + kk * Sv[4];
+      A[7] = mass * C[7] + kk * Sv[5];
+      A[8] = mass * C[8] + kk * Sv[2];
+      const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
+                     s2 = stencil1(x[2], inv_dx);
+      const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
+      if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u ||
+          sort_cell(l0, l1, l2) != cell) {
+        atomicOr(&d.cnt->status, ST_STENCIL);
+        mass = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] = 0.0f;
+        v[0] = v[1] = v[2] = 0.0f;
+      }
+      const float fdx0 = s0.f * dx, fdx1 = s1.f * dx, fdx2 = s2.f * dx;
+      const float b0 = mass * v[0] - (A[0] * fdx0 + A[1] * fdx1 + A[2] * fdx2);
+      const float b1 = mass * v[1] - (A[3] * fdx0 + A[4] * fdx1 + A[5] * fdx2);
+      const float b2 = mass * v[2] - (A[6] * fdx0 + A[7] * fdx1 + A[8] * fdx2);
+      // a_kc = dx A[k][c]: momentum component k, axis c
+      spd[0][tid] = make_float4(mass, b0, b1, b2);
+      spd[1][tid] = make_float4(dx * A[0], dx * A[3], dx * A[6], dx * A[1]);
+      spd[2][tid] = make_float4(dx * A[4], dx * A[7], dx * A[2], dx * A[5]);
+      spd[3][tid] = make_float4(dx * A[8], s2.w[0], s2.w[1], s2.w[2]);
+      sw[tid][0] = s0.w[0];
+      sw[tid][1] = s0.w[1];
+      sw[tid][2] = s0.w[2];
+      sw[tid][3] = s1.w[0];
+      sw[tid][4] = s1.w[1];
+      sw[tid][5] = s1.w[2];
+      scell[tid] = (unsigned char)cell;
     }
-    __syncthreads();
-    tile_store(ts, d.ptile + (long long)b * kTileNodes);
-    __syncthreads();
+    __syncthreads();  // records published, raw free
+    issue(p_nxt);     // next chunk's particle of this thread
+    cp_async_commit();
+    // the slot's 8 range bounds: lane k < 8 finds the first chunk index with
+    // cell >= cz * 16 + col + (k & 1) for cz = k >> 1 (cells sorted)
+    int bnd;
+    {
+      const int k = oij < 8 ? oij : 0;
+      const int c = (k >> 1) * 16 + col + (k & 1);
+      int lo = 0, hi = nc;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (scell[mid] < c)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      bnd = lo;
+    }
+    int qb[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) qb[k] = __shfl_sync(0xffffffffu, bnd, (slot * 9 + k) & 31);
+    if (has_col) {
+#pragma unroll
+      for (int cz = 0; cz < 4; ++cz) {
+        const int q1 = qb[2 * cz + 1];
+        for (int q = qb[2 * cz]; q < q1; ++q) {
+          const float4 u0 = spd[0][q], u1 = spd[1][q], u2 = spd[2][q], u3 = spd[3][q];
+          const float wij = sw[q][wxo] * sw[q][wyo];
+          const float mw = u0.x * wij;
+          // b + a (oi, oj, 0) and the z steps r = a_k2
+          const float p0 = fmaf(u1.w, foj, fmaf(u1.x, foi, u0.y));
+          const float p1 = fmaf(u2.x, foj, fmaf(u1.y, foi, u0.z));
+          const float p2 = fmaf(u2.y, foj, fmaf(u1.z, foi, u0.w));
+          const float r0 = u2.z, r1 = u2.w, r2 = u3.x;
+          const float W0 = wij * u3.y, W1 = wij * u3.z, W2 = wij * u3.w;
+          float4 &n0 = acc[cz], &n1 = acc[cz + 1], &n2 = acc[cz + 2];
+          n0.x = fmaf(mw, u3.y, n0.x);
+          n1.x = fmaf(mw, u3.z, n1.x);
+          n2.x = fmaf(mw, u3.w, n2.x);
+          n0.y = fmaf(W0, p0, n0.y);
+          n0.z = fmaf(W0, p1, n0.z);
+          n0.w = fmaf(W0, p2, n0.w);
+          const float s0 = p0 + r0, s1 = p1 + r1, s2 = p2 + r2;
+          n1.y = fmaf(W1, s0, n1.y);
+          n1.z = fmaf(W1, s1, n1.z);
+          n1.w = fmaf(W1, s2, n1.w);
+          n2.y = fmaf(W2, s0 + r0, n2.y);
+          n2.z = fmaf(W2, s1 + r1, n2.z);
+          n2.w = fmaf(W2, s2 + r2, n2.w);
+        }
+      }
+    }
+    if (nxt.k != cur.k) {  // last chunk of the block: records, then the tile
+      if (has_col) {
+#pragma unroll
+        for (int z = 0; z < 6; ++z) rec[(col * 9 + oij) * 6 + z] = acc[z];
+      }
+#pragma unroll
+      for (int z = 0; z < 6; ++z) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+      __syncthreads();
+      float4 *tile = d.ptile + (long long)(blockIdx.x + cur.k * gridDim.x) * kTileNodes;
+      for (int nd = tid; nd < kTileNodes; nd += kColThreads) {
+        const int I = nd / 36, J = (nd / 6) % 6, Kz = nd % 6;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int oi = 0; oi < 3; ++oi) {
+          const int cx = I - oi;
+          if (cx < 0 || cx > 3) continue;
+#pragma unroll
+          for (int oj = 0; oj < 3; ++oj) {
+            const int cy = J - oj;
+            if (cy < 0 || cy > 3) continue;
+            const float4 r = rec[((cx * 4 + cy) * 9 + oi * 3 + oj) * 6 + Kz];
+            g.x += r.x;
+            g.y += r.y;
+            g.z += r.z;
+            g.w += r.w;
+          }
+        }
+        tile[nd] = g;
+      }
+    }
+    __syncthreads();  // spd, sw, scell and records free
+    cur = nxt;
+    nxt = nn;
+    nn = advance(nn);
+    p_nxt = p_nn;
   }
+  cp_async_wait<0>();
 }
 
 // Grid node sums from the P2G tiles: node (l0, l1, l2) of grid block G lies
@@ -241,51 +436,166 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
   }
 }
 
+// G2P launch metadata of one particle block, held in shared memory for the
+// blocks a CTA owns so that the software pipeline below needs no dependent
+// global loads to find its next chunk.
+struct G2PMeta {
+  int start, cnt, dir, scene;
+  int gb[8];  // grid blocks of the 2x2x2 block neighbourhood (-1: absent)
+};
+
+constexpr int kG2PCh = 19;     // staged particle channels
+constexpr int kG2PMeta = 128;  // blocks per CTA whose metadata is staged
+// staged channel slots
+constexpr int GC_X = 0, GC_F = 3, GC_J = 12, GC_M = 13, GC_VOL = 14, GC_MU = 15, GC_LAM = 16,
+              GC_MAT = 17, GC_ID = 18;
+
+template <int NT>
+constexpr int g2p_smem_bytes() {
+  return 2 * kNodes * 16 + 2 * kG2PCh * NT * 4 + kG2PMeta * (int)sizeof(G2PMeta);
+}
+
+__device__ __forceinline__ G2PMeta g2p_load_meta(const DevPtrs &d, long long n, int b) {
+  G2PMeta m;
+  m.dir = d.bk_dir[b];
+  m.scene = scene_of_dir(d, m.dir);
+  m.start = d.bk_start[b];
+  m.cnt = (int)max(0ll, min((long long)d.bk_count[b], n - m.start));
+  const SceneParams &S = d.scn[m.scene];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) m.gb[t] = neighbour_gb(d, S, m.dir, t);
+  return m;
+}
+
+// G2P (ZSGridToZSParticle, Transfer.cu:1139-1173) with the return mapping and
+// the stress of the new F fused in.  A CTA walks the particle blocks it owns
+// in chunks of NT particles (thread j <-> particle j of the chunk) through a
+// two-stage pipeline: while chunk i computes, the node velocities of chunk
+// i+1's block (216 float4) and chunk i+1's particle channels are in flight
+// as cp.async copies into the other half of double-buffered shared memory,
+// and the permutation entries of chunk i+2 are loading into registers.
 template <bool kFuseRM, bool kFuseBin, int NT>
 __global__ void __launch_bounds__(NT)
     k_g2p(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
           float *__restrict__ pout, int32_t *__restrict__ iout) {
-  __shared__ float sv[3][kNodes];
-  __shared__ int sgb[8];
+  extern __shared__ __align__(16) unsigned char g2p_smem[];
+  float4(*gsm)[kNodes] = reinterpret_cast<float4(*)[kNodes]>(g2p_smem);
+  float(*psm)[kG2PCh][NT] =
+      reinterpret_cast<float(*)[kG2PCh][NT]>(g2p_smem + 2 * kNodes * 16);
+  G2PMeta *meta =
+      reinterpret_cast<G2PMeta *>(g2p_smem + 2 * kNodes * 16 + 2 * kG2PCh * NT * 4);
   const SimParams &P = *d.prm;
-  const long long cap = d.cap;
+  const long long cap = d.cap, n = P.n;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const bool lame = P.has_lame != 0;
-  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    const int dir = d.bk_dir[b];
-    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
-    const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
-    if (threadIdx.x < 8) sgb[threadIdx.x] = neighbour_gb(d, S, dir, threadIdx.x);
-    int K[3];
-    bucket_origin(S, dir - S.dir_off, K);
-    __syncthreads();
-    for (int nd = threadIdx.x; nd < kNodes; nd += NT) {
-      const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
-      const int gb = sgb[((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2)];
-      const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
-      const float4 g =
-          gb >= 0 ? d.grid[(long long)gb * 64 + cell] : make_float4(0.f, 0.f, 0.f, 0.f);
-      sv[0][nd] = g.y;
-      sv[1][nd] = g.z;
-      sv[2][nd] = g.w;
+  const int tid = threadIdx.x;
+  const int nblk = nb > (int)blockIdx.x ? (nb - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  for (int k = tid; k < min(nblk, kG2PMeta); k += NT)
+    meta[k] = g2p_load_meta(d, n, blockIdx.x + k * gridDim.x);
+  __syncthreads();
+
+  // chunk iterator over (k = this CTA's k-th block, c0 = first particle);
+  // `ord` counts blocks, selecting the grid buffer
+  struct Item {
+    int k, c0, ord;
+  };
+  auto cnt_of = [&](int k) {
+    return k < kG2PMeta ? meta[k].cnt : g2p_load_meta(d, n, blockIdx.x + k * gridDim.x).cnt;
+  };
+  auto meta_of = [&](int k) {
+    return k < kG2PMeta ? meta[k] : g2p_load_meta(d, n, blockIdx.x + k * gridDim.x);
+  };
+  auto skip_empty = [&](Item it) {
+    while (it.k < nblk && cnt_of(it.k) == 0) ++it.k;
+    return it;
+  };
+  auto advance = [&](Item it) {
+    if (it.k >= nblk) return it;
+    it.c0 += NT;
+    if (it.c0 >= cnt_of(it.k)) {
+      ++it.k;
+      it.c0 = 0;
+      ++it.ord;
+      it = skip_empty(it);
     }
+    return it;
+  };
+  auto perm_of = [&](const Item &it) {
+    if (it.k >= nblk) return -1;
+    const G2PMeta m = meta_of(it.k);
+    return tid < m.cnt - it.c0 ? d.perm[m.start + it.c0 + tid] : -1;
+  };
+  // issue the copies of chunk `it` into particle buffer `pb`
+  auto issue = [&](const Item &it, int pb, int p) {
+    if (it.c0 == 0) {
+      float4 *g = gsm[it.ord & 1];
+      const bool staged = it.k < kG2PMeta;
+      int dir = 0, scene = 0;
+      if (!staged) {
+        dir = d.bk_dir[blockIdx.x + it.k * gridDim.x];
+        scene = scene_of_dir(d, dir);
+      }
+      for (int nd = tid; nd < kNodes; nd += NT) {
+        const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
+        const int t = ((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2);
+        const int gb = staged ? meta[it.k].gb[t] : neighbour_gb(d, d.scn[scene], dir, t);
+        const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
+        if (gb >= 0)
+          cp_async16(&g[nd], &d.grid[(long long)gb * 64 + cell]);
+        else
+          g[nd] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    if (p >= 0) {
+      float(*q)[NT] = psm[pb];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) cp_async4(&q[GC_X + c][tid], &pin[(CH_X + c) * cap + p]);
+#pragma unroll
+      for (int c = 0; c < 9; ++c) cp_async4(&q[GC_F + c][tid], &pin[(CH_F + c) * cap + p]);
+      cp_async4(&q[GC_J][tid], &pin[CH_J * cap + p]);
+      cp_async4(&q[GC_M][tid], &pin[CH_M * cap + p]);
+      cp_async4(&q[GC_VOL][tid], &pin[CH_VOL * cap + p]);
+      if (lame) {
+        cp_async4(&q[GC_MU][tid], &pin[CH_MU * cap + p]);
+        cp_async4(&q[GC_LAM][tid], &pin[CH_LAM * cap + p]);
+      }
+      cp_async4(&q[GC_MAT][tid], &iin[IC_MAT * cap + p]);
+      cp_async4(&q[GC_ID][tid], &iin[IC_ID * cap + p]);
+    }
+  };
+
+  Item cur = skip_empty(Item{0, 0, 0});
+  Item nxt = advance(cur);
+  Item nn = advance(nxt);
+  int p_cur = perm_of(cur), p_nxt = perm_of(nxt);
+  if (cur.k < nblk) issue(cur, 0, p_cur);
+  cp_async_commit();
+  int buf = 0;
+  while (cur.k < nblk) {
+    const int p_nn = perm_of(nn);  // consumed two iterations from now
+    if (nxt.k < nblk) issue(nxt, buf ^ 1, p_nxt);
+    cp_async_commit();
+    cp_async_wait<1>();  // chunk `cur` has landed
     __syncthreads();
-    const int start = d.bk_start[b];
-    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
-    // warp-uniform trip count: the fused binning below is a warp collective
-    for (int sbase = start; sbase < start + cnt; sbase += NT) {
-      const int s = sbase + (int)threadIdx.x;
-      const bool live = s < start + cnt;
-      const unsigned mask = __ballot_sync(0xffffffffu, live);
-      if (!mask) continue;
-      if (!live) continue;  // live lanes are exactly `mask`
-      const int p = d.perm[s];
-      const int mid = min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1);
+
+    const G2PMeta m = meta_of(cur.k);
+    const SceneParams &S = d.scn[m.scene];
+    const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
+    int K[3];
+    bucket_origin(S, m.dir - S.dir_off, K);
+    const float4 *gv = gsm[cur.ord & 1];
+    const float(*q)[NT] = psm[buf];
+    const bool live = tid < m.cnt - cur.c0;
+    const unsigned mask = __ballot_sync(0xffffffffu, live);
+    if (live) {
+      const int s = m.start + cur.c0 + tid;
+      const int p = p_cur;
+      const int mid = min(max(__float_as_int(q[GC_MAT][tid]), 0), kMaxMaterials - 1);
       const MatParams mp = d.mats[mid];
       float x[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) x[k] = pin[(CH_X + k) * cap + p];
+      for (int k = 0; k < 3; ++k) x[k] = q[GC_X + k][tid];
       const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
                      s2 = stencil1(x[2], inv_dx);
       const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
@@ -300,25 +610,25 @@ __global__ void __launch_bounds__(NT)
         //   Sj = sum_j w_j xj t, Sk = sum_j w_j tk; then over i.
         float xi[3], xj[3], xk[3], wxk[3], wyj[3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          xi[q] = ((float)q - s0.f) * dx;
-          xj[q] = ((float)q - s1.f) * dx;
-          xk[q] = ((float)q - s2.f) * dx;
-          wxk[q] = s2.w[q] * xk[q];
-          wyj[q] = s1.w[q] * xj[q];
+        for (int c = 0; c < 3; ++c) {
+          xi[c] = ((float)c - s0.f) * dx;
+          xj[c] = ((float)c - s1.f) * dx;
+          xk[c] = ((float)c - s2.f) * dx;
+          wxk[c] = s2.w[c] * xk[c];
+          wyj[c] = s1.w[c] * xj[c];
         }
         float cx[3] = {0.f, 0.f, 0.f}, cy[3] = {0.f, 0.f, 0.f}, cz[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          float S[3] = {0.f, 0.f, 0.f}, Sj[3] = {0.f, 0.f, 0.f}, Sk[3] = {0.f, 0.f, 0.f};
+          float Sa[3] = {0.f, 0.f, 0.f}, Sj[3] = {0.f, 0.f, 0.f}, Sk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
           for (int j = 0; j < 3; ++j) {
             const int row = ((l0 + i) * 6 + (l1 + j)) * 6 + l2;
             float t[3] = {0.f, 0.f, 0.f}, tk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
-              const int nd = row + kk;
-              const float g[3] = {sv[0][nd], sv[1][nd], sv[2][nd]};
+              const float4 g4 = gv[row + kk];
+              const float g[3] = {g4.y, g4.z, g4.w};
 #pragma unroll
               for (int a = 0; a < 3; ++a) {
                 t[a] = fmaf(s2.w[kk], g[a], t[a]);
@@ -327,7 +637,7 @@ __global__ void __launch_bounds__(NT)
             }
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-              S[a] = fmaf(s1.w[j], t[a], S[a]);
+              Sa[a] = fmaf(s1.w[j], t[a], Sa[a]);
               Sj[a] = fmaf(wyj[j], t[a], Sj[a]);
               Sk[a] = fmaf(s1.w[j], tk[a], Sk[a]);
             }
@@ -335,8 +645,8 @@ __global__ void __launch_bounds__(NT)
           const float wxi = s0.w[i] * xi[i];
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
-            vel[a] = fmaf(s0.w[i], S[a], vel[a]);
-            cx[a] = fmaf(wxi, S[a], cx[a]);
+            vel[a] = fmaf(s0.w[i], Sa[a], vel[a]);
+            cx[a] = fmaf(wxi, Sa[a], cx[a]);
             cy[a] = fmaf(s0.w[i], Sj[a], cy[a]);
             cz[a] = fmaf(s0.w[i], Sk[a], cz[a]);
           }
@@ -357,11 +667,11 @@ __global__ void __launch_bounds__(NT)
       bool ok_state = true;
       float mu = mp.mu, lam = mp.lam;
       if (lame) {
-        mu = pin[CH_MU * cap + p];
-        lam = pin[CH_LAM * cap + p];
+        mu = q[GC_MU][tid];
+        lam = q[GC_LAM][tid];
       }
       if (mp.type == MPM_EOS) {
-        J = pin[CH_J * cap + p] * (1.0f + dt * (Cn[0] + Cn[4] + Cn[8]));
+        J = q[GC_J][tid] * (1.0f + dt * (Cn[0] + Cn[4] + Cn[8]));
         const float c = cbrtf(J);
 #pragma unroll
         for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? c : 0.0f;
@@ -369,7 +679,7 @@ __global__ void __launch_bounds__(NT)
       } else {
         float Fo[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Fo[k] = pin[(CH_F + k) * cap + p];
+        for (int k = 0; k < 9; ++k) Fo[k] = q[GC_F + k][tid];
         // F <- (I + dt C) F
 #pragma unroll
         for (int r = 0; r < 3; ++r)
@@ -384,7 +694,7 @@ __global__ void __launch_bounds__(NT)
         J = det3(F);
       }
       if (!ok_state) atomicOr(&d.cnt->status, ST_NAN);
-      const float vol = pin[CH_VOL * cap + p];
+      const float vol = q[GC_VOL][tid];
       bool finite = isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(J);
 #pragma unroll
       for (int k = 0; k < 9; ++k) finite = finite && isfinite(F[k]);
@@ -403,7 +713,7 @@ __global__ void __launch_bounds__(NT)
         pout[(CH_F + k) * cap + so] = F[k];
       }
       pout[CH_J * cap + so] = J;
-      pout[CH_M * cap + so] = pin[CH_M * cap + p];
+      pout[CH_M * cap + so] = q[GC_M][tid];
       pout[CH_VOL * cap + so] = vol;
       pout[(CH_S + 0) * cap + so] = vol * tau.xx;
       pout[(CH_S + 1) * cap + so] = vol * tau.yy;
@@ -412,20 +722,27 @@ __global__ void __launch_bounds__(NT)
       pout[(CH_S + 4) * cap + so] = vol * tau.xz;
       pout[(CH_S + 5) * cap + so] = vol * tau.yz;
       if (lame) {
-        pout[CH_MU * cap + so] = pin[CH_MU * cap + p];
-        pout[CH_LAM * cap + so] = pin[CH_LAM * cap + p];
+        pout[CH_MU * cap + so] = mu;
+        pout[CH_LAM * cap + so] = lam;
       }
       iout[IC_MAT * cap + so] = mid;
-      iout[IC_ID * cap + so] = iin[IC_ID * cap + p];
+      iout[IC_ID * cap + so] = __float_as_int(q[GC_ID][tid]);
       if (kFuseBin) {
-        // key of the new position for the next partition (storage slot s)
+        // key of the new position for the next partition (storage slot so)
         const int key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
         d.pkey[so] = key;
         bin_count(d, S, key, mask);
       }
     }
-    __syncthreads();
+    __syncthreads();  // buffers of `cur` free for the chunk after `nxt`
+    cur = nxt;
+    nxt = nn;
+    nn = advance(nn);
+    p_cur = p_nxt;
+    p_nxt = p_nn;
+    buf ^= 1;
   }
+  cp_async_wait<0>();
 }
 
 __device__ __forceinline__ void store_stress(float *__restrict__ pb, long long cap, long long p,
@@ -503,15 +820,20 @@ __global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__r
 }  // namespace
 
 template <int NT> int g2p_occupancy() {
+  constexpr int smem = g2p_smem_bytes<NT>();
+  cudaFuncSetAttribute(k_g2p<true, true, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_g2p<true, false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_g2p<false, false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       smem);
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true, NT>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true, NT>, NT, smem);
   return b > 0 ? b : 1;
 }
 
 void configure_launches(DevPtrs &d) {
   int a = 0;
-  cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, kP2GSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g, kP2GThreads, kP2GSmem);
+  cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g, kColThreads, kColSmem);
   a = a > 0 ? a : 1;
   const LaunchConfig &L = d.launch;
   const int gt = L.g2p_threads == 256 ? 256 : 128;
@@ -524,7 +846,7 @@ void configure_launches(DevPtrs &d) {
 }
 
 void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
-  k_p2g<<<d.grid_p2g, kP2GThreads, kP2GSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+  k_p2g<<<d.grid_p2g, kColThreads, kColSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
 }
 
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
@@ -538,14 +860,15 @@ void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {
 template <int NT>
 void launch_g2p_nt(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
   const int grid = d.grid_g2p;
+  constexpr int smem = g2p_smem_bytes<NT>();
   float *pi = d.pbuf[cur], *po = d.pbuf[1 - cur];
   int32_t *ii = d.ibuf[cur], *io = d.ibuf[1 - cur];
   if (fuse_rm && fuse_bin)
-    k_g2p<true, true, NT><<<grid, NT, 0, s>>>(d, pi, ii, po, io);
+    k_g2p<true, true, NT><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
   else if (fuse_rm)
-    k_g2p<true, false, NT><<<grid, NT, 0, s>>>(d, pi, ii, po, io);
+    k_g2p<true, false, NT><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
   else
-    k_g2p<false, false, NT><<<grid, NT, 0, s>>>(d, pi, ii, po, io);
+    k_g2p<false, false, NT><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
 }
 
 void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
