@@ -77,15 +77,23 @@ constexpr int kColChunk = kColThreads;
 constexpr int kColRaw = 23;            // x3 v3 C9 S6 m key
 constexpr int kColRecs = 16 * 9 * 6;  // float4 records: (column, oi oj, z)
 constexpr int kColMeta = 128;          // blocks per CTA whose metadata is staged
-// shared memory: raw[23][chunk] floats; spd[4][chunk] float4 (m b),
-// (a00 a10 a20 a01), (a11 a21 a02 a12), (a22 wz0 wz1 wz2); sw[chunk][6]
-// wx0..2 wy0..2; the records; the chunk's cells; block metadata
+// shared memory: raw[23][chunk] floats; spd[4][chunk] float4 (b0 b1 a00 a10),
+// (a01 a11 a02 a12), (b2 m a20 a21), (a22 wz0 wz1 wz2), laid out so that
+// the pairs the scatter combines with packed FP32x2 instructions are the
+// halves of one float4; sw[chunk][6] wx0..2 wy0..2; the records; the
+// chunk's cells; block metadata
 constexpr int kColOffSpd = kColRaw * kColChunk * 4;
 constexpr int kColOffW = kColOffSpd + 4 * kColChunk * 16;
 constexpr int kColOffRec = kColOffW + kColChunk * 6 * 4;
 constexpr int kColOffCell = kColOffRec + kColRecs * 16;
 constexpr int kColOffMeta = kColOffCell + ((kColChunk + 15) & ~15);
-constexpr int kColSmem = kColOffMeta + kColMeta * 16;
+// per-block launch metadata staged in shared memory (32 bytes)
+struct ColMeta {
+  int start, cnt, dir, scene;
+  int K[3];  // node index of the block's first node
+  int pad;
+};
+constexpr int kColSmem = kColOffMeta + kColMeta * (int)sizeof(ColMeta);
 static_assert(kColOffSpd % 16 == 0 && kColOffRec % 16 == 0 && kColOffMeta % 16 == 0,
               "float4 / int4 regions must be 16-byte aligned");
 // raw channel slots
@@ -99,7 +107,7 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
   float(*sw)[6] = reinterpret_cast<float(*)[6]>(p2g_smem + kColOffW);
   float4 *rec = reinterpret_cast<float4 *>(p2g_smem + kColOffRec);
   unsigned char *scell = p2g_smem + kColOffCell;
-  int4 *meta = reinterpret_cast<int4 *>(p2g_smem + kColOffMeta);  // (start, cnt, dir, scene)
+  ColMeta *meta = reinterpret_cast<ColMeta *>(p2g_smem + kColOffMeta);
   const SimParams &P = *d.prm;
   const long long cap = d.cap, n = P.n;
   const float dt = P.dt;
@@ -117,7 +125,15 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
     const int b = blockIdx.x + k * gridDim.x;
     const int dir = d.bk_dir[b], start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], n - start));
-    return make_int4(start, cnt, dir, scene_of_dir(d, dir));
+    ColMeta m;
+    m.start = start;
+    m.cnt = cnt;
+    m.dir = dir;
+    m.scene = scene_of_dir(d, dir);
+    const SceneParams &S = d.scn[m.scene];
+    bucket_origin(S, dir - S.dir_off, m.K);
+    m.pad = 0;
+    return m;
   };
   for (int k = tid; k < min(nblk, kColMeta); k += kColThreads) meta[k] = load_meta(k);
   __syncthreads();
@@ -127,13 +143,13 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
     int k, c0;
   };
   auto skip_empty = [&](Item it) {
-    while (it.k < nblk && meta_of(it.k).y == 0) ++it.k;
+    while (it.k < nblk && meta_of(it.k).cnt == 0) ++it.k;
     return it;
   };
   auto advance = [&](Item it) {
     if (it.k >= nblk) return it;
     it.c0 += kColChunk;
-    if (it.c0 >= meta_of(it.k).y) {
+    if (it.c0 >= meta_of(it.k).cnt) {
       ++it.k;
       it.c0 = 0;
       it = skip_empty(it);
@@ -142,8 +158,8 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
   };
   auto perm_of = [&](const Item &it) {
     if (it.k >= nblk) return -1;
-    const int4 m = meta_of(it.k);
-    return tid < m.y - it.c0 ? d.perm[m.x + it.c0 + tid] : -1;
+    const ColMeta m = meta_of(it.k);
+    return tid < m.cnt - it.c0 ? d.perm[m.start + it.c0 + tid] : -1;
   };
   auto issue = [&](int p) {
     if (p < 0) return;
@@ -161,9 +177,11 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
     cp_async4(&q[RC_KEY][tid], &d.pkey[p]);
   };
 
-  float4 acc[6];
+  // node sums of the lane's 6 column nodes: (mom0, mom1) and (mom2, mass)
+  float2 accP[6], accQ[6];
 #pragma unroll
-  for (int z = 0; z < 6; ++z) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int z = 0; z < 6; ++z) accP[z] = accQ[z] = make_float2(0.f, 0.f);
+  const float2 oi2 = make_float2(foi, foi), oj2 = make_float2(foj, foj);
   Item cur = skip_empty(Item{0, 0});
   Item nxt = advance(cur);
   Item nn = advance(nxt);
@@ -172,12 +190,11 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
   cp_async_commit();
   while (cur.k < nblk) {
     const int p_nn = perm_of(nn);
-    const int4 m = meta_of(cur.k);
-    const SceneParams &S = d.scn[m.w];
+    const ColMeta m = meta_of(cur.k);
+    const SceneParams &S = d.scn[m.scene];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
-    int K[3];
-    bucket_origin(S, m.z - S.dir_off, K);
-    const int nc = min(kColChunk, m.y - cur.c0);
+    const int K[3] = {m.K[0], m.K[1], m.K[2]};
+    const int nc = min(kColChunk, m.cnt - cur.c0);
     cp_async_wait<0>();  // this thread's particle of chunk `cur` has landed
     // convert particle tid of the chunk into its scatter record
     if (tid < nc) {
@@ -222,9 +239,9 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
       const float b1 = mass * v[1] - (A[3] * fdx0 + A[4] * fdx1 + A[5] * fdx2);
       const float b2 = mass * v[2] - (A[6] * fdx0 + A[7] * fdx1 + A[8] * fdx2);
       // a_kc = dx A[k][c]: momentum component k, axis c
-      spd[0][tid] = make_float4(mass, b0, b1, b2);
-      spd[1][tid] = make_float4(dx * A[0], dx * A[3], dx * A[6], dx * A[1]);
-      spd[2][tid] = make_float4(dx * A[4], dx * A[7], dx * A[2], dx * A[5]);
+      spd[0][tid] = make_float4(b0, b1, dx * A[0], dx * A[3]);
+      spd[1][tid] = make_float4(dx * A[1], dx * A[4], dx * A[2], dx * A[5]);
+      spd[2][tid] = make_float4(b2, mass, dx * A[6], dx * A[7]);
       spd[3][tid] = make_float4(dx * A[8], s2.w[0], s2.w[1], s2.w[2]);
       sw[tid][0] = s0.w[0];
       sw[tid][1] = s0.w[1];
@@ -263,37 +280,37 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
         for (int q = qb[2 * cz]; q < q1; ++q) {
           const float4 u0 = spd[0][q], u1 = spd[1][q], u2 = spd[2][q], u3 = spd[3][q];
           const float wij = sw[q][wxo] * sw[q][wyo];
-          const float mw = u0.x * wij;
-          // b + a (oi, oj, 0) and the z steps r = a_k2
-          const float p0 = fmaf(u1.w, foj, fmaf(u1.x, foi, u0.y));
-          const float p1 = fmaf(u2.x, foj, fmaf(u1.y, foi, u0.z));
-          const float p2 = fmaf(u2.y, foj, fmaf(u1.z, foi, u0.w));
-          const float r0 = u2.z, r1 = u2.w, r2 = u3.x;
-          const float W0 = wij * u3.y, W1 = wij * u3.z, W2 = wij * u3.w;
-          float4 &n0 = acc[cz], &n1 = acc[cz + 1], &n2 = acc[cz + 2];
-          n0.x = fmaf(mw, u3.y, n0.x);
-          n1.x = fmaf(mw, u3.z, n1.x);
-          n2.x = fmaf(mw, u3.w, n2.x);
-          n0.y = fmaf(W0, p0, n0.y);
-          n0.z = fmaf(W0, p1, n0.z);
-          n0.w = fmaf(W0, p2, n0.w);
-          const float s0 = p0 + r0, s1 = p1 + r1, s2 = p2 + r2;
-          n1.y = fmaf(W1, s0, n1.y);
-          n1.z = fmaf(W1, s1, n1.z);
-          n1.w = fmaf(W1, s2, n1.w);
-          n2.y = fmaf(W2, s0 + r0, n2.y);
-          n2.z = fmaf(W2, s1 + r1, n2.z);
-          n2.w = fmaf(W2, s2 + r2, n2.w);
+          // node values b + a (oi, oj, oz): (k = 0, 1) as one pair, k = 2 and
+          // the mass as the other; the z steps are r = a_k2
+          float2 s01 = __ffma2_rn(make_float2(u1.x, u1.y), oj2,
+                                  __ffma2_rn(make_float2(u0.z, u0.w), oi2,
+                                             make_float2(u0.x, u0.y)));
+          float2 s2m = make_float2(fmaf(u2.w, foj, fmaf(u2.z, foi, u2.x)), u2.y);
+          const float2 r01 = make_float2(u1.z, u1.w);
+          const float r2 = u3.x;
+          const float wz[3] = {u3.y, u3.z, u3.w};
+#pragma unroll
+          for (int oz = 0; oz < 3; ++oz) {
+            const float W = wij * wz[oz];
+            const float2 W2 = make_float2(W, W);
+            accP[cz + oz] = __ffma2_rn(W2, s01, accP[cz + oz]);
+            accQ[cz + oz] = __ffma2_rn(W2, s2m, accQ[cz + oz]);
+            if (oz < 2) {
+              s01 = __fadd2_rn(s01, r01);
+              s2m.x += r2;
+            }
+          }
         }
       }
     }
     if (nxt.k != cur.k) {  // last chunk of the block: records, then the tile
       if (has_col) {
 #pragma unroll
-        for (int z = 0; z < 6; ++z) rec[(col * 9 + oij) * 6 + z] = acc[z];
+        for (int z = 0; z < 6; ++z)
+          rec[(col * 9 + oij) * 6 + z] = make_float4(accQ[z].y, accP[z].x, accP[z].y, accQ[z].x);
       }
 #pragma unroll
-      for (int z = 0; z < 6; ++z) acc[z] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int z = 0; z < 6; ++z) accP[z] = accQ[z] = make_float2(0.f, 0.f);
       __syncthreads();
       float4 *tile = d.ptile + (long long)(blockIdx.x + cur.k * gridDim.x) * kTileNodes;
       for (int nd = tid; nd < kTileNodes; nd += kColThreads) {
@@ -442,6 +459,8 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
 struct G2PMeta {
   int start, cnt, dir, scene;
   int gb[8];  // grid blocks of the 2x2x2 block neighbourhood (-1: absent)
+  int K[3];   // node index of the block's first node
+  int pad;
 };
 
 constexpr int kG2PCh = 19;     // staged particle channels
@@ -464,6 +483,8 @@ __device__ __forceinline__ G2PMeta g2p_load_meta(const DevPtrs &d, long long n, 
   const SceneParams &S = d.scn[m.scene];
 #pragma unroll
   for (int t = 0; t < 8; ++t) m.gb[t] = neighbour_gb(d, S, m.dir, t);
+  bucket_origin(S, m.dir - S.dir_off, m.K);
+  m.pad = 0;
   return m;
 }
 
@@ -582,8 +603,7 @@ __global__ void __launch_bounds__(NT)
     const G2PMeta m = meta_of(cur.k);
     const SceneParams &S = d.scn[m.scene];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
-    int K[3];
-    bucket_origin(S, m.dir - S.dir_off, K);
+    const int K[3] = {m.K[0], m.K[1], m.K[2]};
     const float4 *gv = gsm[cur.ord & 1];
     const float(*q)[NT] = psm[buf];
     const bool live = tid < m.cnt - cur.c0;
