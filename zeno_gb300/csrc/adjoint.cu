@@ -59,7 +59,6 @@ __global__ void __launch_bounds__(kP2GThreads)
   float4 *sg = reinterpret_cast<float4 *>(adj_smem + kAdjSgOffset);
   __shared__ int sgb[8];
   const SimParams &P = *d.prm;
-  const long long cap = d.cap;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const int tid = threadIdx.x;
@@ -88,13 +87,13 @@ __global__ void __launch_bounds__(kP2GThreads)
         float x[3], F[9], xb[3], vb[3], Cb[9], Fb[9];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          x[k] = pin[(CH_X + k) * cap + p];
+          x[k] = pin[pidx((CH_X + k), p)];
           xb[k] = an[(AJ_X + k) * n + p];
           vb[k] = an[(AJ_V + k) * n + p] + dt * xb[k];
         }
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-          F[k] = pin[(CH_F + k) * cap + p];
+          F[k] = pin[pidx((CH_F + k), p)];
           Fb[k] = an[(AJ_F + k) * n + p];
           Cb[k] = an[(AJ_C + k) * n + p];
         }
@@ -258,7 +257,6 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
   __shared__ float4 sg[kNodes];
   __shared__ int sgb[8];
   const SimParams &P = *d.prm;
-  const long long cap = d.cap;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const bool lame = P.has_lame != 0;
@@ -281,25 +279,25 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     for (int s = start + threadIdx.x; s < start + cnt; s += kP2GAdjThreads) {
       const int p = d.perm[s];
-      const MatParams mp = d.mats[min(max(iin[IC_MAT * cap + p], 0), kMaxMaterials - 1)];
+      const MatParams mp = d.mats[min(max(iin[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
       float x[3], v[3], C[9], F[9], Sv[6];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        x[k] = pin[(CH_X + k) * cap + p];
-        v[k] = pin[(CH_V + k) * cap + p];
+        x[k] = pin[pidx((CH_X + k), p)];
+        v[k] = pin[pidx((CH_V + k), p)];
       }
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
-        C[k] = pin[(CH_C + k) * cap + p];
-        F[k] = pin[(CH_F + k) * cap + p];
+        C[k] = pin[pidx((CH_C + k), p)];
+        F[k] = pin[pidx((CH_F + k), p)];
       }
 #pragma unroll
-      for (int k = 0; k < 6; ++k) Sv[k] = pin[(CH_S + k) * cap + p];
-      const float mass = pin[CH_M * cap + p], vol = pin[CH_VOL * cap + p];
+      for (int k = 0; k < 6; ++k) Sv[k] = pin[pidx((CH_S + k), p)];
+      const float mass = pin[pidx(CH_M, p)], vol = pin[pidx(CH_VOL, p)];
       float mu = mp.mu, lam = mp.lam;
       if (lame) {
-        mu = pin[CH_MU * cap + p];
-        lam = pin[CH_LAM * cap + p];
+        mu = pin[pidx(CH_MU, p)];
+        lam = pin[pidx(CH_LAM, p)];
       }
       const float kk = -dt * Dinv;
       const float A[9] = {mass * C[0] + kk * Sv[0], mass * C[1] + kk * Sv[3],

@@ -63,10 +63,13 @@ struct mpm_ctx {
 
 namespace {
 
+// A capacity overflow drops particle or grid blocks, so whatever the next
+// substeps flag (stale slots binned out of the domain, non-finite values) is
+// its consequence: it is reported first.
 int32_t map_status(int bits) {
+  if (bits & ST_CAPACITY) return MPM_ERR_CAPACITY;
   if (bits & ST_NAN) return MPM_ERR_NAN;
   if (bits & ST_OUT_OF_DOMAIN) return MPM_ERR_OUT_OF_DOMAIN;
-  if (bits & ST_CAPACITY) return MPM_ERR_CAPACITY;
   if (bits & ST_TIMEOUT) return MPM_ERR_TIMEOUT;
   if (bits & ST_STENCIL) return MPM_ERR_CFL;
   return MPM_OK;  // ST_BUCKET_OVERSIZE only affects the in-block order
@@ -284,8 +287,8 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
   d.n_scenes = n_scenes;
   configure_launches(d);
   for (int k = 0; k < 2; ++k) {
-    if ((rc = dalloc(c, &d.pbuf[k], (size_t)NCH * cap))) return bail(rc);
-    if ((rc = dalloc(c, &d.ibuf[k], (size_t)NICH * cap))) return bail(rc);
+    if ((rc = dalloc(c, &d.pbuf[k], (size_t)tiled_elems(cap, NCH)))) return bail(rc);
+    if ((rc = dalloc(c, &d.ibuf[k], (size_t)tiled_elems(cap, NICH)))) return bail(rc);
   }
   if ((rc = dalloc(c, &d.pkey, cap)) || (rc = dalloc(c, &d.perm, cap)) ||
       (rc = dalloc(c, &d.perm_tmp, cap)) ||
@@ -303,8 +306,8 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
     return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
   // every slot of the particle-indexed buffers starts as a valid index / id
   for (int k = 0; k < 2; ++k) {
-    cudaMemsetAsync(d.pbuf[k], 0, (size_t)NCH * cap * sizeof(float), c->stream);
-    cudaMemsetAsync(d.ibuf[k], 0, (size_t)NICH * cap * sizeof(int32_t), c->stream);
+    cudaMemsetAsync(d.pbuf[k], 0, (size_t)tiled_elems(cap, NCH) * sizeof(float), c->stream);
+    cudaMemsetAsync(d.ibuf[k], 0, (size_t)tiled_elems(cap, NICH) * sizeof(int32_t), c->stream);
   }
   cudaMemsetAsync(d.perm, 0, (size_t)cap * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.pkey, 0, (size_t)cap * sizeof(int32_t), c->stream);
@@ -762,10 +765,8 @@ int32_t mpm_state_save(mpm_ctx *c, float *dst) {
   if (!dst) return fail(MPM_ERR_INVALID, "null destination");
   const size_t n = (size_t)c->prm.n;
   if (n == 0) return MPM_OK;
-  ZS_CUDA(cudaMemcpy2DAsync(dst, n * sizeof(float), c->d.pbuf[c->cur], c->d.cap * sizeof(float),
-                            n * sizeof(float), MPM_STATE_PLANES, cudaMemcpyDeviceToDevice,
-                            c->stream));
-  return MPM_OK;
+  launch_state_copy(c->d, c->cur, dst, nullptr, (long long)n, c->stream);
+  return launch_check("state save");
 }
 
 int32_t mpm_state_load(mpm_ctx *c, const float *src) {
@@ -775,9 +776,7 @@ int32_t mpm_state_load(mpm_ctx *c, const float *src) {
   if (!src) return fail(MPM_ERR_INVALID, "null source");
   const size_t n = (size_t)c->prm.n;
   if (n == 0) return MPM_OK;
-  ZS_CUDA(cudaMemcpy2DAsync(c->d.pbuf[c->cur], c->d.cap * sizeof(float), src, n * sizeof(float),
-                            n * sizeof(float), MPM_STATE_PLANES, cudaMemcpyDeviceToDevice,
-                            c->stream));
+  launch_state_copy(c->d, c->cur, nullptr, src, (long long)n, c->stream);
   if ((rc = push_params(c))) return rc;
   launch_stress(c->d, c->cur, c->stream);
   if ((rc = launch_check("state load"))) return rc;
@@ -859,13 +858,14 @@ int32_t mpm_partition_download(mpm_ctx *c, int32_t *n_pb, int32_t *pb_dir, int32
   if (gb_dir) ZS_CUDA(cudaMemcpy(gb_dir, c->d.gb_dir, ng * sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (perm) {
     const long long n = c->prm.n;
-    std::vector<int32_t> p(n), id(n);
+    std::vector<int32_t> p(n), ib((size_t)tiled_elems(n, NICH));
     ZS_CUDA(cudaMemcpy(p.data(), c->d.perm, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    ZS_CUDA(cudaMemcpy(id.data(), c->d.ibuf[c->cur] + (size_t)IC_ID * c->d.cap,
-                       n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    // the id channel of the first n slots (tiles of the int store)
+    ZS_CUDA(cudaMemcpy(ib.data(), c->d.ibuf[c->cur], ib.size() * sizeof(int32_t),
+                       cudaMemcpyDeviceToHost));
     const int binned = std::min<long long>(c->h_cnt->n_binned, n);
     for (long long s = 0; s < n; ++s)
-      perm[s] = (s < binned && p[s] >= 0 && p[s] < n) ? id[p[s]] : -1;
+      perm[s] = (s < binned && p[s] >= 0 && p[s] < n) ? ib[iidx(IC_ID, p[s])] : -1;
   }
   return MPM_OK;
 }

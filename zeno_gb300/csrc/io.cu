@@ -16,23 +16,23 @@ __global__ void k_ingest(float *__restrict__ pb, int32_t *__restrict__ ib, long 
        i += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      pb[(CH_X + k) * cap + i] = src.x[3 * i + k];
-      pb[(CH_V + k) * cap + i] = src.v ? src.v[3 * i + k] : 0.0f;
+      pb[pidx((CH_X + k), i)] = src.x[3 * i + k];
+      pb[pidx((CH_V + k), i)] = src.v ? src.v[3 * i + k] : 0.0f;
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      pb[(CH_C + k) * cap + i] = src.C ? src.C[9 * i + k] : 0.0f;
-      pb[(CH_F + k) * cap + i] = src.F ? src.F[9 * i + k] : ((k % 4 == 0) ? 1.0f : 0.0f);
+      pb[pidx((CH_C + k), i)] = src.C ? src.C[9 * i + k] : 0.0f;
+      pb[pidx((CH_F + k), i)] = src.F ? src.F[9 * i + k] : ((k % 4 == 0) ? 1.0f : 0.0f);
     }
-    pb[CH_J * cap + i] = src.J ? src.J[i] : 1.0f;
-    pb[CH_M * cap + i] = src.m[i];
-    pb[CH_VOL * cap + i] = src.vol[i];
+    pb[pidx(CH_J, i)] = src.J ? src.J[i] : 1.0f;
+    pb[pidx(CH_M, i)] = src.m[i];
+    pb[pidx(CH_VOL, i)] = src.vol[i];
     if (src.mu) {
-      pb[CH_MU * cap + i] = src.mu[i];
-      pb[CH_LAM * cap + i] = src.lam[i];
+      pb[pidx(CH_MU, i)] = src.mu[i];
+      pb[pidx(CH_LAM, i)] = src.lam[i];
     }
-    ib[IC_MAT * cap + i] = src.mat ? src.mat[i] : 0;
-    ib[IC_ID * cap + i] = (int32_t)i;
+    ib[iidx(IC_MAT, i)] = src.mat ? src.mat[i] : 0;
+    ib[iidx(IC_ID, i)] = (int32_t)i;
   }
 }
 
@@ -42,19 +42,19 @@ __global__ void k_egest(const float *__restrict__ pb, const int32_t *__restrict_
   float *x = dst, *v = dst + 3 * n, *C = dst + 6 * n, *F = dst + 15 * n, *J = dst + 24 * n;
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
        s += (long long)gridDim.x * blockDim.x) {
-    const long long u = ib[IC_ID * cap + s];
+    const long long u = ib[iidx(IC_ID, s)];
     if (u < 0 || u >= n) continue;  // slot not rewritten after a binning error
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      x[3 * u + k] = pb[(CH_X + k) * cap + s];
-      v[3 * u + k] = pb[(CH_V + k) * cap + s];
+      x[3 * u + k] = pb[pidx((CH_X + k), s)];
+      v[3 * u + k] = pb[pidx((CH_V + k), s)];
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      C[9 * u + k] = pb[(CH_C + k) * cap + s];
-      F[9 * u + k] = pb[(CH_F + k) * cap + s];
+      C[9 * u + k] = pb[pidx((CH_C + k), s)];
+      F[9 * u + k] = pb[pidx((CH_F + k), s)];
     }
-    J[u] = pb[CH_J * cap + s];
+    J[u] = pb[pidx(CH_J, s)];
   }
 }
 
@@ -64,14 +64,36 @@ __global__ void k_set_lame(float *__restrict__ pb, const int32_t *__restrict__ i
                            long long n) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
        s += (long long)gridDim.x * blockDim.x) {
-    const long long u = ib[IC_ID * cap + s];
+    const long long u = ib[iidx(IC_ID, s)];
     if (u < 0 || u >= n) continue;
-    pb[CH_MU * cap + s] = mu[u];
-    pb[CH_LAM * cap + s] = lam[u];
+    pb[pidx(CH_MU, s)] = mu[u];
+    pb[pidx(CH_LAM, s)] = lam[u];
+  }
+}
+
+// state planes [MPM_STATE_PLANES][n] (x v C F J of every slot) <-> the
+// first channels of the tiled store: dst != null saves, src != null loads
+__global__ void k_state_copy(float *__restrict__ pb, float *__restrict__ dst,
+                             const float *__restrict__ src, long long n) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < MPM_STATE_PLANES; ++k) {
+      if (dst)
+        dst[k * n + s] = pb[pidx(k, s)];
+      else
+        pb[pidx(k, s)] = src[k * n + s];
+    }
   }
 }
 
 }  // namespace
+
+void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
+                       cudaStream_t s) {
+  if (n <= 0) return;
+  k_state_copy<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], dst, src, n);
+}
 
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
                      cudaStream_t s) {

@@ -159,6 +159,7 @@ extern "C" int32_t mpm_partition_noalloc(const float *x_planes, int64_t n, float
 
   DevPtrs d{};
   d.pbuf[0] = const_cast<float *>(x_planes);  // planes x[0..n), y[n..2n), z[2n..3n)
+  d.planar_x = 1;
   d.cap = n > 0 ? n : 1;
   d.pkey = reinterpret_cast<int32_t *>(base + kOffKeys);
   d.perm = perm;

@@ -16,23 +16,20 @@
 //           rewrites every directory entry it reads (grid block / particle
 //           block index or -1) and zeroes the counts for the next binning,
 //           so no separate reset is needed
-//   scatter warp-aggregated placement of particle indices into their block
-//   sort    per block, counting sort by cell plus a per-cell insertion sort:
-//           the canonical (block, cell, index) order, independent of atomic
-//           timing
+//   scatter placement of particle indices into their block, one global
+//           atomic per (CTA, block) after a shared-memory count
+//   sort    per block, counting sort by cell and a rank by storage index
+//           inside each cell: the canonical (block, cell, index) order,
+//           independent of atomic timing
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "binning.cuh"
 #include "zsmpm_internal.cuh"
 
 namespace zsmpm {
 namespace {
-
-__device__ __forceinline__ unsigned lanemask_lt() {
-  unsigned m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
 
 __global__ void k_full_dir_clear(DevPtrs d) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.ndir;
@@ -64,8 +61,10 @@ __global__ void k_bin(DevPtrs d, const float *__restrict__ pin) {
     int scene = 0;
     if (i < n) {
       scene = scene_of_particle(d, i);
-      key = bin_key(d.scn[scene], pin[CH_X * cap + i], pin[(CH_X + 1) * cap + i],
-                    pin[(CH_X + 2) * cap + i], &d.cnt->status);
+      float x[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) x[k] = d.planar_x ? pin[k * cap + i] : pin[pidx(CH_X + k, i)];
+      key = bin_key(d.scn[scene], x[0], x[1], x[2], &d.cnt->status);
       d.pkey[i] = key;
     }
     bin_count(d, d.scn[scene], key, 0xffffffffu);
@@ -223,40 +222,87 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
   }
 }
 
-__global__ void k_scatter(DevPtrs d) {
+// Placement of particle indices into their block's range.  A CTA takes
+// kScatterPerCta consecutive storage slots, which (storage following the
+// previous partition) hold few distinct blocks: it counts them in a small
+// shared-memory table, reserves each block's share with one global atomic,
+// and places its particles from there.  A key that finds no table slot is
+// placed with its own global atomic.  The order inside a block is left to
+// the bucket sort.
+constexpr int kScatterThreads = 256;
+constexpr int kScatterPer = 4;
+constexpr int kScatterPerCta = kScatterThreads * kScatterPer;
+constexpr int kScatterSlots = 64;
+
+__global__ void __launch_bounds__(kScatterThreads) k_scatter(DevPtrs d) {
+  __shared__ int tkey[kScatterSlots], tcount[kScatterSlots], tbase[kScatterSlots];
   const long long n = d.prm->n;
-  const int lane = threadIdx.x & 31;
-  const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) - lane;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long w = warp0; w < n; w += stride) {
-    const long long i = w + lane;
-    const int key = (i < n) ? d.pkey[i] : -1;
-    const int dd = key >> 6;
-    const unsigned peers = __match_any_sync(0xffffffffu, dd);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (key >= 0 && lane == leader) base = atomicAdd(&d.dir_fill[dd], __popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (key >= 0) {
-      const long long pos = (long long)base + __popc(peers & lanemask_lt());
+  const int tid = threadIdx.x;
+  for (long long c0 = (long long)blockIdx.x * kScatterPerCta; c0 < n;
+       c0 += (long long)gridDim.x * kScatterPerCta) {
+    if (tid < kScatterSlots) {
+      tkey[tid] = -1;
+      tcount[tid] = 0;
+    }
+    __syncthreads();
+    int slot[kScatterPer], rank[kScatterPer], dd[kScatterPer];
+    const int lane = tid & 31;
+#pragma unroll
+    for (int k = 0; k < kScatterPer; ++k) {
+      const long long i = c0 + k * kScatterThreads + tid;
+      const int key = i < n ? d.pkey[i] : -1;
+      dd[k] = key >> 6;
+      // warp aggregation first: the leader of each key's peers takes the
+      // table entry and the peers' share of its count
+      const unsigned peers = __match_any_sync(0xffffffffu, dd[k]);
+      const int leader = __ffs(peers) - 1;
+      int t_slot = -1, base = 0;
+      if (key >= 0 && lane == leader) {
+        const int h = (int)(((unsigned)dd[k] * 2654435761u) >> 26);  // 6-bit hash
+        for (int probe = 0; probe < kScatterSlots; ++probe) {
+          const int t = (h + probe) & (kScatterSlots - 1);
+          const int old = atomicCAS(&tkey[t], -1, dd[k]);
+          if (old == -1 || old == dd[k]) {
+            t_slot = t;
+            base = atomicAdd(&tcount[t], __popc(peers));
+            break;
+          }
+        }
+        if (t_slot < 0) base = atomicAdd(&d.dir_fill[dd[k]], __popc(peers));  // table full
+      }
+      slot[k] = __shfl_sync(0xffffffffu, t_slot, leader);
+      rank[k] = __shfl_sync(0xffffffffu, base, leader) + __popc(peers & ((1u << lane) - 1u));
+    }
+    __syncthreads();
+    if (tid < kScatterSlots && tkey[tid] >= 0)
+      tbase[tid] = atomicAdd(&d.dir_fill[tkey[tid]], tcount[tid]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScatterPer; ++k) {
+      const long long i = c0 + k * kScatterThreads + tid;
+      if (i >= n || dd[k] < 0) continue;
+      const long long pos = slot[k] >= 0 ? (long long)tbase[slot[k]] + rank[k] : rank[k];
       if (pos < n)
         d.perm[pos] = (int)i;
       else  // stale directory counts after an earlier overflow
         atomicOr(&d.cnt->status, ST_CAPACITY);
     }
+    __syncthreads();  // table reused
   }
 }
 
 // Canonical order inside each particle block: (cell, storage index).
-// A counting sort by cell id (64 bins, integer shared-memory atomics) followed
-// by an insertion sort of each cell's few particles by storage index.  A cell
-// with more than kCellSortMax particles sends the block to an on-chip bitonic
-// sort; a block with more than kSortCap particles is sorted the same way
-// through global scratch (slower; flagged with the informational
-// ST_BUCKET_OVERSIZE bit).
+// A counting sort by cell id (64 bins, integer shared-memory atomics) puts
+// each cell's particles in a contiguous range in arbitrary order; each
+// particle's final slot is then the start of its cell plus the number of the
+// cell's particles with a smaller storage index, all ranks computed at once.
+// A cell with more than kCellSortMax particles sends the block to an on-chip
+// bitonic sort; a block with more than kSortCap particles is sorted through
+// global scratch (slower; flagged with the informational ST_BUCKET_OVERSIZE
+// bit).
 constexpr int kSortThreads = 256;
 constexpr int kSortCap = 2048;
-constexpr int kCellSortMax = 64;
+constexpr int kCellSortMax = 256;
 
 __device__ __forceinline__ void warp_exclusive_scan64(const int *in, int *out) {
   // one warp: 64 values, two per lane
@@ -277,7 +323,7 @@ __device__ __forceinline__ void warp_exclusive_scan64(const int *in, int *out) {
 __global__ void __launch_bounds__(kSortThreads) k_bucket_sort(DevPtrs d) {
   __shared__ __align__(16) int sbuf[2 * kSortCap];
   int *sp = sbuf, *op = sbuf + kSortCap;
-  __shared__ unsigned char sc[kSortCap];
+  __shared__ unsigned char sc[kSortCap], oc[kSortCap];
   __shared__ int ccount[64], cstart[65], cfill[64];
   __shared__ int big_cell;
   const int nb = d.cnt->n_buckets;
@@ -303,30 +349,24 @@ __global__ void __launch_bounds__(kSortThreads) k_bucket_sort(DevPtrs d) {
       }
       __syncthreads();
       if (tid < 32) warp_exclusive_scan64(ccount, cstart);
+      if (tid < 64 && ccount[tid] > kCellSortMax) big_cell = 1;
       __syncthreads();
-      for (int j = tid; j < cnt; j += kSortThreads) {
-        const int c = sc[j];
-        op[cstart[c] + atomicAdd(&cfill[c], 1)] = sp[j];
-      }
-      __syncthreads();
-      if (tid < 64) {
-        const int lo = cstart[tid], hi = cstart[tid + 1];
-        if (hi - lo > kCellSortMax) {
-          big_cell = 1;
-        } else {
-          for (int i = lo + 1; i < hi; ++i) {
-            const int v = op[i];
-            int k = i - 1;
-            while (k >= lo && op[k] > v) {
-              op[k + 1] = op[k];
-              --k;
-            }
-            op[k + 1] = v;
-          }
+      if (!big_cell) {
+        for (int j = tid; j < cnt; j += kSortThreads) {
+          const int c = sc[j];
+          const int o = cstart[c] + atomicAdd(&cfill[c], 1);
+          op[o] = sp[j];
+          oc[o] = (unsigned char)c;
         }
-      }
-      __syncthreads();
-      if (big_cell) {
+        __syncthreads();
+        for (int j = tid; j < cnt; j += kSortThreads) {
+          const int c = oc[j], v = op[j];
+          const int lo = cstart[c], hi = cstart[c + 1];
+          int r = lo;
+          for (int i = lo; i < hi; ++i) r += op[i] < v;
+          d.perm[start + r] = v;
+        }
+      } else {
         // bitonic sort of (cell << 32 | index) over the whole block
         unsigned long long *key = reinterpret_cast<unsigned long long *>(sbuf);  // 16 KB
         int N = 2;
@@ -358,8 +398,6 @@ __global__ void __launch_bounds__(kSortThreads) k_bucket_sort(DevPtrs d) {
         }
         for (int j = tid; j < cnt; j += kSortThreads)
           d.perm[start + j] = (int)(key[j] & 0xffffffffull);
-      } else {
-        for (int j = tid; j < cnt; j += kSortThreads) d.perm[start + j] = op[j];
       }
     } else {
       // oversize block: counting sort by cell through global scratch
@@ -421,8 +459,11 @@ void launch_scan(const DevPtrs &d, cudaStream_t s) {
   k_scan_apply<<<d.ntiles, kScanThreads, 0, s>>>(d);
 }
 
+// one chunk per CTA up to the capacity (fixed for graph capture)
 void launch_scatter(const DevPtrs &d, cudaStream_t s) {
-  k_scatter<<<d.grid_stream > 0 ? d.grid_stream : grid_for(d, 8), 256, 0, s>>>(d);
+  const long long g = (d.cap + kScatterPerCta - 1) / kScatterPerCta;
+  k_scatter<<<(int)std::min<long long>(std::max<long long>(g, 1), 1 << 30), kScatterThreads, 0,
+              s>>>(d);
 }
 
 void launch_bucket_sort(const DevPtrs &d, cudaStream_t s) {

@@ -99,7 +99,7 @@ static_assert(kColOffSpd % 16 == 0 && kColOffRec % 16 == 0 && kColOffMeta % 16 =
 // raw channel slots
 constexpr int RC_X = 0, RC_V = 3, RC_C = 6, RC_S = 15, RC_M = 21, RC_KEY = 22;
 
-__global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__restrict__ pin,
+__global__ void __launch_bounds__(kColThreads, 4) k_p2g(DevPtrs d, const float *__restrict__ pin,
                                                      const int32_t *__restrict__ iin) {
   extern __shared__ __align__(16) unsigned char p2g_smem[];
   float(*raw)[kColChunk] = reinterpret_cast<float(*)[kColChunk]>(p2g_smem);
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
   unsigned char *scell = p2g_smem + kColOffCell;
   ColMeta *meta = reinterpret_cast<ColMeta *>(p2g_smem + kColOffMeta);
   const SimParams &P = *d.prm;
-  const long long cap = d.cap, n = P.n;
+  const long long n = P.n;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -166,14 +166,14 @@ __global__ void __launch_bounds__(kColThreads) k_p2g(DevPtrs d, const float *__r
     float(*q)[kColChunk] = raw;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      cp_async4(&q[RC_X + c][tid], &pin[(CH_X + c) * cap + p]);
-      cp_async4(&q[RC_V + c][tid], &pin[(CH_V + c) * cap + p]);
+      cp_async4(&q[RC_X + c][tid], &pin[pidx((CH_X + c), p)]);
+      cp_async4(&q[RC_V + c][tid], &pin[pidx((CH_V + c), p)]);
     }
 #pragma unroll
-    for (int c = 0; c < 9; ++c) cp_async4(&q[RC_C + c][tid], &pin[(CH_C + c) * cap + p]);
+    for (int c = 0; c < 9; ++c) cp_async4(&q[RC_C + c][tid], &pin[pidx((CH_C + c), p)]);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) cp_async4(&q[RC_S + c][tid], &pin[(CH_S + c) * cap + p]);
-    cp_async4(&q[RC_M][tid], &pin[CH_M * cap + p]);
+    for (int c = 0; c < 6; ++c) cp_async4(&q[RC_S + c][tid], &pin[pidx((CH_S + c), p)]);
+    cp_async4(&q[RC_M][tid], &pin[pidx(CH_M, p)]);
     cp_async4(&q[RC_KEY][tid], &d.pkey[p]);
   };
 
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(NT)
   G2PMeta *meta =
       reinterpret_cast<G2PMeta *>(g2p_smem + 2 * kNodes * 16 + 2 * kG2PCh * NT * 4);
   const SimParams &P = *d.prm;
-  const long long cap = d.cap, n = P.n;
+  const long long n = P.n;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const bool lame = P.has_lame != 0;
@@ -571,18 +571,18 @@ __global__ void __launch_bounds__(NT)
     if (p >= 0) {
       float(*q)[NT] = psm[pb];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) cp_async4(&q[GC_X + c][tid], &pin[(CH_X + c) * cap + p]);
+      for (int c = 0; c < 3; ++c) cp_async4(&q[GC_X + c][tid], &pin[pidx((CH_X + c), p)]);
 #pragma unroll
-      for (int c = 0; c < 9; ++c) cp_async4(&q[GC_F + c][tid], &pin[(CH_F + c) * cap + p]);
-      cp_async4(&q[GC_J][tid], &pin[CH_J * cap + p]);
-      cp_async4(&q[GC_M][tid], &pin[CH_M * cap + p]);
-      cp_async4(&q[GC_VOL][tid], &pin[CH_VOL * cap + p]);
+      for (int c = 0; c < 9; ++c) cp_async4(&q[GC_F + c][tid], &pin[pidx((CH_F + c), p)]);
+      cp_async4(&q[GC_J][tid], &pin[pidx(CH_J, p)]);
+      cp_async4(&q[GC_M][tid], &pin[pidx(CH_M, p)]);
+      cp_async4(&q[GC_VOL][tid], &pin[pidx(CH_VOL, p)]);
       if (lame) {
-        cp_async4(&q[GC_MU][tid], &pin[CH_MU * cap + p]);
-        cp_async4(&q[GC_LAM][tid], &pin[CH_LAM * cap + p]);
+        cp_async4(&q[GC_MU][tid], &pin[pidx(CH_MU, p)]);
+        cp_async4(&q[GC_LAM][tid], &pin[pidx(CH_LAM, p)]);
       }
-      cp_async4(&q[GC_MAT][tid], &iin[IC_MAT * cap + p]);
-      cp_async4(&q[GC_ID][tid], &iin[IC_ID * cap + p]);
+      cp_async4(&q[GC_MAT][tid], &iin[iidx(IC_MAT, p)]);
+      cp_async4(&q[GC_ID][tid], &iin[iidx(IC_ID, p)]);
     }
   };
 
@@ -724,29 +724,29 @@ __global__ void __launch_bounds__(NT)
       const int so = d.keep_order ? p : s;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        pout[(CH_X + k) * cap + so] = x[k];
-        pout[(CH_V + k) * cap + so] = vel[k];
+        pout[pidx((CH_X + k), so)] = x[k];
+        pout[pidx((CH_V + k), so)] = vel[k];
       }
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
-        pout[(CH_C + k) * cap + so] = Cn[k];
-        pout[(CH_F + k) * cap + so] = F[k];
+        pout[pidx((CH_C + k), so)] = Cn[k];
+        pout[pidx((CH_F + k), so)] = F[k];
       }
-      pout[CH_J * cap + so] = J;
-      pout[CH_M * cap + so] = q[GC_M][tid];
-      pout[CH_VOL * cap + so] = vol;
-      pout[(CH_S + 0) * cap + so] = vol * tau.xx;
-      pout[(CH_S + 1) * cap + so] = vol * tau.yy;
-      pout[(CH_S + 2) * cap + so] = vol * tau.zz;
-      pout[(CH_S + 3) * cap + so] = vol * tau.xy;
-      pout[(CH_S + 4) * cap + so] = vol * tau.xz;
-      pout[(CH_S + 5) * cap + so] = vol * tau.yz;
+      pout[pidx(CH_J, so)] = J;
+      pout[pidx(CH_M, so)] = q[GC_M][tid];
+      pout[pidx(CH_VOL, so)] = vol;
+      pout[pidx((CH_S + 0), so)] = vol * tau.xx;
+      pout[pidx((CH_S + 1), so)] = vol * tau.yy;
+      pout[pidx((CH_S + 2), so)] = vol * tau.zz;
+      pout[pidx((CH_S + 3), so)] = vol * tau.xy;
+      pout[pidx((CH_S + 4), so)] = vol * tau.xz;
+      pout[pidx((CH_S + 5), so)] = vol * tau.yz;
       if (lame) {
-        pout[CH_MU * cap + so] = mu;
-        pout[CH_LAM * cap + so] = lam;
+        pout[pidx(CH_MU, so)] = mu;
+        pout[pidx(CH_LAM, so)] = lam;
       }
-      iout[IC_MAT * cap + so] = mid;
-      iout[IC_ID * cap + so] = __float_as_int(q[GC_ID][tid]);
+      iout[iidx(IC_MAT, so)] = mid;
+      iout[iidx(IC_ID, so)] = __float_as_int(q[GC_ID][tid]);
       if (kFuseBin) {
         // key of the new position for the next partition (storage slot so)
         const int key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
@@ -765,14 +765,14 @@ __global__ void __launch_bounds__(NT)
   cp_async_wait<0>();
 }
 
-__device__ __forceinline__ void store_stress(float *__restrict__ pb, long long cap, long long p,
-                                             float vol, const Sym3 &t) {
-  pb[(CH_S + 0) * cap + p] = vol * t.xx;
-  pb[(CH_S + 1) * cap + p] = vol * t.yy;
-  pb[(CH_S + 2) * cap + p] = vol * t.zz;
-  pb[(CH_S + 3) * cap + p] = vol * t.xy;
-  pb[(CH_S + 4) * cap + p] = vol * t.xz;
-  pb[(CH_S + 5) * cap + p] = vol * t.yz;
+__device__ __forceinline__ void store_stress(float *__restrict__ pb, long long p, float vol,
+                                             const Sym3 &t) {
+  pb[pidx((CH_S + 0), p)] = vol * t.xx;
+  pb[pidx((CH_S + 1), p)] = vol * t.yy;
+  pb[pidx((CH_S + 2), p)] = vol * t.zz;
+  pb[pidx((CH_S + 3), p)] = vol * t.xy;
+  pb[pidx((CH_S + 4), p)] = vol * t.xz;
+  pb[pidx((CH_S + 5), p)] = vol * t.yz;
 }
 
 // ZSReturnMapping as its own pass (in place, storage order); refreshes the
@@ -780,28 +780,28 @@ __device__ __forceinline__ void store_stress(float *__restrict__ pb, long long c
 __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
                                  const int32_t *__restrict__ ibuf) {
   const SimParams &P = *d.prm;
-  const long long cap = d.cap, n = P.n;
+  const long long n = P.n;
   const bool lame = P.has_lame != 0;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
-    const MatParams mp = d.mats[min(max(ibuf[IC_MAT * cap + p], 0), kMaxMaterials - 1)];
+    const MatParams mp = d.mats[min(max(ibuf[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
     if (mp.type == MPM_EOS || mp.plastic != MPM_PLASTIC_NADP) continue;
     float F[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) F[k] = pbuf[(CH_F + k) * cap + p];
+    for (int k = 0; k < 9; ++k) F[k] = pbuf[pidx((CH_F + k), p)];
     float mu = mp.mu, lam = mp.lam;
     if (lame) {
-      mu = pbuf[CH_MU * cap + p];
-      lam = pbuf[CH_LAM * cap + p];
+      mu = pbuf[pidx(CH_MU, p)];
+      lam = pbuf[pidx(CH_LAM, p)];
     }
     Sym3 tau;
     const int r = project_dp(mu, lam, mp.alpha, F, tau);
     if (r < 0) atomicOr(&d.cnt->status, ST_NAN);
     if (r > 0) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) pbuf[(CH_F + k) * cap + p] = F[k];
-      pbuf[CH_J * cap + p] = det3(F);
-      store_stress(pbuf, cap, p, pbuf[CH_VOL * cap + p], tau);
+      for (int k = 0; k < 9; ++k) pbuf[pidx((CH_F + k), p)] = F[k];
+      pbuf[pidx(CH_J, p)] = det3(F);
+      store_stress(pbuf, p, pbuf[pidx(CH_VOL, p)], tau);
     }
   }
 }
@@ -810,30 +810,30 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
 // reads, recomputed after an upload or a change of materials.
 __global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__restrict__ ibuf) {
   const SimParams &P = *d.prm;
-  const long long cap = d.cap, n = P.n;
+  const long long n = P.n;
   const bool lame = P.has_lame != 0;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
-    const MatParams mp = d.mats[min(max(ibuf[IC_MAT * cap + p], 0), kMaxMaterials - 1)];
+    const MatParams mp = d.mats[min(max(ibuf[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
     float F[9];
     float J = 1.0f;
     if (mp.type == MPM_EOS) {
-      J = pbuf[CH_J * cap + p];
+      J = pbuf[pidx(CH_J, p)];
 #pragma unroll
       for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? 1.0f : 0.0f;
     } else {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) F[k] = pbuf[(CH_F + k) * cap + p];
+      for (int k = 0; k < 9; ++k) F[k] = pbuf[pidx((CH_F + k), p)];
     }
     float mu = mp.mu, lam = mp.lam;
     if (lame) {
-      mu = pbuf[CH_MU * cap + p];
-      lam = pbuf[CH_LAM * cap + p];
+      mu = pbuf[pidx(CH_MU, p)];
+      lam = pbuf[pidx(CH_LAM, p)];
     }
     Sym3 tau;
     if (!kirchhoff(mp.type, mu, lam, mp.bulk, mp.gamma, F, J, tau))
       atomicOr(&d.cnt->status, ST_NAN);
-    store_stress(pbuf, cap, p, pbuf[CH_VOL * cap + p], tau);
+    store_stress(pbuf, p, pbuf[pidx(CH_VOL, p)], tau);
   }
 }
 

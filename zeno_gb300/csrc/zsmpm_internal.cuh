@@ -1,10 +1,14 @@
 // Internal declarations shared by the zsmpm translation units.
 //
 // HBM layout (one context):
-//  * particles: two buffers (current / next substep), each `NCH` float planes
-//    of `cap` floats plus `NICH` int32 planes.  A plane holds one scalar
-//    channel for every particle, so a warp reads 32 consecutive particles of
-//    a channel as one 128-byte line.  The substep re-orders particles by
+//  * particles: two buffers (current / next substep), each `NCH` float
+//    channels plus `NICH` int32 channels, tiled by 32 particle slots: element
+//    (channel ch, slot p) of a store of nch channels sits at
+//    ((p / 32) * nch + ch) * 32 + p % 32.  A warp reads one channel of 32
+//    consecutive slots as one 128-byte line, and the channels of a slot are
+//    a fixed 128 bytes apart, so every channel access of a particle is one
+//    base address plus a constant offset, and the channels of a block of
+//    particles share a few pages.  The substep re-orders particles by
 //    (block, cell) as G2P writes the next buffer, so the next substep's
 //    reads through the sort permutation are near-sequential.
 //  * block directory: dense int32 arrays over every 4^3 block of the domain
@@ -40,6 +44,20 @@ enum : int {
 // int particle channels
 enum : int { IC_MAT = 0, IC_ID = 1, NICH = 2 };
 
+// tiled particle store (see the layout note above)
+constexpr int kPTile = 32;
+__host__ __device__ __forceinline__ long long tix(long long p, int ch, int nch) {
+  return ((p >> 5) * nch + ch) * kPTile + (p & (kPTile - 1));
+}
+__host__ __device__ __forceinline__ long long pidx(int ch, long long p) { return tix(p, ch, NCH); }
+__host__ __device__ __forceinline__ long long iidx(int ch, long long p) {
+  return tix(p, ch, NICH);
+}
+// elements of a store of nch channels for `cap` slots
+inline long long tiled_elems(long long cap, int nch) {
+  return (cap + kPTile - 1) / kPTile * kPTile * nch;
+}
+
 // device status bits (OR-ed into Counters::status)
 enum : int {
   ST_OUT_OF_DOMAIN = 1,
@@ -52,8 +70,8 @@ enum : int {
 
 constexpr int kMaxMaterials = 256;
 constexpr int kMaxScenes = 4096;
-constexpr int kScanTile = 2048;       // directory entries per scan tile
-constexpr int kScanThreads = 256;     // 8 entries per thread
+constexpr int kScanTile = 512;        // directory entries per scan tile
+constexpr int kScanThreads = 256;     // 2 entries per thread
 constexpr int kScanPerThread = kScanTile / kScanThreads;
 constexpr int kTileNodes = 216;       // 6^3 nodes of one particle block's stencils
 
@@ -116,6 +134,7 @@ struct DevPtrs {
   float4 *ptile;      // per particle block: its 6^3 P2G node sums (216 float4)
   float4 *ptile_adj;  // the same for the G2P adjoint (differentiable mode)
   int keep_order;     // differentiable mode: G2P writes each particle to its own slot
+  int planar_x;       // pbuf[0] holds positions as 3 planes of `cap` floats (binning only)
   int32_t *tile_sums;
   int ntiles;
   Counters *cnt;
@@ -170,6 +189,8 @@ struct IngestSrc {
   const int32_t *mat;
 };
 void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s);
+void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
+                       cudaStream_t s);
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
                      cudaStream_t s);
 // writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
