@@ -209,7 +209,9 @@ int32_t mpm_state_load(mpm_ctx *ctx, const float *src_planes);
  * adj_next, the adjoint planes of state n+1, writes adj_prev, the adjoint
  * planes of state n, and adds the gradients with respect to every
  * particle's mu and lam to grad_mu / grad_lam (n floats each, device).  The
- * state is not advanced.  Fixed-corotated and Neo-Hookean materials. */
+ * state is not advanced.  Fixed-corotated, Neo-Hookean and StVK-Hencky
+ * materials, the last with or without the Drucker-Prager projection (sand);
+ * not the equation-of-state fluid (MPM_ERR_INVALID). */
 int32_t mpm_adjoint_substep(mpm_ctx *ctx, float dt, const float *adj_next, float *adj_prev,
                             float *grad_mu, float *grad_lam);
 

@@ -8,7 +8,8 @@
 //         x' = x + dt v',  F' = (I + dt C') F
 // Given the adjoints (x', v', C', F')-bar of the next state, the three
 // kernels here produce the adjoints of this state and of mu, lam:
-//   k_g2p_adjoint   per particle block: recomputes G2P, forms
+//   k_g2p_adjoint   per particle block: recomputes G2P, takes F'b back through
+//                   the Drucker-Prager projection (sand), forms
 //                   Cb = C'b + dt F'b F^T, vb = v'b + dt x'b, F-bar = (I + dt C')^T F'b,
 //                   x-bar through the weights, and scatters the node adjoint
 //                   v_i-bar += W (vb + Dinv Cb (x_i - x_p)) into tiles
@@ -52,8 +53,9 @@ constexpr int kAdjSmem = kAdjSgOffset + kNodes * 16;
 static_assert(kAdjSgOffset % 16 == 0, "float4 staging must be 16-byte aligned");
 
 __global__ void __launch_bounds__(kP2GThreads)
-    k_g2p_adjoint(DevPtrs d, const float *__restrict__ pin, const float *__restrict__ an,
-                  float *__restrict__ ap, long long n) {
+    k_g2p_adjoint(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
+                  const float *__restrict__ an, float *__restrict__ ap, float *__restrict__ gmu,
+                  float *__restrict__ glam, long long n) {
   extern __shared__ __align__(16) unsigned char adj_smem[];
   const TileSmem ts = tile_smem(adj_smem);
   float4 *sg = reinterpret_cast<float4 *>(adj_smem + kAdjSgOffset);
@@ -62,6 +64,7 @@ __global__ void __launch_bounds__(kP2GThreads)
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const int tid = threadIdx.x;
+  const bool lame = P.has_lame != 0;
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     tile_zero(ts);
     const int dir = d.bk_dir[b];
@@ -97,13 +100,6 @@ __global__ void __launch_bounds__(kP2GThreads)
           Fb[k] = an[(AJ_F + k) * n + p];
           Cb[k] = an[(AJ_C + k) * n + p];
         }
-        // C'b += dt F'b F^T
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            Cb[r * 3 + c] += dt * (Fb[r * 3] * F[c * 3] + Fb[r * 3 + 1] * F[c * 3 + 1] +
-                                   Fb[r * 3 + 2] * F[c * 3 + 2]);
         const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
                        s2 = stencil1(x[2], inv_dx);
         const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
@@ -115,6 +111,54 @@ __global__ void __launch_bounds__(kP2GThreads)
         float gx[3] = {0.f, 0.f, 0.f};
         const bool inside = (unsigned)l0 <= 3u && (unsigned)l1 <= 3u && (unsigned)l2 <= 3u;
         if (!inside) atomicOr(&d.cnt->status, ST_STENCIL);
+        // forward C' (times 1/Dinv) of this substep
+        if (inside) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk) {
+                const float4 g4 = sg[((l0 + i) * 6 + (l1 + jj)) * 6 + (l2 + kk)];
+                const float g[3] = {g4.y, g4.z, g4.w};
+                const float W = s0.w[i] * s1.w[jj] * s2.w[kk];
+                const float xx[3] = {((float)i - s0.f) * dx, ((float)jj - s1.f) * dx,
+                                     ((float)kk - s2.f) * dx};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                  Cn[a * 3 + 0] += W * g[a] * xx[0];
+                  Cn[a * 3 + 1] += W * g[a] * xx[1];
+                  Cn[a * 3 + 2] += W * g[a] * xx[2];
+                }
+              }
+        }
+        // Drucker-Prager return mapping: F'b is the adjoint of the projected
+        // F; take it back to the trial F = (I + dt C') F
+        const MatParams mp = d.mats[min(max(iin[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
+        if (mp.type != MPM_EOS && mp.plastic == MPM_PLASTIC_NADP) {
+          float Ft[9];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              Ft[r * 3 + c] = F[r * 3 + c] + dt * Dinv *
+                                                 (Cn[r * 3 + 0] * F[0 * 3 + c] +
+                                                  Cn[r * 3 + 1] * F[1 * 3 + c] +
+                                                  Cn[r * 3 + 2] * F[2 * 3 + c]);
+          const float mu = lame ? pin[pidx(CH_MU, p)] : mp.mu;
+          const float lam = lame ? pin[pidx(CH_LAM, p)] : mp.lam;
+          float mub = 0.f, lamb = 0.f;
+          dp_projection_vjp(mu, lam, mp.alpha, Ft, Fb, mub, lamb);
+          gmu[p] += mub;
+          glam[p] += lamb;
+        }
+        // C'b += dt F'b F^T
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Cb[r * 3 + c] += dt * (Fb[r * 3] * F[c * 3] + Fb[r * 3 + 1] * F[c * 3 + 1] +
+                                   Fb[r * 3 + 2] * F[c * 3 + 2]);
         if (inside) {
 #pragma unroll
           for (int i = 0; i < 3; ++i)
@@ -138,10 +182,7 @@ __global__ void __launch_bounds__(kP2GThreads)
                                 Dinv * (g[0] * Cx[0] + g[1] * Cx[1] + g[2] * Cx[2]);
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                  // forward C', then x-bar via dW and via (x_i - x_p)
-                  Cn[a * 3 + 0] += W * g[a] * xx[0];
-                  Cn[a * 3 + 1] += W * g[a] * xx[1];
-                  Cn[a * 3 + 2] += W * g[a] * xx[2];
+                  // x-bar via dW and via (x_i - x_p)
                   const float CTg = Cb[0 * 3 + a] * g[0] + Cb[1 * 3 + a] * g[1] + Cb[2 * 3 + a] * g[2];
                   gx[a] += dW[a] * s - Dinv * W * CTg;
                 }
@@ -361,6 +402,8 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
         fcr_vjp(mu, lam, F, tb, Fb, mub, lamb);
       else if (mp.type == MPM_NHK)
         nhk_vjp(mu, lam, F, tb, Fb, mub, lamb);
+      else if (mp.type == MPM_STVK)
+        hencky_vjp(mu, lam, F, tb, Fb, mub, lamb);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         ap[(AJ_X + k) * n + p] += gx[k];
@@ -381,10 +424,11 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
 
 }  // namespace
 
-void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, long long n,
-                        cudaStream_t s) {
+void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, float *gmu,
+                        float *glam, long long n, cudaStream_t s) {
   cudaFuncSetAttribute(k_g2p_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmem);
-  k_g2p_adjoint<<<d.num_sms * 2, kP2GThreads, kAdjSmem, s>>>(d, d.pbuf[cur], an, ap, n);
+  k_g2p_adjoint<<<d.num_sms * 2, kP2GThreads, kAdjSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur], an,
+                                                            ap, gmu, glam, n);
 }
 
 void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s) {

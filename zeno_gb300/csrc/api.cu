@@ -407,11 +407,11 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
                           cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   c->n_materials = n;
+  // adjoints exist for the elastic models and for sand (StVK-Hencky with or
+  // without the Drucker-Prager projection); not for the equation-of-state fluid
   c->differentiable = true;
   for (int i = 0; i < n; ++i)
-    if (!((mats[i].type == MPM_FCR || mats[i].type == MPM_NHK) &&
-          mats[i].plasticity == MPM_PLASTIC_NONE))
-      c->differentiable = false;
+    if (mats[i].type == MPM_EOS) c->differentiable = false;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
   if (c->prm.n > 0) {  // stored stresses follow the new parameters
@@ -795,14 +795,15 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
     return fail(MPM_ERR_INVALID, "null adjoint buffer");
   if (!c->differentiable)
     return fail(MPM_ERR_INVALID,
-                "the adjoint covers fixed-corotated and Neo-Hookean materials without plasticity");
+                "the adjoint covers fixed-corotated, Neo-Hookean and StVK-Hencky (with or without "
+                "the Drucker-Prager projection) materials, not the equation-of-state fluid");
   if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
   enqueue_bin_if_needed(c);
   enqueue_sort(c);
   launch_p2g(c->d, c->cur, c->stream);
   launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
   const long long n = c->prm.n;
-  launch_g2p_adjoint(c->d, c->cur, adj_next, adj_prev, n, c->stream);
+  launch_g2p_adjoint(c->d, c->cur, adj_next, adj_prev, grad_mu, grad_lam, n, c->stream);
   launch_grid_adjoint(c->d, c->stream);
   launch_p2g_adjoint(c->d, c->cur, adj_prev, grad_mu, grad_lam, n, c->stream);
   if ((rc = launch_check("adjoint substep"))) return rc;

@@ -462,6 +462,226 @@ __device__ __forceinline__ void nhk_vjp(float mu, float lam, const float (&F)[9]
   lamb += trtb * log1pf(Jm1);
 }
 
+// ---------------------------------------------------------------------------
+// Adjoints of isotropic functions of B = F F^T (StVK-Hencky stress, the
+// Drucker-Prager projection).  For T(B) = U diag(t(b)) U^T (b the eigenvalues
+// of B, U its eigenvectors) and a symmetric adjoint G of T, the adjoint of B
+// is (Daleckii-Krein)
+//   B-bar = U [ D o (U^T G U) off the diagonal, diag(Jt^T diag(U^T G U)) ] U^T,
+//   D_ij = (t_i - t_j) / (b_i - b_j),  Jt_ik = dt_i / db_k,
+// and F-bar += 2 B-bar F.  The divided differences are written as functions
+// of u = (b_i - b_j) / b_j; for near-equal eigenvalues (|u| < 1e-3, where the
+// FP32 difference of the closed forms cancels) they come from FP64 series.
+
+// log1p(u) / u
+__device__ __forceinline__ float log1p_over(float u) {
+  if (fabsf(u) < 1e-3f) {
+    const double x = u;
+    return (float)(1.0 - x * (0.5 - x * (1.0 / 3.0 - x * 0.25)));
+  }
+  return log1pf(u) / u;
+}
+
+// ((1 + u)^a - 1) / u = expm1(a log1p(u)) / u
+__device__ __forceinline__ float pow1p_m1_over(float a, float u) {
+  if (fabsf(u) < 1e-3f) {
+    const double x = u, y = a;
+    return (float)(y * (1.0 + x * ((y - 1.0) * 0.5 + x * (y - 1.0) * (y - 2.0) / 6.0)));
+  }
+  return expm1f(a * log1pf(u)) / u;
+}
+
+// B-bar from the symmetric world-frame adjoint G of T, the eigenvectors Q
+// (columns), D (symmetric, off-diagonal used) and Jt; returns B-bar (3x3,
+// symmetric) and the eigen-frame diagonal Gh_ii
+__device__ __forceinline__ void iso_adjoint(const float (&Q)[9], const float (&G)[9],
+                                            const float (&D)[9], const float (&Jt)[9],
+                                            float (&Bb)[9], float (&Gd)[3]) {
+  float QG[9], Gh[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)  // QG = Q^T G
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      QG[i * 3 + j] = Q[0 * 3 + i] * G[0 * 3 + j] + Q[1 * 3 + i] * G[1 * 3 + j] +
+                      Q[2 * 3 + i] * G[2 * 3 + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)  // Gh = Q^T G Q
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Gh[i * 3 + j] = QG[i * 3 + 0] * Q[0 * 3 + j] + QG[i * 3 + 1] * Q[1 * 3 + j] +
+                      QG[i * 3 + 2] * Q[2 * 3 + j];
+  float H[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Gd[i] = Gh[i * 4];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) H[i * 3 + j] = i == j ? 0.0f : Gh[i * 3 + j] * D[i * 3 + j];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) H[k * 4] = Gd[0] * Jt[0 * 3 + k] + Gd[1] * Jt[1 * 3 + k] + Gd[2] * Jt[2 * 3 + k];
+  float QH[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)  // QH = Q H
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      QH[i * 3 + j] = Q[i * 3 + 0] * H[0 * 3 + j] + Q[i * 3 + 1] * H[1 * 3 + j] +
+                      Q[i * 3 + 2] * H[2 * 3 + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)  // Bb = Q H Q^T
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Bb[i * 3 + j] = QH[i * 3 + 0] * Q[j * 3 + 0] + QH[i * 3 + 1] * Q[j * 3 + 1] +
+                      QH[i * 3 + 2] * Q[j * 3 + 2];
+}
+
+// Fb += 2 Bb F
+__device__ __forceinline__ void add_2BbF(const float (&Bb)[9], const float (&F)[9],
+                                         float (&Fb)[9]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      Fb[i * 3 + j] += 2.0f * (Bb[i * 3 + 0] * F[0 * 3 + j] + Bb[i * 3 + 1] * F[1 * 3 + j] +
+                               Bb[i * 3 + 2] * F[2 * 3 + j]);
+}
+
+// StVK-Hencky, tau = U diag(2mu e_i + lam sum e) U^T, e_i = log(b_i) / 2: given
+// the adjoint tb of tau (3x3), adds to Fb, mub, lamb.  D_ij = mu (log b_i -
+// log b_j) / (b_i - b_j), Jt_ik = (2mu delta_ik + lam) / (2 b_k).
+__device__ __forceinline__ void hencky_vjp(float mu, float lam, const float (&F)[9],
+                                           const float (&tb)[9], float (&Fb)[9], float &mub,
+                                           float &lamb) {
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  float w[3], Q[9];
+  sym_eig3(E, w, Q);
+  float b[3], e[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    b[k] = 1.0f + w[k];
+    e[k] = 0.5f * log1pf(w[k]);
+  }
+  float G[9], D[9], Jt[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      G[i * 3 + j] = 0.5f * (tb[i * 3 + j] + tb[j * 3 + i]);
+      D[i * 3 + j] = i == j ? 0.0f : mu * log1p_over((w[i] - w[j]) / b[j]) / b[j];
+      Jt[i * 3 + j] = ((i == j ? 2.0f * mu : 0.0f) + lam) / (2.0f * b[j]);
+    }
+  float Bb[9], Gd[3];
+  iso_adjoint(Q, G, D, Jt, Bb, Gd);
+  add_2BbF(Bb, F, Fb);
+  const float tr = e[0] + e[1] + e[2];
+  mub += 2.0f * (Gd[0] * e[0] + Gd[1] * e[1] + Gd[2] * e[2]);
+  lamb += (Gd[0] + Gd[1] + Gd[2]) * tr;
+}
+
+// Adjoint of the Drucker-Prager projection F_new = N(B) F (project_dp, B the
+// trial B = F F^T, N = U diag(m) U^T, m_i = exp(e'_i - e_i)): given Fb =
+// F_new-bar, replaces it by the trial F-bar N F_new-bar + 2 B-bar F (B-bar from
+// G = sym(F_new-bar F^T)) and adds the yield condition's mu, lam terms.
+// Cases (the same tests on the same FP32 eigenvalues as project_dp):
+//   elastic: N = I;
+//   tension (sum e >= 0): m_i = b_i^-1/2, Jt_ii = -b_i^-3/2 / 2,
+//       D_ij = -1 / (s_i s_j (s_i + s_j)), s = sqrt(b);
+//   projected: m_i = exp(g_i), g = -k h, h = e - tr/3, k = 1 + c alpha tr / |h|,
+//       c = (3 lam + 2 mu) / (2 mu); dg_i/de_j = -P_ij - c alpha (h^_i + tr (P_ij -
+//       h^_i h^_j) / |h|), P = I - 1/3, Jt_ij = m_i dg_i/de_j / (2 b_j), and
+//       D_ij = m_j ((b_i/b_j)^(-k/2) - 1) / (b_i - b_j).
+__device__ __forceinline__ void dp_projection_vjp(float mu, float lam, float alpha,
+                                                  const float (&F)[9], float (&Fb)[9],
+                                                  float &mub, float &lamb) {
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  float w[3], Q[9];
+  sym_eig3(E, w, Q);
+  if (!(w[0] > -1.0f && w[1] > -1.0f && w[2] > -1.0f)) return;  // degenerate: forward flagged it
+  float b[3], e[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    b[k] = 1.0f + w[k];
+    e[k] = 0.5f * log1pf(w[k]);
+  }
+  const float tr = e[0] + e[1] + e[2];
+  float m[3], D[9], Jt[9];
+  float hh[3] = {0.f, 0.f, 0.f}, c = 0.f;
+  bool projected = false;
+  if (tr >= 0.0f) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      m[i] = expf(-e[i]);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float si = sqrtf(b[i]), sj = sqrtf(b[j]);
+        D[i * 3 + j] = i == j ? 0.0f : -1.0f / (si * sj * (si + sj));
+        Jt[i * 3 + j] = i == j ? -0.5f / (b[i] * si) : 0.0f;
+      }
+    }
+  } else {
+    const float h0 = e[0] - tr / 3.0f, h1 = e[1] - tr / 3.0f, h2 = e[2] - tr / 3.0f;
+    const float nrm = sqrtf(h0 * h0 + h1 * h1 + h2 * h2);
+    c = (3.0f * lam + 2.0f * mu) / (2.0f * mu);
+    const float dg = nrm + c * tr * alpha;
+    if (dg <= 0.0f) return;  // elastic: F_new = F
+    projected = true;
+    const float k = dg / nrm;
+    const float h[3] = {h0, h1, h2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      hh[i] = h[i] / nrm;
+      m[i] = expf(-k * h[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float P = (i == j ? 1.0f : 0.0f) - 1.0f / 3.0f;
+        const float dgde = -P - c * alpha * (hh[i] + tr * (P - hh[i] * hh[j]) / nrm);
+        Jt[i * 3 + j] = m[i] * dgde / (2.0f * b[j]);
+        D[i * 3 + j] =
+            i == j ? 0.0f : m[j] * pow1p_m1_over(-0.5f * k, (w[i] - w[j]) / b[j]) / b[j];
+      }
+  }
+  // G = sym(F_new-bar F^T)
+  float G[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float a = Fb[i * 3 + 0] * F[j * 3 + 0] + Fb[i * 3 + 1] * F[j * 3 + 1] +
+                      Fb[i * 3 + 2] * F[j * 3 + 2];
+      const float t = Fb[j * 3 + 0] * F[i * 3 + 0] + Fb[j * 3 + 1] * F[i * 3 + 1] +
+                      Fb[j * 3 + 2] * F[i * 3 + 2];
+      G[i * 3 + j] = 0.5f * (a + t);
+    }
+  float Bb[9], Gd[3];
+  iso_adjoint(Q, G, D, Jt, Bb, Gd);
+  // N F_new-bar
+  const Sym3 N = qdqt(Q, m[0], m[1], m[2]);
+  const float Nm[9] = {N.xx, N.xy, N.xz, N.xy, N.yy, N.yz, N.xz, N.yz, N.zz};
+  float out[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      out[i * 3 + j] = Nm[i * 3 + 0] * Fb[0 * 3 + j] + Nm[i * 3 + 1] * Fb[1 * 3 + j] +
+                       Nm[i * 3 + 2] * Fb[2 * 3 + j];
+  add_2BbF(Bb, F, out);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Fb[k] = out[k];
+  if (projected) {
+    // dg_i/dc = -alpha tr h^_i; dc/dmu = -3 lam / (2 mu^2), dc/dlam = 3 / (2 mu)
+    const float dLdc = -alpha * tr * (Gd[0] * m[0] * hh[0] + Gd[1] * m[1] * hh[1] +
+                                      Gd[2] * m[2] * hh[2]);
+    mub += dLdc * (-3.0f * lam / (2.0f * mu * mu));
+    lamb += dLdc * (3.0f / (2.0f * mu));
+  }
+}
+
 // dw/df of the quadratic B-spline weights (per axis): w0' = f - 1.5,
 // w1' = -2 (f - 1), w2' = f - 0.5
 __device__ __forceinline__ void stencil_dw(float f, float (&dw)[3]) {

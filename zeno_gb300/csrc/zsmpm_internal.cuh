@@ -177,8 +177,8 @@ void set_last_error(const std::string &msg);
 
 // adjoint.cu: the three adjoint kernels of one substep (an / ap: adjoint
 // planes of the next / this state, n particles each)
-void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, long long n,
-                        cudaStream_t s);
+void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, float *gmu,
+                        float *glam, long long n, cudaStream_t s);
 void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s);
 void launch_p2g_adjoint(const DevPtrs &d, int cur, float *ap, float *gmu, float *glam, long long n,
                         cudaStream_t s);

@@ -15,7 +15,8 @@ upload-order mode and exposes `rollout(v0, E) -> x_final` as a
   segment of states.
 
 Gradients are returned for v0 (n x 3) and E (n); other initial data are
-constants.  Fixed-corotated and Neo-Hookean materials.
+constants.  Fixed-corotated, Neo-Hookean and StVK-Hencky materials, the last
+with or without the Drucker-Prager projection (sand).
 """
 from __future__ import annotations
 

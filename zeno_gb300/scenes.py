@@ -232,6 +232,30 @@ def diff_velocity(n: int, seed: int = 4):
     return np.tile([[0.3, -3.0, 0.1]], (n, 1)) + 0.2 * normal(seed, 0, n * 3).reshape(-1, 3)
 
 
+def sand_column(seed: int = 0, dx: float = 1.0 / 512, cells=(128, 256, 64), E: float = 1e5,
+                friction_angle_deg: float = 30.0):
+    """Seeded column collapse of Drucker-Prager sand (StVK-Hencky, nu = 0.3,
+    rho = 1000): a cells[0] x cells[1] x cells[2] column x 8 ppc standing on the
+    floor band (y up, gravity -9.8), sticky walls 3 cells thick, dt = 1e-4.  At
+    dx = 1/512 the default 128 x 256 x 64 cells hold 2^24 = 16,777,216
+    particles (0.25 x 0.5 x 0.125 of the unit box)."""
+    mats = [Material(STVK, E=E, nu=0.3, plasticity=PLASTIC_NADP,
+                     friction_angle_deg=friction_angle_deg)]
+    scene = Scene.unit_box(dx, bc_type=BC_STICKY, bc_thickness=3, dt=1e-4, materials=mats)
+    res = int(round(1.0 / dx))
+    lo = (np.floor(0.1 * res) * dx, 4 * dx, np.floor(0.4 * res) * dx)
+    x = box_particles(lo, cells, dx, 8, seed, 0)
+    parts = make_particles(x, dx, 8, mats, np.zeros(x.shape[0], np.int32))
+    return scene, parts
+
+
+def sand_velocity(n: int, seed: int = 5):
+    """Initial velocity of the sand rollouts: downward (0, -2, 0) m/s plus
+    N(0, 0.3^2) per component, which drives the column into the floor so that
+    the Drucker-Prager projection is active."""
+    return np.tile([[0.0, -2.0, 0.0]], (n, 1)) + 0.3 * normal(seed, 0, n * 3).reshape(-1, 3)
+
+
 def batched_counts(n_scenes: int = 256, lo: int = 2048, hi: int = 200000, seed: int = 1):
     """Per-scene particle counts drawn log-uniform in [lo, hi]."""
     u = uniform(seed, 0, n_scenes)
