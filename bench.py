@@ -167,7 +167,9 @@ def batched_form(zsmpm, steps: int, dev: int):
     pairs = scenes.batched_workload()
     scns, mats, parts, offs = zsmpm.concat_scenes(pairs)
     dt = pairs[0][0].dt
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the context's kernels and the events
+    # below are ordered on it whatever stream the caller left current
+    stream = torch.cuda.Stream(device=dev)
     ctx = zsmpm.BatchContext(scns, mats, max_particles=parts.n, device=dev)
     ctx.set_stream(stream.cuda_stream)
     ctx.upload_batch(parts, offs)
@@ -265,7 +267,9 @@ def differentiable_form(zsmpm, dev: int, steps: int = 64, ckpt: int = 16):
     # the same scene on the plain path, same substeps
     p = parts.copy()
     p.v = v0.astype(np.float32)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the context's kernels and the events
+    # below are ordered on it whatever stream the caller left current
+    stream = torch.cuda.Stream(device=dev)
     ctx = zsmpm.Context(scene, max_particles=n, device=dev)
     ctx.set_stream(stream.cuda_stream)
     ctx.upload(p)
@@ -307,6 +311,90 @@ def differentiable_form(zsmpm, dev: int, steps: int = 64, ckpt: int = 16):
             "checkpoint_bytes": sim.peak_checkpoint_bytes,
             "note": "wall time of rollout + backward (host loop of per-substep calls, both "
                     "synchronised); plain: CUDA events over the same 64 substeps in one call"}
+
+
+def sand_form(zsmpm, dev: int, steps: int = 128, ckpt: int = 8):
+    """The large differentiable rollout: a 16,777,216-particle Drucker-Prager
+    sand column (128 x 256 x 64 cells x 8 ppc, dx = 1/512) thrown at the floor,
+    128 substeps forward + backward with a checkpoint every 8 substeps (each
+    segment recomputed in the backward pass), centre-of-mass loss, gradient
+    with respect to the per-particle initial velocity.  Reported next to the
+    plain path advancing the same scene the same substeps, with the device
+    memory the run held at its peak and the v0 gradient checked against a
+    central difference of the FP32 forward (h = 1e-3 along a random
+    direction)."""
+    import torch
+    from zeno_gb300 import diff, scenes
+    scene, parts = scenes.sand_column()
+    n = parts.n
+    E = np.full(n, float(scene.materials[0].E))
+    v0 = scenes.sand_velocity(n)
+    free0, total = torch.cuda.mem_get_info(dev)
+    # dense column: about n / 512 particle blocks; grid blocks with the halo
+    # stay below 4x that
+    sim = diff.Rollout(scene, parts, steps, ckpt, device=dev, max_grid_blocks=max(65536, n // 128))
+    target = (0.7, 0.5, 0.5)
+    peak_used = [total - free0]
+
+    def note():
+        f, _ = torch.cuda.mem_get_info(dev)
+        peak_used[0] = max(peak_used[0], total - f)
+
+    def fwd_bwd():
+        v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+        e = torch.tensor(E, dtype=torch.float64, device="cuda", requires_grad=True)
+        L = diff.com_loss(sim.rollout(v, e), target)
+        note()
+        L.backward()
+        note()
+        return v.grad
+
+    def loss(v):
+        with torch.no_grad():
+            x = sim.rollout(torch.tensor(v, dtype=torch.float32, device="cuda"),
+                            torch.tensor(E, dtype=torch.float64, device="cuda"))
+            return float(diff.com_loss(x, target))
+
+    fwd_bwd()  # warm-up (graphs, allocator)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    gv = fwd_bwd()
+    torch.cuda.synchronize()
+    t_fb = time.perf_counter() - t0
+    # plain path, same scene and substeps
+    p = parts.copy()
+    p.v = v0.astype(np.float32)
+    # a dedicated (non-default) stream: the context's kernels and the events
+    # below are ordered on it whatever stream the caller left current
+    stream = torch.cuda.Stream(device=dev)
+    ctx = zsmpm.Context(scene, max_particles=n, device=dev, max_grid_blocks=max(65536, n // 128))
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(p)
+    ctx.substep(scene.dt, 3)
+    ctx.upload(p)
+    ctx.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.substep(scene.dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) * 1e-3
+    st = ctx.stats()
+    ctx.close()
+    dv = np.tile([[1.0, 0.5, -0.3]], (n, 1)) + 0.5 * scenes.normal(5, 0, n * 3).reshape(-1, 3)
+    h = 1e-3
+    fd_v = (loss(v0 + h * dv) - loss(v0 - h * dv)) / (2 * h)
+    ad_v = float((gv.double().cpu().numpy() * dv).sum())
+    return {"workload": f"{n:,} Drucker-Prager sand particles (128x256x64 cells x 8 ppc), "
+                        f"dx=1/512, column thrown at the floor, {steps} substeps, checkpoint "
+                        f"every {ckpt} with recomputation, centre-of-mass loss, gradient wrt v0",
+            "value": n * steps / t_fb, "unit": METRIC, "ms_fwd_bwd": 1e3 * t_fb,
+            "ms_plain": 1e3 * t_plain, "plain": n * steps / t_plain,
+            "speedup_over_plain": t_plain / t_fb, "fwd_bwd_cost_over_plain": t_fb / t_plain,
+            "grad_v0_rel_err_vs_fd32": abs(ad_v - fd_v) / abs(fd_v),
+            "device_bytes_peak": int(peak_used[0]), "hbm_budget_bytes": 150 * 10**9,
+            "checkpoint_bytes": sim.peak_checkpoint_bytes, "plain_status": st["status"]}
 
 
 def cpu_baseline(parts, scene, target_s: float = 10.0):
@@ -494,6 +582,7 @@ def run_gpu(args):
     if not args.no_forms:
         forms["batched"] = batched_form(zsmpm, max(10, min(args.steps, 100)), dev)
         forms["fwd_bwd"] = differentiable_form(zsmpm, dev)
+        forms["fwd_bwd_sand_16M"] = sand_form(zsmpm, dev)
     if rank != 0:
         if pg:
             pg.barrier()

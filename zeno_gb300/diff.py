@@ -30,7 +30,8 @@ X, V, Cc, Fc, J = slice(0, 3), slice(3, 6), slice(6, 15), slice(15, 24), 24
 
 
 class Rollout:
-    def __init__(self, scene, parts, n_substeps: int, ckpt_every: int = 16, device: int = 0):
+    def __init__(self, scene, parts, n_substeps: int, ckpt_every: int = 16, device: int = 0,
+                 max_grid_blocks: int = 0):
         if len(scene.materials) != 1:
             raise ValueError("one material per rollout (per-particle E carries the variation)")
         self.scene = scene
@@ -41,7 +42,8 @@ class Rollout:
         self.nu = float(scene.materials[0].nu)
         self.dev = torch.device("cuda", device)
         self.stream = torch.cuda.Stream(device=self.dev)
-        self.ctx = zsmpm.Context(scene, max_particles=parts.n, device=device)
+        self.ctx = zsmpm.Context(scene, max_particles=parts.n, device=device,
+                                 max_grid_blocks=max_grid_blocks)
         self.ctx.set_stream(self.stream.cuda_stream)
         self.ctx.set_order_mode(True)
         p = parts.copy()
