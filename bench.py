@@ -186,7 +186,15 @@ def batched_form(zsmpm, steps: int, dev: int):
     ms_b = e0.elapsed_time(e1)
     ctx.sync()
     st = ctx.stats()
+    # sample for the parity check of the cpu_baseline leg: scenes 0 and 1
+    # after 20 substeps of the batch
+    check_steps = 20
+    ctx.upload_batch(parts, offs)
+    ctx.substep(dt, check_steps)
+    out = ctx.download(("x", "v"))
     ctx.close()
+    check = [(pairs[k][0], pairs[k][1], out["x"][offs[k]:offs[k + 1]],
+              out["v"][offs[k]:offs[k + 1]]) for k in (0, 1)]
     # the same scenes, each on its own plain context, one after another
     ctxs = []
     for scene, p in pairs:
@@ -215,7 +223,8 @@ def batched_form(zsmpm, steps: int, dev: int):
             "kernel_launches_per_step": KERNELS_PER_SUBSTEP,
             "launch_config": tuned["config"],
             "note": "plain_sequential: the same scenes, one plain context each, default launch "
-                    "shapes; batched: autotuned launch shapes"}
+                    "shapes; batched: autotuned launch shapes",
+            "_check": {"substeps": check_steps, "scenes": check}}
 
 
 def differentiable_form(zsmpm, dev: int, steps: int = 64, ckpt: int = 16):
@@ -397,10 +406,25 @@ def sand_form(zsmpm, dev: int, steps: int = 128, ckpt: int = 8):
             "checkpoint_bytes": sim.peak_checkpoint_bytes, "plain_status": st["status"]}
 
 
-def cpu_baseline(parts, scene, target_s: float = 10.0):
-    """FP32 OpenMP restatement (oracle/) on all host cores, bounded sample."""
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def cpu_baseline(parts, scene, checks=None, target_s: float = 10.0):
+    """FP32 OpenMP restatement (oracle/) on all host cores, bounded sample;
+    then, as the checker, the FP64 oracle on the GPU samples in `checks`
+    (plain: the bench scene after a few substeps; batched: two scenes of the
+    batch), giving the relative L2 error of positions and velocities."""
     from oracle import oracle
     oracle.build()
+    parity = {}
+    for name, (sc, pt, steps, gx, gv) in (checks or {}).items():
+        ref, st = oracle.run(sc, pt, steps, "f64")
+        parity[name] = {"rel_l2_x": rel_l2(gx, ref.x), "rel_l2_v": rel_l2(gv, ref.v),
+                        "substeps": steps, "particles": int(pt.n), "reference": "FP64 oracle",
+                        "oracle_status": st["status"]}
     cores = oracle.max_threads()
     t0 = time.perf_counter()
     q, st = oracle.run(scene, parts, 1, "f32")
@@ -411,7 +435,8 @@ def cpu_baseline(parts, scene, target_s: float = 10.0):
     dt = time.perf_counter() - t0
     return {"value": parts.n * steps / dt, "unit": METRIC, "cores": cores, "kind": "port",
             "sample": f"{steps} substeps of the full {parts.n:,}-particle scene "
-                      f"(after 1 warm-up substep), FP32 OpenMP restatement of the node bodies"}
+                      f"(after 1 warm-up substep), FP32 OpenMP restatement of the node bodies",
+            "parity": parity}
 
 
 def run_reference(args):
@@ -480,6 +505,13 @@ def run_gpu(args):
     dt = scene.dt
     from zeno_gb300 import autotune
     tuned = autotune.tune(ctx, dt, state=lambda: ctx.upload(parts))
+    # sample for the parity check of the cpu_baseline leg: 3 substeps from the
+    # initial state
+    check_steps = 3
+    ctx.upload(parts)
+    ctx.substep(dt, check_steps)
+    plain_out = ctx.download(("x", "v"))
+    ctx.upload(parts)
 
     # warm-up (captures both graph parities)
     ctx.substep(dt, max(args.warmup, 3))
@@ -588,7 +620,16 @@ def run_gpu(args):
             pg.barrier()
             pg.destroy_process_group()
         return 0
-    cpu = None if args.no_cpu else cpu_baseline(parts, scene)
+    checks = {"plain": (scene, parts, check_steps, plain_out["x"], plain_out["v"])}
+    bchk = forms.get("batched", {}).pop("_check", None)
+    if bchk:
+        for k, (sc, pt, gx, gv) in enumerate(bchk["scenes"]):
+            checks[f"batched_scene_{k}"] = (sc, pt, bchk["substeps"], gx, gv)
+    cpu = None
+    parity = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(parts, scene, checks)
+        parity = cpu.pop("parity")
     clocks = sampler.summary(c0, c1)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
@@ -610,6 +651,7 @@ def run_gpu(args):
         "stage_ms": {k: round(v, 5) for k, v in stage_ms.items()},
         "stage_sum_ms": sub_ms,
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": {"value": ws * n * e2e_steps / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                 "step": "upload full particle state from pinned host memory, 1 substep, "
