@@ -350,38 +350,67 @@ __global__ void __launch_bounds__(kColThreads, 4) k_p2g(DevPtrs d, const float *
 // applies UpdateZSGrid and bit 2 ApplyBoundaryOnZSGrid to the sum.
 __device__ __forceinline__ void update_node(const SceneParams &S, float dt, int mode, int ldir,
                                             int cell, float4 &g, float &vmax);
+__device__ __forceinline__ void update_node_at(const SceneParams &S, float dt, int mode,
+                                               const int (&I)[3], float4 &g, float &vmax);
 
-__global__ void k_grid_gather(DevPtrs d, int mode) {
+// One 64-thread group per grid block, 4 blocks per CTA: the group fetches its
+// block's scene, node origin and the (particle block) tiles of the 8 blocks
+// whose tiles can cover it once into shared memory; each thread then sums
+// its node's <= 8 tile entries and applies the update.
+constexpr int kGatherBlocks = 4;
+
+__global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, int mode) {
+  __shared__ int sbk[kGatherBlocks][8];
+  __shared__ int sorg[kGatherBlocks][4];  // node origin, scene
   const SimParams &P = *d.prm;
-  const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
+  const int ng = min(d.cnt->n_gblocks, d.cap_gblocks);
+  const int grp = threadIdx.x >> 6, cell = threadIdx.x & 63;
+  const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
   float vmax = 0.0f;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
-    const int gdir = d.gb_dir[gb];
-    const SceneParams &S = d.scn[scene_of_dir(d, gdir)];
-    const int dy = S.block_dims[1], dz = S.block_dims[2];
-    const int ldir = gdir - S.dir_off;
-    const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
-    const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
-    float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int o = 0; o < 8; ++o) {
-      const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
-      if ((o0 && (l0 >= 2 || c0 < 1)) || (o1 && (l1 >= 2 || c1 < 1)) ||
-          (o2 && (l2 >= 2 || c2 < 1)))
-        continue;
-      const int bk = d.dir_bk[gdir - (o0 * dy + o1) * dz - o2];
-      if (bk < 0) continue;
-      const float4 t = d.ptile[(long long)bk * kTileNodes +
-                               ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2)];
-      g.x += t.x;
-      g.y += t.y;
-      g.z += t.z;
-      g.w += t.w;
+  for (int g0 = blockIdx.x * kGatherBlocks; g0 < ng; g0 += gridDim.x * kGatherBlocks) {
+    const int gb = g0 + grp;
+    if (cell < 8 && gb < ng) {
+      const int gdir = d.gb_dir[gb];
+      const int sc = scene_of_dir(d, gdir);
+      const SceneParams &S = d.scn[sc];
+      const int dy = S.block_dims[1], dz = S.block_dims[2];
+      const int ldir = gdir - S.dir_off;
+      const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
+      const int o0 = cell >> 2, o1 = (cell >> 1) & 1, o2 = cell & 1;
+      int bk = -1;
+      if (!((o0 && c0 < 1) || (o1 && c1 < 1) || (o2 && c2 < 1)))
+        bk = d.dir_bk[gdir - (o0 * dy + o1) * dz - o2];
+      sbk[grp][cell] = bk;
+      if (cell == 0) {
+        sorg[grp][0] = (c0 + S.block_lo[0]) * 4;
+        sorg[grp][1] = (c1 + S.block_lo[1]) * 4;
+        sorg[grp][2] = (c2 + S.block_lo[2]) * 4;
+        sorg[grp][3] = sc;
+      }
     }
-    if (g.x != 0.0f) update_node(S, P.dt, mode, ldir, cell, g, vmax);
-    d.grid[idx] = g;
+    __syncthreads();
+    if (gb < ng) {
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int o = 0; o < 8; ++o) {
+        const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
+        if ((o0 && l0 >= 2) || (o1 && l1 >= 2) || (o2 && l2 >= 2)) continue;
+        const int bk = sbk[grp][o];
+        if (bk < 0) continue;
+        const float4 t = d.ptile[(long long)bk * kTileNodes +
+                                 ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2)];
+        g.x += t.x;
+        g.y += t.y;
+        g.z += t.z;
+        g.w += t.w;
+      }
+      if (g.x != 0.0f) {
+        const int I[3] = {sorg[grp][0] + l0, sorg[grp][1] + l1, sorg[grp][2] + l2};
+        update_node_at(d.scn[sorg[grp][3]], P.dt, mode, I, g, vmax);
+      }
+      d.grid[(long long)gb * 64 + cell] = g;
+    }
+    __syncthreads();  // shared entries reused
   }
   if (mode & 1) {
 #pragma unroll
@@ -399,6 +428,16 @@ __global__ void k_grid_gather(DevPtrs d, int mode) {
 // it only when it points into the wall (collider velocity 0).
 __device__ __forceinline__ void update_node(const SceneParams &S, float dt, int mode, int ldir,
                                             int cell, float4 &g, float &vmax) {
+  const int dz = S.block_dims[2], dy = S.block_dims[1];
+  const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
+                    (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
+                    ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
+  update_node_at(S, dt, mode, I, g, vmax);
+}
+
+// the same at the node's global index I
+__device__ __forceinline__ void update_node_at(const SceneParams &S, float dt, int mode,
+                                               const int (&I)[3], float4 &g, float &vmax) {
   if (mode & 1) {
     const float r = 1.0f / g.x;
     g.y = g.y * r + S.gravity[0] * dt;
@@ -407,10 +446,6 @@ __device__ __forceinline__ void update_node(const SceneParams &S, float dt, int 
     vmax = fmaxf(vmax, g.y * g.y + g.z * g.z + g.w * g.w);
   }
   if ((mode & 2) && S.bc_type != MPM_BC_NONE) {
-    const int dz = S.block_dims[2], dy = S.block_dims[1];
-    const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
-                      (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
-                      ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
     float vel[3] = {g.y, g.z, g.w};
     bool any = false;
     const int t = S.bc_thickness;
@@ -496,7 +531,7 @@ __device__ __forceinline__ G2PMeta g2p_load_meta(const DevPtrs &d, long long n, 
 // as cp.async copies into the other half of double-buffered shared memory,
 // and the permutation entries of chunk i+2 are loading into registers.
 template <bool kFuseRM, bool kFuseBin, int NT>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 768 / NT)
     k_g2p(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
           float *__restrict__ pout, int32_t *__restrict__ iout) {
   extern __shared__ __align__(16) unsigned char g2p_smem[];
@@ -870,7 +905,7 @@ void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
 }
 
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
-  k_grid_gather<<<d.grid_stream, 256, 0, s>>>(d, mode);
+  k_grid_gather<<<d.grid_stream, 64 * kGatherBlocks, 0, s>>>(d, mode);
 }
 
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {
