@@ -499,7 +499,7 @@ struct G2PMeta {
 };
 
 constexpr int kG2PCh = 19;     // staged particle channels
-constexpr int kG2PMeta = 128;  // blocks per CTA whose metadata is staged
+constexpr int kG2PMeta = 32;   // blocks per CTA whose metadata is staged
 // staged channel slots
 constexpr int GC_X = 0, GC_F = 3, GC_J = 12, GC_M = 13, GC_VOL = 14, GC_MU = 15, GC_LAM = 16,
               GC_MAT = 17, GC_ID = 18;
