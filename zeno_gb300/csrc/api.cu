@@ -474,11 +474,6 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
   if (n > 0 && (!x || !m || !vol)) return fail(MPM_ERR_INVALID, "x, m and vol are required");
   if ((mu == nullptr) != (lam == nullptr)) return fail(MPM_ERR_INVALID, "mu and lam go together");
   if (c->n_materials <= 0) return fail(MPM_ERR_STATE, "set materials before uploading");
-  if (mat) {
-    for (int64_t i = 0; i < n; ++i)
-      if (mat[i] < 0 || mat[i] >= c->n_materials)
-        return fail(MPM_ERR_INVALID, "material id out of range");
-  }
   const int alt = 1 - c->cur;
   float *st = c->d.pbuf[alt];
   int32_t *ist = c->d.ibuf[alt];
@@ -502,8 +497,17 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
     return rc;
   src.mat = nullptr;
   if (mat && n > 0) {
+    // material ids are checked on the device, against the staged copy, before
+    // the store is touched: the wait overlaps the copies the upload needs anyway
     ZS_CUDA(cudaMemcpyAsync(ist, mat, N * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
     src.mat = ist;
+    ZS_CUDA(cudaMemsetAsync(&c->d.cnt->bad_material, 0, sizeof(int), c->stream));
+    launch_check_materials(c->d, ist, n, c->n_materials, c->stream);
+    if ((rc = launch_check("material check"))) return rc;
+    ZS_CUDA(cudaMemcpyAsync(&c->h_cnt->bad_material, &c->d.cnt->bad_material, sizeof(int),
+                            cudaMemcpyDeviceToHost, c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->h_cnt->bad_material) return fail(MPM_ERR_INVALID, "material id out of range");
   }
   launch_ingest(c->d, c->cur, src, n, c->stream);
   if ((rc = launch_check("ingest"))) return rc;

@@ -87,7 +87,23 @@ __global__ void k_state_copy(float *__restrict__ pb, float *__restrict__ dst,
   }
 }
 
+// every material id in [0, n_materials)? (bad_material was zeroed before)
+__global__ void k_check_materials(const int32_t *__restrict__ mat, long long n, int n_materials,
+                                  Counters *cnt) {
+  bool bad = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    bad |= (unsigned)mat[i] >= (unsigned)n_materials;
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) cnt->bad_material = 1;
+}
+
 }  // namespace
+
+void launch_check_materials(const DevPtrs &d, const int32_t *mat, long long n, int n_materials,
+                            cudaStream_t s) {
+  if (n <= 0) return;
+  k_check_materials<<<d.num_sms * 4, 256, 0, s>>>(mat, n, n_materials, d.cnt);
+}
 
 void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
                        cudaStream_t s) {

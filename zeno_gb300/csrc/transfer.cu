@@ -76,7 +76,7 @@ constexpr int kColThreads = 192;
 constexpr int kColChunk = kColThreads;
 constexpr int kColRaw = 23;            // x3 v3 C9 S6 m key
 constexpr int kColRecs = 16 * 9 * 6;  // float4 records: (column, oi oj, z)
-constexpr int kColMeta = 128;          // blocks per CTA whose metadata is staged
+constexpr int kColMeta = 64;           // blocks per CTA whose metadata is staged
 // shared memory: raw[23][chunk] floats; spd[4][chunk] float4 (b0 b1 a00 a10),
 // (a01 a11 a02 a12), (b2 m a20 a21), (a22 wz0 wz1 wz2), laid out so that
 // the pairs the scatter combines with packed FP32x2 instructions are the
@@ -499,7 +499,7 @@ struct G2PMeta {
 };
 
 constexpr int kG2PCh = 19;     // staged particle channels
-constexpr int kG2PMeta = 32;   // blocks per CTA whose metadata is staged
+constexpr int kG2PMeta = 64;   // blocks per CTA whose metadata is staged
 // staged channel slots
 constexpr int GC_X = 0, GC_F = 3, GC_J = 12, GC_M = 13, GC_VOL = 14, GC_MU = 15, GC_LAM = 16,
               GC_MAT = 17, GC_ID = 18;

@@ -86,7 +86,8 @@ struct Counters {
   int status;
   unsigned max_vel_sqr_bits;
   int n_binned;
-  int pad[3];
+  int bad_material;  // set by the upload check of material ids
+  int pad[2];
 };
 
 // Device-resident parameters; the host updates them with one small copy
@@ -189,6 +190,8 @@ struct IngestSrc {
   const int32_t *mat;
 };
 void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s);
+void launch_check_materials(const DevPtrs &d, const int32_t *mat, long long n, int n_materials,
+                            cudaStream_t s);
 void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
                        cudaStream_t s);
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
