@@ -78,6 +78,34 @@ typedef struct mpm_boundary {
   int32_t hi[3];
 } mpm_boundary;
 
+/* Level-set collider: MakeZSLevelSet + ToZSBoundary (Generation.cu:1521-1647),
+ * resolved per grid node by ApplyBoundaryOnZSGrid (Boundary.cu:83-163).  The
+ * signed distance is a dense grid of dims[0] x dims[1] x dims[2] samples (x
+ * fastest) at origin + (i, j, k) * spacing in collider space, interpolated
+ * trilinearly; its material velocity is 3 planes of the same layout or one
+ * constant.  A node at world position p maps to collider space as
+ * X = R^T (p - b) / s; it is inside when s * phi(X) < 0, with normal R grad phi
+ * and collider velocity R v(X) + db/dt (Boundary.cu:299-301).  R is the
+ * rotation of the yaw (about y), pitch (about x) and roll (about z) angles,
+ * applied as R = Ry(yaw) Rx(pitch) Rz(roll).  sticky: v = v_obj; slip: the
+ * normal part of v - v_obj is removed; separate: only when it points into
+ * the collider (ApplyGridBoundaryOnZSGrid, Boundary.cu:56-67). */
+typedef struct mpm_collider_desc {
+  int32_t type;             /* MPM_BC_STICKY, MPM_BC_SLIP or MPM_BC_SEPARATE */
+  int32_t scene;            /* scene of a batched context, -1: every scene */
+  int32_t dims[3];          /* samples per axis, >= 2 */
+  float origin[3];          /* collider-space position of sample (0, 0, 0) */
+  float spacing;            /* sample spacing, > 0 */
+  const float *sdf;         /* dims[0]*dims[1]*dims[2] signed distances (host) */
+  const float *velocity;    /* 3 planes of material velocity (host), or NULL */
+  float const_velocity[3];  /* the material velocity when velocity == NULL */
+  float translation[3];     /* b */
+  float translation_rate[3];/* db/dt */
+  float scale;              /* s, > 0 */
+  float scale_rate;         /* ds/dt */
+  float ypr_deg[3];         /* yaw, pitch, roll in degrees */
+} mpm_collider_desc;
+
 /* Context = MakeZSGrid + MakeZSPartition + the particle store
  * (Generation.cu:1470-1512, Generation.cpp:690-1145).  The sparse grid of
  * 4^3-cell blocks lives inside a block directory: block coordinates
@@ -140,6 +168,15 @@ int32_t mpm_set_materials(mpm_ctx *ctx, const mpm_material *mats, int32_t n);
 int32_t mpm_set_boundary(mpm_ctx *ctx, const mpm_boundary *bc);
 /* UpdateZSGrid "gravity" / "Accel" inputs (MPMPipeline.cu:838-846) */
 int32_t mpm_set_gravity(mpm_ctx *ctx, float gx, float gy, float gz);
+/* Level-set colliders (at most MPM_MAX_COLLIDERS per context), applied in
+ * order after the box walls by every boundary application.  mpm_substep
+ * advances them by dt at the start of each substep; the stage path advances
+ * them only through mpm_step_colliders (StepZSBoundary, Generation.cu:1662-1685:
+ * b += db/dt dt, s += ds/dt dt). */
+#define MPM_MAX_COLLIDERS 16
+int32_t mpm_add_collider(mpm_ctx *ctx, const mpm_collider_desc *desc, int32_t *id);
+int32_t mpm_clear_colliders(mpm_ctx *ctx);
+int32_t mpm_step_colliders(mpm_ctx *ctx, float dt);
 
 /* ToZSParticles (Generation.cpp:690-1145): host arrays -> device store.
  * NULL optional arrays take the reference defaults: v = 0, C = 0, F = I,

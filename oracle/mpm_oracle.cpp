@@ -361,6 +361,13 @@ int build_partition(const orc_scene &sc, int64_t n, const R *x, Partition &P, in
 }
 
 template <class R> struct Sim {
+  // colliders with their moving state (b, s) in R
+  struct Col {
+    const orc_collider *c;
+    R Rm[9], b[3], s;
+  };
+  std::vector<Col> cols;
+
   const orc_scene &sc;
   Dir dir;
   std::vector<Params<R>> mats;
@@ -375,6 +382,115 @@ template <class R> struct Sim {
       dir.dims[d] = s.block_dims[d];
     }
     for (int i = 0; i < s.n_materials; ++i) mats.push_back(material_params<R>(s.materials[i]));
+    for (int i = 0; i < s.n_colliders; ++i) {
+      Col c;
+      c.c = &s.colliders[i];
+      rotation_ypr(c.c->ypr_deg, c.Rm);
+      for (int a = 0; a < 3; ++a) c.b[a] = R(c.c->translation[a]);
+      c.s = R(c.c->scale);
+      cols.push_back(c);
+    }
+  }
+
+  // R = Ry(yaw) Rx(pitch) Rz(roll), angles in degrees
+  static void rotation_ypr(const float *ypr, R *Rm) {
+    const R k = R(3.14159265358979323846) / R(180);
+    const R cy = std::cos(R(ypr[0]) * k), sy = std::sin(R(ypr[0]) * k);
+    const R cp = std::cos(R(ypr[1]) * k), sp = std::sin(R(ypr[1]) * k);
+    const R cr = std::cos(R(ypr[2]) * k), sr = std::sin(R(ypr[2]) * k);
+    const R Ry[9] = {cy, 0, sy, 0, 1, 0, -sy, 0, cy};
+    const R Rx[9] = {1, 0, 0, 0, cp, -sp, 0, sp, cp};
+    const R Rz[9] = {cr, -sr, 0, sr, cr, 0, 0, 0, 1};
+    R A[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        A[i * 3 + j] = 0;
+        for (int l = 0; l < 3; ++l) A[i * 3 + j] += Ry[i * 3 + l] * Rx[l * 3 + j];
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        Rm[i * 3 + j] = 0;
+        for (int l = 0; l < 3; ++l) Rm[i * 3 + j] += A[i * 3 + l] * Rz[l * 3 + j];
+      }
+  }
+
+  // StepZSBoundary (Generation.cu:1662-1685): b += db/dt dt, s += ds/dt dt
+  void step_colliders(R dt) {
+    for (Col &c : cols) {
+      for (int a = 0; a < 3; ++a) c.b[a] += R(c.c->translation_rate[a]) * dt;
+      c.s += R(c.c->scale_rate) * dt;
+    }
+  }
+
+  // The level-set colliders on the velocity of the node at index I, in order
+  // (ApplyBoundaryOnZSGrid with a level set, Boundary.cu:83-163): trilinear
+  // signed distance and its gradient at X = R^T (p - b) / s, p = I dx; inside
+  // when negative; collider velocity R v(X) + db/dt (Boundary.cu:299-301);
+  // sticky / slip / separate as ApplyGridBoundaryOnZSGrid (Boundary.cu:56-67).
+  void apply_colliders(const int32_t *I, R *vel) const {
+    for (const Col &cl : cols) {
+      const orc_collider &c = *cl.c;
+      R p[3], q[3], X[3], u[3], t[3];
+      int64_t i0[3];
+      bool outside = false;
+      for (int a = 0; a < 3; ++a) p[a] = R(I[a]) * R(sc.dx);
+      for (int a = 0; a < 3; ++a) q[a] = (p[a] - cl.b[a]) / cl.s;
+      for (int a = 0; a < 3; ++a) X[a] = cl.Rm[0 * 3 + a] * q[0] + cl.Rm[1 * 3 + a] * q[1] + cl.Rm[2 * 3 + a] * q[2];
+      for (int a = 0; a < 3; ++a) {
+        u[a] = (X[a] - R(c.origin[a])) / R(c.spacing);
+        if (!(u[a] >= 0 && u[a] <= R(c.dims[a] - 1))) outside = true;
+      }
+      if (outside) continue;
+      for (int a = 0; a < 3; ++a) {
+        i0[a] = std::min<int64_t>(int64_t(std::floor(u[a])), c.dims[a] - 2);
+        t[a] = u[a] - R(i0[a]);
+      }
+      const int64_t sx = 1, sy = c.dims[0], sz = int64_t(c.dims[0]) * c.dims[1];
+      auto at = [&](const float *g, int dx, int dy, int dz) {
+        return R(g[(i0[0] + dx) * sx + (i0[1] + dy) * sy + (i0[2] + dz) * sz]);
+      };
+      auto tri = [&](const float *g, R *grad) {
+        R val = 0;
+        if (grad) grad[0] = grad[1] = grad[2] = 0;
+        for (int k = 0; k < 8; ++k) {
+          const int bx = (k >> 2) & 1, by = (k >> 1) & 1, bz = k & 1;
+          const R wx = bx ? t[0] : R(1) - t[0], wy = by ? t[1] : R(1) - t[1],
+                  wz = bz ? t[2] : R(1) - t[2];
+          const R f = at(g, bx, by, bz);
+          val += wx * wy * wz * f;
+          if (grad) {
+            grad[0] += (bx ? R(1) : R(-1)) * wy * wz * f;
+            grad[1] += wx * (by ? R(1) : R(-1)) * wz * f;
+            grad[2] += wx * wy * (bz ? R(1) : R(-1)) * f;
+          }
+        }
+        return val;
+      };
+      R g[3];
+      const R phi = tri(c.sdf, g);
+      if (!(phi < 0)) continue;
+      R nr[3];
+      for (int a = 0; a < 3; ++a) nr[a] = cl.Rm[a * 3 + 0] * g[0] + cl.Rm[a * 3 + 1] * g[1] + cl.Rm[a * 3 + 2] * g[2];
+      const R nn = std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+      const R rn = nn > 0 ? R(1) / nn : R(0);
+      R nrm[3] = {nr[0] * rn, nr[1] * rn, nr[2] * rn};
+      R vl[3] = {R(c.const_velocity[0]), R(c.const_velocity[1]), R(c.const_velocity[2])};
+      if (c.velocity) {
+        const int64_t plane = sz * c.dims[2];
+        for (int a = 0; a < 3; ++a) vl[a] = tri(c.velocity + a * plane, nullptr);
+      }
+      R vo[3];
+      for (int a = 0; a < 3; ++a)
+        vo[a] = cl.Rm[a * 3 + 0] * vl[0] + cl.Rm[a * 3 + 1] * vl[1] + cl.Rm[a * 3 + 2] * vl[2] +
+                R(c.translation_rate[a]);
+      if (c.type == ORC_BC_STICKY) {
+        for (int a = 0; a < 3; ++a) vel[a] = vo[a];
+        continue;
+      }
+      const R proj = nrm[0] * (vel[0] - vo[0]) + nrm[1] * (vel[1] - vo[1]) + nrm[2] * (vel[2] - vo[2]);
+      if (c.type == ORC_BC_SLIP || (c.type == ORC_BC_SEPARATE && proj < 0))
+        for (int a = 0; a < 3; ++a) vel[a] -= proj * nrm[a];
+    }
   }
 
   // Quadratic B-spline stencil (Hu et al. 2018 MLS-MPM; Jiang et al. 2016
@@ -406,6 +522,7 @@ template <class R> struct Sim {
 
   int substep(int64_t n, R *x, R *v, R *C, R *F, R *J, const R *m, const R *vol,
               const int32_t *mat, const R *mu, const R *lam, R dt) {
+    if (sc.collider_autostep) step_colliders(dt);  // the fused substep's collider time
     int rc = build_partition<R>(sc, n, x, P, nthreads);
     if (rc) return rc;
     // ZSGridFromZSPartition: zero every channel of every block
@@ -480,6 +597,7 @@ template <class R> struct Sim {
                               (c[1] + dir.lo[1]) * 4 + ((cell >> 2) & 3),
                               (c[2] + dir.lo[2]) * 4 + (cell & 3)};
         apply_bc(I, vel);
+        apply_colliders(I, vel);
         for (int d = 0; d < 3; ++d) nd[1 + d] = vel[d];
       }
     }

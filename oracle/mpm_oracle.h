@@ -52,6 +52,25 @@ typedef struct orc_material {
   float bulk, gamma;        /* equation-of-state fluid */
 } orc_material;
 
+/* Level-set collider (MakeZSLevelSet + ToZSBoundary, Generation.cu:1521-1647;
+ * resolved per node as in ApplyBoundaryOnZSGrid, Boundary.cu:83-163): dense
+ * signed distances sdf[i + dims0 (j + dims1 k)] at origin + (i, j, k) spacing
+ * in collider space; X = R^T (p - b) / s with R = Ry(yaw) Rx(pitch) Rz(roll). */
+typedef struct orc_collider {
+  int32_t type;   /* ORC_BC_STICKY / SLIP / SEPARATE */
+  int32_t dims[3];
+  float origin[3];
+  float spacing;
+  const float *sdf;
+  const float *velocity; /* 3 planes or NULL */
+  float const_velocity[3];
+  float translation[3];
+  float translation_rate[3];
+  float scale;
+  float scale_rate;
+  float ypr_deg[3];
+} orc_collider;
+
 typedef struct orc_scene {
   float dx;
   float gravity[3];
@@ -63,6 +82,9 @@ typedef struct orc_scene {
   int32_t bc_hi[3];      /* node index of the upper domain face */
   int32_t n_materials;
   const orc_material *materials;
+  int32_t n_colliders;
+  const orc_collider *colliders;
+  int32_t collider_autostep; /* 1: advance colliders by dt at the start of each substep */
 } orc_scene;
 
 typedef struct orc_stats {

@@ -25,11 +25,21 @@ class OrcMaterial(C.Structure):
                 ("bulk", C.c_float), ("gamma", C.c_float)]
 
 
+class OrcCollider(C.Structure):
+    _fields_ = [("type", C.c_int32), ("dims", C.c_int32 * 3), ("origin", C.c_float * 3),
+                ("spacing", C.c_float), ("sdf", C.c_void_p), ("velocity", C.c_void_p),
+                ("const_velocity", C.c_float * 3), ("translation", C.c_float * 3),
+                ("translation_rate", C.c_float * 3), ("scale", C.c_float),
+                ("scale_rate", C.c_float), ("ypr_deg", C.c_float * 3)]
+
+
 class OrcScene(C.Structure):
     _fields_ = [("dx", C.c_float), ("gravity", C.c_float * 3), ("block_lo", C.c_int32 * 3),
                 ("block_dims", C.c_int32 * 3), ("bc_type", C.c_int32),
                 ("bc_thickness", C.c_int32), ("bc_lo", C.c_int32 * 3), ("bc_hi", C.c_int32 * 3),
-                ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial))]
+                ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial)),
+                ("n_colliders", C.c_int32), ("colliders", C.POINTER(OrcCollider)),
+                ("collider_autostep", C.c_int32)]
 
 
 class OrcStats(C.Structure):
@@ -89,11 +99,31 @@ class _SceneHolder:
         mats = (OrcMaterial * max(1, len(scene.materials)))(
             *[make_material(m) for m in scene.materials])
         self.mats = mats
+        cols = list(getattr(scene, "colliders", []) or [])
+        self.arrays = []  # keeps the sample grids alive
+
+        def arr(a):
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            self.arrays.append(a)
+            return a.ctypes.data
+
+        carr = (OrcCollider * max(1, len(cols)))()
+        for i, c in enumerate(cols):
+            nz, ny, nx = c.sdf.shape
+            carr[i] = OrcCollider(int(c.type), (C.c_int32 * 3)(nx, ny, nz),
+                                  (C.c_float * 3)(*c.origin), float(c.spacing), arr(c.sdf),
+                                  arr(c.velocity) if c.velocity is not None else None,
+                                  (C.c_float * 3)(*c.const_velocity),
+                                  (C.c_float * 3)(*c.translation),
+                                  (C.c_float * 3)(*c.translation_rate), float(c.scale),
+                                  float(c.scale_rate), (C.c_float * 3)(*c.ypr_deg))
+        self.cols = carr
         self.s = OrcScene(float(scene.dx), (C.c_float * 3)(*scene.gravity),
                           (C.c_int32 * 3)(*scene.block_lo), (C.c_int32 * 3)(*scene.block_dims),
                           int(scene.bc_type), int(scene.bc_thickness),
                           (C.c_int32 * 3)(*scene.bc_lo), (C.c_int32 * 3)(*scene.bc_hi),
-                          len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)))
+                          len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)),
+                          len(cols), C.cast(carr, C.POINTER(OrcCollider)), 1)
 
 
 def partition(scene, x: np.ndarray) -> dict:

@@ -207,3 +207,39 @@ def test_order_stable_fp64(oracle_mod):
     b, _ = oracle_mod.run(scene, parts, 5, "f64", nthreads=4)
     np.testing.assert_array_equal(a.x, b.x)
     np.testing.assert_array_equal(a.v, b.v)
+
+
+# ---- level-set colliders (known answers) ----
+
+def _slab_scene(ctype, v0):
+    """A 4x4x4-cell slab of particles moving with v0, every stencil node of
+    every particle inside the half-space y < 0.6 of a plane collider."""
+    dx = 1.0 / 32
+    scene = S.Scene.unit_box(dx, bc_type=S.BC_NONE, dt=1e-3,
+                             materials=[S.Material(S.FCR, E=1e3, nu=0.3)])
+    scene.colliders = [S.plane_collider(0.6, 1.5, 1.0 / 16, type=ctype)]
+    x = S.box_particles((0.4, 0.3, 0.4), (4, 4, 4), dx, 8, 0, 0)
+    v = np.tile(np.asarray(v0, np.float32), (x.shape[0], 1))
+    return scene, S.make_particles(x, dx, 8, scene.materials, np.zeros(x.shape[0], np.int32), v=v)
+
+
+def test_collider_sticky_stops_particles(oracle_mod):
+    scene, parts = _slab_scene(S.BC_STICKY, (0.3, -1.0, 0.2))
+    out, st = oracle_mod.run(scene, parts, 1, "f64")
+    assert st["status"] == 0
+    np.testing.assert_allclose(out.v, 0.0, atol=1e-12)
+
+
+def test_collider_slip_keeps_tangential_velocity(oracle_mod):
+    scene, parts = _slab_scene(S.BC_SLIP, (0.3, -1.0, 0.2))
+    out, _ = oracle_mod.run(scene, parts, 1, "f64")
+    np.testing.assert_allclose(out.v[:, 0], 0.3, atol=1e-9)
+    np.testing.assert_allclose(out.v[:, 1], 0.0, atol=1e-9)  # normal part (and gravity) removed
+    np.testing.assert_allclose(out.v[:, 2], 0.2, atol=1e-9)
+
+
+def test_collider_separate_releases_outgoing_motion(oracle_mod):
+    scene, parts = _slab_scene(S.BC_SEPARATE, (0.3, 1.0, 0.2))
+    out, _ = oracle_mod.run(scene, parts, 1, "f64")
+    np.testing.assert_allclose(out.v[:, 1], 1.0 - 9.8 * scene.dt, atol=1e-9)
+    np.testing.assert_allclose(out.v[:, 0], 0.3, atol=1e-9)

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "binning.cuh"
+#include "colliders.cuh"
 #include "mpm_math.cuh"
 #include "tile_scatter.cuh"
 #include "zsmpm_internal.cuh"
@@ -264,6 +265,29 @@ __global__ void k_grid_adjoint(DevPtrs d) {
       const float vp[3] = {fw.y * r + S.gravity[0] * P.dt, fw.z * r + S.gravity[1] * P.dt,
                            fw.w * r + S.gravity[2] * P.dt};
       float vb[3] = {ad.y, ad.z, ad.w};
+      const int scene = scene_of_dir(d, gdir);
+      const int nc = P.n_colliders;
+      if (nc > 0) {
+        // the colliders act after the walls: their transpose comes first
+        const int I[3] = {(c0 + S.block_lo[0]) * 4 + l0, (c1 + S.block_lo[1]) * 4 + l1,
+                          (c2 + S.block_lo[2]) * 4 + l2};
+        float vw[3] = {vp[0], vp[1], vp[2]};
+        if (S.bc_type != MPM_BC_NONE) {
+          bool any = false;
+          const int th = S.bc_thickness;
+          for (int a = 0; a < 3; ++a) {
+            const bool lower = I[a] < S.bc_lo[a] + th, upper = I[a] > S.bc_hi[a] - th;
+            if (!(lower || upper)) continue;
+            any = true;
+            if (S.bc_type == MPM_BC_SLIP) vw[a] = 0.0f;
+            if (S.bc_type == MPM_BC_SEPARATE && ((lower && vw[a] < 0.0f) || (upper && vw[a] > 0.0f)))
+              vw[a] = 0.0f;
+          }
+          if (any && S.bc_type == MPM_BC_STICKY) vw[0] = vw[1] = vw[2] = 0.0f;
+        }
+        const float p[3] = {(float)I[0] * S.dx, (float)I[1] * S.dx, (float)I[2] * S.dx};
+        apply_colliders_adjoint(d, nc, scene, p, vw, vb);
+      }
       if (S.bc_type != MPM_BC_NONE) {
         const int I[3] = {(c0 + S.block_lo[0]) * 4 + l0, (c1 + S.block_lo[1]) * 4 + l1,
                           (c2 + S.block_lo[2]) * 4 + l2};

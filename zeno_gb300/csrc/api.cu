@@ -55,6 +55,8 @@ struct mpm_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   Counters *h_cnt = nullptr;  // pinned
   std::vector<void *> allocs;
+  std::vector<void *> collider_allocs;  // sample grids of the level-set colliders
+  std::vector<ColliderDev> colliders;   // host copy (positions as set)
   cudaEvent_t events[MPM_NUM_STAGES + 1] = {};
   std::vector<SceneParams> scenes;
   int n_materials = 0;
@@ -116,6 +118,13 @@ int32_t set_dt(mpm_ctx *c, float dt) {
   return push_params(c);
 }
 
+void set_auto_step(mpm_ctx *c, int v) {
+  if (c->prm.auto_step != v) {
+    c->prm.auto_step = v;
+    c->prm_dirty = true;
+  }
+}
+
 int32_t check(mpm_ctx *c) {
   if (!c) return fail(MPM_ERR_INVALID, "null context");
   cudaError_t e = cudaSetDevice(c->device);
@@ -163,6 +172,7 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   launch_p2g(c->d, cur, c->stream);
   mark(MPM_STAGE_GRID_UPDATE);
   launch_grid_gather(c->d, 3, c->stream);
+  if (!c->colliders.empty()) launch_apply_colliders(c->d, c->stream);
   mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, 1, c->stream);
   mark(MPM_NUM_STAGES);
@@ -300,7 +310,7 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
       (rc = dalloc(c, &d.grid, (size_t)capg * 64)) ||
       (rc = dalloc(c, &d.tile_sums, (size_t)3 * d.ntiles)) || (rc = dalloc(c, &d.cnt, 1)) ||
       (rc = dalloc(c, &d.prm, 1)) || (rc = dalloc(c, &d.scn, n_scenes)) ||
-      (rc = dalloc(c, &d.mats, kMaxMaterials)))
+      (rc = dalloc(c, &d.mats, kMaxMaterials)) || (rc = dalloc(c, &d.colliders, kMaxColliders)))
     return bail(rc);
   if (cudaMallocHost(&c->h_cnt, sizeof(Counters)) != cudaSuccess)
     return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
@@ -363,6 +373,7 @@ int32_t mpm_ctx_destroy(mpm_ctx *c) {
   for (cudaEvent_t e : c->events)
     if (e) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
+  for (void *p : c->collider_allocs) cudaFree(p);
   if (c->h_cnt) cudaFreeHost(c->h_cnt);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -436,6 +447,119 @@ int32_t mpm_set_boundary(mpm_ctx *c, const mpm_boundary *bc) {
   }
   c->prm_dirty = true;
   return push_params(c);
+}
+
+// R = Ry(yaw) Rx(pitch) Rz(roll), angles in degrees
+static void ypr_rotation(const float ypr_deg[3], float R[9]) {
+  const double k = 3.14159265358979323846 / 180.0;
+  const double cy = std::cos(ypr_deg[0] * k), sy = std::sin(ypr_deg[0] * k);
+  const double cp = std::cos(ypr_deg[1] * k), sp = std::sin(ypr_deg[1] * k);
+  const double cr = std::cos(ypr_deg[2] * k), sr = std::sin(ypr_deg[2] * k);
+  const double Ry[9] = {cy, 0, sy, 0, 1, 0, -sy, 0, cy};
+  const double Rx[9] = {1, 0, 0, 0, cp, -sp, 0, sp, cp};
+  const double Rz[9] = {cr, -sr, 0, sr, cr, 0, 0, 0, 1};
+  double A[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      A[i * 3 + j] = 0;
+      for (int l = 0; l < 3; ++l) A[i * 3 + j] += Ry[i * 3 + l] * Rx[l * 3 + j];
+    }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double v = 0;
+      for (int l = 0; l < 3; ++l) v += A[i * 3 + l] * Rz[l * 3 + j];
+      R[i * 3 + j] = (float)v;
+    }
+}
+
+// the captured substep graphs contain the collider pass or not
+static void drop_graphs(mpm_ctx *c) {
+  for (int k = 0; k < 2; ++k)
+    if (c->graph[k]) {
+      cudaGraphExecDestroy(c->graph[k]);
+      c->graph[k] = nullptr;
+    }
+}
+
+int32_t mpm_add_collider(mpm_ctx *c, const mpm_collider_desc *desc, int32_t *id) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!desc || !desc->sdf) return fail(MPM_ERR_INVALID, "null collider or signed distance grid");
+  if (desc->type != MPM_BC_STICKY && desc->type != MPM_BC_SLIP && desc->type != MPM_BC_SEPARATE)
+    return fail(MPM_ERR_INVALID, "collider type must be sticky, slip or separate");
+  if (desc->scene < -1 || desc->scene >= (int)c->scenes.size())
+    return fail(MPM_ERR_INVALID, "collider scene out of range");
+  long long cells = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (desc->dims[a] < 2) return fail(MPM_ERR_INVALID, "collider grid needs >= 2 samples per axis");
+    cells *= desc->dims[a];
+  }
+  if (!(desc->spacing > 0.0f) || !(desc->scale > 0.0f))
+    return fail(MPM_ERR_INVALID, "collider spacing and scale must be positive");
+  if ((int)c->colliders.size() >= kMaxColliders)
+    return fail(MPM_ERR_CAPACITY, "at most MPM_MAX_COLLIDERS colliders per context");
+  ColliderDev cd{};
+  ypr_rotation(desc->ypr_deg, cd.R);
+  for (int a = 0; a < 3; ++a) {
+    cd.b[a] = desc->translation[a];
+    cd.db[a] = desc->translation_rate[a];
+    cd.origin[a] = desc->origin[a];
+    cd.dims[a] = desc->dims[a];
+    cd.cvel[a] = desc->const_velocity[a];
+  }
+  cd.s = desc->scale;
+  cd.ds = desc->scale_rate;
+  cd.inv_h = 1.0f / desc->spacing;
+  cd.type = desc->type;
+  cd.scene = desc->scene;
+  cd.has_vel = desc->velocity != nullptr;
+  float *buf = nullptr;
+  const size_t floats = (size_t)cells * (cd.has_vel ? 4 : 1);
+  cudaError_t e = cudaMalloc(&buf, floats * sizeof(float));
+  if (e != cudaSuccess) return fail(MPM_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->collider_allocs.push_back(buf);
+  ZS_CUDA(cudaMemcpyAsync(buf, desc->sdf, cells * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  cd.sdf = buf;
+  cd.vel = nullptr;
+  if (cd.has_vel) {
+    ZS_CUDA(cudaMemcpyAsync(buf + cells, desc->velocity, 3 * cells * sizeof(float),
+                            cudaMemcpyHostToDevice, c->stream));
+    cd.vel = buf + cells;
+  }
+  const int k = (int)c->colliders.size();
+  c->colliders.push_back(cd);
+  // only the new entry: the device copies of earlier colliders may have moved
+  ZS_CUDA(cudaMemcpyAsync(c->d.colliders + k, &c->colliders[k], sizeof(ColliderDev),
+                          cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));  // the host sources may go away
+  c->prm.n_colliders = k + 1;
+  c->prm_dirty = true;
+  if (id) *id = k;
+  if (k == 0) drop_graphs(c);
+  return push_params(c);
+}
+
+int32_t mpm_clear_colliders(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  c->prm.n_colliders = 0;
+  c->prm_dirty = true;
+  if ((rc = push_params(c))) return rc;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));  // no kernel still reads the sample grids
+  for (void *p : c->collider_allocs) cudaFree(p);
+  c->collider_allocs.clear();
+  if (!c->colliders.empty()) drop_graphs(c);
+  c->colliders.clear();
+  return MPM_OK;
+}
+
+int32_t mpm_step_colliders(mpm_ctx *c, float dt) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!std::isfinite(dt)) return fail(MPM_ERR_INVALID, "dt must be finite");
+  if ((rc = push_params(c))) return rc;
+  if (c->prm.n_colliders > 0) launch_step_colliders(c->d, dt, c->stream);
+  return launch_check("step colliders");
 }
 
 int32_t mpm_set_gravity(mpm_ctx *c, float gx, float gy, float gz) {
@@ -591,6 +715,7 @@ int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *
 int32_t mpm_partition(mpm_ctx *c) {
   int32_t rc = check(c);
   if (rc) return rc;
+  set_auto_step(c, 0);  // the stage path moves colliders only on request
   if ((rc = push_params(c)) || (rc = prepare_partition(c))) return rc;
   enqueue_bin_if_needed(c);
   enqueue_sort(c);
@@ -642,6 +767,7 @@ int32_t mpm_apply_boundary(mpm_ctx *c) {
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "boundary needs a partition");
   if ((rc = push_params(c))) return rc;
   launch_grid_update(c->d, 2, c->stream);
+  if (!c->colliders.empty()) launch_apply_colliders(c->d, c->stream);
   return launch_check("boundary");
 }
 
@@ -671,6 +797,7 @@ int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
   int32_t rc = check(c);
   if (rc) return rc;
   if (n_substeps < 0) return fail(MPM_ERR_INVALID, "negative substep count");
+  set_auto_step(c, 1);
   if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
   if (n_substeps > 0) enqueue_bin_if_needed(c);
   const bool graphs = graphs_enabled();
@@ -694,6 +821,7 @@ int32_t mpm_substep_timed(mpm_ctx *c, float dt, float *stage_ms, int32_t n_stage
   if (rc) return rc;
   if (!stage_ms || n_stages < MPM_NUM_STAGES)
     return fail(MPM_ERR_INVALID, "stage_ms needs MPM_NUM_STAGES entries");
+  set_auto_step(c, 1);
   if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
   if (!c->events[0]) {
     for (int i = 0; i <= MPM_NUM_STAGES; ++i) ZS_CUDA(cudaEventCreate(&c->events[i]));
@@ -801,11 +929,16 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
     return fail(MPM_ERR_INVALID,
                 "the adjoint covers fixed-corotated, Neo-Hookean and StVK-Hencky (with or without "
                 "the Drucker-Prager projection) materials, not the equation-of-state fluid");
+  for (const ColliderDev &cd : c->colliders)
+    if (cd.db[0] != 0.0f || cd.db[1] != 0.0f || cd.db[2] != 0.0f || cd.ds != 0.0f)
+      return fail(MPM_ERR_INVALID, "the adjoint takes static colliders only");
+  set_auto_step(c, 0);
   if ((rc = set_dt(c, dt)) || (rc = prepare_partition(c))) return rc;
   enqueue_bin_if_needed(c);
   enqueue_sort(c);
   launch_p2g(c->d, c->cur, c->stream);
   launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
+  if (!c->colliders.empty()) launch_apply_colliders(c->d, c->stream);
   const long long n = c->prm.n;
   launch_g2p_adjoint(c->d, c->cur, adj_next, adj_prev, grad_mu, grad_lam, n, c->stream);
   launch_grid_adjoint(c->d, c->stream);

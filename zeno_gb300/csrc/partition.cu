@@ -26,6 +26,7 @@
 #include <algorithm>
 
 #include "binning.cuh"
+#include "colliders.cuh"
 #include "zsmpm_internal.cuh"
 
 namespace zsmpm {
@@ -114,7 +115,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
   __shared__ int red[3][kScanThreads / 32];
   __shared__ int tile_prefix[3];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (blockIdx.x == 0 && tid == 0) d.cnt->max_vel_sqr_bits = 0u;
+  if (blockIdx.x == 0 && tid == 0) {
+    d.cnt->max_vel_sqr_bits = 0u;
+    // the fused substep moves the colliders to this substep's time
+    if (d.prm->auto_step) step_colliders(d, d.prm->n_colliders, d.prm->dt);
+  }
   int pf = 0, pc = 0, pe = 0;
   for (int t = tid; t < (int)blockIdx.x; t += kScanThreads) {
     pf += d.tile_sums[3 * t];

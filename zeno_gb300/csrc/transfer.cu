@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "binning.cuh"
+#include "colliders.cuh"
 #include "cp_async.cuh"
 #include "mpm_math.cuh"
 #include "tile_scatter.cuh"
@@ -348,10 +349,12 @@ __global__ void __launch_bounds__(kColThreads, 4) k_p2g(DevPtrs d, const float *
 // coordinate l + 4 o when that is < 6.  The <= 8 tiles are added in the fixed
 // order o = (0,0,0), (0,0,1), ..., so the sums are reproducible.  mode bit 1
 // applies UpdateZSGrid and bit 2 ApplyBoundaryOnZSGrid to the sum.
-__device__ __forceinline__ void update_node(const SceneParams &S, float dt, int mode, int ldir,
-                                            int cell, float4 &g, float &vmax);
-__device__ __forceinline__ void update_node_at(const SceneParams &S, float dt, int mode,
-                                               const int (&I)[3], float4 &g, float &vmax);
+__device__ __forceinline__ void update_node(const DevPtrs &d, int scene, const SceneParams &S,
+                                            float dt, int mode, int ldir, int cell, float4 &g,
+                                            float &vmax);
+__device__ __forceinline__ void update_node_at(const DevPtrs &d, int scene, const SceneParams &S,
+                                               float dt, int mode, const int (&I)[3], float4 &g,
+                                               float &vmax);
 
 // One 64-thread group per grid block, 4 blocks per CTA: the group fetches its
 // block's scene, node origin and the (particle block) tiles of the 8 blocks
@@ -406,7 +409,7 @@ __global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, i
       }
       if (g.x != 0.0f) {
         const int I[3] = {sorg[grp][0] + l0, sorg[grp][1] + l1, sorg[grp][2] + l2};
-        update_node_at(d.scn[sorg[grp][3]], P.dt, mode, I, g, vmax);
+        update_node_at(d, sorg[grp][3], d.scn[sorg[grp][3]], P.dt, mode, I, g, vmax);
       }
       d.grid[(long long)gb * 64 + cell] = g;
     }
@@ -426,18 +429,20 @@ __global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, i
 // I_a < lo_a + thickness and in the upper wall when I_a > hi_a - thickness;
 // sticky sets v = 0, slip removes the wall-normal component, separate removes
 // it only when it points into the wall (collider velocity 0).
-__device__ __forceinline__ void update_node(const SceneParams &S, float dt, int mode, int ldir,
-                                            int cell, float4 &g, float &vmax) {
+__device__ __forceinline__ void update_node(const DevPtrs &d, int scene, const SceneParams &S,
+                                            float dt, int mode, int ldir, int cell, float4 &g,
+                                            float &vmax) {
   const int dz = S.block_dims[2], dy = S.block_dims[1];
   const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
                     (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
                     ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
-  update_node_at(S, dt, mode, I, g, vmax);
+  update_node_at(d, scene, S, dt, mode, I, g, vmax);
 }
 
 // the same at the node's global index I
-__device__ __forceinline__ void update_node_at(const SceneParams &S, float dt, int mode,
-                                               const int (&I)[3], float4 &g, float &vmax) {
+__device__ __forceinline__ void update_node_at(const DevPtrs &d, int scene, const SceneParams &S,
+                                               float dt, int mode, const int (&I)[3], float4 &g,
+                                               float &vmax) {
   if (mode & 1) {
     const float r = 1.0f / g.x;
     g.y = g.y * r + S.gravity[0] * dt;
@@ -476,8 +481,9 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
     float4 g = d.grid[idx];
     if (g.x == 0.0f) continue;
     const int gdir = d.gb_dir[idx >> 6];
-    const SceneParams &S = d.scn[scene_of_dir(d, gdir)];
-    update_node(S, P.dt, mode, gdir - S.dir_off, (int)(idx & 63), g, vmax);
+    const int sc = scene_of_dir(d, gdir);
+    const SceneParams &S = d.scn[sc];
+    update_node(d, sc, S, P.dt, mode, gdir - S.dir_off, (int)(idx & 63), g, vmax);
     d.grid[idx] = g;
   }
   if (mode & 1) {
@@ -906,6 +912,45 @@ void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
 
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
   k_grid_gather<<<d.grid_stream, 64 * kGatherBlocks, 0, s>>>(d, mode);
+}
+
+// ApplyBoundaryOnZSGrid with level sets: the colliders of each node's scene,
+// after the box walls (its own pass, launched only when colliders exist)
+__global__ void k_apply_colliders(DevPtrs d) {
+  const int nc = d.prm->n_colliders;
+  const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    float4 g = d.grid[idx];
+    if (g.x == 0.0f) continue;
+    const int gdir = d.gb_dir[idx >> 6];
+    const int sc = scene_of_dir(d, gdir);
+    const SceneParams &S = d.scn[sc];
+    const int dz = S.block_dims[2], dy = S.block_dims[1];
+    const int ldir = gdir - S.dir_off, cell = (int)(idx & 63);
+    const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
+                      (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
+                      ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
+    const float p[3] = {(float)I[0] * S.dx, (float)I[1] * S.dx, (float)I[2] * S.dx};
+    float vel[3] = {g.y, g.z, g.w};
+    apply_colliders(d, nc, sc, p, vel);
+    g.y = vel[0];
+    g.z = vel[1];
+    g.w = vel[2];
+    d.grid[idx] = g;
+  }
+}
+
+void launch_apply_colliders(const DevPtrs &d, cudaStream_t s) {
+  k_apply_colliders<<<d.grid_stream, 256, 0, s>>>(d);
+}
+
+__global__ void k_step_colliders(DevPtrs d, float dt) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) step_colliders(d, d.prm->n_colliders, dt);
+}
+
+void launch_step_colliders(const DevPtrs &d, float dt, cudaStream_t s) {
+  k_step_colliders<<<1, 32, 0, s>>>(d, dt);
 }
 
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {

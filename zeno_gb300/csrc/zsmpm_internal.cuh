@@ -95,7 +95,27 @@ struct Counters {
 struct SimParams {
   float dt;
   int has_lame;
-  long long n;  // particles of all scenes
+  int n_colliders;  // level-set colliders in DevPtrs::colliders
+  int auto_step;    // the fused substep advances the colliders by dt
+  long long n;      // particles of all scenes
+};
+
+// Level-set collider (MakeZSLevelSet + ToZSBoundary): dense signed distance
+// grid in collider space, transform X = R^T (p - b) / s.
+constexpr int kMaxColliders = MPM_MAX_COLLIDERS;
+struct ColliderDev {
+  float R[9];       // rotation, row-major
+  float b[3], db[3];
+  float s, ds;
+  float origin[3];
+  float inv_h;      // 1 / sample spacing
+  int dims[3];
+  int type;         // MPM_BC_*
+  int scene;        // -1: every scene
+  int has_vel;
+  float cvel[3];    // material velocity when has_vel == 0
+  const float *sdf;
+  const float *vel;  // 3 planes, or null
 };
 
 // One scene of a context: its grid spacing, its slice of the concatenated
@@ -134,6 +154,7 @@ struct DevPtrs {
   float4 *grid;
   float4 *ptile;      // per particle block: its 6^3 P2G node sums (216 float4)
   float4 *ptile_adj;  // the same for the G2P adjoint (differentiable mode)
+  ColliderDev *colliders;  // kMaxColliders entries (device)
   int keep_order;     // differentiable mode: G2P writes each particle to its own slot
   int planar_x;       // pbuf[0] holds positions as 3 planes of `cap` floats (binning only)
   int32_t *tile_sums;
@@ -165,6 +186,8 @@ void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s);
 // gravity, bit 2: boundary (mode 0 leaves m, mv as the reference P2G does)
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s);
 // mode bit 1: momentum -> velocity + gravity, bit 2: boundary, on the grid
+void launch_step_colliders(const DevPtrs &d, float dt, cudaStream_t s);
+void launch_apply_colliders(const DevPtrs &d, cudaStream_t s);
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s);
 // fuse_rm: return mapping in G2P; fuse_bin: bin the new positions for the
 // next partition

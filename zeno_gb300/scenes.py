@@ -64,6 +64,49 @@ class Material:
 
 
 @dataclass
+class Collider:
+    """Level-set collider (MakeZSLevelSet + ToZSBoundary): signed distances
+    sdf[k, j, i] (x fastest) at origin + (i, j, k) * spacing in collider
+    space, an optional material velocity field velocity[3, k, j, i] (else
+    const_velocity), the transform X = R^T (p - b) / s with R from yaw
+    (about y), pitch (about x), roll (about z) in degrees, and the rates of b
+    and s."""
+    sdf: np.ndarray
+    origin: tuple = (0.0, 0.0, 0.0)
+    spacing: float = 1.0
+    type: int = 1  # BC_STICKY
+    velocity: np.ndarray = None
+    const_velocity: tuple = (0.0, 0.0, 0.0)
+    translation: tuple = (0.0, 0.0, 0.0)
+    translation_rate: tuple = (0.0, 0.0, 0.0)
+    scale: float = 1.0
+    scale_rate: float = 0.0
+    ypr_deg: tuple = (0.0, 0.0, 0.0)
+    scene: int = -1
+
+
+def sphere_collider(center, radius: float, spacing: float, type: int = 1, pad: int = 3, **kw):
+    """Sphere |X| - radius sampled on a cube of spacing `spacing` around the
+    collider-space origin, placed at `center` (the translation)."""
+    n = int(np.ceil(radius / spacing)) + pad
+    g = (np.arange(2 * n + 1) - n) * spacing
+    Z, Y, X = np.meshgrid(g, g, g, indexing="ij")
+    sdf = (np.sqrt(X * X + Y * Y + Z * Z) - radius).astype(np.float32)
+    return Collider(sdf=sdf, origin=(-n * spacing,) * 3, spacing=spacing, type=type,
+                    translation=tuple(center), **kw)
+
+
+def plane_collider(height: float, extent: float, spacing: float, type: int = 1, **kw):
+    """Half-space y < height (signed distance y - height, exact under
+    trilinear interpolation) sampled over [-extent, extent]^3."""
+    n = int(np.ceil(extent / spacing))
+    g = (np.arange(2 * n + 1) - n) * spacing
+    Z, Y, X = np.meshgrid(g, g, g, indexing="ij")
+    sdf = (Y - height).astype(np.float32)
+    return Collider(sdf=sdf, origin=(-n * spacing,) * 3, spacing=spacing, type=type, **kw)
+
+
+@dataclass
 class Scene:
     """Grid, boundary and material description of one MPM scene."""
     dx: float
@@ -76,6 +119,7 @@ class Scene:
     bc_hi: tuple = (0, 0, 0)
     materials: list = field(default_factory=list)
     dt: float = 1e-4
+    colliders: list = field(default_factory=list)
 
     @staticmethod
     def unit_box(dx: float, **kw) -> "Scene":

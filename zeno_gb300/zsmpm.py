@@ -50,6 +50,14 @@ class SceneDesc(C.Structure):
                 ("gravity", C.c_float * 3), ("boundary", Boundary)]
 
 
+class ColliderDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("scene", C.c_int32), ("dims", C.c_int32 * 3),
+                ("origin", C.c_float * 3), ("spacing", C.c_float), ("sdf", C.c_void_p),
+                ("velocity", C.c_void_p), ("const_velocity", C.c_float * 3),
+                ("translation", C.c_float * 3), ("translation_rate", C.c_float * 3),
+                ("scale", C.c_float), ("scale_rate", C.c_float), ("ypr_deg", C.c_float * 3)]
+
+
 class LaunchConfig(C.Structure):
     _fields_ = [("p2g_ctas_per_sm", C.c_int32), ("g2p_ctas_per_sm", C.c_int32),
                 ("sort_ctas_per_sm", C.c_int32), ("stream_ctas_per_sm", C.c_int32),
@@ -70,7 +78,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
-           "mpm_adjoint_substep"]
+           "mpm_adjoint_substep", "mpm_add_collider", "mpm_clear_colliders",
+           "mpm_step_colliders"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 
@@ -100,6 +109,9 @@ def load(path: str = LIB_PATH):
         "mpm_set_materials": ([P, C.POINTER(Material), i32], i32),
         "mpm_set_boundary": ([P, C.POINTER(Boundary)], i32),
         "mpm_set_gravity": ([P, f32, f32, f32], i32),
+        "mpm_add_collider": ([P, P, P], i32),
+        "mpm_clear_colliders": ([P], i32),
+        "mpm_step_colliders": ([P, f32], i32),
         "mpm_particles_upload": ([P, i64] + [P] * 10, i32),
         "mpm_particles_set_lame": ([P, P, P], i32),
         "mpm_particles_download": ([P] + [P] * 5, i32),
@@ -159,6 +171,34 @@ class Context:
         self.set_materials(scene.materials)
         self.set_boundary(scene.bc_type, scene.bc_thickness, scene.bc_lo, scene.bc_hi)
         self.set_gravity(*scene.gravity)
+        for c in getattr(scene, "colliders", []) or []:
+            self.add_collider(c)
+
+    def add_collider(self, c, scene: int = None) -> int:
+        """mpm_add_collider for a scenes.Collider; returns its index."""
+        sdf = np.ascontiguousarray(c.sdf, dtype=np.float32)
+        nz, ny, nx = sdf.shape
+        vel = None if c.velocity is None else np.ascontiguousarray(c.velocity, dtype=np.float32)
+        if vel is not None and vel.shape != (3, nz, ny, nx):
+            raise ValueError("collider velocity must have shape (3,) + sdf.shape")
+        desc = ColliderDesc(int(c.type), int(c.scene if scene is None else scene),
+                            (C.c_int32 * 3)(nx, ny, nz), (C.c_float * 3)(*c.origin),
+                            float(c.spacing), sdf.ctypes.data,
+                            vel.ctypes.data if vel is not None else None,
+                            (C.c_float * 3)(*c.const_velocity), (C.c_float * 3)(*c.translation),
+                            (C.c_float * 3)(*c.translation_rate), float(c.scale),
+                            float(c.scale_rate), (C.c_float * 3)(*c.ypr_deg))
+        idx = C.c_int32(-1)
+        self._check(self._L.mpm_add_collider(self.h, C.byref(desc), C.byref(idx)),
+                    "mpm_add_collider")
+        return idx.value
+
+    def clear_colliders(self):
+        self._check(self._L.mpm_clear_colliders(self.h), "mpm_clear_colliders")
+
+    def step_colliders(self, dt: float):
+        """StepZSBoundary: b += db/dt dt, s += ds/dt dt (stage path)."""
+        self._check(self._L.mpm_step_colliders(self.h, float(dt)), "mpm_step_colliders")
 
     @property
     def dir_size(self) -> int:
