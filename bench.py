@@ -227,6 +227,49 @@ def batched_form(zsmpm, steps: int, dev: int):
             "_check": {"substeps": check_steps, "scenes": check}}
 
 
+def collider_form(zsmpm, steps: int, dev: int):
+    """The plain four-material scene with a level-set collider: a slip sphere
+    (radius 0.1, sample spacing dx) at (0.7, 0.35, 0.36), pressing down at
+    0.5 m/s into the top of the Neo-Hookean region, stepped on the device
+    every substep; against the same context with no collider, timed in the
+    same way."""
+    import torch
+    from zeno_gb300 import scenes
+    scene, parts = make_workload()
+    stream = torch.cuda.Stream(device=dev)
+    ctx = zsmpm.Context(scene, max_particles=parts.n, device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed():
+        ctx.upload(parts)
+        ctx.substep(scene.dt, 5)
+        ctx.sync()
+        e0.record(stream)
+        ctx.substep(scene.dt, steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        ctx.sync()
+        return ms, ctx.stats()
+
+    ms_free, _ = timed()
+    ctx.add_collider(scenes.sphere_collider((0.7, 0.35, 0.36), 0.1, scene.dx, scenes.BC_SLIP,
+                                            translation_rate=(0.0, -0.5, 0.0)))
+    ms_col, st = timed()
+    stage = [ctx.substep_timed(scene.dt) for _ in range(10)]
+    ctx.sync()
+    ctx.close()
+    return {"workload": "plain 2,097,152-particle four-material scene + a moving slip sphere "
+                        "collider (dense 59^3 signed-distance samples)",
+            "value": parts.n * steps / (ms_col * 1e-3), "unit": METRIC, "steps": steps,
+            "ms_per_step": ms_col / steps, "ms_per_step_without_collider": ms_free / steps,
+            "collider_ms_per_step": (ms_col - ms_free) / steps,
+            "grid_update_stage_ms": statistics.mean(r["grid_update"] for r in stage),
+            "status": st["status"]}
+
+
 def differentiable_form(zsmpm, dev: int, steps: int = 64, ckpt: int = 16):
     """The differentiable form: 65,536 fixed-corotated particles at dx = 1/128
     (E ~ U[3e4, 1e5] per particle), 64 substeps with a checkpoint every 16,
@@ -613,6 +656,7 @@ def run_gpu(args):
     forms = {}
     if not args.no_forms:
         forms["batched"] = batched_form(zsmpm, max(10, min(args.steps, 100)), dev)
+        forms["collider"] = collider_form(zsmpm, max(10, min(args.steps, 500)), dev)
         forms["fwd_bwd"] = differentiable_form(zsmpm, dev)
         forms["fwd_bwd_sand_16M"] = sand_form(zsmpm, dev)
     if rank != 0:

@@ -176,7 +176,8 @@ int32_t mpm_set_gravity(mpm_ctx *ctx, float gx, float gy, float gz);
 #define MPM_MAX_COLLIDERS 16
 int32_t mpm_add_collider(mpm_ctx *ctx, const mpm_collider_desc *desc, int32_t *id);
 int32_t mpm_clear_colliders(mpm_ctx *ctx);
-int32_t mpm_step_colliders(mpm_ctx *ctx, float dt);
+/* id: the collider from mpm_add_collider, or -1 for every collider */
+int32_t mpm_step_colliders(mpm_ctx *ctx, int32_t id, float dt);
 
 /* ToZSParticles (Generation.cpp:690-1145): host arrays -> device store.
  * NULL optional arrays take the reference defaults: v = 0, C = 0, F = I,
@@ -206,7 +207,13 @@ int32_t mpm_grid_clear(mpm_ctx *ctx);
 int32_t mpm_p2g(mpm_ctx *ctx, float dt);
 /* max_vel_sqr: host pointer that receives MaxVelSqr (synchronises), or NULL */
 int32_t mpm_grid_update(mpm_ctx *ctx, float dt, float *max_vel_sqr);
+/* the box walls, then every collider in id order */
 int32_t mpm_apply_boundary(mpm_ctx *ctx);
+/* one ApplyBoundaryOnZSGrid of a wall boundary (Boundary.cu:83-163 with the
+ * domain walls only) or of the level-set collider `id` (-1: every collider);
+ * node graphs that apply several boundaries call these in graph order */
+int32_t mpm_apply_walls(mpm_ctx *ctx);
+int32_t mpm_apply_collider(mpm_ctx *ctx, int32_t id);
 int32_t mpm_g2p(mpm_ctx *ctx, float dt);
 int32_t mpm_return_mapping(mpm_ctx *ctx);
 

@@ -20,7 +20,8 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ZSPartitionForZSParticles", "ExpandZSPartition", "ZSGridFromZSPartition",
          "ZSParticleToZSGrid", "UpdateZSGrid", "ApplyBoundaryOnZSGrid", "ToZSBoundary",
          "ZSGridToZSParticle", "ZSReturnMapping", "AdjustParticleMaterial",
-         "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject"]
+         "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
+         "StepZSBoundary"]
 
 
 def parse_braces(s, i):

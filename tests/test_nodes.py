@@ -10,7 +10,10 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 # sockets this backend adds to reference nodes (documented extensions)
-EXTRA_INPUTS = {"ToZSBoundary": {"dx", "thickness", "domain_min", "domain_max"}}
+EXTRA_INPUTS = {"ToZSBoundary": {"dx", "thickness", "domain_min", "domain_max"},
+                # dense level sets filled from a primitive or an analytic shape
+                "MakeZSLevelSet": {"sdf_prim", "dims", "shape", "center", "radius", "height",
+                                   "extent"}}
 # enum inputs whose option list this backend extends
 EXTENDED_ENUMS = {("ConfigConstitutiveModel", "type")}
 

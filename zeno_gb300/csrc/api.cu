@@ -172,7 +172,7 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   launch_p2g(c->d, cur, c->stream);
   mark(MPM_STAGE_GRID_UPDATE);
   launch_grid_gather(c->d, 3, c->stream);
-  if (!c->colliders.empty()) launch_apply_colliders(c->d, c->stream);
+  if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
   mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, 1, c->stream);
   mark(MPM_NUM_STAGES);
@@ -513,6 +513,7 @@ int32_t mpm_add_collider(mpm_ctx *c, const mpm_collider_desc *desc, int32_t *id)
   cd.type = desc->type;
   cd.scene = desc->scene;
   cd.has_vel = desc->velocity != nullptr;
+  collider_world_box(cd);
   float *buf = nullptr;
   const size_t floats = (size_t)cells * (cd.has_vel ? 4 : 1);
   cudaError_t e = cudaMalloc(&buf, floats * sizeof(float));
@@ -553,12 +554,14 @@ int32_t mpm_clear_colliders(mpm_ctx *c) {
   return MPM_OK;
 }
 
-int32_t mpm_step_colliders(mpm_ctx *c, float dt) {
+int32_t mpm_step_colliders(mpm_ctx *c, int32_t id, float dt) {
   int32_t rc = check(c);
   if (rc) return rc;
   if (!std::isfinite(dt)) return fail(MPM_ERR_INVALID, "dt must be finite");
+  if (id < -1 || id >= (int32_t)c->colliders.size())
+    return fail(MPM_ERR_INVALID, "collider id out of range");
   if ((rc = push_params(c))) return rc;
-  if (c->prm.n_colliders > 0) launch_step_colliders(c->d, dt, c->stream);
+  if (c->prm.n_colliders > 0) launch_step_colliders(c->d, id, dt, c->stream);
   return launch_check("step colliders");
 }
 
@@ -767,8 +770,29 @@ int32_t mpm_apply_boundary(mpm_ctx *c) {
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "boundary needs a partition");
   if ((rc = push_params(c))) return rc;
   launch_grid_update(c->d, 2, c->stream);
-  if (!c->colliders.empty()) launch_apply_colliders(c->d, c->stream);
+  if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
   return launch_check("boundary");
+}
+
+int32_t mpm_apply_walls(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "boundary needs a partition");
+  if ((rc = push_params(c))) return rc;
+  launch_grid_update(c->d, 2, c->stream);
+  return launch_check("walls");
+}
+
+int32_t mpm_apply_collider(mpm_ctx *c, int32_t id) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "collider needs a partition");
+  if (id < -1 || id >= (int32_t)c->colliders.size())
+    return fail(MPM_ERR_INVALID, "collider id out of range");
+  if (c->colliders.empty()) return MPM_OK;
+  if ((rc = push_params(c))) return rc;
+  launch_apply_colliders(c->d, id, c->stream);
+  return launch_check("collider");
 }
 
 int32_t mpm_g2p(mpm_ctx *c, float dt) {
@@ -938,7 +962,7 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
   enqueue_sort(c);
   launch_p2g(c->d, c->cur, c->stream);
   launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
-  if (!c->colliders.empty()) launch_apply_colliders(c->d, c->stream);
+  if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
   const long long n = c->prm.n;
   launch_g2p_adjoint(c->d, c->cur, adj_next, adj_prev, grad_mu, grad_lam, n, c->stream);
   launch_grid_adjoint(c->d, c->stream);

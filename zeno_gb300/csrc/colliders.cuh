@@ -105,9 +105,9 @@ __device__ __forceinline__ bool collider_in_scene(const ColliderDev &c, int scen
 }
 
 // every collider of the scene, in order, on the velocity of the node at p
-__device__ __forceinline__ void apply_colliders(const DevPtrs &d, int nc, int scene,
+__device__ __forceinline__ void apply_colliders(const DevPtrs &d, int k0, int k1, int scene,
                                                const float (&p)[3], float (&v)[3]) {
-  for (int k = 0; k < nc; ++k) {
+  for (int k = k0; k < k1; ++k) {
     const ColliderDev &c = d.colliders[k];
     if (!collider_in_scene(c, scene) || c.type == MPM_BC_NONE) continue;
     float n[3];
@@ -150,7 +150,21 @@ __device__ __forceinline__ void step_colliders(const DevPtrs &d, int nc, float d
 #pragma unroll
     for (int a = 0; a < 3; ++a) c.b[a] += c.db[a] * dt;
     c.s += c.ds * dt;
+    collider_world_box(c);
   }
+}
+
+// is p inside the world box of any collider k0..k1-1 of the scene
+__device__ __forceinline__ bool near_colliders(const DevPtrs &d, int k0, int k1, int scene,
+                                              const float (&p)[3]) {
+  for (int k = k0; k < k1; ++k) {
+    const ColliderDev &c = d.colliders[k];
+    if (!collider_in_scene(c, scene) || c.type == MPM_BC_NONE) continue;
+    if (p[0] >= c.lo[0] && p[0] <= c.hi[0] && p[1] >= c.lo[1] && p[1] <= c.hi[1] &&
+        p[2] >= c.lo[2] && p[2] <= c.hi[2])
+      return true;
+  }
+  return false;
 }
 
 }  // namespace zsmpm

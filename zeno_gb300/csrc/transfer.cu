@@ -916,13 +916,15 @@ void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
 
 // ApplyBoundaryOnZSGrid with level sets: the colliders of each node's scene,
 // after the box walls (its own pass, launched only when colliders exist)
-__global__ void k_apply_colliders(DevPtrs d) {
+// collider `id` (-1: every collider, in id order) on the active grid nodes
+__global__ void k_apply_colliders(DevPtrs d, int id) {
   const int nc = d.prm->n_colliders;
+  const int k0 = id < 0 ? 0 : id, k1 = id < 0 ? nc : min(id + 1, nc);
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
        idx += (long long)gridDim.x * blockDim.x) {
-    float4 g = d.grid[idx];
-    if (g.x == 0.0f) continue;
+    // the node's position first: only nodes in a collider's world box read
+    // the grid
     const int gdir = d.gb_dir[idx >> 6];
     const int sc = scene_of_dir(d, gdir);
     const SceneParams &S = d.scn[sc];
@@ -932,8 +934,11 @@ __global__ void k_apply_colliders(DevPtrs d) {
                       (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
                       ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
     const float p[3] = {(float)I[0] * S.dx, (float)I[1] * S.dx, (float)I[2] * S.dx};
+    if (!near_colliders(d, k0, k1, sc, p)) continue;
+    float4 g = d.grid[idx];
+    if (g.x == 0.0f) continue;
     float vel[3] = {g.y, g.z, g.w};
-    apply_colliders(d, nc, sc, p, vel);
+    apply_colliders(d, k0, k1, sc, p, vel);
     g.y = vel[0];
     g.z = vel[1];
     g.w = vel[2];
@@ -941,16 +946,25 @@ __global__ void k_apply_colliders(DevPtrs d) {
   }
 }
 
-void launch_apply_colliders(const DevPtrs &d, cudaStream_t s) {
-  k_apply_colliders<<<d.grid_stream, 256, 0, s>>>(d);
+void launch_apply_colliders(const DevPtrs &d, int id, cudaStream_t s) {
+  k_apply_colliders<<<d.grid_stream, 256, 0, s>>>(d, id);
 }
 
-__global__ void k_step_colliders(DevPtrs d, float dt) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) step_colliders(d, d.prm->n_colliders, dt);
+// StepZSBoundary on collider `id` (-1: every collider)
+__global__ void k_step_colliders(DevPtrs d, int id, float dt) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const int nc = d.prm->n_colliders;
+  for (int k = 0; k < nc; ++k) {
+    if (id >= 0 && k != id) continue;
+    ColliderDev &c = d.colliders[k];
+    for (int a = 0; a < 3; ++a) c.b[a] += c.db[a] * dt;
+    c.s += c.ds * dt;
+    collider_world_box(c);
+  }
 }
 
-void launch_step_colliders(const DevPtrs &d, float dt, cudaStream_t s) {
-  k_step_colliders<<<1, 32, 0, s>>>(d, dt);
+void launch_step_colliders(const DevPtrs &d, int id, float dt, cudaStream_t s) {
+  k_step_colliders<<<1, 32, 0, s>>>(d, id, dt);
 }
 
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {

@@ -116,7 +116,36 @@ struct ColliderDev {
   float cvel[3];    // material velocity when has_vel == 0
   const float *sdf;
   const float *vel;  // 3 planes, or null
+  float lo[3], hi[3];  // world box holding the sample grid (with a margin)
 };
+
+// world bounding box of the collider's sample grid under p = s R X + b,
+// padded so that rounding in the node test never puts a node the test
+// accepts outside it; kept current wherever b or s change
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline void collider_world_box(ColliderDev &c) {
+  float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  float big = 0.0f;
+  for (int k = 0; k < 8; ++k) {
+    float X[3];
+    for (int a = 0; a < 3; ++a)
+      X[a] = c.origin[a] + (((k >> a) & 1) ? (float)(c.dims[a] - 1) / c.inv_h : 0.0f);
+    for (int a = 0; a < 3; ++a) {
+      const float w = c.s * (c.R[a * 3 + 0] * X[0] + c.R[a * 3 + 1] * X[1] + c.R[a * 3 + 2] * X[2]) + c.b[a];
+      lo[a] = w < lo[a] ? w : lo[a];
+      hi[a] = w > hi[a] ? w : hi[a];
+      const float m = w < 0.0f ? -w : w;
+      big = m > big ? m : big;
+    }
+  }
+  const float pad = 1e-4f * (1.0f + big);
+  for (int a = 0; a < 3; ++a) {
+    c.lo[a] = lo[a] - pad;
+    c.hi[a] = hi[a] + pad;
+  }
+}
 
 // One scene of a context: its grid spacing, its slice of the concatenated
 // block directory, its boundary and gravity.  A context holds one scene
@@ -186,8 +215,8 @@ void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s);
 // gravity, bit 2: boundary (mode 0 leaves m, mv as the reference P2G does)
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s);
 // mode bit 1: momentum -> velocity + gravity, bit 2: boundary, on the grid
-void launch_step_colliders(const DevPtrs &d, float dt, cudaStream_t s);
-void launch_apply_colliders(const DevPtrs &d, cudaStream_t s);
+void launch_step_colliders(const DevPtrs &d, int id, float dt, cudaStream_t s);
+void launch_apply_colliders(const DevPtrs &d, int id, cudaStream_t s);
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s);
 // fuse_rm: return mapping in G2P; fuse_bin: bin the new positions for the
 // next partition

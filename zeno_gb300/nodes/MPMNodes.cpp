@@ -32,6 +32,9 @@ inline std::vector<vec3f> *vel(PrimitiveObject &p, bool create) {
   }
   return &p.verts.attr<vec3f>("vel");
 }
+inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::string &k) {
+  return p.verts.has_attr(k) ? &p.verts.attr<float>(k) : nullptr;
+}
 }  // namespace prim_access
 }  // namespace zeno
 #else
@@ -47,6 +50,10 @@ inline std::vector<vec3f> *vel(PrimitiveObject &p, bool create) {
     return &p.attrs3["vel"];
   }
   return &it->second;
+}
+inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::string &k) {
+  auto it = p.attrs1.find(k);
+  return it == p.attrs1.end() ? nullptr : &it->second;
 }
 }  // namespace prim_access
 }  // namespace zeno
@@ -103,15 +110,59 @@ struct ZenoGrid : IObject {
   std::shared_ptr<ZenoPartition> partition;
 };
 
-// ToZSBoundary output (Structures.hpp:807-835), analytic box collider
+// MakeZSLevelSet output (Structures.hpp: ZenoLevelSet): here a dense grid of
+// signed distances (x fastest) at origin + (i, j, k) * dx, with an optional
+// material velocity field (3 planes) or a constant velocity
+struct ZenoLevelSet : IObject {
+  float dx = 0.1f;
+  std::string transferScheme = "unknown", category = "cellcentered";
+  int dims[3] = {0, 0, 0};
+  vec3f origin{0.f, 0.f, 0.f};
+  std::vector<float> sdf;
+  std::vector<float> vel;  // empty or 3 * dims product
+  vec3f const_vel{0.f, 0.f, 0.f};
+};
+
+// ToZSBoundary output (Structures.hpp:807-835): the analytic box walls, or a
+// level-set collider with its transform (attached to a context on first use)
 struct ZenoBoundary : IObject {
   mpm_boundary bc{};
+  std::shared_ptr<ZenoLevelSet> ls;
+  mpm_collider_desc col{};
+  std::weak_ptr<MpmContext> attached;
+  int32_t collider_id = -1;
 };
 
 namespace {
 
 float get_dt(const INode &node) {
   return node.get_input<NumericObject>("dt")->get<float>();
+}
+
+// Make a boundary take effect in the context: box walls replace the
+// context's walls; a level-set collider joins the context's colliders once
+// (every boundary application then resolves the walls and all colliders,
+// each projection being idempotent).
+void attach_boundary(const std::shared_ptr<MpmContext> &ctx, ZenoBoundary &b) {
+  if (!b.ls) {
+    check(mpm_set_boundary(ctx->h, &b.bc), "mpm_set_boundary");
+    return;
+  }
+  if (b.attached.lock() == ctx) return;
+  mpm_collider_desc c = b.col;
+  const ZenoLevelSet &ls = *b.ls;
+  for (int a = 0; a < 3; ++a) {
+    c.dims[a] = ls.dims[a];
+    c.origin[a] = ls.origin[a];
+    c.const_velocity[a] = ls.const_vel[a];
+  }
+  c.spacing = ls.dx;
+  c.sdf = ls.sdf.data();
+  c.velocity = ls.vel.empty() ? nullptr : ls.vel.data();
+  int32_t id = -1;
+  check(mpm_add_collider(ctx->h, &c, &id), "mpm_add_collider");
+  b.attached = ctx;
+  b.collider_id = id;
 }
 
 std::shared_ptr<MpmContext> bound_ctx(const std::shared_ptr<ZenoPartition> &p, const char *node) {
@@ -404,26 +455,144 @@ ZENDEFNODE(UpdateZSGrid, {
                              {"MPM"},
                          });
 
-/// ToZSBoundary (Generation.cu:1597-1647).  The level-set collider input
-/// (ZSLevelSet) is replaced by the analytic walls of the domain box
-/// [domain_min, domain_max] (node indices from world coordinates / dx), of
-/// `thickness` cells; translation / rotation of the collider are not
-/// supported (the walls are static).
+/// MakeZSLevelSet (Generation.cu:1521-1595).  The reference makes an empty
+/// sparse level set that VDB conversions fill; here the level set is a dense
+/// grid of spacing dx, filled from `sdf_prim` (vertices on a regular grid of
+/// `dims` samples, x fastest, float attribute "sdf", optional vec3
+/// attribute "vel") or from an analytic `shape` (sphere of `radius` around
+/// `center`; half-space y < `height` over `center` +- `extent`).  For the
+/// category const_velocity, `aux` is the collider's material velocity.
+struct MakeZSLevelSet : INode {
+  void apply() override {
+    auto ls = std::make_shared<ZenoLevelSet>();
+    ls->dx = get_input2<float>("dx");
+    ls->transferScheme = get_input2<std::string>("transfer");
+    ls->category = get_input2<std::string>("category");
+    const std::string &ts = ls->transferScheme;
+    if (ts != "unknown" && ts != "apic" && ts != "flip" && ts != "aflip" && ts != "boundary")
+      throw std::runtime_error("MakeZSLevelSet: unrecognized transfer scheme [" + ts + "]");
+    const std::string &cat = ls->category;
+    if (cat != "cellcentered" && cat != "collocated" && cat != "staggered" && cat != "const_velocity")
+      throw std::runtime_error("MakeZSLevelSet: unknown levelset (grid) category [" + cat + "]");
+    if (!(ls->dx > 0.f)) throw std::runtime_error("MakeZSLevelSet: dx must be positive");
+    if (cat == "const_velocity" && has_input<NumericObject>("aux"))
+      ls->const_vel = get_input<NumericObject>("aux")->get<vec3f>();
+    const float h = ls->dx;
+    if (has_input<PrimitiveObject>("sdf_prim")) {
+      auto prim = get_input<PrimitiveObject>("sdf_prim");
+      const vec3f d = get_input<NumericObject>("dims")->get<vec3f>();
+      long long cells = 1;
+      for (int a = 0; a < 3; ++a) {
+        ls->dims[a] = (int)std::lround(d[a]);
+        if (ls->dims[a] < 2) throw std::runtime_error("MakeZSLevelSet: dims must be >= 2");
+        cells *= ls->dims[a];
+      }
+      const auto &pos = prim_access::pos(*prim);
+      const auto *sdf = prim_access::float_attr(*prim, "sdf");
+      if (!sdf || (long long)sdf->size() != cells || (long long)pos.size() != cells)
+        throw std::runtime_error("MakeZSLevelSet: sdf_prim needs dims[0]*dims[1]*dims[2] "
+                                 "vertices with a float attribute \"sdf\"");
+      ls->origin = pos[0];
+      ls->sdf = *sdf;
+      if (auto *v = prim_access::vel(*prim, false); v && (long long)v->size() == cells) {
+        ls->vel.resize(3 * cells);
+        for (long long i = 0; i < cells; ++i)
+          for (int a = 0; a < 3; ++a) ls->vel[a * cells + i] = (*v)[i][a];
+      }
+    } else {
+      const std::string shape = get_input2<std::string>("shape");
+      vec3f c{0.f, 0.f, 0.f};
+      if (has_input<NumericObject>("center")) c = get_input<NumericObject>("center")->get<vec3f>();
+      float half = 0.f;
+      if (shape == "sphere")
+        half = get_input2<float>("radius") + 3.f * h;
+      else if (shape == "plane")
+        half = get_input2<float>("extent");
+      else
+        throw std::runtime_error("MakeZSLevelSet: give sdf_prim or an analytic shape "
+                                 "(sphere, plane)");
+      const int n = (int)std::ceil(half / h);
+      for (int a = 0; a < 3; ++a) {
+        ls->dims[a] = 2 * n + 1;
+        ls->origin[a] = c[a] - n * h;
+      }
+      const float r = get_input2<float>("radius"), y0 = get_input2<float>("height");
+      const int m = 2 * n + 1;
+      ls->sdf.resize((size_t)m * m * m);
+      for (int k = 0; k < m; ++k)
+        for (int j = 0; j < m; ++j)
+          for (int i = 0; i < m; ++i) {
+            const float p[3] = {ls->origin[0] + i * h, ls->origin[1] + j * h, ls->origin[2] + k * h};
+            float v;
+            if (shape == "sphere")
+              v = std::sqrt((p[0] - c[0]) * (p[0] - c[0]) + (p[1] - c[1]) * (p[1] - c[1]) +
+                            (p[2] - c[2]) * (p[2] - c[2])) - r;
+            else
+              v = p[1] - y0;
+            ls->sdf[((size_t)k * m + j) * m + i] = v;
+          }
+    }
+    set_output("ZSLevelSet", std::move(ls));
+  }
+};
+ZENDEFNODE(MakeZSLevelSet, {
+                               {{"float", "dx", "0.1"},
+                                "aux",
+                                {"enum unknown apic flip aflip boundary", "transfer", "unknown"},
+                                {"enum cellcentered collocated staggered const_velocity",
+                                 "category", "cellcentered"},
+                                "sdf_prim",
+                                "dims",
+                                {"enum none sphere plane", "shape", "none"},
+                                "center",
+                                {"float", "radius", "0.1"},
+                                {"float", "height", "0"},
+                                {"float", "extent", "0.5"}},
+                               {"ZSLevelSet"},
+                               {},
+                               {"SOP"},
+                           });
+
+/// ToZSBoundary (Generation.cu:1597-1647).  With a ZSLevelSet input the
+/// boundary is that level-set collider under translation (+ rate), scale
+/// (+ rate) and yaw-pitch-roll angles in degrees, attached to the context
+/// by the first ApplyBoundaryOnZSGrid that uses it.  Without one, the
+/// boundary is the analytic walls of the domain box [domain_min,
+/// domain_max] (node indices from world coordinates / dx), `thickness`
+/// cells thick (the additive inputs).
 struct ToZSBoundary : INode {
   void apply() override {
-    if (has_input("ZSLevelSet"))
-      throw std::runtime_error("level-set colliders are not supported by this backend; "
-                               "use the analytic box walls (domain_min / domain_max)");
     auto b = std::make_shared<ZenoBoundary>();
     const std::string type = get_input2<std::string>("type");
-    if (type == "sticky" || type == "Sticky")
-      b->bc.type = MPM_BC_STICKY;
-    else if (type == "slip" || type == "Slip")
-      b->bc.type = MPM_BC_SLIP;
+    int t = MPM_BC_STICKY;  // the reference's fallback (Generation.cu:1611)
+    if (type == "slip" || type == "Slip")
+      t = MPM_BC_SLIP;
     else if (type == "separate" || type == "Separate")
-      b->bc.type = MPM_BC_SEPARATE;
-    else
-      b->bc.type = MPM_BC_STICKY;  // the reference's fallback (Generation.cu:1611)
+      t = MPM_BC_SEPARATE;
+    if (has_input<ZenoLevelSet>("ZSLevelSet")) {
+      b->ls = get_input<ZenoLevelSet>("ZSLevelSet");
+      mpm_collider_desc &c = b->col;
+      c = mpm_collider_desc{};
+      c.type = t;
+      c.scene = -1;
+      c.scale = 1.0f;
+      auto vec = [&](const char *k, float (&dst)[3]) {
+        if (has_input<NumericObject>(k)) {
+          const vec3f v = get_input<NumericObject>(k)->get<vec3f>();
+          for (int a = 0; a < 3; ++a) dst[a] = v[a];
+        }
+      };
+      vec("translation", c.translation);
+      vec("translation_rate", c.translation_rate);
+      vec("ypr_angles", c.ypr_deg);
+      if (has_input<NumericObject>("scale")) c.scale = get_input<NumericObject>("scale")->get<float>();
+      if (has_input<NumericObject>("scale_rate"))
+        c.scale_rate = get_input<NumericObject>("scale_rate")->get<float>();
+      b->bc.type = MPM_BC_NONE;
+      set_output("ZSBoundary", b);
+      return;
+    }
+    b->bc.type = t;
     b->bc.thickness = get_input2<int>("thickness");
     const float dx = get_input2<float>("dx");
     vec3f lo{0.f, 0.f, 0.f}, hi{1.f, 1.f, 1.f};
@@ -461,8 +630,12 @@ struct ApplyBoundaryOnZSGrid : INode {
       auto table = get_input<ZenoPartition>("ZSPartition");
       auto ctx = bound_ctx(table, "ApplyBoundaryOnZSGrid");
       auto b = get_input<ZenoBoundary>("ZSBoundary");
-      check(mpm_set_boundary(ctx->h, &b->bc), "mpm_set_boundary");
-      check(mpm_apply_boundary(ctx->h), "mpm_apply_boundary");
+      attach_boundary(ctx, *b);
+      // this boundary only: the walls, or this level set's collider
+      if (b->ls)
+        check(mpm_apply_collider(ctx->h, b->collider_id), "mpm_apply_collider");
+      else
+        check(mpm_apply_walls(ctx->h), "mpm_apply_walls");
     }
     set_output("ZSGrid", grid);
   }
@@ -473,6 +646,26 @@ ZENDEFNODE(ApplyBoundaryOnZSGrid, {
                                       {},
                                       {"MPM"},
                                   });
+
+/// StepZSBoundary (Generation.cu:1662-1685): b += db/dt dt, s += ds/dt dt,
+/// on the boundary and, once attached, on its collider in the context
+struct StepZSBoundary : INode {
+  void apply() override {
+    auto b = get_input<ZenoBoundary>("ZSBoundary");
+    const float dt = get_input2<float>("dt");
+    b->col.scale += b->col.scale_rate * dt;
+    for (int a = 0; a < 3; ++a) b->col.translation[a] += b->col.translation_rate[a] * dt;
+    if (auto ctx = b->attached.lock(); ctx && b->collider_id >= 0)
+      check(mpm_step_colliders(ctx->h, b->collider_id, dt), "mpm_step_colliders");
+    set_output("ZSBoundary", b);
+  }
+};
+ZENDEFNODE(StepZSBoundary, {
+                               {"ZSBoundary", {"float", "dt", "0"}},
+                               {"ZSBoundary"},
+                               {},
+                               {"MPM"},
+                           });
 
 /// ZSGridToZSParticle (Transfer.cu:1069-1173), APIC transfer
 struct ZSGridToZSParticle : INode {
@@ -624,8 +817,11 @@ struct ZSMPMSubstep : INode {
     }
     check(mpm_set_gravity(ctx->h, acc[0], acc[1], acc[2]), "mpm_set_gravity");
     if (has_input<ZenoBoundary>("ZSBoundary"))
-      check(mpm_set_boundary(ctx->h, &get_input<ZenoBoundary>("ZSBoundary")->bc),
-            "mpm_set_boundary");
+      attach_boundary(ctx, *get_input<ZenoBoundary>("ZSBoundary"));
+    // a level-set collider after the walls; the substeps advance it on the
+    // device (b += db/dt dt, s += ds/dt dt at the start of each substep)
+    if (has_input<ZenoBoundary>("ZSCollider"))
+      attach_boundary(ctx, *get_input<ZenoBoundary>("ZSCollider"));
     check(mpm_substep(ctx->h, get_dt(*this), get_input2<int>("substeps")), "mpm_substep");
     mpm_stats st{};
     check(mpm_get_stats(ctx->h, &st), "mpm_get_stats");
@@ -637,6 +833,7 @@ struct ZSMPMSubstep : INode {
 ZENDEFNODE(ZSMPMSubstep, {
                              {"ZSParticles",
                               "ZSBoundary",
+                              "ZSCollider",
                               "dt",
                               {"float", "gravity", "-9.8"},
                               "Accel",

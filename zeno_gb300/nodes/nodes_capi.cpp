@@ -78,7 +78,8 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       const char *type, const char *plasticity, float E, float nu,
                       float density, float ppc, const char *bc_type, int32_t bc_thickness,
                       float dt, float gravity, int32_t substeps, float *out_x, float *out_v,
-                      float *out_max_vel_sqr, char *err, int64_t err_cap) {
+                      float *out_max_vel_sqr, char *err, int64_t err_cap,
+                      const char *ls_shape, const float *ls, const char *ls_type) {
   using namespace zeno;
   try {
     Graph g;
@@ -115,12 +116,36 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
     g.setNodeInput("bnd", "dx", num(dx));
     g.setNodeInput("bnd", "thickness", inum(bc_thickness));
     for (const char *id : {"model", "pars", "table", "grid", "bnd"}) g.markOnce(id);
+    // optional level-set collider: ls = {dx, center[3], radius, height, extent,
+    // translation[3], translation_rate[3], scale, scale_rate, ypr[3]}
+    const bool collider = ls_shape && ls && std::string(ls_shape) != "none";
+    if (collider) {
+      auto v3 = [](const float *a) { return std::make_shared<NumericObject>(vec3f{a[0], a[1], a[2]}); };
+      g.addNode("MakeZSLevelSet", "ls");
+      g.setNodeInput("ls", "dx", num(ls[0]));
+      g.setNodeInput("ls", "shape", str(ls_shape));
+      g.setNodeInput("ls", "center", v3(ls + 1));
+      g.setNodeInput("ls", "radius", num(ls[4]));
+      g.setNodeInput("ls", "height", num(ls[5]));
+      g.setNodeInput("ls", "extent", num(ls[6]));
+      g.addNode("ToZSBoundary", "lsb");
+      g.bindNodeInput("lsb", "ZSLevelSet", "ls", "ZSLevelSet");
+      g.setNodeInput("lsb", "translation", v3(ls + 7));
+      g.setNodeInput("lsb", "translation_rate", v3(ls + 10));
+      g.setNodeInput("lsb", "scale", num(ls[13]));
+      g.setNodeInput("lsb", "scale_rate", num(ls[14]));
+      g.setNodeInput("lsb", "ypr_angles", v3(ls + 15));
+      g.setNodeInput("lsb", "type", str(ls_type ? ls_type : "sticky"));
+      g.markOnce("ls");
+      g.markOnce("lsb");
+    }
     auto dtobj = num(dt);
     std::string last;
     if (fused) {
       g.addNode("ZSMPMSubstep", "step");
       g.bindNodeInput("step", "ZSParticles", "pars", "ZSParticles");
       g.bindNodeInput("step", "ZSBoundary", "bnd", "ZSBoundary");
+      if (collider) g.bindNodeInput("step", "ZSCollider", "lsb", "ZSBoundary");
       g.setNodeInput("step", "dt", dtobj);
       g.setNodeInput("step", "gravity", num(gravity));
       g.setNodeInput("step", "substeps", inum(substeps));
@@ -150,8 +175,20 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("bc", "ZSPartition", "expand", "ZSPartition");
       g.bindNodeInput("bc", "ZSGrid", "update", "ZSGrid");
       g.bindNodeInput("bc", "ZSBoundary", "bnd", "ZSBoundary");
+      const char *grid_src = "bc";
+      if (collider) {
+        // StepZSBoundary then the collider, after the walls, every substep
+        g.addNode("StepZSBoundary", "stepb");
+        g.bindNodeInput("stepb", "ZSBoundary", "lsb", "ZSBoundary");
+        g.setNodeInput("stepb", "dt", dtobj);
+        g.addNode("ApplyBoundaryOnZSGrid", "bc2");
+        g.bindNodeInput("bc2", "ZSPartition", "expand", "ZSPartition");
+        g.bindNodeInput("bc2", "ZSGrid", "bc", "ZSGrid");
+        g.bindNodeInput("bc2", "ZSBoundary", "stepb", "ZSBoundary");
+        grid_src = "bc2";
+      }
       g.addNode("ZSGridToZSParticle", "g2p");
-      g.bindNodeInput("g2p", "ZSGrid", "bc", "ZSGrid");
+      g.bindNodeInput("g2p", "ZSGrid", grid_src, "ZSGrid");
       g.bindNodeInput("g2p", "ZSPartition", "expand", "ZSPartition");
       g.bindNodeInput("g2p", "ZSParticles", "pars", "ZSParticles");
       g.setNodeInput("g2p", "dt", dtobj);

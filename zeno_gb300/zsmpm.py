@@ -74,7 +74,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_batch_create", "mpm_batch_upload",
            "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
            "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
-           "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_g2p", "mpm_return_mapping",
+           "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_apply_walls",
+           "mpm_apply_collider", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
@@ -111,7 +112,7 @@ def load(path: str = LIB_PATH):
         "mpm_set_gravity": ([P, f32, f32, f32], i32),
         "mpm_add_collider": ([P, P, P], i32),
         "mpm_clear_colliders": ([P], i32),
-        "mpm_step_colliders": ([P, f32], i32),
+        "mpm_step_colliders": ([P, i32, f32], i32),
         "mpm_particles_upload": ([P, i64] + [P] * 10, i32),
         "mpm_particles_set_lame": ([P, P, P], i32),
         "mpm_particles_download": ([P] + [P] * 5, i32),
@@ -120,6 +121,8 @@ def load(path: str = LIB_PATH):
         "mpm_p2g": ([P, f32], i32),
         "mpm_grid_update": ([P, f32, P], i32),
         "mpm_apply_boundary": ([P], i32),
+        "mpm_apply_walls": ([P], i32),
+        "mpm_apply_collider": ([P, i32], i32),
         "mpm_g2p": ([P, f32], i32),
         "mpm_return_mapping": ([P], i32),
         "mpm_substep": ([P, f32, i32], i32),
@@ -196,9 +199,11 @@ class Context:
     def clear_colliders(self):
         self._check(self._L.mpm_clear_colliders(self.h), "mpm_clear_colliders")
 
-    def step_colliders(self, dt: float):
-        """StepZSBoundary: b += db/dt dt, s += ds/dt dt (stage path)."""
-        self._check(self._L.mpm_step_colliders(self.h, float(dt)), "mpm_step_colliders")
+    def step_colliders(self, dt: float, collider: int = -1):
+        """StepZSBoundary: b += db/dt dt, s += ds/dt dt (stage path), for one
+        collider or (-1) every collider."""
+        self._check(self._L.mpm_step_colliders(self.h, int(collider), float(dt)),
+                    "mpm_step_colliders")
 
     @property
     def dir_size(self) -> int:
@@ -310,6 +315,12 @@ class Context:
 
     def apply_boundary(self):
         self._check(self._L.mpm_apply_boundary(self.h), "mpm_apply_boundary")
+
+    def apply_walls(self):
+        self._check(self._L.mpm_apply_walls(self.h), "mpm_apply_walls")
+
+    def apply_collider(self, collider=-1):
+        self._check(self._L.mpm_apply_collider(self.h, collider), "mpm_apply_collider")
 
     def g2p(self, dt):
         self._check(self._L.mpm_g2p(self.h, dt), "mpm_g2p")
@@ -490,7 +501,7 @@ def load_nodes(path: str = NODES_LIB_PATH):
     L.zsn_run_graph.argtypes = [C.c_int32, C.c_int64, P, P, C.c_float, C.c_char_p, C.c_char_p,
                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_char_p,
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
-                                C.c_char_p, C.c_int64]
+                                C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -511,8 +522,14 @@ def node_descriptors() -> dict:
 
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
-                   fused=False):
-    """Run the zeno MPM substep graph headless through the C++ node layer."""
+                   fused=False, levelset=None):
+    """Run the zeno MPM substep graph headless through the C++ node layer.
+    levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
+    applied after the walls -- in the stage graph through StepZSBoundary and a
+    second ApplyBoundaryOnZSGrid every substep, in the fused graph as
+    ZSMPMSubstep's ZSCollider: shape ("sphere" | "plane"), dx, center,
+    radius, height, extent, translation, translation_rate, scale, scale_rate,
+    ypr, type."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -521,9 +538,21 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     ov = np.zeros_like(x)
     vmax = np.zeros(1, np.float32)
     err = C.create_string_buffer(1024)
+    shape, lsp, lst = None, None, None
+    if levelset:
+        ls = levelset
+        vals = ([ls.get("dx", 1.0 / 64)] + list(ls.get("center", (0.0, 0.0, 0.0))) +
+                [ls.get("radius", 0.1), ls.get("height", 0.0), ls.get("extent", 0.5)] +
+                list(ls.get("translation", (0.0, 0.0, 0.0))) +
+                list(ls.get("translation_rate", (0.0, 0.0, 0.0))) +
+                [ls.get("scale", 1.0), ls.get("scale_rate", 0.0)] + list(ls.get("ypr", (0.0, 0.0, 0.0))))
+        lsp = np.asarray(vals, np.float32)
+        shape = ls["shape"].encode()
+        lst = ls.get("type", "sticky").encode()
     rc = L.zsn_run_graph(1 if fused else 0, n, _p(x), _p(v), dx, type.encode(),
                          plasticity.encode(), E, nu, density, ppc, bc.encode(), thickness, dt,
-                         gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024)
+                         gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024, shape,
+                         _p(lsp) if lsp is not None else None, lst)
     if rc != 0:
         raise RuntimeError(err.value.decode())
     return ox, ov, float(vmax[0])
