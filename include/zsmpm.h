@@ -56,6 +56,8 @@ enum { MPM_FCR = 0, MPM_NHK = 1, MPM_STVK = 2, MPM_EOS = 3 };
 enum { MPM_PLASTIC_NONE = 0, MPM_PLASTIC_NADP = 1 };
 /* collider types: ToZSBoundary "type" (Generation.cu:1601-1611) */
 enum { MPM_BC_NONE = 0, MPM_BC_STICKY = 1, MPM_BC_SLIP = 2, MPM_BC_SEPARATE = 3 };
+/* grid transfer schemes: MakeZSGrid "transfer" (Generation.cu:1493-1504) */
+enum { MPM_TRANSFER_APIC = 0, MPM_TRANSFER_FLIP = 1, MPM_TRANSFER_AFLIP = 2 };
 
 /* Material of ConfigConstitutiveModel (Generation.cu:18-103): E, nu ->
  * Lame parameters; Drucker-Prager friction angle in degrees; bulk modulus
@@ -200,6 +202,23 @@ int32_t mpm_particles_set_lame(mpm_ctx *ctx, const float *mu, const float *lam);
 /* UpdatePrimitiveFromZSParticles (Generation.cu:1088-1158): device store ->
  * host arrays in the upload order; NULL skips a channel. */
 int32_t mpm_particles_download(mpm_ctx *ctx, float *x, float *v, float *C, float *F, float *J);
+/* One per-particle attribute in the upload order, by its channel name in the
+ * reference's particle store (Generation.cpp:868-903): get "beta", "m",
+ * "vol", "J", "mu", "lam"; set "beta" (host arrays of n floats). */
+int32_t mpm_particles_get_attr(mpm_ctx *ctx, const char *name, float *values);
+int32_t mpm_particles_set_attr(mpm_ctx *ctx, const char *name, const float *values);
+
+/* MakeZSGrid "transfer" of the context's grid: MPM_TRANSFER_APIC (default),
+ * MPM_TRANSFER_FLIP or MPM_TRANSFER_AFLIP (the grid gains the vstar channel,
+ * Generation.cu:1495-1500; P2G Transfer.cu:891-984, grid update
+ * MPMPipeline.cu:878-897, boundary on vstar Boundary.cu:90-101, G2P
+ * Transfer.cu:1174-1257).  Allocates the vstar grid on first use. */
+int32_t mpm_set_transfer(mpm_ctx *ctx, int32_t scheme);
+/* ComputeParticleBeta (Boundary.cu:172-516) on the current particles: with
+ * collider = -1 beta = 0.5 where det F > 1 (J for the equation-of-state
+ * fluid), else 0; with a collider id, first beta = 0 for particles that at
+ * x + dt v are inside that collider and move into it. */
+int32_t mpm_compute_particle_beta(mpm_ctx *ctx, float dt, int32_t collider);
 
 /* Stage entry points (one reference node each). */
 int32_t mpm_partition(mpm_ctx *ctx);

@@ -17,6 +17,10 @@
 //   APIC G2P           projects/CuLagrange/mpm/Transfer.cu:1139-1173
 //   return mapping     projects/CuLagrange/mpm/MPMPipeline.cu:958-971
 //   particle init      projects/CuLagrange/mpm/Generation.cpp:944-966
+//   FLIP / AFLIP P2G   projects/CuLagrange/mpm/Transfer.cu:891-984
+//   FLIP grid update   projects/CuLagrange/mpm/MPMPipeline.cu:878-897
+//   FLIP / AFLIP G2P   projects/CuLagrange/mpm/Transfer.cu:1174-1257
+//   particle beta      projects/CuLagrange/mpm/Boundary.cu:172-516
 // zpc (which holds the arithmetic) is absent; each restated formula below
 // names the published method it follows.
 #include "mpm_oracle.h"
@@ -373,7 +377,10 @@ template <class R> struct Sim {
   std::vector<Params<R>> mats;
   int nthreads;
   Partition P;
-  std::vector<R> grid;  // [gb][64][4] = m, mv (then v)
+  // [gb][64][kNG] = m, mv (then v), and for the FLIP transfers vstar: the
+  // momentum change of the grid forces (then the updated velocity)
+  static constexpr int kNG = 7;
+  std::vector<R> grid;
   R max_vel_sqr = 0;
 
   Sim(const orc_scene &s, int nt) : sc(s), nthreads(nt) {
@@ -422,73 +429,79 @@ template <class R> struct Sim {
     }
   }
 
-  // The level-set colliders on the velocity of the node at index I, in order
-  // (ApplyBoundaryOnZSGrid with a level set, Boundary.cu:83-163): trilinear
-  // signed distance and its gradient at X = R^T (p - b) / s, p = I dx; inside
-  // when negative; collider velocity R v(X) + db/dt (Boundary.cu:299-301);
+  // Level-set collider `cl` at world position p (ApplyBoundaryOnZSGrid with a
+  // level set, Boundary.cu:83-163): trilinear signed distance and its gradient
+  // at X = R^T (p - b) / s; inside when negative; unit normal R grad phi /
+  // |R grad phi|, collider velocity R v(X) + db/dt (Boundary.cu:299-301).
+  // False outside the sample grid or outside the collider.
+  bool collider_hit(const Col &cl, const R *p, R *nrm, R *vo) const {
+    const orc_collider &c = *cl.c;
+    R q[3], X[3], u[3], t[3];
+    int64_t i0[3];
+    for (int a = 0; a < 3; ++a) q[a] = (p[a] - cl.b[a]) / cl.s;
+    for (int a = 0; a < 3; ++a) X[a] = cl.Rm[0 * 3 + a] * q[0] + cl.Rm[1 * 3 + a] * q[1] + cl.Rm[2 * 3 + a] * q[2];
+    for (int a = 0; a < 3; ++a) {
+      u[a] = (X[a] - R(c.origin[a])) / R(c.spacing);
+      if (!(u[a] >= 0 && u[a] <= R(c.dims[a] - 1))) return false;
+    }
+    for (int a = 0; a < 3; ++a) {
+      i0[a] = std::min<int64_t>(int64_t(std::floor(u[a])), c.dims[a] - 2);
+      t[a] = u[a] - R(i0[a]);
+    }
+    const int64_t sx = 1, sy = c.dims[0], sz = int64_t(c.dims[0]) * c.dims[1];
+    auto at = [&](const float *g, int dx, int dy, int dz) {
+      return R(g[(i0[0] + dx) * sx + (i0[1] + dy) * sy + (i0[2] + dz) * sz]);
+    };
+    auto tri = [&](const float *g, R *grad) {
+      R val = 0;
+      if (grad) grad[0] = grad[1] = grad[2] = 0;
+      for (int k = 0; k < 8; ++k) {
+        const int bx = (k >> 2) & 1, by = (k >> 1) & 1, bz = k & 1;
+        const R wx = bx ? t[0] : R(1) - t[0], wy = by ? t[1] : R(1) - t[1],
+                wz = bz ? t[2] : R(1) - t[2];
+        const R f = at(g, bx, by, bz);
+        val += wx * wy * wz * f;
+        if (grad) {
+          grad[0] += (bx ? R(1) : R(-1)) * wy * wz * f;
+          grad[1] += wx * (by ? R(1) : R(-1)) * wz * f;
+          grad[2] += wx * wy * (bz ? R(1) : R(-1)) * f;
+        }
+      }
+      return val;
+    };
+    R g[3];
+    const R phi = tri(c.sdf, g);
+    if (!(phi < 0)) return false;
+    R nr[3];
+    for (int a = 0; a < 3; ++a) nr[a] = cl.Rm[a * 3 + 0] * g[0] + cl.Rm[a * 3 + 1] * g[1] + cl.Rm[a * 3 + 2] * g[2];
+    const R nn = std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
+    const R rn = nn > 0 ? R(1) / nn : R(0);
+    for (int a = 0; a < 3; ++a) nrm[a] = nr[a] * rn;
+    R vl[3] = {R(c.const_velocity[0]), R(c.const_velocity[1]), R(c.const_velocity[2])};
+    if (c.velocity) {
+      const int64_t plane = sz * c.dims[2];
+      for (int a = 0; a < 3; ++a) vl[a] = tri(c.velocity + a * plane, nullptr);
+    }
+    for (int a = 0; a < 3; ++a)
+      vo[a] = cl.Rm[a * 3 + 0] * vl[0] + cl.Rm[a * 3 + 1] * vl[1] + cl.Rm[a * 3 + 2] * vl[2] +
+              R(c.translation_rate[a]);
+    return true;
+  }
+
+  // The level-set colliders on the velocity of the node at index I, in order;
   // sticky / slip / separate as ApplyGridBoundaryOnZSGrid (Boundary.cu:56-67).
   void apply_colliders(const int32_t *I, R *vel) const {
+    R p[3];
+    for (int a = 0; a < 3; ++a) p[a] = R(I[a]) * R(sc.dx);
     for (const Col &cl : cols) {
-      const orc_collider &c = *cl.c;
-      R p[3], q[3], X[3], u[3], t[3];
-      int64_t i0[3];
-      bool outside = false;
-      for (int a = 0; a < 3; ++a) p[a] = R(I[a]) * R(sc.dx);
-      for (int a = 0; a < 3; ++a) q[a] = (p[a] - cl.b[a]) / cl.s;
-      for (int a = 0; a < 3; ++a) X[a] = cl.Rm[0 * 3 + a] * q[0] + cl.Rm[1 * 3 + a] * q[1] + cl.Rm[2 * 3 + a] * q[2];
-      for (int a = 0; a < 3; ++a) {
-        u[a] = (X[a] - R(c.origin[a])) / R(c.spacing);
-        if (!(u[a] >= 0 && u[a] <= R(c.dims[a] - 1))) outside = true;
-      }
-      if (outside) continue;
-      for (int a = 0; a < 3; ++a) {
-        i0[a] = std::min<int64_t>(int64_t(std::floor(u[a])), c.dims[a] - 2);
-        t[a] = u[a] - R(i0[a]);
-      }
-      const int64_t sx = 1, sy = c.dims[0], sz = int64_t(c.dims[0]) * c.dims[1];
-      auto at = [&](const float *g, int dx, int dy, int dz) {
-        return R(g[(i0[0] + dx) * sx + (i0[1] + dy) * sy + (i0[2] + dz) * sz]);
-      };
-      auto tri = [&](const float *g, R *grad) {
-        R val = 0;
-        if (grad) grad[0] = grad[1] = grad[2] = 0;
-        for (int k = 0; k < 8; ++k) {
-          const int bx = (k >> 2) & 1, by = (k >> 1) & 1, bz = k & 1;
-          const R wx = bx ? t[0] : R(1) - t[0], wy = by ? t[1] : R(1) - t[1],
-                  wz = bz ? t[2] : R(1) - t[2];
-          const R f = at(g, bx, by, bz);
-          val += wx * wy * wz * f;
-          if (grad) {
-            grad[0] += (bx ? R(1) : R(-1)) * wy * wz * f;
-            grad[1] += wx * (by ? R(1) : R(-1)) * wz * f;
-            grad[2] += wx * wy * (bz ? R(1) : R(-1)) * f;
-          }
-        }
-        return val;
-      };
-      R g[3];
-      const R phi = tri(c.sdf, g);
-      if (!(phi < 0)) continue;
-      R nr[3];
-      for (int a = 0; a < 3; ++a) nr[a] = cl.Rm[a * 3 + 0] * g[0] + cl.Rm[a * 3 + 1] * g[1] + cl.Rm[a * 3 + 2] * g[2];
-      const R nn = std::sqrt(nr[0] * nr[0] + nr[1] * nr[1] + nr[2] * nr[2]);
-      const R rn = nn > 0 ? R(1) / nn : R(0);
-      R nrm[3] = {nr[0] * rn, nr[1] * rn, nr[2] * rn};
-      R vl[3] = {R(c.const_velocity[0]), R(c.const_velocity[1]), R(c.const_velocity[2])};
-      if (c.velocity) {
-        const int64_t plane = sz * c.dims[2];
-        for (int a = 0; a < 3; ++a) vl[a] = tri(c.velocity + a * plane, nullptr);
-      }
-      R vo[3];
-      for (int a = 0; a < 3; ++a)
-        vo[a] = cl.Rm[a * 3 + 0] * vl[0] + cl.Rm[a * 3 + 1] * vl[1] + cl.Rm[a * 3 + 2] * vl[2] +
-                R(c.translation_rate[a]);
-      if (c.type == ORC_BC_STICKY) {
+      R nrm[3], vo[3];
+      if (!collider_hit(cl, p, nrm, vo)) continue;
+      if (cl.c->type == ORC_BC_STICKY) {
         for (int a = 0; a < 3; ++a) vel[a] = vo[a];
         continue;
       }
       const R proj = nrm[0] * (vel[0] - vo[0]) + nrm[1] * (vel[1] - vo[1]) + nrm[2] * (vel[2] - vo[2]);
-      if (c.type == ORC_BC_SLIP || (c.type == ORC_BC_SEPARATE && proj < 0))
+      if (cl.c->type == ORC_BC_SLIP || (cl.c->type == ORC_BC_SEPARATE && proj < 0))
         for (int a = 0; a < 3; ++a) vel[a] -= proj * nrm[a];
     }
   }
@@ -496,10 +509,13 @@ template <class R> struct Sim {
   // Quadratic B-spline stencil (Hu et al. 2018 MLS-MPM; Jiang et al. 2016
   // course notes): f = x/dx - base in [0.5, 1.5),
   // w0 = (1.5-f)^2/2, w1 = 3/4 - (f-1)^2, w2 = (f-0.5)^2/2.
+  // dw[d][o] = d w_o / d f, the derivative with respect to the particle's
+  // position in cells: w0' = f - 3/2, w1' = -2 (f - 1), w2' = f - 1/2.
   struct Stencil {
     int32_t base[3];
     R fx[3];
     R w[3][3];
+    R dw[3][3];
   };
   void stencil(const R *x, Stencil &st) const {
     const R inv_dx = R(1) / R(sc.dx);
@@ -510,6 +526,9 @@ template <class R> struct Sim {
       st.w[d][0] = R(0.5) * (R(1.5) - f) * (R(1.5) - f);
       st.w[d][1] = R(0.75) - (f - R(1)) * (f - R(1));
       st.w[d][2] = R(0.5) * (f - R(0.5)) * (f - R(0.5));
+      st.dw[d][0] = f - R(1.5);
+      st.dw[d][1] = R(-2) * (f - R(1));
+      st.dw[d][2] = f - R(0.5);
     }
   }
   R *node(const int32_t *I) {
@@ -517,16 +536,17 @@ template <class R> struct Sim {
     for (int d = 0; d < 3; ++d) bc[d] = (I[d] >> 2) - dir.lo[d];
     const int32_t gb = P.dir2gb[dir.index(bc)];
     const int cell = ((I[0] & 3) << 4) | ((I[1] & 3) << 2) | (I[2] & 3);
-    return &grid[(int64_t(gb) * 64 + cell) * 4];
+    return &grid[(int64_t(gb) * 64 + cell) * kNG];
   }
 
   int substep(int64_t n, R *x, R *v, R *C, R *F, R *J, const R *m, const R *vol,
-              const int32_t *mat, const R *mu, const R *lam, R dt) {
+              const int32_t *mat, const R *mu, const R *lam, const R *beta, R dt) {
+    const int tr = sc.transfer;
     if (sc.collider_autostep) step_colliders(dt);  // the fused substep's collider time
     int rc = build_partition<R>(sc, n, x, P, nthreads);
     if (rc) return rc;
     // ZSGridFromZSPartition: zero every channel of every block
-    grid.assign(P.gb_dir.size() * 64 * 4, R(0));
+    grid.assign(P.gb_dir.size() * 64 * kNG, R(0));
 
     const R dx = R(sc.dx), inv_dx = R(1) / dx;
     const R Dinv = R(4) * inv_dx * inv_dx;
@@ -545,14 +565,19 @@ template <class R> struct Sim {
         for (int64_t s = P.pb_start[b]; s < P.pb_start[b] + P.pb_count[b]; ++s) {
           const int64_t p = P.perm[s];
           Params<R> mp = mats[mat[p]];
-          if (mu && lam) {  // per-particle override (Transfer.cu:861-864)
+          // per-particle override (Transfer.cu:861-864, 950-953); the FLIP
+          // P2G has none (Transfer.cu:897-907)
+          if (mu && lam && tr != ORC_TRANSFER_FLIP) {
             mp.mu = mu[p];
             mp.lam = lam[p];
           }
           R tau[9];
           if (!kirchhoff(mp, F + 9 * p, J[p], tau)) bad |= 1;
+          // contrib = -dt Dinv vol P F^T (APIC, AFLIP), -dt vol P F^T (FLIP,
+          // which contracts it with the weight gradient instead)
           R contrib[9];
-          for (int i = 0; i < 9; ++i) contrib[i] = -dt * Dinv * vol[p] * tau[i];
+          const R kc = tr == ORC_TRANSFER_FLIP ? -dt * vol[p] : -dt * Dinv * vol[p];
+          for (int i = 0; i < 9; ++i) contrib[i] = kc * tau[i];
           Stencil st;
           stencil(x + 3 * p, st);
           const R *Cp = C + 9 * p, *vp = v + 3 * p;
@@ -566,12 +591,31 @@ template <class R> struct Sim {
                 const R W = st.w[0][i] * st.w[1][j] * st.w[2][k];
                 R *g = node(I);
                 g[0] += mass * W;
+                if (tr == ORC_TRANSFER_FLIP) {
+                  // Transfer.cu:924-934: v += W m v_p, vstar += W (contrib grad W)
+                  // with grad W = d W / d x_p
+                  const R gw[3] = {st.dw[0][i] * st.w[1][j] * st.w[2][k] * inv_dx,
+                                   st.w[0][i] * st.dw[1][j] * st.w[2][k] * inv_dx,
+                                   st.w[0][i] * st.w[1][j] * st.dw[2][k] * inv_dx};
+                  for (int d = 0; d < 3; ++d) {
+                    const R fdt = contrib[d * 3 + 0] * gw[0] + contrib[d * 3 + 1] * gw[1] +
+                                  contrib[d * 3 + 2] * gw[2];
+                    g[1 + d] += W * mass * vp[d];
+                    g[4 + d] += W * fdt;
+                  }
+                  continue;
+                }
                 for (int d = 0; d < 3; ++d) {
                   const R Cx = Cp[d * 3 + 0] * xixp[0] + Cp[d * 3 + 1] * xixp[1] +
                                Cp[d * 3 + 2] * xixp[2];
                   const R fdt = contrib[d * 3 + 0] * xixp[0] + contrib[d * 3 + 1] * xixp[1] +
                                 contrib[d * 3 + 2] * xixp[2];
-                  g[1 + d] += W * (mass * (vp[d] + Cx) + fdt);
+                  if (tr == ORC_TRANSFER_AFLIP) {  // Transfer.cu:976-980
+                    g[1 + d] += W * (mass * (vp[d] + Cx));
+                    g[4 + d] += W * fdt;
+                  } else {
+                    g[1 + d] += W * (mass * (vp[d] + Cx) + fdt);
+                  }
                 }
               }
         }
@@ -587,18 +631,35 @@ template <class R> struct Sim {
       int32_t c[3];
       dir.coords(P.gb_dir[gb], c);
       for (int cell = 0; cell < 64; ++cell) {
-        R *nd = &grid[(gb * 64 + cell) * 4];
+        R *nd = &grid[(gb * 64 + cell) * kNG];
         if (nd[0] == R(0)) continue;
         const R rm = R(1) / nd[0];
-        R vel[3];
-        for (int d = 0; d < 3; ++d) vel[d] = nd[1 + d] * rm + g[d] * dt;
-        vmax = std::max(vmax, vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
         const int32_t I[3] = {(c[0] + dir.lo[0]) * 4 + (cell >> 4),
                               (c[1] + dir.lo[1]) * 4 + ((cell >> 2) & 3),
                               (c[2] + dir.lo[2]) * 4 + (cell & 3)};
-        apply_bc(I, vel);
-        apply_colliders(I, vel);
-        for (int d = 0; d < 3; ++d) nd[1 + d] = vel[d];
+        R vel[3];
+        if (tr == ORC_TRANSFER_APIC) {
+          for (int d = 0; d < 3; ++d) vel[d] = nd[1 + d] * rm + g[d] * dt;
+          vmax = std::max(vmax, vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+          apply_bc(I, vel);
+          apply_colliders(I, vel);
+          for (int d = 0; d < 3; ++d) nd[1 + d] = vel[d];
+        } else {
+          // MPMPipeline.cu:882-893: v = mv / m; vstar = vstar / m + v + g dt;
+          // MaxVelSqr of vstar; the boundary acts on vstar (Boundary.cu:90-101)
+          R vs[3];
+          for (int d = 0; d < 3; ++d) {
+            vel[d] = nd[1 + d] * rm;
+            vs[d] = nd[4 + d] * rm + vel[d] + g[d] * dt;
+          }
+          vmax = std::max(vmax, vs[0] * vs[0] + vs[1] * vs[1] + vs[2] * vs[2]);
+          apply_bc(I, vs);
+          apply_colliders(I, vs);
+          for (int d = 0; d < 3; ++d) {
+            nd[1 + d] = vel[d];
+            nd[4 + d] = vs[d];
+          }
+        }
       }
     }
     max_vel_sqr = vmax;
@@ -608,7 +669,10 @@ template <class R> struct Sim {
     for (int64_t p = 0; p < n; ++p) {
       Stencil st;
       stencil(x + 3 * p, st);
-      R vel[3] = {0, 0, 0}, Cn[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      // vel = sum W v_i; vs = sum W vstar_i (FLIP transfers); Cn = Dinv sum W
+      // u_i (x_i - x_p)^T with u = v (APIC) or vstar (AFLIP), or the velocity
+      // gradient sum vstar_i (grad W)^T (FLIP)
+      R vel[3] = {0, 0, 0}, vs[3] = {0, 0, 0}, Cn[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j)
           for (int k = 0; k < 3; ++k) {
@@ -616,17 +680,45 @@ template <class R> struct Sim {
             const R xixp[3] = {(R(i) - st.fx[0]) * dx, (R(j) - st.fx[1]) * dx,
                                (R(k) - st.fx[2]) * dx};
             const R W = st.w[0][i] * st.w[1][j] * st.w[2][k];
-            const R *gv = node(I) + 1;
+            const R *gv = node(I) + 1, *gs = node(I) + 4;
+            if (tr == ORC_TRANSFER_FLIP) {
+              const R gw[3] = {st.dw[0][i] * st.w[1][j] * st.w[2][k] * inv_dx,
+                               st.w[0][i] * st.dw[1][j] * st.w[2][k] * inv_dx,
+                               st.w[0][i] * st.w[1][j] * st.dw[2][k] * inv_dx};
+              for (int a = 0; a < 3; ++a) {
+                vel[a] += gv[a] * W;
+                vs[a] += gs[a] * W;
+                for (int bb = 0; bb < 3; ++bb) Cn[a * 3 + bb] += gs[a] * gw[bb];
+              }
+              continue;
+            }
+            const R *gu = tr == ORC_TRANSFER_AFLIP ? gs : gv;
             for (int a = 0; a < 3; ++a) {
               vel[a] += gv[a] * W;
-              for (int bb = 0; bb < 3; ++bb) Cn[a * 3 + bb] += W * Dinv * gv[a] * xixp[bb];
+              vs[a] += gs[a] * W;
+              for (int bb = 0; bb < 3; ++bb) Cn[a * 3 + bb] += W * Dinv * gu[a] * xixp[bb];
             }
           }
-      for (int a = 0; a < 3; ++a) {
-        v[3 * p + a] = vel[a];
-        x[3 * p + a] += vel[a] * dt;
+      if (tr == ORC_TRANSFER_APIC) {
+        for (int a = 0; a < 3; ++a) {
+          v[3 * p + a] = vel[a];
+          x[3 * p + a] += vel[a] * dt;
+        }
+        for (int i = 0; i < 9; ++i) C[9 * p + i] = Cn[i];
+      } else {
+        // Transfer.cu:1203-1211 (AFLIP), 1245-1250 (FLIP): flip = 0.99,
+        // v = vstar + flip (v_p - vel); AFLIP x += dt (vstar + beta flip
+        // (v_p - vel)) and C = Cn; FLIP x += dt vstar, C unchanged
+        const R flip = R(0.99);
+        const R bp = beta ? beta[p] : R(0);
+        for (int a = 0; a < 3; ++a) {
+          const R d0 = v[3 * p + a] - vel[a];
+          v[3 * p + a] = vs[a] + flip * d0;
+          x[3 * p + a] += tr == ORC_TRANSFER_AFLIP ? dt * (vs[a] + bp * flip * d0) : vs[a] * dt;
+        }
+        if (tr == ORC_TRANSFER_AFLIP)
+          for (int i = 0; i < 9; ++i) C[9 * p + i] = Cn[i];
       }
-      for (int i = 0; i < 9; ++i) C[9 * p + i] = Cn[i];
       const Params<R> &mp = mats[mat[p]];
       R *Fp = F + 9 * p;
       if (mp.type == ORC_EOS) {
@@ -683,9 +775,11 @@ template <class R> struct Sim {
 
 template <class R>
 int32_t run(const orc_scene *scene, int64_t n, R *x, R *v, R *C, R *F, R *J, const R *m,
-            const R *vol, const int32_t *mat, const R *mu, const R *lam, R dt, int32_t nsteps,
-            int32_t nthreads, orc_stats *stats) {
+            const R *vol, const int32_t *mat, const R *mu, const R *lam, const R *beta, R dt,
+            int32_t nsteps, int32_t nthreads, orc_stats *stats) {
   if (!scene || n < 0 || nsteps < 0) return ORC_ERR_INVALID;
+  if (scene->transfer < ORC_TRANSFER_APIC || scene->transfer > ORC_TRANSFER_AFLIP)
+    return ORC_ERR_INVALID;
   for (int64_t p = 0; p < n; ++p)
     if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
 #ifdef _OPENMP
@@ -696,7 +790,7 @@ int32_t run(const orc_scene *scene, int64_t n, R *x, R *v, R *C, R *F, R *J, con
   Sim<R> sim(*scene, nthreads);
   int32_t rc = ORC_OK;
   for (int32_t s = 0; s < nsteps && rc == ORC_OK; ++s)
-    rc = sim.substep(n, x, v, C, F, J, m, vol, mat, mu, lam, dt);
+    rc = sim.substep(n, x, v, C, F, J, m, vol, mat, mu, lam, beta, dt);
   if (stats) {
     stats->max_vel_sqr = double(sim.max_vel_sqr);
     stats->n_pblocks = int64_t(sim.P.pb_dir.size());
@@ -734,16 +828,49 @@ int32_t orc_partition(const orc_scene *scene, int64_t n, const float *x, int64_t
 
 int32_t orc_run_f64(const orc_scene *scene, int64_t n, double *x, double *v, double *C, double *F,
                     double *J, const double *m, const double *vol, const int32_t *mat,
-                    const double *mu, const double *lam, double dt, int32_t nsteps,
-                    int32_t nthreads, orc_stats *stats) {
-  return run<double>(scene, n, x, v, C, F, J, m, vol, mat, mu, lam, dt, nsteps, nthreads, stats);
+                    const double *mu, const double *lam, const double *beta, double dt,
+                    int32_t nsteps, int32_t nthreads, orc_stats *stats) {
+  return run<double>(scene, n, x, v, C, F, J, m, vol, mat, mu, lam, beta, dt, nsteps, nthreads,
+                     stats);
 }
 
 int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v, float *C, float *F,
                     float *J, const float *m, const float *vol, const int32_t *mat,
-                    const float *mu, const float *lam, float dt, int32_t nsteps,
-                    int32_t nthreads, orc_stats *stats) {
-  return run<float>(scene, n, x, v, C, F, J, m, vol, mat, mu, lam, dt, nsteps, nthreads, stats);
+                    const float *mu, const float *lam, const float *beta, float dt,
+                    int32_t nsteps, int32_t nthreads, orc_stats *stats) {
+  return run<float>(scene, n, x, v, C, F, J, m, vol, mat, mu, lam, beta, dt, nsteps, nthreads,
+                    stats);
+}
+
+// ComputeParticleBeta (Boundary.cu:172-516) without a boundary (:490-499)
+// and with a level-set boundary (determine_beta_sdf, :285-315): at
+// x + dt v, a particle inside the collider moving into it, (v - v_obj) . n
+// < 0, gets beta = 0; otherwise beta = 0.5 where J = det F > Jp_critical = 1
+// (the value for every model here; 1.1 is the Cam-Clay one), else 0.  The
+// equation-of-state fluid keeps J instead of F.
+int32_t orc_particle_beta_f64(const orc_scene *scene, int64_t n, const double *x, const double *v,
+                              const double *F, const double *J, const int32_t *mat, double dt,
+                              int32_t collider, double *beta) {
+  if (!scene || n < 0 || !beta || collider >= scene->n_colliders) return ORC_ERR_INVALID;
+  Sim<double> sim(*scene, 1);
+  for (int64_t p = 0; p < n; ++p) {
+    if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
+    if (collider >= 0) {
+      double pos[3], nrm[3], vo[3];
+      for (int a = 0; a < 3; ++a) pos[a] = x[3 * p + a] + dt * v[3 * p + a];
+      if (sim.collider_hit(sim.cols[collider], pos, nrm, vo)) {
+        const double vn = (v[3 * p] - vo[0]) * nrm[0] + (v[3 * p + 1] - vo[1]) * nrm[1] +
+                          (v[3 * p + 2] - vo[2]) * nrm[2];
+        if (vn < 0) {
+          beta[p] = 0;
+          continue;
+        }
+      }
+    }
+    const double Jp = sim.mats[mat[p]].type == ORC_EOS ? J[p] : det3(F + 9 * p);
+    beta[p] = Jp > 1.0 ? 0.5 : 0.0;
+  }
+  return ORC_OK;
 }
 
 void orc_sym_eig3(const double *A, double *w, double *Q) { sym_eig3<double>(A, w, Q, kSweeps); }

@@ -14,6 +14,11 @@
  *   ApplyBoundaryOnZSGrid       projects/CuLagrange/mpm/Boundary.cu:56-67,105-116
  *   ZSGridToZSParticle (APIC)   projects/CuLagrange/mpm/Transfer.cu:1137-1173
  *   ZSReturnMapping             projects/CuLagrange/mpm/MPMPipeline.cu:953-972
+ *   FLIP / AFLIP transfers      projects/CuLagrange/mpm/Transfer.cu:891-984 (P2G),
+ *                               MPMPipeline.cu:878-897 (grid update),
+ *                               Transfer.cu:1174-1257 (G2P)
+ *   ComputeParticleBeta         projects/CuLagrange/mpm/Boundary.cu:172-516
+ *                               (no-boundary and level-set forms)
  * The arithmetic the reference delegates to zpc (absent from the reference
  * tree; submodule projects/CUDA/zpc, pinned commit unknown) is restated from
  * the published methods named at each function in mpm_oracle.cpp.
@@ -35,6 +40,8 @@ extern "C" {
 enum { ORC_FCR = 0, ORC_NHK = 1, ORC_STVK = 2, ORC_EOS = 3 };
 enum { ORC_PLASTIC_NONE = 0, ORC_PLASTIC_NADP = 1 };
 enum { ORC_BC_NONE = 0, ORC_BC_STICKY = 1, ORC_BC_SLIP = 2, ORC_BC_SEPARATE = 3 };
+/* MakeZSGrid "transfer" (Generation.cu:1493-1504) */
+enum { ORC_TRANSFER_APIC = 0, ORC_TRANSFER_FLIP = 1, ORC_TRANSFER_AFLIP = 2 };
 
 enum {
   ORC_OK = 0,
@@ -85,6 +92,7 @@ typedef struct orc_scene {
   int32_t n_colliders;
   const orc_collider *colliders;
   int32_t collider_autostep; /* 1: advance colliders by dt at the start of each substep */
+  int32_t transfer;          /* ORC_TRANSFER_* */
 } orc_scene;
 
 typedef struct orc_stats {
@@ -106,19 +114,30 @@ int32_t orc_partition(const orc_scene *scene, int64_t n, const float *x,
                       int32_t *pb_count, int64_t *perm, int64_t cap_gb,
                       int32_t *n_gb, int32_t *gb_dir);
 
-/* nsteps substeps in double precision, order-stable scatter (the oracle). */
+/* nsteps substeps in double precision, order-stable scatter (the oracle).
+ * beta: the particles' AFLIP positional-adjustment factor (NULL: 0). */
 int32_t orc_run_f64(const orc_scene *scene, int64_t n, double *x, double *v,
                     double *C, double *F, double *J, const double *m,
                     const double *vol, const int32_t *mat, const double *mu,
-                    const double *lam, double dt, int32_t nsteps,
-                    int32_t nthreads, orc_stats *stats);
+                    const double *lam, const double *beta, double dt,
+                    int32_t nsteps, int32_t nthreads, orc_stats *stats);
 
 /* Same substeps in single precision with OpenMP (the CPU baseline). */
 int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v,
                     float *C, float *F, float *J, const float *m,
                     const float *vol, const int32_t *mat, const float *mu,
-                    const float *lam, float dt, int32_t nsteps,
-                    int32_t nthreads, orc_stats *stats);
+                    const float *lam, const float *beta, float dt,
+                    int32_t nsteps, int32_t nthreads, orc_stats *stats);
+
+/* ComputeParticleBeta (Boundary.cu:172-516) in double precision: with
+ * collider < 0 the criterion of the node without a boundary (beta = 0.5 where
+ * det F > 1, else 0; J for the equation-of-state fluid); with the index of
+ * one of the scene's colliders, first the level-set test at x + dt v
+ * (beta = 0 where the particle moves into the collider). */
+int32_t orc_particle_beta_f64(const orc_scene *scene, int64_t n, const double *x,
+                              const double *v, const double *F, const double *J,
+                              const int32_t *mat, double dt, int32_t collider,
+                              double *beta);
 
 /* Symmetric 3x3 eigen-decomposition used by the constitutive models
  * (exported for known-answer tests): A = Q diag(w) Q^T, Q column-major

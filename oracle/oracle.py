@@ -39,7 +39,7 @@ class OrcScene(C.Structure):
                 ("bc_thickness", C.c_int32), ("bc_lo", C.c_int32 * 3), ("bc_hi", C.c_int32 * 3),
                 ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial)),
                 ("n_colliders", C.c_int32), ("colliders", C.POINTER(OrcCollider)),
-                ("collider_autostep", C.c_int32)]
+                ("collider_autostep", C.c_int32), ("transfer", C.c_int32)]
 
 
 class OrcStats(C.Structure):
@@ -70,10 +70,13 @@ def lib():
         L.orc_partition.restype = C.c_int32
         for name, real in (("orc_run_f64", C.c_double), ("orc_run_f32", C.c_float)):
             f = getattr(L, name)
-            f.argtypes = [C.POINTER(OrcScene), C.c_int64] + [P] * 10 + [real, C.c_int32,
+            f.argtypes = [C.POINTER(OrcScene), C.c_int64] + [P] * 11 + [real, C.c_int32,
                                                                         C.c_int32,
                                                                         C.POINTER(OrcStats)]
             f.restype = C.c_int32
+        L.orc_particle_beta_f64.argtypes = [C.POINTER(OrcScene), C.c_int64, P, P, P, P, P,
+                                            C.c_double, C.c_int32, P]
+        L.orc_particle_beta_f64.restype = C.c_int32
         L.orc_sym_eig3.argtypes = [P, P, P]
         L.orc_kirchhoff.argtypes = [C.POINTER(OrcMaterial), P, C.c_double, P]
         L.orc_kirchhoff.restype = C.c_int32
@@ -123,7 +126,8 @@ class _SceneHolder:
                           int(scene.bc_type), int(scene.bc_thickness),
                           (C.c_int32 * 3)(*scene.bc_lo), (C.c_int32 * 3)(*scene.bc_hi),
                           len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)),
-                          len(cols), C.cast(carr, C.POINTER(OrcCollider)), 1)
+                          len(cols), C.cast(carr, C.POINTER(OrcCollider)), 1,
+                          int(getattr(scene, "transfer", 0)))
 
 
 def partition(scene, x: np.ndarray) -> dict:
@@ -154,7 +158,7 @@ def run(scene, parts, nsteps: int, precision: str = "f64", nthreads: int = 0,
     (particles, stats).  inplace needs contiguous arrays of the precision."""
     dtype = np.float64 if precision == "f64" else np.float32
     p = parts if inplace else parts.copy(dtype=dtype)
-    for k in ("x", "v", "C", "F", "J", "m", "vol", "mu", "lam"):
+    for k in ("x", "v", "C", "F", "J", "m", "vol", "mu", "lam", "beta"):
         a = getattr(p, k)
         if a is not None:
             if inplace and (a.dtype != dtype or not a.flags.c_contiguous):
@@ -165,11 +169,26 @@ def run(scene, parts, nsteps: int, precision: str = "f64", nthreads: int = 0,
     st = OrcStats()
     fn = lib().orc_run_f64 if precision == "f64" else lib().orc_run_f32
     rc = fn(C.byref(h.s), p.n, _ptr(p.x), _ptr(p.v), _ptr(p.C), _ptr(p.F), _ptr(p.J),
-            _ptr(p.m), _ptr(p.vol), _ptr(p.mat), _ptr(p.mu), _ptr(p.lam),
+            _ptr(p.m), _ptr(p.vol), _ptr(p.mat), _ptr(p.mu), _ptr(p.lam), _ptr(p.beta),
             float(scene.dt if dt is None else dt), int(nsteps), int(nthreads), C.byref(st))
     stats = {"status": rc, "max_vel_sqr": st.max_vel_sqr, "n_pblocks": st.n_pblocks,
              "n_gblocks": st.n_gblocks}
     return p, stats
+
+
+def particle_beta(scene, parts, dt: float | None = None, collider: int = -1) -> np.ndarray:
+    """ComputeParticleBeta in FP64: beta per particle (upload order)."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    h = _SceneHolder(scene)
+    x, v, F, J = f(parts.x), f(parts.v), f(parts.F), f(parts.J)
+    mat = np.ascontiguousarray(parts.mat, dtype=np.int32)
+    beta = np.zeros(parts.n)
+    rc = lib().orc_particle_beta_f64(C.byref(h.s), parts.n, _ptr(x), _ptr(v), _ptr(F), _ptr(J),
+                                     _ptr(mat), float(scene.dt if dt is None else dt),
+                                     int(collider), _ptr(beta))
+    if rc != 0:
+        raise RuntimeError(f"oracle beta failed with status {rc}")
+    return beta
 
 
 def sym_eig3(A: np.ndarray):

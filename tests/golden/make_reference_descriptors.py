@@ -21,7 +21,7 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ZSParticleToZSGrid", "UpdateZSGrid", "ApplyBoundaryOnZSGrid", "ToZSBoundary",
          "ZSGridToZSParticle", "ZSReturnMapping", "AdjustParticleMaterial",
          "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
-         "StepZSBoundary"]
+         "StepZSBoundary", "ComputeParticleBeta"]
 
 
 def parse_braces(s, i):

@@ -310,7 +310,8 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
       (rc = dalloc(c, &d.grid, (size_t)capg * 64)) ||
       (rc = dalloc(c, &d.tile_sums, (size_t)3 * d.ntiles)) || (rc = dalloc(c, &d.cnt, 1)) ||
       (rc = dalloc(c, &d.prm, 1)) || (rc = dalloc(c, &d.scn, n_scenes)) ||
-      (rc = dalloc(c, &d.mats, kMaxMaterials)) || (rc = dalloc(c, &d.colliders, kMaxColliders)))
+      (rc = dalloc(c, &d.mats, kMaxMaterials)) || (rc = dalloc(c, &d.colliders, kMaxColliders)) ||
+      (rc = dalloc(c, &d.beta, cap)))
     return bail(rc);
   if (cudaMallocHost(&c->h_cnt, sizeof(Counters)) != cudaSuccess)
     return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
@@ -321,6 +322,7 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
   }
   cudaMemsetAsync(d.perm, 0, (size_t)cap * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.pkey, 0, (size_t)cap * sizeof(int32_t), c->stream);
+  cudaMemsetAsync(d.beta, 0, (size_t)cap * sizeof(float), c->stream);
   cudaMemsetAsync(d.dir_count, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_fill, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_gb, 0xff, ndir * sizeof(int32_t), c->stream);
@@ -638,6 +640,8 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
   }
   launch_ingest(c->d, c->cur, src, n, c->stream);
   if ((rc = launch_check("ingest"))) return rc;
+  if (n > 0)  // ToZSParticles: beta = 0 (Generation.cpp:944-966)
+    ZS_CUDA(cudaMemsetAsync(c->d.beta, 0, (size_t)n * sizeof(float), c->stream));
   c->prm.n = n;
   c->prm.has_lame = mu ? 1 : 0;
   for (int s = 0; s < ns; ++s) c->scenes[s].p_off = scene_offsets ? scene_offsets[s] : 0;
@@ -713,6 +717,91 @@ int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *
     return rc;
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   return MPM_OK;
+}
+
+int32_t mpm_particles_get_attr(mpm_ctx *c, const char *name, float *values) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
+  const std::string a(name);
+  const long long n = c->prm.n;
+  if (a == "beta") {
+    if (n > 0)
+      ZS_CUDA(cudaMemcpyAsync(values, c->d.beta, n * sizeof(float), cudaMemcpyDeviceToHost,
+                              c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+  }
+  int ch = -1;
+  if (a == "m") ch = CH_M;
+  if (a == "vol") ch = CH_VOL;
+  if (a == "J") ch = CH_J;
+  if (a == "mu" || a == "lam") {
+    if (!c->prm.has_lame) return fail(MPM_ERR_STATE, "no per-particle Lame parameters set");
+    ch = a == "mu" ? CH_MU : CH_LAM;
+  }
+  if (ch < 0) return fail(MPM_ERR_INVALID, "unknown particle attribute '" + a + "'");
+  float *st = c->d.pbuf[1 - c->cur];
+  launch_egest_channel(c->d, c->cur, ch, st, n, c->stream);
+  if ((rc = launch_check("attribute"))) return rc;
+  if (n > 0)
+    ZS_CUDA(cudaMemcpyAsync(values, st, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_particles_set_attr(mpm_ctx *c, const char *name, const float *values) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
+  if (std::string(name) != "beta")
+    return fail(MPM_ERR_INVALID, std::string("attribute '") + name + "' cannot be set");
+  const long long n = c->prm.n;
+  if (n > 0)
+    ZS_CUDA(cudaMemcpyAsync(c->d.beta, values, n * sizeof(float), cudaMemcpyHostToDevice,
+                            c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_set_transfer(mpm_ctx *c, int32_t scheme) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (scheme < MPM_TRANSFER_APIC || scheme > MPM_TRANSFER_AFLIP)
+    return fail(MPM_ERR_INVALID, "unknown transfer scheme");
+  if (scheme != MPM_TRANSFER_APIC && c->d.keep_order)
+    return fail(MPM_ERR_INVALID, "the differentiable form takes the APIC transfer only");
+  if (scheme == c->d.transfer) return MPM_OK;
+  DevPtrs &d = c->d;
+  if (scheme != MPM_TRANSFER_APIC && !d.grid2) {
+    if ((rc = dalloc(c, &d.grid2, (size_t)d.cap_gblocks * 64)) ||
+        (rc = dalloc(c, &d.ptile2, (size_t)d.cap_gblocks * kTileNodes)))
+      return rc;
+    configure_flip_launches(d);
+  }
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  d.transfer = scheme;
+  c->prm.transfer = scheme;
+  c->prm_dirty = true;
+  drop_graphs(c);  // the graphs hold the other transfer's kernels
+  if ((rc = push_params(c))) return rc;
+  if (c->prm.n > 0) {  // the stored stress follows the scheme's Lame parameters
+    launch_stress(d, c->cur, c->stream);
+    if ((rc = launch_check("stress"))) return rc;
+  }
+  c->partition_valid = false;  // a stage-path grid of the old scheme is stale
+  return MPM_OK;
+}
+
+int32_t mpm_compute_particle_beta(mpm_ctx *c, float dt, int32_t collider) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (collider < -1 || collider >= (int32_t)c->colliders.size())
+    return fail(MPM_ERR_INVALID, "collider id out of range");
+  if (c->prm.n == 0) return MPM_OK;
+  if ((rc = push_params(c))) return rc;
+  launch_particle_beta(c->d, c->cur, dt, collider, c->stream);
+  return launch_check("particle beta");
 }
 
 int32_t mpm_partition(mpm_ctx *c) {
@@ -902,6 +991,8 @@ int32_t mpm_get_launch_config(mpm_ctx *c, mpm_launch_config *cfg) {
 int32_t mpm_set_order_mode(mpm_ctx *c, int32_t keep) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if (keep && c->d.transfer != MPM_TRANSFER_APIC)
+    return fail(MPM_ERR_INVALID, "the differentiable form takes the APIC transfer only");
   if (keep && !c->d.ptile_adj && (rc = dalloc(c, &c->d.ptile_adj, (size_t)c->d.cap_gblocks * kTileNodes)))
     return rc;
   ZS_CUDA(cudaStreamSynchronize(c->stream));

@@ -16,6 +16,30 @@
 
 namespace zsmpm {
 
+// ApplyBoundaryOnZSGrid with the analytic box walls at node index I: a node
+// is in the lower wall of axis a when I_a < lo_a + thickness and in the
+// upper wall when I_a > hi_a - thickness; sticky sets v = 0, slip removes the
+// wall-normal component, separate removes it only when it points into the
+// wall (collider velocity 0, Boundary.cu:56-67).
+__device__ __forceinline__ void apply_walls(const SceneParams &S, const int (&I)[3],
+                                            float (&vel)[3]) {
+  if (S.bc_type == MPM_BC_NONE) return;
+  bool any = false;
+  const int t = S.bc_thickness;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const bool lower = I[a] < S.bc_lo[a] + t, upper = I[a] > S.bc_hi[a] - t;
+    if (!(lower || upper)) continue;
+    any = true;
+    if (S.bc_type == MPM_BC_SLIP) vel[a] = 0.0f;
+    if (S.bc_type == MPM_BC_SEPARATE) {
+      if (lower && vel[a] < 0.0f) vel[a] = 0.0f;
+      if (upper && vel[a] > 0.0f) vel[a] = 0.0f;
+    }
+  }
+  if (any && S.bc_type == MPM_BC_STICKY) vel[0] = vel[1] = vel[2] = 0.0f;
+}
+
 // signed distance (world units), unit normal and collider velocity at p;
 // false when p is outside the collider's grid or not inside the collider
 __device__ __forceinline__ bool collider_hit(const ColliderDev &c, const float (&p)[3],
@@ -154,17 +178,5 @@ __device__ __forceinline__ void step_colliders(const DevPtrs &d, int nc, float d
   }
 }
 
-// is p inside the world box of any collider k0..k1-1 of the scene
-__device__ __forceinline__ bool near_colliders(const DevPtrs &d, int k0, int k1, int scene,
-                                              const float (&p)[3]) {
-  for (int k = k0; k < k1; ++k) {
-    const ColliderDev &c = d.colliders[k];
-    if (!collider_in_scene(c, scene) || c.type == MPM_BC_NONE) continue;
-    if (p[0] >= c.lo[0] && p[0] <= c.hi[0] && p[1] >= c.lo[1] && p[1] <= c.hi[1] &&
-        p[2] >= c.lo[2] && p[2] <= c.hi[2])
-      return true;
-  }
-  return false;
-}
 
 }  // namespace zsmpm

@@ -58,6 +58,17 @@ __global__ void k_egest(const float *__restrict__ pb, const int32_t *__restrict_
   }
 }
 
+// one float channel of the store -> dst in upload order
+__global__ void k_egest_channel(const float *__restrict__ pb, const int32_t *__restrict__ ib,
+                                int ch, float *__restrict__ dst, long long n) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
+       s += (long long)gridDim.x * blockDim.x) {
+    const long long u = ib[iidx(IC_ID, s)];
+    if (u < 0 || u >= n) continue;
+    dst[u] = pb[pidx(ch, s)];
+  }
+}
+
 // per-particle Lame overrides given in upload order -> storage order
 __global__ void k_set_lame(float *__restrict__ pb, const int32_t *__restrict__ ib, long long cap,
                            const float *__restrict__ mu, const float *__restrict__ lam,
@@ -109,6 +120,12 @@ void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, 
                        cudaStream_t s) {
   if (n <= 0) return;
   k_state_copy<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], dst, src, n);
+}
+
+void launch_egest_channel(const DevPtrs &d, int cur, int ch, float *dst, long long n,
+                          cudaStream_t s) {
+  if (n <= 0) return;
+  k_egest_channel<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], ch, dst, n);
 }
 
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,

@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "binning.cuh"
+#include "blocks.cuh"
 #include "colliders.cuh"
 #include "cp_async.cuh"
 #include "mpm_math.cuh"
@@ -32,24 +33,6 @@
 namespace zsmpm {
 namespace {
 
-
-// node index of the first node of the particle block at (scene-local)
-// directory index `ldir`
-__device__ __forceinline__ void bucket_origin(const SceneParams &S, int ldir, int (&K)[3]) {
-  const int dz = S.block_dims[2], dy = S.block_dims[1];
-  const int c2 = ldir % dz, c1 = (ldir / dz) % dy, c0 = ldir / (dz * dy);
-  K[0] = (c0 + S.block_lo[0]) * 4;
-  K[1] = (c1 + S.block_lo[1]) * 4;
-  K[2] = (c2 + S.block_lo[2]) * 4;
-}
-
-// grid block of each of the 2x2x2 blocks around the particle block at
-// (global) directory index `dir`
-__device__ __forceinline__ int neighbour_gb(const DevPtrs &d, const SceneParams &S, int dir,
-                                            int t) {
-  const int dz = S.block_dims[2], dy = S.block_dims[1];
-  return d.dir_gb[dir + ((t >> 2) * dy + ((t >> 1) & 1)) * dz + (t & 1)];
-}
 
 // P2G of one particle block (ZSParticleToZSGrid::p2g_apic, Transfer.cu:849-889):
 // per particle the affine matrix A = m C - dt Dinv S (S = vol tau from the
@@ -425,10 +408,7 @@ __global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, i
 
 // UpdateZSGrid (MPMPipeline.cu:852-877): v = mv / m + g dt where m != 0,
 // running max of |v|^2; then ApplyBoundaryOnZSGrid (Boundary.cu:105-116) with
-// the analytic box walls: a node is in the lower wall of axis a when
-// I_a < lo_a + thickness and in the upper wall when I_a > hi_a - thickness;
-// sticky sets v = 0, slip removes the wall-normal component, separate removes
-// it only when it points into the wall (collider velocity 0).
+// the analytic box walls (apply_walls).
 __device__ __forceinline__ void update_node(const DevPtrs &d, int scene, const SceneParams &S,
                                             float dt, int mode, int ldir, int cell, float4 &g,
                                             float &vmax) {
@@ -452,20 +432,7 @@ __device__ __forceinline__ void update_node_at(const DevPtrs &d, int scene, cons
   }
   if ((mode & 2) && S.bc_type != MPM_BC_NONE) {
     float vel[3] = {g.y, g.z, g.w};
-    bool any = false;
-    const int t = S.bc_thickness;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const bool lower = I[a] < S.bc_lo[a] + t, upper = I[a] > S.bc_hi[a] - t;
-      if (!(lower || upper)) continue;
-      any = true;
-      if (S.bc_type == MPM_BC_SLIP) vel[a] = 0.0f;
-      if (S.bc_type == MPM_BC_SEPARATE) {
-        if (lower && vel[a] < 0.0f) vel[a] = 0.0f;
-        if (upper && vel[a] > 0.0f) vel[a] = 0.0f;
-      }
-    }
-    if (any && S.bc_type == MPM_BC_STICKY) vel[0] = vel[1] = vel[2] = 0.0f;
+    apply_walls(S, I, vel);
     g.y = vel[0];
     g.z = vel[1];
     g.w = vel[2];
@@ -494,16 +461,6 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
   }
 }
 
-// G2P launch metadata of one particle block, held in shared memory for the
-// blocks a CTA owns so that the software pipeline below needs no dependent
-// global loads to find its next chunk.
-struct G2PMeta {
-  int start, cnt, dir, scene;
-  int gb[8];  // grid blocks of the 2x2x2 block neighbourhood (-1: absent)
-  int K[3];   // node index of the block's first node
-  int pad;
-};
-
 constexpr int kG2PCh = 19;     // staged particle channels
 constexpr int kG2PMeta = 64;   // blocks per CTA whose metadata is staged
 // staged channel slots
@@ -515,19 +472,6 @@ constexpr int g2p_smem_bytes() {
   return 2 * kNodes * 16 + 2 * kG2PCh * NT * 4 + kG2PMeta * (int)sizeof(G2PMeta);
 }
 
-__device__ __forceinline__ G2PMeta g2p_load_meta(const DevPtrs &d, long long n, int b) {
-  G2PMeta m;
-  m.dir = d.bk_dir[b];
-  m.scene = scene_of_dir(d, m.dir);
-  m.start = d.bk_start[b];
-  m.cnt = (int)max(0ll, min((long long)d.bk_count[b], n - m.start));
-  const SceneParams &S = d.scn[m.scene];
-#pragma unroll
-  for (int t = 0; t < 8; ++t) m.gb[t] = neighbour_gb(d, S, m.dir, t);
-  bucket_origin(S, m.dir - S.dir_off, m.K);
-  m.pad = 0;
-  return m;
-}
 
 // G2P (ZSGridToZSParticle, Transfer.cu:1139-1173) with the return mapping and
 // the stress of the new F fused in.  A CTA walks the particle blocks it owns
@@ -842,6 +786,10 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
 #pragma unroll
       for (int k = 0; k < 9; ++k) pbuf[pidx((CH_F + k), p)] = F[k];
       pbuf[pidx(CH_J, p)] = det3(F);
+      // the FLIP P2G takes the material's Lame parameters (Transfer.cu:897-907)
+      if (lame && d.transfer == MPM_TRANSFER_FLIP &&
+          !kirchhoff(mp.type, mp.mu, mp.lam, mp.bulk, mp.gamma, F, 1.0f, tau))
+        atomicOr(&d.cnt->status, ST_NAN);
       store_stress(pbuf, p, pbuf[pidx(CH_VOL, p)], tau);
     }
   }
@@ -867,7 +815,7 @@ __global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__r
       for (int k = 0; k < 9; ++k) F[k] = pbuf[pidx((CH_F + k), p)];
     }
     float mu = mp.mu, lam = mp.lam;
-    if (lame) {
+    if (lame && d.transfer != MPM_TRANSFER_FLIP) {  // FLIP: Transfer.cu:897-907
       mu = pbuf[pidx(CH_MU, p)];
       lam = pbuf[pidx(CH_LAM, p)];
     }
@@ -907,42 +855,67 @@ void configure_launches(DevPtrs &d) {
 }
 
 void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
+  if (d.transfer != MPM_TRANSFER_APIC) return launch_p2g_flip(d, cur, s);
   k_p2g<<<d.grid_p2g, kColThreads, kColSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
 }
 
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
+  if (d.transfer != MPM_TRANSFER_APIC) return launch_grid_gather_flip(d, mode, s);
   k_grid_gather<<<d.grid_stream, 64 * kGatherBlocks, 0, s>>>(d, mode);
 }
 
-// ApplyBoundaryOnZSGrid with level sets: the colliders of each node's scene,
-// after the box walls (its own pass, launched only when colliders exist)
-// collider `id` (-1: every collider, in id order) on the active grid nodes
+// ApplyBoundaryOnZSGrid with level sets: collider `id` (-1: every collider,
+// in id order) on the active nodes, after the box walls; its own pass,
+// launched only when colliders exist.  One warp per grid block: the warp
+// finds the block's node box once and skips the block unless the box meets
+// the world box of one of the colliders, so only blocks near a collider read
+// the grid (two nodes per lane).
 __global__ void k_apply_colliders(DevPtrs d, int id) {
   const int nc = d.prm->n_colliders;
   const int k0 = id < 0 ? 0 : id, k1 = id < 0 ? nc : min(id + 1, nc);
-  const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-       idx += (long long)gridDim.x * blockDim.x) {
-    // the node's position first: only nodes in a collider's world box read
-    // the grid
-    const int gdir = d.gb_dir[idx >> 6];
+  const int ng = min(d.cnt->n_gblocks, d.cap_gblocks);
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < ng; gb += nw) {
+    const int gdir = d.gb_dir[gb];
     const int sc = scene_of_dir(d, gdir);
     const SceneParams &S = d.scn[sc];
     const int dz = S.block_dims[2], dy = S.block_dims[1];
-    const int ldir = gdir - S.dir_off, cell = (int)(idx & 63);
-    const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
-                      (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
-                      ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
-    const float p[3] = {(float)I[0] * S.dx, (float)I[1] * S.dx, (float)I[2] * S.dx};
-    if (!near_colliders(d, k0, k1, sc, p)) continue;
-    float4 g = d.grid[idx];
-    if (g.x == 0.0f) continue;
-    float vel[3] = {g.y, g.z, g.w};
-    apply_colliders(d, k0, k1, sc, p, vel);
-    g.y = vel[0];
-    g.z = vel[1];
-    g.w = vel[2];
-    d.grid[idx] = g;
+    const int ldir = gdir - S.dir_off;
+    const int I0[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4, (((ldir / dz) % dy) + S.block_lo[1]) * 4,
+                       ((ldir % dz) + S.block_lo[2]) * 4};
+    const float lo[3] = {(float)I0[0] * S.dx, (float)I0[1] * S.dx, (float)I0[2] * S.dx};
+    const float hi[3] = {(float)(I0[0] + 3) * S.dx, (float)(I0[1] + 3) * S.dx, (float)(I0[2] + 3) * S.dx};
+    bool near = false;
+    for (int k = k0; k < k1 && !near; ++k) {
+      const ColliderDev &c = d.colliders[k];
+      if (!collider_in_scene(c, sc) || c.type == MPM_BC_NONE) continue;
+      near = hi[0] >= c.lo[0] && lo[0] <= c.hi[0] && hi[1] >= c.lo[1] && lo[1] <= c.hi[1] &&
+             hi[2] >= c.lo[2] && lo[2] <= c.hi[2];
+    }
+    if (!near) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int cell = lane + 32 * h;
+      const long long idx = (long long)gb * 64 + cell;
+      if (d.grid[idx].x == 0.0f) continue;
+      const float p[3] = {(float)(I0[0] + (cell >> 4)) * S.dx, (float)(I0[1] + ((cell >> 2) & 3)) * S.dx,
+                          (float)(I0[2] + (cell & 3)) * S.dx};
+      if (d.transfer == MPM_TRANSFER_APIC) {
+        float4 g = d.grid[idx];
+        float vel[3] = {g.y, g.z, g.w};
+        apply_colliders(d, k0, k1, sc, p, vel);
+        g.y = vel[0];
+        g.z = vel[1];
+        g.w = vel[2];
+        d.grid[idx] = g;
+      } else {  // the FLIP grids resolve collisions on vstar (Boundary.cu:90-101)
+        float4 h4 = d.grid2[idx];
+        float vel[3] = {h4.x, h4.y, h4.z};
+        apply_colliders(d, k0, k1, sc, p, vel);
+        d.grid2[idx] = make_float4(vel[0], vel[1], vel[2], h4.w);
+      }
+    }
   }
 }
 
@@ -968,6 +941,7 @@ void launch_step_colliders(const DevPtrs &d, int id, float dt, cudaStream_t s) {
 }
 
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {
+  if (d.transfer != MPM_TRANSFER_APIC) return launch_grid_update_flip(d, mode, s);
   k_grid_update<<<d.num_sms * 8, 256, 0, s>>>(d, mode);
 }
 
@@ -986,6 +960,7 @@ void launch_g2p_nt(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStr
 }
 
 void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
+  if (d.transfer != MPM_TRANSFER_APIC) return launch_g2p_flip(d, cur, fuse_rm, fuse_bin, s);
   if (d.g2p_threads == 256)
     launch_g2p_nt<256>(d, cur, fuse_rm, fuse_bin, s);
   else

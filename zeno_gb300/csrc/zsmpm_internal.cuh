@@ -15,7 +15,8 @@
 //    box (a perfect hash of block coordinates), holding particle counts,
 //    scatter cursors and the grid block index.
 //  * grid: `cap_gblocks` blocks x 64 nodes x float4 (m, mv / v), node cell id
-//    (i << 4) | (j << 2) | k inside the block.
+//    (i << 4) | (j << 2) | k inside the block; with the FLIP transfers a
+//    second grid of float4 (vstar, 0) in the same node order.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -97,6 +98,7 @@ struct SimParams {
   int has_lame;
   int n_colliders;  // level-set colliders in DevPtrs::colliders
   int auto_step;    // the fused substep advances the colliders by dt
+  int transfer;     // MPM_TRANSFER_* (MakeZSGrid "transfer")
   long long n;      // particles of all scenes
 };
 
@@ -181,7 +183,12 @@ struct DevPtrs {
   int32_t *bk_dir, *bk_start, *bk_count;
   int cap_gblocks;
   float4 *grid;
+  float4 *grid2;      // FLIP transfers: (vstar, 0) per node, else null
   float4 *ptile;      // per particle block: its 6^3 P2G node sums (216 float4)
+  float4 *ptile2;     // FLIP transfers: the vstar sums of the same tiles
+  float *beta;        // AFLIP positional adjustment per particle, by upload index
+                      // (ComputeParticleBeta; 0 at upload), outside the
+                      // double-buffered store so that APIC substeps keep it
   float4 *ptile_adj;  // the same for the G2P adjoint (differentiable mode)
   ColliderDev *colliders;  // kMaxColliders entries (device)
   int keep_order;     // differentiable mode: G2P writes each particle to its own slot
@@ -196,8 +203,20 @@ struct DevPtrs {
   int num_sms;
   int grid_p2g, grid_g2p;  // persistent grids: SMs x resident CTAs per SM
   int grid_sort, grid_stream, g2p_threads;
+  int transfer;                      // MPM_TRANSFER_* (host copy of SimParams::transfer)
+  int grid_p2g_flip, grid_g2p_flip;  // persistent grids of the FLIP transfer kernels
   LaunchConfig launch;
 };
+
+// flip.cu: the FLIP / AFLIP transfers (the launch_* functions of transfer.cu
+// dispatch to them when d.transfer is not APIC)
+void configure_flip_launches(DevPtrs &d);
+void launch_p2g_flip(const DevPtrs &d, int cur, cudaStream_t s);
+void launch_grid_gather_flip(const DevPtrs &d, int mode, cudaStream_t s);
+void launch_grid_update_flip(const DevPtrs &d, int mode, cudaStream_t s);
+void launch_g2p_flip(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s);
+// ComputeParticleBeta: collider -1 (volume criterion only) or a collider id
+void launch_particle_beta(const DevPtrs &d, int cur, float dt, int collider, cudaStream_t s);
 
 // partition.cu
 void launch_bin(const DevPtrs &d, int cur, cudaStream_t s);
@@ -250,6 +269,8 @@ void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *la
                      cudaStream_t s);
 // writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
 void launch_egest(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s);
+void launch_egest_channel(const DevPtrs &d, int cur, int ch, float *dst, long long n,
+                          cudaStream_t s);
 
 #ifdef __CUDACC__
 // scene of a (global) directory index: the last scene whose slice starts at

@@ -165,6 +165,13 @@ void attach_boundary(const std::shared_ptr<MpmContext> &ctx, ZenoBoundary &b) {
   b.collider_id = id;
 }
 
+// MakeZSGrid "transfer" -> MPM_TRANSFER_*
+int32_t transfer_of(const ZenoGrid &g) {
+  if (g.transferScheme == "flip") return MPM_TRANSFER_FLIP;
+  if (g.transferScheme == "aflip") return MPM_TRANSFER_AFLIP;
+  return MPM_TRANSFER_APIC;
+}
+
 std::shared_ptr<MpmContext> bound_ctx(const std::shared_ptr<ZenoPartition> &p, const char *node) {
   if (!p->ctx)
     throw std::runtime_error(std::string(node) +
@@ -332,9 +339,12 @@ struct MakeZSGrid : INode {
     auto grid = std::make_shared<ZenoGrid>();
     grid->dx = get_input2<float>("dx");
     grid->transferScheme = get_input2<std::string>("transfer");
-    if (grid->transferScheme != "apic")
-      throw std::runtime_error("unrecognized transfer scheme [" + grid->transferScheme +
-                               "] (this backend implements apic)");
+    const std::string &ts = grid->transferScheme;
+    if (ts == "boundary")
+      throw std::runtime_error("boundary grids (transfer [boundary]) are not implemented by this "
+                               "backend");
+    if (ts != "apic" && ts != "flip" && ts != "aflip")
+      throw std::runtime_error("unrecognized transfer scheme [" + ts + "]");
     set_output("ZSGrid", grid);
   }
 };
@@ -360,6 +370,7 @@ struct ZSPartitionForZSParticles : INode {
       throw std::runtime_error("ZSGrid dx differs from the dx of the particles' model");
     table->ctx = pars->ctx;
     grid->ctx = pars->ctx;
+    check(mpm_set_transfer(pars->ctx->h, transfer_of(*grid)), "mpm_set_transfer");
     check(mpm_partition(pars->ctx->h), "mpm_partition");
     table->rebuilt = true;
     set_output("ZSPartition", table);
@@ -667,7 +678,38 @@ ZENDEFNODE(StepZSBoundary, {
                                {"MPM"},
                            });
 
-/// ZSGridToZSParticle (Transfer.cu:1069-1173), APIC transfer
+/// ComputeParticleBeta (Boundary.cu:172-516): beta for the AFLIP position
+/// update.  With a level-set ZSBoundary, particles that at x + dt v are
+/// inside it and move into it get 0; otherwise 0.5 where det F > 1, else 0.
+/// A ZSBoundary of box walls (no level set) gives the volume criterion only;
+/// boundary grids (transfer "boundary") are not implemented.
+struct ComputeParticleBeta : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    auto ctx = pars->ctx;
+    int32_t collider = -1;
+    if (has_input<ZenoGrid>("ZSBoundary(Grid)"))
+      throw std::runtime_error("ComputeParticleBeta: boundary grids are not implemented; pass a "
+                               "level-set ZSBoundary");
+    if (has_input<ZenoBoundary>("ZSBoundary(Grid)")) {
+      auto b = get_input<ZenoBoundary>("ZSBoundary(Grid)");
+      if (b->ls) {
+        attach_boundary(ctx, *b);
+        collider = b->collider_id;
+      }
+    }
+    check(mpm_compute_particle_beta(ctx->h, get_dt(*this), collider), "mpm_compute_particle_beta");
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(ComputeParticleBeta, {
+                                    {"ZSParticles", "ZSPartition", "ZSBoundary(Grid)", "dt"},
+                                    {"ZSParticles"},
+                                    {},
+                                    {"MPM"},
+                                });
+
+/// ZSGridToZSParticle (Transfer.cu:1069-1173)
 struct ZSGridToZSParticle : INode {
   void apply() override {
     auto grid = get_input<ZenoGrid>("ZSGrid");
@@ -822,6 +864,10 @@ struct ZSMPMSubstep : INode {
     // device (b += db/dt dt, s += ds/dt dt at the start of each substep)
     if (has_input<ZenoBoundary>("ZSCollider"))
       attach_boundary(ctx, *get_input<ZenoBoundary>("ZSCollider"));
+    // the transfer scheme of a MakeZSGrid (default APIC)
+    if (has_input<ZenoGrid>("ZSGrid"))
+      check(mpm_set_transfer(ctx->h, transfer_of(*get_input<ZenoGrid>("ZSGrid"))),
+            "mpm_set_transfer");
     check(mpm_substep(ctx->h, get_dt(*this), get_input2<int>("substeps")), "mpm_substep");
     mpm_stats st{};
     check(mpm_get_stats(ctx->h, &st), "mpm_get_stats");
@@ -834,6 +880,7 @@ ZENDEFNODE(ZSMPMSubstep, {
                              {"ZSParticles",
                               "ZSBoundary",
                               "ZSCollider",
+                              "ZSGrid",
                               "dt",
                               {"float", "gravity", "-9.8"},
                               "Accel",

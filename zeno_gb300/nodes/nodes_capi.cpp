@@ -79,7 +79,8 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       float density, float ppc, const char *bc_type, int32_t bc_thickness,
                       float dt, float gravity, int32_t substeps, float *out_x, float *out_v,
                       float *out_max_vel_sqr, char *err, int64_t err_cap,
-                      const char *ls_shape, const float *ls, const char *ls_type) {
+                      const char *ls_shape, const float *ls, const char *ls_type,
+                      const char *transfer) {
   using namespace zeno;
   try {
     Graph g;
@@ -111,6 +112,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
     g.addNode("MakeZSPartition", "table");
     g.addNode("MakeZSGrid", "grid");
     g.setNodeInput("grid", "dx", num(dx));
+    g.setNodeInput("grid", "transfer", str(transfer ? transfer : "apic"));
     g.addNode("ToZSBoundary", "bnd");
     g.setNodeInput("bnd", "type", str(bc_type));
     g.setNodeInput("bnd", "dx", num(dx));
@@ -146,6 +148,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("step", "ZSParticles", "pars", "ZSParticles");
       g.bindNodeInput("step", "ZSBoundary", "bnd", "ZSBoundary");
       if (collider) g.bindNodeInput("step", "ZSCollider", "lsb", "ZSBoundary");
+      g.bindNodeInput("step", "ZSGrid", "grid", "ZSGrid");
       g.setNodeInput("step", "dt", dtobj);
       g.setNodeInput("step", "gravity", num(gravity));
       g.setNodeInput("step", "substeps", inum(substeps));

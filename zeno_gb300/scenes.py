@@ -22,6 +22,8 @@ import numpy as np
 FCR, NHK, STVK, EOS = 0, 1, 2, 3
 PLASTIC_NONE, PLASTIC_NADP = 0, 1
 BC_NONE, BC_STICKY, BC_SLIP, BC_SEPARATE = 0, 1, 2, 3
+# MakeZSGrid "transfer": APIC, FLIP (PIC/FLIP blend 0.99), affine FLIP
+TRANSFER_APIC, TRANSFER_FLIP, TRANSFER_AFLIP = 0, 1, 2
 
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 _M1 = np.uint64(0xBF58476D1CE4E5B9)
@@ -120,6 +122,7 @@ class Scene:
     materials: list = field(default_factory=list)
     dt: float = 1e-4
     colliders: list = field(default_factory=list)
+    transfer: int = TRANSFER_APIC
 
     @staticmethod
     def unit_box(dx: float, **kw) -> "Scene":
@@ -144,6 +147,7 @@ class Particles:
     mat: np.ndarray
     mu: np.ndarray | None = None
     lam: np.ndarray | None = None
+    beta: np.ndarray | None = None  # AFLIP positional adjustment (ComputeParticleBeta)
 
     @property
     def n(self) -> int:
@@ -157,7 +161,7 @@ class Particles:
                 return np.array(a, dtype=dtype, copy=True)
             return np.array(a, copy=True)
         return Particles(*(c(getattr(self, k)) for k in
-                           ("x", "v", "C", "F", "J", "m", "vol", "mat", "mu", "lam")))
+                           ("x", "v", "C", "F", "J", "m", "vol", "mat", "mu", "lam", "beta")))
 
 
 def lame(E: float, nu: float) -> tuple[float, float]:

@@ -75,7 +75,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
            "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_apply_walls",
-           "mpm_apply_collider", "mpm_g2p", "mpm_return_mapping",
+           "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
+           "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
@@ -122,6 +123,10 @@ def load(path: str = LIB_PATH):
         "mpm_grid_update": ([P, f32, P], i32),
         "mpm_apply_boundary": ([P], i32),
         "mpm_apply_walls": ([P], i32),
+        "mpm_set_transfer": ([P, i32], i32),
+        "mpm_compute_particle_beta": ([P, f32, i32], i32),
+        "mpm_particles_get_attr": ([P, C.c_char_p, P], i32),
+        "mpm_particles_set_attr": ([P, C.c_char_p, P], i32),
         "mpm_apply_collider": ([P, i32], i32),
         "mpm_g2p": ([P, f32], i32),
         "mpm_return_mapping": ([P], i32),
@@ -176,6 +181,29 @@ class Context:
         self.set_gravity(*scene.gravity)
         for c in getattr(scene, "colliders", []) or []:
             self.add_collider(c)
+        if getattr(scene, "transfer", 0):
+            self.set_transfer(scene.transfer)
+
+    def set_transfer(self, scheme: int):
+        """MakeZSGrid "transfer": scenes.TRANSFER_APIC / FLIP / AFLIP."""
+        self._check(self._L.mpm_set_transfer(self.h, int(scheme)), "mpm_set_transfer")
+
+    def compute_particle_beta(self, dt: float, collider: int = -1):
+        """ComputeParticleBeta: the volume criterion, and with a collider id
+        first the level-set test of that collider."""
+        self._check(self._L.mpm_compute_particle_beta(self.h, float(dt), int(collider)),
+                    "mpm_compute_particle_beta")
+
+    def get_attr(self, name: str) -> np.ndarray:
+        out = np.empty(self.n, np.float32)
+        self._check(self._L.mpm_particles_get_attr(self.h, name.encode(), _p(out)),
+                    "mpm_particles_get_attr")
+        return out
+
+    def set_attr(self, name: str, values):
+        vals = _f32(values, (self.n,))
+        self._check(self._L.mpm_particles_set_attr(self.h, name.encode(), _p(vals)),
+                    "mpm_particles_set_attr")
 
     def add_collider(self, c, scene: int = None) -> int:
         """mpm_add_collider for a scenes.Collider; returns its index."""
@@ -266,6 +294,8 @@ class Context:
                                                  _p(m), _p(vol), _p(mat), _p(mu), _p(lam)),
                     "mpm_particles_upload")
         self.n = n
+        if getattr(parts, "beta", None) is not None:
+            self.set_attr("beta", parts.beta)
 
     def upload_raw(self, n, x, v=None, Cm=None, F=None, J=None, m=None, vol=None, mat=None,
                    mu=None, lam=None):
@@ -501,7 +531,7 @@ def load_nodes(path: str = NODES_LIB_PATH):
     L.zsn_run_graph.argtypes = [C.c_int32, C.c_int64, P, P, C.c_float, C.c_char_p, C.c_char_p,
                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_char_p,
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
-                                C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p]
+                                C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -522,14 +552,14 @@ def node_descriptors() -> dict:
 
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
-                   fused=False, levelset=None):
+                   fused=False, levelset=None, transfer="apic"):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
     second ApplyBoundaryOnZSGrid every substep, in the fused graph as
     ZSMPMSubstep's ZSCollider: shape ("sphere" | "plane"), dx, center,
     radius, height, extent, translation, translation_rate, scale, scale_rate,
-    ypr, type."""
+    ypr, type.  transfer: MakeZSGrid "transfer" (apic, flip, aflip)."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -552,7 +582,7 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     rc = L.zsn_run_graph(1 if fused else 0, n, _p(x), _p(v), dx, type.encode(),
                          plasticity.encode(), E, nu, density, ppc, bc.encode(), thickness, dt,
                          gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024, shape,
-                         _p(lsp) if lsp is not None else None, lst)
+                         _p(lsp) if lsp is not None else None, lst, transfer.encode())
     if rc != 0:
         raise RuntimeError(err.value.decode())
     return ox, ov, float(vmax[0])
