@@ -270,6 +270,82 @@ def collider_form(zsmpm, steps: int, dev: int):
             "status": st["status"]}
 
 
+def transfer_form(zsmpm, steps: int, dev: int, scheme: int):
+    """The plain four-material scene with the FLIP (0.99 blend) or affine
+    FLIP transfer (MakeZSGrid transfer = flip | aflip), timed like the
+    headline; plus a 3-substep sample for the parity check."""
+    import torch
+    scene, parts = make_workload()
+    scene.transfer = scheme
+    stream = torch.cuda.Stream(device=dev)
+    ctx = zsmpm.Context(scene, max_particles=parts.n, device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ctx.upload(parts)
+    ctx.substep(scene.dt, 3)
+    check = ctx.download(("x", "v"))
+    ctx.upload(parts)
+    ctx.substep(scene.dt, 5)
+    ctx.sync()
+    e0.record(stream)
+    ctx.substep(scene.dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ctx.sync()
+    st = ctx.stats()
+    stage = [ctx.substep_timed(scene.dt) for _ in range(10)]
+    ctx.sync()
+    ctx.close()
+    name = {1: "flip", 2: "aflip"}[scheme]
+    return {"workload": f"plain 2,097,152-particle four-material scene, transfer={name}",
+            "value": parts.n * steps / (ms * 1e-3), "unit": METRIC, "steps": steps,
+            "ms_per_step": ms / steps,
+            "stage_ms": {k: round(statistics.mean(r[k] for r in stage), 5) for k in stage[0]},
+            "status": st["status"],
+            "_check": (scene, parts, 3, check["x"], check["v"])}
+
+
+def frame_output_form(zsmpm, dev: int, frames: int = 6, per_frame: int = 100):
+    """Frame write-back of the plain 2M scene: `frames` frames of
+    `per_frame` substeps, each frame's x and v written to page-locked host
+    arrays -- synchronously (device reorder + copy, then the next frame) and
+    asynchronously (mpm_frame_begin: snapshot, copy overlapped with the next
+    frame's substeps) -- wall time of the whole loop."""
+    import torch
+    scene, parts = make_workload()
+    n = parts.n
+    x = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    v = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    ctx = zsmpm.Context(scene, max_particles=n, device=dev)
+    out = {}
+    for mode in ("sync", "async"):
+        ctx.upload(parts)
+        ctx.substep(scene.dt, 5)
+        ctx.frame_begin(x, v)
+        ctx.frame_wait()
+        ctx.sync()
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            ctx.substep(scene.dt, per_frame)
+            if mode == "sync":
+                ctx.download_raw(x, v)
+            else:
+                ctx.frame_begin(x, v)
+        ctx.frame_wait()
+        ctx.sync()
+        out[mode] = time.perf_counter() - t0
+    ctx.close()
+    return {"workload": f"plain 2,097,152-particle scene, {frames} frames x {per_frame} substeps, "
+                        "x and v of every frame to pinned host memory",
+            "value": n * frames * per_frame / out["async"], "unit": METRIC,
+            "sync_value": n * frames * per_frame / out["sync"],
+            "d2h_bytes_per_frame": x.nbytes + v.nbytes,
+            "ms_per_frame_async": 1e3 * out["async"] / frames,
+            "ms_per_frame_sync": 1e3 * out["sync"] / frames}
+
+
 def differentiable_form(zsmpm, dev: int, steps: int = 64, ckpt: int = 16):
     """The differentiable form: 65,536 fixed-corotated particles at dx = 1/128
     (E ~ U[3e4, 1e5] per particle), 64 substeps with a checkpoint every 16,
@@ -458,8 +534,9 @@ def rel_l2(a, b):
 def cpu_baseline(parts, scene, checks=None, target_s: float = 10.0):
     """FP32 OpenMP restatement (oracle/) on all host cores, bounded sample;
     then, as the checker, the FP64 oracle on the GPU samples in `checks`
-    (plain: the bench scene after a few substeps; batched: two scenes of the
-    batch), giving the relative L2 error of positions and velocities."""
+    (plain, flip, aflip: the bench scene after a few substeps; batched: two
+    scenes of the batch), giving the relative L2 error of positions and
+    velocities."""
     from oracle import oracle
     oracle.build()
     parity = {}
@@ -657,6 +734,11 @@ def run_gpu(args):
     if not args.no_forms:
         forms["batched"] = batched_form(zsmpm, max(10, min(args.steps, 100)), dev)
         forms["collider"] = collider_form(zsmpm, max(10, min(args.steps, 500)), dev)
+        from zeno_gb300 import scenes as _S
+        forms["flip"] = transfer_form(zsmpm, max(10, min(args.steps, 500)), dev, _S.TRANSFER_FLIP)
+        forms["aflip"] = transfer_form(zsmpm, max(10, min(args.steps, 500)), dev,
+                                       _S.TRANSFER_AFLIP)
+        forms["frame_output"] = frame_output_form(zsmpm, dev)
         forms["fwd_bwd"] = differentiable_form(zsmpm, dev)
         forms["fwd_bwd_sand_16M"] = sand_form(zsmpm, dev)
     if rank != 0:
@@ -665,6 +747,10 @@ def run_gpu(args):
             pg.destroy_process_group()
         return 0
     checks = {"plain": (scene, parts, check_steps, plain_out["x"], plain_out["v"])}
+    for name in ("flip", "aflip"):
+        tchk = forms.get(name, {}).pop("_check", None)
+        if tchk:
+            checks[name] = tchk
     bchk = forms.get("batched", {}).pop("_check", None)
     if bchk:
         for k, (sc, pt, gx, gv) in enumerate(bchk["scenes"]):

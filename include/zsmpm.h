@@ -203,10 +203,25 @@ int32_t mpm_particles_set_lame(mpm_ctx *ctx, const float *mu, const float *lam);
  * host arrays in the upload order; NULL skips a channel. */
 int32_t mpm_particles_download(mpm_ctx *ctx, float *x, float *v, float *C, float *F, float *J);
 /* One per-particle attribute in the upload order, by its channel name in the
- * reference's particle store (Generation.cpp:868-903): get "beta", "m",
- * "vol", "J", "mu", "lam"; set "beta" (host arrays of n floats). */
+ * reference's particle store (Generation.cpp:868-903): get "beta", "vms",
+ * "m", "vol", "J", "mu", "lam"; set "beta" (host arrays of n floats). */
 int32_t mpm_particles_get_attr(mpm_ctx *ctx, const char *name, float *values);
 int32_t mpm_particles_set_attr(mpm_ctx *ctx, const char *name, const float *values);
+/* ComputeVonMises (Generation.cu:1873-1920): the von Mises stress of the
+ * StVK-Hencky particles (other models keep their value, 0 at upload) from
+ * the principal Cauchy stresses c_i = (2 mu e_i + lam sum e) / J, e_i = ln s_i:
+ * vms = sqrt(((c0-c1)^2 + (c1-c2)^2 + (c2-c0)^2) / 2), or log10(vms + 1)
+ * with by_log1p (the node's default); read back as the attribute "vms". */
+int32_t mpm_compute_von_mises(mpm_ctx *ctx, int32_t by_log1p);
+/* UpdatePrimitiveFromZSParticles (Generation.cu:1088-1158) off the critical
+ * path: mpm_frame_begin snapshots x and v in upload order on the device (on
+ * the context's stream, after the work enqueued so far) and copies the
+ * snapshot to x, v (n x 3 floats each; page-locked memory makes the copy
+ * asynchronous) on a second stream, so substeps enqueued afterwards overlap
+ * the copy; mpm_frame_wait blocks until it has landed.  One frame in flight:
+ * a second mpm_frame_begin first waits for the previous one. */
+int32_t mpm_frame_begin(mpm_ctx *ctx, float *x, float *v);
+int32_t mpm_frame_wait(mpm_ctx *ctx);
 
 /* MakeZSGrid "transfer" of the context's grid: MPM_TRANSFER_APIC (default),
  * MPM_TRANSFER_FLIP or MPM_TRANSFER_AFLIP (the grid gains the vstar channel,

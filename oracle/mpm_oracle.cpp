@@ -842,6 +842,42 @@ int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v, float
                     stats);
 }
 
+// ComputeVonMises (Generation.cu:1873-1920): singular values of F from the
+// eigenvalues of F^T F (Jacobi), Hencky strains e_i = ln s_i, principal
+// Cauchy stresses c_i = (2 mu e_i + lam sum e) / (s0 s1 s2) of the
+// StVK-Hencky model (Klar et al. 2016), vms = sqrt(((c0 - c1)^2 + (c1 - c2)^2
+// + (c2 - c0)^2) / 2), log10(vms + 1) with by_log1p.
+int32_t orc_von_mises_f64(const orc_scene *scene, int64_t n, const double *F, const int32_t *mat,
+                          int32_t by_log1p, double *vms) {
+  if (!scene || n < 0 || !vms) return ORC_ERR_INVALID;
+  for (int64_t p = 0; p < n; ++p) {
+    if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
+    const Params<double> mp = material_params<double>(scene->materials[mat[p]]);
+    if (mp.type != ORC_STVK) continue;
+    const double *Fp = F + 9 * p;
+    double A[9], w[3], Q[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        A[i * 3 + j] = 0;
+        for (int k = 0; k < 3; ++k) A[i * 3 + j] += Fp[k * 3 + i] * Fp[k * 3 + j];
+      }
+    sym_eig3<double>(A, w, Q, kSweeps);
+    double e[3], tr = 0;
+    for (int i = 0; i < 3; ++i) {
+      e[i] = 0.5 * std::log(w[i]);
+      tr += e[i];
+    }
+    const double J = std::exp(tr);
+    double c[3];
+    for (int i = 0; i < 3; ++i) c[i] = (2.0 * mp.mu * e[i] + mp.lam * tr) / J;
+    double s2 = 0;
+    for (int d = 0; d < 3; ++d) s2 += (c[d] - c[(d + 1) % 3]) * (c[d] - c[(d + 1) % 3]);
+    const double v = std::sqrt(0.5 * s2);
+    vms[p] = by_log1p ? std::log10(v + 1.0) : v;
+  }
+  return ORC_OK;
+}
+
 // ComputeParticleBeta (Boundary.cu:172-516) without a boundary (:490-499)
 // and with a level-set boundary (determine_beta_sdf, :285-315): at
 // x + dt v, a particle inside the collider moving into it, (v - v_obj) . n

@@ -134,6 +134,13 @@ int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v,
  * det F > 1, else 0; J for the equation-of-state fluid); with the index of
  * one of the scene's colliders, first the level-set test at x + dt v
  * (beta = 0 where the particle moves into the collider). */
+/* ComputeVonMises (Generation.cu:1873-1920) in double: for the StVK-Hencky
+ * particles vms = sqrt(sum_d (c_d - c_{d+1})^2 / 2) of the principal Cauchy
+ * stresses c_i = (2 mu e_i + lam sum e) / J, e_i = ln s_i (s the singular
+ * values of F), log10(vms + 1) with by_log1p; other particles keep vms. */
+int32_t orc_von_mises_f64(const orc_scene *scene, int64_t n, const double *F,
+                          const int32_t *mat, int32_t by_log1p, double *vms);
+
 int32_t orc_particle_beta_f64(const orc_scene *scene, int64_t n, const double *x,
                               const double *v, const double *F, const double *J,
                               const int32_t *mat, double dt, int32_t collider,

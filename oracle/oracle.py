@@ -77,6 +77,8 @@ def lib():
         L.orc_particle_beta_f64.argtypes = [C.POINTER(OrcScene), C.c_int64, P, P, P, P, P,
                                             C.c_double, C.c_int32, P]
         L.orc_particle_beta_f64.restype = C.c_int32
+        L.orc_von_mises_f64.argtypes = [C.POINTER(OrcScene), C.c_int64, P, P, C.c_int32, P]
+        L.orc_von_mises_f64.restype = C.c_int32
         L.orc_sym_eig3.argtypes = [P, P, P]
         L.orc_kirchhoff.argtypes = [C.POINTER(OrcMaterial), P, C.c_double, P]
         L.orc_kirchhoff.restype = C.c_int32
@@ -189,6 +191,20 @@ def particle_beta(scene, parts, dt: float | None = None, collider: int = -1) -> 
     if rc != 0:
         raise RuntimeError(f"oracle beta failed with status {rc}")
     return beta
+
+
+def von_mises(scene, parts, by_log1p: bool = True, vms: np.ndarray | None = None) -> np.ndarray:
+    """ComputeVonMises in FP64 (upload order); particles of other models keep
+    the value in `vms` (default 0)."""
+    F = np.ascontiguousarray(parts.F, dtype=np.float64)
+    mat = np.ascontiguousarray(parts.mat, dtype=np.int32)
+    out = np.zeros(parts.n) if vms is None else np.array(vms, dtype=np.float64)
+    h = _SceneHolder(scene)
+    rc = lib().orc_von_mises_f64(C.byref(h.s), parts.n, _ptr(F), _ptr(mat), int(by_log1p),
+                                 _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle von Mises failed with status {rc}")
+    return out
 
 
 def sym_eig3(A: np.ndarray):

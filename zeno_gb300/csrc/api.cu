@@ -61,6 +61,11 @@ struct mpm_ctx {
   std::vector<SceneParams> scenes;
   int n_materials = 0;
   bool differentiable = false;  // every material has an adjoint
+  // asynchronous frame output: device snapshot, copy stream, events
+  float *frame_buf = nullptr;
+  cudaStream_t frame_stream = nullptr;
+  cudaEvent_t frame_ready = nullptr, frame_done = nullptr;
+  bool frame_pending = false;
 };
 
 namespace {
@@ -172,7 +177,7 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   launch_p2g(c->d, cur, c->stream);
   mark(MPM_STAGE_GRID_UPDATE);
   launch_grid_gather(c->d, 3, c->stream);
-  if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
+  if (!c->colliders.empty()) launch_apply_colliders_listed(c->d, c->stream);
   mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, 1, c->stream);
   mark(MPM_NUM_STAGES);
@@ -311,7 +316,8 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
       (rc = dalloc(c, &d.tile_sums, (size_t)3 * d.ntiles)) || (rc = dalloc(c, &d.cnt, 1)) ||
       (rc = dalloc(c, &d.prm, 1)) || (rc = dalloc(c, &d.scn, n_scenes)) ||
       (rc = dalloc(c, &d.mats, kMaxMaterials)) || (rc = dalloc(c, &d.colliders, kMaxColliders)) ||
-      (rc = dalloc(c, &d.beta, cap)))
+      (rc = dalloc(c, &d.beta, cap)) || (rc = dalloc(c, &d.vms, cap)) ||
+      (rc = dalloc(c, &d.near_gb, capg)))
     return bail(rc);
   if (cudaMallocHost(&c->h_cnt, sizeof(Counters)) != cudaSuccess)
     return bail(fail(MPM_ERR_CUDA, "cudaMallocHost"));
@@ -323,6 +329,7 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
   cudaMemsetAsync(d.perm, 0, (size_t)cap * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.pkey, 0, (size_t)cap * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.beta, 0, (size_t)cap * sizeof(float), c->stream);
+  cudaMemsetAsync(d.vms, 0, (size_t)cap * sizeof(float), c->stream);
   cudaMemsetAsync(d.dir_count, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_fill, 0, ndir * sizeof(int32_t), c->stream);
   cudaMemsetAsync(d.dir_gb, 0xff, ndir * sizeof(int32_t), c->stream);
@@ -374,6 +381,12 @@ int32_t mpm_ctx_destroy(mpm_ctx *c) {
     if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
   for (cudaEvent_t e : c->events)
     if (e) cudaEventDestroy(e);
+  if (c->frame_stream) {
+    cudaStreamSynchronize(c->frame_stream);
+    cudaStreamDestroy(c->frame_stream);
+  }
+  if (c->frame_ready) cudaEventDestroy(c->frame_ready);
+  if (c->frame_done) cudaEventDestroy(c->frame_done);
   for (void *p : c->allocs) cudaFree(p);
   for (void *p : c->collider_allocs) cudaFree(p);
   if (c->h_cnt) cudaFreeHost(c->h_cnt);
@@ -640,8 +653,10 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
   }
   launch_ingest(c->d, c->cur, src, n, c->stream);
   if ((rc = launch_check("ingest"))) return rc;
-  if (n > 0)  // ToZSParticles: beta = 0 (Generation.cpp:944-966)
+  if (n > 0) {  // ToZSParticles: beta = 0, vms = 0 (Generation.cpp:944-966)
     ZS_CUDA(cudaMemsetAsync(c->d.beta, 0, (size_t)n * sizeof(float), c->stream));
+    ZS_CUDA(cudaMemsetAsync(c->d.vms, 0, (size_t)n * sizeof(float), c->stream));
+  }
   c->prm.n = n;
   c->prm.has_lame = mu ? 1 : 0;
   for (int s = 0; s < ns; ++s) c->scenes[s].p_off = scene_offsets ? scene_offsets[s] : 0;
@@ -725,10 +740,10 @@ int32_t mpm_particles_get_attr(mpm_ctx *c, const char *name, float *values) {
   if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
   const std::string a(name);
   const long long n = c->prm.n;
-  if (a == "beta") {
+  if (a == "beta" || a == "vms") {  // planes by upload index
     if (n > 0)
-      ZS_CUDA(cudaMemcpyAsync(values, c->d.beta, n * sizeof(float), cudaMemcpyDeviceToHost,
-                              c->stream));
+      ZS_CUDA(cudaMemcpyAsync(values, a == "beta" ? c->d.beta : c->d.vms, n * sizeof(float),
+                              cudaMemcpyDeviceToHost, c->stream));
     ZS_CUDA(cudaStreamSynchronize(c->stream));
     return MPM_OK;
   }
@@ -761,6 +776,51 @@ int32_t mpm_particles_set_attr(mpm_ctx *c, const char *name, const float *values
     ZS_CUDA(cudaMemcpyAsync(c->d.beta, values, n * sizeof(float), cudaMemcpyHostToDevice,
                             c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
+int32_t mpm_compute_von_mises(mpm_ctx *c, int32_t by_log1p) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (c->prm.n == 0) return MPM_OK;
+  if ((rc = push_params(c))) return rc;
+  launch_von_mises(c->d, c->cur, by_log1p ? 1 : 0, c->stream);
+  return launch_check("von Mises");
+}
+
+int32_t mpm_frame_wait(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->frame_pending) return MPM_OK;
+  ZS_CUDA(cudaEventSynchronize(c->frame_done));
+  c->frame_pending = false;
+  return MPM_OK;
+}
+
+int32_t mpm_frame_begin(mpm_ctx *c, float *x, float *v) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = mpm_frame_wait(c))) return rc;  // the snapshot buffer is free again
+  const long long n = c->prm.n;
+  if (n == 0) return MPM_OK;
+  if (!c->frame_buf) {
+    if ((rc = dalloc(c, &c->frame_buf, (size_t)6 * c->d.cap))) return rc;
+    ZS_CUDA(cudaStreamCreateWithFlags(&c->frame_stream, cudaStreamNonBlocking));
+    ZS_CUDA(cudaEventCreateWithFlags(&c->frame_ready, cudaEventDisableTiming));
+    ZS_CUDA(cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming));
+  }
+  launch_snapshot_xv(c->d, c->cur, c->frame_buf, n, c->stream);
+  if ((rc = launch_check("frame snapshot"))) return rc;
+  ZS_CUDA(cudaEventRecord(c->frame_ready, c->stream));
+  ZS_CUDA(cudaStreamWaitEvent(c->frame_stream, c->frame_ready, 0));
+  if (x)
+    ZS_CUDA(cudaMemcpyAsync(x, c->frame_buf, 3 * n * sizeof(float), cudaMemcpyDeviceToHost,
+                            c->frame_stream));
+  if (v)
+    ZS_CUDA(cudaMemcpyAsync(v, c->frame_buf + 3 * n, 3 * n * sizeof(float),
+                            cudaMemcpyDeviceToHost, c->frame_stream));
+  ZS_CUDA(cudaEventRecord(c->frame_done, c->frame_stream));
+  c->frame_pending = true;
   return MPM_OK;
 }
 

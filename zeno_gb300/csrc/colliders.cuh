@@ -167,6 +167,31 @@ __device__ __forceinline__ void apply_colliders_adjoint(const DevPtrs &d, int nc
   }
 }
 
+// does the node box [I0, I0 + 3] dx of a grid block meet the world box of
+// one of the colliders k0..k1-1 of the scene
+__device__ __forceinline__ bool block_near_colliders(const DevPtrs &d, int k0, int k1, int scene,
+                                                     const int (&I0)[3], float dx) {
+  const float lo[3] = {(float)I0[0] * dx, (float)I0[1] * dx, (float)I0[2] * dx};
+  const float hi[3] = {(float)(I0[0] + 3) * dx, (float)(I0[1] + 3) * dx, (float)(I0[2] + 3) * dx};
+  for (int k = k0; k < k1; ++k) {
+    const ColliderDev &c = d.colliders[k];
+    if (!collider_in_scene(c, scene) || c.type == MPM_BC_NONE) continue;
+    if (hi[0] >= c.lo[0] && lo[0] <= c.hi[0] && hi[1] >= c.lo[1] && lo[1] <= c.hi[1] &&
+        hi[2] >= c.lo[2] && lo[2] <= c.hi[2])
+      return true;
+  }
+  return false;
+}
+
+// the gather's note of a grid block near a collider (its origin I0)
+__device__ __forceinline__ void note_near_block(const DevPtrs &d, int nc, int scene,
+                                                const int (&I0)[3], float dx, int gb) {
+  if (nc > 0 && block_near_colliders(d, 0, nc, scene, I0, dx)) {
+    const int i = atomicAdd(&d.cnt->n_near, 1);
+    if (i < d.cap_gblocks) d.near_gb[i] = gb;
+  }
+}
+
 // b += db/dt dt, s += ds/dt dt for every collider (StepZSBoundary)
 __device__ __forceinline__ void step_colliders(const DevPtrs &d, int nc, float dt) {
   for (int k = 0; k < nc; ++k) {

@@ -458,10 +458,13 @@ __global__ void __launch_bounds__(64 * kFGatherBlocks) k_grid_gather_flip(DevPtr
         bk = d.dir_bk[gdir - (o0 * dy + o1) * dz - o2];
       sbk[grp][cell] = bk;
       if (cell == 0) {
-        sorg[grp][0] = (c0 + S.block_lo[0]) * 4;
-        sorg[grp][1] = (c1 + S.block_lo[1]) * 4;
-        sorg[grp][2] = (c2 + S.block_lo[2]) * 4;
+        const int I0[3] = {(c0 + S.block_lo[0]) * 4, (c1 + S.block_lo[1]) * 4,
+                           (c2 + S.block_lo[2]) * 4};
+        sorg[grp][0] = I0[0];
+        sorg[grp][1] = I0[1];
+        sorg[grp][2] = I0[2];
         sorg[grp][3] = sc;
+        if (mode & 2) note_near_block(d, P.n_colliders, sc, I0, S.dx, gb);
       }
     }
     __syncthreads();

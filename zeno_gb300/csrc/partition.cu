@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (blockIdx.x == 0 && tid == 0) {
     d.cnt->max_vel_sqr_bits = 0u;
+    d.cnt->n_near = 0;
     // the fused substep moves the colliders to this substep's time
     if (d.prm->auto_step) step_colliders(d, d.prm->n_colliders, d.prm->dt);
   }

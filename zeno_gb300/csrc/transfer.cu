@@ -368,10 +368,13 @@ __global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, i
         bk = d.dir_bk[gdir - (o0 * dy + o1) * dz - o2];
       sbk[grp][cell] = bk;
       if (cell == 0) {
-        sorg[grp][0] = (c0 + S.block_lo[0]) * 4;
-        sorg[grp][1] = (c1 + S.block_lo[1]) * 4;
-        sorg[grp][2] = (c2 + S.block_lo[2]) * 4;
+        const int I0[3] = {(c0 + S.block_lo[0]) * 4, (c1 + S.block_lo[1]) * 4,
+                           (c2 + S.block_lo[2]) * 4};
+        sorg[grp][0] = I0[0];
+        sorg[grp][1] = I0[1];
+        sorg[grp][2] = I0[2];
         sorg[grp][3] = sc;
+        if (mode & 2) note_near_block(d, P.n_colliders, sc, I0, S.dx, gb);
       }
     }
     __syncthreads();
@@ -866,17 +869,19 @@ void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
 
 // ApplyBoundaryOnZSGrid with level sets: collider `id` (-1: every collider,
 // in id order) on the active nodes, after the box walls; its own pass,
-// launched only when colliders exist.  One warp per grid block: the warp
-// finds the block's node box once and skips the block unless the box meets
-// the world box of one of the colliders, so only blocks near a collider read
-// the grid (two nodes per lane).
-__global__ void k_apply_colliders(DevPtrs d, int id) {
+// launched only when colliders exist.  One warp per grid block, two nodes
+// per lane.  Listed form (the fused substep): the blocks the gather noted
+// as near a collider.  Full form (the stage path, whose colliders may move
+// between gather and boundary): every block, skipped by the warp unless its
+// node box meets the world box of a collider.
+__global__ void k_apply_colliders(DevPtrs d, int id, int listed) {
   const int nc = d.prm->n_colliders;
   const int k0 = id < 0 ? 0 : id, k1 = id < 0 ? nc : min(id + 1, nc);
-  const int ng = min(d.cnt->n_gblocks, d.cap_gblocks);
+  const int ng = listed ? min(d.cnt->n_near, d.cap_gblocks) : min(d.cnt->n_gblocks, d.cap_gblocks);
   const int lane = threadIdx.x & 31;
   const int nw = gridDim.x * (blockDim.x >> 5);
-  for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < ng; gb += nw) {
+  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < ng; w += nw) {
+    const int gb = listed ? d.near_gb[w] : w;
     const int gdir = d.gb_dir[gb];
     const int sc = scene_of_dir(d, gdir);
     const SceneParams &S = d.scn[sc];
@@ -884,16 +889,7 @@ __global__ void k_apply_colliders(DevPtrs d, int id) {
     const int ldir = gdir - S.dir_off;
     const int I0[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4, (((ldir / dz) % dy) + S.block_lo[1]) * 4,
                        ((ldir % dz) + S.block_lo[2]) * 4};
-    const float lo[3] = {(float)I0[0] * S.dx, (float)I0[1] * S.dx, (float)I0[2] * S.dx};
-    const float hi[3] = {(float)(I0[0] + 3) * S.dx, (float)(I0[1] + 3) * S.dx, (float)(I0[2] + 3) * S.dx};
-    bool near = false;
-    for (int k = k0; k < k1 && !near; ++k) {
-      const ColliderDev &c = d.colliders[k];
-      if (!collider_in_scene(c, sc) || c.type == MPM_BC_NONE) continue;
-      near = hi[0] >= c.lo[0] && lo[0] <= c.hi[0] && hi[1] >= c.lo[1] && lo[1] <= c.hi[1] &&
-             hi[2] >= c.lo[2] && lo[2] <= c.hi[2];
-    }
-    if (!near) continue;
+    if (!listed && !block_near_colliders(d, k0, k1, sc, I0, S.dx)) continue;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int cell = lane + 32 * h;
@@ -920,7 +916,11 @@ __global__ void k_apply_colliders(DevPtrs d, int id) {
 }
 
 void launch_apply_colliders(const DevPtrs &d, int id, cudaStream_t s) {
-  k_apply_colliders<<<d.grid_stream, 256, 0, s>>>(d, id);
+  k_apply_colliders<<<d.grid_stream, 256, 0, s>>>(d, id, 0);
+}
+
+void launch_apply_colliders_listed(const DevPtrs &d, cudaStream_t s) {
+  k_apply_colliders<<<d.num_sms * 4, 256, 0, s>>>(d, -1, 1);
 }
 
 // StepZSBoundary on collider `id` (-1: every collider)

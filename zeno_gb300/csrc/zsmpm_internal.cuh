@@ -88,7 +88,8 @@ struct Counters {
   unsigned max_vel_sqr_bits;
   int n_binned;
   int bad_material;  // set by the upload check of material ids
-  int pad[2];
+  int n_near;        // grid blocks the fused substep's gather found near a collider
+  int pad;
 };
 
 // Device-resident parameters; the host updates them with one small copy
@@ -191,6 +192,8 @@ struct DevPtrs {
                       // double-buffered store so that APIC substeps keep it
   float4 *ptile_adj;  // the same for the G2P adjoint (differentiable mode)
   ColliderDev *colliders;  // kMaxColliders entries (device)
+  int32_t *near_gb;        // cap_gblocks entries: the grid blocks near a collider
+  float *vms;              // ComputeVonMises per particle, by upload index (0 at upload)
   int keep_order;     // differentiable mode: G2P writes each particle to its own slot
   int planar_x;       // pbuf[0] holds positions as 3 planes of `cap` floats (binning only)
   int32_t *tile_sums;
@@ -218,6 +221,10 @@ void launch_g2p_flip(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaS
 // ComputeParticleBeta: collider -1 (volume criterion only) or a collider id
 void launch_particle_beta(const DevPtrs &d, int cur, float dt, int collider, cudaStream_t s);
 
+// output.cu
+void launch_von_mises(const DevPtrs &d, int cur, int by_log1p, cudaStream_t s);
+void launch_snapshot_xv(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s);
+
 // partition.cu
 void launch_bin(const DevPtrs &d, int cur, cudaStream_t s);
 void launch_scan(const DevPtrs &d, cudaStream_t s);
@@ -236,6 +243,9 @@ void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s);
 // mode bit 1: momentum -> velocity + gravity, bit 2: boundary, on the grid
 void launch_step_colliders(const DevPtrs &d, int id, float dt, cudaStream_t s);
 void launch_apply_colliders(const DevPtrs &d, int id, cudaStream_t s);
+// every collider on the grid blocks the preceding gather listed as near one
+// (the fused substep: colliders stepped before the gather)
+void launch_apply_colliders_listed(const DevPtrs &d, cudaStream_t s);
 void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s);
 // fuse_rm: return mapping in G2P; fuse_bin: bin the new positions for the
 // next partition

@@ -678,6 +678,24 @@ ZENDEFNODE(StepZSBoundary, {
                                {"MPM"},
                            });
 
+/// ComputeVonMises (Generation.cu:1873-1920): the von Mises stress of the
+/// StVK-Hencky particles into their "vms" attribute (log10(vms + 1) by
+/// default).
+struct ComputeVonMises : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const int option = get_param<int>("by_log1p(base10)");
+    check(mpm_compute_von_mises(pars->ctx->h, option), "mpm_compute_von_mises");
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(ComputeVonMises, {
+                                {"ZSParticles"},
+                                {"ZSParticles"},
+                                {{"int", "by_log1p(base10)", "1"}},
+                                {"MPM"},
+                            });
+
 /// ComputeParticleBeta (Boundary.cu:172-516): beta for the AFLIP position
 /// update.  With a level-set ZSBoundary, particles that at x + dt v are
 /// inside it and move into it get 0; otherwise 0.5 where det F > 1, else 0.

@@ -76,7 +76,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_apply_walls",
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
-           "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_g2p", "mpm_return_mapping",
+           "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
+           "mpm_frame_begin", "mpm_frame_wait", "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
@@ -127,6 +128,9 @@ def load(path: str = LIB_PATH):
         "mpm_compute_particle_beta": ([P, f32, i32], i32),
         "mpm_particles_get_attr": ([P, C.c_char_p, P], i32),
         "mpm_particles_set_attr": ([P, C.c_char_p, P], i32),
+        "mpm_compute_von_mises": ([P, i32], i32),
+        "mpm_frame_begin": ([P, P, P], i32),
+        "mpm_frame_wait": ([P], i32),
         "mpm_apply_collider": ([P, i32], i32),
         "mpm_g2p": ([P, f32], i32),
         "mpm_return_mapping": ([P], i32),
@@ -204,6 +208,20 @@ class Context:
         vals = _f32(values, (self.n,))
         self._check(self._L.mpm_particles_set_attr(self.h, name.encode(), _p(vals)),
                     "mpm_particles_set_attr")
+
+    def compute_von_mises(self, by_log1p: bool = True):
+        """ComputeVonMises; the result is the attribute "vms"."""
+        self._check(self._L.mpm_compute_von_mises(self.h, 1 if by_log1p else 0),
+                    "mpm_compute_von_mises")
+
+    def frame_begin(self, x, v):
+        """Asynchronous write-back of x, v (caller-owned float32 (n, 3) arrays,
+        page-locked for an overlapped copy); frame_wait() before reading."""
+        self._frame = (x, v)
+        self._check(self._L.mpm_frame_begin(self.h, _p(x), _p(v)), "mpm_frame_begin")
+
+    def frame_wait(self):
+        self._check(self._L.mpm_frame_wait(self.h), "mpm_frame_wait")
 
     def add_collider(self, c, scene: int = None) -> int:
         """mpm_add_collider for a scenes.Collider; returns its index."""
