@@ -30,6 +30,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -277,8 +278,16 @@ template <class R> inline void particle_base(const R *x, R inv_dx, int32_t *base
 // iteration of ExpandZSPartition over all 26 neighbours).  Particle blocks
 // are sorted by directory index; inside a block particles are ordered by
 // (cell id, particle index), which is the stable order by (block, cell).
+// extra: point sets (cloth vertices and elements) whose blocks and their 26
+// neighbours join the grid blocks without forming particle blocks
+struct PointSet {
+  const double *x;
+  int64_t n;
+};
+
 template <class R>
-int build_partition(const orc_scene &sc, int64_t n, const R *x, Partition &P, int nthreads) {
+int build_partition(const orc_scene &sc, int64_t n, const R *x, Partition &P, int nthreads,
+                    const std::vector<PointSet> &extra = {}) {
   Dir dir;
   for (int d = 0; d < 3; ++d) {
     dir.lo[d] = sc.block_lo[d];
@@ -344,6 +353,21 @@ int build_partition(const orc_scene &sc, int64_t n, const R *x, Partition &P, in
 
   // halo: every particle block and its 26 neighbours
   std::vector<uint8_t> mark(D, 0);
+  for (const PointSet &ps : extra)
+    for (int64_t i = 0; i < ps.n; ++i) {
+      int32_t base[3], bc[3];
+      particle_base(ps.x + 3 * i, 1.0 / double(sc.dx), base);
+      for (int d = 0; d < 3; ++d) {
+        bc[d] = (base[d] >> 2) - dir.lo[d];
+        if (bc[d] < 1 || bc[d] > dir.dims[d] - 2) return ORC_ERR_OUT_OF_DOMAIN;
+      }
+      for (int a = -1; a <= 1; ++a)
+        for (int b = -1; b <= 1; ++b)
+          for (int c = -1; c <= 1; ++c) {
+            const int32_t cn[3] = {bc[0] + a, bc[1] + b, bc[2] + c};
+            mark[dir.index(cn)] = 1;
+          }
+    }
   for (int64_t b = 0; b < nb; ++b) {
     int32_t c[3];
     dir.coords(P.pb_dir[b], c);
@@ -539,11 +563,329 @@ template <class R> struct Sim {
     return &grid[(int64_t(gb) * 64 + cell) * kNG];
   }
 
+  // ---- codimensional cloth (FP64 only) ----
+  //
+  // Gram-Schmidt QR of the columns of F (Jiang et al. 2017, sec. 4): q0 =
+  // f0 / |f0|, q1 the normalised part of f1 orthogonal to q0, q2 = q0 x q1;
+  // R = Q^T F upper triangular with a signed R22 (negative once the element
+  // is inverted through its normal).
+  static void gram_schmidt(const double *F, double *Q, double *Rm) {
+    double f[3][3];
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) f[j][i] = F[i * 3 + j];
+    auto dot = [](const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    double q0[3], q1[3], q2[3];
+    const double r00 = std::sqrt(dot(f[0], f[0]));
+    for (int i = 0; i < 3; ++i) q0[i] = f[0][i] / r00;
+    const double r01 = dot(q0, f[1]);
+    double u[3];
+    for (int i = 0; i < 3; ++i) u[i] = f[1][i] - r01 * q0[i];
+    const double r11 = std::sqrt(dot(u, u));
+    for (int i = 0; i < 3; ++i) q1[i] = u[i] / r11;
+    q2[0] = q0[1] * q1[2] - q0[2] * q1[1];
+    q2[1] = q0[2] * q1[0] - q0[0] * q1[2];
+    q2[2] = q0[0] * q1[1] - q0[1] * q1[0];
+    for (int i = 0; i < 3; ++i) {
+      Q[i * 3 + 0] = q0[i];
+      Q[i * 3 + 1] = q1[i];
+      Q[i * 3 + 2] = q2[i];
+    }
+    for (int i = 0; i < 9; ++i) Rm[i] = 0;
+    Rm[0] = r00;
+    Rm[1] = r01;
+    Rm[2] = dot(q0, f[2]);
+    Rm[4] = r11;
+    Rm[5] = dot(q1, f[2]);
+    Rm[8] = dot(q2, f[2]);
+  }
+
+  // first Piola-Kirchhoff stress of a 2x2 deformation [a b; c d] (the
+  // in-plane part of R): fixed corotated P = 2 mu (F - R) + lam (J - 1) cof F
+  // (R the closest rotation, Stomakhin et al. 2012), Neo-Hookean P = mu (F -
+  // F^-T) + lam ln J F^-T, StVK-Hencky P = U diag((2 mu e_i + lam sum e) /
+  // s_i) V^T, e_i = ln s_i (Klar et al. 2016).
+  static void first_piola_2d(int model, double mu, double lam, const double *F2, double *P2) {
+    const double a = F2[0], b = F2[1], c = F2[2], d = F2[3];
+    const double J = a * d - b * c;
+    const double cof[4] = {d, -c, -b, a};  // J F^-T
+    if (model == ORC_FCR) {
+      const double p = a + d, q = c - b, nn = std::sqrt(p * p + q * q);
+      const double Rr[4] = {p / nn, -q / nn, q / nn, p / nn};
+      for (int i = 0; i < 4; ++i) P2[i] = 2 * mu * (F2[i] - Rr[i]) + lam * (J - 1) * cof[i];
+      return;
+    }
+    if (model == ORC_NHK) {
+      for (int i = 0; i < 4; ++i) P2[i] = mu * (F2[i] - cof[i] / J) + lam * std::log(J) * cof[i] / J;
+      return;
+    }
+    // StVK-Hencky: P = F V diag((2 mu e_i + lam tr e) / s_i^2) V^T from F^T F = V S^2 V^T
+    const double c00 = a * a + c * c, c01 = a * b + c * d, c11 = b * b + d * d;
+    const double tr = c00 + c11, det = c00 * c11 - c01 * c01;
+    const double disc = std::sqrt(std::max(0.0, 0.25 * tr * tr - det));
+    const double l0 = 0.5 * tr + disc, l1 = 0.5 * tr - disc;
+    double v0[2];
+    if (std::fabs(c01) > 1e-300) {
+      v0[0] = l0 - c11;
+      v0[1] = c01;
+    } else if (c00 >= c11) {
+      v0[0] = 1;
+      v0[1] = 0;
+    } else {
+      v0[0] = 0;
+      v0[1] = 1;
+    }
+    const double nv = std::sqrt(v0[0] * v0[0] + v0[1] * v0[1]);
+    v0[0] /= nv;
+    v0[1] /= nv;
+    const double v1[2] = {-v0[1], v0[0]};
+    const double e0 = 0.5 * std::log(l0), e1 = 0.5 * std::log(l1);
+    const double g0 = (2 * mu * e0 + lam * (e0 + e1)) / l0, g1 = (2 * mu * e1 + lam * (e0 + e1)) / l1;
+    const double S[4] = {g0 * v0[0] * v0[0] + g1 * v1[0] * v1[0], g0 * v0[0] * v0[1] + g1 * v1[0] * v1[1],
+                         g0 * v0[1] * v0[0] + g1 * v1[1] * v1[0], g0 * v0[1] * v0[1] + g1 * v1[1] * v1[1]};
+    P2[0] = a * S[0] + b * S[2];
+    P2[1] = a * S[1] + b * S[3];
+    P2[2] = c * S[0] + d * S[2];
+    P2[3] = c * S[1] + d * S[3];
+  }
+
+  // gradient of the node weight with respect to the particle position
+  void weight_grad(const Stencil &st, int i, int j, int k, double *g) const {
+    const double inv_dx = 1.0 / double(sc.dx);
+    g[0] = st.dw[0][i] * st.w[1][j] * st.w[2][k] * inv_dx;
+    g[1] = st.w[0][i] * st.dw[1][j] * st.w[2][k] * inv_dx;
+    g[2] = st.w[0][i] * st.w[1][j] * st.dw[2][k] * inv_dx;
+  }
+
+  // ZSParticleToZSGrid for the cloth (p2g_surface, Transfer.cu:656-842):
+  // each element scatters its mass and momentum and the normal-direction
+  // force P_c3 (grad W . d_c3) (-vol dt) (type i), and hands the in-plane
+  // force to its vertices as impulses (type ii); then each vertex scatters
+  // its mass, momentum and impulse.  FLIP grids take the forces in vstar.
+  void cloth_p2g(orc_cloth &cl, double dt) {
+    const int tr = sc.transfer;
+    const bool flip_style = tr != ORC_TRANSFER_APIC, affine = tr != ORC_TRANSFER_FLIP;
+    const double dx = sc.dx;
+    std::vector<double> imp(3 * cl.n_verts, 0.0);
+    for (int64_t e = 0; e < cl.n_eles; ++e) {
+      const double *F = cl.eF + 9 * e, *dm = cl.ed + 9 * e, *Di = cl.eDmInv + 9 * e;
+      double Q[9], Rm[9];
+      gram_schmidt(F, Q, Rm);
+      const double R2[4] = {Rm[0], Rm[1], Rm[3], Rm[4]};
+      double P2[4];
+      first_piola_2d(cl.model, cl.emu[e], cl.elam[e], R2, P2);
+      double P[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          P[i * 3 + j] = j < 2 ? Q[i * 3 + 0] * P2[0 * 2 + j] + Q[i * 3 + 1] * P2[1 * 2 + j] : 0.0;
+      const double g = cl.gamma;
+      double gf = 0;
+      if (Rm[8] < 1) {
+        const double vv = 1 - Rm[8];
+        gf = -double(cl.k) * vv * vv;
+      }
+      double A[9] = {g * Rm[2] * Rm[2], g * Rm[2] * Rm[5], g * Rm[2] * Rm[8],
+                     0, g * Rm[5] * Rm[5], g * Rm[5] * Rm[8], 0, 0, gf * Rm[8]};
+      A[3] = A[1];
+      A[6] = A[2];
+      A[7] = A[5];
+      // R^-1 of the upper-triangular R, then P += Q A R^-T
+      const double i00 = 1 / Rm[0], i11 = 1 / Rm[4], i22 = 1 / Rm[8];
+      const double i01 = -Rm[1] * i00 * i11, i12 = -Rm[5] * i11 * i22;
+      const double i02 = (Rm[1] * Rm[5] - Rm[2] * Rm[4]) * i00 * i11 * i22;
+      const double Ri[9] = {i00, i01, i02, 0, i11, i12, 0, 0, i22};
+      double QA[9], T[9];
+      mul_AB(Q, A, QA);
+      mul_ABt(QA, Ri, T);
+      for (int i = 0; i < 9; ++i) P[i] += T[i];
+      const double Pc3[3] = {P[2], P[5], P[8]}, dc3[3] = {dm[2], dm[5], dm[8]};
+      const double mass = cl.em[e], vol = cl.evol[e];
+      const double *ve = cl.ev + 3 * e, *Ce = cl.eC + 9 * e;
+      Stencil st;
+      stencil(cl.ex + 3 * e, st);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k) {
+            const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+            const double xixp[3] = {(i - st.fx[0]) * dx, (j - st.fx[1]) * dx, (k - st.fx[2]) * dx};
+            const double W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+            double gw[3];
+            weight_grad(st, i, j, k, gw);
+            const double s = (gw[0] * dc3[0] + gw[1] * dc3[1] + gw[2] * dc3[2]) * (-vol * dt);
+            R *nd = node(I);
+            nd[0] += W * mass;
+            for (int a = 0; a < 3; ++a) {
+              const double Cx = affine ? Ce[a * 3 + 0] * xixp[0] + Ce[a * 3 + 1] * xixp[1] + Ce[a * 3 + 2] * xixp[2] : 0.0;
+              nd[1 + a] += W * mass * (ve[a] + Cx) + (flip_style ? 0.0 : Pc3[a] * s);
+              if (flip_style) nd[4 + a] += Pc3[a] * s;
+            }
+          }
+      // type (ii): vertex impulses from the in-plane columns of P
+      const double r0[2] = {Di[0], Di[1]}, r1[2] = {Di[3], Di[4]};
+      const int32_t *t = cl.inds + 3 * e;
+      for (int vi = 0; vi < 3; ++vi) {
+        double Dr[2], coeff;
+        if (vi == 0) {
+          Dr[0] = r0[0] + r1[0];
+          Dr[1] = r0[1] + r1[1];
+          coeff = vol * dt;
+        } else {
+          const double *r = vi == 1 ? r0 : r1;
+          Dr[0] = r[0];
+          Dr[1] = r[1];
+          coeff = -vol * dt;
+        }
+        for (int a = 0; a < 3; ++a) imp[3 * t[vi] + a] += coeff * (P[a * 3 + 0] * Dr[0] + P[a * 3 + 1] * Dr[1]);
+      }
+    }
+    for (int64_t p = 0; p < cl.n_verts; ++p) {
+      const double mass = cl.vm[p], *vp = cl.vv + 3 * p, *Cp = cl.vC + 9 * p;
+      Stencil st;
+      stencil(cl.vx + 3 * p, st);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k) {
+            const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+            const double xixp[3] = {(i - st.fx[0]) * dx, (j - st.fx[1]) * dx, (k - st.fx[2]) * dx};
+            const double W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+            R *nd = node(I);
+            nd[0] += W * mass;
+            for (int a = 0; a < 3; ++a) {
+              const double Cx = affine ? Cp[a * 3 + 0] * xixp[0] + Cp[a * 3 + 1] * xixp[1] + Cp[a * 3 + 2] * xixp[2] : 0.0;
+              if (flip_style) {
+                nd[1 + a] += W * mass * (vp[a] + Cx);
+                nd[4 + a] += W * imp[3 * p + a];
+              } else {
+                nd[1 + a] += W * (mass * (vp[a] + Cx) + imp[3 * p + a]);
+              }
+            }
+          }
+    }
+  }
+
+  // affine velocity Dinv sum W u_i (x_i - x_p)^T at x with u = v or vstar,
+  // and sum W v, sum W vstar; symmetric part damped by (1 - dc)
+  void cloth_gather(const double *x, bool use_vstar, double dc, double *vel, double *vs,
+                    double *Cn) {
+    const double dx = sc.dx, Dinv = 4.0 / (dx * dx);
+    Stencil st;
+    stencil(x, st);
+    for (int a = 0; a < 3; ++a) vel[a] = vs[a] = 0;
+    for (int i = 0; i < 9; ++i) Cn[i] = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+          const double xixp[3] = {(i - st.fx[0]) * dx, (j - st.fx[1]) * dx, (k - st.fx[2]) * dx};
+          const double W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+          const R *nd = node(I);
+          for (int a = 0; a < 3; ++a) {
+            vel[a] += W * nd[1 + a];
+            vs[a] += W * nd[4 + a];
+            const double u = use_vstar ? nd[4 + a] : nd[1 + a];
+            for (int b = 0; b < 3; ++b) Cn[a * 3 + b] += W * Dinv * u * xixp[b];
+          }
+        }
+    double D[9];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+        D[a * 3 + b] = 0.5 * (Cn[a * 3 + b] - Cn[b * 3 + a]) + (1 - dc) * 0.5 * (Cn[a * 3 + b] + Cn[b * 3 + a]);
+    for (int i = 0; i < 9; ++i) Cn[i] = D[i];
+  }
+
+  // ZSGridToZSParticle for the cloth (Transfer.cu:1287-1445): vertices as
+  // damped APIC (or the FLIP-style blend with beta 0), then elements: damped
+  // C, centroid position and mean velocity of their vertices, d1 = p1 - p0,
+  // d2 = p2 - p0, d3 += (dt C + dt^2 / 2 C^2) d3, F = d DmInv.
+  void cloth_g2p(orc_cloth &cl, double dt) {
+    const bool flip_style = sc.transfer != ORC_TRANSFER_APIC;
+    const double dc = cl.dc;
+    for (int64_t p = 0; p < cl.n_verts; ++p) {
+      double vel[3], vs[3], Cn[9];
+      cloth_gather(cl.vx + 3 * p, flip_style, dc, vel, vs, Cn);
+      for (int a = 0; a < 3; ++a) {
+        if (flip_style) {
+          const double d0 = cl.vv[3 * p + a] - vel[a];
+          cl.vv[3 * p + a] = vs[a] + 0.99 * d0;
+          cl.vx[3 * p + a] += dt * vs[a];  // beta = 0
+        } else {
+          cl.vv[3 * p + a] = vel[a];
+          cl.vx[3 * p + a] += vel[a] * dt;
+        }
+      }
+      for (int i = 0; i < 9; ++i) cl.vC[9 * p + i] = Cn[i];
+    }
+    for (int64_t e = 0; e < cl.n_eles; ++e) {
+      double vel[3], vs[3], Cn[9];
+      cloth_gather(cl.ex + 3 * e, flip_style, dc, vel, vs, Cn);
+      for (int i = 0; i < 9; ++i) cl.eC[9 * e + i] = Cn[i];
+      const int32_t *t = cl.inds + 3 * e;
+      const double *p0 = cl.vx + 3 * t[0], *p1 = cl.vx + 3 * t[1], *p2 = cl.vx + 3 * t[2];
+      double *d = cl.ed + 9 * e;
+      double d3[3] = {d[2], d[5], d[8]}, CC[9], M[9], n3[3];
+      mul_AB(Cn, Cn, CC);
+      for (int i = 0; i < 9; ++i) M[i] = dt * Cn[i] + 0.5 * dt * dt * CC[i];
+      for (int a = 0; a < 3; ++a) n3[a] = d3[a] + M[a * 3 + 0] * d3[0] + M[a * 3 + 1] * d3[1] + M[a * 3 + 2] * d3[2];
+      for (int a = 0; a < 3; ++a) {
+        cl.ex[3 * e + a] = (p0[a] + p1[a] + p2[a]) / 3;
+        cl.ev[3 * e + a] = (cl.vv[3 * t[0] + a] + cl.vv[3 * t[1] + a] + cl.vv[3 * t[2] + a]) / 3;
+        d[a * 3 + 0] = p1[a] - p0[a];
+        d[a * 3 + 1] = p2[a] - p0[a];
+        d[a * 3 + 2] = n3[a];
+      }
+      mul_AB(d, cl.eDmInv + 9 * e, cl.eF + 9 * e);
+    }
+  }
+
+  // ZSReturnMapping for the cloth (return_mapping_surface,
+  // MPMPipeline.cu:973-1011) on R of d = Q R: no shear resistance beyond
+  // friction, no tension across the normal; fc = tan(fa / pi) as the node
+  // computes it (MPMPipeline.cu:1120).
+  void cloth_return_mapping(orc_cloth &cl) {
+    const double gamma = cl.gamma, k = cl.k, fc = std::tan(double(cl.fa) / 3.14159265358979323846);
+    for (int64_t e = 0; e < cl.n_eles; ++e) {
+      double *d = cl.ed + 9 * e;
+      double Q[9], Rm[9];
+      gram_schmidt(d, Q, Rm);
+      bool apply = false;
+      if (gamma == 0) {
+        Rm[2] = Rm[5] = 0;
+        Rm[8] = std::min(Rm[8], 1.0);
+        apply = true;
+      } else if (Rm[8] > 1) {
+        Rm[2] = Rm[5] = 0;
+        Rm[8] = 1;
+        apply = true;
+      } else if (Rm[8] <= 0) {
+        Rm[2] = Rm[5] = 0;
+        Rm[8] = std::max(Rm[8], -1.0);
+        apply = true;
+      } else if (Rm[8] < 1) {
+        const double rr = Rm[2] * Rm[2] + Rm[5] * Rm[5], r = Rm[8] - 1, gk = gamma / k;
+        const double zz = fc * r * r;
+        if (gk * gk * rr - zz * zz > 0) {
+          const double scale = zz / (gk * std::sqrt(rr));
+          Rm[2] *= scale;
+          Rm[5] *= scale;
+          apply = true;
+        }
+      }
+      if (apply) {
+        mul_AB(Q, Rm, d);
+        mul_AB(d, cl.eDmInv + 9 * e, cl.eF + 9 * e);
+      }
+    }
+  }
+
   int substep(int64_t n, R *x, R *v, R *C, R *F, R *J, const R *m, const R *vol,
               const int32_t *mat, const R *mu, const R *lam, const R *beta, R dt) {
     const int tr = sc.transfer;
     if (sc.collider_autostep) step_colliders(dt);  // the fused substep's collider time
-    int rc = build_partition<R>(sc, n, x, P, nthreads);
+    std::vector<PointSet> extra;
+    if (std::is_same<R, double>::value && sc.cloth) {
+      extra.push_back({sc.cloth->vx, sc.cloth->n_verts});
+      extra.push_back({sc.cloth->ex, sc.cloth->n_eles});
+    }
+    int rc = build_partition<R>(sc, n, x, P, nthreads, extra);
     if (rc) return rc;
     // ZSGridFromZSPartition: zero every channel of every block
     grid.assign(P.gb_dir.size() * 64 * kNG, R(0));
@@ -621,6 +963,9 @@ template <class R> struct Sim {
         }
       }
     }
+
+    if constexpr (std::is_same<R, double>::value)
+      if (sc.cloth) cloth_p2g(*sc.cloth, double(dt));
 
     // UpdateZSGrid (APIC branch) then ApplyBoundaryOnZSGrid, node-wise
     const int64_t ng = int64_t(P.gb_dir.size());
@@ -745,6 +1090,11 @@ template <class R> struct Sim {
       if (!std::isfinite(x[3 * p]) || !std::isfinite(x[3 * p + 1]) || !std::isfinite(x[3 * p + 2]))
         bad |= 1;
     }
+    if constexpr (std::is_same<R, double>::value)
+      if (sc.cloth) {
+        cloth_g2p(*sc.cloth, double(dt));
+        cloth_return_mapping(*sc.cloth);
+      }
     return bad ? ORC_ERR_NAN : ORC_OK;
   }
 
@@ -780,6 +1130,7 @@ int32_t run(const orc_scene *scene, int64_t n, R *x, R *v, R *C, R *F, R *J, con
   if (!scene || n < 0 || nsteps < 0) return ORC_ERR_INVALID;
   if (scene->transfer < ORC_TRANSFER_APIC || scene->transfer > ORC_TRANSFER_AFLIP)
     return ORC_ERR_INVALID;
+  if (scene->cloth && !std::is_same<R, double>::value) return ORC_ERR_INVALID;
   for (int64_t p = 0; p < n; ++p)
     if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
 #ifdef _OPENMP
@@ -919,6 +1270,104 @@ int32_t orc_kirchhoff(const orc_material *mat, const double *F, double J, double
 int32_t orc_project_dp(const orc_material *mat, double *F) {
   const Params<double> p = material_params<double>(*mat);
   return project_dp<double>(p, F);
+}
+
+// ToZSCloth (Generation.cpp:489-688): per triangle, area A (double), vol =
+// max(A dx, 10 eps_float), centroid position and velocity, d = [p1 - p0,
+// p2 - p0, n] with n = normalize(normalize(d1) x normalize(d2)); each vertex
+// gets a third of the volume of its triangles; m = vol density.  The rest
+// shape D* = [|d1|, d1.d2/|d1|, 0; 0, |d1 x d2|/|d1|, 0; 0, 0, 1] (d1, d2 in
+// the triangle's own frame: the reference rotates n to z and d1 to x),
+// DmInv = D*^-1, F = d DmInv; a triangle with a near-zero side of D* gets
+// mu = lam = 0.
+int32_t orc_cloth_init_f64(int64_t n_verts, const float *x, const float *v, int64_t n_tris,
+                           const int32_t *tris, float dx, float density, float E, float nu,
+                           orc_cloth *out) {
+  if (!out || n_verts < 0 || n_tris < 0) return ORC_ERR_INVALID;
+  const float mu = E / (2.0f * (1.0f + nu)), lam = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+  std::vector<float> dof_vol(n_verts, 0.0f);
+  const double feps = std::numeric_limits<float>::epsilon();
+  for (int64_t e = 0; e < n_tris; ++e) {
+    const int32_t *t = tris + 3 * e;
+    for (int i = 0; i < 3; ++i)
+      if (t[i] < 0 || t[i] >= n_verts) return ORC_ERR_INVALID;
+    double p[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int a = 0; a < 3; ++a) p[i][a] = x[3 * t[i] + a];
+    double e1[3], e2[3], cr[3];
+    for (int a = 0; a < 3; ++a) {
+      e1[a] = p[1][a] - p[0][a];
+      e2[a] = p[2][a] - p[0][a];
+    }
+    cr[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    cr[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    cr[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const double area = 0.5 * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    const float vol = float(std::max(area * double(dx), feps * 10.0));
+    out->evol[e] = vol;
+    out->em[e] = double(vol * density);
+    for (int a = 0; a < 3; ++a) {
+      const float c = (x[3 * t[0] + a] + x[3 * t[1] + a] + x[3 * t[2] + a]) / 3.0f;
+      out->ex[3 * e + a] = c;
+      out->ev[3 * e + a] = v ? double((v[3 * t[0] + a] + v[3 * t[1] + a] + v[3 * t[2] + a]) / 3.0f) : 0.0;
+    }
+    // d columns in float as the reference stores them
+    float d1[3], d2[3];
+    for (int a = 0; a < 3; ++a) {
+      d1[a] = x[3 * t[1] + a] - x[3 * t[0] + a];
+      d2[a] = x[3 * t[2] + a] - x[3 * t[0] + a];
+    }
+    const double n1 = std::sqrt(double(d1[0]) * d1[0] + double(d1[1]) * d1[1] + double(d1[2]) * d1[2]);
+    const double n2 = std::sqrt(double(d2[0]) * d2[0] + double(d2[1]) * d2[1] + double(d2[2]) * d2[2]);
+    double u1[3], u2[3], nn[3];
+    for (int a = 0; a < 3; ++a) {
+      u1[a] = d1[a] / n1;
+      u2[a] = d2[a] / n2;
+    }
+    nn[0] = u1[1] * u2[2] - u1[2] * u2[1];
+    nn[1] = u1[2] * u2[0] - u1[0] * u2[2];
+    nn[2] = u1[0] * u2[1] - u1[1] * u2[0];
+    const double nl = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+    float n3[3];
+    for (int a = 0; a < 3; ++a) n3[a] = float(nn[a] / nl);
+    double *d = out->ed + 9 * e;
+    for (int a = 0; a < 3; ++a) {
+      d[a * 3 + 0] = d1[a];
+      d[a * 3 + 1] = d2[a];
+      d[a * 3 + 2] = n3[a];
+    }
+    // rest shape in the triangle's frame, from the stored (float) columns
+    const double t0[3] = {d1[0], d1[1], d1[2]}, t1[3] = {d2[0], d2[1], d2[2]};
+    const double l0 = std::sqrt(t0[0] * t0[0] + t0[1] * t0[1] + t0[2] * t0[2]);
+    const double dot01 = t0[0] * t1[0] + t0[1] * t1[1] + t0[2] * t1[2];
+    const double cx = t0[1] * t1[2] - t0[2] * t1[1], cy = t0[2] * t1[0] - t0[0] * t1[2],
+                 cz = t0[0] * t1[1] - t0[1] * t1[0];
+    const double a00 = l0, a01 = dot01 / l0, a11 = std::sqrt(cx * cx + cy * cy + cz * cz) / l0;
+    double Di[9] = {1 / a00, -a01 / (a00 * a11), 0, 0, 1 / a11, 0, 0, 0, 1};
+    const bool degenerate = std::fabs(a11) <= 10 * feps || std::fabs(a00) <= 10 * feps;
+    out->emu[e] = degenerate ? 0.0 : mu;
+    out->elam[e] = degenerate ? 0.0 : lam;
+    for (int i = 0; i < 9; ++i) out->eDmInv[9 * e + i] = float(Di[i]);
+    double Fd[9];
+    mul_AB(d, Di, Fd);
+    for (int i = 0; i < 9; ++i) out->eF[9 * e + i] = float(Fd[i]);
+    for (int i = 0; i < 9; ++i) out->eC[9 * e + i] = 0;
+    for (int i = 0; i < 3; ++i) {
+      out->inds[3 * e + i] = t[i];
+      dof_vol[t[i]] += vol / 3.0f;
+    }
+  }
+  for (int64_t p = 0; p < n_verts; ++p) {
+    out->vm[p] = double(dof_vol[p] * density);
+    for (int a = 0; a < 3; ++a) {
+      out->vx[3 * p + a] = x[3 * p + a];
+      out->vv[3 * p + a] = v ? v[3 * p + a] : 0.0f;
+    }
+    for (int i = 0; i < 9; ++i) out->vC[9 * p + i] = 0;
+  }
+  out->n_verts = n_verts;
+  out->n_eles = n_tris;
+  return ORC_OK;
 }
 
 int32_t orc_max_threads(void) {

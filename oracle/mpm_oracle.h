@@ -78,6 +78,24 @@ typedef struct orc_collider {
   float ypr_deg[3];
 } orc_collider;
 
+/* Codimensional cloth (ToZSCloth, Generation.cpp:432-689): a triangle mesh
+ * whose vertices and per-triangle quadrature points ("elements") both carry
+ * mass; element state d = [d1 d2 d3] (two edges and the normal direction),
+ * DmInv, F = d DmInv; stepped by the surface branches of the transfer nodes
+ * (Transfer.cu:656-842 P2G, 1287-1445 G2P) and ZSReturnMapping
+ * (MPMPipeline.cu:973-1011).  Arrays are in/out, row-major 3x3. */
+typedef struct orc_cloth {
+  int32_t model;          /* ORC_FCR / ORC_NHK / ORC_STVK: the in-plane model */
+  float gamma, k, fa, dc; /* ToZSCloth stiffness_shear, stiffness_normal,
+                             friction_angle, damping_coeff */
+  int64_t n_verts, n_eles;
+  double *vx, *vv, *vC;   /* vertices: x (3), v (3), C (9) */
+  double *vm;             /* vertex mass */
+  double *ex, *ev, *eC, *eF, *ed, *eDmInv; /* elements */
+  double *em, *evol, *emu, *elam;
+  int32_t *inds;          /* 3 vertex indices per element */
+} orc_cloth;
+
 typedef struct orc_scene {
   float dx;
   float gravity[3];
@@ -93,6 +111,7 @@ typedef struct orc_scene {
   const orc_collider *colliders;
   int32_t collider_autostep; /* 1: advance colliders by dt at the start of each substep */
   int32_t transfer;          /* ORC_TRANSFER_* */
+  orc_cloth *cloth;          /* NULL, or one cloth stepped with the particles (FP64 only) */
 } orc_scene;
 
 typedef struct orc_stats {
@@ -158,6 +177,14 @@ int32_t orc_kirchhoff(const orc_material *mat, const double *F, double J,
 
 /* Drucker-Prager return mapping of F in place; returns 1 if projected. */
 int32_t orc_project_dp(const orc_material *mat, double *F);
+
+/* ToZSCloth's set-up of the vertex and element arrays of `out` (allocated
+ * by the caller for n_verts / n_tris) from a mesh: positions x, optional
+ * velocities v (n_verts x 3 floats), triangles tris (n_tris x 3), the
+ * model's dx (thickness), density and E, nu. */
+int32_t orc_cloth_init_f64(int64_t n_verts, const float *x, const float *v, int64_t n_tris,
+                           const int32_t *tris, float dx, float density, float E, float nu,
+                           orc_cloth *out);
 
 int32_t orc_max_threads(void);
 

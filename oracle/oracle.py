@@ -33,13 +33,26 @@ class OrcCollider(C.Structure):
                 ("scale_rate", C.c_float), ("ypr_deg", C.c_float * 3)]
 
 
+class OrcCloth(C.Structure):
+    _fields_ = [("model", C.c_int32), ("gamma", C.c_float), ("k", C.c_float), ("fa", C.c_float),
+                ("dc", C.c_float), ("n_verts", C.c_int64), ("n_eles", C.c_int64)] + \
+               [(k, C.c_void_p) for k in ("vx", "vv", "vC", "vm", "ex", "ev", "eC", "eF", "ed",
+                                          "eDmInv", "em", "evol", "emu", "elam", "inds")]
+
+
+CLOTH_VERT = {"vx": 3, "vv": 3, "vC": 9, "vm": 1}
+CLOTH_ELE = {"ex": 3, "ev": 3, "eC": 9, "eF": 9, "ed": 9, "eDmInv": 9, "em": 1, "evol": 1,
+             "emu": 1, "elam": 1}
+
+
 class OrcScene(C.Structure):
     _fields_ = [("dx", C.c_float), ("gravity", C.c_float * 3), ("block_lo", C.c_int32 * 3),
                 ("block_dims", C.c_int32 * 3), ("bc_type", C.c_int32),
                 ("bc_thickness", C.c_int32), ("bc_lo", C.c_int32 * 3), ("bc_hi", C.c_int32 * 3),
                 ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial)),
                 ("n_colliders", C.c_int32), ("colliders", C.POINTER(OrcCollider)),
-                ("collider_autostep", C.c_int32), ("transfer", C.c_int32)]
+                ("collider_autostep", C.c_int32), ("transfer", C.c_int32),
+                ("cloth", C.POINTER(OrcCloth))]
 
 
 class OrcStats(C.Structure):
@@ -79,6 +92,9 @@ def lib():
         L.orc_particle_beta_f64.restype = C.c_int32
         L.orc_von_mises_f64.argtypes = [C.POINTER(OrcScene), C.c_int64, P, P, C.c_int32, P]
         L.orc_von_mises_f64.restype = C.c_int32
+        L.orc_cloth_init_f64.argtypes = [C.c_int64, P, P, C.c_int64, P, C.c_float, C.c_float,
+                                         C.c_float, C.c_float, C.POINTER(OrcCloth)]
+        L.orc_cloth_init_f64.restype = C.c_int32
         L.orc_sym_eig3.argtypes = [P, P, P]
         L.orc_kirchhoff.argtypes = [C.POINTER(OrcMaterial), P, C.c_double, P]
         L.orc_kirchhoff.restype = C.c_int32
@@ -129,7 +145,11 @@ class _SceneHolder:
                           (C.c_int32 * 3)(*scene.bc_lo), (C.c_int32 * 3)(*scene.bc_hi),
                           len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)),
                           len(cols), C.cast(carr, C.POINTER(OrcCollider)), 1,
-                          int(getattr(scene, "transfer", 0)))
+                          int(getattr(scene, "transfer", 0)), None)
+
+    def attach_cloth(self, cl: "OrcCloth"):
+        self.cloth = cl
+        self.s.cloth = C.pointer(cl)
 
 
 def partition(scene, x: np.ndarray) -> dict:
@@ -205,6 +225,51 @@ def von_mises(scene, parts, by_log1p: bool = True, vms: np.ndarray | None = None
     if rc != 0:
         raise RuntimeError(f"oracle von Mises failed with status {rc}")
     return out
+
+
+def _cloth_struct(mesh, state) -> OrcCloth:
+    st = OrcCloth(int(mesh.model), float(mesh.gamma), float(mesh.k), float(mesh.fa),
+                  float(mesh.dc), int(state["vx"].shape[0]), int(state["ex"].shape[0]))
+    for k in list(CLOTH_VERT) + list(CLOTH_ELE) + ["inds"]:
+        setattr(st, k, state[k].ctypes.data)
+    return st
+
+
+def cloth_init(mesh, dx: float) -> dict:
+    """ToZSCloth in FP64: the vertex and element arrays of a scenes.ClothMesh."""
+    x = np.ascontiguousarray(mesh.x, dtype=np.float32)
+    v = None if mesh.v is None else np.ascontiguousarray(mesh.v, dtype=np.float32)
+    tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
+    nv, ne = x.shape[0], tris.shape[0]
+    state = {k: np.zeros((nv, c) if c > 1 else nv) for k, c in CLOTH_VERT.items()}
+    state.update({k: np.zeros((ne, c) if c > 1 else ne) for k, c in CLOTH_ELE.items()})
+    state["inds"] = np.zeros((ne, 3), np.int32)
+    st = _cloth_struct(mesh, state)
+    rc = lib().orc_cloth_init_f64(nv, _ptr(x), _ptr(v), ne, _ptr(tris), float(dx),
+                                  float(mesh.density), float(mesh.E), float(mesh.nu), C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"oracle cloth init failed with status {rc}")
+    return state
+
+
+def run_cloth(scene, parts, mesh, state: dict, nsteps: int, dt: float | None = None):
+    """FP64 substeps of the particles together with one cloth (state from
+    cloth_init, copied); returns (particles, cloth state, stats)."""
+    state = {k: np.array(a, copy=True) for k, a in state.items()}
+    p = parts.copy(dtype=np.float64)
+    for k in ("x", "v", "C", "F", "J", "m", "vol", "mu", "lam", "beta"):
+        a = getattr(p, k)
+        if a is not None:
+            setattr(p, k, np.ascontiguousarray(a, dtype=np.float64))
+    p.mat = np.ascontiguousarray(p.mat, dtype=np.int32)
+    h = _SceneHolder(scene)
+    h.attach_cloth(_cloth_struct(mesh, state))
+    st = OrcStats()
+    rc = lib().orc_run_f64(C.byref(h.s), p.n, _ptr(p.x), _ptr(p.v), _ptr(p.C), _ptr(p.F),
+                           _ptr(p.J), _ptr(p.m), _ptr(p.vol), _ptr(p.mat), _ptr(p.mu),
+                           _ptr(p.lam), _ptr(p.beta), float(scene.dt if dt is None else dt),
+                           int(nsteps), 0, C.byref(st))
+    return p, state, {"status": rc, "max_vel_sqr": st.max_vel_sqr, "n_gblocks": st.n_gblocks}
 
 
 def sym_eig3(A: np.ndarray):

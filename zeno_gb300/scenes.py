@@ -109,6 +109,45 @@ def plane_collider(height: float, extent: float, spacing: float, type: int = 1, 
 
 
 @dataclass
+class ClothMesh:
+    """A triangle mesh stepped as codimensional cloth (ToZSCloth): vertex
+    positions x (nv, 3), optional velocities v, triangles tris (nt, 3), the
+    in-plane elastic model (FCR, NHK or STVK) with E, nu, density, and the
+    cloth parameters stiffness_shear (gamma), stiffness_normal (k),
+    friction_angle (fa) and damping_coeff (dc)."""
+    x: np.ndarray
+    tris: np.ndarray
+    v: np.ndarray = None
+    model: int = FCR
+    E: float = 1e4
+    nu: float = 0.3
+    density: float = 1000.0
+    gamma: float = 0.0
+    k: float = 800.0
+    fa: float = 0.0
+    dc: float = 0.0
+
+
+def cloth_sheet(center, size: float, n: int, jitter: float = 0.0, seed: int = 0, **kw) -> ClothMesh:
+    """A square sheet of (n+1)^2 vertices in the plane y = center[1],
+    2 n^2 triangles; vertices optionally jittered in-plane by jitter * size/n."""
+    g = np.linspace(-0.5, 0.5, n + 1) * size
+    X, Z = np.meshgrid(g, g, indexing="ij")
+    x = np.stack([X.ravel() + center[0], np.full(X.size, float(center[1])), Z.ravel() + center[2]],
+                 axis=1)
+    if jitter:
+        u = uniform(seed, 17, x.shape[0] * 2).reshape(-1, 2) - 0.5
+        x[:, 0] += jitter * size / n * u[:, 0]
+        x[:, 2] += jitter * size / n * u[:, 1]
+    tris = []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = i * (n + 1) + j, (i + 1) * (n + 1) + j, i * (n + 1) + j + 1, (i + 1) * (n + 1) + j + 1
+            tris += [(a, b, d), (a, d, c)]
+    return ClothMesh(x=x.astype(np.float32), tris=np.array(tris, np.int32), **kw)
+
+
+@dataclass
 class Scene:
     """Grid, boundary and material description of one MPM scene."""
     dx: float
