@@ -346,6 +346,53 @@ def frame_output_form(zsmpm, dev: int, frames: int = 6, per_frame: int = 100):
             "ms_per_frame_sync": 1e3 * out["sync"] / frames}
 
 
+def cloth_form(zsmpm, steps: int, dev: int, n: int = 384):
+    """The plain four-material scene with a codimensional cloth sheet
+    (ToZSCloth, fixed-corotated, (n+1)^2 vertices and 2 n^2 triangles over
+    0.8 x 0.8 at y = 0.45, falling at 1 m/s) stepped in the same substeps;
+    against the same context without the cloth, timed in the same way."""
+    import torch
+    from zeno_gb300 import scenes
+    scene, parts = make_workload()
+    stream = torch.cuda.Stream(device=dev)
+    ctx = zsmpm.Context(scene, max_particles=parts.n, device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed():
+        ctx.upload(parts)
+        ctx.substep(scene.dt, 5)
+        ctx.sync()
+        e0.record(stream)
+        ctx.substep(scene.dt, steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        ctx.sync()
+        return ms, ctx.stats()
+
+    ms_free, _ = timed()
+    mesh = scenes.cloth_sheet((0.5, 0.45, 0.5), 0.8, n, E=5e4, nu=0.3, density=300.0,
+                              gamma=100.0, k=800.0, fa=30.0, dc=0.02)
+    mesh.v = np.tile(np.array([0.0, -1.0, 0.0], np.float32), (mesh.x.shape[0], 1))
+    ctx.add_cloth(mesh)
+    ms_cloth, st = timed()
+    stage = [ctx.substep_timed(scene.dt) for _ in range(10)]
+    ctx.sync()
+    ctx.close()
+    nv, ne = mesh.x.shape[0], mesh.tris.shape[0]
+    return {"workload": f"plain 2,097,152-particle four-material scene + a {nv:,}-vertex, "
+                        f"{ne:,}-triangle fixed-corotated cloth sheet",
+            "value": parts.n * steps / (ms_cloth * 1e-3), "unit": METRIC, "steps": steps,
+            "ms_per_step": ms_cloth / steps, "ms_per_step_without_cloth": ms_free / steps,
+            "cloth_ms_per_step": (ms_cloth - ms_free) / steps,
+            "cloth_points_per_s": (nv + ne) * steps / ((ms_cloth - ms_free) * 1e-3),
+            "grid_update_stage_ms": statistics.mean(r["grid_update"] for r in stage),
+            "g2p_stage_ms": statistics.mean(r["g2p"] for r in stage),
+            "status": st["status"]}
+
+
 def differentiable_form(zsmpm, dev: int, steps: int = 64, ckpt: int = 16):
     """The differentiable form: 65,536 fixed-corotated particles at dx = 1/128
     (E ~ U[3e4, 1e5] per particle), 64 substeps with a checkpoint every 16,
@@ -739,6 +786,7 @@ def run_gpu(args):
         forms["aflip"] = transfer_form(zsmpm, max(10, min(args.steps, 500)), dev,
                                        _S.TRANSFER_AFLIP)
         forms["frame_output"] = frame_output_form(zsmpm, dev)
+        forms["cloth"] = cloth_form(zsmpm, max(10, min(args.steps, 300)), dev)
         forms["fwd_bwd"] = differentiable_form(zsmpm, dev)
         forms["fwd_bwd_sand_16M"] = sand_form(zsmpm, dev)
     if rank != 0:

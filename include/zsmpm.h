@@ -181,6 +181,32 @@ int32_t mpm_clear_colliders(mpm_ctx *ctx);
 /* id: the collider from mpm_add_collider, or -1 for every collider */
 int32_t mpm_step_colliders(mpm_ctx *ctx, int32_t id, float dt);
 
+/* Codimensional cloth: ToZSCloth (Generation.cpp:432-689).  A triangle mesh
+ * whose vertices and per-triangle quadrature points both carry mass:
+ * element volume = area x dx (the thickness), vertex volume = a third of its
+ * triangles'; in-plane model MPM_FCR / MPM_NHK / MPM_STVK with E, nu; the
+ * ToZSCloth inputs stiffness_shear (gamma), stiffness_normal (k),
+ * friction_angle (fa, used as tan(fa / pi) like ZSReturnMapping,
+ * MPMPipeline.cu:1120) and damping_coeff (dc).  One cloth per single-scene
+ * context, stepped by every substep entry point with the particles
+ * (Transfer.cu:656-842 P2G, 1287-1445 G2P, MPMPipeline.cu:973-1011 return
+ * mapping, the latter applied in G2P).  Not differentiable. */
+typedef struct mpm_cloth_desc {
+  int64_t n_verts;
+  const float *x; /* n_verts x 3 */
+  const float *v; /* n_verts x 3, or NULL (at rest) */
+  int64_t n_tris;
+  const int32_t *tris; /* n_tris x 3 vertex indices */
+  int32_t model;
+  float E, nu, density;
+  float stiffness_shear, stiffness_normal, friction_angle, damping_coeff;
+} mpm_cloth_desc;
+int32_t mpm_cloth_create(mpm_ctx *ctx, const mpm_cloth_desc *desc);
+/* the cloth's state (NULL skips an array): vertices x, v (n_verts x 3), C
+ * (n_verts x 9); elements x, v (n_tris x 3), C, F, d (n_tris x 9, row-major) */
+int32_t mpm_cloth_download(mpm_ctx *ctx, float *vx, float *vv, float *vC, float *ex, float *ev,
+                           float *eC, float *eF, float *ed);
+
 /* ToZSParticles (Generation.cpp:690-1145): host arrays -> device store.
  * NULL optional arrays take the reference defaults: v = 0, C = 0, F = I,
  * J = 1.  mu / lam are the per-particle overrides added by

@@ -21,7 +21,7 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ZSParticleToZSGrid", "UpdateZSGrid", "ApplyBoundaryOnZSGrid", "ToZSBoundary",
          "ZSGridToZSParticle", "ZSReturnMapping", "AdjustParticleMaterial",
          "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
-         "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises"]
+         "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises", "ToZSCloth"]
 
 
 def parse_braces(s, i):
@@ -55,6 +55,7 @@ def main():
     for f in FILES:
         src = open(os.path.join(REF, f)).read()
         src = re.sub(r"//[^\n]*", "", src)
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"ZENDEFNODE\(\s*(\w+)\s*,", src):
             name = m.group(1)
             if name not in NODES:

@@ -1,0 +1,133 @@
+"""Codimensional cloth on the GPU against the FP64 oracle: ToZSCloth's
+set-up, a stretched sheet on its own (three in-plane models, APIC and the
+FLIP transfers), a sheet falling onto a jelly block through the shared grid,
+and the stage path against the fused substep."""
+import numpy as np
+import pytest
+
+from zeno_gb300 import scenes as S
+
+from .conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _empty():
+    z = lambda *sh: np.zeros((0,) + sh, np.float32)
+    return S.Particles(z(3), z(3), z(3, 3), z(3, 3), z(), z(), z(), np.zeros(0, np.int32))
+
+
+def _sheet(model=S.FCR, gamma=100.0, n=12, **kw):
+    mesh = S.cloth_sheet((0.5, 0.55, 0.5), 0.3, n, jitter=0.3, seed=5, model=model, E=3e4,
+                         nu=0.3, density=500.0, gamma=gamma, k=800.0, fa=30.0, dc=0.05, **kw)
+    c = np.array([0.5, 0.55, 0.5])
+    r = mesh.x - c
+    # stretch in-plane, a little twist and a push down
+    mesh.v = (0.8 * r + np.cross([0.0, 2.0, 0.0], r) + [0.0, -0.3, 0.0]).astype(np.float32)
+    return mesh
+
+
+def _gpu(zsmpm, scene, parts, mesh, steps, staged=False):
+    with zsmpm.Context(scene, max_particles=max(parts.n, 1)) as ctx:
+        ctx.upload(parts)
+        ctx.add_cloth(mesh)
+        init = ctx.cloth_download()
+        if staged:
+            for _ in range(steps):
+                ctx.staged_substep(scene.dt)
+        else:
+            ctx.substep(scene.dt, steps)
+        st = ctx.sync() or ctx.stats()
+        out = ctx.cloth_download()
+        mpm = ctx.download(("x", "v")) if parts.n else None
+    return init, out, mpm, st
+
+
+def test_cloth_setup_matches_oracle(zsmpm_mod, oracle_mod):
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    mesh = _sheet()
+    init, _, _, _ = _gpu(zsmpm_mod, scene, _empty(), mesh, 0)
+    ref = oracle_mod.cloth_init(mesh, scene.dx)
+    for k in ("vx", "vv", "ex", "ev", "eF", "ed"):
+        np.testing.assert_allclose(init[k], ref[k].reshape(init[k].shape), rtol=1e-6, atol=1e-7,
+                                   err_msg=k)
+
+
+@pytest.mark.parametrize("model", [S.FCR, S.NHK, S.STVK])
+@pytest.mark.parametrize("tr", [S.TRANSFER_APIC, S.TRANSFER_FLIP, S.TRANSFER_AFLIP])
+def test_sheet_matches_oracle(zsmpm_mod, oracle_mod, model, tr):
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    scene.transfer = tr
+    mesh = _sheet(model)
+    # FP32 state resolves these small strains to ~1e-4 relative; APIC forgets
+    # the per-substep error, the FLIP blend carries it forward (the gap to the
+    # FP64 oracle grows about 5e-6 per substep while two GPU runs agree to
+    # 1e-7), so the FLIP transfers are compared over fewer substeps
+    steps = 40 if tr == S.TRANSFER_APIC else 10
+    _, out, _, st = _gpu(zsmpm_mod, scene, _empty(), mesh, steps)
+    ref0 = oracle_mod.cloth_init(mesh, scene.dx)
+    _, ref, rst = oracle_mod.run_cloth(scene, _empty(), mesh, ref0, steps)
+    assert st["status"] == 0 and rst["status"] == 0
+    assert rel_l2(out["vx"], ref["vx"]) < 1e-6
+    assert rel_l2(out["vv"], ref["vv"]) < 1e-4
+    assert rel_l2(out["eF"], ref["eF"].reshape(-1, 9)) < 1e-5
+    # the sheet deformed: F left the rest rotations
+    assert np.abs(np.linalg.det(out["eF"].reshape(-1, 3, 3)) - 1).max() > 1e-3
+
+
+def test_sheet_on_jelly_matches_oracle(zsmpm_mod, oracle_mod):
+    """A sheet dropped onto a jelly cube: the two couple through the grid."""
+    scene, parts = S.jelly_cube(cells=10)
+    mesh = S.cloth_sheet((0.475, 0.55, 0.475), 0.35, 14, jitter=0.2, seed=3, E=2e4, nu=0.3,
+                         density=300.0, gamma=50.0, k=800.0, fa=30.0, dc=0.02)
+    mesh.v = np.tile(np.array([0.0, -1.5, 0.0], np.float32), (mesh.x.shape[0], 1))
+    steps = 100
+    _, out, mpm, st = _gpu(zsmpm_mod, scene, parts, mesh, steps)
+    ref0 = oracle_mod.cloth_init(mesh, scene.dx)
+    p, ref, rst = oracle_mod.run_cloth(scene, parts, mesh, ref0, steps)
+    free, _ = oracle_mod.run(scene, parts, steps, "f64")
+    assert st["status"] == 0 and rst["status"] == 0
+    assert rel_l2(out["vx"], ref["vx"]) < 1e-6 and rel_l2(out["vv"], ref["vv"]) < 1e-4
+    assert rel_l2(mpm["x"], p.x) < 1e-6 and rel_l2(mpm["v"], p.v) < 1e-4
+    # the cloth pushed the block
+    assert rel_l2(p.v, free.v) > 1e-3
+
+
+def test_stage_path_matches_fused(zsmpm_mod):
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    mesh = _sheet()
+    _, fused, _, _ = _gpu(zsmpm_mod, scene, _empty(), mesh, 20)
+    _, staged, _, _ = _gpu(zsmpm_mod, scene, _empty(), mesh, 20, staged=True)
+    # float atomics: the summation order differs from run to run
+    assert rel_l2(staged["vx"], fused["vx"]) < 1e-6 and rel_l2(staged["vv"], fused["vv"]) < 1e-4
+
+
+def test_cloth_rejects_differentiable_form(zsmpm_mod):
+    scene = S.Scene.unit_box(1.0 / 64, materials=[S.Material()])
+    with zsmpm_mod.Context(scene, max_particles=1) as ctx:
+        ctx.upload(_empty())
+        ctx.add_cloth(_sheet())
+        with pytest.raises(zsmpm_mod.MPMError, match="cloth"):
+            ctx.set_order_mode(True)
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_node_graph_cloth(zsmpm_mod, oracle_mod, fused):
+    """ConfigConstitutiveModel -> ToZSParticles + ToZSCloth, stepped by the
+    stage nodes (ZSPartitionForZSParticles' ZSCloth input) or ZSMPMSubstep,
+    written back by UpdatePrimitiveFromZSParticles; against the oracle."""
+    scene, parts = S.jelly_cube(cells=8)
+    scene.bc_type = S.BC_STICKY
+    scene.materials = [S.Material(S.FCR, E=5e4, nu=0.3)]
+    mesh = S.cloth_sheet((0.475, 0.5, 0.475), 0.3, 10, jitter=0.2, seed=4, model=S.FCR, E=5e4,
+                         nu=0.3, density=1000.0, gamma=50.0, k=800.0, fa=30.0, dc=0.02)
+    mesh.v = np.tile(np.array([0.0, -1.0, 0.0], np.float32), (mesh.x.shape[0], 1))
+    steps = 30
+    x, v, _, cx, cv = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", E=5e4, nu=0.3,
+                                               substeps=steps, bc="sticky", thickness=3,
+                                               fused=fused, cloth=mesh)
+    ref0 = oracle_mod.cloth_init(mesh, scene.dx)
+    p, ref, st = oracle_mod.run_cloth(scene, parts, mesh, ref0, steps)
+    assert st["status"] == 0
+    assert rel_l2(cx, ref["vx"]) < 1e-6 and rel_l2(cv, ref["vv"]) < 1e-4
+    assert rel_l2(x, p.x) < 1e-6 and rel_l2(v, p.v) < 1e-4

@@ -22,7 +22,7 @@ NODES_LIB = os.path.join(PKG, "libzsmpm_nodes.so")
 NODES = os.path.join(PKG, "nodes")
 NODE_SOURCES = ["MPMNodes.cpp", "nodes_capi.cpp"]
 
-SOURCES = ["partition.cu", "transfer.cu", "flip.cu", "adjoint.cu", "io.cu", "output.cu", "api.cu", "noalloc.cu"]
+SOURCES = ["partition.cu", "transfer.cu", "flip.cu", "cloth.cu", "adjoint.cu", "io.cu", "output.cu", "api.cu", "noalloc.cu"]
 HEADERS = ["zsmpm_internal.cuh", "mpm_math.cuh", "binning.cuh", "tile_scatter.cuh", "cp_async.cuh",
            "colliders.cuh", "blocks.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

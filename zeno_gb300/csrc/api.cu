@@ -167,7 +167,9 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], c->stream);
   };
+  const bool cloth = c->d.cloth.n_verts > 0;
   mark(MPM_STAGE_SCAN);
+  if (cloth) launch_cloth_mark(c->d, c->stream);  // the cloth's grid blocks
   launch_scan(c->d, c->stream);
   mark(MPM_STAGE_SCATTER);
   launch_scatter(c->d, c->stream);
@@ -176,10 +178,18 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   mark(MPM_STAGE_P2G);
   launch_p2g(c->d, cur, c->stream);
   mark(MPM_STAGE_GRID_UPDATE);
-  launch_grid_gather(c->d, 3, c->stream);
-  if (!c->colliders.empty()) launch_apply_colliders_listed(c->d, c->stream);
+  if (cloth) {  // particle sums, the cloth's scatter, then the update
+    launch_grid_gather(c->d, 0, c->stream);
+    launch_cloth_p2g(c->d, c->stream);
+    launch_grid_update(c->d, 3, c->stream);
+    if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
+  } else {
+    launch_grid_gather(c->d, 3, c->stream);
+    if (!c->colliders.empty()) launch_apply_colliders_listed(c->d, c->stream);
+  }
   mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, 1, c->stream);
+  if (cloth) launch_cloth_g2p(c->d, c->stream);
   mark(MPM_NUM_STAGES);
 }
 
@@ -779,6 +789,150 @@ int32_t mpm_particles_set_attr(mpm_ctx *c, const char *name, const float *values
   return MPM_OK;
 }
 
+int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!desc || desc->n_verts <= 0 || desc->n_tris <= 0 || !desc->x || !desc->tris)
+    return fail(MPM_ERR_INVALID, "a cloth needs vertices and triangles");
+  if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "a cloth needs a single-scene context");
+  if (c->d.cloth.n_verts > 0) return fail(MPM_ERR_STATE, "one cloth per context");
+  if (c->d.keep_order) return fail(MPM_ERR_INVALID, "the differentiable form takes no cloth");
+  if (desc->model != MPM_FCR && desc->model != MPM_NHK && desc->model != MPM_STVK)
+    return fail(MPM_ERR_INVALID, "cloth model must be fixed-corotated, Neo-Hookean or StVK-Hencky");
+  if (!(desc->stiffness_normal > 0.0f) && desc->stiffness_shear != 0.0f)
+    return fail(MPM_ERR_INVALID, "stiffness_normal must be positive with a shear stiffness");
+  const int64_t nv = desc->n_verts, ne = desc->n_tris;
+  if (nv >= (int64_t(1) << 31) || ne >= (int64_t(1) << 31))
+    return fail(MPM_ERR_CAPACITY, "cloth larger than 2^31 vertices or triangles");
+  for (int64_t i = 0; i < 3 * ne; ++i)
+    if (desc->tris[i] < 0 || desc->tris[i] >= nv) return fail(MPM_ERR_INVALID, "triangle index out of range");
+  // ToZSCloth (Generation.cpp:497-688): areas and frames in double, stored as float
+  const float E = desc->E, nu = desc->nu;
+  const float mu = E / (2.0f * (1.0f + nu)), lam = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+  const float dx = c->scenes[0].dx, rho = desc->density;
+  const double feps = 1.1920928955078125e-07;
+  std::vector<float> vx(3 * nv), vv(3 * nv, 0.0f), vC(9 * nv, 0.0f), vm(nv), dof(nv, 0.0f);
+  std::vector<float> ex(3 * ne), ev(3 * ne, 0.0f), eC(9 * ne, 0.0f), eF(9 * ne), ed(9 * ne),
+      eDi(9 * ne), em(ne), evol(ne), emu(ne), elam(ne);
+  const float *X = desc->x, *V = desc->v;
+  for (int64_t e = 0; e < ne; ++e) {
+    const int32_t *t = desc->tris + 3 * e;
+    float d1[3], d2[3];
+    for (int a = 0; a < 3; ++a) {
+      d1[a] = X[3 * t[1] + a] - X[3 * t[0] + a];
+      d2[a] = X[3 * t[2] + a] - X[3 * t[0] + a];
+    }
+    double e1[3], e2[3];
+    for (int a = 0; a < 3; ++a) {
+      e1[a] = double(X[3 * t[1] + a]) - double(X[3 * t[0] + a]);
+      e2[a] = double(X[3 * t[2] + a]) - double(X[3 * t[0] + a]);
+    }
+    const double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                          e1[0] * e2[1] - e1[1] * e2[0]};
+    const double area = 0.5 * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    const float vol = float(std::max(area * double(dx), 10.0 * feps));
+    evol[e] = vol;
+    em[e] = vol * rho;
+    for (int a = 0; a < 3; ++a) {
+      ex[3 * e + a] = (X[3 * t[0] + a] + X[3 * t[1] + a] + X[3 * t[2] + a]) / 3.0f;
+      if (V) ev[3 * e + a] = (V[3 * t[0] + a] + V[3 * t[1] + a] + V[3 * t[2] + a]) / 3.0f;
+    }
+    // normal from the normalised edges; rest shape in the triangle's frame:
+    // D* = [|d1|, d1.d2/|d1|, 0; 0, |d1 x d2|/|d1|, 0; 0, 0, 1]
+    double n1 = 0, n2 = 0, dot = 0;
+    for (int a = 0; a < 3; ++a) {
+      n1 += double(d1[a]) * d1[a];
+      n2 += double(d2[a]) * d2[a];
+      dot += double(d1[a]) * d2[a];
+    }
+    n1 = std::sqrt(n1);
+    n2 = std::sqrt(n2);
+    const double u1[3] = {d1[0] / n1, d1[1] / n1, d1[2] / n1}, u2[3] = {d2[0] / n2, d2[1] / n2, d2[2] / n2};
+    const double nn[3] = {u1[1] * u2[2] - u1[2] * u2[1], u1[2] * u2[0] - u1[0] * u2[2],
+                          u1[0] * u2[1] - u1[1] * u2[0]};
+    const double nl = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+    const double cx = double(d1[1]) * d2[2] - double(d1[2]) * d2[1], cy = double(d1[2]) * d2[0] - double(d1[0]) * d2[2],
+                 cz = double(d1[0]) * d2[1] - double(d1[1]) * d2[0];
+    const double a00 = n1, a01 = dot / n1, a11 = std::sqrt(cx * cx + cy * cy + cz * cz) / n1;
+    const double Di[9] = {1 / a00, -a01 / (a00 * a11), 0, 0, 1 / a11, 0, 0, 0, 1};
+    const bool degenerate = std::fabs(a11) <= 10 * feps || std::fabs(a00) <= 10 * feps;
+    emu[e] = degenerate ? 0.0f : mu;
+    elam[e] = degenerate ? 0.0f : lam;
+    float dcol[9];
+    for (int a = 0; a < 3; ++a) {
+      dcol[a * 3 + 0] = d1[a];
+      dcol[a * 3 + 1] = d2[a];
+      dcol[a * 3 + 2] = float(nn[a] / nl);
+    }
+    for (int i = 0; i < 9; ++i) {
+      ed[9 * e + i] = dcol[i];
+      eDi[9 * e + i] = float(Di[i]);
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double sum = 0;
+        for (int l = 0; l < 3; ++l) sum += double(dcol[i * 3 + l]) * Di[l * 3 + j];
+        eF[9 * e + i * 3 + j] = float(sum);
+      }
+    for (int i = 0; i < 3; ++i) dof[t[i]] += vol / 3.0f;
+  }
+  for (int64_t p = 0; p < nv; ++p) {
+    vm[p] = dof[p] * rho;
+    for (int a = 0; a < 3; ++a) {
+      vx[3 * p + a] = X[3 * p + a];
+      if (V) vv[3 * p + a] = V[3 * p + a];
+    }
+  }
+  ClothDev &cl = c->d.cloth;
+  ClothDev nc{};
+  auto up = [&](float **dst, const std::vector<float> &h) -> int32_t {
+    int32_t r = dalloc(c, dst, h.size());
+    if (r) return r;
+    ZS_CUDA(cudaMemcpyAsync(*dst, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    return MPM_OK;
+  };
+  if ((rc = up(&nc.vx, vx)) || (rc = up(&nc.vv, vv)) || (rc = up(&nc.vC, vC)) || (rc = up(&nc.vm, vm)) ||
+      (rc = up(&nc.imp, std::vector<float>(3 * nv, 0.0f))) || (rc = up(&nc.ex, ex)) ||
+      (rc = up(&nc.ev, ev)) || (rc = up(&nc.eC, eC)) || (rc = up(&nc.eF, eF)) || (rc = up(&nc.ed, ed)) ||
+      (rc = up(&nc.eDmInv, eDi)) || (rc = up(&nc.em, em)) || (rc = up(&nc.evol, evol)) ||
+      (rc = up(&nc.emu, emu)) || (rc = up(&nc.elam, elam)))
+    return rc;
+  if ((rc = dalloc(c, &nc.inds, (size_t)3 * ne))) return rc;
+  ZS_CUDA(cudaMemcpyAsync(nc.inds, desc->tris, 3 * ne * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  nc.n_verts = nv;
+  nc.n_eles = ne;
+  nc.model = desc->model;
+  nc.gamma = desc->stiffness_shear;
+  nc.k = desc->stiffness_normal;
+  nc.fc = std::tan(desc->friction_angle / 3.14159265358979323846f);
+  nc.dc = desc->damping_coeff;
+  cl = nc;
+  drop_graphs(c);  // the substep gains the cloth's kernels
+  c->partition_valid = false;
+  return MPM_OK;
+}
+
+int32_t mpm_cloth_download(mpm_ctx *c, float *vx, float *vv, float *vC, float *ex, float *ev,
+                           float *eC, float *eF, float *ed) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  const ClothDev &cl = c->d.cloth;
+  if (cl.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
+  auto get = [&](float *h, const float *dsrc, long long count) -> int32_t {
+    if (!h) return MPM_OK;
+    ZS_CUDA(cudaMemcpyAsync(h, dsrc, count * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    return MPM_OK;
+  };
+  const long long nv = cl.n_verts, ne = cl.n_eles;
+  if ((rc = get(vx, cl.vx, 3 * nv)) || (rc = get(vv, cl.vv, 3 * nv)) || (rc = get(vC, cl.vC, 9 * nv)) ||
+      (rc = get(ex, cl.ex, 3 * ne)) || (rc = get(ev, cl.ev, 3 * ne)) || (rc = get(eC, cl.eC, 9 * ne)) ||
+      (rc = get(eF, cl.eF, 9 * ne)) || (rc = get(ed, cl.ed, 9 * ne)))
+    return rc;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
 int32_t mpm_compute_von_mises(mpm_ctx *c, int32_t by_log1p) {
   int32_t rc = check(c);
   if (rc) return rc;
@@ -870,6 +1024,7 @@ int32_t mpm_partition(mpm_ctx *c) {
   set_auto_step(c, 0);  // the stage path moves colliders only on request
   if ((rc = push_params(c)) || (rc = prepare_partition(c))) return rc;
   enqueue_bin_if_needed(c);
+  if (c->d.cloth.n_verts > 0) launch_cloth_mark(c->d, c->stream);
   enqueue_sort(c);
   if ((rc = launch_check("partition"))) return rc;
   c->partition_valid = true;
@@ -891,6 +1046,7 @@ int32_t mpm_p2g(mpm_ctx *c, float dt) {
   if ((rc = set_dt(c, dt))) return rc;
   launch_p2g(c->d, c->cur, c->stream);
   launch_grid_gather(c->d, 0, c->stream);  // grid = m, mv as after the reference P2G
+  if (c->d.cloth.n_verts > 0) launch_cloth_p2g(c->d, c->stream);
   return launch_check("p2g");
 }
 
@@ -950,6 +1106,7 @@ int32_t mpm_g2p(mpm_ctx *c, float dt) {
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "g2p needs the partition used by p2g");
   if ((rc = set_dt(c, dt))) return rc;
   launch_g2p(c->d, c->cur, 0, 0, c->stream);
+  if (c->d.cloth.n_verts > 0) launch_cloth_g2p(c->d, c->stream);
   if ((rc = launch_check("g2p"))) return rc;
   c->cur = 1 - c->cur;
   c->partition_valid = false;
@@ -1053,6 +1210,8 @@ int32_t mpm_set_order_mode(mpm_ctx *c, int32_t keep) {
   if (rc) return rc;
   if (keep && c->d.transfer != MPM_TRANSFER_APIC)
     return fail(MPM_ERR_INVALID, "the differentiable form takes the APIC transfer only");
+  if (keep && c->d.cloth.n_verts > 0)
+    return fail(MPM_ERR_INVALID, "the differentiable form takes no cloth");
   if (keep && !c->d.ptile_adj && (rc = dalloc(c, &c->d.ptile_adj, (size_t)c->d.cap_gblocks * kTileNodes)))
     return rc;
   ZS_CUDA(cudaStreamSynchronize(c->stream));

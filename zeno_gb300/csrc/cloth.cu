@@ -1,0 +1,492 @@
+// Codimensional cloth (ToZSCloth, Generation.cpp:432-689; Jiang et al. 2017,
+// "Anisotropic elastoplasticity for cloth, knit and hair frictional
+// contact"): a triangle mesh whose vertices and per-triangle quadrature
+// points ("elements") both carry mass on the MPM grid.
+//  * mark: the blocks of every vertex and element and their 26 neighbours
+//    join the grid blocks of the next partition (no particle blocks);
+//  * P2G (p2g_surface, Transfer.cu:656-842): per element, P from the
+//    Gram-Schmidt QR of F (in-plane 2x2 model stress, normal compression -k
+//    (1 - r33)^2 and shear gamma terms, P += Q A R^-T), the normal-direction
+//    force P_c3 (grad W . d_c3)(-vol dt) and the element's mass and momentum
+//    on its 27 nodes (type i), the in-plane force as impulses on its three
+//    vertices (type ii); then per vertex its mass, momentum and impulse.
+//    FLIP grids take the forces in vstar.  Float atomics into the grid the
+//    particle tiles were gathered into (grid update after this);
+//  * G2P (Transfer.cu:1287-1445): vertices as damped APIC (C = skew + (1 -
+//    dc) sym; or the FLIP-style blend), then elements: damped C, centroid
+//    and mean velocity of their vertices, d1 = p1 - p0, d2 = p2 - p0, d3 +=
+//    (dt C + dt^2 / 2 C^2) d3, F = d DmInv, and the surface return mapping
+//    (MPMPipeline.cu:973-1011) on d = Q R.
+#include <cuda_runtime.h>
+
+#include "binning.cuh"
+#include "mpm_math.cuh"
+#include "zsmpm_internal.cuh"
+
+namespace zsmpm {
+namespace {
+
+struct V3 {
+  float x, y, z;
+};
+__device__ __forceinline__ V3 ld3(const float *p) { return V3{p[0], p[1], p[2]}; }
+
+// grid node index of node I of scene 0, or -1 outside the grid blocks
+__device__ __forceinline__ long long node_of(const DevPtrs &d, const SceneParams &S, int i0, int i1,
+                                             int i2) {
+  const int b0 = (i0 >> 2) - S.block_lo[0], b1 = (i1 >> 2) - S.block_lo[1],
+            b2 = (i2 >> 2) - S.block_lo[2];
+  if ((unsigned)b0 >= (unsigned)S.block_dims[0] || (unsigned)b1 >= (unsigned)S.block_dims[1] ||
+      (unsigned)b2 >= (unsigned)S.block_dims[2])
+    return -1;
+  const int gb = d.dir_gb[S.dir_off + (b0 * S.block_dims[1] + b1) * S.block_dims[2] + b2];
+  if (gb < 0 || gb >= d.cap_gblocks) return -1;
+  return (long long)gb * 64 + (((i0 & 3) << 4) | ((i1 & 3) << 2) | (i2 & 3));
+}
+
+// w' of the quadratic B-spline with respect to the particle position (cells)
+__device__ __forceinline__ float wgrad(const Stencil1 &s, int o) {
+  return o == 0 ? s.f - 1.5f : (o == 1 ? -2.0f * (s.f - 1.0f) : s.f - 0.5f);
+}
+
+// Gram-Schmidt QR of the columns of F (row-major): q2 = q0 x q1, R = Q^T F
+// upper triangular with a signed r22
+__device__ __forceinline__ void gram_schmidt(const float (&F)[9], float (&Q)[9], float (&R)[9]) {
+  const float f0[3] = {F[0], F[3], F[6]}, f1[3] = {F[1], F[4], F[7]}, f2[3] = {F[2], F[5], F[8]};
+  const float r00 = sqrtf(f0[0] * f0[0] + f0[1] * f0[1] + f0[2] * f0[2]);
+  const float q0[3] = {f0[0] / r00, f0[1] / r00, f0[2] / r00};
+  const float r01 = q0[0] * f1[0] + q0[1] * f1[1] + q0[2] * f1[2];
+  const float u[3] = {f1[0] - r01 * q0[0], f1[1] - r01 * q0[1], f1[2] - r01 * q0[2]};
+  const float r11 = sqrtf(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  const float q1[3] = {u[0] / r11, u[1] / r11, u[2] / r11};
+  const float q2[3] = {q0[1] * q1[2] - q0[2] * q1[1], q0[2] * q1[0] - q0[0] * q1[2],
+                       q0[0] * q1[1] - q0[1] * q1[0]};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Q[i * 3 + 0] = q0[i];
+    Q[i * 3 + 1] = q1[i];
+    Q[i * 3 + 2] = q2[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = 0.0f;
+  R[0] = r00;
+  R[1] = r01;
+  R[2] = q0[0] * f2[0] + q0[1] * f2[1] + q0[2] * f2[2];
+  R[4] = r11;
+  R[5] = q1[0] * f2[0] + q1[1] * f2[1] + q1[2] * f2[2];
+  R[8] = q2[0] * f2[0] + q2[1] * f2[1] + q2[2] * f2[2];
+}
+
+// first Piola-Kirchhoff stress of a 2x2 deformation [a b; c d]: fixed
+// corotated 2 mu (F - R) + lam (J - 1) cof F (Stomakhin et al. 2012, R the
+// closest rotation), Neo-Hookean mu (F - F^-T) + lam ln J F^-T, StVK-Hencky
+// F V diag((2 mu e_i + lam sum e) / s_i^2) V^T (Klar et al. 2016)
+__device__ __forceinline__ void first_piola_2d(int model, float mu, float lam, const float (&F)[4],
+                                               float (&P)[4]) {
+  const float a = F[0], b = F[1], c = F[2], d = F[3];
+  const float J = a * d - b * c;
+  const float cof[4] = {d, -c, -b, a};
+  if (model == MPM_FCR) {
+    const float p = a + d, q = c - b, rn = rsqrtf(p * p + q * q);
+    const float Rr[4] = {p * rn, -q * rn, q * rn, p * rn};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) P[i] = 2.0f * mu * (F[i] - Rr[i]) + lam * (J - 1.0f) * cof[i];
+    return;
+  }
+  if (model == MPM_NHK) {
+    const float rJ = 1.0f / J, l = lam * logf(J);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) P[i] = mu * (F[i] - cof[i] * rJ) + l * cof[i] * rJ;
+    return;
+  }
+  const float c00 = a * a + c * c, c01 = a * b + c * d, c11 = b * b + d * d;
+  const float tr = c00 + c11, det = c00 * c11 - c01 * c01;
+  const float disc = sqrtf(fmaxf(0.0f, 0.25f * (c00 - c11) * (c00 - c11) + c01 * c01));
+  const float l0 = 0.5f * tr + disc, l1 = det / l0;  // l1 from the product: no cancellation
+  float v0[2];
+  if (fabsf(c01) > 0.0f) {
+    v0[0] = l0 - c11;
+    v0[1] = c01;
+  } else if (c00 >= c11) {
+    v0[0] = 1.0f;
+    v0[1] = 0.0f;
+  } else {
+    v0[0] = 0.0f;
+    v0[1] = 1.0f;
+  }
+  const float nv = rsqrtf(v0[0] * v0[0] + v0[1] * v0[1]);
+  v0[0] *= nv;
+  v0[1] *= nv;
+  const float v1[2] = {-v0[1], v0[0]};
+  const float e0 = 0.5f * logf(l0), e1 = 0.5f * logf(l1);
+  const float g0 = (2.0f * mu * e0 + lam * (e0 + e1)) / l0, g1 = (2.0f * mu * e1 + lam * (e0 + e1)) / l1;
+  const float S[4] = {g0 * v0[0] * v0[0] + g1 * v1[0] * v1[0], g0 * v0[0] * v0[1] + g1 * v1[0] * v1[1],
+                      g0 * v0[1] * v0[0] + g1 * v1[1] * v1[0], g0 * v0[1] * v0[1] + g1 * v1[1] * v1[1]};
+  P[0] = a * S[0] + b * S[2];
+  P[1] = a * S[1] + b * S[3];
+  P[2] = c * S[0] + d * S[2];
+  P[3] = c * S[1] + d * S[3];
+}
+
+__device__ __forceinline__ void matmul3(const float (&A)[9], const float (&B)[9], float (&C)[9]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[i * 3 + j] = A[i * 3 + 0] * B[0 * 3 + j] + A[i * 3 + 1] * B[1 * 3 + j] + A[i * 3 + 2] * B[2 * 3 + j];
+}
+
+// the blocks of the cloth's vertices and elements (and their neighbours)
+// join the next partition's grid blocks
+__global__ void k_cloth_mark(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const long long n = cl.n_verts + cl.n_eles;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float *x = i < cl.n_verts ? cl.vx + 3 * i : cl.ex + 3 * (i - cl.n_verts);
+    const int key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
+    if (key < 0) continue;
+    const int dd = key >> 6, dy = S.block_dims[1], dz = S.block_dims[2];
+    for (int a = -1; a <= 1; ++a)
+      for (int b = -1; b <= 1; ++b)
+        for (int c = -1; c <= 1; ++c) d.dir_flag[dd + (a * dy + b) * dz + c] = 1;
+  }
+}
+
+// element P2G (type i on the grid, type ii impulses on the vertices)
+__global__ void k_cloth_p2g_elements(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const float dt = d.prm->dt, dx = S.dx, inv_dx = S.inv_dx;
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC, affine = d.transfer != MPM_TRANSFER_FLIP;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cl.n_eles;
+       e += (long long)gridDim.x * blockDim.x) {
+    float F[9], dm[9], Q[9], R[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      F[i] = cl.eF[9 * e + i];
+      dm[i] = cl.ed[9 * e + i];
+    }
+    gram_schmidt(F, Q, R);
+    const float R2[4] = {R[0], R[1], R[3], R[4]};
+    float P2[4];
+    first_piola_2d(cl.model, cl.emu[e], cl.elam[e], R2, P2);
+    float P[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      P[i * 3 + 0] = Q[i * 3 + 0] * P2[0] + Q[i * 3 + 1] * P2[2];
+      P[i * 3 + 1] = Q[i * 3 + 0] * P2[1] + Q[i * 3 + 1] * P2[3];
+      P[i * 3 + 2] = 0.0f;
+    }
+    const float g = cl.gamma;
+    float gf = 0.0f;
+    if (R[8] < 1.0f) {
+      const float vv = 1.0f - R[8];
+      gf = -cl.k * vv * vv;
+    }
+    const float A[9] = {g * R[2] * R[2], g * R[2] * R[5], g * R[2] * R[8],
+                        g * R[2] * R[5], g * R[5] * R[5], g * R[5] * R[8],
+                        g * R[2] * R[8], g * R[5] * R[8], gf * R[8]};
+    const float i00 = 1.0f / R[0], i11 = 1.0f / R[4], i22 = 1.0f / R[8];
+    const float i01 = -R[1] * i00 * i11, i12 = -R[5] * i11 * i22;
+    const float i02 = (R[1] * R[5] - R[2] * R[4]) * i00 * i11 * i22;
+    const float RiT[9] = {i00, 0.0f, 0.0f, i01, i11, 0.0f, i02, i12, i22};  // R^-T
+    float QA[9], T[9];
+    matmul3(Q, A, QA);
+    matmul3(QA, RiT, T);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) P[i] += T[i];
+    const float mass = cl.em[e], vol = cl.evol[e];
+    const V3 ve = ld3(cl.ev + 3 * e);
+    float C[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = affine ? cl.eC[9 * e + i] : 0.0f;
+    const float x[3] = {cl.ex[3 * e], cl.ex[3 * e + 1], cl.ex[3 * e + 2]};
+    const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx), s2 = stencil1(x[2], inv_dx);
+    const float kf = -vol * dt;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
+          if (idx < 0) {
+            atomicOr(&d.cnt->status, ST_STENCIL);
+            continue;
+          }
+          const float W = s0.w[i] * s1.w[j] * s2.w[k];
+          const float gw[3] = {wgrad(s0, i) * s1.w[j] * s2.w[k] * inv_dx,
+                               s0.w[i] * wgrad(s1, j) * s2.w[k] * inv_dx,
+                               s0.w[i] * s1.w[j] * wgrad(s2, k) * inv_dx};
+          const float sft = (gw[0] * dm[2] + gw[1] * dm[5] + gw[2] * dm[8]) * kf;
+          const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
+          const float vn[3] = {ve.x, ve.y, ve.z};
+          float mom[3], fo[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float Cx = C[a * 3 + 0] * xi[0] + C[a * 3 + 1] * xi[1] + C[a * 3 + 2] * xi[2];
+            fo[a] = P[a * 3 + 2] * sft;
+            mom[a] = W * mass * (vn[a] + Cx) + (flip_style ? 0.0f : fo[a]);
+          }
+          float4 *g4 = d.grid + idx;
+          atomicAdd(&g4->x, W * mass);
+          atomicAdd(&g4->y, mom[0]);
+          atomicAdd(&g4->z, mom[1]);
+          atomicAdd(&g4->w, mom[2]);
+          if (flip_style) {
+            float4 *h4 = d.grid2 + idx;
+            atomicAdd(&h4->x, fo[0]);
+            atomicAdd(&h4->y, fo[1]);
+            atomicAdd(&h4->z, fo[2]);
+          }
+        }
+    // type (ii): impulses from the in-plane columns of P through DmInv rows
+    const float r0[2] = {cl.eDmInv[9 * e + 0], cl.eDmInv[9 * e + 1]};
+    const float r1[2] = {cl.eDmInv[9 * e + 3], cl.eDmInv[9 * e + 4]};
+#pragma unroll
+    for (int vi = 0; vi < 3; ++vi) {
+      const int t = cl.inds[3 * e + vi];
+      if (t < 0 || t >= cl.n_verts) continue;
+      float Dr0, Dr1, coeff;
+      if (vi == 0) {
+        Dr0 = r0[0] + r1[0];
+        Dr1 = r0[1] + r1[1];
+        coeff = vol * dt;
+      } else {
+        Dr0 = vi == 1 ? r0[0] : r1[0];
+        Dr1 = vi == 1 ? r0[1] : r1[1];
+        coeff = -vol * dt;
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        atomicAdd(&cl.imp[3 * t + a], coeff * (P[a * 3 + 0] * Dr0 + P[a * 3 + 1] * Dr1));
+    }
+  }
+}
+
+// vertex P2G: mass, momentum and the impulse of its elements
+__global__ void k_cloth_p2g_verts(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const float dx = S.dx, inv_dx = S.inv_dx;
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC, affine = d.transfer != MPM_TRANSFER_FLIP;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < cl.n_verts;
+       p += (long long)gridDim.x * blockDim.x) {
+    const float mass = cl.vm[p];
+    const float vp[3] = {cl.vv[3 * p], cl.vv[3 * p + 1], cl.vv[3 * p + 2]};
+    const float im[3] = {cl.imp[3 * p], cl.imp[3 * p + 1], cl.imp[3 * p + 2]};
+    float C[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = affine ? cl.vC[9 * p + i] : 0.0f;
+    const Stencil1 s0 = stencil1(cl.vx[3 * p], inv_dx), s1 = stencil1(cl.vx[3 * p + 1], inv_dx),
+                   s2 = stencil1(cl.vx[3 * p + 2], inv_dx);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
+          if (idx < 0) {
+            atomicOr(&d.cnt->status, ST_STENCIL);
+            continue;
+          }
+          const float W = s0.w[i] * s1.w[j] * s2.w[k];
+          const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
+          float mom[3];
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const float Cx = C[a * 3 + 0] * xi[0] + C[a * 3 + 1] * xi[1] + C[a * 3 + 2] * xi[2];
+            mom[a] = flip_style ? W * mass * (vp[a] + Cx) : W * (mass * (vp[a] + Cx) + im[a]);
+          }
+          float4 *g4 = d.grid + idx;
+          atomicAdd(&g4->x, W * mass);
+          atomicAdd(&g4->y, mom[0]);
+          atomicAdd(&g4->z, mom[1]);
+          atomicAdd(&g4->w, mom[2]);
+          if (flip_style) {
+            float4 *h4 = d.grid2 + idx;
+            atomicAdd(&h4->x, W * im[0]);
+            atomicAdd(&h4->y, W * im[1]);
+            atomicAdd(&h4->z, W * im[2]);
+          }
+        }
+  }
+}
+
+// sum W v, sum W vstar and the damped affine velocity (from v, or vstar on
+// FLIP grids) at x
+__device__ __forceinline__ void cloth_gather(const DevPtrs &d, const SceneParams &S, const float *x,
+                                             bool flip_style, float dc, float (&vel)[3],
+                                             float (&vs)[3], float (&Cn)[9]) {
+  const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
+  const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx), s2 = stencil1(x[2], inv_dx);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) vel[a] = vs[a] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Cn[i] = 0.0f;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) {
+        const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
+        if (idx < 0) {
+          atomicOr(&d.cnt->status, ST_STENCIL);
+          continue;
+        }
+        const float W = s0.w[i] * s1.w[j] * s2.w[k];
+        const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
+        const float4 g = d.grid[idx];
+        const float v[3] = {g.y, g.z, g.w};
+        float u[3] = {v[0], v[1], v[2]};
+        if (flip_style) {
+          const float4 h = d.grid2[idx];
+          vs[0] += W * h.x;
+          vs[1] += W * h.y;
+          vs[2] += W * h.z;
+          u[0] = h.x;
+          u[1] = h.y;
+          u[2] = h.z;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          vel[a] += W * v[a];
+#pragma unroll
+          for (int b = 0; b < 3; ++b) Cn[a * 3 + b] += W * Dinv * u[a] * xi[b];
+        }
+      }
+  float D[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      D[a * 3 + b] = 0.5f * (Cn[a * 3 + b] - Cn[b * 3 + a]) + (1.0f - dc) * 0.5f * (Cn[a * 3 + b] + Cn[b * 3 + a]);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Cn[i] = D[i];
+}
+
+__global__ void k_cloth_g2p_verts(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const float dt = d.prm->dt;
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < cl.n_verts;
+       p += (long long)gridDim.x * blockDim.x) {
+    float vel[3], vs[3], Cn[9];
+    cloth_gather(d, S, cl.vx + 3 * p, flip_style, cl.dc, vel, vs, Cn);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (flip_style) {  // beta = 0 for the cloth
+        const float d0 = cl.vv[3 * p + a] - vel[a];
+        cl.vv[3 * p + a] = vs[a] + 0.99f * d0;
+        cl.vx[3 * p + a] += dt * vs[a];
+      } else {
+        cl.vv[3 * p + a] = vel[a];
+        cl.vx[3 * p + a] += vel[a] * dt;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) cl.vC[9 * p + i] = Cn[i];
+  }
+}
+
+// element G2P and the surface return mapping (after the vertices moved)
+__global__ void k_cloth_g2p_elements(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const float dt = d.prm->dt;
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cl.n_eles;
+       e += (long long)gridDim.x * blockDim.x) {
+    float vel[3], vs[3], Cn[9];
+    cloth_gather(d, S, cl.ex + 3 * e, flip_style, cl.dc, vel, vs, Cn);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) cl.eC[9 * e + i] = Cn[i];
+    int t[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) t[i] = min(max(cl.inds[3 * e + i], 0), (int)cl.n_verts - 1);
+    float p[3][3], v[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        p[i][a] = cl.vx[3 * t[i] + a];
+        v[i][a] = cl.vv[3 * t[i] + a];
+      }
+    float dm[9], CC[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) dm[i] = cl.ed[9 * e + i];
+    matmul3(Cn, Cn, CC);
+    const float d3[3] = {dm[2], dm[5], dm[8]};
+    float n3[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float s = d3[a];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) s += (dt * Cn[a * 3 + b] + 0.5f * dt * dt * CC[a * 3 + b]) * d3[b];
+      n3[a] = s;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      cl.ex[3 * e + a] = (p[0][a] + p[1][a] + p[2][a]) / 3.0f;
+      cl.ev[3 * e + a] = (v[0][a] + v[1][a] + v[2][a]) / 3.0f;
+      dm[a * 3 + 0] = p[1][a] - p[0][a];
+      dm[a * 3 + 1] = p[2][a] - p[0][a];
+      dm[a * 3 + 2] = n3[a];
+    }
+    // return_mapping_surface on d = Q R
+    float Q[9], R[9];
+    gram_schmidt(dm, Q, R);
+    const float gamma = cl.gamma, k = cl.k, fc = cl.fc;
+    bool apply = false;
+    if (gamma == 0.0f) {
+      R[2] = R[5] = 0.0f;
+      R[8] = fminf(R[8], 1.0f);
+      apply = true;
+    } else if (R[8] > 1.0f) {
+      R[2] = R[5] = 0.0f;
+      R[8] = 1.0f;
+      apply = true;
+    } else if (R[8] <= 0.0f) {
+      R[2] = R[5] = 0.0f;
+      R[8] = fmaxf(R[8], -1.0f);
+      apply = true;
+    } else if (R[8] < 1.0f) {
+      const float rr = R[2] * R[2] + R[5] * R[5], r = R[8] - 1.0f, gk = gamma / k;
+      const float zz = fc * r * r;
+      if (gk * gk * rr - zz * zz > 0.0f) {
+        const float scale = zz / (gk * sqrtf(rr));
+        R[2] *= scale;
+        R[5] *= scale;
+        apply = true;
+      }
+    }
+    if (apply) matmul3(Q, R, dm);
+    float Di[9], Fn[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Di[i] = cl.eDmInv[9 * e + i];
+    matmul3(dm, Di, Fn);
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      cl.ed[9 * e + i] = dm[i];
+      cl.eF[9 * e + i] = Fn[i];
+      finite = finite && isfinite(Fn[i]);
+    }
+    if (!finite) atomicOr(&d.cnt->status, ST_NAN);
+  }
+}
+
+}  // namespace
+
+void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
+  k_cloth_mark<<<d.num_sms * 4, 256, 0, s>>>(d);
+}
+
+void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
+  cudaMemsetAsync(d.cloth.imp, 0, (size_t)d.cloth.n_verts * 3 * sizeof(float), s);
+  k_cloth_p2g_elements<<<d.num_sms * 4, 128, 0, s>>>(d);
+  k_cloth_p2g_verts<<<d.num_sms * 4, 128, 0, s>>>(d);
+}
+
+void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s) {
+  k_cloth_g2p_verts<<<d.num_sms * 4, 128, 0, s>>>(d);
+  k_cloth_g2p_elements<<<d.num_sms * 4, 128, 0, s>>>(d);
+}
+
+}  // namespace zsmpm

@@ -150,6 +150,18 @@ inline void collider_world_box(ColliderDev &c) {
   }
 }
 
+// Codimensional cloth (ToZSCloth): vertex and element arrays (AoS, row-major
+// 3x3 matrices), the in-plane model and the cloth parameters; n_verts = 0
+// when the context holds no cloth.
+struct ClothDev {
+  long long n_verts, n_eles;
+  int model;                 // MPM_FCR / MPM_NHK / MPM_STVK
+  float gamma, k, fc, dc;    // shear stiffness, normal stiffness, tan(fa / pi), damping
+  float *vx, *vv, *vC, *vm, *imp;
+  float *ex, *ev, *eC, *eF, *ed, *eDmInv, *em, *evol, *emu, *elam;
+  int32_t *inds;
+};
+
 // One scene of a context: its grid spacing, its slice of the concatenated
 // block directory, its boundary and gravity.  A context holds one scene
 // (the plain substep) or many independent scenes (the batched substep).
@@ -194,6 +206,7 @@ struct DevPtrs {
   ColliderDev *colliders;  // kMaxColliders entries (device)
   int32_t *near_gb;        // cap_gblocks entries: the grid blocks near a collider
   float *vms;              // ComputeVonMises per particle, by upload index (0 at upload)
+  ClothDev cloth;          // n_verts = 0: no cloth
   int keep_order;     // differentiable mode: G2P writes each particle to its own slot
   int planar_x;       // pbuf[0] holds positions as 3 planes of `cap` floats (binning only)
   int32_t *tile_sums;
@@ -220,6 +233,11 @@ void launch_grid_update_flip(const DevPtrs &d, int mode, cudaStream_t s);
 void launch_g2p_flip(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s);
 // ComputeParticleBeta: collider -1 (volume criterion only) or a collider id
 void launch_particle_beta(const DevPtrs &d, int cur, float dt, int collider, cudaStream_t s);
+
+// cloth.cu
+void launch_cloth_mark(const DevPtrs &d, cudaStream_t s);
+void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s);
+void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s);
 
 // output.cu
 void launch_von_mises(const DevPtrs &d, int cur, int by_log1p, cudaStream_t s);

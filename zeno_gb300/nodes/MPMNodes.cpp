@@ -35,6 +35,7 @@ inline std::vector<vec3f> *vel(PrimitiveObject &p, bool create) {
 inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::string &k) {
   return p.verts.has_attr(k) ? &p.verts.attr<float>(k) : nullptr;
 }
+inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris.values; }
 }  // namespace prim_access
 }  // namespace zeno
 #else
@@ -55,6 +56,7 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
   auto it = p.attrs1.find(k);
   return it == p.attrs1.end() ? nullptr : &it->second;
 }
+inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris; }
 }  // namespace prim_access
 }  // namespace zeno
 #endif
@@ -89,6 +91,11 @@ struct ZenoConstitutiveModel : IObject {
 // ToZSParticles output (Structures.hpp:134-531)
 struct ZenoParticles : IObject {
   std::shared_ptr<MpmContext> ctx;
+  // ToZSCloth: the mesh and cloth parameters, attached to the context of the
+  // particles it is stepped with (one cloth per context)
+  bool cloth = false;
+  mpm_cloth_desc cloth_desc{};
+  std::weak_ptr<MpmContext> cloth_ctx;
   std::shared_ptr<PrimitiveObject> prim;  // the source primitive, written back by
                                           // UpdatePrimitiveFromZSParticles
   std::shared_ptr<ZenoConstitutiveModel> model;
@@ -172,6 +179,29 @@ int32_t transfer_of(const ZenoGrid &g) {
   return MPM_TRANSFER_APIC;
 }
 
+// a ToZSCloth cloth joins the particles' context once; its primitive
+// provides the mesh
+void attach_cloth(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &cl) {
+  if (!cl.cloth) throw std::runtime_error("ZSCloth: the input is not a ToZSCloth output");
+  if (cl.cloth_ctx.lock() == ctx) return;
+  if (cl.cloth_ctx.lock()) throw std::runtime_error("ZSCloth: the cloth belongs to another context");
+  auto &pos = prim_access::pos(*cl.prim);
+  const auto &tr = prim_access::tris(*cl.prim);
+  std::vector<int32_t> tris(3 * tr.size());
+  for (size_t i = 0; i < tr.size(); ++i)
+    for (int a = 0; a < 3; ++a) tris[3 * i + a] = tr[i][a];
+  const auto *v = prim_access::vel(*cl.prim, false);
+  mpm_cloth_desc d = cl.cloth_desc;
+  d.n_verts = (int64_t)pos.size();
+  d.x = pos.empty() ? nullptr : pos[0].data();
+  d.v = v && v->size() == pos.size() ? (*v)[0].data() : nullptr;
+  d.n_tris = (int64_t)tr.size();
+  d.tris = tris.data();
+  check(mpm_cloth_create(ctx->h, &d), "mpm_cloth_create");
+  cl.cloth_ctx = ctx;
+  cl.ctx = ctx;
+}
+
 std::shared_ptr<MpmContext> bound_ctx(const std::shared_ptr<ZenoPartition> &p, const char *node) {
   if (!p->ctx)
     throw std::runtime_error(std::string(node) +
@@ -240,6 +270,48 @@ ZENDEFNODE(ConfigConstitutiveModel, {
                                         {},
                                         {"MPM"},
                                     });
+
+/// ToZSCloth (Generation.cpp:432-689): a triangle mesh as codimensional
+/// cloth with the model's in-plane elasticity; the cloth joins the context of
+/// the particles it is stepped with (ZSMPMSubstep / ZSPartitionForZSParticles
+/// input "ZSCloth").
+struct ToZSCloth : INode {
+  void apply() override {
+    auto model = get_input<ZenoConstitutiveModel>("ZSModel");
+    auto prim = get_input<PrimitiveObject>("prim");
+    if (prim_access::tris(*prim).empty())
+      throw std::runtime_error("ToZSCloth: the primitive has no triangles");
+    const int type = model->mat.type;
+    if (type != MPM_FCR && type != MPM_NHK && type != MPM_STVK)
+      throw std::runtime_error("ToZSCloth: the model must be fcr, nhk or stvk");
+    auto out = std::make_shared<ZenoParticles>();
+    out->prim = prim;
+    out->model = model;
+    out->cloth = true;
+    out->category = 2;  // ZenoParticles::surface
+    mpm_cloth_desc &d = out->cloth_desc;
+    d.model = type;
+    d.E = model->mat.E;
+    d.nu = model->mat.nu;
+    d.density = model->density;
+    d.stiffness_shear = get_input2<float>("stiffness_shear");
+    d.stiffness_normal = get_input2<float>("stiffness_normal");
+    d.friction_angle = get_input2<float>("friction_angle");
+    d.damping_coeff = get_input2<float>("damping_coeff");
+    set_output("ZSParticles", out);
+  }
+};
+ZENDEFNODE(ToZSCloth, {
+                          {"ZSModel",
+                           "prim",
+                           {"float", "stiffness_shear", "0."},
+                           {"float", "stiffness_normal", "800."},
+                           {"float", "friction_angle", "0."},
+                           {"float", "damping_coeff", "0."}},
+                          {"ZSParticles"},
+                          {},
+                          {"MPM"},
+                      });
 
 /// ToZSParticles (Generation.cpp:690-1145): m = vol * density, F = I, C = 0.
 /// The device context is sized for the primitive: its block directory spans
@@ -371,13 +443,16 @@ struct ZSPartitionForZSParticles : INode {
     table->ctx = pars->ctx;
     grid->ctx = pars->ctx;
     check(mpm_set_transfer(pars->ctx->h, transfer_of(*grid)), "mpm_set_transfer");
+    if (has_input<ZenoParticles>("ZSCloth"))  // a cloth stepped with these particles
+      attach_cloth(pars->ctx, *get_input<ZenoParticles>("ZSCloth"));
     check(mpm_partition(pars->ctx->h), "mpm_partition");
     table->rebuilt = true;
     set_output("ZSPartition", table);
   }
 };
 ZENDEFNODE(ZSPartitionForZSParticles, {
-                                          {"ZSPartition", "ZSGrid", "ZSParticles", {"float", "ppb", "1"}},
+                                          {"ZSPartition", "ZSGrid", "ZSParticles", {"float", "ppb", "1"},
+                                           "ZSCloth"},
                                           {"ZSPartition"},
                                           {{"enum force cache", "strategy", "force"}},
                                           {"MPM"},
@@ -807,6 +882,26 @@ ZENDEFNODE(AdjustParticleMaterial, {
 struct UpdatePrimitiveFromZSParticles : INode {
   void apply() override {
     auto pars = get_input<ZenoParticles>("ZSParticles");
+    if (pars->cloth) {  // the cloth's vertices back into its mesh
+      auto ctx = pars->cloth_ctx.lock();
+      if (ctx && pars->prim) {
+        auto &pos = prim_access::pos(*pars->prim);
+        const int64_t n = (int64_t)pos.size();
+        std::vector<float> x(3 * n), v(3 * n);
+        check(mpm_cloth_download(ctx->h, x.data(), v.data(), nullptr, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr),
+              "mpm_cloth_download");
+        auto &vel = *prim_access::vel(*pars->prim, true);
+        vel.resize(n);
+        for (int64_t i = 0; i < n; ++i)
+          for (int d = 0; d < 3; ++d) {
+            pos[i][d] = x[3 * i + d];
+            vel[i][d] = v[3 * i + d];
+          }
+      }
+      set_output("ZSParticles", pars);
+      return;
+    }
     if (pars->prim) {
       const int64_t n = pars->n;
       std::vector<float> x(3 * n), v(3 * n);
@@ -882,6 +977,8 @@ struct ZSMPMSubstep : INode {
     // device (b += db/dt dt, s += ds/dt dt at the start of each substep)
     if (has_input<ZenoBoundary>("ZSCollider"))
       attach_boundary(ctx, *get_input<ZenoBoundary>("ZSCollider"));
+    if (has_input<ZenoParticles>("ZSCloth"))
+      attach_cloth(ctx, *get_input<ZenoParticles>("ZSCloth"));
     // the transfer scheme of a MakeZSGrid (default APIC)
     if (has_input<ZenoGrid>("ZSGrid"))
       check(mpm_set_transfer(ctx->h, transfer_of(*get_input<ZenoGrid>("ZSGrid"))),
@@ -899,6 +996,7 @@ ZENDEFNODE(ZSMPMSubstep, {
                               "ZSBoundary",
                               "ZSCollider",
                               "ZSGrid",
+                              "ZSCloth",
                               "dt",
                               {"float", "gravity", "-9.8"},
                               "Accel",

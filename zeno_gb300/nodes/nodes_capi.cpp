@@ -80,7 +80,9 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       float dt, float gravity, int32_t substeps, float *out_x, float *out_v,
                       float *out_max_vel_sqr, char *err, int64_t err_cap,
                       const char *ls_shape, const float *ls, const char *ls_type,
-                      const char *transfer) {
+                      const char *transfer, int64_t cloth_nv, const float *cloth_x,
+                      const float *cloth_v, int64_t cloth_nt, const int32_t *cloth_tris,
+                      const float *cloth_params, float *cloth_out_x, float *cloth_out_v) {
   using namespace zeno;
   try {
     Graph g;
@@ -141,6 +143,33 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.markOnce("ls");
       g.markOnce("lsb");
     }
+    // optional cloth: cloth_params = {stiffness_shear, stiffness_normal,
+    // friction_angle, damping_coeff}; the same model as the particles
+    std::shared_ptr<PrimitiveObject> cprim;
+    const bool cloth = cloth_nv > 0 && cloth_x && cloth_nt > 0 && cloth_tris && cloth_params;
+    if (cloth) {
+      cprim = std::make_shared<PrimitiveObject>();
+      auto &cp = cprim->verts();
+      cp.resize(cloth_nv);
+      auto &cv = cprim->attrs3["vel"];
+      cv.resize(cloth_nv);
+      for (int64_t i = 0; i < cloth_nv; ++i)
+        for (int d = 0; d < 3; ++d) {
+          cp[i][d] = cloth_x[3 * i + d];
+          cv[i][d] = cloth_v ? cloth_v[3 * i + d] : 0.0f;
+        }
+      cprim->tris.resize(cloth_nt);
+      for (int64_t i = 0; i < cloth_nt; ++i)
+        for (int d = 0; d < 3; ++d) cprim->tris[i][d] = cloth_tris[3 * i + d];
+      g.addNode("ToZSCloth", "cloth");
+      g.bindNodeInput("cloth", "ZSModel", "model", "ZSModel");
+      g.setNodeInput("cloth", "prim", cprim);
+      g.setNodeInput("cloth", "stiffness_shear", num(cloth_params[0]));
+      g.setNodeInput("cloth", "stiffness_normal", num(cloth_params[1]));
+      g.setNodeInput("cloth", "friction_angle", num(cloth_params[2]));
+      g.setNodeInput("cloth", "damping_coeff", num(cloth_params[3]));
+      g.markOnce("cloth");
+    }
     auto dtobj = num(dt);
     std::string last;
     if (fused) {
@@ -149,6 +178,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("step", "ZSBoundary", "bnd", "ZSBoundary");
       if (collider) g.bindNodeInput("step", "ZSCollider", "lsb", "ZSBoundary");
       g.bindNodeInput("step", "ZSGrid", "grid", "ZSGrid");
+      if (cloth) g.bindNodeInput("step", "ZSCloth", "cloth", "ZSParticles");
       g.setNodeInput("step", "dt", dtobj);
       g.setNodeInput("step", "gravity", num(gravity));
       g.setNodeInput("step", "substeps", inum(substeps));
@@ -159,6 +189,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("part", "ZSPartition", "table", "ZSPartition");
       g.bindNodeInput("part", "ZSGrid", "grid", "ZSGrid");
       g.bindNodeInput("part", "ZSParticles", "pars", "ZSParticles");
+      if (cloth) g.bindNodeInput("part", "ZSCloth", "cloth", "ZSParticles");
       g.addNode("ExpandZSPartition", "expand");
       g.bindNodeInput("expand", "ZSPartition", "part", "ZSPartition");
       g.addNode("ZSGridFromZSPartition", "clear");
@@ -216,6 +247,18 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
         out_x[3 * i + d] = p[i][d];
         out_v[3 * i + d] = pv[i][d];
       }
+    if (cloth) {  // UpdatePrimitiveFromZSParticles on the cloth
+      g.addNode("UpdatePrimitiveFromZSParticles", "cout");
+      g.setNodeInput("cout", "ZSParticles", g.getNodeOutput("cloth", "ZSParticles"));
+      g.applyNodes({"cout"});
+      const auto &cp = cprim->verts();
+      const auto &cv = cprim->attrs3["vel"];
+      for (int64_t i = 0; i < cloth_nv; ++i)
+        for (int d = 0; d < 3; ++d) {
+          if (cloth_out_x) cloth_out_x[3 * i + d] = cp[i][d];
+          if (cloth_out_v) cloth_out_v[3 * i + d] = cv[i][d];
+        }
+    }
     return 0;
   } catch (const std::exception &e) {
     copy_out(e.what(), err, err_cap);

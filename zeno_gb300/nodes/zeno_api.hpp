@@ -28,6 +28,7 @@
 namespace zeno {
 
 using vec3f = std::array<float, 3>;
+using vec3i = std::array<int, 3>;
 
 struct IObject {
   virtual ~IObject() = default;
@@ -63,6 +64,7 @@ struct StringObject : IObject {
 struct PrimitiveObject : IObject {
   std::map<std::string, std::vector<vec3f>> attrs3;
   std::map<std::string, std::vector<float>> attrs1;
+  std::vector<vec3i> tris;  // triangle vertex indices
   std::vector<vec3f> &verts() { return attrs3["pos"]; }
   size_t size() const {
     auto it = attrs3.find("pos");

@@ -77,7 +77,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_apply_walls",
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
            "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
-           "mpm_frame_begin", "mpm_frame_wait", "mpm_g2p", "mpm_return_mapping",
+           "mpm_frame_begin", "mpm_frame_wait", "mpm_cloth_create", "mpm_cloth_download",
+           "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
@@ -129,6 +130,8 @@ def load(path: str = LIB_PATH):
         "mpm_particles_get_attr": ([P, C.c_char_p, P], i32),
         "mpm_particles_set_attr": ([P, C.c_char_p, P], i32),
         "mpm_compute_von_mises": ([P, i32], i32),
+        "mpm_cloth_create": ([P, P], i32),
+        "mpm_cloth_download": ([P] + [P] * 8, i32),
         "mpm_frame_begin": ([P, P, P], i32),
         "mpm_frame_wait": ([P], i32),
         "mpm_apply_collider": ([P, i32], i32),
@@ -164,6 +167,14 @@ def _f32(a, shape):
     if a is None:
         return None
     return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(shape))
+
+
+class ClothDesc(C.Structure):
+    _fields_ = [("n_verts", C.c_int64), ("x", C.c_void_p), ("v", C.c_void_p),
+                ("n_tris", C.c_int64), ("tris", C.c_void_p), ("model", C.c_int32),
+                ("E", C.c_float), ("nu", C.c_float), ("density", C.c_float),
+                ("stiffness_shear", C.c_float), ("stiffness_normal", C.c_float),
+                ("friction_angle", C.c_float), ("damping_coeff", C.c_float)]
 
 
 class Context:
@@ -208,6 +219,30 @@ class Context:
         vals = _f32(values, (self.n,))
         self._check(self._L.mpm_particles_set_attr(self.h, name.encode(), _p(vals)),
                     "mpm_particles_set_attr")
+
+    def add_cloth(self, mesh):
+        """ToZSCloth for a scenes.ClothMesh: the cloth is stepped with the
+        particles by every substep entry point."""
+        x = np.ascontiguousarray(mesh.x, dtype=np.float32)
+        v = None if mesh.v is None else np.ascontiguousarray(mesh.v, dtype=np.float32)
+        tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
+        desc = ClothDesc(x.shape[0], x.ctypes.data, v.ctypes.data if v is not None else None,
+                         tris.shape[0], tris.ctypes.data, int(mesh.model), float(mesh.E),
+                         float(mesh.nu), float(mesh.density), float(mesh.gamma), float(mesh.k),
+                         float(mesh.fa), float(mesh.dc))
+        self._check(self._L.mpm_cloth_create(self.h, C.byref(desc)), "mpm_cloth_create")
+        self._cloth_n = (x.shape[0], tris.shape[0])
+
+    def cloth_download(self) -> dict:
+        nv, ne = self._cloth_n
+        out = {"vx": np.empty((nv, 3), np.float32), "vv": np.empty((nv, 3), np.float32),
+               "vC": np.empty((nv, 9), np.float32), "ex": np.empty((ne, 3), np.float32),
+               "ev": np.empty((ne, 3), np.float32), "eC": np.empty((ne, 9), np.float32),
+               "eF": np.empty((ne, 9), np.float32), "ed": np.empty((ne, 9), np.float32)}
+        self._check(self._L.mpm_cloth_download(self.h, *[_p(out[k]) for k in
+                                                         ("vx", "vv", "vC", "ex", "ev", "eC",
+                                                          "eF", "ed")]), "mpm_cloth_download")
+        return out
 
     def compute_von_mises(self, by_log1p: bool = True):
         """ComputeVonMises; the result is the attribute "vms"."""
@@ -549,7 +584,8 @@ def load_nodes(path: str = NODES_LIB_PATH):
     L.zsn_run_graph.argtypes = [C.c_int32, C.c_int64, P, P, C.c_float, C.c_char_p, C.c_char_p,
                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_char_p,
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
-                                C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p]
+                                C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
+                                C.c_int64, P, P, C.c_int64, P, P, P, P]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -570,14 +606,17 @@ def node_descriptors() -> dict:
 
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
-                   fused=False, levelset=None, transfer="apic"):
+                   fused=False, levelset=None, transfer="apic", cloth=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
     second ApplyBoundaryOnZSGrid every substep, in the fused graph as
     ZSMPMSubstep's ZSCollider: shape ("sphere" | "plane"), dx, center,
     radius, height, extent, translation, translation_rate, scale, scale_rate,
-    ypr, type.  transfer: MakeZSGrid "transfer" (apic, flip, aflip)."""
+    ypr, type.  transfer: MakeZSGrid "transfer" (apic, flip, aflip).
+    cloth: optional scenes.ClothMesh run through ToZSCloth (the particles'
+    model) and written back by UpdatePrimitiveFromZSParticles; the return
+    value then ends with the cloth's vertex positions and velocities."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -597,10 +636,23 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
         lsp = np.asarray(vals, np.float32)
         shape = ls["shape"].encode()
         lst = ls.get("type", "sticky").encode()
+    cl = {}
+    if cloth is not None:
+        cl["x"] = np.ascontiguousarray(cloth.x, dtype=np.float32)
+        cl["v"] = None if cloth.v is None else np.ascontiguousarray(cloth.v, dtype=np.float32)
+        cl["t"] = np.ascontiguousarray(cloth.tris, dtype=np.int32)
+        cl["p"] = np.array([cloth.gamma, cloth.k, cloth.fa, cloth.dc], np.float32)
+        cl["ox"] = np.zeros_like(cl["x"])
+        cl["ov"] = np.zeros_like(cl["x"])
     rc = L.zsn_run_graph(1 if fused else 0, n, _p(x), _p(v), dx, type.encode(),
                          plasticity.encode(), E, nu, density, ppc, bc.encode(), thickness, dt,
                          gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024, shape,
-                         _p(lsp) if lsp is not None else None, lst, transfer.encode())
+                         _p(lsp) if lsp is not None else None, lst, transfer.encode(),
+                         cl["x"].shape[0] if cl else 0, _p(cl.get("x")), _p(cl.get("v")),
+                         cl["t"].shape[0] if cl else 0, _p(cl.get("t")), _p(cl.get("p")),
+                         _p(cl.get("ox")), _p(cl.get("ov")))
     if rc != 0:
         raise RuntimeError(err.value.decode())
+    if cl:
+        return ox, ov, float(vmax[0]), cl["ox"], cl["ov"]
     return ox, ov, float(vmax[0])
