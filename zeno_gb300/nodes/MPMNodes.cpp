@@ -179,6 +179,54 @@ int32_t transfer_of(const ZenoGrid &g) {
   return MPM_TRANSFER_APIC;
 }
 
+// A device context for a particle set / mesh: the directory covers
+// [lo, hi] (the optional domain inputs), else the bounding box of `pos`
+// grown by its own extent (at least 32 cells) on every side.
+std::shared_ptr<MpmContext> make_context(const ZenoConstitutiveModel &model,
+                                         const std::vector<vec3f> &pos, const float *lo_in,
+                                         const float *hi_in, int64_t max_particles) {
+  const float dx = model.dx;
+  float lo[3], hi[3];
+  if (lo_in && hi_in) {
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = lo_in[d];
+      hi[d] = hi_in[d];
+    }
+  } else {
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::numeric_limits<float>::max();
+      hi[d] = -std::numeric_limits<float>::max();
+    }
+    for (const auto &p : pos)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], p[d]);
+        hi[d] = std::max(hi[d], p[d]);
+      }
+    if (pos.empty())
+      for (int d = 0; d < 3; ++d) lo[d] = hi[d] = 0.0f;
+    for (int d = 0; d < 3; ++d) {
+      const float grow = std::max(hi[d] - lo[d], 32.0f * dx);
+      lo[d] -= grow;
+      hi[d] += grow;
+    }
+  }
+  mpm_ctx_desc desc{};
+  desc.device = 0;
+  desc.dx = dx;
+  for (int d = 0; d < 3; ++d) {
+    const int b0 = (int)std::floor(lo[d] / dx / 4.0f) - 1;
+    const int b1 = (int)std::floor(hi[d] / dx / 4.0f) + 2;
+    desc.block_lo[d] = b0;
+    desc.block_dims[d] = std::max(3, b1 - b0 + 1);
+  }
+  desc.max_particles = std::max<int64_t>(max_particles, 1);
+  auto ctx = std::make_shared<MpmContext>();
+  ctx->dx = dx;
+  check(mpm_ctx_create(&desc, &ctx->h), "mpm_ctx_create");
+  check(mpm_set_materials(ctx->h, &model.mat, 1), "mpm_set_materials");
+  return ctx;
+}
+
 // a ToZSCloth cloth joins the particles' context once; its primitive
 // provides the mesh
 void attach_cloth(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &cl) {
@@ -200,6 +248,17 @@ void attach_cloth(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &cl) {
   check(mpm_cloth_create(ctx->h, &d), "mpm_cloth_create");
   cl.cloth_ctx = ctx;
   cl.ctx = ctx;
+}
+
+// a ToZSCloth cloth used on its own as the ZSParticles of a substep gets a
+// context of its own (no particles)
+void ensure_cloth_ctx(ZenoParticles &pars) {
+  if (!pars.cloth || pars.ctx) return;
+  auto ctx = make_context(*pars.model, prim_access::pos(*pars.prim), nullptr, nullptr, 1);
+  check(mpm_particles_upload(ctx->h, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                             nullptr, nullptr, nullptr, nullptr),
+        "mpm_particles_upload");
+  attach_cloth(ctx, pars);
 }
 
 std::shared_ptr<MpmContext> bound_ctx(const std::shared_ptr<ZenoPartition> &p, const char *node) {
@@ -328,51 +387,48 @@ struct ToZSParticles : INode {
     out->model = model;
     out->n = n;
     out->category = get_input2<int>("category");
-    if (out->category != 0)
-      throw std::runtime_error("only mpm particles (category 0) are supported by this backend");
-
-    const float dx = model->dx;
     float lo[3], hi[3];
-    if (has_input<NumericObject>("domain_min") && has_input<NumericObject>("domain_max")) {
+    const bool domain = has_input<NumericObject>("domain_min") && has_input<NumericObject>("domain_max");
+    if (domain) {
       auto a = get_input<NumericObject>("domain_min")->get<vec3f>();
       auto b = get_input<NumericObject>("domain_max")->get<vec3f>();
       for (int d = 0; d < 3; ++d) {
         lo[d] = a[d];
         hi[d] = b[d];
       }
-    } else {
-      for (int d = 0; d < 3; ++d) {
-        lo[d] = std::numeric_limits<float>::max();
-        hi[d] = -std::numeric_limits<float>::max();
-      }
-      for (const auto &p : pos)
-        for (int d = 0; d < 3; ++d) {
-          lo[d] = std::min(lo[d], p[d]);
-          hi[d] = std::max(hi[d], p[d]);
-        }
-      if (n == 0)
-        for (int d = 0; d < 3; ++d) lo[d] = hi[d] = 0.0f;
-      for (int d = 0; d < 3; ++d) {
-        const float grow = std::max(hi[d] - lo[d], 32.0f * dx);
-        lo[d] -= grow;
-        hi[d] += grow;
-      }
     }
-    mpm_ctx_desc desc{};
-    desc.device = 0;
-    desc.dx = dx;
-    for (int d = 0; d < 3; ++d) {
-      const int b0 = (int)std::floor(lo[d] / dx / 4.0f) - 1;
-      const int b1 = (int)std::floor(hi[d] / dx / 4.0f) + 2;
-      desc.block_lo[d] = b0;
-      desc.block_dims[d] = std::max(3, b1 - b0 + 1);
+    if (out->category != 0) {
+      // a mesh (Generation.cpp:738-749): triangles become a surface (cloth)
+      // with the defaults of Generation.cpp:695-699 (k = 800, gamma = fa =
+      // dc = 0); curves and tetrahedra are not implemented
+      if (prim_access::tris(*prim).empty())
+        throw std::runtime_error("ToZSParticles: category " + std::to_string(out->category) +
+                                 " needs a triangle mesh (curves and tetrahedra are not "
+                                 "implemented by this backend)");
+      const int type = model->mat.type;
+      if (type != MPM_FCR && type != MPM_NHK && type != MPM_STVK)
+        throw std::runtime_error("ToZSParticles: a surface takes fcr, nhk or stvk");
+      out->n = 0;
+      out->cloth = true;
+      out->category = 2;  // ZenoParticles::surface
+      mpm_cloth_desc &cd = out->cloth_desc;
+      cd.model = type;
+      cd.E = model->mat.E;
+      cd.nu = model->mat.nu;
+      cd.density = model->density;
+      cd.stiffness_shear = 0.0f;
+      cd.stiffness_normal = 800.0f;
+      cd.friction_angle = 0.0f;
+      cd.damping_coeff = 0.0f;
+      auto ctx = make_context(*model, pos, domain ? lo : nullptr, domain ? hi : nullptr, 1);
+      check(mpm_particles_upload(ctx->h, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr, nullptr, nullptr),
+            "mpm_particles_upload");
+      attach_cloth(ctx, *out);
+      set_output("ZSParticles", out);
+      return;
     }
-    desc.max_particles = std::max<int64_t>(n, 1);
-    auto ctx = std::make_shared<MpmContext>();
-    ctx->dx = dx;
-    check(mpm_ctx_create(&desc, &ctx->h), "mpm_ctx_create");
-    check(mpm_set_materials(ctx->h, &model->mat, 1), "mpm_set_materials");
-
+    auto ctx = make_context(*model, pos, domain ? lo : nullptr, domain ? hi : nullptr, n);
     std::vector<float> x(3 * n), v(3 * n, 0.0f), m(n, model->volume * model->density),
         vol(n, model->volume);
     for (int64_t i = 0; i < n; ++i)
@@ -435,6 +491,7 @@ struct ZSPartitionForZSParticles : INode {
     auto table = get_input<ZenoPartition>("ZSPartition");
     auto grid = get_input<ZenoGrid>("ZSGrid");
     auto pars = get_input<ZenoParticles>("ZSParticles");
+    ensure_cloth_ctx(*pars);
     const std::string strategy = get_param<std::string>("strategy");
     if (strategy != "force" && strategy != "cache")
       throw std::runtime_error("unknown partition strategy [" + strategy + "]");
@@ -962,6 +1019,7 @@ ZENDEFNODE(ZSParticlesToPrimitiveObject, {
 struct ZSMPMSubstep : INode {
   void apply() override {
     auto pars = get_input<ZenoParticles>("ZSParticles");
+    ensure_cloth_ctx(*pars);
     auto ctx = pars->ctx;
     float acc[3] = {0.0f, get_input2<float>("gravity"), 0.0f};
     if (has_input("Accel")) {
