@@ -200,7 +200,15 @@ typedef struct mpm_cloth_desc {
   int32_t model;
   float E, nu, density;
   float stiffness_shear, stiffness_normal, friction_angle, damping_coeff;
+  /* MPM_MESH_SURFACE: tris holds n_tris triangles (3 indices each);
+   * MPM_MESH_CURVE: n_tris segments (2 indices each), ToZSParticles' curve
+   * category (Generation.cpp:837-858): element volume = length dx^2, frame
+   * d = [p1 - p0, n1, n2], StVK-Hencky cross-section, p2g_curve
+   * (Transfer.cu:174-356), curve G2P (:1445-1513), return_mapping_curve
+   * (MPMPipeline.cu:1012-1093) */
+  int32_t kind;
 } mpm_cloth_desc;
+enum { MPM_MESH_SURFACE = 0, MPM_MESH_CURVE = 1 };
 int32_t mpm_cloth_create(mpm_ctx *ctx, const mpm_cloth_desc *desc);
 /* the cloth's state (NULL skips an array): vertices x, v (n_verts x 3), C
  * (n_verts x 9); elements x, v (n_tris x 3), C, F, d (n_tris x 9, row-major) */

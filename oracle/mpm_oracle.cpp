@@ -656,6 +656,66 @@ template <class R> struct Sim {
     g[2] = st.w[0][i] * st.w[1][j] * st.dw[2][k] * inv_dx;
   }
 
+  // p2g_curve (Transfer.cu:174-356) for one segment: the cross-section
+  // block of R through the StVK-Hencky model, P00 = k (r00 - 1), P = Q P,
+  // shear A (gamma) times the diagonal of R's cofactors over det R as the
+  // reference computes it, the force P_c23 (d_c23^T grad W)(-vol dt) on the
+  // element's nodes (type i), +-vol dt P_c0 DmInv00 on its two vertices
+  // (type ii)
+  void curve_p2g(orc_cloth &cl, int64_t e, const double *Q, const double *Rm, double dt,
+                 std::vector<double> &imp) {
+    const int tr = sc.transfer;
+    const bool flip_style = tr != ORC_TRANSFER_APIC, affine = tr != ORC_TRANSFER_FLIP;
+    const double dx = sc.dx;
+    const double *dm = cl.ed + 9 * e, *Di = cl.eDmInv + 9 * e;
+    const double R2[4] = {Rm[4], Rm[5], 0.0, Rm[8]};
+    double P2[4];
+    first_piola_2d(ORC_STVK, cl.emu[e], cl.elam[e], R2, P2);
+    double Pl[9] = {double(cl.k) * (Rm[0] - 1), 0, 0, 0, P2[0], P2[1], 0, P2[2], P2[3]}, P[9];
+    mul_AB(Q, Pl, P);
+    const double g = cl.gamma;
+    const double rr = Rm[1] * Rm[1] + Rm[2] * Rm[2];
+    double A[9] = {rr * g, (Rm[4] * Rm[1] + Rm[5] * Rm[2]) * g, Rm[8] * Rm[2] * g, 0, 0, 0, 0, 0, 0};
+    A[3] = A[1];
+    A[6] = A[2];
+    double invJ = Rm[0] * Rm[4] * Rm[8];
+    if (invJ != 0) invJ = 1 / invJ;
+    const double Rit[9] = {Rm[4] * Rm[8] * invJ, 0, 0, 0, Rm[0] * Rm[8] * invJ, 0, 0, 0, Rm[0] * Rm[4] * invJ};
+    double QA[9], T[9];
+    mul_AB(Q, A, QA);
+    mul_AB(QA, Rit, T);
+    for (int i = 0; i < 9; ++i) P[i] += T[i];
+    const double mass = cl.em[e], vol = cl.evol[e];
+    const double *ve = cl.ev + 3 * e, *Ce = cl.eC + 9 * e;
+    Stencil st;
+    stencil(cl.ex + 3 * e, st);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+          const double xixp[3] = {(i - st.fx[0]) * dx, (j - st.fx[1]) * dx, (k - st.fx[2]) * dx};
+          const double W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+          double gw[3];
+          weight_grad(st, i, j, k, gw);
+          const double s1 = (dm[1] * gw[0] + dm[4] * gw[1] + dm[7] * gw[2]) * (-vol * dt);
+          const double s2 = (dm[2] * gw[0] + dm[5] * gw[1] + dm[8] * gw[2]) * (-vol * dt);
+          R *nd = node(I);
+          nd[0] += W * mass;
+          for (int a = 0; a < 3; ++a) {
+            const double vft = P[a * 3 + 1] * s1 + P[a * 3 + 2] * s2;
+            const double Cx = affine ? Ce[a * 3 + 0] * xixp[0] + Ce[a * 3 + 1] * xixp[1] + Ce[a * 3 + 2] * xixp[2] : 0.0;
+            nd[1 + a] += W * mass * (ve[a] + Cx) + (flip_style ? 0.0 : vft);
+            if (flip_style) nd[4 + a] += vft;
+          }
+        }
+    const int32_t *t = cl.inds + 3 * e;
+    for (int a = 0; a < 3; ++a) {
+      const double f = vol * dt * P[a * 3 + 0] * Di[0];
+      imp[3 * t[0] + a] += f;
+      imp[3 * t[1] + a] -= f;
+    }
+  }
+
   // ZSParticleToZSGrid for the cloth (p2g_surface, Transfer.cu:656-842):
   // each element scatters its mass and momentum and the normal-direction
   // force P_c3 (grad W . d_c3) (-vol dt) (type i), and hands the in-plane
@@ -666,10 +726,15 @@ template <class R> struct Sim {
     const bool flip_style = tr != ORC_TRANSFER_APIC, affine = tr != ORC_TRANSFER_FLIP;
     const double dx = sc.dx;
     std::vector<double> imp(3 * cl.n_verts, 0.0);
+    const bool curve = cl.kind == ORC_MESH_CURVE;
     for (int64_t e = 0; e < cl.n_eles; ++e) {
       const double *F = cl.eF + 9 * e, *dm = cl.ed + 9 * e, *Di = cl.eDmInv + 9 * e;
       double Q[9], Rm[9];
       gram_schmidt(F, Q, Rm);
+      if (curve) {
+        curve_p2g(cl, e, Q, Rm, dt, imp);
+        continue;
+      }
       const double R2[4] = {Rm[0], Rm[1], Rm[3], Rm[4]};
       double P2[4];
       first_piola_2d(cl.model, cl.emu[e], cl.elam[e], R2, P2);
@@ -819,6 +884,25 @@ template <class R> struct Sim {
       cloth_gather(cl.ex + 3 * e, flip_style, dc, vel, vs, Cn);
       for (int i = 0; i < 9; ++i) cl.eC[9 * e + i] = Cn[i];
       const int32_t *t = cl.inds + 3 * e;
+      if (cl.kind == ORC_MESH_CURVE) {  // Transfer.cu:1445-1513
+        const double *p0 = cl.vx + 3 * t[0], *p1 = cl.vx + 3 * t[1];
+        double *d = cl.ed + 9 * e;
+        double CC[9], M[9];
+        mul_AB(Cn, Cn, CC);
+        for (int i = 0; i < 9; ++i) M[i] = dt * Cn[i] + 0.5 * dt * dt * CC[i];
+        double dn[9];
+        for (int a = 0; a < 3; ++a) {
+          cl.ex[3 * e + a] = (p0[a] + p1[a]) / 2;
+          cl.ev[3 * e + a] = (cl.vv[3 * t[0] + a] + cl.vv[3 * t[1] + a]) / 2;
+          dn[a * 3 + 0] = p1[a] - p0[a];
+          for (int c = 1; c < 3; ++c)
+            dn[a * 3 + c] = d[a * 3 + c] + M[a * 3 + 0] * d[0 * 3 + c] + M[a * 3 + 1] * d[1 * 3 + c] +
+                            M[a * 3 + 2] * d[2 * 3 + c];
+        }
+        for (int i = 0; i < 9; ++i) d[i] = dn[i];
+        mul_AB(d, cl.eDmInv + 9 * e, cl.eF + 9 * e);
+        continue;
+      }
       const double *p0 = cl.vx + 3 * t[0], *p1 = cl.vx + 3 * t[1], *p2 = cl.vx + 3 * t[2];
       double *d = cl.ed + 9 * e;
       double d3[3] = {d[2], d[5], d[8]}, CC[9], M[9], n3[3];
@@ -836,6 +920,44 @@ template <class R> struct Sim {
     }
   }
 
+  // return_mapping_curve (MPMPipeline.cu:1012-1093) with its hard-coded
+  // alpha = alpha_tangent = cohesion = 0: the cross-section's Hencky strain
+  // e = ln |s| of R's lower-right block (|s| >= 128 eps) is projected to its
+  // mean part when compressive (sum e < 0; to zero if already isotropic within
+  // eps) and to zero otherwise, so that block becomes exp(e_mean) times its
+  // closest rotation; the frictional shear (r01, r02) is then always removed
+  // (zero cohesion cone).
+  void curve_return_mapping(orc_cloth &cl, int64_t e, const double *Q, double *Rm) {
+    const double feps = 1.1920928955078125e-07;
+    const double a = Rm[4], b = Rm[5], c = Rm[7], dd = Rm[8];
+    // singular values of [a b; c d]
+    const double E = 0.5 * (a + dd), Fv = 0.5 * (a - dd), G = 0.5 * (c + b), H = 0.5 * (c - b);
+    const double q = std::sqrt(E * E + H * H), r = std::sqrt(Fv * Fv + G * G);
+    const double s0 = q + r, s1 = q - r;
+    double eps[2] = {std::log(std::max(std::fabs(s0), feps * 128)), std::log(std::max(std::fabs(s1), feps * 128))};
+    const double tr = eps[0] + eps[1];
+    if (tr < 0) {
+      const double h0 = eps[0] - 0.5 * tr, h1 = eps[1] - 0.5 * tr;
+      const double hn = std::sqrt(h0 * h0 + h1 * h1);
+      if (hn < feps)
+        eps[0] = eps[1] = 0;
+      else
+        eps[0] = eps[1] = 0.5 * tr;
+    } else {
+      eps[0] = eps[1] = 0;
+    }
+    const double scale = std::exp(eps[0]);  // both equal
+    const double p = a + dd, qq = c - b, nn = std::sqrt(p * p + qq * qq);
+    Rm[4] = scale * p / nn;
+    Rm[5] = -scale * qq / nn;
+    Rm[7] = scale * qq / nn;
+    Rm[8] = scale * p / nn;
+    // shear: gamma == 0, or gamma |R2 r| > 0 with zero cohesion, clears it
+    Rm[1] = Rm[2] = 0;
+    mul_AB(Q, Rm, cl.ed + 9 * e);
+    mul_AB(cl.ed + 9 * e, cl.eDmInv + 9 * e, cl.eF + 9 * e);
+  }
+
   // ZSReturnMapping for the cloth (return_mapping_surface,
   // MPMPipeline.cu:973-1011) on R of d = Q R: no shear resistance beyond
   // friction, no tension across the normal; fc = tan(fa / pi) as the node
@@ -846,6 +968,10 @@ template <class R> struct Sim {
       double *d = cl.ed + 9 * e;
       double Q[9], Rm[9];
       gram_schmidt(d, Q, Rm);
+      if (cl.kind == ORC_MESH_CURVE) {
+        curve_return_mapping(cl, e, Q, Rm);
+        continue;
+      }
       bool apply = false;
       if (gamma == 0) {
         Rm[2] = Rm[5] = 0;
@@ -1367,6 +1493,80 @@ int32_t orc_cloth_init_f64(int64_t n_verts, const float *x, const float *v, int6
   }
   out->n_verts = n_verts;
   out->n_eles = n_tris;
+  return ORC_OK;
+}
+
+int32_t orc_curve_init_f64(int64_t n_verts, const float *x, const float *v, int64_t n_segs,
+                           const int32_t *segs, float dx, float density, float E, float nu,
+                           orc_cloth *out) {
+  if (!out || n_verts < 0 || n_segs < 0) return ORC_ERR_INVALID;
+  const float mu = E / (2.0f * (1.0f + nu)), lam = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+  std::vector<float> dof_vol(n_verts, 0.0f);
+  const double feps = std::numeric_limits<float>::epsilon();
+  for (int64_t e = 0; e < n_segs; ++e) {
+    const int32_t *t = segs + 2 * e;
+    for (int i = 0; i < 2; ++i)
+      if (t[i] < 0 || t[i] >= n_verts) return ORC_ERR_INVALID;
+    double len2 = 0;
+    float d1[3];
+    for (int a = 0; a < 3; ++a) {
+      const double dd = double(x[3 * t[1] + a]) - double(x[3 * t[0] + a]);
+      len2 += dd * dd;
+      d1[a] = x[3 * t[1] + a] - x[3 * t[0] + a];
+    }
+    const float vol = float(std::max(std::sqrt(len2) * double(dx) * double(dx), feps * 10.0));
+    out->evol[e] = vol;
+    out->em[e] = double(vol * density);
+    for (int a = 0; a < 3; ++a) {
+      out->ex[3 * e + a] = (x[3 * t[0] + a] + x[3 * t[1] + a]) / 2.0f;
+      out->ev[3 * e + a] = v ? double((v[3 * t[0] + a] + v[3 * t[1] + a]) / 2.0f) : 0.0;
+    }
+    const double ln[3] = {d1[0], d1[1], d1[2]};
+    // a vector orthogonal to ln (Hughes & Moller 1999)
+    double o[3];
+    if (std::fabs(ln[0]) > std::fabs(ln[2])) {
+      o[0] = -ln[1];
+      o[1] = ln[0];
+      o[2] = 0;
+    } else {
+      o[0] = 0;
+      o[1] = -ln[2];
+      o[2] = ln[1];
+    }
+    const double on = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+    double n1[3] = {o[0] / on, o[1] / on, o[2] / on};
+    double n2[3] = {ln[1] * n1[2] - ln[2] * n1[1], ln[2] * n1[0] - ln[0] * n1[2], ln[0] * n1[1] - ln[1] * n1[0]};
+    const double n2n = std::sqrt(n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2]);
+    double *d = out->ed + 9 * e;
+    for (int a = 0; a < 3; ++a) {
+      d[a * 3 + 0] = d1[a];
+      d[a * 3 + 1] = float(n1[a]);
+      d[a * 3 + 2] = float(n2[a] / n2n);
+    }
+    const double tl = std::sqrt(d[0] * d[0] + d[3] * d[3] + d[6] * d[6]);
+    const double Di[9] = {1 / tl, 0, 0, 0, 1, 0, 0, 0, 1};
+    out->emu[e] = tl <= feps ? 0.0 : mu;
+    out->elam[e] = tl <= feps ? 0.0 : lam;
+    for (int i = 0; i < 9; ++i) out->eDmInv[9 * e + i] = float(Di[i]);
+    double Fd[9];
+    mul_AB(d, Di, Fd);
+    for (int i = 0; i < 9; ++i) out->eF[9 * e + i] = float(Fd[i]);
+    for (int i = 0; i < 9; ++i) out->eC[9 * e + i] = 0;
+    out->inds[3 * e + 0] = t[0];
+    out->inds[3 * e + 1] = t[1];
+    out->inds[3 * e + 2] = t[1];
+    for (int i = 0; i < 2; ++i) dof_vol[t[i]] += vol / 2.0f;
+  }
+  for (int64_t p = 0; p < n_verts; ++p) {
+    out->vm[p] = double(dof_vol[p] * density);
+    for (int a = 0; a < 3; ++a) {
+      out->vx[3 * p + a] = x[3 * p + a];
+      out->vv[3 * p + a] = v ? v[3 * p + a] : 0.0f;
+    }
+    for (int i = 0; i < 9; ++i) out->vC[9 * p + i] = 0;
+  }
+  out->n_verts = n_verts;
+  out->n_eles = n_segs;
   return ORC_OK;
 }
 

@@ -84,8 +84,11 @@ typedef struct orc_collider {
  * DmInv, F = d DmInv; stepped by the surface branches of the transfer nodes
  * (Transfer.cu:656-842 P2G, 1287-1445 G2P) and ZSReturnMapping
  * (MPMPipeline.cu:973-1011).  Arrays are in/out, row-major 3x3. */
+enum { ORC_MESH_SURFACE = 0, ORC_MESH_CURVE = 1 };
 typedef struct orc_cloth {
-  int32_t model;          /* ORC_FCR / ORC_NHK / ORC_STVK: the in-plane model */
+  int32_t kind;           /* ORC_MESH_SURFACE (triangles) or ORC_MESH_CURVE (segments) */
+  int32_t model;          /* ORC_FCR / ORC_NHK / ORC_STVK: the in-plane model
+                             (curves: StVK-Hencky with the model's mu, lam) */
   float gamma, k, fa, dc; /* ToZSCloth stiffness_shear, stiffness_normal,
                              friction_angle, damping_coeff */
   int64_t n_verts, n_eles;
@@ -93,7 +96,7 @@ typedef struct orc_cloth {
   double *vm;             /* vertex mass */
   double *ex, *ev, *eC, *eF, *ed, *eDmInv; /* elements */
   double *em, *evol, *emu, *elam;
-  int32_t *inds;          /* 3 vertex indices per element */
+  int32_t *inds;          /* 3 vertex indices per element (curves: the first 2) */
 } orc_cloth;
 
 typedef struct orc_scene {
@@ -184,6 +187,13 @@ int32_t orc_project_dp(const orc_material *mat, double *F);
  * model's dx (thickness), density and E, nu. */
 int32_t orc_cloth_init_f64(int64_t n_verts, const float *x, const float *v, int64_t n_tris,
                            const int32_t *tris, float dx, float density, float E, float nu,
+                           orc_cloth *out);
+/* ToZSParticles' set-up of a curve mesh (Generation.cpp:837-858, 1096-1112):
+ * segments (n_segs x 2); element volume = length dx^2, d = [p1 - p0, n1, n2]
+ * with n1 a unit vector orthogonal to the segment (Hughes-Moller choice) and
+ * n2 = normalize(d1 x n1); D* = diag(|d1|, 1, 1). */
+int32_t orc_curve_init_f64(int64_t n_verts, const float *x, const float *v, int64_t n_segs,
+                           const int32_t *segs, float dx, float density, float E, float nu,
                            orc_cloth *out);
 
 int32_t orc_max_threads(void);

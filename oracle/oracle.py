@@ -34,7 +34,8 @@ class OrcCollider(C.Structure):
 
 
 class OrcCloth(C.Structure):
-    _fields_ = [("model", C.c_int32), ("gamma", C.c_float), ("k", C.c_float), ("fa", C.c_float),
+    _fields_ = [("kind", C.c_int32), ("model", C.c_int32), ("gamma", C.c_float), ("k", C.c_float),
+                ("fa", C.c_float),
                 ("dc", C.c_float), ("n_verts", C.c_int64), ("n_eles", C.c_int64)] + \
                [(k, C.c_void_p) for k in ("vx", "vv", "vC", "vm", "ex", "ev", "eC", "eF", "ed",
                                           "eDmInv", "em", "evol", "emu", "elam", "inds")]
@@ -95,6 +96,8 @@ def lib():
         L.orc_cloth_init_f64.argtypes = [C.c_int64, P, P, C.c_int64, P, C.c_float, C.c_float,
                                          C.c_float, C.c_float, C.POINTER(OrcCloth)]
         L.orc_cloth_init_f64.restype = C.c_int32
+        L.orc_curve_init_f64.argtypes = L.orc_cloth_init_f64.argtypes
+        L.orc_curve_init_f64.restype = C.c_int32
         L.orc_sym_eig3.argtypes = [P, P, P]
         L.orc_kirchhoff.argtypes = [C.POINTER(OrcMaterial), P, C.c_double, P]
         L.orc_kirchhoff.restype = C.c_int32
@@ -227,16 +230,23 @@ def von_mises(scene, parts, by_log1p: bool = True, vms: np.ndarray | None = None
     return out
 
 
+def _is_curve(mesh) -> bool:
+    return np.asarray(mesh.tris).shape[1] == 2
+
+
 def _cloth_struct(mesh, state) -> OrcCloth:
-    st = OrcCloth(int(mesh.model), float(mesh.gamma), float(mesh.k), float(mesh.fa),
-                  float(mesh.dc), int(state["vx"].shape[0]), int(state["ex"].shape[0]))
+    curve = _is_curve(mesh)
+    st = OrcCloth(1 if curve else 0, 2 if curve else int(mesh.model), float(mesh.gamma),
+                  float(mesh.k), float(mesh.fa), float(mesh.dc), int(state["vx"].shape[0]),
+                  int(state["ex"].shape[0]))
     for k in list(CLOTH_VERT) + list(CLOTH_ELE) + ["inds"]:
         setattr(st, k, state[k].ctypes.data)
     return st
 
 
 def cloth_init(mesh, dx: float) -> dict:
-    """ToZSCloth in FP64: the vertex and element arrays of a scenes.ClothMesh."""
+    """ToZSCloth (triangles) or ToZSParticles' curve set-up (segments) in FP64:
+    the vertex and element arrays of a scenes.ClothMesh."""
     x = np.ascontiguousarray(mesh.x, dtype=np.float32)
     v = None if mesh.v is None else np.ascontiguousarray(mesh.v, dtype=np.float32)
     tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
@@ -245,8 +255,9 @@ def cloth_init(mesh, dx: float) -> dict:
     state.update({k: np.zeros((ne, c) if c > 1 else ne) for k, c in CLOTH_ELE.items()})
     state["inds"] = np.zeros((ne, 3), np.int32)
     st = _cloth_struct(mesh, state)
-    rc = lib().orc_cloth_init_f64(nv, _ptr(x), _ptr(v), ne, _ptr(tris), float(dx),
-                                  float(mesh.density), float(mesh.E), float(mesh.nu), C.byref(st))
+    fn = lib().orc_curve_init_f64 if _is_curve(mesh) else lib().orc_cloth_init_f64
+    rc = fn(nv, _ptr(x), _ptr(v), ne, _ptr(tris), float(dx), float(mesh.density), float(mesh.E),
+            float(mesh.nu), C.byref(st))
     if rc != 0:
         raise RuntimeError(f"oracle cloth init failed with status {rc}")
     return state

@@ -249,3 +249,135 @@ def test_cloth_substep_matches_numpy(oracle_mod, model, gamma):
         # absolute tolerance for their cancellation
         np.testing.assert_allclose(out[k], ref[k], rtol=1e-9, atol=1e-8 if k in ("vC", "eC") else 1e-11,
                                    err_msg=k)
+
+
+# ---- curves (hair): ToZSParticles' segment set-up, p2g_curve, curve G2P and
+# return mapping ----
+
+def test_curve_init(oracle_mod):
+    mesh = S.curve_strands((0.45, 0.6, 0.5), 0.1, 3, 5, 0.02, E=2e4, nu=0.3, density=900.0)
+    # bend the strands a little so segments are not axis-aligned
+    mesh.x[:, 0] += 0.01 * np.sin(40 * mesh.x[:, 1]).astype(np.float32)
+    dx = 1.0 / 64
+    st = oracle_mod.cloth_init(mesh, dx)
+    vv = np.zeros(len(mesh.x), np.float32)
+    for e, (a, b) in enumerate(mesh.tris):
+        L = np.linalg.norm(mesh.x[b].astype(np.float64) - mesh.x[a])
+        vol = np.float32(max(L * dx * dx, 10 * np.finfo(np.float32).eps))
+        assert st["evol"][e] == vol
+        d = st["ed"][e].reshape(3, 3)
+        np.testing.assert_allclose(d[:, 0], mesh.x[b] - mesh.x[a], atol=0)
+        # n1, n2 unit, orthogonal to the segment and each other
+        np.testing.assert_allclose(np.linalg.norm(d[:, 1:], axis=0), 1.0, atol=1e-6)
+        np.testing.assert_allclose(d[:, 0] @ d[:, 1:], 0.0, atol=1e-6)
+        assert abs(d[:, 1] @ d[:, 2]) < 1e-6
+        np.testing.assert_allclose(st["eDmInv"][e].reshape(3, 3), np.diag([1 / L, 1, 1]), rtol=1e-6)
+        vv[[a, b]] += vol / np.float32(2)
+    np.testing.assert_allclose(st["vm"], vv * np.float32(900.0), rtol=1e-6)
+
+
+def _numpy_curve_substep(mesh, st, dx, dt, g):
+    s = {k: np.array(a, dtype=np.float64 if k != "inds" else np.int32) for k, a in st.items()}
+    grid = {}
+
+    def add(I, m, mv):
+        e = grid.setdefault(I, np.zeros(4))
+        e[0] += m
+        e[1:] += mv
+    imp = np.zeros_like(s["vx"])
+    for e in range(len(s["ex"])):
+        F = s["eF"][e].reshape(3, 3)
+        d = s["ed"][e].reshape(3, 3)
+        Q, R = _gs(F)
+        P2 = _piola2(S.STVK, s["emu"][e], s["elam"][e], R[1:, 1:])
+        P = np.zeros((3, 3))
+        P[0, 0] = mesh.k * (R[0, 0] - 1)
+        P[1:, 1:] = P2
+        P = Q @ P
+        ga = mesh.gamma
+        A = np.zeros((3, 3))
+        A[0, 0] = (R[0, 1] ** 2 + R[0, 2] ** 2) * ga
+        A[0, 1] = A[1, 0] = (R[1, 1] * R[0, 1] + R[1, 2] * R[0, 2]) * ga
+        A[0, 2] = A[2, 0] = R[2, 2] * R[0, 2] * ga
+        Rit = np.diag([R[1, 1] * R[2, 2], R[0, 0] * R[2, 2], R[0, 0] * R[1, 1]]) / np.prod(np.diag(R))
+        P = P + Q @ A @ Rit
+        vol, m = s["evol"][e], s["em"][e]
+        for I, W, xixp, gW in _spline(s["ex"][e], dx):
+            vft = P[:, 1:] @ (d[:, 1:].T @ gW) * (-vol * dt)
+            add(I, W * m, W * m * (s["ev"][e] + s["eC"][e].reshape(3, 3) @ xixp) + vft)
+        a, b = s["inds"][e][:2]
+        f = vol * dt * P[:, 0] * s["eDmInv"][e][0]
+        imp[a] += f
+        imp[b] -= f
+    for p in range(len(s["vx"])):
+        for I, W, xixp, _ in _spline(s["vx"][p], dx):
+            add(I, W * s["vm"][p], W * (s["vm"][p] * (s["vv"][p] + s["vC"][p].reshape(3, 3) @ xixp) + imp[p]))
+    gv = {I: e[1:] / e[0] + np.asarray(g) * dt for I, e in grid.items()}
+    Dinv = 4 / dx ** 2
+
+    def gather(xp):
+        vel, C = np.zeros(3), np.zeros((3, 3))
+        for I, W, xixp, _ in _spline(xp, dx):
+            vel += W * gv[I]
+            C += W * Dinv * np.outer(gv[I], xixp)
+        return vel, 0.5 * (C - C.T) + (1 - mesh.dc) * 0.5 * (C + C.T)
+    for p in range(len(s["vx"])):
+        vel, C = gather(s["vx"][p])
+        s["vv"][p], s["vC"][p] = vel, C.ravel()
+        s["vx"][p] = s["vx"][p] + vel * dt
+    feps = np.finfo(np.float32).eps
+    for e in range(len(s["ex"])):
+        _, C = gather(s["ex"][e])
+        s["eC"][e] = C.ravel()
+        a, b = s["inds"][e][:2]
+        s["ex"][e] = (s["vx"][a] + s["vx"][b]) / 2
+        s["ev"][e] = (s["vv"][a] + s["vv"][b]) / 2
+        d = s["ed"][e].reshape(3, 3).copy()
+        d23 = d[:, 1:] + (dt * C + 0.5 * dt * dt * C @ C) @ d[:, 1:]
+        d = np.concatenate([(s["vx"][b] - s["vx"][a])[:, None], d23], axis=1)
+        # return mapping
+        Q, R = _gs(d)
+        U, sv, Vt = np.linalg.svd(R[1:, 1:])
+        eps = np.log(np.maximum(np.abs(sv), 128 * feps))
+        tr = eps.sum()
+        if tr < 0:
+            h = eps - 0.5 * tr
+            eps = np.zeros(2) if np.linalg.norm(h) < feps else eps - h
+        else:
+            eps = np.zeros(2)
+        Rot = U @ Vt
+        if np.linalg.det(Rot) < 0:
+            U[:, -1] *= -1
+            Rot = U @ Vt
+        R[1:, 1:] = Rot * np.exp(eps[0])
+        R[0, 1] = R[0, 2] = 0.0
+        d = Q @ R
+        s["ed"][e] = d.ravel()
+        s["eF"][e] = (d @ s["eDmInv"][e].reshape(3, 3)).ravel()
+    return s
+
+
+@pytest.mark.parametrize("gamma", [0.0, 100.0])
+def test_curve_substep_matches_numpy(oracle_mod, gamma):
+    scene = S.Scene.unit_box(1.0 / 32, bc_type=S.BC_NONE, materials=[S.Material()])
+    mesh = S.curve_strands((0.45, 0.6, 0.5), 0.12, 2, 4, 0.03, E=4e4, nu=0.3, density=900.0,
+                           gamma=gamma, k=900.0, dc=0.05)
+    mesh.x[:, 2] += 0.01 * np.cos(30 * mesh.x[:, 1]).astype(np.float32)
+    st = oracle_mod.cloth_init(mesh, scene.dx)
+    rng = S.uniform(11, 0, 18 * len(st["ex"])).reshape(-1, 2, 9)
+    for e in range(len(st["ex"])):
+        Q, _ = _gs(st["eF"][e].reshape(3, 3))
+        Rt = np.triu(np.array([[1.03, 0.02, -0.01], [0, 0.97, 0.03], [0, 0, 1.02]]) +
+                     0.02 * (rng[e, 0].reshape(3, 3) - 0.5))
+        F = Q @ Rt
+        st["eF"][e] = F.ravel()
+        st["ed"][e] = (F @ np.linalg.inv(st["eDmInv"][e].reshape(3, 3))).ravel()
+        st["eC"][e] = 0.3 * (rng[e, 1] - 0.5)
+    st["vv"][:] = 0.2 * (S.uniform(3, 0, st["vv"].size).reshape(-1, 3) - 0.5)
+    st["ev"][:] = 0.2 * (S.uniform(4, 0, st["ev"].size).reshape(-1, 3) - 0.5)
+    _, out, stats = oracle_mod.run_cloth(scene, _empty(), mesh, st, 1)
+    assert stats["status"] == 0
+    ref = _numpy_curve_substep(mesh, st, scene.dx, scene.dt, np.array(scene.gravity, np.float32))
+    for k in ("vx", "vv", "vC", "ex", "ev", "eC", "ed", "eF"):
+        np.testing.assert_allclose(out[k], ref[k], rtol=1e-9,
+                                   atol=1e-8 if k in ("vC", "eC") else 1e-11, err_msg=k)

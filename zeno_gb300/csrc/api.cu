@@ -799,13 +799,17 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
   if (c->d.keep_order) return fail(MPM_ERR_INVALID, "the differentiable form takes no cloth");
   if (desc->model != MPM_FCR && desc->model != MPM_NHK && desc->model != MPM_STVK)
     return fail(MPM_ERR_INVALID, "cloth model must be fixed-corotated, Neo-Hookean or StVK-Hencky");
+  if (desc->kind != MPM_MESH_SURFACE && desc->kind != MPM_MESH_CURVE)
+    return fail(MPM_ERR_INVALID, "mesh kind must be MPM_MESH_SURFACE or MPM_MESH_CURVE");
+  const bool curve = desc->kind == MPM_MESH_CURVE;
+  const int per = curve ? 2 : 3;
   if (!(desc->stiffness_normal > 0.0f) && desc->stiffness_shear != 0.0f)
     return fail(MPM_ERR_INVALID, "stiffness_normal must be positive with a shear stiffness");
   const int64_t nv = desc->n_verts, ne = desc->n_tris;
   if (nv >= (int64_t(1) << 31) || ne >= (int64_t(1) << 31))
     return fail(MPM_ERR_CAPACITY, "cloth larger than 2^31 vertices or triangles");
-  for (int64_t i = 0; i < 3 * ne; ++i)
-    if (desc->tris[i] < 0 || desc->tris[i] >= nv) return fail(MPM_ERR_INVALID, "triangle index out of range");
+  for (int64_t i = 0; i < per * ne; ++i)
+    if (desc->tris[i] < 0 || desc->tris[i] >= nv) return fail(MPM_ERR_INVALID, "mesh index out of range");
   // ToZSCloth (Generation.cpp:497-688): areas and frames in double, stored as float
   const float E = desc->E, nu = desc->nu;
   const float mu = E / (2.0f * (1.0f + nu)), lam = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
@@ -815,8 +819,69 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
   std::vector<float> ex(3 * ne), ev(3 * ne, 0.0f), eC(9 * ne, 0.0f), eF(9 * ne), ed(9 * ne),
       eDi(9 * ne), em(ne), evol(ne), emu(ne), elam(ne);
   const float *X = desc->x, *V = desc->v;
-  for (int64_t e = 0; e < ne; ++e) {
+  std::vector<int32_t> inds(3 * ne);
+  for (int64_t e = 0; e < ne && curve; ++e) {
+    // ToZSParticles' curve set-up (Generation.cpp:837-858, 1096-1112)
+    const int32_t *t = desc->tris + 2 * e;
+    double len2 = 0;
+    float d1[3];
+    for (int a = 0; a < 3; ++a) {
+      const double dd = double(X[3 * t[1] + a]) - double(X[3 * t[0] + a]);
+      len2 += dd * dd;
+      d1[a] = X[3 * t[1] + a] - X[3 * t[0] + a];
+    }
+    const float vol = float(std::max(std::sqrt(len2) * double(dx) * double(dx), 10.0 * feps));
+    evol[e] = vol;
+    em[e] = vol * rho;
+    for (int a = 0; a < 3; ++a) {
+      ex[3 * e + a] = (X[3 * t[0] + a] + X[3 * t[1] + a]) / 2.0f;
+      if (V) ev[3 * e + a] = (V[3 * t[0] + a] + V[3 * t[1] + a]) / 2.0f;
+    }
+    // n1: a unit vector orthogonal to the segment (Hughes & Moller 1999);
+    // n2 = normalize(d1 x n1)
+    const double ln[3] = {d1[0], d1[1], d1[2]};
+    double o[3];
+    if (std::fabs(ln[0]) > std::fabs(ln[2])) {
+      o[0] = -ln[1];
+      o[1] = ln[0];
+      o[2] = 0;
+    } else {
+      o[0] = 0;
+      o[1] = -ln[2];
+      o[2] = ln[1];
+    }
+    const double on = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+    const double n1[3] = {o[0] / on, o[1] / on, o[2] / on};
+    const double n2[3] = {ln[1] * n1[2] - ln[2] * n1[1], ln[2] * n1[0] - ln[0] * n1[2],
+                          ln[0] * n1[1] - ln[1] * n1[0]};
+    const double n2n = std::sqrt(n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2]);
+    float dcol[9];
+    for (int a = 0; a < 3; ++a) {
+      dcol[a * 3 + 0] = d1[a];
+      dcol[a * 3 + 1] = float(n1[a]);
+      dcol[a * 3 + 2] = float(n2[a] / n2n);
+    }
+    const double tl = std::sqrt(double(dcol[0]) * dcol[0] + double(dcol[3]) * dcol[3] + double(dcol[6]) * dcol[6]);
+    const double Di[9] = {1 / tl, 0, 0, 0, 1, 0, 0, 0, 1};
+    emu[e] = tl <= feps ? 0.0f : mu;
+    elam[e] = tl <= feps ? 0.0f : lam;
+    for (int i = 0; i < 9; ++i) {
+      ed[9 * e + i] = dcol[i];
+      eDi[9 * e + i] = float(Di[i]);
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double sum = 0;
+        for (int l = 0; l < 3; ++l) sum += double(dcol[i * 3 + l]) * Di[l * 3 + j];
+        eF[9 * e + i * 3 + j] = float(sum);
+      }
+    inds[3 * e] = t[0];
+    inds[3 * e + 1] = inds[3 * e + 2] = t[1];
+    for (int i = 0; i < 2; ++i) dof[t[i]] += vol / 2.0f;
+  }
+  for (int64_t e = 0; e < ne && !curve; ++e) {
     const int32_t *t = desc->tris + 3 * e;
+    for (int i = 0; i < 3; ++i) inds[3 * e + i] = t[i];
     float d1[3], d2[3];
     for (int a = 0; a < 3; ++a) {
       d1[a] = X[3 * t[1] + a] - X[3 * t[0] + a];
@@ -898,11 +963,12 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
       (rc = up(&nc.emu, emu)) || (rc = up(&nc.elam, elam)))
     return rc;
   if ((rc = dalloc(c, &nc.inds, (size_t)3 * ne))) return rc;
-  ZS_CUDA(cudaMemcpyAsync(nc.inds, desc->tris, 3 * ne * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(nc.inds, inds.data(), 3 * ne * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   nc.n_verts = nv;
   nc.n_eles = ne;
-  nc.model = desc->model;
+  nc.kind = desc->kind;
+  nc.model = curve ? MPM_STVK : desc->model;  // curves: StVK-Hencky (Generation.cpp:761-769)
   nc.gamma = desc->stiffness_shear;
   nc.k = desc->stiffness_normal;
   nc.fc = std::tan(desc->friction_angle / 3.14159265358979323846f);

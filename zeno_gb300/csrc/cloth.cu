@@ -17,6 +17,11 @@
 //    and mean velocity of their vertices, d1 = p1 - p0, d2 = p2 - p0, d3 +=
 //    (dt C + dt^2 / 2 C^2) d3, F = d DmInv, and the surface return mapping
 //    (MPMPipeline.cu:973-1011) on d = Q R.
+// Curves (ToZSParticles' segment meshes, hair) take the same passes with
+// p2g_curve (Transfer.cu:174-356: StVK-Hencky cross-section, stretch
+// k (r00 - 1), type ii through DmInv00 on the two vertices), the curve G2P
+// (:1445-1513: d2, d3 advected with C) and return_mapping_curve
+// (MPMPipeline.cu:1012-1093).
 #include <cuda_runtime.h>
 
 #include "binning.cuh"
@@ -169,32 +174,64 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
       dm[i] = cl.ed[9 * e + i];
     }
     gram_schmidt(F, Q, R);
-    const float R2[4] = {R[0], R[1], R[3], R[4]};
-    float P2[4];
-    first_piola_2d(cl.model, cl.emu[e], cl.elam[e], R2, P2);
-    float P[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      P[i * 3 + 0] = Q[i * 3 + 0] * P2[0] + Q[i * 3 + 1] * P2[2];
-      P[i * 3 + 1] = Q[i * 3 + 0] * P2[1] + Q[i * 3 + 1] * P2[3];
-      P[i * 3 + 2] = 0.0f;
-    }
+    const bool curve = cl.kind == MPM_MESH_CURVE;
     const float g = cl.gamma;
-    float gf = 0.0f;
-    if (R[8] < 1.0f) {
-      const float vv = 1.0f - R[8];
-      gf = -cl.k * vv * vv;
+    float P[9], A[9], Rt[9];
+    if (!curve) {
+      // surface: the in-plane block, normal compression and shear
+      const float R2[4] = {R[0], R[1], R[3], R[4]};
+      float P2[4];
+      first_piola_2d(cl.model, cl.emu[e], cl.elam[e], R2, P2);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        P[i * 3 + 0] = Q[i * 3 + 0] * P2[0] + Q[i * 3 + 1] * P2[2];
+        P[i * 3 + 1] = Q[i * 3 + 0] * P2[1] + Q[i * 3 + 1] * P2[3];
+        P[i * 3 + 2] = 0.0f;
+      }
+      float gf = 0.0f;
+      if (R[8] < 1.0f) {
+        const float vv = 1.0f - R[8];
+        gf = -cl.k * vv * vv;
+      }
+      const float Av[9] = {g * R[2] * R[2], g * R[2] * R[5], g * R[2] * R[8],
+                           g * R[2] * R[5], g * R[5] * R[5], g * R[5] * R[8],
+                           g * R[2] * R[8], g * R[5] * R[8], gf * R[8]};
+      const float i00 = 1.0f / R[0], i11 = 1.0f / R[4], i22 = 1.0f / R[8];
+      const float i01 = -R[1] * i00 * i11, i12 = -R[5] * i11 * i22;
+      const float i02 = (R[1] * R[5] - R[2] * R[4]) * i00 * i11 * i22;
+      const float RiT[9] = {i00, 0.0f, 0.0f, i01, i11, 0.0f, i02, i12, i22};  // R^-T
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        A[i] = Av[i];
+        Rt[i] = RiT[i];
+      }
+    } else {
+      // curve: StVK-Hencky cross-section block, stretch k (r00 - 1), shear A
+      // times the diagonal of R's cofactors over det R (Transfer.cu:204-237)
+      const float R2[4] = {R[4], R[5], 0.0f, R[8]};
+      float P2[4];
+      first_piola_2d(MPM_STVK, cl.emu[e], cl.elam[e], R2, P2);
+      const float Pl[9] = {cl.k * (R[0] - 1.0f), 0.0f, 0.0f, 0.0f, P2[0], P2[1], 0.0f, P2[2], P2[3]};
+      float QP[9];
+      matmul3(Q, Pl, QP);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) P[i] = QP[i];
+      const float rr = R[1] * R[1] + R[2] * R[2];
+      const float a01 = (R[4] * R[1] + R[5] * R[2]) * g, a02 = R[8] * R[2] * g;
+      const float Av[9] = {rr * g, a01, a02, a01, 0.0f, 0.0f, a02, 0.0f, 0.0f};
+      float invJ = R[0] * R[4] * R[8];
+      if (invJ != 0.0f) invJ = 1.0f / invJ;
+      const float Rit[9] = {R[4] * R[8] * invJ, 0.0f, 0.0f, 0.0f, R[0] * R[8] * invJ, 0.0f,
+                            0.0f, 0.0f, R[0] * R[4] * invJ};
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        A[i] = Av[i];
+        Rt[i] = Rit[i];
+      }
     }
-    const float A[9] = {g * R[2] * R[2], g * R[2] * R[5], g * R[2] * R[8],
-                        g * R[2] * R[5], g * R[5] * R[5], g * R[5] * R[8],
-                        g * R[2] * R[8], g * R[5] * R[8], gf * R[8]};
-    const float i00 = 1.0f / R[0], i11 = 1.0f / R[4], i22 = 1.0f / R[8];
-    const float i01 = -R[1] * i00 * i11, i12 = -R[5] * i11 * i22;
-    const float i02 = (R[1] * R[5] - R[2] * R[4]) * i00 * i11 * i22;
-    const float RiT[9] = {i00, 0.0f, 0.0f, i01, i11, 0.0f, i02, i12, i22};  // R^-T
     float QA[9], T[9];
     matmul3(Q, A, QA);
-    matmul3(QA, RiT, T);
+    matmul3(QA, Rt, T);
 #pragma unroll
     for (int i = 0; i < 9; ++i) P[i] += T[i];
     const float mass = cl.em[e], vol = cl.evol[e];
@@ -217,14 +254,16 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
           const float gw[3] = {wgrad(s0, i) * s1.w[j] * s2.w[k] * inv_dx,
                                s0.w[i] * wgrad(s1, j) * s2.w[k] * inv_dx,
                                s0.w[i] * s1.w[j] * wgrad(s2, k) * inv_dx};
-          const float sft = (gw[0] * dm[2] + gw[1] * dm[5] + gw[2] * dm[8]) * kf;
+          // surface: P_c3 (grad W . d_c3); curve: P_c23 (d_c23^T grad W); times -vol dt
+          const float s2f = (gw[0] * dm[2] + gw[1] * dm[5] + gw[2] * dm[8]) * kf;
+          const float s1f = curve ? (gw[0] * dm[1] + gw[1] * dm[4] + gw[2] * dm[7]) * kf : 0.0f;
           const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
           const float vn[3] = {ve.x, ve.y, ve.z};
           float mom[3], fo[3];
 #pragma unroll
           for (int a = 0; a < 3; ++a) {
             const float Cx = C[a * 3 + 0] * xi[0] + C[a * 3 + 1] * xi[1] + C[a * 3 + 2] * xi[2];
-            fo[a] = P[a * 3 + 2] * sft;
+            fo[a] = P[a * 3 + 1] * s1f + P[a * 3 + 2] * s2f;
             mom[a] = W * mass * (vn[a] + Cx) + (flip_style ? 0.0f : fo[a]);
           }
           float4 *g4 = d.grid + idx;
@@ -239,6 +278,18 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
             atomicAdd(&h4->z, fo[2]);
           }
         }
+    if (curve) {  // type (ii): +-vol dt P_c0 DmInv00 on the two vertices
+      const int t0 = cl.inds[3 * e], t1 = cl.inds[3 * e + 1];
+      const float di = cl.eDmInv[9 * e];
+      if (t0 < 0 || t0 >= cl.n_verts || t1 < 0 || t1 >= cl.n_verts) continue;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float f = vol * dt * P[a * 3 + 0] * di;
+        atomicAdd(&cl.imp[3 * t0 + a], f);
+        atomicAdd(&cl.imp[3 * t1 + a], -f);
+      }
+      continue;
+    }
     // type (ii): impulses from the in-plane columns of P through DmInv rows
     const float r0[2] = {cl.eDmInv[9 * e + 0], cl.eDmInv[9 * e + 1]};
     const float r1[2] = {cl.eDmInv[9 * e + 3], cl.eDmInv[9 * e + 4]};
@@ -360,6 +411,67 @@ __device__ __forceinline__ void cloth_gather(const DevPtrs &d, const SceneParams
   for (int i = 0; i < 9; ++i) Cn[i] = D[i];
 }
 
+// curve element G2P (Transfer.cu:1445-1513) and return_mapping_curve
+// (MPMPipeline.cu:1012-1093, alpha = alpha_tangent = cohesion = 0): the
+// cross-section's Hencky strain of R's lower-right block is projected to its
+// mean when compressive (to zero when already isotropic within eps) and to
+// zero otherwise, the block becomes exp(e_mean) times its closest rotation,
+// and the shear (r01, r02) is cleared
+__device__ __forceinline__ void curve_g2p(const DevPtrs &d, const ClothDev &cl, long long e, int t0,
+                                          int t1, float dt, const float (&Cn)[9]) {
+  float dm[9], CC[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) dm[i] = cl.ed[9 * e + i];
+  matmul3(Cn, Cn, CC);
+  float dn[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float p0 = cl.vx[3 * t0 + a], p1 = cl.vx[3 * t1 + a];
+    cl.ex[3 * e + a] = (p0 + p1) / 2.0f;
+    cl.ev[3 * e + a] = (cl.vv[3 * t0 + a] + cl.vv[3 * t1 + a]) / 2.0f;
+    dn[a * 3 + 0] = p1 - p0;
+#pragma unroll
+    for (int c = 1; c < 3; ++c) {
+      float s = dm[a * 3 + c];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) s += (dt * Cn[a * 3 + b] + 0.5f * dt * dt * CC[a * 3 + b]) * dm[b * 3 + c];
+      dn[a * 3 + c] = s;
+    }
+  }
+  float Q[9], R[9];
+  gram_schmidt(dn, Q, R);
+  const float feps = 1.1920928955078125e-07f;
+  const float a = R[4], b = R[5], c = R[7], dd = R[8];
+  const float E = 0.5f * (a + dd), Fv = 0.5f * (a - dd), G = 0.5f * (c + b), H = 0.5f * (c - b);
+  const float q = sqrtf(E * E + H * H), r = sqrtf(Fv * Fv + G * G);
+  float e0 = logf(fmaxf(fabsf(q + r), 128.0f * feps)), e1 = logf(fmaxf(fabsf(q - r), 128.0f * feps));
+  const float tr = e0 + e1;
+  float em = 0.0f;
+  if (tr < 0.0f) {
+    const float h0 = e0 - 0.5f * tr, h1 = e1 - 0.5f * tr;
+    em = sqrtf(h0 * h0 + h1 * h1) < feps ? 0.0f : 0.5f * tr;
+  }
+  const float sc = expf(em), rn = 1.0f / sqrtf((a + dd) * (a + dd) + (c - b) * (c - b));
+  R[4] = sc * (a + dd) * rn;
+  R[5] = -sc * (c - b) * rn;
+  R[7] = sc * (c - b) * rn;
+  R[8] = sc * (a + dd) * rn;
+  R[1] = R[2] = 0.0f;
+  matmul3(Q, R, dn);
+  float Di[9], Fn[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Di[i] = cl.eDmInv[9 * e + i];
+  matmul3(dn, Di, Fn);
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    cl.ed[9 * e + i] = dn[i];
+    cl.eF[9 * e + i] = Fn[i];
+    finite = finite && isfinite(Fn[i]);
+  }
+  if (!finite) atomicOr(&d.cnt->status, ST_NAN);
+}
+
 __global__ void k_cloth_g2p_verts(DevPtrs d) {
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
@@ -400,6 +512,10 @@ __global__ void k_cloth_g2p_elements(DevPtrs d) {
     int t[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) t[i] = min(max(cl.inds[3 * e + i], 0), (int)cl.n_verts - 1);
+    if (cl.kind == MPM_MESH_CURVE) {
+      curve_g2p(d, cl, e, t[0], t[1], dt, Cn);
+      continue;
+    }
     float p[3][3], v[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)

@@ -155,7 +155,9 @@ inline void collider_world_box(ColliderDev &c) {
 // when the context holds no cloth.
 struct ClothDev {
   long long n_verts, n_eles;
-  int model;                 // MPM_FCR / MPM_NHK / MPM_STVK
+  int kind;                  // MPM_MESH_SURFACE / MPM_MESH_CURVE (inds: 3 per element,
+                             // curves use the first 2)
+  int model;                 // MPM_FCR / MPM_NHK / MPM_STVK (curves: MPM_STVK)
   float gamma, k, fc, dc;    // shear stiffness, normal stiffness, tan(fa / pi), damping
   float *vx, *vv, *vC, *vm, *imp;
   float *ex, *ev, *eC, *eF, *ed, *eDmInv, *em, *evol, *emu, *elam;

@@ -36,6 +36,7 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
   return p.verts.has_attr(k) ? &p.verts.attr<float>(k) : nullptr;
 }
 inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris.values; }
+inline const std::vector<vec2i> &lines(PrimitiveObject &p) { return p.lines.values; }
 }  // namespace prim_access
 }  // namespace zeno
 #else
@@ -57,6 +58,7 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
   return it == p.attrs1.end() ? nullptr : &it->second;
 }
 inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris; }
+inline const std::vector<vec2i> &lines(PrimitiveObject &p) { return p.lines; }
 }  // namespace prim_access
 }  // namespace zeno
 #endif
@@ -234,17 +236,22 @@ void attach_cloth(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &cl) {
   if (cl.cloth_ctx.lock() == ctx) return;
   if (cl.cloth_ctx.lock()) throw std::runtime_error("ZSCloth: the cloth belongs to another context");
   auto &pos = prim_access::pos(*cl.prim);
-  const auto &tr = prim_access::tris(*cl.prim);
-  std::vector<int32_t> tris(3 * tr.size());
-  for (size_t i = 0; i < tr.size(); ++i)
-    for (int a = 0; a < 3; ++a) tris[3 * i + a] = tr[i][a];
-  const auto *v = prim_access::vel(*cl.prim, false);
   mpm_cloth_desc d = cl.cloth_desc;
+  std::vector<int32_t> idx;
+  if (d.kind == MPM_MESH_CURVE) {
+    const auto &ln = prim_access::lines(*cl.prim);
+    for (const auto &l : ln) idx.insert(idx.end(), {l[0], l[1]});
+    d.n_tris = (int64_t)ln.size();
+  } else {
+    const auto &tr = prim_access::tris(*cl.prim);
+    for (const auto &t : tr) idx.insert(idx.end(), {t[0], t[1], t[2]});
+    d.n_tris = (int64_t)tr.size();
+  }
+  const auto *v = prim_access::vel(*cl.prim, false);
   d.n_verts = (int64_t)pos.size();
   d.x = pos.empty() ? nullptr : pos[0].data();
   d.v = v && v->size() == pos.size() ? (*v)[0].data() : nullptr;
-  d.n_tris = (int64_t)tr.size();
-  d.tris = tris.data();
+  d.tris = idx.data();
   check(mpm_cloth_create(ctx->h, &d), "mpm_cloth_create");
   cl.cloth_ctx = ctx;
   cl.ctx = ctx;
@@ -398,20 +405,22 @@ struct ToZSParticles : INode {
       }
     }
     if (out->category != 0) {
-      // a mesh (Generation.cpp:738-749): triangles become a surface (cloth)
-      // with the defaults of Generation.cpp:695-699 (k = 800, gamma = fa =
-      // dc = 0); curves and tetrahedra are not implemented
-      if (prim_access::tris(*prim).empty())
+      // a mesh (Generation.cpp:738-749): triangles become a surface (cloth),
+      // segments a curve (hair), with the defaults of Generation.cpp:695-699
+      // (k = 800, gamma = fa = dc = 0); tetrahedra are not implemented
+      const bool tri = !prim_access::tris(*prim).empty(), seg = !prim_access::lines(*prim).empty();
+      if (!tri && !seg)
         throw std::runtime_error("ToZSParticles: category " + std::to_string(out->category) +
-                                 " needs a triangle mesh (curves and tetrahedra are not "
+                                 " needs a triangle or segment mesh (tetrahedra are not "
                                  "implemented by this backend)");
       const int type = model->mat.type;
       if (type != MPM_FCR && type != MPM_NHK && type != MPM_STVK)
         throw std::runtime_error("ToZSParticles: a surface takes fcr, nhk or stvk");
       out->n = 0;
       out->cloth = true;
-      out->category = 2;  // ZenoParticles::surface
+      out->category = tri ? 2 : 1;  // ZenoParticles::surface / curve
       mpm_cloth_desc &cd = out->cloth_desc;
+      cd.kind = tri ? MPM_MESH_SURFACE : MPM_MESH_CURVE;
       cd.model = type;
       cd.E = model->mat.E;
       cd.nu = model->mat.nu;

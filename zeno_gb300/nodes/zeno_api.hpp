@@ -29,6 +29,7 @@ namespace zeno {
 
 using vec3f = std::array<float, 3>;
 using vec3i = std::array<int, 3>;
+using vec2i = std::array<int, 2>;
 
 struct IObject {
   virtual ~IObject() = default;
@@ -65,6 +66,7 @@ struct PrimitiveObject : IObject {
   std::map<std::string, std::vector<vec3f>> attrs3;
   std::map<std::string, std::vector<float>> attrs1;
   std::vector<vec3i> tris;  // triangle vertex indices
+  std::vector<vec2i> lines; // segment vertex indices
   std::vector<vec3f> &verts() { return attrs3["pos"]; }
   size_t size() const {
     auto it = attrs3.find("pos");

@@ -110,11 +110,12 @@ def plane_collider(height: float, extent: float, spacing: float, type: int = 1, 
 
 @dataclass
 class ClothMesh:
-    """A triangle mesh stepped as codimensional cloth (ToZSCloth): vertex
-    positions x (nv, 3), optional velocities v, triangles tris (nt, 3), the
-    in-plane elastic model (FCR, NHK or STVK) with E, nu, density, and the
-    cloth parameters stiffness_shear (gamma), stiffness_normal (k),
-    friction_angle (fa) and damping_coeff (dc)."""
+    """A mesh stepped as codimensional MPM: a triangle mesh as cloth
+    (ToZSCloth; tris (nt, 3)) or a segment mesh as curves (ToZSParticles'
+    curve category; tris (ns, 2)), vertex positions x (nv, 3), optional
+    velocities v, the elastic model (FCR, NHK or STVK; curves always take
+    StVK-Hencky with the same E, nu) with density, and stiffness_shear
+    (gamma), stiffness_normal (k), friction_angle (fa), damping_coeff (dc)."""
     x: np.ndarray
     tris: np.ndarray
     v: np.ndarray = None
@@ -126,6 +127,21 @@ class ClothMesh:
     k: float = 800.0
     fa: float = 0.0
     dc: float = 0.0
+
+
+def curve_strands(origin, length: float, n_strands: int, n_segs: int, spacing: float,
+                  **kw) -> ClothMesh:
+    """n_strands straight strands of n_segs segments hanging along -y from a
+    row of roots at origin + (i spacing, 0, 0); ToZSParticles' defaults
+    (gamma = fa = dc = 0, k = 800) unless given."""
+    xs, segs = [], []
+    for s_ in range(n_strands):
+        base = len(xs)
+        for j in range(n_segs + 1):
+            xs.append((origin[0] + s_ * spacing, origin[1] - j * length / n_segs, origin[2]))
+        segs += [(base + j, base + j + 1) for j in range(n_segs)]
+    kw.setdefault("model", STVK)
+    return ClothMesh(x=np.array(xs, np.float32), tris=np.array(segs, np.int32), **kw)
 
 
 def cloth_sheet(center, size: float, n: int, jitter: float = 0.0, seed: int = 0, **kw) -> ClothMesh:

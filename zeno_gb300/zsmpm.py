@@ -174,7 +174,8 @@ class ClothDesc(C.Structure):
                 ("n_tris", C.c_int64), ("tris", C.c_void_p), ("model", C.c_int32),
                 ("E", C.c_float), ("nu", C.c_float), ("density", C.c_float),
                 ("stiffness_shear", C.c_float), ("stiffness_normal", C.c_float),
-                ("friction_angle", C.c_float), ("damping_coeff", C.c_float)]
+                ("friction_angle", C.c_float), ("damping_coeff", C.c_float),
+                ("kind", C.c_int32)]
 
 
 class Context:
@@ -221,15 +222,16 @@ class Context:
                     "mpm_particles_set_attr")
 
     def add_cloth(self, mesh):
-        """ToZSCloth for a scenes.ClothMesh: the cloth is stepped with the
-        particles by every substep entry point."""
+        """ToZSCloth for a scenes.ClothMesh of triangles, or ToZSParticles'
+        curve set-up for one of segments (tris of shape (n, 2)): the mesh is
+        stepped with the particles by every substep entry point."""
         x = np.ascontiguousarray(mesh.x, dtype=np.float32)
         v = None if mesh.v is None else np.ascontiguousarray(mesh.v, dtype=np.float32)
         tris = np.ascontiguousarray(mesh.tris, dtype=np.int32)
         desc = ClothDesc(x.shape[0], x.ctypes.data, v.ctypes.data if v is not None else None,
                          tris.shape[0], tris.ctypes.data, int(mesh.model), float(mesh.E),
                          float(mesh.nu), float(mesh.density), float(mesh.gamma), float(mesh.k),
-                         float(mesh.fa), float(mesh.dc))
+                         float(mesh.fa), float(mesh.dc), 1 if tris.shape[1] == 2 else 0)
         self._check(self._L.mpm_cloth_create(self.h, C.byref(desc)), "mpm_cloth_create")
         self._cloth_n = (x.shape[0], tris.shape[0])
 
