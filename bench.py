@@ -662,6 +662,7 @@ def run_gpu(args):
         pg = dist
     from zeno_gb300 import zsmpm
     scene, parts = make_workload()
+    scene.transfer = {"apic": 0, "flip": 1, "aflip": 2}[args.transfer]
     ctx = zsmpm.Context(scene, max_particles=parts.n, device=dev)
     # a dedicated stream (a non-zero handle): the context's kernels and the
     # timing events below are ordered on it
@@ -858,7 +859,11 @@ def main():
                     help="skip the batched / differentiable forms reported beside the headline")
     ap.add_argument("--quick", action="store_true",
                     help="device timing only (no clock sampling, e2e or CPU legs): for ncu")
+    ap.add_argument("--transfer", default="apic", choices=["apic", "flip", "aflip"],
+                    help="grid transfer of the --quick run (profiling the FLIP kernels)")
     args = ap.parse_args()
+    if args.transfer != "apic" and not args.quick:
+        ap.error("--transfer applies to --quick runs; the headline is the APIC substep")
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -218,7 +218,11 @@ int32_t mpm_cloth_download(mpm_ctx *ctx, float *vx, float *vv, float *vC, float 
 /* ToZSParticles (Generation.cpp:690-1145): host arrays -> device store.
  * NULL optional arrays take the reference defaults: v = 0, C = 0, F = I,
  * J = 1.  mu / lam are the per-particle overrides added by
- * AdjustParticleMaterial (Temp.cu:16-56); both NULL or both set. */
+ * AdjustParticleMaterial (Temp.cu:16-56); both NULL or both set.  Large
+ * uploads are copied in pieces that overlap the device-side conversion;
+ * page-locked host arrays give the full host-link rate.  A material id out
+ * of range fails with MPM_ERR_INVALID and leaves the context without
+ * particles. */
 int32_t mpm_particles_upload(mpm_ctx *ctx, int64_t n, const float *x, const float *v,
                              const float *C, const float *F, const float *J,
                              const float *m, const float *vol, const int32_t *mat,

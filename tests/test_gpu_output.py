@@ -55,3 +55,42 @@ def test_frame_output_equals_download(zsmpm_mod):
     np.testing.assert_array_equal(snap_v, ref10["v"])
     np.testing.assert_array_equal(x, now["x"])
     np.testing.assert_array_equal(v, now["v"])
+
+
+def test_pinned_upload_download(zsmpm_mod):
+    """Page-locked host arrays (the fast host-link path) give the same results
+    as pageable ones, bit for bit, and keep the material check."""
+    import torch
+    scene, parts = S.multi_material(dx=1.0 / 64, region_cells=(16, 8, 8))
+    n = parts.n
+    pin = lambda shape, dt=torch.float32: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    arrs = {"x": pin((n, 3)), "v": pin((n, 3)), "C": pin((n, 9)), "F": pin((n, 9)), "J": pin((n,)),
+            "m": pin((n,)), "vol": pin((n,)), "mat": pin((n,), torch.int32)}
+    arrs["x"][:] = parts.x
+    arrs["v"][:] = parts.v
+    arrs["C"][:] = parts.C.reshape(n, 9)
+    arrs["F"][:] = parts.F.reshape(n, 9)
+    arrs["J"][:] = parts.J
+    arrs["m"][:] = parts.m
+    arrs["vol"][:] = parts.vol
+    arrs["mat"][:] = parts.mat
+    ox, ov, oF = pin((n, 3)), pin((n, 3)), pin((n, 9))
+    with zsmpm_mod.Context(scene, max_particles=n) as ctx:
+        ctx.upload_raw(n, arrs["x"], arrs["v"], arrs["C"], arrs["F"], arrs["J"], arrs["m"],
+                       arrs["vol"], arrs["mat"])
+        ctx.substep(scene.dt, 5)
+        ctx._check(ctx._L.mpm_particles_download(ctx.h, zsmpm_mod._p(ox), zsmpm_mod._p(ov), None,
+                                                 zsmpm_mod._p(oF), None), "download")
+    with zsmpm_mod.Context(scene, max_particles=n) as ctx:
+        ctx.upload(parts)
+        ctx.substep(scene.dt, 5)
+        ref = ctx.download(("x", "v", "F"))
+    np.testing.assert_array_equal(ox, ref["x"])
+    np.testing.assert_array_equal(ov, ref["v"])
+    np.testing.assert_array_equal(oF, ref["F"].reshape(n, 9))
+    # an out-of-range material id in a page-locked array is still caught
+    arrs["mat"][0] = 7
+    with zsmpm_mod.Context(scene, max_particles=n) as ctx:
+        with pytest.raises(zsmpm_mod.MPMError, match="material"):
+            ctx.upload_raw(n, arrs["x"], arrs["v"], None, None, None, arrs["m"], arrs["vol"],
+                           arrs["mat"])

@@ -40,6 +40,8 @@ int32_t fail(int32_t code, const std::string &msg) {
 
 void zsmpm::set_last_error(const std::string &msg) { g_last_error = msg; }
 
+constexpr int kUploadChunks = 4;  // pieces of a large upload, pipelined
+
 struct mpm_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
@@ -61,6 +63,9 @@ struct mpm_ctx {
   std::vector<SceneParams> scenes;
   int n_materials = 0;
   bool differentiable = false;  // every material has an adjoint
+  // pipelined upload: host-to-device copies on their own stream
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[kUploadChunks + 1] = {};
   // asynchronous frame output: device snapshot, copy stream, events
   float *frame_buf = nullptr;
   cudaStream_t frame_stream = nullptr;
@@ -396,6 +401,12 @@ int32_t mpm_ctx_destroy(mpm_ctx *c) {
     cudaStreamDestroy(c->frame_stream);
   }
   if (c->frame_ready) cudaEventDestroy(c->frame_ready);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  for (cudaEvent_t e : c->copy_ev)
+    if (e) cudaEventDestroy(e);
   if (c->frame_done) cudaEventDestroy(c->frame_done);
   for (void *p : c->allocs) cudaFree(p);
   for (void *p : c->collider_allocs) cudaFree(p);
@@ -627,60 +638,72 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
   if ((mu == nullptr) != (lam == nullptr)) return fail(MPM_ERR_INVALID, "mu and lam go together");
   if (c->n_materials <= 0) return fail(MPM_ERR_STATE, "set materials before uploading");
   const int alt = 1 - c->cur;
-  float *st = c->d.pbuf[alt];
+  float *st = c->d.pbuf[alt];  // staging: the other buffer is free between substeps
   int32_t *ist = c->d.ibuf[alt];
-  IngestSrc src{};
-  auto put = [&](const float *h, size_t off, size_t count, const float **dst) -> int32_t {
-    if (!h) {
-      *dst = nullptr;
-      return MPM_OK;
-    }
-    ZS_CUDA(cudaMemcpyAsync(st + off, h, count * sizeof(float), cudaMemcpyHostToDevice,
-                            c->stream));
-    *dst = st + off;
-    return MPM_OK;
-  };
   const size_t N = (size_t)n;
-  if ((rc = put(x, 0, 3 * N, &src.x)) || (rc = put(v, 3 * N, 3 * N, &src.v)) ||
-      (rc = put(C, 6 * N, 9 * N, &src.C)) || (rc = put(F, 15 * N, 9 * N, &src.F)) ||
-      (rc = put(J, 24 * N, N, &src.J)) || (rc = put(m, 25 * N, N, &src.m)) ||
-      (rc = put(vol, 26 * N, N, &src.vol)) || (rc = put(mu, 27 * N, N, &src.mu)) ||
-      (rc = put(lam, 28 * N, N, &src.lam)))
-    return rc;
-  src.mat = nullptr;
-  if (mat && n > 0) {
-    // material ids are checked on the device, against the staged copy, before
-    // the store is touched: the wait overlaps the copies the upload needs anyway
-    ZS_CUDA(cudaMemcpyAsync(ist, mat, N * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
-    src.mat = ist;
-    ZS_CUDA(cudaMemsetAsync(&c->d.cnt->bad_material, 0, sizeof(int), c->stream));
-    launch_check_materials(c->d, ist, n, c->n_materials, c->stream);
-    if ((rc = launch_check("material check"))) return rc;
-    ZS_CUDA(cudaMemcpyAsync(&c->h_cnt->bad_material, &c->d.cnt->bad_material, sizeof(int),
-                            cudaMemcpyDeviceToHost, c->stream));
-    ZS_CUDA(cudaStreamSynchronize(c->stream));
-    if (c->h_cnt->bad_material) return fail(MPM_ERR_INVALID, "material id out of range");
-  }
-  launch_ingest(c->d, c->cur, src, n, c->stream);
-  if ((rc = launch_check("ingest"))) return rc;
-  if (n > 0) {  // ToZSParticles: beta = 0, vms = 0 (Generation.cpp:944-966)
-    ZS_CUDA(cudaMemsetAsync(c->d.beta, 0, (size_t)n * sizeof(float), c->stream));
-    ZS_CUDA(cudaMemsetAsync(c->d.vms, 0, (size_t)n * sizeof(float), c->stream));
+  IngestSrc src{};
+  const float *const hs[9] = {x, v, C, F, J, m, vol, mu, lam};
+  const size_t off[9] = {0, 3 * N, 6 * N, 15 * N, 24 * N, 25 * N, 26 * N, 27 * N, 28 * N};
+  const int width[9] = {3, 3, 9, 9, 1, 1, 1, 1, 1};
+  const float **dsts[9] = {&src.x, &src.v, &src.C, &src.F, &src.J, &src.m, &src.vol, &src.mu, &src.lam};
+  for (int a = 0; a < 9; ++a) *dsts[a] = hs[a] ? st + off[a] : nullptr;
+  src.mat = mat ? ist : nullptr;
+  // chunks of the particle range: the copies of chunk k + 1 (on the copy
+  // stream) overlap the material check and ingest of chunk k (on the
+  // context's stream); one synchronisation at the end
+  const int K = n >= (1 << 20) ? kUploadChunks : 1;
+  if (!c->copy_stream) {
+    ZS_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k <= kUploadChunks; ++k)
+      ZS_CUDA(cudaEventCreateWithFlags(&c->copy_ev[k], cudaEventDisableTiming));
   }
   c->prm.n = n;
   c->prm.has_lame = mu ? 1 : 0;
   for (int s = 0; s < ns; ++s) c->scenes[s].p_off = scene_offsets ? scene_offsets[s] : 0;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
-  launch_stress(c->d, c->cur, c->stream);  // S = vol * tau read by P2G
-  if ((rc = launch_check("stress"))) return rc;
+  if (n > 0) {
+    ZS_CUDA(cudaEventRecord(c->copy_ev[kUploadChunks], c->stream));  // staging free from here
+    ZS_CUDA(cudaStreamWaitEvent(c->copy_stream, c->copy_ev[kUploadChunks], 0));
+    ZS_CUDA(cudaMemsetAsync(&c->d.cnt->bad_material, 0, sizeof(int), c->stream));
+  }
+  for (int k = 0; k < K && n > 0; ++k) {
+    const long long b0 = n * k / K, b1 = n * (k + 1) / K;
+    for (int a = 0; a < 9; ++a)
+      if (hs[a])
+        ZS_CUDA(cudaMemcpyAsync(st + off[a] + b0 * width[a], hs[a] + b0 * width[a],
+                                (b1 - b0) * width[a] * sizeof(float), cudaMemcpyHostToDevice,
+                                c->copy_stream));
+    if (mat)
+      ZS_CUDA(cudaMemcpyAsync(ist + b0, mat + b0, (b1 - b0) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                              c->copy_stream));
+    ZS_CUDA(cudaEventRecord(c->copy_ev[k], c->copy_stream));
+    ZS_CUDA(cudaStreamWaitEvent(c->stream, c->copy_ev[k], 0));
+    if (mat) launch_check_materials(c->d, ist + b0, b1 - b0, c->n_materials, c->stream);
+    launch_ingest(c->d, c->cur, src, b0, b1, c->stream);
+    launch_stress(c->d, c->cur, c->stream, b0, b1);  // S = vol * tau read by P2G
+    if ((rc = launch_check("ingest"))) return rc;
+  }
+  if (n > 0) {  // ToZSParticles: beta = 0, vms = 0 (Generation.cpp:944-966)
+    ZS_CUDA(cudaMemsetAsync(c->d.beta, 0, (size_t)n * sizeof(float), c->stream));
+    ZS_CUDA(cudaMemsetAsync(c->d.vms, 0, (size_t)n * sizeof(float), c->stream));
+  }
   // a fresh store: clear the status word and the whole directory
   ZS_CUDA(cudaMemsetAsync(&c->d.cnt->status, 0, sizeof(int), c->stream));
   c->needs_full_clear = true;
   c->partition_valid = false;
   c->binned = false;
   c->substeps = 0;
+  if (mat && n > 0)
+    ZS_CUDA(cudaMemcpyAsync(&c->h_cnt->bad_material, &c->d.cnt->bad_material, sizeof(int),
+                            cudaMemcpyDeviceToHost, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
+  if (mat && n > 0 && c->h_cnt->bad_material) {  // the store is not usable: no particles
+    c->prm.n = 0;
+    c->prm_dirty = true;
+    push_params(c);
+    return fail(MPM_ERR_INVALID, "material id out of range (the context holds no particles)");
+  }
   return MPM_OK;
 }
 
@@ -728,7 +751,11 @@ int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *
   if (rc) return rc;
   const long long n = c->prm.n;
   float *st = c->d.pbuf[1 - c->cur];
-  launch_egest(c->d, c->cur, st, n, c->stream);
+  // only the requested channels are gathered into upload order
+  launch_egest(c->d, c->cur,
+               EgestDst{x ? st : nullptr, v ? st + 3 * n : nullptr, C ? st + 6 * n : nullptr,
+                        F ? st + 15 * n : nullptr, J ? st + 24 * n : nullptr},
+               n, c->stream);
   if ((rc = launch_check("egest"))) return rc;
   const size_t N = (size_t)n;
   auto get = [&](float *h, size_t off, size_t count) -> int32_t {

@@ -10,9 +10,10 @@
 namespace zsmpm {
 namespace {
 
+// particles [b0, b1) of the staged arrays into slots b0..b1-1
 __global__ void k_ingest(float *__restrict__ pb, int32_t *__restrict__ ib, long long cap,
-                         IngestSrc src, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+                         IngestSrc src, long long b0, long long b1) {
+  for (long long i = b0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < b1;
        i += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -36,25 +37,25 @@ __global__ void k_ingest(float *__restrict__ pb, int32_t *__restrict__ ib, long 
   }
 }
 
-// dst layout: x (3n) | v (3n) | C (9n) | F (9n) | J (n), each in upload order
+// x (n x 3), v, C (n x 9), F, J in upload order; any destination may be
+// null, device memory or host memory the device can address
 __global__ void k_egest(const float *__restrict__ pb, const int32_t *__restrict__ ib,
-                        long long cap, float *__restrict__ dst, long long n) {
-  float *x = dst, *v = dst + 3 * n, *C = dst + 6 * n, *F = dst + 15 * n, *J = dst + 24 * n;
+                        long long cap, EgestDst o, long long n) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
        s += (long long)gridDim.x * blockDim.x) {
     const long long u = ib[iidx(IC_ID, s)];
     if (u < 0 || u >= n) continue;  // slot not rewritten after a binning error
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      x[3 * u + k] = pb[pidx((CH_X + k), s)];
-      v[3 * u + k] = pb[pidx((CH_V + k), s)];
+      if (o.x) o.x[3 * u + k] = pb[pidx((CH_X + k), s)];
+      if (o.v) o.v[3 * u + k] = pb[pidx((CH_V + k), s)];
     }
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      C[9 * u + k] = pb[pidx((CH_C + k), s)];
-      F[9 * u + k] = pb[pidx((CH_F + k), s)];
+      if (o.C) o.C[9 * u + k] = pb[pidx((CH_C + k), s)];
+      if (o.F) o.F[9 * u + k] = pb[pidx((CH_F + k), s)];
     }
-    J[u] = pb[pidx(CH_J, s)];
+    if (o.J) o.J[u] = pb[pidx(CH_J, s)];
   }
 }
 
@@ -134,12 +135,13 @@ void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *la
   k_set_lame<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], d.cap, mu, lam, n);
 }
 
-void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s) {
-  if (n <= 0) return;
-  k_ingest<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], d.cap, src, n);
+void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long b0, long long b1,
+                   cudaStream_t s) {
+  if (b1 <= b0) return;
+  k_ingest<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], d.cap, src, b0, b1);
 }
 
-void launch_egest(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s) {
+void launch_egest(const DevPtrs &d, int cur, EgestDst dst, long long n, cudaStream_t s) {
   if (n <= 0) return;
   k_egest<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], d.cap, dst, n);
 }

@@ -800,11 +800,12 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
 
 // S = vol * tau of every particle from its current F (or J): the stress P2G
 // reads, recomputed after an upload or a change of materials.
-__global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__restrict__ ibuf) {
+__global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__restrict__ ibuf,
+                         long long b0, long long b1) {
   const SimParams &P = *d.prm;
-  const long long n = P.n;
+  const long long n = b1 < 0 ? P.n : b1;
   const bool lame = P.has_lame != 0;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+  for (long long p = b0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     const MatParams mp = d.mats[min(max(ibuf[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
     float F[9];
@@ -971,8 +972,8 @@ void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s) {
   k_return_mapping<<<d.num_sms * 8, 256, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
 }
 
-void launch_stress(const DevPtrs &d, int cur, cudaStream_t s) {
-  k_stress<<<d.num_sms * 8, 256, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+void launch_stress(const DevPtrs &d, int cur, cudaStream_t s, long long b0, long long b1) {
+  k_stress<<<d.num_sms * 8, 256, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur], b0, b1);
 }
 
 }  // namespace zsmpm

@@ -272,7 +272,8 @@ void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s);
 void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s);
 void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s);
 // vol * Kirchhoff stress of every particle from its current F (or J)
-void launch_stress(const DevPtrs &d, int cur, cudaStream_t s);
+// slots [b0, b1) (b1 < 0: every particle)
+void launch_stress(const DevPtrs &d, int cur, cudaStream_t s, long long b0 = 0, long long b1 = -1);
 
 // api.cu: the text mpm_last_error() returns on this thread
 void set_last_error(const std::string &msg);
@@ -290,7 +291,8 @@ struct IngestSrc {
   const float *x, *v, *C, *F, *J, *m, *vol, *mu, *lam;
   const int32_t *mat;
 };
-void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long n, cudaStream_t s);
+void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long b0, long long b1,
+                   cudaStream_t s);
 void launch_check_materials(const DevPtrs &d, const int32_t *mat, long long n, int n_materials,
                             cudaStream_t s);
 void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
@@ -298,7 +300,10 @@ void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, 
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
                      cudaStream_t s);
 // writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
-void launch_egest(const DevPtrs &d, int cur, float *dst, long long n, cudaStream_t s);
+struct EgestDst {
+  float *x, *v, *C, *F, *J;
+};
+void launch_egest(const DevPtrs &d, int cur, EgestDst dst, long long n, cudaStream_t s);
 void launch_egest_channel(const DevPtrs &d, int cur, int ch, float *dst, long long n,
                           cudaStream_t s);
 
