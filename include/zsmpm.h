@@ -215,6 +215,13 @@ int32_t mpm_cloth_create(mpm_ctx *ctx, const mpm_cloth_desc *desc);
 int32_t mpm_cloth_download(mpm_ctx *ctx, float *vx, float *vv, float *vC, float *ex, float *ev,
                            float *eC, float *eF, float *ed);
 
+/* ToTrackerParticles (Generation.cu:105-170): n points (x, optional v,
+ * n x 3) that join the partition and are advected in every substep's G2P by
+ * the grid velocity (Transfer.cu:1259-1285; the grid's transferred "v" also
+ * on FLIP grids), with no P2G.  One tracker set per single-scene context. */
+int32_t mpm_trackers_create(mpm_ctx *ctx, int64_t n, const float *x, const float *v);
+int32_t mpm_trackers_download(mpm_ctx *ctx, float *x, float *v);
+
 /* ToZSParticles (Generation.cpp:690-1145): host arrays -> device store.
  * NULL optional arrays take the reference defaults: v = 0, C = 0, F = I,
  * J = 1.  mu / lam are the per-particle overrides added by

@@ -563,6 +563,28 @@ template <class R> struct Sim {
     return &grid[(int64_t(gb) * 64 + cell) * kNG];
   }
 
+  // ZSGridToZSParticle for tracker points (Transfer.cu:1259-1285): the
+  // grid's "v" channel interpolated, x += v dt
+  void tracker_g2p(orc_trackers &tk, double dt) {
+    for (int64_t p = 0; p < tk.n; ++p) {
+      Stencil st;
+      stencil(tk.x + 3 * p, st);
+      double vel[3] = {0, 0, 0};
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int k = 0; k < 3; ++k) {
+            const int32_t I[3] = {st.base[0] + i, st.base[1] + j, st.base[2] + k};
+            const double W = st.w[0][i] * st.w[1][j] * st.w[2][k];
+            const R *nd = node(I);
+            for (int a = 0; a < 3; ++a) vel[a] += W * nd[1 + a];
+          }
+      for (int a = 0; a < 3; ++a) {
+        tk.v[3 * p + a] = vel[a];
+        tk.x[3 * p + a] += vel[a] * dt;
+      }
+    }
+  }
+
   // ---- codimensional cloth (FP64 only) ----
   //
   // Gram-Schmidt QR of the columns of F (Jiang et al. 2017, sec. 4): q0 =
@@ -1011,6 +1033,7 @@ template <class R> struct Sim {
       extra.push_back({sc.cloth->vx, sc.cloth->n_verts});
       extra.push_back({sc.cloth->ex, sc.cloth->n_eles});
     }
+    if (std::is_same<R, double>::value && sc.trackers) extra.push_back({sc.trackers->x, sc.trackers->n});
     int rc = build_partition<R>(sc, n, x, P, nthreads, extra);
     if (rc) return rc;
     // ZSGridFromZSPartition: zero every channel of every block
@@ -1216,11 +1239,13 @@ template <class R> struct Sim {
       if (!std::isfinite(x[3 * p]) || !std::isfinite(x[3 * p + 1]) || !std::isfinite(x[3 * p + 2]))
         bad |= 1;
     }
-    if constexpr (std::is_same<R, double>::value)
+    if constexpr (std::is_same<R, double>::value) {
       if (sc.cloth) {
         cloth_g2p(*sc.cloth, double(dt));
         cloth_return_mapping(*sc.cloth);
       }
+      if (sc.trackers) tracker_g2p(*sc.trackers, double(dt));
+    }
     return bad ? ORC_ERR_NAN : ORC_OK;
   }
 
@@ -1256,7 +1281,7 @@ int32_t run(const orc_scene *scene, int64_t n, R *x, R *v, R *C, R *F, R *J, con
   if (!scene || n < 0 || nsteps < 0) return ORC_ERR_INVALID;
   if (scene->transfer < ORC_TRANSFER_APIC || scene->transfer > ORC_TRANSFER_AFLIP)
     return ORC_ERR_INVALID;
-  if (scene->cloth && !std::is_same<R, double>::value) return ORC_ERR_INVALID;
+  if ((scene->cloth || scene->trackers) && !std::is_same<R, double>::value) return ORC_ERR_INVALID;
   for (int64_t p = 0; p < n; ++p)
     if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
 #ifdef _OPENMP

@@ -99,6 +99,15 @@ typedef struct orc_cloth {
   int32_t *inds;          /* 3 vertex indices per element (curves: the first 2) */
 } orc_cloth;
 
+/* Tracker particles (ToTrackerParticles, Generation.cu:105-170): points
+ * that join the partition and are advected by the grid velocity in G2P
+ * (Transfer.cu:1259-1285: v = sum W v_i of the grid's "v", x += v dt), with
+ * no P2G. */
+typedef struct orc_trackers {
+  int64_t n;
+  double *x, *v; /* n x 3, in/out */
+} orc_trackers;
+
 typedef struct orc_scene {
   float dx;
   float gravity[3];
@@ -115,6 +124,7 @@ typedef struct orc_scene {
   int32_t collider_autostep; /* 1: advance colliders by dt at the start of each substep */
   int32_t transfer;          /* ORC_TRANSFER_* */
   orc_cloth *cloth;          /* NULL, or one cloth stepped with the particles (FP64 only) */
+  orc_trackers *trackers;    /* NULL, or tracker points (FP64 only) */
 } orc_scene;
 
 typedef struct orc_stats {

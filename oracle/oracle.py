@@ -46,6 +46,10 @@ CLOTH_ELE = {"ex": 3, "ev": 3, "eC": 9, "eF": 9, "ed": 9, "eDmInv": 9, "em": 1, 
              "emu": 1, "elam": 1}
 
 
+class OrcTrackers(C.Structure):
+    _fields_ = [("n", C.c_int64), ("x", C.c_void_p), ("v", C.c_void_p)]
+
+
 class OrcScene(C.Structure):
     _fields_ = [("dx", C.c_float), ("gravity", C.c_float * 3), ("block_lo", C.c_int32 * 3),
                 ("block_dims", C.c_int32 * 3), ("bc_type", C.c_int32),
@@ -53,7 +57,7 @@ class OrcScene(C.Structure):
                 ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial)),
                 ("n_colliders", C.c_int32), ("colliders", C.POINTER(OrcCollider)),
                 ("collider_autostep", C.c_int32), ("transfer", C.c_int32),
-                ("cloth", C.POINTER(OrcCloth))]
+                ("cloth", C.POINTER(OrcCloth)), ("trackers", C.POINTER(OrcTrackers))]
 
 
 class OrcStats(C.Structure):
@@ -148,11 +152,15 @@ class _SceneHolder:
                           (C.c_int32 * 3)(*scene.bc_lo), (C.c_int32 * 3)(*scene.bc_hi),
                           len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)),
                           len(cols), C.cast(carr, C.POINTER(OrcCollider)), 1,
-                          int(getattr(scene, "transfer", 0)), None)
+                          int(getattr(scene, "transfer", 0)), None, None)
 
     def attach_cloth(self, cl: "OrcCloth"):
         self.cloth = cl
         self.s.cloth = C.pointer(cl)
+
+    def attach_trackers(self, tk: "OrcTrackers"):
+        self.trackers = tk
+        self.s.trackers = C.pointer(tk)
 
 
 def partition(scene, x: np.ndarray) -> dict:
@@ -263,10 +271,16 @@ def cloth_init(mesh, dx: float) -> dict:
     return state
 
 
-def run_cloth(scene, parts, mesh, state: dict, nsteps: int, dt: float | None = None):
+def run_cloth(scene, parts, mesh, state: dict, nsteps: int, dt: float | None = None,
+              trackers: np.ndarray | None = None):
     """FP64 substeps of the particles together with one cloth (state from
-    cloth_init, copied); returns (particles, cloth state, stats)."""
-    state = {k: np.array(a, copy=True) for k, a in state.items()}
+    cloth_init, copied; mesh None for none) and optional tracker points
+    (positions (n, 3)); returns (particles, cloth state, stats), the state
+    holding the trackers' "tx", "tv" when given."""
+    state = {k: np.array(a, copy=True) for k, a in (state or {}).items()}
+    if trackers is not None:
+        state["tx"] = np.ascontiguousarray(trackers, dtype=np.float64).reshape(-1, 3).copy()
+        state["tv"] = np.zeros_like(state["tx"])
     p = parts.copy(dtype=np.float64)
     for k in ("x", "v", "C", "F", "J", "m", "vol", "mu", "lam", "beta"):
         a = getattr(p, k)
@@ -274,7 +288,11 @@ def run_cloth(scene, parts, mesh, state: dict, nsteps: int, dt: float | None = N
             setattr(p, k, np.ascontiguousarray(a, dtype=np.float64))
     p.mat = np.ascontiguousarray(p.mat, dtype=np.int32)
     h = _SceneHolder(scene)
-    h.attach_cloth(_cloth_struct(mesh, state))
+    if mesh is not None:
+        h.attach_cloth(_cloth_struct(mesh, state))
+    if trackers is not None:
+        h.attach_trackers(OrcTrackers(state["tx"].shape[0], state["tx"].ctypes.data,
+                                      state["tv"].ctypes.data))
     st = OrcStats()
     rc = lib().orc_run_f64(C.byref(h.s), p.n, _ptr(p.x), _ptr(p.v), _ptr(p.C), _ptr(p.F),
                            _ptr(p.J), _ptr(p.m), _ptr(p.vol), _ptr(p.mat), _ptr(p.mu),

@@ -11,8 +11,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 # sockets this backend adds to reference nodes (documented extensions)
 EXTRA_INPUTS = {"ToZSBoundary": {"dx", "thickness", "domain_min", "domain_max"},
-                # a ToZSCloth cloth stepped with the partitioned particles
-                "ZSPartitionForZSParticles": {"ZSCloth"},
+                # a ToZSCloth cloth and ToTrackerParticles points stepped with
+                # the partitioned particles
+                "ZSPartitionForZSParticles": {"ZSCloth", "ZSTrackers"},
                 # dense level sets filled from a primitive or an analytic shape
                 "MakeZSLevelSet": {"sdf_prim", "dims", "shape", "center", "radius", "height",
                                    "extent"}}

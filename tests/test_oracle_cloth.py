@@ -381,3 +381,35 @@ def test_curve_substep_matches_numpy(oracle_mod, gamma):
     for k in ("vx", "vv", "vC", "ex", "ev", "eC", "ed", "eF"):
         np.testing.assert_allclose(out[k], ref[k], rtol=1e-9,
                                    atol=1e-8 if k in ("vC", "eC") else 1e-11, err_msg=k)
+
+
+def test_trackers_follow_free_fall(oracle_mod):
+    """Tracker points deep inside a block in free fall (uniform velocity, no
+    stress, away from the walls) see only nodes carrying that velocity: they
+    move exactly with the block; points far outside see empty nodes and stay."""
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, dt=1e-4,
+                             materials=[S.Material(S.FCR, E=5e4, nu=0.3)])
+    x = S.box_particles((0.35, 0.35, 0.35), (12, 12, 12), scene.dx, 8, 0, 0)
+    parts = S.make_particles(x, scene.dx, 8, scene.materials, np.zeros(x.shape[0], np.int32))
+    v0 = np.array([0.2, -0.4, 0.1])
+    parts.v = np.tile(v0.astype(np.float32), (parts.n, 1))
+    inner = 0.40 + 0.08 * S.uniform(1, 0, 180).reshape(-1, 3)
+    outer = np.array([[0.8, 0.8, 0.8], [0.15, 0.75, 0.2]])
+    pts = np.concatenate([inner, outer]).astype(np.float32)
+    steps = 10
+    p, ref, st = oracle_mod.run_cloth(scene, parts, None, None, steps, trackers=pts)
+    assert st["status"] == 0
+    # the scene holds gravity and the velocities in float32
+    v0 = v0.astype(np.float32).astype(np.float64)
+    g = np.array(scene.gravity, np.float32).astype(np.float64)
+    v_end = v0 + steps * scene.dt * g
+    # x_k+1 = x_k + v_k+1 dt with v_k+1 = v0 + (k+1) g dt
+    dx_end = steps * scene.dt * v0 + scene.dt ** 2 * g * steps * (steps + 1) / 2
+    np.testing.assert_allclose(ref["tv"][:-2], np.tile(v_end, (60, 1)), rtol=0, atol=1e-9)
+    np.testing.assert_allclose(ref["tx"][:-2] - pts[:-2].astype(np.float64),
+                               np.tile(dx_end, (60, 1)), rtol=0, atol=1e-9)
+    np.testing.assert_array_equal(ref["tv"][-2:], 0.0)
+    np.testing.assert_array_equal(ref["tx"][-2:], pts[-2:].astype(np.float64))
+    # massless: the particles move as without the points
+    free, _ = oracle_mod.run(scene, parts, steps, "f64")
+    np.testing.assert_array_equal(p.x, free.x)

@@ -172,9 +172,10 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], c->stream);
   };
-  const bool cloth = c->d.cloth.n_verts > 0;
+  const bool cloth = c->d.cloth.n_verts > 0, trackers = c->d.n_trackers > 0;
   mark(MPM_STAGE_SCAN);
   if (cloth) launch_cloth_mark(c->d, c->stream);  // the cloth's grid blocks
+  if (trackers) launch_tracker_mark(c->d, c->stream);
   launch_scan(c->d, c->stream);
   mark(MPM_STAGE_SCATTER);
   launch_scatter(c->d, c->stream);
@@ -195,6 +196,7 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, 1, c->stream);
   if (cloth) launch_cloth_g2p(c->d, c->stream);
+  if (trackers) launch_tracker_g2p(c->d, c->stream);
   mark(MPM_NUM_STAGES);
 }
 
@@ -1026,6 +1028,39 @@ int32_t mpm_cloth_download(mpm_ctx *c, float *vx, float *vv, float *vC, float *e
   return MPM_OK;
 }
 
+int32_t mpm_trackers_create(mpm_ctx *c, int64_t n, const float *x, const float *v) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (n <= 0 || !x) return fail(MPM_ERR_INVALID, "trackers need positions");
+  if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "trackers need a single-scene context");
+  if (c->d.n_trackers > 0) return fail(MPM_ERR_STATE, "one tracker set per context");
+  float *tx = nullptr, *tv = nullptr;
+  if ((rc = dalloc(c, &tx, (size_t)3 * n)) || (rc = dalloc(c, &tv, (size_t)3 * n))) return rc;
+  ZS_CUDA(cudaMemcpyAsync(tx, x, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  if (v)
+    ZS_CUDA(cudaMemcpyAsync(tv, v, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  else
+    ZS_CUDA(cudaMemsetAsync(tv, 0, 3 * n * sizeof(float), c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->d.tx = tx;
+  c->d.tv = tv;
+  c->d.n_trackers = n;
+  drop_graphs(c);  // the substep gains the trackers' kernels
+  c->partition_valid = false;
+  return MPM_OK;
+}
+
+int32_t mpm_trackers_download(mpm_ctx *c, float *x, float *v) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  const long long n = c->d.n_trackers;
+  if (n == 0) return fail(MPM_ERR_STATE, "no trackers in this context");
+  if (x) ZS_CUDA(cudaMemcpyAsync(x, c->d.tx, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  if (v) ZS_CUDA(cudaMemcpyAsync(v, c->d.tv, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  return MPM_OK;
+}
+
 int32_t mpm_compute_von_mises(mpm_ctx *c, int32_t by_log1p) {
   int32_t rc = check(c);
   if (rc) return rc;
@@ -1118,6 +1153,7 @@ int32_t mpm_partition(mpm_ctx *c) {
   if ((rc = push_params(c)) || (rc = prepare_partition(c))) return rc;
   enqueue_bin_if_needed(c);
   if (c->d.cloth.n_verts > 0) launch_cloth_mark(c->d, c->stream);
+  if (c->d.n_trackers > 0) launch_tracker_mark(c->d, c->stream);
   enqueue_sort(c);
   if ((rc = launch_check("partition"))) return rc;
   c->partition_valid = true;
@@ -1200,6 +1236,7 @@ int32_t mpm_g2p(mpm_ctx *c, float dt) {
   if ((rc = set_dt(c, dt))) return rc;
   launch_g2p(c->d, c->cur, 0, 0, c->stream);
   if (c->d.cloth.n_verts > 0) launch_cloth_g2p(c->d, c->stream);
+  if (c->d.n_trackers > 0) launch_tracker_g2p(c->d, c->stream);
   if ((rc = launch_check("g2p"))) return rc;
   c->cur = 1 - c->cur;
   c->partition_valid = false;

@@ -588,7 +588,62 @@ __global__ void k_cloth_g2p_elements(DevPtrs d) {
   }
 }
 
+// tracker points (ToTrackerParticles): their blocks join the partition
+__global__ void k_tracker_mark(DevPtrs d) {
+  const SceneParams &S = d.scn[0];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.n_trackers;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float *x = d.tx + 3 * i;
+    const int key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
+    if (key < 0) continue;
+    const int dd = key >> 6, dy = S.block_dims[1], dz = S.block_dims[2];
+    for (int a = -1; a <= 1; ++a)
+      for (int b = -1; b <= 1; ++b)
+        for (int c = -1; c <= 1; ++c) d.dir_flag[dd + (a * dy + b) * dz + c] = 1;
+  }
+}
+
+// tracker G2P (Transfer.cu:1259-1285): v = sum W v_i of the grid's "v"
+// channel (also on FLIP grids), x += v dt
+__global__ void k_tracker_g2p(DevPtrs d) {
+  const SceneParams &S = d.scn[0];
+  const float dt = d.prm->dt, inv_dx = S.inv_dx;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < d.n_trackers;
+       p += (long long)gridDim.x * blockDim.x) {
+    float *x = d.tx + 3 * p;
+    const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx), s2 = stencil1(x[2], inv_dx);
+    float vel[3] = {0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) {
+          const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
+          if (idx < 0) {
+            atomicOr(&d.cnt->status, ST_STENCIL);
+            continue;
+          }
+          const float W = s0.w[i] * s1.w[j] * s2.w[k];
+          const float4 g = d.grid[idx];
+          vel[0] += W * g.y;
+          vel[1] += W * g.z;
+          vel[2] += W * g.w;
+        }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      d.tv[3 * p + a] = vel[a];
+      x[a] += vel[a] * dt;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_tracker_mark(const DevPtrs &d, cudaStream_t s) {
+  k_tracker_mark<<<d.num_sms * 4, 256, 0, s>>>(d);
+}
+
+void launch_tracker_g2p(const DevPtrs &d, cudaStream_t s) {
+  k_tracker_g2p<<<d.num_sms * 4, 128, 0, s>>>(d);
+}
 
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
   k_cloth_mark<<<d.num_sms * 4, 256, 0, s>>>(d);

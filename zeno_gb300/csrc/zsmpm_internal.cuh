@@ -209,6 +209,9 @@ struct DevPtrs {
   int32_t *near_gb;        // cap_gblocks entries: the grid blocks near a collider
   float *vms;              // ComputeVonMises per particle, by upload index (0 at upload)
   ClothDev cloth;          // n_verts = 0: no cloth
+  // ToTrackerParticles: points advected by the grid velocity, no P2G
+  long long n_trackers;
+  float *tx, *tv;
   int keep_order;     // differentiable mode: G2P writes each particle to its own slot
   int planar_x;       // pbuf[0] holds positions as 3 planes of `cap` floats (binning only)
   int32_t *tile_sums;
@@ -240,6 +243,8 @@ void launch_particle_beta(const DevPtrs &d, int cur, float dt, int collider, cud
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s);
 void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s);
 void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s);
+void launch_tracker_mark(const DevPtrs &d, cudaStream_t s);
+void launch_tracker_g2p(const DevPtrs &d, cudaStream_t s);
 
 // output.cu
 void launch_von_mises(const DevPtrs &d, int cur, int by_log1p, cudaStream_t s);

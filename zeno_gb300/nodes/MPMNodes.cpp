@@ -98,6 +98,10 @@ struct ZenoParticles : IObject {
   bool cloth = false;
   mpm_cloth_desc cloth_desc{};
   std::weak_ptr<MpmContext> cloth_ctx;
+  // ToTrackerParticles: massless points carried by the grid velocity,
+  // attached to the context of the particles they are stepped with
+  bool tracker = false;
+  std::weak_ptr<MpmContext> tracker_ctx;
   std::shared_ptr<PrimitiveObject> prim;  // the source primitive, written back by
                                           // UpdatePrimitiveFromZSParticles
   std::shared_ptr<ZenoConstitutiveModel> model;
@@ -257,9 +261,29 @@ void attach_cloth(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &cl) {
   cl.ctx = ctx;
 }
 
+// ToTrackerParticles points join the particles' context once; the
+// primitive's "pos" ("vel" when present) seeds them
+void attach_trackers(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &tk) {
+  if (!tk.tracker) throw std::runtime_error("ZSTrackers: the input is not a ToTrackerParticles output");
+  if (tk.tracker_ctx.lock() == ctx) return;
+  if (tk.tracker_ctx.lock())
+    throw std::runtime_error("ZSTrackers: the trackers belong to another context");
+  auto &pos = prim_access::pos(*tk.prim);
+  if (pos.empty()) throw std::runtime_error("ZSTrackers: the primitive has no points");
+  const auto *v = prim_access::vel(*tk.prim, false);
+  check(mpm_trackers_create(ctx->h, (int64_t)pos.size(), pos[0].data(),
+                            v && v->size() == pos.size() ? (*v)[0].data() : nullptr),
+        "mpm_trackers_create");
+  tk.tracker_ctx = ctx;
+  tk.ctx = ctx;
+}
+
 // a ToZSCloth cloth used on its own as the ZSParticles of a substep gets a
 // context of its own (no particles)
 void ensure_cloth_ctx(ZenoParticles &pars) {
+  if (pars.tracker && !pars.ctx)
+    throw std::runtime_error("tracker particles carry no mass: step them through the ZSTrackers "
+                             "input with the particles that move them");
   if (!pars.cloth || pars.ctx) return;
   auto ctx = make_context(*pars.model, prim_access::pos(*pars.prim), nullptr, nullptr, 1);
   check(mpm_particles_upload(ctx->h, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -378,6 +402,31 @@ ZENDEFNODE(ToZSCloth, {
                           {},
                           {"MPM"},
                       });
+
+/// ToTrackerParticles (Generation.cu:105-187): the primitive's points as
+/// massless tracker particles that the substeps move with the grid's
+/// velocity (v = sum W v_i, x += v dt; Transfer.cu:1259-1285).  They are
+/// stepped with the particles of a ZSPartitionForZSParticles or ZSMPMSubstep
+/// (input "ZSTrackers") and written back by UpdatePrimitiveFromZSParticles.
+/// The reference's element centroids of a triangle primitive only feed its
+/// wind impulse and are not kept.
+struct ToTrackerParticles : INode {
+  void apply() override {
+    auto prim = get_input<PrimitiveObject>("prim");
+    auto out = std::make_shared<ZenoParticles>();
+    out->prim = prim;
+    out->tracker = true;
+    out->category = 4;  // ZenoParticles::tracker
+    out->n = (int64_t)prim_access::pos(*prim).size();
+    set_output("ZSParticles", out);
+  }
+};
+ZENDEFNODE(ToTrackerParticles, {
+                                   {"prim"},
+                                   {"ZSParticles"},
+                                   {},
+                                   {"MPM"},
+                               });
 
 /// ToZSParticles (Generation.cpp:690-1145): m = vol * density, F = I, C = 0.
 /// The device context is sized for the primitive: its block directory spans
@@ -511,6 +560,8 @@ struct ZSPartitionForZSParticles : INode {
     check(mpm_set_transfer(pars->ctx->h, transfer_of(*grid)), "mpm_set_transfer");
     if (has_input<ZenoParticles>("ZSCloth"))  // a cloth stepped with these particles
       attach_cloth(pars->ctx, *get_input<ZenoParticles>("ZSCloth"));
+    if (has_input<ZenoParticles>("ZSTrackers"))
+      attach_trackers(pars->ctx, *get_input<ZenoParticles>("ZSTrackers"));
     check(mpm_partition(pars->ctx->h), "mpm_partition");
     table->rebuilt = true;
     set_output("ZSPartition", table);
@@ -518,7 +569,7 @@ struct ZSPartitionForZSParticles : INode {
 };
 ZENDEFNODE(ZSPartitionForZSParticles, {
                                           {"ZSPartition", "ZSGrid", "ZSParticles", {"float", "ppb", "1"},
-                                           "ZSCloth"},
+                                           "ZSCloth", "ZSTrackers"},
                                           {"ZSPartition"},
                                           {{"enum force cache", "strategy", "force"}},
                                           {"MPM"},
@@ -948,6 +999,24 @@ ZENDEFNODE(AdjustParticleMaterial, {
 struct UpdatePrimitiveFromZSParticles : INode {
   void apply() override {
     auto pars = get_input<ZenoParticles>("ZSParticles");
+    if (pars->tracker) {  // the tracker points back into their primitive
+      auto ctx = pars->tracker_ctx.lock();
+      if (ctx && pars->prim) {
+        auto &pos = prim_access::pos(*pars->prim);
+        const int64_t n = (int64_t)pos.size();
+        std::vector<float> x(3 * n), v(3 * n);
+        check(mpm_trackers_download(ctx->h, x.data(), v.data()), "mpm_trackers_download");
+        auto &vel = *prim_access::vel(*pars->prim, true);
+        vel.resize(n);
+        for (int64_t i = 0; i < n; ++i)
+          for (int d = 0; d < 3; ++d) {
+            pos[i][d] = x[3 * i + d];
+            vel[i][d] = v[3 * i + d];
+          }
+      }
+      set_output("ZSParticles", pars);
+      return;
+    }
     if (pars->cloth) {  // the cloth's vertices back into its mesh
       auto ctx = pars->cloth_ctx.lock();
       if (ctx && pars->prim) {
@@ -1046,6 +1115,8 @@ struct ZSMPMSubstep : INode {
       attach_boundary(ctx, *get_input<ZenoBoundary>("ZSCollider"));
     if (has_input<ZenoParticles>("ZSCloth"))
       attach_cloth(ctx, *get_input<ZenoParticles>("ZSCloth"));
+    if (has_input<ZenoParticles>("ZSTrackers"))
+      attach_trackers(ctx, *get_input<ZenoParticles>("ZSTrackers"));
     // the transfer scheme of a MakeZSGrid (default APIC)
     if (has_input<ZenoGrid>("ZSGrid"))
       check(mpm_set_transfer(ctx->h, transfer_of(*get_input<ZenoGrid>("ZSGrid"))),
@@ -1064,6 +1135,7 @@ ZENDEFNODE(ZSMPMSubstep, {
                               "ZSCollider",
                               "ZSGrid",
                               "ZSCloth",
+                              "ZSTrackers",
                               "dt",
                               {"float", "gravity", "-9.8"},
                               "Accel",

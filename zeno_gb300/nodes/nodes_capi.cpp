@@ -82,7 +82,9 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       const char *ls_shape, const float *ls, const char *ls_type,
                       const char *transfer, int64_t cloth_nv, const float *cloth_x,
                       const float *cloth_v, int64_t cloth_nt, const int32_t *cloth_tris,
-                      const float *cloth_params, float *cloth_out_x, float *cloth_out_v) {
+                      const float *cloth_params, float *cloth_out_x, float *cloth_out_v,
+                      int64_t tracker_n, const float *tracker_x, float *tracker_out_x,
+                      float *tracker_out_v) {
   using namespace zeno;
   try {
     Graph g;
@@ -170,6 +172,19 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.setNodeInput("cloth", "damping_coeff", num(cloth_params[3]));
       g.markOnce("cloth");
     }
+    // optional tracker points (ToTrackerParticles), moved by the grid
+    std::shared_ptr<PrimitiveObject> tprim;
+    const bool trackers = tracker_n > 0 && tracker_x;
+    if (trackers) {
+      tprim = std::make_shared<PrimitiveObject>();
+      auto &tp = tprim->verts();
+      tp.resize(tracker_n);
+      for (int64_t i = 0; i < tracker_n; ++i)
+        for (int d = 0; d < 3; ++d) tp[i][d] = tracker_x[3 * i + d];
+      g.addNode("ToTrackerParticles", "trk");
+      g.setNodeInput("trk", "prim", tprim);
+      g.markOnce("trk");
+    }
     auto dtobj = num(dt);
     std::string last;
     if (fused) {
@@ -179,6 +194,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       if (collider) g.bindNodeInput("step", "ZSCollider", "lsb", "ZSBoundary");
       g.bindNodeInput("step", "ZSGrid", "grid", "ZSGrid");
       if (cloth) g.bindNodeInput("step", "ZSCloth", "cloth", "ZSParticles");
+      if (trackers) g.bindNodeInput("step", "ZSTrackers", "trk", "ZSParticles");
       g.setNodeInput("step", "dt", dtobj);
       g.setNodeInput("step", "gravity", num(gravity));
       g.setNodeInput("step", "substeps", inum(substeps));
@@ -190,6 +206,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("part", "ZSGrid", "grid", "ZSGrid");
       g.bindNodeInput("part", "ZSParticles", "pars", "ZSParticles");
       if (cloth) g.bindNodeInput("part", "ZSCloth", "cloth", "ZSParticles");
+      if (trackers) g.bindNodeInput("part", "ZSTrackers", "trk", "ZSParticles");
       g.addNode("ExpandZSPartition", "expand");
       g.bindNodeInput("expand", "ZSPartition", "part", "ZSPartition");
       g.addNode("ZSGridFromZSPartition", "clear");
@@ -257,6 +274,18 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
         for (int d = 0; d < 3; ++d) {
           if (cloth_out_x) cloth_out_x[3 * i + d] = cp[i][d];
           if (cloth_out_v) cloth_out_v[3 * i + d] = cv[i][d];
+        }
+    }
+    if (trackers) {  // UpdatePrimitiveFromZSParticles on the trackers
+      g.addNode("UpdatePrimitiveFromZSParticles", "tout");
+      g.setNodeInput("tout", "ZSParticles", g.getNodeOutput("trk", "ZSParticles"));
+      g.applyNodes({"tout"});
+      const auto &tp = tprim->verts();
+      const auto &tv = tprim->attrs3["vel"];
+      for (int64_t i = 0; i < tracker_n; ++i)
+        for (int d = 0; d < 3; ++d) {
+          if (tracker_out_x) tracker_out_x[3 * i + d] = tp[i][d];
+          if (tracker_out_v) tracker_out_v[3 * i + d] = tv[i][d];
         }
     }
     return 0;

@@ -78,6 +78,7 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
            "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
            "mpm_frame_begin", "mpm_frame_wait", "mpm_cloth_create", "mpm_cloth_download",
+           "mpm_trackers_create", "mpm_trackers_download",
            "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
@@ -131,6 +132,8 @@ def load(path: str = LIB_PATH):
         "mpm_particles_set_attr": ([P, C.c_char_p, P], i32),
         "mpm_compute_von_mises": ([P, i32], i32),
         "mpm_cloth_create": ([P, P], i32),
+        "mpm_trackers_create": ([P, i64, P, P], i32),
+        "mpm_trackers_download": ([P, P, P], i32),
         "mpm_cloth_download": ([P] + [P] * 8, i32),
         "mpm_frame_begin": ([P, P, P], i32),
         "mpm_frame_wait": ([P], i32),
@@ -234,6 +237,20 @@ class Context:
                          float(mesh.fa), float(mesh.dc), 1 if tris.shape[1] == 2 else 0)
         self._check(self._L.mpm_cloth_create(self.h, C.byref(desc)), "mpm_cloth_create")
         self._cloth_n = (x.shape[0], tris.shape[0])
+
+    def add_trackers(self, x, v=None):
+        """ToTrackerParticles: points advected by the grid in every substep."""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
+        self._check(self._L.mpm_trackers_create(self.h, x.shape[0], _p(x), _p(v)),
+                    "mpm_trackers_create")
+        self._n_trackers = x.shape[0]
+
+    def trackers_download(self):
+        x = np.empty((self._n_trackers, 3), np.float32)
+        v = np.empty_like(x)
+        self._check(self._L.mpm_trackers_download(self.h, _p(x), _p(v)), "mpm_trackers_download")
+        return x, v
 
     def cloth_download(self) -> dict:
         nv, ne = self._cloth_n
@@ -587,7 +604,7 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_char_p,
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
-                                C.c_int64, P, P, C.c_int64, P, P, P, P]
+                                C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -608,7 +625,7 @@ def node_descriptors() -> dict:
 
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
-                   fused=False, levelset=None, transfer="apic", cloth=None):
+                   fused=False, levelset=None, transfer="apic", cloth=None, trackers=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -618,7 +635,10 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     ypr, type.  transfer: MakeZSGrid "transfer" (apic, flip, aflip).
     cloth: optional scenes.ClothMesh run through ToZSCloth (the particles'
     model) and written back by UpdatePrimitiveFromZSParticles; the return
-    value then ends with the cloth's vertex positions and velocities."""
+    value then ends with the cloth's vertex positions and velocities.
+    trackers: optional (n, 3) points run through ToTrackerParticles and
+    written back the same way; the return value then ends with their
+    positions and velocities."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -646,15 +666,25 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
         cl["p"] = np.array([cloth.gamma, cloth.k, cloth.fa, cloth.dc], np.float32)
         cl["ox"] = np.zeros_like(cl["x"])
         cl["ov"] = np.zeros_like(cl["x"])
+    tk = {}
+    if trackers is not None:
+        tk["x"] = np.ascontiguousarray(trackers, dtype=np.float32).reshape(-1, 3)
+        tk["ox"] = np.zeros_like(tk["x"])
+        tk["ov"] = np.zeros_like(tk["x"])
     rc = L.zsn_run_graph(1 if fused else 0, n, _p(x), _p(v), dx, type.encode(),
                          plasticity.encode(), E, nu, density, ppc, bc.encode(), thickness, dt,
                          gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024, shape,
                          _p(lsp) if lsp is not None else None, lst, transfer.encode(),
                          cl["x"].shape[0] if cl else 0, _p(cl.get("x")), _p(cl.get("v")),
                          cl["t"].shape[0] if cl else 0, _p(cl.get("t")), _p(cl.get("p")),
-                         _p(cl.get("ox")), _p(cl.get("ov")))
+                         _p(cl.get("ox")), _p(cl.get("ov")),
+                         tk["x"].shape[0] if tk else 0, _p(tk.get("x")), _p(tk.get("ox")),
+                         _p(tk.get("ov")))
     if rc != 0:
         raise RuntimeError(err.value.decode())
+    out = (ox, ov, float(vmax[0]))
     if cl:
-        return ox, ov, float(vmax[0]), cl["ox"], cl["ov"]
-    return ox, ov, float(vmax[0])
+        out += (cl["ox"], cl["ov"])
+    if tk:
+        out += (tk["ox"], tk["ov"])
+    return out
