@@ -234,6 +234,18 @@ int32_t mpm_particles_upload(mpm_ctx *ctx, int64_t n, const float *x, const floa
                              const float *C, const float *F, const float *J,
                              const float *m, const float *vol, const int32_t *mat,
                              const float *mu, const float *lam);
+/* mpm_particles_upload without the final wait: the copies and the
+ * conversion are enqueued on the context's streams and the call returns, so
+ * that the upload of one context overlaps the substeps and frame copies of
+ * another.  The host arrays must stay unchanged until the next
+ * synchronising call on the context (mpm_sync, mpm_get_stats, a download);
+ * page-locked arrays keep the copies asynchronous.  A material id out of
+ * range is reported by the next mpm_sync as MPM_ERR_INVALID (the substeps
+ * clamp it meanwhile). */
+int32_t mpm_particles_upload_async(mpm_ctx *ctx, int64_t n, const float *x, const float *v,
+                                   const float *C, const float *F, const float *J,
+                                   const float *m, const float *vol, const int32_t *mat,
+                                   const float *mu, const float *lam);
 /* Upload of all scenes of a batched context: scene s owns particles
  * [scene_offsets[s], scene_offsets[s+1]) of the arrays (n_scenes + 1 offsets,
  * from 0 to n); arrays as in mpm_particles_upload. */

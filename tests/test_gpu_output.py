@@ -94,3 +94,55 @@ def test_pinned_upload_download(zsmpm_mod):
         with pytest.raises(zsmpm_mod.MPMError, match="material"):
             ctx.upload_raw(n, arrs["x"], arrs["v"], None, None, None, arrs["m"], arrs["vol"],
                            arrs["mat"])
+
+
+def _pinned_parts(parts):
+    import torch
+    n = parts.n
+    pin = lambda shape, dt=torch.float32: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    out = S.Particles(pin((n, 3)), pin((n, 3)), pin((n, 3, 3)), pin((n, 3, 3)), pin((n,)),
+                      pin((n,)), pin((n,)), pin((n,), torch.int32))
+    for k in ("x", "v", "C", "F", "J", "m", "vol", "mat"):
+        getattr(out, k)[:] = getattr(parts, k)
+    return out
+
+
+def test_async_upload_double_buffered(zsmpm_mod):
+    """Two contexts alternating mpm_particles_upload_async, a substep and
+    mpm_frame_begin (the pipelined host round trip) give, step for step, the
+    bit-exact result of the synchronous upload / substep / download."""
+    import torch
+    scene, parts = S.multi_material(dx=1.0 / 64, region_cells=(16, 8, 8))
+    n = parts.n
+    host = _pinned_parts(parts)
+    with zsmpm_mod.Context(scene, max_particles=n) as ctx:
+        ctx.upload(parts)
+        ctx.substep(scene.dt, 1)
+        ref = ctx.download(("x", "v"))
+    outs = [tuple(torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+                  for _ in range(2)) for _ in range(2)]
+    ctxs = [zsmpm_mod.Context(scene, max_particles=n) for _ in range(2)]
+    try:
+        for k in range(6):
+            c = ctxs[k & 1]
+            c.upload_async(host)
+            c.substep(scene.dt, 1)
+            c.frame_begin(*outs[k & 1])
+        for c, (x, v) in zip(ctxs, outs):
+            c.frame_wait()
+            c.sync()
+            np.testing.assert_array_equal(x, ref["x"])
+            np.testing.assert_array_equal(v, ref["v"])
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def test_async_upload_reports_bad_material(zsmpm_mod):
+    scene, parts = S.multi_material(dx=1.0 / 64, region_cells=(16, 8, 8))
+    host = _pinned_parts(parts)
+    host.mat[3] = 9
+    with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+        ctx.upload_async(host)
+        with pytest.raises(zsmpm_mod.MPMError, match="material"):
+            ctx.sync()

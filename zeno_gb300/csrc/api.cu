@@ -84,6 +84,7 @@ int32_t map_status(int bits) {
   if (bits & ST_OUT_OF_DOMAIN) return MPM_ERR_OUT_OF_DOMAIN;
   if (bits & ST_TIMEOUT) return MPM_ERR_TIMEOUT;
   if (bits & ST_STENCIL) return MPM_ERR_CFL;
+  if (bits & ST_MATERIAL) return MPM_ERR_INVALID;
   return MPM_OK;  // ST_BUCKET_OVERSIZE only affects the in-block order
 }
 
@@ -94,6 +95,7 @@ const char *status_text(int32_t st) {
     case MPM_ERR_CAPACITY: return "more grid blocks than the context's capacity";
     case MPM_ERR_TIMEOUT: return "a bounded device-side wait gave up";
     case MPM_ERR_CFL: return "a particle moved out of its block's stencil window";
+    case MPM_ERR_INVALID: return "material id out of range in an asynchronous upload";
     default: return "";
   }
 }
@@ -622,7 +624,7 @@ namespace {
 int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const float *x,
                     const float *v, const float *C, const float *F, const float *J,
                     const float *m, const float *vol, const int32_t *mat, const float *mu,
-                    const float *lam) {
+                    const float *lam, bool async = false) {
   int32_t rc = check(c);
   if (rc) return rc;
   const int ns = (int)c->scenes.size();
@@ -696,6 +698,10 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
   c->partition_valid = false;
   c->binned = false;
   c->substeps = 0;
+  if (async) {  // the verdict of the material check goes to the status word
+    if (mat && n > 0) launch_flag_materials(c->d, c->stream);
+    return launch_check("upload");
+  }
   if (mat && n > 0)
     ZS_CUDA(cudaMemcpyAsync(&c->h_cnt->bad_material, &c->d.cnt->bad_material, sizeof(int),
                             cudaMemcpyDeviceToHost, c->stream));
@@ -718,6 +724,13 @@ int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float 
                              const float *vol, const int32_t *mat, const float *mu,
                              const float *lam) {
   return upload_impl(c, nullptr, n, x, v, C, F, J, m, vol, mat, mu, lam);
+}
+
+int32_t mpm_particles_upload_async(mpm_ctx *c, int64_t n, const float *x, const float *v,
+                                   const float *C, const float *F, const float *J,
+                                   const float *m, const float *vol, const int32_t *mat,
+                                   const float *mu, const float *lam) {
+  return upload_impl(c, nullptr, n, x, v, C, F, J, m, vol, mat, mu, lam, true);
 }
 
 int32_t mpm_batch_upload(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const float *x,

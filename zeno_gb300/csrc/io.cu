@@ -109,7 +109,15 @@ __global__ void k_check_materials(const int32_t *__restrict__ mat, long long n, 
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) cnt->bad_material = 1;
 }
 
+__global__ void k_flag_materials(Counters *cnt) {
+  if (cnt->bad_material) atomicOr(&cnt->status, ST_MATERIAL);
+}
+
 }  // namespace
+
+void launch_flag_materials(const DevPtrs &d, cudaStream_t s) {
+  k_flag_materials<<<1, 1, 0, s>>>(d.cnt);
+}
 
 void launch_check_materials(const DevPtrs &d, const int32_t *mat, long long n, int n_materials,
                             cudaStream_t s) {

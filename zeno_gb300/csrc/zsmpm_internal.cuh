@@ -66,7 +66,8 @@ enum : int {
   ST_NAN = 4,
   ST_BUCKET_OVERSIZE = 8,
   ST_TIMEOUT = 16,
-  ST_STENCIL = 32
+  ST_STENCIL = 32,
+  ST_MATERIAL = 64  // a material id of an asynchronous upload out of range
 };
 
 constexpr int kMaxMaterials = 256;
@@ -300,6 +301,8 @@ void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long b0, long 
                    cudaStream_t s);
 void launch_check_materials(const DevPtrs &d, const int32_t *mat, long long n, int n_materials,
                             cudaStream_t s);
+// the material check's verdict into the status word (asynchronous upload)
+void launch_flag_materials(const DevPtrs &d, cudaStream_t s);
 void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
                        cudaStream_t s);
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,

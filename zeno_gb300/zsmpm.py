@@ -73,7 +73,7 @@ class Stats(C.Structure):
 EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destroy",
            "mpm_batch_create", "mpm_batch_upload",
            "mpm_set_stream", "mpm_set_materials", "mpm_set_boundary", "mpm_set_gravity",
-           "mpm_particles_upload", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
+           "mpm_particles_upload", "mpm_particles_upload_async", "mpm_particles_set_lame", "mpm_particles_download", "mpm_partition", "mpm_grid_clear",
            "mpm_p2g", "mpm_grid_update", "mpm_apply_boundary", "mpm_apply_walls",
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
            "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
@@ -118,6 +118,7 @@ def load(path: str = LIB_PATH):
         "mpm_clear_colliders": ([P], i32),
         "mpm_step_colliders": ([P, i32, f32], i32),
         "mpm_particles_upload": ([P, i64] + [P] * 10, i32),
+        "mpm_particles_upload_async": ([P, i64] + [P] * 10, i32),
         "mpm_particles_set_lame": ([P, P, P], i32),
         "mpm_particles_download": ([P] + [P] * 5, i32),
         "mpm_partition": ([P], i32),
@@ -368,6 +369,29 @@ class Context:
         self.n = n
         if getattr(parts, "beta", None) is not None:
             self.set_attr("beta", parts.beta)
+
+    def upload_async(self, parts):
+        """mpm_particles_upload_async: returns once the copies and the
+        conversion are enqueued; the arrays (kept referenced here) must stay
+        unchanged until the next sync, and page-locked arrays keep the copies
+        asynchronous.  A bad material id surfaces at the next sync."""
+        n = parts.n
+        x = _f32(parts.x, (n, 3))
+        v = _f32(parts.v, (n, 3))
+        Cm = _f32(parts.C, (n, 9))
+        F = _f32(parts.F, (n, 9))
+        J = _f32(parts.J, (n,))
+        m = _f32(parts.m, (n,))
+        vol = _f32(parts.vol, (n,))
+        mat = np.ascontiguousarray(parts.mat, dtype=np.int32)
+        mu = _f32(parts.mu, (n,))
+        lam = _f32(parts.lam, (n,))
+        self._keep = (x, v, Cm, F, J, m, vol, mat, mu, lam)
+        self._check(self._L.mpm_particles_upload_async(self.h, n, _p(x), _p(v), _p(Cm), _p(F),
+                                                       _p(J), _p(m), _p(vol), _p(mat), _p(mu),
+                                                       _p(lam)),
+                    "mpm_particles_upload_async")
+        self.n = n
 
     def upload_raw(self, n, x, v=None, Cm=None, F=None, J=None, m=None, vol=None, mat=None,
                    mu=None, lam=None):
