@@ -21,7 +21,7 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ZSParticleToZSGrid", "UpdateZSGrid", "ApplyBoundaryOnZSGrid", "ToZSBoundary",
          "ZSGridToZSParticle", "ZSReturnMapping", "AdjustParticleMaterial",
          "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
-         "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises", "ToZSCloth",
+         "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises", "ToZSCloth", "WriteZSParticles",
          "ToTrackerParticles"]
 
 

@@ -66,3 +66,43 @@ def test_fused_node_with_levelset_collider_equals_stage_graph(zsmpm_mod):
     a = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", **kw)
     b = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", fused=True, **kw)
     assert rel_l2(a[0], b[0]) < 1e-6 and rel_l2(a[1], b[1]) < 1e-5
+
+
+def _read_geo(path):
+    """The points of a Houdini classic ASCII .geo file with one float point
+    attribute: (positions, attribute values, attribute name)."""
+    lines = open(path).read().split("\n")
+    assert lines[0] == "PGEOMETRY V5"
+    npts = int(lines[1].split()[1])
+    assert lines[4] == "PointAttrib"
+    name = lines[5].split()[0]
+    pts = np.array([[float(t) for t in ln.replace("(", " ").replace(")", " ").split()]
+                    for ln in lines[6:6 + npts]])
+    assert lines[6 + npts] == "beginExtra" and lines[7 + npts] == "endExtra"
+    return pts[:, :3], pts[:, 4], name
+
+
+def test_write_zs_particles(zsmpm_mod, oracle_mod, tmp_path):
+    """ComputeVonMises -> WriteZSParticles after the substeps of a sand
+    column: the file holds every particle's position and von Mises stress in
+    upload order, equal to the oracle's."""
+    scene, parts = S.jelly_cube(cells=6)
+    scene.bc_type = S.BC_STICKY
+    # the node's defaults: density 1000, friction angle 35 degrees
+    scene.materials = [S.Material(S.STVK, E=5e4, nu=0.3, plasticity=S.PLASTIC_NADP,
+                                  friction_angle_deg=35.0)]
+    parts.v = (0.5 * S.normal(3, 0, parts.n * 3).reshape(-1, 3)).astype(np.float32)
+    path = str(tmp_path / "pars.geo")
+    x, v, _ = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", plasticity="nadp",
+                                       E=5e4, nu=0.3, substeps=10, bc="sticky", thickness=3,
+                                       write_path=path)
+    px, stress, name = _read_geo(path)
+    assert name == "stress" and px.shape == (parts.n, 3)
+    np.testing.assert_allclose(px, x, rtol=0, atol=1e-7)
+    ref, _ = oracle_mod.run(scene, parts, 10, "f64")
+    vms = oracle_mod.von_mises(scene, ref)  # by_log1p, the node's default
+    np.testing.assert_allclose(stress, vms, rtol=1e-4, atol=1e-5)
+    assert stress.max() > 0
+    with pytest.raises(RuntimeError, match="geo"):
+        zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", plasticity="nadp", E=5e4,
+                                 nu=0.3, substeps=1, write_path=str(tmp_path / "pars.bgeo"))

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -887,6 +888,47 @@ ZENDEFNODE(ComputeVonMises, {
                                 {{"int", "by_log1p(base10)", "1"}},
                                 {"MPM"},
                             });
+
+/// WriteZSParticles (Generation.cu:1842-1871): the particles' positions and
+/// their von Mises stress ("vms", from ComputeVonMises; 0 before it) as a
+/// point file at `path`, in upload order.  The reference writes through
+/// Partio (absent here); this writes the Houdini classic ASCII geometry
+/// format (".geo": the PGEOMETRY V5 header, a float point attribute
+/// "stress", one "x y z 1 (stress)" line per point), which Partio and
+/// Houdini read.  Other extensions are refused.
+struct WriteZSParticles : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const std::string path = get_input2<std::string>("path");
+    if (path.size() < 4 || path.compare(path.size() - 4, 4, ".geo") != 0)
+      throw std::runtime_error("WriteZSParticles: only the ASCII .geo format is written "
+                               "(path '" + path + "')");
+    if (!pars->ctx || pars->cloth || pars->tracker)
+      throw std::runtime_error("WriteZSParticles: the input holds no MPM particles");
+    const int64_t n = pars->n;
+    std::vector<float> x(3 * n), vms(n);
+    check(mpm_particles_download(pars->ctx->h, x.data(), nullptr, nullptr, nullptr, nullptr),
+          "mpm_particles_download");
+    check(mpm_particles_get_attr(pars->ctx->h, "vms", vms.data()), "mpm_particles_get_attr");
+    std::FILE *f = std::fopen(path.c_str(), "w");
+    if (!f) throw std::runtime_error("WriteZSParticles: cannot open '" + path + "'");
+    std::fprintf(f, "PGEOMETRY V5\nNPoints %lld NPrims 0\nNPointGroups 0 NPrimGroups 0\n",
+                 (long long)n);
+    std::fprintf(f, "NPointAttrib 1 NVertexAttrib 0 NPrimAttrib 0 NAttrib 0\n");
+    std::fprintf(f, "PointAttrib\nstress 1 float 0\n");
+    for (int64_t i = 0; i < n; ++i)
+      std::fprintf(f, "%.9g %.9g %.9g 1 (%.9g)\n", x[3 * i], x[3 * i + 1], x[3 * i + 2], vms[i]);
+    std::fprintf(f, "beginExtra\nendExtra\n");
+    const bool ok = std::fclose(f) == 0;
+    if (!ok) throw std::runtime_error("WriteZSParticles: writing '" + path + "' failed");
+  }
+};
+ZENDEFNODE(WriteZSParticles, {
+                                 {"ZSParticles", {"string", "path", ""}},
+                                 {},
+                                 {},
+                                 {"MPM"},
+                             });
 
 /// ComputeParticleBeta (Boundary.cu:172-516): beta for the AFLIP position
 /// update.  With a level-set ZSBoundary, particles that at x + dt v are

@@ -84,7 +84,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       const float *cloth_v, int64_t cloth_nt, const int32_t *cloth_tris,
                       const float *cloth_params, float *cloth_out_x, float *cloth_out_v,
                       int64_t tracker_n, const float *tracker_x, float *tracker_out_x,
-                      float *tracker_out_v) {
+                      float *tracker_out_v, const char *write_path) {
   using namespace zeno;
   try {
     Graph g;
@@ -259,6 +259,14 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
     g.addNode("UpdatePrimitiveFromZSParticles", "out");
     g.setNodeInput("out", "ZSParticles", g.getNodeOutput(last, "ZSParticles"));
     g.applyNodes({"out"});
+    if (write_path && write_path[0]) {  // ComputeVonMises -> WriteZSParticles
+      g.addNode("ComputeVonMises", "vms");
+      g.setNodeInput("vms", "ZSParticles", g.getNodeOutput(last, "ZSParticles"));
+      g.addNode("WriteZSParticles", "write");
+      g.bindNodeInput("write", "ZSParticles", "vms", "ZSParticles");
+      g.setNodeInput("write", "path", str(write_path));
+      g.applyNodes({"write"});
+    }
     for (int64_t i = 0; i < n; ++i)
       for (int d = 0; d < 3; ++d) {
         out_x[3 * i + d] = p[i][d];

@@ -628,7 +628,8 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_float, C.c_float, C.c_float, C.c_float, C.c_char_p,
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
-                                C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P]
+                                C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P,
+                                C.c_char_p]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -649,7 +650,8 @@ def node_descriptors() -> dict:
 
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
-                   fused=False, levelset=None, transfer="apic", cloth=None, trackers=None):
+                   fused=False, levelset=None, transfer="apic", cloth=None, trackers=None,
+                   write_path=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -662,7 +664,8 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     value then ends with the cloth's vertex positions and velocities.
     trackers: optional (n, 3) points run through ToTrackerParticles and
     written back the same way; the return value then ends with their
-    positions and velocities."""
+    positions and velocities.  write_path: after the substeps, ComputeVonMises
+    and WriteZSParticles to this .geo file."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -703,7 +706,7 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
                          cl["t"].shape[0] if cl else 0, _p(cl.get("t")), _p(cl.get("p")),
                          _p(cl.get("ox")), _p(cl.get("ov")),
                          tk["x"].shape[0] if tk else 0, _p(tk.get("x")), _p(tk.get("ox")),
-                         _p(tk.get("ov")))
+                         _p(tk.get("ov")), write_path.encode() if write_path else None)
     if rc != 0:
         raise RuntimeError(err.value.decode())
     out = (ox, ov, float(vmax[0]))
