@@ -214,6 +214,22 @@ int32_t mpm_cloth_create(mpm_ctx *ctx, const mpm_cloth_desc *desc);
  * (n_verts x 9); elements x, v (n_tris x 3), C, F, d (n_tris x 9, row-major) */
 int32_t mpm_cloth_download(mpm_ctx *ctx, float *vx, float *vv, float *vC, float *ex, float *ev,
                            float *eC, float *eF, float *ed);
+/* ConstructBendingSprings (Generation.cu:563-1001) on the context's triangle
+ * cloth, from its current state.  MPM_BENDING_VERTEX: one spring between the
+ * two vertices opposite each interior (consistently oriented) edge, k = E /
+ * (24 (1 - nu^2)) stiffness (the smaller E, nu of the two triangles), rest
+ * length their current distance; every substep's P2G then adds, while a
+ * spring is shorter than its rest length, impulses -+ thickness^2 len k
+ * (1 - len / rl) dt along it to its two vertices (p2g_vert_bending_force,
+ * Transfer.cu:357-400; thickness = the model's dx in the reference).
+ * MPM_BENDING_ANGLE: the reference's hinge force is identically zero
+ * (Transfer.cu:466-480), so the hinges are only counted.
+ * MPM_BENDING_ELEMENT fails: the reference tags those pairs as vertex
+ * springs without vertex indices (Generation.cu:779, Transfer.cu:374).
+ * *n_out (optional) receives the number of pairs / hinges. */
+enum { MPM_BENDING_VERTEX = 0, MPM_BENDING_ELEMENT = 1, MPM_BENDING_ANGLE = 2 };
+int32_t mpm_cloth_add_bending(mpm_ctx *ctx, int32_t type, float stiffness, float thickness,
+                              int64_t *n_out);
 
 /* ToTrackerParticles (Generation.cu:105-170): n points (x, optional v,
  * n x 3) that join the partition and are advected in every substep's G2P by

@@ -824,6 +824,24 @@ template <class R> struct Sim {
         for (int a = 0; a < 3; ++a) imp[3 * t[vi] + a] += coeff * (P[a * 3 + 0] * Dr[0] + P[a * 3 + 1] * Dr[1]);
       }
     }
+    // vertex bending springs (p2g_vert_bending_force, Transfer.cu:357-400):
+    // while a spring between the two vertices opposite an interior edge is
+    // shorter than its rest length, impulses -+ t^2 len k (1 - len / rl) dt
+    // along x1 - x0 on its ends, scattered with each end's weights -- the
+    // same sums as adding them to the ends' vertex impulses
+    for (int64_t s = 0; s < cl.n_springs; ++s) {
+      const int32_t a0 = cl.spring_v[2 * s], a1 = cl.spring_v[2 * s + 1];
+      const double *x0 = cl.vx + 3 * a0, *x1 = cl.vx + 3 * a1;
+      double dir[3] = {x1[0] - x0[0], x1[1] - x0[1], x1[2] - x0[2]};
+      const double len = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+      const double rl = cl.spring_rl[s];
+      if (!(len < rl) || len == 0) continue;
+      const double c = cl.thickness * cl.thickness * len * cl.spring_k[s] * (1 - len / rl) * dt / len;
+      for (int a = 0; a < 3; ++a) {
+        imp[3 * a0 + a] -= c * dir[a];
+        imp[3 * a1 + a] += c * dir[a];
+      }
+    }
     for (int64_t p = 0; p < cl.n_verts; ++p) {
       const double mass = cl.vm[p], *vp = cl.vv + 3 * p, *Cp = cl.vC + 9 * p;
       Stencil st;

@@ -97,6 +97,12 @@ typedef struct orc_cloth {
   double *ex, *ev, *eC, *eF, *ed, *eDmInv; /* elements */
   double *em, *evol, *emu, *elam;
   int32_t *inds;          /* 3 vertex indices per element (curves: the first 2) */
+  /* vertex bending springs (ConstructBendingSprings "vertex"): n_springs
+   * vertex pairs, stiffness and rest length each; thickness = the model's dx */
+  int64_t n_springs;
+  const int32_t *spring_v;
+  const double *spring_k, *spring_rl;
+  double thickness;
 } orc_cloth;
 
 /* Tracker particles (ToTrackerParticles, Generation.cu:105-170): points

@@ -38,7 +38,9 @@ class OrcCloth(C.Structure):
                 ("fa", C.c_float),
                 ("dc", C.c_float), ("n_verts", C.c_int64), ("n_eles", C.c_int64)] + \
                [(k, C.c_void_p) for k in ("vx", "vv", "vC", "vm", "ex", "ev", "eC", "eF", "ed",
-                                          "eDmInv", "em", "evol", "emu", "elam", "inds")]
+                                          "eDmInv", "em", "evol", "emu", "elam", "inds")] + \
+               [("n_springs", C.c_int64), ("spring_v", C.c_void_p), ("spring_k", C.c_void_p),
+                ("spring_rl", C.c_void_p), ("thickness", C.c_double)]
 
 
 CLOTH_VERT = {"vx": 3, "vv": 3, "vC": 9, "vm": 1}
@@ -249,7 +251,67 @@ def _cloth_struct(mesh, state) -> OrcCloth:
                   int(state["ex"].shape[0]))
     for k in list(CLOTH_VERT) + list(CLOTH_ELE) + ["inds"]:
         setattr(st, k, state[k].ctypes.data)
+    if "spring_v" in state and len(state["spring_v"]):
+        st.n_springs = int(state["spring_v"].shape[0])
+        st.spring_v = state["spring_v"].ctypes.data
+        st.spring_k = state["spring_k"].ctypes.data
+        st.spring_rl = state["spring_rl"].ctypes.data
+        st.thickness = float(state["thickness"])
     return st
+
+
+def cloth_bending(state: dict, stiffness: float, thickness: float, kind: str = "vertex") -> int:
+    """ConstructBendingSprings (Generation.cu:563-1001) on a cloth state from
+    cloth_init, in FP64, adding the springs to `state`; returns their count.
+    Interior edges are found the reference's way: each triangle registers its
+    directed edges (vi, vj) with vi < vj in its cyclic order (tri[2] -> tri[0]
+    -> tri[1] -> tri[2]), and a directed edge vi -> vj with vi > vj whose
+    reverse is registered by the neighbour becomes one pair.  "vertex": a
+    spring between the edge's two opposite vertices, k = E / (24 (1 - nu^2))
+    stiffness with the smaller E and nu of the two triangles (from their mu,
+    lam), rest length their current distance.  "angle": the hinges exist in
+    the reference but its force is identically zero (p2g_angle_bending_force,
+    Transfer.cu:466-480: the angle is declared again inside a block and the
+    outer one, 0, enters the force), so nothing is added.  "element" pairs are
+    tagged as vertex springs without the vertex indices those read
+    (Generation.cu:779, Transfer.cu:374): undefined, refused."""
+    if kind == "element":
+        raise ValueError("element bending springs are undefined in the reference")
+    if kind not in ("vertex", "angle"):
+        raise ValueError(f"unknown bending spring type {kind!r}")
+    tris = np.asarray(state["inds"], dtype=np.int64)
+    mu, lam = np.asarray(state["emu"]), np.asarray(state["elam"])
+    E = mu * (3 * lam + 2 * mu) / (lam + mu)
+    nu = lam / (2 * (lam + mu))
+    edge_ele = {}
+    for e, t in enumerate(tris):
+        vi = int(t[2])
+        for vj in t:
+            vj = int(vj)
+            if vi < vj:
+                edge_ele[(vi, vj)] = e
+            vi = vj
+    pairs, ks = [], []
+    for e, t in enumerate(tris):
+        vi, vj = int(t[1]), int(t[2])
+        for vk in t:
+            vk = int(vk)
+            if vi > vj and (vj, vi) in edge_ele:
+                ne = edge_ele[(vj, vi)]
+                other = [int(w) for w in tris[ne] if w != vi and w != vj][0]
+                pairs.append((other, vk))
+                ks.append(min(E[e], E[ne]) / (24 * (1 - min(nu[e], nu[ne]) ** 2)) * stiffness)
+            vi, vj = vj, vk
+    if kind == "angle":
+        return len(pairs)
+    sv = np.array(pairs, dtype=np.int32).reshape(-1, 2)
+    x = np.asarray(state["vx"])
+    state["spring_v"] = np.ascontiguousarray(sv)
+    state["spring_k"] = np.array(ks, dtype=np.float64)
+    state["spring_rl"] = (np.linalg.norm(x[sv[:, 1]] - x[sv[:, 0]], axis=1) if len(sv)
+                          else np.zeros(0))
+    state["thickness"] = np.float64(thickness)
+    return len(pairs)
 
 
 def cloth_init(mesh, dx: float) -> dict:

@@ -22,6 +22,7 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ZSGridToZSParticle", "ZSReturnMapping", "AdjustParticleMaterial",
          "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
          "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises", "ToZSCloth", "WriteZSParticles",
+         "ConstructBendingSprings",
          "ToTrackerParticles"]
 
 

@@ -162,3 +162,80 @@ def test_curves_match_oracle(zsmpm_mod, oracle_mod, gamma, tr):
     # the frame columns d2, d3 integrate C every substep: FP32 drift of a few
     # 1e-7 per substep
     assert rel_l2(out["eF"], ref["eF"].reshape(-1, 9)) < 5e-5
+
+
+def _contracting_sheet(model=S.FCR):
+    mesh = S.cloth_sheet((0.5, 0.55, 0.5), 0.3, 12, jitter=0.3, seed=5, model=model, E=3e4,
+                         nu=0.3, density=500.0, gamma=50.0, k=800.0, fa=30.0, dc=0.05)
+    c = np.array([0.5, 0.55, 0.5])
+    mesh.v = (-1.5 * (mesh.x - c) + [0.0, -0.2, 0.0]).astype(np.float32)
+    return mesh
+
+
+def _gpu_bending(zsmpm, scene, mesh, steps, stiffness, kind="vertex"):
+    with zsmpm.Context(scene, max_particles=1) as ctx:
+        ctx.upload(_empty())
+        ctx.add_cloth(mesh)
+        n = ctx.add_cloth_bending(stiffness, kind) if kind else 0
+        ctx.substep(scene.dt, steps)
+        st = ctx.sync() or ctx.stats()
+        out = ctx.cloth_download()
+    return n, out, st
+
+
+@pytest.mark.parametrize("tr", [S.TRANSFER_APIC, S.TRANSFER_AFLIP])
+def test_bending_springs_match_oracle(zsmpm_mod, oracle_mod, tr):
+    """ConstructBendingSprings "vertex" on a contracting sheet: the springs
+    between the vertices opposite each interior edge push back; against the
+    oracle, and the springs change the motion."""
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    scene.transfer = tr
+    mesh = _contracting_sheet()
+    # stiffness 300 changes the motion by a few percent; much stiffer springs
+    # make the sheet ill-conditioned (a 1e-7 perturbation grows 100-fold)
+    steps, stiff = (30 if tr == S.TRANSFER_APIC else 10), 300.0
+    n, out, st = _gpu_bending(zsmpm_mod, scene, mesh, steps, stiff)
+    ref0 = oracle_mod.cloth_init(mesh, scene.dx)
+    assert n == oracle_mod.cloth_bending(ref0, stiff, scene.dx) > 0
+    _, ref, rst = oracle_mod.run_cloth(scene, _empty(), mesh, ref0, steps)
+    assert st["status"] == 0 and rst["status"] == 0
+    assert rel_l2(out["vx"], ref["vx"]) < 1e-6
+    assert rel_l2(out["vv"], ref["vv"]) < 1e-4
+    _, free, _ = _gpu_bending(zsmpm_mod, scene, mesh, steps, stiff, kind=None)
+    assert rel_l2(out["vv"], free["vv"]) > 3e-3
+
+
+def test_bending_angle_and_element(zsmpm_mod):
+    """"angle" hinges add nothing (the reference's hinge force is identically
+    zero); "element" is refused."""
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    mesh = _contracting_sheet()
+    n, out, _ = _gpu_bending(zsmpm_mod, scene, mesh, 20, 1e5, kind="angle")
+    _, free, _ = _gpu_bending(zsmpm_mod, scene, mesh, 20, 1e5, kind=None)
+    assert n > 0
+    assert rel_l2(out["vv"], free["vv"]) < 1e-6  # float atomics: equal up to summation order
+    with pytest.raises(zsmpm_mod.MPMError, match="undefined"):
+        _gpu_bending(zsmpm_mod, scene, mesh, 1, 1e5, kind="element")
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_node_graph_bending(zsmpm_mod, oracle_mod, fused):
+    """ToZSCloth -> ConstructBendingSprings (vertex) into the ZSBending input
+    with the cloth as ZSCloth, against the oracle."""
+    scene, parts = S.jelly_cube(cells=8)
+    scene.bc_type = S.BC_STICKY
+    scene.materials = [S.Material(S.FCR, E=5e4, nu=0.3)]
+    mesh = S.cloth_sheet((0.475, 0.5, 0.475), 0.3, 10, jitter=0.2, seed=4, model=S.FCR, E=5e4,
+                         nu=0.3, density=1000.0, gamma=50.0, k=800.0, fa=30.0, dc=0.02)
+    c = mesh.x.mean(axis=0)
+    mesh.v = (-1.5 * (mesh.x - c) + [0.0, -1.0, 0.0]).astype(np.float32)
+    steps, stiff = 30, 300.0
+    x, v, _, cx, cv = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", E=5e4, nu=0.3,
+                                               substeps=steps, bc="sticky", thickness=3,
+                                               fused=fused, cloth=mesh, bending=("vertex", stiff))
+    ref0 = oracle_mod.cloth_init(mesh, scene.dx)
+    oracle_mod.cloth_bending(ref0, stiff, scene.dx)
+    p, ref, st = oracle_mod.run_cloth(scene, parts, mesh, ref0, steps)
+    assert st["status"] == 0
+    assert rel_l2(cx, ref["vx"]) < 1e-6 and rel_l2(cv, ref["vv"]) < 1e-4
+    assert rel_l2(x, p.x) < 1e-6 and rel_l2(v, p.v) < 1e-4

@@ -83,26 +83,24 @@ def _read_geo(path):
 
 
 def test_write_zs_particles(zsmpm_mod, oracle_mod, tmp_path):
-    """ComputeVonMises -> WriteZSParticles after the substeps of a sand
-    column: the file holds every particle's position and von Mises stress in
-    upload order, equal to the oracle's."""
+    """ComputeVonMises -> WriteZSParticles after the substeps of a thrown
+    StVK-Hencky block: the file holds every particle's position and von Mises
+    stress in upload order, equal to the oracle's."""
     scene, parts = S.jelly_cube(cells=6)
     scene.bc_type = S.BC_STICKY
-    # the node's defaults: density 1000, friction angle 35 degrees
-    scene.materials = [S.Material(S.STVK, E=5e4, nu=0.3, plasticity=S.PLASTIC_NADP,
-                                  friction_angle_deg=35.0)]
+    scene.materials = [S.Material(S.STVK, E=5e4, nu=0.3)]  # density 1000, the node's default
     parts.v = (0.5 * S.normal(3, 0, parts.n * 3).reshape(-1, 3)).astype(np.float32)
     path = str(tmp_path / "pars.geo")
-    x, v, _ = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", plasticity="nadp",
-                                       E=5e4, nu=0.3, substeps=10, bc="sticky", thickness=3,
-                                       write_path=path)
+    x, v, _ = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", E=5e4, nu=0.3,
+                                       substeps=10, bc="sticky", thickness=3, write_path=path)
     px, stress, name = _read_geo(path)
     assert name == "stress" and px.shape == (parts.n, 3)
     np.testing.assert_allclose(px, x, rtol=0, atol=1e-7)
     ref, _ = oracle_mod.run(scene, parts, 10, "f64")
+    assert rel_l2(x, ref.x) < 1e-6
     vms = oracle_mod.von_mises(scene, ref)  # by_log1p, the node's default
-    np.testing.assert_allclose(stress, vms, rtol=1e-4, atol=1e-5)
-    assert stress.max() > 0
+    assert vms.min() > 0.5  # stressed everywhere: log10(vms + 1) of a few hundred Pa
+    np.testing.assert_allclose(stress, vms, rtol=1e-3, atol=1e-4)
     with pytest.raises(RuntimeError, match="geo"):
-        zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", plasticity="nadp", E=5e4,
-                                 nu=0.3, substeps=1, write_path=str(tmp_path / "pars.bgeo"))
+        zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", E=5e4, nu=0.3, substeps=1,
+                                 write_path=str(tmp_path / "pars.bgeo"))

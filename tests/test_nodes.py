@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 EXTRA_INPUTS = {"ToZSBoundary": {"dx", "thickness", "domain_min", "domain_max"},
                 # a ToZSCloth cloth and ToTrackerParticles points stepped with
                 # the partitioned particles
-                "ZSPartitionForZSParticles": {"ZSCloth", "ZSTrackers"},
+                "ZSPartitionForZSParticles": {"ZSCloth", "ZSTrackers", "ZSBending"},
                 # dense level sets filled from a primitive or an analytic shape
                 "MakeZSLevelSet": {"sdf_prim", "dims", "shape", "center", "radius", "height",
                                    "extent"}}

@@ -131,7 +131,8 @@ def _spline(xp, dx):
 
 
 def _numpy_substep(mesh, st, dx, dt, g):
-    s = {k: np.array(a, dtype=np.float64 if k != "inds" else np.int32) for k, a in st.items()}
+    s = {k: np.array(a, dtype=np.int32 if k in ("inds", "spring_v") else np.float64)
+         for k, a in st.items()}
     grid = {}
 
     def add(I, m, mv):
@@ -164,6 +165,18 @@ def _numpy_substep(mesh, st, dx, dt, g):
     for p in range(len(s["vx"])):
         for I, W, xixp, _ in _spline(s["vx"][p], dx):
             add(I, W * s["vm"][p], W * (s["vm"][p] * (s["vv"][p] + s["vC"][p].reshape(3, 3) @ xixp) + imp[p]))
+    # vertex bending springs, scattered with each end's own weights as the
+    # reference does (p2g_vert_bending_force)
+    for (a0, a1), kk, rl in zip(s.get("spring_v", []), s.get("spring_k", []),
+                                s.get("spring_rl", [])):
+        dv = s["vx"][a1] - s["vx"][a0]
+        ln = np.linalg.norm(dv)
+        if ln < rl:
+            f = s["thickness"] ** 2 * ln * kk * (1 - ln / rl) * dt * dv / ln
+            for I, W, _, _ in _spline(s["vx"][a0], dx):
+                add(I, 0.0, -W * f)
+            for I, W, _, _ in _spline(s["vx"][a1], dx):
+                add(I, 0.0, W * f)
     gv = {I: e[1:] / e[0] + np.asarray(g) * dt for I, e in grid.items()}
     Dinv = 4 / dx ** 2
 
@@ -413,3 +426,57 @@ def test_trackers_follow_free_fall(oracle_mod):
     # massless: the particles move as without the points
     free, _ = oracle_mod.run(scene, parts, steps, "f64")
     np.testing.assert_array_equal(p.x, free.x)
+
+
+# ---- bending springs (ConstructBendingSprings, p2g_vert_bending_force) ----
+
+def test_bending_springs_construction(oracle_mod):
+    """Two triangles sharing the edge 1-2 (consistently oriented) make one
+    spring between the opposite vertices 0 and 3 with k = E / (24 (1 - nu^2))
+    stiffness; on a sheet, one spring per interior edge."""
+    mesh = S.cloth_sheet((0.5, 0.5, 0.5), 0.1, 1, jitter=0.0, seed=0, E=3e4, nu=0.3)
+    mesh.x = np.array([[0.5, 0.5, 0.5], [0.55, 0.5, 0.5], [0.5, 0.5, 0.55], [0.56, 0.5, 0.56]],
+                      np.float32)
+    mesh.tris = np.array([[0, 1, 2], [2, 1, 3]], np.int32)
+    mesh.v = None
+    st = oracle_mod.cloth_init(mesh, 1.0 / 64)
+    assert oracle_mod.cloth_bending(st, 0.5, 1.0 / 64) == 1
+    assert sorted(st["spring_v"][0].tolist()) == [0, 3]
+    np.testing.assert_allclose(st["spring_k"][0], 3e4 / (24 * (1 - 0.09)) * 0.5, rtol=1e-6)
+    np.testing.assert_allclose(st["spring_rl"][0], np.linalg.norm(mesh.x[3] - mesh.x[0]), rtol=1e-7)
+    assert oracle_mod.cloth_bending(dict(st), 0.5, 1.0 / 64, "angle") == 1
+    with pytest.raises(ValueError, match="undefined"):
+        oracle_mod.cloth_bending(dict(st), 0.5, 1.0 / 64, "element")
+    sheet = S.cloth_sheet((0.5, 0.5, 0.5), 0.2, 6, jitter=0.2, seed=2)
+    st = oracle_mod.cloth_init(sheet, 1.0 / 64)
+    edges = {}
+    for t in sheet.tris:
+        for a, b in ((t[0], t[1]), (t[1], t[2]), (t[2], t[0])):
+            key = (min(a, b), max(a, b))
+            edges[key] = edges.get(key, 0) + 1
+    interior = sum(1 for c in edges.values() if c == 2)
+    assert oracle_mod.cloth_bending(st, 1.0, 1.0 / 64) == interior > 0
+
+
+def test_bending_springs_substep_matches_numpy(oracle_mod):
+    """One substep of a shrunken sheet (every spring shorter than its rest
+    length) against the numpy restatement, and the springs change it."""
+    scene = S.Scene.unit_box(1.0 / 32, bc_type=S.BC_NONE, materials=[S.Material()])
+    mesh = S.cloth_sheet((0.5, 0.5, 0.5), 0.15, 3, jitter=0.3, seed=1, model=S.FCR, E=5e4,
+                         gamma=50.0, k=800.0, fa=25.0, dc=0.05)
+    st = oracle_mod.cloth_init(mesh, scene.dx)
+    n = oracle_mod.cloth_bending(st, 2e6, scene.dx)
+    assert n > 0
+    c = st["vx"].mean(axis=0)
+    st["vx"][:] = c + 0.9 * (st["vx"] - c)
+    st["vv"][:] = 0.2 * (S.uniform(3, 0, st["vv"].size).reshape(-1, 3) - 0.5)
+    _, out, stats = oracle_mod.run_cloth(scene, _empty(), mesh, st, 1)
+    assert stats["status"] == 0
+    ref = _numpy_substep(mesh, st, scene.dx, scene.dt, np.array(scene.gravity, np.float32))
+    for k in ("vx", "vv", "vC"):
+        # the stiff springs make C large: cancellation bound relative to it
+        np.testing.assert_allclose(out[k], ref[k], rtol=1e-8,
+                                   atol=1e-10 * np.abs(ref[k]).max() + 1e-12, err_msg=k)
+    plain = {k: a for k, a in st.items() if not k.startswith("spring") and k != "thickness"}
+    _, free, _ = oracle_mod.run_cloth(scene, _empty(), mesh, plain, 1)
+    assert np.abs(free["vv"] - out["vv"]).max() > 1e-3 * np.abs(out["vv"]).max()

@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "zsmpm_internal.cuh"
@@ -1018,6 +1019,111 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
   cl = nc;
   drop_graphs(c);  // the substep gains the cloth's kernels
   c->partition_valid = false;
+  return MPM_OK;
+}
+
+int32_t mpm_cloth_add_bending(mpm_ctx *c, int32_t type, float stiffness, float thickness,
+                              int64_t *n_out) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  ClothDev &cl = c->d.cloth;
+  if (cl.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
+  if (cl.kind != MPM_MESH_SURFACE) return fail(MPM_ERR_INVALID, "bending springs need a triangle mesh");
+  if (type == MPM_BENDING_ELEMENT)
+    return fail(MPM_ERR_INVALID,
+                "element bending springs are undefined in the reference (the pairs are tagged "
+                "as vertex springs without vertex indices)");
+  if (type != MPM_BENDING_VERTEX && type != MPM_BENDING_ANGLE)
+    return fail(MPM_ERR_INVALID, "unknown bending spring type");
+  if (cl.n_springs > 0) return fail(MPM_ERR_STATE, "the cloth already has bending springs");
+  if (!std::isfinite(stiffness) || !std::isfinite(thickness))
+    return fail(MPM_ERR_INVALID, "non-finite bending stiffness or thickness");
+  // ConstructBendingSprings (Generation.cu:563-1001) on the host from the
+  // cloth's current state: triangles register their directed edges (vi, vj)
+  // with vi < vj in cyclic order (tri[2] -> tri[0] -> tri[1] -> tri[2]); an
+  // edge vi -> vj with vi > vj whose reverse was registered joins the two
+  // triangles, and the vertices opposite the edge form one pair
+  const long long nv = cl.n_verts, ne = cl.n_eles;
+  std::vector<int32_t> inds(3 * ne);
+  std::vector<float> vx(3 * nv), emu(ne), elam(ne);
+  ZS_CUDA(cudaMemcpyAsync(inds.data(), cl.inds, inds.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(vx.data(), cl.vx, vx.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(emu.data(), cl.emu, ne * 4, cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(elam.data(), cl.elam, ne * 4, cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  std::unordered_map<uint64_t, int32_t> edge_ele;
+  edge_ele.reserve(3 * ne);
+  auto key = [](int32_t a, int32_t b) { return (uint64_t(uint32_t(a)) << 32) | uint32_t(b); };
+  for (long long e = 0; e < ne; ++e) {
+    const int32_t *t = &inds[3 * e];
+    int32_t vi = t[2];
+    for (int v = 0; v < 3; ++v) {
+      const int32_t vj = t[v];
+      if (vi < vj) edge_ele[key(vi, vj)] = (int32_t)e;
+      vi = vj;
+    }
+  }
+  // E, nu from mu, lam: E = mu (3 lam + 2 mu) / (lam + mu), nu = lam / (2 (lam + mu))
+  auto E_of = [&](long long e) {
+    const double mu = emu[e], lam = elam[e];
+    return mu * (3 * lam + 2 * mu) / (lam + mu);
+  };
+  auto nu_of = [&](long long e) {
+    const double mu = emu[e], lam = elam[e];
+    return lam / (2 * (lam + mu));
+  };
+  std::vector<int32_t> sv;
+  std::vector<float> sk, srl;
+  long long hinges = 0;
+  for (long long e = 0; e < ne; ++e) {
+    const int32_t *t = &inds[3 * e];
+    int32_t vi = t[1], vj = t[2];
+    for (int v = 0; v < 3; ++v) {
+      const int32_t vk = t[v];
+      if (vi > vj) {
+        auto it = edge_ele.find(key(vj, vi));
+        if (it != edge_ele.end()) {
+          const int32_t nb = it->second;
+          int32_t other = -1;
+          for (int q = 0; q < 3; ++q)
+            if (inds[3 * nb + q] != vi && inds[3 * nb + q] != vj) {
+              other = inds[3 * nb + q];
+              break;
+            }
+          ++hinges;
+          if (type == MPM_BENDING_VERTEX && other >= 0) {
+            const double Em = std::min(E_of(e), E_of(nb)), num = std::min(nu_of(e), nu_of(nb));
+            sv.push_back(other);
+            sv.push_back(vk);
+            sk.push_back(float(Em / (24.0 * (1.0 - num * num)) * stiffness));
+            double l2 = 0;
+            for (int a = 0; a < 3; ++a) {
+              const double dd = double(vx[3 * vk + a]) - double(vx[3 * other + a]);
+              l2 += dd * dd;
+            }
+            srl.push_back(float(std::sqrt(l2)));
+          }
+        }
+      }
+      vi = vj;
+      vj = vk;
+    }
+  }
+  // "angle": the reference's hinge force is identically zero (its angle is
+  // declared again inside a block, Transfer.cu:466-480, and the outer one,
+  // 0, enters the force), so the hinges are counted and nothing is added
+  if (n_out) *n_out = hinges;
+  const long long ns = (long long)sk.size();
+  if (ns == 0) return MPM_OK;
+  if ((rc = dalloc(c, &cl.sv, (size_t)2 * ns)) || (rc = dalloc(c, &cl.sk, (size_t)ns)) ||
+      (rc = dalloc(c, &cl.srl, (size_t)ns)))
+    return rc;
+  ZS_CUDA(cudaMemcpy(cl.sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice));
+  ZS_CUDA(cudaMemcpy(cl.sk, sk.data(), sk.size() * 4, cudaMemcpyHostToDevice));
+  ZS_CUDA(cudaMemcpy(cl.srl, srl.data(), srl.size() * 4, cudaMemcpyHostToDevice));
+  cl.thickness = thickness;
+  cl.n_springs = ns;
+  drop_graphs(c);  // the substep gains the springs' kernel
   return MPM_OK;
 }
 

@@ -361,6 +361,32 @@ __global__ void k_cloth_p2g_verts(DevPtrs d) {
   }
 }
 
+// vertex bending springs (p2g_vert_bending_force, Transfer.cu:357-400): a
+// spring shorter than its rest length pushes its two vertices apart with
+// impulses -+ t^2 len k (1 - len / rl) dt along x1 - x0.  The reference
+// scatters each with its vertex's weights into the grid's "v" (vstar on FLIP
+// grids); adding it to the vertex's impulse, which the vertex P2G scatters
+// the same way, gives the same sums.
+__global__ void k_cloth_bending(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const float dt = d.prm->dt, t2 = cl.thickness * cl.thickness;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < cl.n_springs;
+       s += (long long)gridDim.x * blockDim.x) {
+    const int a0 = cl.sv[2 * s], a1 = cl.sv[2 * s + 1];
+    const float dv[3] = {cl.vx[3 * a1] - cl.vx[3 * a0], cl.vx[3 * a1 + 1] - cl.vx[3 * a0 + 1],
+                         cl.vx[3 * a1 + 2] - cl.vx[3 * a0 + 2]};
+    const float len = sqrtf(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    const float rl = cl.srl[s];
+    if (!(len < rl) || len == 0.0f) continue;
+    const float c = t2 * len * cl.sk[s] * (1.0f - len / rl) * dt / len;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicAdd(&cl.imp[3 * a0 + a], -c * dv[a]);
+      atomicAdd(&cl.imp[3 * a1 + a], c * dv[a]);
+    }
+  }
+}
+
 // sum W v, sum W vstar and the damped affine velocity (from v, or vstar on
 // FLIP grids) at x
 __device__ __forceinline__ void cloth_gather(const DevPtrs &d, const SceneParams &S, const float *x,
@@ -651,6 +677,7 @@ void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
 
 void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
   cudaMemsetAsync(d.cloth.imp, 0, (size_t)d.cloth.n_verts * 3 * sizeof(float), s);
+  if (d.cloth.n_springs > 0) k_cloth_bending<<<d.num_sms * 4, 128, 0, s>>>(d);
   k_cloth_p2g_elements<<<d.num_sms * 4, 128, 0, s>>>(d);
   k_cloth_p2g_verts<<<d.num_sms * 4, 128, 0, s>>>(d);
 }

@@ -163,6 +163,12 @@ struct ClothDev {
   float *vx, *vv, *vC, *vm, *imp;
   float *ex, *ev, *eC, *eF, *ed, *eDmInv, *em, *evol, *emu, *elam;
   int32_t *inds;
+  // vertex bending springs (ConstructBendingSprings "vertex"): vertex pairs,
+  // stiffness, rest length; thickness = the model's dx
+  long long n_springs;
+  int32_t *sv;
+  float *sk, *srl;
+  float thickness;
 };
 
 // One scene of a context: its grid spacing, its slice of the concatenated

@@ -103,6 +103,13 @@ struct ZenoParticles : IObject {
   // attached to the context of the particles they are stepped with
   bool tracker = false;
   std::weak_ptr<MpmContext> tracker_ctx;
+  // ConstructBendingSprings: springs over the vertices of the ToZSCloth cloth
+  // `surf`, added to the context that steps that cloth
+  bool bending = false;
+  int32_t bending_type = MPM_BENDING_VERTEX;
+  float bending_stiffness = 0.0f;
+  std::shared_ptr<ZenoParticles> surf;
+  std::weak_ptr<MpmContext> bending_ctx;
   std::shared_ptr<PrimitiveObject> prim;  // the source primitive, written back by
                                           // UpdatePrimitiveFromZSParticles
   std::shared_ptr<ZenoConstitutiveModel> model;
@@ -279,12 +286,33 @@ void attach_trackers(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &tk) 
   tk.ctx = ctx;
 }
 
+// ConstructBendingSprings springs join the context of their cloth once
+void attach_bending(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &bs) {
+  if (!bs.bending || !bs.surf)
+    throw std::runtime_error("ZSBending: the input is not a ConstructBendingSprings output");
+  if (bs.bending_ctx.lock() == ctx) return;
+  if (bs.bending_ctx.lock())
+    throw std::runtime_error("ZSBending: the springs belong to another context");
+  if (bs.surf->cloth_ctx.lock() != ctx)
+    throw std::runtime_error("ZSBending: the springs' cloth is not stepped with these particles "
+                             "(pass it as ZSCloth too)");
+  const float thickness = bs.surf->model ? bs.surf->model->dx : ctx->dx;
+  int64_t n = 0;
+  check(mpm_cloth_add_bending(ctx->h, bs.bending_type, bs.bending_stiffness, thickness, &n),
+        "mpm_cloth_add_bending");
+  bs.bending_ctx = ctx;
+  bs.n = n;
+}
+
 // a ToZSCloth cloth used on its own as the ZSParticles of a substep gets a
 // context of its own (no particles)
 void ensure_cloth_ctx(ZenoParticles &pars) {
   if (pars.tracker && !pars.ctx)
     throw std::runtime_error("tracker particles carry no mass: step them through the ZSTrackers "
                              "input with the particles that move them");
+  if (pars.bending && !pars.ctx)
+    throw std::runtime_error("bending springs are stepped through the ZSBending input, with "
+                             "their cloth as ZSCloth");
   if (!pars.cloth || pars.ctx) return;
   auto ctx = make_context(*pars.model, prim_access::pos(*pars.prim), nullptr, nullptr, 1);
   check(mpm_particles_upload(ctx->h, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -403,6 +431,45 @@ ZENDEFNODE(ToZSCloth, {
                           {},
                           {"MPM"},
                       });
+
+/// ConstructBendingSprings (Generation.cu:563-1001) on a ToZSCloth cloth:
+/// "vertex" springs between the vertices opposite each interior edge (k =
+/// E / (24 (1 - nu^2)) bending_stiffness, rest length at attachment), pushing
+/// them apart while compressed; "angle" hinges, whose force is identically
+/// zero in the reference (Transfer.cu:466-480); "element" (the reference's
+/// default) is undefined there (its pairs are tagged as vertex springs
+/// without vertex indices) and fails when attached.  The springs join the
+/// substep through the ZSBending input of ZSPartitionForZSParticles or
+/// ZSMPMSubstep, with their cloth as ZSCloth.
+struct ConstructBendingSprings : INode {
+  void apply() override {
+    auto surf = get_input<ZenoParticles>("ZSSurfPrim");
+    if (!surf->cloth || surf->cloth_desc.kind != MPM_MESH_SURFACE)
+      throw std::runtime_error("ConstructBendingSprings: ZSSurfPrim is not a ToZSCloth surface");
+    const std::string type = get_param<std::string>("type");
+    auto out = std::make_shared<ZenoParticles>();
+    out->bending = true;
+    if (type == "vertex")
+      out->bending_type = MPM_BENDING_VERTEX;
+    else if (type == "element")
+      out->bending_type = MPM_BENDING_ELEMENT;
+    else if (type == "angle")
+      out->bending_type = MPM_BENDING_ANGLE;
+    else
+      throw std::runtime_error("ConstructBendingSprings: unknown type [" + type + "]");
+    out->bending_stiffness = get_input2<float>("bending_stiffness");
+    out->surf = surf;
+    out->model = surf->model;
+    out->category = out->bending_type == MPM_BENDING_ANGLE ? 7 : 5;  // bending / vert_bending_spring
+    set_output("ZSSpringPrim", out);
+  }
+};
+ZENDEFNODE(ConstructBendingSprings, {
+                                        {"ZSSurfPrim", {"float", "bending_stiffness", "0.01"}},
+                                        {"ZSSpringPrim"},
+                                        {{"enum vertex element angle", "type", "element"}},
+                                        {"MPM"},
+                                    });
 
 /// ToTrackerParticles (Generation.cu:105-187): the primitive's points as
 /// massless tracker particles that the substeps move with the grid's
@@ -563,6 +630,8 @@ struct ZSPartitionForZSParticles : INode {
       attach_cloth(pars->ctx, *get_input<ZenoParticles>("ZSCloth"));
     if (has_input<ZenoParticles>("ZSTrackers"))
       attach_trackers(pars->ctx, *get_input<ZenoParticles>("ZSTrackers"));
+    if (has_input<ZenoParticles>("ZSBending"))
+      attach_bending(pars->ctx, *get_input<ZenoParticles>("ZSBending"));
     check(mpm_partition(pars->ctx->h), "mpm_partition");
     table->rebuilt = true;
     set_output("ZSPartition", table);
@@ -570,7 +639,7 @@ struct ZSPartitionForZSParticles : INode {
 };
 ZENDEFNODE(ZSPartitionForZSParticles, {
                                           {"ZSPartition", "ZSGrid", "ZSParticles", {"float", "ppb", "1"},
-                                           "ZSCloth", "ZSTrackers"},
+                                           "ZSCloth", "ZSTrackers", "ZSBending"},
                                           {"ZSPartition"},
                                           {{"enum force cache", "strategy", "force"}},
                                           {"MPM"},
@@ -1159,6 +1228,8 @@ struct ZSMPMSubstep : INode {
       attach_cloth(ctx, *get_input<ZenoParticles>("ZSCloth"));
     if (has_input<ZenoParticles>("ZSTrackers"))
       attach_trackers(ctx, *get_input<ZenoParticles>("ZSTrackers"));
+    if (has_input<ZenoParticles>("ZSBending"))
+      attach_bending(ctx, *get_input<ZenoParticles>("ZSBending"));
     // the transfer scheme of a MakeZSGrid (default APIC)
     if (has_input<ZenoGrid>("ZSGrid"))
       check(mpm_set_transfer(ctx->h, transfer_of(*get_input<ZenoGrid>("ZSGrid"))),
@@ -1178,6 +1249,7 @@ ZENDEFNODE(ZSMPMSubstep, {
                               "ZSGrid",
                               "ZSCloth",
                               "ZSTrackers",
+                              "ZSBending",
                               "dt",
                               {"float", "gravity", "-9.8"},
                               "Accel",

@@ -84,7 +84,8 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       const float *cloth_v, int64_t cloth_nt, const int32_t *cloth_tris,
                       const float *cloth_params, float *cloth_out_x, float *cloth_out_v,
                       int64_t tracker_n, const float *tracker_x, float *tracker_out_x,
-                      float *tracker_out_v, const char *write_path) {
+                      float *tracker_out_v, const char *write_path, const char *bending_type,
+                      float bending_stiffness) {
   using namespace zeno;
   try {
     Graph g;
@@ -172,6 +173,15 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.setNodeInput("cloth", "damping_coeff", num(cloth_params[3]));
       g.markOnce("cloth");
     }
+    // optional ConstructBendingSprings on the cloth
+    const bool bending = cloth && bending_type && bending_type[0];
+    if (bending) {
+      g.addNode("ConstructBendingSprings", "bend");
+      g.bindNodeInput("bend", "ZSSurfPrim", "cloth", "ZSParticles");
+      g.setNodeInput("bend", "bending_stiffness", num(bending_stiffness));
+      g.setNodeInput("bend", "type:", str(bending_type));
+      g.markOnce("bend");
+    }
     // optional tracker points (ToTrackerParticles), moved by the grid
     std::shared_ptr<PrimitiveObject> tprim;
     const bool trackers = tracker_n > 0 && tracker_x;
@@ -195,6 +205,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("step", "ZSGrid", "grid", "ZSGrid");
       if (cloth) g.bindNodeInput("step", "ZSCloth", "cloth", "ZSParticles");
       if (trackers) g.bindNodeInput("step", "ZSTrackers", "trk", "ZSParticles");
+      if (bending) g.bindNodeInput("step", "ZSBending", "bend", "ZSSpringPrim");
       g.setNodeInput("step", "dt", dtobj);
       g.setNodeInput("step", "gravity", num(gravity));
       g.setNodeInput("step", "substeps", inum(substeps));
@@ -207,6 +218,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.bindNodeInput("part", "ZSParticles", "pars", "ZSParticles");
       if (cloth) g.bindNodeInput("part", "ZSCloth", "cloth", "ZSParticles");
       if (trackers) g.bindNodeInput("part", "ZSTrackers", "trk", "ZSParticles");
+      if (bending) g.bindNodeInput("part", "ZSBending", "bend", "ZSSpringPrim");
       g.addNode("ExpandZSPartition", "expand");
       g.bindNodeInput("expand", "ZSPartition", "part", "ZSPartition");
       g.addNode("ZSGridFromZSPartition", "clear");

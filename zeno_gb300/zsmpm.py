@@ -78,6 +78,7 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
            "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
            "mpm_frame_begin", "mpm_frame_wait", "mpm_cloth_create", "mpm_cloth_download",
+           "mpm_cloth_add_bending",
            "mpm_trackers_create", "mpm_trackers_download",
            "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
@@ -134,6 +135,7 @@ def load(path: str = LIB_PATH):
         "mpm_compute_von_mises": ([P, i32], i32),
         "mpm_cloth_create": ([P, P], i32),
         "mpm_trackers_create": ([P, i64, P, P], i32),
+        "mpm_cloth_add_bending": ([P, i32, C.c_float, C.c_float, P], i32),
         "mpm_trackers_download": ([P, P, P], i32),
         "mpm_cloth_download": ([P] + [P] * 8, i32),
         "mpm_frame_begin": ([P, P, P], i32),
@@ -238,6 +240,16 @@ class Context:
                          float(mesh.fa), float(mesh.dc), 1 if tris.shape[1] == 2 else 0)
         self._check(self._L.mpm_cloth_create(self.h, C.byref(desc)), "mpm_cloth_create")
         self._cloth_n = (x.shape[0], tris.shape[0])
+
+    def add_cloth_bending(self, stiffness: float, kind: str = "vertex", thickness: float = None) -> int:
+        """ConstructBendingSprings on the context's cloth ("vertex" or "angle";
+        thickness defaults to the grid dx); returns the pair / hinge count."""
+        t = {"vertex": 0, "element": 1, "angle": 2}[kind]
+        n = C.c_int64(0)
+        th = self.scene.dx if thickness is None else thickness
+        self._check(self._L.mpm_cloth_add_bending(self.h, t, float(stiffness), float(th),
+                                                  C.byref(n)), "mpm_cloth_add_bending")
+        return int(n.value)
 
     def add_trackers(self, x, v=None):
         """ToTrackerParticles: points advected by the grid in every substep."""
@@ -629,7 +641,7 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
                                 C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P,
-                                C.c_char_p]
+                                C.c_char_p, C.c_char_p, C.c_float]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -651,7 +663,7 @@ def node_descriptors() -> dict:
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
                    fused=False, levelset=None, transfer="apic", cloth=None, trackers=None,
-                   write_path=None):
+                   write_path=None, bending=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -665,7 +677,8 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     trackers: optional (n, 3) points run through ToTrackerParticles and
     written back the same way; the return value then ends with their
     positions and velocities.  write_path: after the substeps, ComputeVonMises
-    and WriteZSParticles to this .geo file."""
+    and WriteZSParticles to this .geo file.  bending: (type, stiffness) of a
+    ConstructBendingSprings on the cloth, fed to the ZSBending inputs."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -706,7 +719,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
                          cl["t"].shape[0] if cl else 0, _p(cl.get("t")), _p(cl.get("p")),
                          _p(cl.get("ox")), _p(cl.get("ov")),
                          tk["x"].shape[0] if tk else 0, _p(tk.get("x")), _p(tk.get("ox")),
-                         _p(tk.get("ov")), write_path.encode() if write_path else None)
+                         _p(tk.get("ov")), write_path.encode() if write_path else None,
+                         bending[0].encode() if bending else None,
+                         float(bending[1]) if bending else 0.0)
     if rc != 0:
         raise RuntimeError(err.value.decode())
     out = (ox, ov, float(vmax[0]))
