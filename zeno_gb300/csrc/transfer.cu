@@ -50,14 +50,17 @@ namespace {
 //
 // Particles of a block are sorted by the z-major cell id (l2, l0, l1), so a
 // chunk of the block holds cells of every column.  A CTA walks its blocks in
-// chunks of kColChunk particles (thread j <-> particle j): each thread
-// converts its own particle's raw channels into a scatter record, and as
-// soon as the records are published it issues the cp.async copies of its
+// chunks of kColChunk particles (thread j < kColChunk <-> particle j): each
+// thread converts its own particle's raw channels into a scatter record, and
+// as soon as the records are published it issues the cp.async copies of its
 // particle of the next chunk into the raw buffer, so that those loads are in
 // flight while the current chunk scatters; the permutation entries of the
-// chunk after that load into registers.
+// chunk after that load into registers.  A chunk is one cell layer of a
+// block at the nominal 8 particles per cell (16 cells x 8), so the 16
+// columns scatter equal shares before the chunk's barrier (a chunk of 192,
+// one and a half layers, gave half the columns twice the work: 7 % slower).
 constexpr int kColThreads = 192;
-constexpr int kColChunk = kColThreads;
+constexpr int kColChunk = 128;
 constexpr int kColRaw = 23;            // x3 v3 C9 S6 m key
 constexpr int kColRecs = 16 * 9 * 6;  // float4 records: (column, oi oj, z)
 constexpr int kColMeta = 64;           // blocks per CTA whose metadata is staged
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(kColThreads, 4) k_p2g(DevPtrs d, const float *
   auto perm_of = [&](const Item &it) {
     if (it.k >= nblk) return -1;
     const ColMeta m = meta_of(it.k);
-    return tid < m.cnt - it.c0 ? d.perm[m.start + it.c0 + tid] : -1;
+    return tid < kColChunk && tid < m.cnt - it.c0 ? d.perm[m.start + it.c0 + tid] : -1;
   };
   auto issue = [&](int p) {
     if (p < 0) return;
