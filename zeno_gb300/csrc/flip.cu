@@ -73,7 +73,9 @@ template <bool kAffine> struct FLayout {
   static constexpr int rec4 = FRaw<kAffine>::N * kFChunk * 4;
   static constexpr int sw = rec4 + 7 * kFChunk * 16;
   static constexpr int sa = sw + kFChunk * 6 * 4;
-  static constexpr int region_end = sa + kFChunk * 6 * 4;
+  static constexpr int region_end = sa + kFChunk * 6 * 4 > rec4 + 2 * kFRecs * 16
+                                        ? sa + kFChunk * 6 * 4
+                                        : rec4 + 2 * kFRecs * 16;
   static constexpr int recA = rec4;
   static constexpr int recB = recA + kFRecs * 16;
   static constexpr int cell = region_end;
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kFThreads, 3)
   auto perm_of = [&](const Item &it) {
     if (it.k >= nblk) return -1;
     const FMeta m = meta_of(it.k);
-    return tid < m.cnt - it.c0 ? d.perm[m.start + it.c0 + tid] : -1;
+    return tid < kFChunk && tid < m.cnt - it.c0 ? d.perm[m.start + it.c0 + tid] : -1;
   };
   auto issue = [&](int p) {
     if (p < 0) return;
