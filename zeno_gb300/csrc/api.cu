@@ -655,8 +655,10 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
   src.mat = mat ? ist : nullptr;
   // chunks of the particle range: the copies of chunk k + 1 (on the copy
   // stream) overlap the material check and ingest of chunk k (on the
-  // context's stream); one synchronisation at the end
-  const int K = n >= (1 << 20) ? kUploadChunks : 1;
+  // context's stream); one synchronisation at the end.  An asynchronous
+  // upload copies in one piece: its conversion overlaps the next upload of
+  // another context instead, and fewer, larger copies keep the link busier
+  const int K = n >= (1 << 20) && !async ? kUploadChunks : 1;
   if (!c->copy_stream) {
     ZS_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (int k = 0; k <= kUploadChunks; ++k)
