@@ -51,6 +51,17 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(value: float, pg, device: str = "cuda") -> float:
+    """The largest of the ranks' values (a job's time is its slowest rank's);
+    `pg` is torch.distributed (NCCL: device tensors) or None for one rank."""
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_workload():
     from zeno_gb300 import scenes
     return scenes.multi_material(seed=0)
@@ -708,10 +719,7 @@ def run_gpu(args):
         pg.barrier()
     sampler.stop()
     ms = e0.elapsed_time(e1)
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, pg)
     ctx.sync()
     st = ctx.stats()
     value = ws * parts.n * args.steps / (ms * 1e-3)
@@ -769,10 +777,7 @@ def run_gpu(args):
         ctx.substep(dt, 1)
         ctx.download_raw(ox, ov)
     t_e2e = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([t_e2e], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(t_e2e, pg)
     ctx.sync()
     h2d = sum(a.nbytes for a in (hx, hv, hC, hF, hJ, hm, hvol, hmat))
     d2h = ox.nbytes + ov.nbytes
@@ -812,10 +817,7 @@ def run_gpu(args):
     for c in pipe:
         c.frame_wait()
     t_pipe = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([t_pipe], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_pipe = float(t.item())
+    t_pipe = max_over_ranks(t_pipe, pg)
     pipe_ok = True
     for c, (px, pv) in zip(pipe, outs):
         c.sync()
