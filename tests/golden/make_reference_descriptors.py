@@ -22,7 +22,8 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ZSGridToZSParticle", "ZSReturnMapping", "AdjustParticleMaterial",
          "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
          "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises", "ToZSCloth", "WriteZSParticles",
-         "ConstructBendingSprings",
+         "ConstructBendingSprings", "RetrievePrimitiveFromZSParticles",
+         "ExtractPrimitiveFromZSParticles",
          "ToTrackerParticles"]
 
 

@@ -1173,6 +1173,41 @@ ZENDEFNODE(UpdatePrimitiveFromZSParticles, {
                                                {"MPM"},
                                            });
 
+/// RetrievePrimitiveFromZSParticles (Generation.cu:1695-1715): the source
+/// primitive the particles were made from (as the last write-back left it).
+struct RetrievePrimitiveFromZSParticles : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    if (!pars->prim) throw std::runtime_error("there are no zsparticles!");
+    set_output("prim", pars->prim);
+  }
+};
+ZENDEFNODE(RetrievePrimitiveFromZSParticles, {
+                                                 {"ZSParticles"},
+                                                 {"prim"},
+                                                 {},
+                                                 {"MPM"},
+                                             });
+
+/// ExtractPrimitiveFromZSParticles (Generation.cu:1717-1742): the source
+/// primitive, and the particle object emptied (its device context released
+/// once no partition or grid holds it).
+struct ExtractPrimitiveFromZSParticles : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    if (!pars->prim) throw std::runtime_error("there are no zsparticles!");
+    auto prim = pars->prim;
+    *pars = ZenoParticles();
+    set_output("prim", prim);
+  }
+};
+ZENDEFNODE(ExtractPrimitiveFromZSParticles, {
+                                                {"ZSParticles"},
+                                                {"prim"},
+                                                {},
+                                                {"MPM"},
+                                            });
+
 /// ZSParticlesToPrimitiveObject (Generation.cu:1744-1833): a new primitive
 /// with "pos" and "vel"
 struct ZSParticlesToPrimitiveObject : INode {
