@@ -23,7 +23,8 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "UpdatePrimitiveFromZSParticles", "ZSParticlesToPrimitiveObject", "MakeZSLevelSet",
          "StepZSBoundary", "ComputeParticleBeta", "ComputeVonMises", "ToZSCloth", "WriteZSParticles",
          "ConstructBendingSprings", "RetrievePrimitiveFromZSParticles",
-         "ExtractPrimitiveFromZSParticles",
+         "ExtractPrimitiveFromZSParticles", "UpdatePrimitiveAttributesFromZSParticles",
+         "UpdatePrimitiveAttrFromZSParticles",
          "ToTrackerParticles"]
 
 

@@ -104,3 +104,19 @@ def test_write_zs_particles(zsmpm_mod, oracle_mod, tmp_path):
     with pytest.raises(RuntimeError, match="geo"):
         zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", E=5e4, nu=0.3, substeps=1,
                                  write_path=str(tmp_path / "pars.bgeo"))
+
+
+@pytest.mark.parametrize("attr", [("v", 3), ("J", 1), ("m", 1)])
+def test_update_primitive_attr(zsmpm_mod, attr):
+    """UpdatePrimitiveAttrFromZSParticles after the substeps writes the
+    particle channel into the source primitive in upload order."""
+    scene, parts = S.jelly_cube(cells=6)
+    parts.v = (0.3 * S.normal(5, 0, parts.n * 3).reshape(-1, 3)).astype(np.float32)
+    x, v, _, a = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", E=5e4, nu=0.3,
+                                          substeps=5, bc="sticky", thickness=3, attr=attr)
+    if attr[0] == "v":
+        np.testing.assert_array_equal(a, v)
+    elif attr[0] == "m":
+        np.testing.assert_allclose(a, parts.m, rtol=1e-6)
+    else:
+        assert 0.9 < a.min() <= a.max() < 1.1 and a.std() > 0

@@ -12,8 +12,10 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <set>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #ifdef ZSMPM_WITH_ZENO
@@ -38,6 +40,16 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
 }
 inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris.values; }
 inline const std::vector<vec2i> &lines(PrimitiveObject &p) { return p.lines.values; }
+// float / vec3f attribute `k` of the vertices (tris: of the triangles),
+// created when absent, sized to the element count
+template <class T> std::vector<T> &attr(PrimitiveObject &p, bool tris, const std::string &k) {
+  if (tris) {
+    if (!p.tris.has_attr(k)) p.tris.add_attr<T>(k);
+    return p.tris.attr<T>(k);
+  }
+  if (!p.verts.has_attr(k)) p.verts.add_attr<T>(k);
+  return p.verts.attr<T>(k);
+}
 }  // namespace prim_access
 }  // namespace zeno
 #else
@@ -60,6 +72,16 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
 }
 inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris; }
 inline const std::vector<vec2i> &lines(PrimitiveObject &p) { return p.lines; }
+template <class T> std::vector<T> &attr(PrimitiveObject &p, bool tris, const std::string &k) {
+  const size_t n = tris ? p.tris.size() : p.size();
+  std::vector<T> *a;
+  if constexpr (std::is_same_v<T, float>)
+    a = tris ? &p.tri_attrs1[k] : &p.attrs1[k];
+  else
+    a = tris ? &p.tri_attrs3[k] : (k == "pos" ? &p.verts() : &p.attrs3[k]);
+  a->resize(n);
+  return *a;
+}
 }  // namespace prim_access
 }  // namespace zeno
 #endif
@@ -1207,6 +1229,142 @@ ZENDEFNODE(ExtractPrimitiveFromZSParticles, {
                                                 {},
                                                 {"MPM"},
                                             });
+
+namespace {
+
+// A particle channel of a ZSParticles object in upload order: its width
+// (1 or 3) and values.  MPM particles: x, v and the scalar attributes of
+// mpm_particles_get_attr; cloth and curve vertices ("vert") and elements
+// ("quad"): x, v; tracker points: x, v.
+int fetch_channel(ZenoParticles &pars, bool quad, const std::string &name,
+                  std::vector<float> &out) {
+  auto fail = [&]() -> int {
+    throw std::runtime_error("the particles has no specified channel [" + name + "]");
+  };
+  if (name != "x" && name != "v" && (pars.cloth || pars.tracker || quad)) return fail();
+  if (pars.cloth) {
+    auto ctx = pars.cloth_ctx.lock();
+    if (!ctx) throw std::runtime_error("the cloth is not attached to a context yet");
+    const int64_t nv = (int64_t)prim_access::pos(*pars.prim).size();
+    const int64_t ne = pars.cloth_desc.kind == MPM_MESH_CURVE
+                           ? (int64_t)prim_access::lines(*pars.prim).size()
+                           : (int64_t)prim_access::tris(*pars.prim).size();
+    out.assign(3 * (quad ? ne : nv), 0.0f);
+    float *dst = out.data();
+    check(mpm_cloth_download(ctx->h, !quad && name == "x" ? dst : nullptr,
+                             !quad && name == "v" ? dst : nullptr, nullptr,
+                             quad && name == "x" ? dst : nullptr, quad && name == "v" ? dst : nullptr,
+                             nullptr, nullptr, nullptr),
+          "mpm_cloth_download");
+    return 3;
+  }
+  if (pars.tracker) {
+    auto ctx = pars.tracker_ctx.lock();
+    if (!ctx) throw std::runtime_error("the trackers are not attached to a context yet");
+    out.assign(3 * pars.n, 0.0f);
+    check(mpm_trackers_download(ctx->h, name == "x" ? out.data() : nullptr,
+                                name == "v" ? out.data() : nullptr),
+          "mpm_trackers_download");
+    return 3;
+  }
+  if (!pars.ctx) return fail();
+  if (name == "x" || name == "v") {
+    out.assign(3 * pars.n, 0.0f);
+    check(mpm_particles_download(pars.ctx->h, name == "x" ? out.data() : nullptr,
+                                 name == "v" ? out.data() : nullptr, nullptr, nullptr, nullptr),
+          "mpm_particles_download");
+    return 3;
+  }
+  static const std::set<std::string> scalars = {"J", "m", "vol", "vms", "beta", "mu", "lam"};
+  if (!scalars.count(name)) return fail();
+  out.assign(pars.n, 0.0f);
+  check(mpm_particles_get_attr(pars.ctx->h, name.c_str(), out.data()), "mpm_particles_get_attr");
+  return 1;
+}
+
+// the channel into the primitive's vertex (or triangle) attribute; x of the
+// vertices becomes "pos"
+void store_channel(PrimitiveObject &prim, bool quad, const std::string &name, int dim,
+                   const std::vector<float> &v) {
+  const std::string dst = (!quad && name == "x") ? "pos" : name;
+  if (dim == 1) {
+    auto &a = prim_access::attr<float>(prim, quad, dst);
+    const size_t n = std::min(a.size(), v.size());
+    for (size_t i = 0; i < n; ++i) a[i] = v[i];
+  } else {
+    auto &a = prim_access::attr<vec3f>(prim, quad, dst);
+    const size_t n = std::min(a.size(), v.size() / 3);
+    for (size_t i = 0; i < n; ++i) a[i] = vec3f{v[3 * i], v[3 * i + 1], v[3 * i + 2]};
+  }
+}
+
+}  // namespace
+
+/// UpdatePrimitiveAttributesFromZSParticles (Generation.cu:1165-1286): the
+/// named channels (separated by any of " :;,.") into attributes of the
+/// source primitive's vertices ("vert"; x becomes pos) or triangles ("quad",
+/// the cloth's elements); channels must be scalars or 3-vectors.
+struct UpdatePrimitiveAttributesFromZSParticles : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const std::string tags = get_input2<std::string>("attrs");
+    const bool quad = get_param<std::string>("location") == "quad";
+    if (!pars->prim) throw std::runtime_error("there are no zsparticles!");
+    std::set<std::string> names;
+    const std::string seps = " :;,.";
+    size_t st = tags.find_first_not_of(seps);
+    while (st != std::string::npos) {
+      const size_t ed = tags.find_first_of(seps, st);
+      names.insert(tags.substr(st, ed == std::string::npos ? std::string::npos : ed - st));
+      st = ed == std::string::npos ? ed : tags.find_first_not_of(seps, ed);
+    }
+    std::vector<float> buf;
+    for (const auto &name : names) {
+      const int dim = fetch_channel(*pars, quad, name, buf);
+      store_channel(*pars->prim, quad, name, dim, buf);
+    }
+    set_output("ZSParticles", pars);
+    set_output("prim", pars->prim);
+  }
+};
+ZENDEFNODE(UpdatePrimitiveAttributesFromZSParticles, {
+                                                         {"ZSParticles", {"string", "attrs", ""}},
+                                                         {"ZSParticles", "prim"},
+                                                         {{"enum vert quad", "location", "vert"}},
+                                                         {"MPM"},
+                                                     });
+
+/// UpdatePrimitiveAttrFromZSParticles (Generation.cu:1288-1468): one channel
+/// into a float or vec3f attribute of the source primitive's vertices or
+/// triangles (the type must match the channel's width).
+struct UpdatePrimitiveAttrFromZSParticles : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    const std::string name = get_input2<std::string>("attr");
+    const std::string type = get_param<std::string>("type");
+    const std::string location = get_param<std::string>("location");
+    if (location != "vert" && location != "quad")
+      throw std::runtime_error("UNRECOGINIZED LOCATION SPECIFIED");
+    if (type != "float" && type != "vec3f") throw std::runtime_error("INVALID SPECIFIED TYPE");
+    if (pars->prim) {
+      std::vector<float> buf;
+      const bool quad = location == "quad";
+      const int dim = fetch_channel(*pars, quad, name, buf);
+      if (dim != (type == "float" ? 1 : 3))
+        throw std::runtime_error("UpdatePrimitiveAttrFromZSParticles: channel [" + name +
+                                 "] has width " + std::to_string(dim) + ", not " + type);
+      store_channel(*pars->prim, quad, name, dim, buf);
+    }
+    set_output("ZSParticles", pars);
+  }
+};
+ZENDEFNODE(UpdatePrimitiveAttrFromZSParticles,
+           {
+               {"ZSParticles", {"string", "attr", "x"}},
+               {"ZSParticles"},
+               {{"enum float vec3f", "type", "vec3f"}, {"enum vert quad", "location", "vert"}},
+               {"MPM"},
+           });
 
 /// ZSParticlesToPrimitiveObject (Generation.cu:1744-1833): a new primitive
 /// with "pos" and "vel"

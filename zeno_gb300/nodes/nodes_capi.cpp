@@ -85,7 +85,8 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       const float *cloth_params, float *cloth_out_x, float *cloth_out_v,
                       int64_t tracker_n, const float *tracker_x, float *tracker_out_x,
                       float *tracker_out_v, const char *write_path, const char *bending_type,
-                      float bending_stiffness) {
+                      float bending_stiffness, const char *attr_name, int32_t attr_dim,
+                      float *attr_out) {
   using namespace zeno;
   try {
     Graph g;
@@ -271,6 +272,22 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
     g.addNode("UpdatePrimitiveFromZSParticles", "out");
     g.setNodeInput("out", "ZSParticles", g.getNodeOutput(last, "ZSParticles"));
     g.applyNodes({"out"});
+    if (attr_name && attr_name[0] && attr_out) {  // UpdatePrimitiveAttrFromZSParticles
+      g.addNode("UpdatePrimitiveAttrFromZSParticles", "attr");
+      g.setNodeInput("attr", "ZSParticles", g.getNodeOutput(last, "ZSParticles"));
+      g.setNodeInput("attr", "attr", str(attr_name));
+      g.setNodeInput("attr", "type:", str(attr_dim == 1 ? "float" : "vec3f"));
+      g.applyNodes({"attr"});
+      const std::string key = std::string(attr_name) == "x" ? "pos" : attr_name;
+      if (attr_dim == 1) {
+        const auto &a = prim->attrs1.at(key);
+        for (int64_t i = 0; i < n; ++i) attr_out[i] = a[i];
+      } else {
+        const auto &a = prim->attrs3.at(key);
+        for (int64_t i = 0; i < n; ++i)
+          for (int d = 0; d < 3; ++d) attr_out[3 * i + d] = a[i][d];
+      }
+    }
     if (write_path && write_path[0]) {  // ComputeVonMises -> WriteZSParticles
       g.addNode("ComputeVonMises", "vms");
       g.setNodeInput("vms", "ZSParticles", g.getNodeOutput(last, "ZSParticles"));

@@ -67,6 +67,8 @@ struct PrimitiveObject : IObject {
   std::map<std::string, std::vector<float>> attrs1;
   std::vector<vec3i> tris;  // triangle vertex indices
   std::vector<vec2i> lines; // segment vertex indices
+  std::map<std::string, std::vector<vec3f>> tri_attrs3;  // per-triangle attributes
+  std::map<std::string, std::vector<float>> tri_attrs1;
   std::vector<vec3f> &verts() { return attrs3["pos"]; }
   size_t size() const {
     auto it = attrs3.find("pos");

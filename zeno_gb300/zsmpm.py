@@ -641,7 +641,7 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
                                 C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P,
-                                C.c_char_p, C.c_char_p, C.c_float]
+                                C.c_char_p, C.c_char_p, C.c_float, C.c_char_p, C.c_int32, P]
     L.zsn_run_graph.restype = C.c_int32
     _nodes = L
     return L
@@ -663,7 +663,7 @@ def node_descriptors() -> dict:
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
                    fused=False, levelset=None, transfer="apic", cloth=None, trackers=None,
-                   write_path=None, bending=None):
+                   write_path=None, bending=None, attr=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -678,7 +678,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     written back the same way; the return value then ends with their
     positions and velocities.  write_path: after the substeps, ComputeVonMises
     and WriteZSParticles to this .geo file.  bending: (type, stiffness) of a
-    ConstructBendingSprings on the cloth, fed to the ZSBending inputs."""
+    ConstructBendingSprings on the cloth, fed to the ZSBending inputs.  attr:
+    (name, width) of an UpdatePrimitiveAttrFromZSParticles after the
+    substeps; the attribute's values are appended to the return value."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -706,6 +708,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
         cl["p"] = np.array([cloth.gamma, cloth.k, cloth.fa, cloth.dc], np.float32)
         cl["ox"] = np.zeros_like(cl["x"])
         cl["ov"] = np.zeros_like(cl["x"])
+    aout = None
+    if attr:
+        aout = np.zeros((n, 3) if attr[1] == 3 else n, np.float32)
     tk = {}
     if trackers is not None:
         tk["x"] = np.ascontiguousarray(trackers, dtype=np.float32).reshape(-1, 3)
@@ -721,7 +726,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
                          tk["x"].shape[0] if tk else 0, _p(tk.get("x")), _p(tk.get("ox")),
                          _p(tk.get("ov")), write_path.encode() if write_path else None,
                          bending[0].encode() if bending else None,
-                         float(bending[1]) if bending else 0.0)
+                         float(bending[1]) if bending else 0.0,
+                         attr[0].encode() if attr else None, int(attr[1]) if attr else 0,
+                         _p(aout))
     if rc != 0:
         raise RuntimeError(err.value.decode())
     out = (ox, ov, float(vmax[0]))
@@ -729,4 +736,6 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
         out += (cl["ox"], cl["ov"])
     if tk:
         out += (tk["ox"], tk["ov"])
+    if attr:
+        out += (aout,)
     return out
