@@ -267,15 +267,10 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
             mom[a] = W * mass * (vn[a] + Cx) + (flip_style ? 0.0f : fo[a]);
           }
           float4 *g4 = d.grid + idx;
-          atomicAdd(&g4->x, W * mass);
-          atomicAdd(&g4->y, mom[0]);
-          atomicAdd(&g4->z, mom[1]);
-          atomicAdd(&g4->w, mom[2]);
+          atomicAdd(g4, make_float4(W * mass, mom[0], mom[1], mom[2]));  // one 16-byte atomic
           if (flip_style) {
             float4 *h4 = d.grid2 + idx;
-            atomicAdd(&h4->x, fo[0]);
-            atomicAdd(&h4->y, fo[1]);
-            atomicAdd(&h4->z, fo[2]);
+            atomicAdd(h4, make_float4(fo[0], fo[1], fo[2], 0.0f));
           }
         }
     if (curve) {  // type (ii): +-vol dt P_c0 DmInv00 on the two vertices
@@ -347,15 +342,10 @@ __global__ void k_cloth_p2g_verts(DevPtrs d) {
             mom[a] = flip_style ? W * mass * (vp[a] + Cx) : W * (mass * (vp[a] + Cx) + im[a]);
           }
           float4 *g4 = d.grid + idx;
-          atomicAdd(&g4->x, W * mass);
-          atomicAdd(&g4->y, mom[0]);
-          atomicAdd(&g4->z, mom[1]);
-          atomicAdd(&g4->w, mom[2]);
+          atomicAdd(g4, make_float4(W * mass, mom[0], mom[1], mom[2]));  // one 16-byte atomic
           if (flip_style) {
             float4 *h4 = d.grid2 + idx;
-            atomicAdd(&h4->x, W * im[0]);
-            atomicAdd(&h4->y, W * im[1]);
-            atomicAdd(&h4->z, W * im[2]);
+            atomicAdd(h4, make_float4(W * im[0], W * im[1], W * im[2], 0.0f));
           }
         }
   }
