@@ -1002,7 +1002,7 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
     return MPM_OK;
   };
   if ((rc = up(&nc.vx, vx)) || (rc = up(&nc.vv, vv)) || (rc = up(&nc.vC, vC)) || (rc = up(&nc.vm, vm)) ||
-      (rc = up(&nc.imp, std::vector<float>(3 * nv, 0.0f))) || (rc = up(&nc.ex, ex)) ||
+      (rc = up(&nc.imp, std::vector<float>(4 * nv, 0.0f))) || (rc = up(&nc.ex, ex)) ||
       (rc = up(&nc.ev, ev)) || (rc = up(&nc.eC, eC)) || (rc = up(&nc.eF, eF)) || (rc = up(&nc.ed, ed)) ||
       (rc = up(&nc.eDmInv, eDi)) || (rc = up(&nc.em, em)) || (rc = up(&nc.evol, evol)) ||
       (rc = up(&nc.emu, emu)) || (rc = up(&nc.elam, elam)))

@@ -49,6 +49,11 @@ __device__ __forceinline__ long long node_of(const DevPtrs &d, const SceneParams
   return (long long)gb * 64 + (((i0 & 3) << 4) | ((i1 & 3) << 2) | (i2 & 3));
 }
 
+// a vertex's impulse sum (x, y, z, unused): one 16-byte atomic per update
+__device__ __forceinline__ float4 *imp4(const ClothDev &cl, long long v) {
+  return reinterpret_cast<float4 *>(cl.imp) + v;
+}
+
 // w' of the quadratic B-spline with respect to the particle position (cells)
 __device__ __forceinline__ float wgrad(const Stencil1 &s, int o) {
   return o == 0 ? s.f - 1.5f : (o == 1 ? -2.0f * (s.f - 1.0f) : s.f - 0.5f);
@@ -277,12 +282,10 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
       const int t0 = cl.inds[3 * e], t1 = cl.inds[3 * e + 1];
       const float di = cl.eDmInv[9 * e];
       if (t0 < 0 || t0 >= cl.n_verts || t1 < 0 || t1 >= cl.n_verts) continue;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float f = vol * dt * P[a * 3 + 0] * di;
-        atomicAdd(&cl.imp[3 * t0 + a], f);
-        atomicAdd(&cl.imp[3 * t1 + a], -f);
-      }
+      const float4 f = make_float4(vol * dt * P[0] * di, vol * dt * P[3] * di,
+                                   vol * dt * P[6] * di, 0.0f);
+      atomicAdd(imp4(cl, t0), f);
+      atomicAdd(imp4(cl, t1), make_float4(-f.x, -f.y, -f.z, 0.0f));
       continue;
     }
     // type (ii): impulses from the in-plane columns of P through DmInv rows
@@ -302,9 +305,9 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
         Dr1 = vi == 1 ? r0[1] : r1[1];
         coeff = -vol * dt;
       }
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        atomicAdd(&cl.imp[3 * t + a], coeff * (P[a * 3 + 0] * Dr0 + P[a * 3 + 1] * Dr1));
+      atomicAdd(imp4(cl, t), make_float4(coeff * (P[0] * Dr0 + P[1] * Dr1),
+                                         coeff * (P[3] * Dr0 + P[4] * Dr1),
+                                         coeff * (P[6] * Dr0 + P[7] * Dr1), 0.0f));
     }
   }
 }
@@ -319,7 +322,8 @@ __global__ void k_cloth_p2g_verts(DevPtrs d) {
        p += (long long)gridDim.x * blockDim.x) {
     const float mass = cl.vm[p];
     const float vp[3] = {cl.vv[3 * p], cl.vv[3 * p + 1], cl.vv[3 * p + 2]};
-    const float im[3] = {cl.imp[3 * p], cl.imp[3 * p + 1], cl.imp[3 * p + 2]};
+    const float4 im4 = *imp4(cl, p);
+    const float im[3] = {im4.x, im4.y, im4.z};
     float C[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) C[i] = affine ? cl.vC[9 * p + i] : 0.0f;
@@ -369,11 +373,8 @@ __global__ void k_cloth_bending(DevPtrs d) {
     const float rl = cl.srl[s];
     if (!(len < rl) || len == 0.0f) continue;
     const float c = t2 * len * cl.sk[s] * (1.0f - len / rl) * dt / len;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      atomicAdd(&cl.imp[3 * a0 + a], -c * dv[a]);
-      atomicAdd(&cl.imp[3 * a1 + a], c * dv[a]);
-    }
+    atomicAdd(imp4(cl, a0), make_float4(-c * dv[0], -c * dv[1], -c * dv[2], 0.0f));
+    atomicAdd(imp4(cl, a1), make_float4(c * dv[0], c * dv[1], c * dv[2], 0.0f));
   }
 }
 
@@ -666,7 +667,7 @@ void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
 }
 
 void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
-  cudaMemsetAsync(d.cloth.imp, 0, (size_t)d.cloth.n_verts * 3 * sizeof(float), s);
+  cudaMemsetAsync(d.cloth.imp, 0, (size_t)d.cloth.n_verts * 4 * sizeof(float), s);
   if (d.cloth.n_springs > 0) k_cloth_bending<<<d.num_sms * 4, 128, 0, s>>>(d);
   k_cloth_p2g_elements<<<d.num_sms * 4, 128, 0, s>>>(d);
   k_cloth_p2g_verts<<<d.num_sms * 4, 128, 0, s>>>(d);

@@ -160,7 +160,8 @@ struct ClothDev {
                              // curves use the first 2)
   int model;                 // MPM_FCR / MPM_NHK / MPM_STVK (curves: MPM_STVK)
   float gamma, k, fc, dc;    // shear stiffness, normal stiffness, tan(fa / pi), damping
-  float *vx, *vv, *vC, *vm, *imp;
+  float *vx, *vv, *vC, *vm;
+  float *imp;  // per vertex (x, y, z, unused): the impulse sums of a P2G
   float *ex, *ev, *eC, *eF, *ed, *eDmInv, *em, *evol, *emu, *elam;
   int32_t *inds;
   // vertex bending springs (ConstructBendingSprings "vertex"): vertex pairs,
