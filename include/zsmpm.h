@@ -277,7 +277,9 @@ int32_t mpm_particles_set_lame(mpm_ctx *ctx, const float *mu, const float *lam);
 int32_t mpm_particles_download(mpm_ctx *ctx, float *x, float *v, float *C, float *F, float *J);
 /* One per-particle attribute in the upload order, by its channel name in the
  * reference's particle store (Generation.cpp:868-903): get "beta", "vms",
- * "m", "vol", "J", "mu", "lam"; set "beta" (host arrays of n floats). */
+ * "m", "vol", "J", "mu", "lam"; set "beta" (host arrays of n floats).  Get
+ * "cloth_beta": the beta of the cloth's vertices (n_verts floats), set by
+ * mpm_compute_particle_beta on a triangle cloth (and settable). */
 int32_t mpm_particles_get_attr(mpm_ctx *ctx, const char *name, float *values);
 int32_t mpm_particles_set_attr(mpm_ctx *ctx, const char *name, const float *values);
 /* ComputeVonMises (Generation.cu:1873-1920): the von Mises stress of the

@@ -898,7 +898,7 @@ template <class R> struct Sim {
   }
 
   // ZSGridToZSParticle for the cloth (Transfer.cu:1287-1445): vertices as
-  // damped APIC (or the FLIP-style blend with beta 0), then elements: damped
+  // damped APIC (or the FLIP-style blend with the vertices' beta), then elements: damped
   // C, centroid position and mean velocity of their vertices, d1 = p1 - p0,
   // d2 = p2 - p0, d3 += (dt C + dt^2 / 2 C^2) d3, F = d DmInv.
   void cloth_g2p(orc_cloth &cl, double dt) {
@@ -910,8 +910,9 @@ template <class R> struct Sim {
       for (int a = 0; a < 3; ++a) {
         if (flip_style) {
           const double d0 = cl.vv[3 * p + a] - vel[a];
+          const double beta = cl.vbeta ? cl.vbeta[p] : 0.0;
           cl.vv[3 * p + a] = vs[a] + 0.99 * d0;
-          cl.vx[3 * p + a] += dt * vs[a];  // beta = 0
+          cl.vx[3 * p + a] += dt * (vs[a] + beta * 0.99 * d0);
         } else {
           cl.vv[3 * p + a] = vel[a];
           cl.vx[3 * p + a] += vel[a] * dt;
@@ -1425,6 +1426,34 @@ int32_t orc_particle_beta_f64(const orc_scene *scene, int64_t n, const double *x
     }
     const double Jp = sim.mats[mat[p]].type == ORC_EOS ? J[p] : det3(F + 9 * p);
     beta[p] = Jp > 1.0 ? 0.5 : 0.0;
+  }
+  return ORC_OK;
+}
+
+int32_t orc_cloth_beta_f64(const orc_scene *scene, orc_cloth *cl, double dt, int32_t collider) {
+  if (!scene || !cl || !cl->vbeta || collider >= scene->n_colliders) return ORC_ERR_INVALID;
+  if (cl->kind != ORC_MESH_SURFACE) return ORC_ERR_INVALID;
+  Sim<double> sim(*scene, 1);
+  for (int64_t e = 0; e < cl->n_eles; ++e) {
+    const int32_t *t = cl->inds + 3 * e;
+    const double *ve = cl->ev + 3 * e;
+    double value = -1;
+    if (collider >= 0) {
+      double pos[3], nrm[3], vo[3];
+      for (int a = 0; a < 3; ++a) pos[a] = cl->ex[3 * e + a] + dt * ve[a];
+      if (sim.collider_hit(sim.cols[collider], pos, nrm, vo) &&
+          (ve[0] - vo[0]) * nrm[0] + (ve[1] - vo[1]) * nrm[1] + (ve[2] - vo[2]) * nrm[2] < 0)
+        value = 0;
+    }
+    if (value < 0) {
+      double Q[9], Rm[9];
+      Sim<double>::gram_schmidt(cl->ed + 9 * e, Q, Rm);
+      const double Jn = std::fabs(Rm[0] * Rm[4] - Rm[3] * Rm[1]);
+      const double J0inv = std::fabs(det3(cl->eDmInv + 9 * e));
+      const double J = det3(cl->eF + 9 * e) / (Jn * J0inv);
+      value = J > 1.0 ? 0.2 : 0.0;
+    }
+    for (int k = 0; k < 3; ++k) cl->vbeta[t[k]] = value;
   }
   return ORC_OK;
 }

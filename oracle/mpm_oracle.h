@@ -103,6 +103,9 @@ typedef struct orc_cloth {
   const int32_t *spring_v;
   const double *spring_k, *spring_rl;
   double thickness;
+  /* ComputeParticleBeta on the surface (NULL: 0): per-vertex beta of the
+   * FLIP-style vertex position update x += dt (vstar + beta 0.99 (v0 - v)) */
+  double *vbeta;
 } orc_cloth;
 
 /* Tracker particles (ToTrackerParticles, Generation.cu:105-170): points
@@ -159,6 +162,14 @@ int32_t orc_run_f64(const orc_scene *scene, int64_t n, double *x, double *v,
                     const double *vol, const int32_t *mat, const double *mu,
                     const double *lam, const double *beta, double dt,
                     int32_t nsteps, int32_t nthreads, orc_stats *stats);
+
+/* ComputeParticleBeta on a triangle cloth (Boundary.cu:316-360, 460-490):
+ * per element in index order (a vertex keeps the value of the last element
+ * that has it), beta 0 for its vertices when, with collider >= 0, its
+ * centroid at x + dt v is inside the collider and moving into it; else 0.2
+ * when the normal stretch det F / (|r00 r11 - r10 r01| |det DmInv|) of d =
+ * QR exceeds 1, else 0.  Writes cl->vbeta (n_verts). */
+int32_t orc_cloth_beta_f64(const orc_scene *scene, orc_cloth *cl, double dt, int32_t collider);
 
 /* Same substeps in single precision with OpenMP (the CPU baseline). */
 int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v,

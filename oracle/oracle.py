@@ -40,7 +40,7 @@ class OrcCloth(C.Structure):
                [(k, C.c_void_p) for k in ("vx", "vv", "vC", "vm", "ex", "ev", "eC", "eF", "ed",
                                           "eDmInv", "em", "evol", "emu", "elam", "inds")] + \
                [("n_springs", C.c_int64), ("spring_v", C.c_void_p), ("spring_k", C.c_void_p),
-                ("spring_rl", C.c_void_p), ("thickness", C.c_double)]
+                ("spring_rl", C.c_void_p), ("thickness", C.c_double), ("vbeta", C.c_void_p)]
 
 
 CLOTH_VERT = {"vx": 3, "vv": 3, "vC": 9, "vm": 1}
@@ -104,6 +104,9 @@ def lib():
         L.orc_cloth_init_f64.restype = C.c_int32
         L.orc_curve_init_f64.argtypes = L.orc_cloth_init_f64.argtypes
         L.orc_curve_init_f64.restype = C.c_int32
+        L.orc_cloth_beta_f64.argtypes = [C.POINTER(OrcScene), C.POINTER(OrcCloth), C.c_double,
+                                         C.c_int32]
+        L.orc_cloth_beta_f64.restype = C.c_int32
         L.orc_sym_eig3.argtypes = [P, P, P]
         L.orc_kirchhoff.argtypes = [C.POINTER(OrcMaterial), P, C.c_double, P]
         L.orc_kirchhoff.restype = C.c_int32
@@ -244,11 +247,15 @@ def _is_curve(mesh) -> bool:
     return np.asarray(mesh.tris).shape[1] == 2
 
 
-def _cloth_struct(mesh, state) -> OrcCloth:
-    curve = _is_curve(mesh)
-    st = OrcCloth(1 if curve else 0, 2 if curve else int(mesh.model), float(mesh.gamma),
-                  float(mesh.k), float(mesh.fa), float(mesh.dc), int(state["vx"].shape[0]),
-                  int(state["ex"].shape[0]))
+def _cloth_struct(mesh, state, kind=None) -> OrcCloth:
+    if mesh is None:  # the state alone (set-up free helpers)
+        st = OrcCloth(int(kind), 0, 0.0, 0.0, 0.0, 0.0, int(state["vx"].shape[0]),
+                      int(state["ex"].shape[0]))
+    else:
+        curve = _is_curve(mesh)
+        st = OrcCloth(1 if curve else 0, 2 if curve else int(mesh.model), float(mesh.gamma),
+                      float(mesh.k), float(mesh.fa), float(mesh.dc), int(state["vx"].shape[0]),
+                      int(state["ex"].shape[0]))
     for k in list(CLOTH_VERT) + list(CLOTH_ELE) + ["inds"]:
         setattr(st, k, state[k].ctypes.data)
     if "spring_v" in state and len(state["spring_v"]):
@@ -257,7 +264,22 @@ def _cloth_struct(mesh, state) -> OrcCloth:
         st.spring_k = state["spring_k"].ctypes.data
         st.spring_rl = state["spring_rl"].ctypes.data
         st.thickness = float(state["thickness"])
+    if "vbeta" in state:
+        st.vbeta = state["vbeta"].ctypes.data
     return st
+
+
+def cloth_beta(scene, state: dict, dt: float, collider: int = -1) -> np.ndarray:
+    """ComputeParticleBeta on a triangle cloth state from cloth_init, in FP64
+    (orc_cloth_beta_f64): sets and returns state["vbeta"], the per-vertex beta
+    the FLIP-style vertex update then uses."""
+    state["vbeta"] = np.zeros(state["vx"].shape[0])
+    h = _SceneHolder(scene)
+    st = _cloth_struct(None, state, kind=0)
+    rc = lib().orc_cloth_beta_f64(C.byref(h.s), C.byref(st), float(dt), int(collider))
+    if rc != 0:
+        raise RuntimeError(f"oracle cloth beta failed with status {rc}")
+    return state["vbeta"]
 
 
 def cloth_bending(state: dict, stiffness: float, thickness: float, kind: str = "vertex") -> int:

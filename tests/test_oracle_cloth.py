@@ -480,3 +480,47 @@ def test_bending_springs_substep_matches_numpy(oracle_mod):
     plain = {k: a for k, a in st.items() if not k.startswith("spring") and k != "thickness"}
     _, free, _ = oracle_mod.run_cloth(scene, _empty(), mesh, plain, 1)
     assert np.abs(free["vv"] - out["vv"]).max() > 1e-3 * np.abs(out["vv"]).max()
+
+
+def test_cloth_beta(oracle_mod):
+    """ComputeParticleBeta on a triangle cloth: per element in index order (a
+    vertex keeps the last element's value), 0.2 when the normal stretch
+    det F / (|r00 r11| |det DmInv|) of d = QR exceeds 1, else 0; against a
+    numpy loop.  With a collider, elements whose centroid (at x + dt v) is
+    inside it and moving in give 0."""
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    mesh = S.cloth_sheet((0.5, 0.5, 0.5), 0.3, 8, jitter=0.2, seed=6)
+    st = oracle_mod.cloth_init(mesh, scene.dx)
+    s = S.uniform(4, 0, len(st["ex"]))
+    for e in range(len(st["ex"])):
+        d = st["ed"][e].reshape(3, 3).copy()
+        d[:, 2] *= 0.9 + 0.2 * s[e]  # normal compressed or stretched
+        st["ed"][e] = d.ravel()
+        st["eF"][e] = (d @ st["eDmInv"][e].reshape(3, 3)).ravel()
+    beta = oracle_mod.cloth_beta(scene, st, scene.dt).copy()
+    ref = np.zeros(len(st["vx"]))
+    for e, t in enumerate(st["inds"]):
+        F = st["eF"][e].reshape(3, 3)
+        _, R = _gs(st["ed"][e].reshape(3, 3))
+        Jn = abs(R[0, 0] * R[1, 1] - R[1, 0] * R[0, 1])
+        J = np.linalg.det(F) / (Jn * abs(np.linalg.det(st["eDmInv"][e].reshape(3, 3))))
+        ref[t] = 0.2 if J > 1 else 0.0
+    np.testing.assert_array_equal(beta, ref)
+    assert 0 < (beta > 0).sum() < len(beta)
+    # a sphere around the sheet's centre; centroids move towards its centre
+    scene.colliders = [S.sphere_collider((0.5, 0.5, 0.5), 0.08, scene.dx, S.BC_SLIP)]
+    st["ev"][:] = -(st["ex"] - 0.5) * 2.0
+    with_col = oracle_mod.cloth_beta(scene, st, scene.dt, 0).copy()
+    r = np.linalg.norm(st["ex"] + scene.dt * st["ev"] - 0.5, axis=1)
+    assert (r < 0.07).any()
+    # a vertex whose last element is well inside the sphere gets 0, one whose
+    # last element is well outside keeps the volume criterion's value
+    last = {}
+    for e, t in enumerate(st["inds"]):
+        for v in t:
+            last[int(v)] = e
+    for v, e in last.items():
+        if r[e] < 0.07:
+            assert with_col[v] == 0.0
+        elif r[e] > 0.09:
+            assert with_col[v] == ref[v]

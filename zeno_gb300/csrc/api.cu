@@ -795,6 +795,13 @@ int32_t mpm_particles_get_attr(mpm_ctx *c, const char *name, float *values) {
   if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
   const std::string a(name);
   const long long n = c->prm.n;
+  if (a == "cloth_beta") {  // the cloth's vertices (n_verts values)
+    if (c->d.cloth.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
+    ZS_CUDA(cudaMemcpyAsync(values, c->d.cloth.vbeta, c->d.cloth.n_verts * sizeof(float),
+                            cudaMemcpyDeviceToHost, c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+  }
   if (a == "beta" || a == "vms") {  // planes by upload index
     if (n > 0)
       ZS_CUDA(cudaMemcpyAsync(values, a == "beta" ? c->d.beta : c->d.vms, n * sizeof(float),
@@ -824,6 +831,13 @@ int32_t mpm_particles_set_attr(mpm_ctx *c, const char *name, const float *values
   int32_t rc = check(c);
   if (rc) return rc;
   if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
+  if (std::string(name) == "cloth_beta") {  // the cloth's vertices (n_verts values)
+    if (c->d.cloth.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
+    ZS_CUDA(cudaMemcpyAsync(c->d.cloth.vbeta, values, c->d.cloth.n_verts * sizeof(float),
+                            cudaMemcpyHostToDevice, c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+  }
   if (std::string(name) != "beta")
     return fail(MPM_ERR_INVALID, std::string("attribute '") + name + "' cannot be set");
   const long long n = c->prm.n;
@@ -1005,9 +1019,11 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
       (rc = up(&nc.imp, std::vector<float>(4 * nv, 0.0f))) || (rc = up(&nc.ex, ex)) ||
       (rc = up(&nc.ev, ev)) || (rc = up(&nc.eC, eC)) || (rc = up(&nc.eF, eF)) || (rc = up(&nc.ed, ed)) ||
       (rc = up(&nc.eDmInv, eDi)) || (rc = up(&nc.em, em)) || (rc = up(&nc.evol, evol)) ||
-      (rc = up(&nc.emu, emu)) || (rc = up(&nc.elam, elam)))
+      (rc = up(&nc.emu, emu)) || (rc = up(&nc.elam, elam)) ||
+      (rc = up(&nc.vbeta, std::vector<float>(nv, 0.0f))))  // ToZSCloth: beta = 0
     return rc;
-  if ((rc = dalloc(c, &nc.inds, (size_t)3 * ne))) return rc;
+  if ((rc = dalloc(c, &nc.inds, (size_t)3 * ne)) || (rc = dalloc(c, &nc.vowner, (size_t)nv)))
+    return rc;
   ZS_CUDA(cudaMemcpyAsync(nc.inds, inds.data(), 3 * ne * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   nc.n_verts = nv;
@@ -1261,9 +1277,11 @@ int32_t mpm_compute_particle_beta(mpm_ctx *c, float dt, int32_t collider) {
   if (rc) return rc;
   if (collider < -1 || collider >= (int32_t)c->colliders.size())
     return fail(MPM_ERR_INVALID, "collider id out of range");
-  if (c->prm.n == 0) return MPM_OK;
   if ((rc = push_params(c))) return rc;
-  launch_particle_beta(c->d, c->cur, dt, collider, c->stream);
+  if (c->prm.n > 0) launch_particle_beta(c->d, c->cur, dt, collider, c->stream);
+  // a triangle cloth's vertices (curves keep beta 0, as in the reference)
+  if (c->d.cloth.n_verts > 0 && c->d.cloth.kind == MPM_MESH_SURFACE)
+    launch_cloth_beta(c->d, dt, collider, c->stream);
   return launch_check("particle beta");
 }
 

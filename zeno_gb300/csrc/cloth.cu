@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "binning.cuh"
+#include "colliders.cuh"
 #include "mpm_math.cuh"
 #include "zsmpm_internal.cuh"
 
@@ -500,10 +501,11 @@ __global__ void k_cloth_g2p_verts(DevPtrs d) {
     cloth_gather(d, S, cl.vx + 3 * p, flip_style, cl.dc, vel, vs, Cn);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      if (flip_style) {  // beta = 0 for the cloth
+      if (flip_style) {  // x += dt (vstar + beta 0.99 (v0 - v)), Transfer.cu:1320-1331
         const float d0 = cl.vv[3 * p + a] - vel[a];
+        const float beta = cl.vbeta[p];
         cl.vv[3 * p + a] = vs[a] + 0.99f * d0;
-        cl.vx[3 * p + a] += dt * vs[a];
+        cl.vx[3 * p + a] += dt * (vs[a] + beta * 0.99f * d0);
       } else {
         cl.vv[3 * p + a] = vel[a];
         cl.vx[3 * p + a] += vel[a] * dt;
@@ -605,6 +607,60 @@ __global__ void k_cloth_g2p_elements(DevPtrs d) {
   }
 }
 
+// ComputeParticleBeta on a triangle cloth (Boundary.cu:316-360, 460-490):
+// each element decides 0.2 (normal stretch det F / (|r00 r11 - r10 r01|
+// |det DmInv|) of d = QR above 1) or 0 (else, or, with a collider, its
+// centroid at x + dt v inside the collider and moving in) for its three
+// vertices.  The reference's elements race for shared vertices; here a
+// vertex takes its highest-numbered element's value (the outcome of running
+// the elements in index order): a first pass finds that element, the second
+// writes.
+__global__ void k_cloth_beta_owner(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cl.n_eles;
+       e += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int t = cl.inds[3 * e + k];
+      if (t >= 0 && t < cl.n_verts) atomicMax(&cl.vowner[t], (int)e);
+    }
+}
+
+__global__ void k_cloth_beta(DevPtrs d, float dt, int collider) {
+  const ClothDev &cl = d.cloth;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cl.n_eles;
+       e += (long long)gridDim.x * blockDim.x) {
+    float value = -1.0f;
+    const float v[3] = {cl.ev[3 * e], cl.ev[3 * e + 1], cl.ev[3 * e + 2]};
+    if (collider >= 0) {
+      const float x[3] = {cl.ex[3 * e] + dt * v[0], cl.ex[3 * e + 1] + dt * v[1],
+                          cl.ex[3 * e + 2] + dt * v[2]};
+      float nrm[3], vo[3];
+      if (collider_hit(d.colliders[collider], x, nrm, vo) &&
+          (v[0] - vo[0]) * nrm[0] + (v[1] - vo[1]) * nrm[1] + (v[2] - vo[2]) * nrm[2] < 0.0f)
+        value = 0.0f;
+    }
+    if (value < 0.0f) {
+      float F[9], dm[9], Di[9], Q[9], R[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        F[k] = cl.eF[9 * e + k];
+        dm[k] = cl.ed[9 * e + k];
+        Di[k] = cl.eDmInv[9 * e + k];
+      }
+      gram_schmidt(dm, Q, R);
+      const float Jn = fabsf(R[0] * R[4] - R[3] * R[1]);
+      const float J = det3(F) / (Jn * fabsf(det3(Di)));
+      value = J > 1.0f ? 0.2f : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int t = cl.inds[3 * e + k];
+      if (t >= 0 && t < cl.n_verts && cl.vowner[t] == (int)e) cl.vbeta[t] = value;
+    }
+  }
+}
+
 // tracker points (ToTrackerParticles): their blocks join the partition
 __global__ void k_tracker_mark(DevPtrs d) {
   const SceneParams &S = d.scn[0];
@@ -660,6 +716,12 @@ void launch_tracker_mark(const DevPtrs &d, cudaStream_t s) {
 
 void launch_tracker_g2p(const DevPtrs &d, cudaStream_t s) {
   k_tracker_g2p<<<d.num_sms * 4, 128, 0, s>>>(d);
+}
+
+void launch_cloth_beta(const DevPtrs &d, float dt, int collider, cudaStream_t s) {
+  cudaMemsetAsync(d.cloth.vowner, 0xff, (size_t)d.cloth.n_verts * sizeof(int32_t), s);  // -1
+  k_cloth_beta_owner<<<d.num_sms * 4, 128, 0, s>>>(d);
+  k_cloth_beta<<<d.num_sms * 4, 128, 0, s>>>(d, dt, collider);
 }
 
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {

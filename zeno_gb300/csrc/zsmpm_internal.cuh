@@ -162,6 +162,8 @@ struct ClothDev {
   float gamma, k, fc, dc;    // shear stiffness, normal stiffness, tan(fa / pi), damping
   float *vx, *vv, *vC, *vm;
   float *imp;  // per vertex (x, y, z, unused): the impulse sums of a P2G
+  float *vbeta;     // ComputeParticleBeta per vertex (FLIP-style position update)
+  int32_t *vowner;  // scratch of the beta pass: the last element of each vertex
   float *ex, *ev, *eC, *eF, *ed, *eDmInv, *em, *evol, *emu, *elam;
   int32_t *inds;
   // vertex bending springs (ConstructBendingSprings "vertex"): vertex pairs,
@@ -251,6 +253,8 @@ void launch_particle_beta(const DevPtrs &d, int cur, float dt, int collider, cud
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s);
 void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s);
 void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s);
+// ComputeParticleBeta on the cloth's vertices (triangle meshes)
+void launch_cloth_beta(const DevPtrs &d, float dt, int collider, cudaStream_t s);
 void launch_tracker_mark(const DevPtrs &d, cudaStream_t s);
 void launch_tracker_g2p(const DevPtrs &d, cudaStream_t s);
 

@@ -251,6 +251,18 @@ class Context:
                                                   C.byref(n)), "mpm_cloth_add_bending")
         return int(n.value)
 
+    def cloth_beta(self) -> np.ndarray:
+        """The cloth vertices' beta (ComputeParticleBeta on the cloth)."""
+        out = np.empty(self._cloth_n[0], np.float32)
+        self._check(self._L.mpm_particles_get_attr(self.h, b"cloth_beta", _p(out)),
+                    "mpm_particles_get_attr")
+        return out
+
+    def set_cloth_beta(self, values):
+        vals = _f32(values, (self._cloth_n[0],))
+        self._check(self._L.mpm_particles_set_attr(self.h, b"cloth_beta", _p(vals)),
+                    "mpm_particles_set_attr")
+
     def add_trackers(self, x, v=None):
         """ToTrackerParticles: points advected by the grid in every substep."""
         x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
