@@ -197,15 +197,15 @@ def batched_form(zsmpm, steps: int, dev: int):
     ms_b = e0.elapsed_time(e1)
     ctx.sync()
     st = ctx.stats()
-    # sample for the parity check of the cpu_baseline leg: scenes 0 and 1
-    # after 20 substeps of the batch
+    # sample for the parity check of the cpu_baseline leg: scenes 0-7 after
+    # 20 substeps of the batch
     check_steps = 20
     ctx.upload_batch(parts, offs)
     ctx.substep(dt, check_steps)
     out = ctx.download(("x", "v"))
     ctx.close()
     check = [(pairs[k][0], pairs[k][1], out["x"][offs[k]:offs[k + 1]],
-              out["v"][offs[k]:offs[k + 1]]) for k in (0, 1)]
+              out["v"][offs[k]:offs[k + 1]]) for k in range(min(8, len(pairs)))]
     # the same scenes, each on its own plain context, one after another
     ctxs = []
     for scene, p in pairs:
@@ -599,6 +599,16 @@ def cpu_baseline(parts, scene, checks=None, target_s: float = 10.0):
     oracle.build()
     parity = {}
     for name, (sc, pt, steps, gx, gv) in (checks or {}).items():
+        if isinstance(steps, (tuple, list)):  # checkpoints: the error's growth
+            growth, ref, done = [], pt, 0
+            for k, x_k, v_k in zip(steps, gx, gv):
+                ref, st = oracle.run(sc, ref, k - done, "f64")
+                done = k
+                growth.append({"substeps": k, "rel_l2_x": rel_l2(x_k, ref.x),
+                               "rel_l2_v": rel_l2(v_k, ref.v)})
+            parity[name] = dict(growth[-1], particles=int(pt.n), reference="FP64 oracle",
+                                oracle_status=st["status"], growth=growth)
+            continue
         ref, st = oracle.run(sc, pt, steps, "f64")
         parity[name] = {"rel_l2_x": rel_l2(gx, ref.x), "rel_l2_v": rel_l2(gv, ref.v),
                         "substeps": steps, "particles": int(pt.n), "reference": "FP64 oracle",
@@ -684,12 +694,17 @@ def run_gpu(args):
     dt = scene.dt
     from zeno_gb300 import autotune
     tuned = autotune.tune(ctx, dt, state=lambda: ctx.upload(parts))
-    # sample for the parity check of the cpu_baseline leg: 3 substeps from the
-    # initial state
-    check_steps = 3
+    # sample for the parity check of the cpu_baseline leg: 100 substeps from
+    # the initial state, with the state at 1 and 10 substeps on the way
+    check_steps = (1, 10, 100)
     ctx.upload(parts)
-    ctx.substep(dt, check_steps)
-    plain_out = ctx.download(("x", "v"))
+    check_x, check_v, done = [], [], 0
+    for k in check_steps:
+        ctx.substep(dt, k - done)
+        done = k
+        o = ctx.download(("x", "v"))
+        check_x.append(o["x"])
+        check_v.append(o["v"])
     ctx.upload(parts)
 
     # warm-up (captures both graph parities)
@@ -841,7 +856,7 @@ def run_gpu(args):
             pg.barrier()
             pg.destroy_process_group()
         return 0
-    checks = {"plain": (scene, parts, check_steps, plain_out["x"], plain_out["v"])}
+    checks = {"plain": (scene, parts, check_steps, check_x, check_v)}
     for name in ("flip", "aflip"):
         tchk = forms.get(name, {}).pop("_check", None)
         if tchk:

@@ -413,9 +413,13 @@ int32_t mpm_grid_download(mpm_ctx *ctx, float *nodes, int64_t cap_floats);
  * Its scratch is one file-scope device array of 32 MiB that every GPU loading
  * the library holds until the process exits; sizes above
  * ZSMPM_NOALLOC_MAX_PARTICLES particles or ZSMPM_NOALLOC_MAX_BLOCKS directory
- * blocks are rejected with MPM_ERR_CAPACITY.  The first call on a device sets
- * up that device's scratch address (make it before any stream capture).
- * Calls share the scratch: calls that overlap on the GPU race. */
+ * blocks are rejected with MPM_ERR_CAPACITY (each block_dims entry is checked
+ * on its own, so a product that would overflow is rejected too).  The first
+ * call on a device sets up that device's scratch address (make it before any
+ * stream capture); the address is not valid after cudaDeviceReset.  If cap_pb
+ * is below the number of non-empty blocks the call returns MPM_ERR_CAPACITY
+ * with *n_pb set to that number.  Calls share the scratch: calls that overlap
+ * on the GPU race. */
 #define ZSMPM_NOALLOC_MAX_PARTICLES (1 << 20)
 #define ZSMPM_NOALLOC_MAX_BLOCKS (1 << 19)
 int32_t mpm_partition_noalloc(const float *x_planes, int64_t n, float dx,

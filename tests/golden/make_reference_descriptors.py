@@ -1,18 +1,20 @@
 """Extract the ZENDEFNODE descriptors of the reference MPM nodes.
 
-Reads the reference sources (zenustech/zeno, checked out at
-/root/reference) and writes reference_node_descriptors.json next to this
-script: {node: {"inputs": [[type, name, default], ...], "outputs": ...,
-"params": ..., "categories": [...]}}.  Run once where the reference is
-present; the JSON is the committed fixture the node tests compare against.
+Reads the reference sources (a zenustech/zeno checkout, given as the first
+argument or by the ZENO_REFERENCE environment variable) and writes
+reference_node_descriptors.json next to this script: {node: {"inputs":
+[[type, name, default], ...], "outputs": ..., "params": ..., "categories":
+[...]}}.  Run once where the reference is present; the JSON is the committed
+fixture the node tests compare against.
 """
 import json
 import os
 import re
 import sys
 
-REF_DEFAULT = "/root/reference"
-REF = sys.argv[1] if len(sys.argv) > 1 else REF_DEFAULT
+# the zeno checkout to read, or None (then the scripts and tests that need
+# it are skipped)
+REF_DEFAULT = os.environ.get("ZENO_REFERENCE")
 FILES = ["projects/CuLagrange/mpm/Generation.cu", "projects/CuLagrange/mpm/Generation.cpp",
          "projects/CuLagrange/mpm/MPMPipeline.cu", "projects/CuLagrange/mpm/Transfer.cu",
          "projects/CuLagrange/mpm/Boundary.cu", "projects/CuLagrange/mpm/Temp.cu"]
@@ -55,6 +57,9 @@ def socket(x):
 
 
 def main():
+    REF = sys.argv[1] if len(sys.argv) > 1 else REF_DEFAULT
+    if not REF:
+        sys.exit("give the zeno checkout as the first argument or in ZENO_REFERENCE")
     found = {}
     for f in FILES:
         src = open(os.path.join(REF, f)).read()

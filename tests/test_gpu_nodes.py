@@ -120,3 +120,27 @@ def test_update_primitive_attr(zsmpm_mod, attr):
         np.testing.assert_allclose(a, parts.m, rtol=1e-6)
     else:
         assert 0.9 < a.min() <= a.max() < 1.1 and a.std() > 0
+
+
+def test_node_graph_sand_friction_angle_from_params(zsmpm_mod, oracle_mod):
+    """A Drucker-Prager sand block thrown at the floor, configured the way a
+    zeno graph does it: ConfigConstitutiveModel plasticity=nadp with
+    params={friction_angle: 30}.  It must match the oracle at 30 degrees;
+    at the 35-degree default the motion is measurably different."""
+    def sand(fa):
+        scene, parts = S.jelly_cube(cells=8)
+        scene.materials = [S.Material(S.STVK, E=5e4, nu=0.3, plasticity=S.PLASTIC_NADP,
+                                      friction_angle_deg=fa)]
+        parts.x[:, 1] -= 0.29
+        parts.v[:] = np.array([0.8, -3.0, 0.0], np.float32)
+        return scene, parts
+    steps = 150
+    scene, parts = sand(30.0)
+    x, v, _ = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "stvk", plasticity="nadp",
+                                       E=5e4, nu=0.3, substeps=steps, bc="sticky", thickness=3,
+                                       params={"friction_angle": 30.0})
+    ref, st = oracle_mod.run(scene, parts, steps, "f64")
+    assert st["status"] == 0
+    assert rel_l2(x, ref.x) < 1e-4 and rel_l2(v, ref.v) < 1e-4
+    ref35, _ = oracle_mod.run(*sand(35.0), steps, "f64")
+    assert rel_l2(v, ref35.v) > 1e-2

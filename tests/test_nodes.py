@@ -5,6 +5,7 @@ make_reference_descriptors.py from the reference sources)."""
 import json
 import os
 
+import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -67,9 +68,10 @@ def test_node_file_compiles_against_zeno_headers():
     import shutil
     import subprocess
     from .golden.make_reference_descriptors import REF_DEFAULT
-    zeno_inc = os.environ.get("ZENO_INCLUDE", os.path.join(REF_DEFAULT, "zeno", "include"))
-    if not os.path.isdir(zeno_inc):
-        pytest.skip("zeno headers not present")
+    zeno_inc = os.environ.get("ZENO_INCLUDE") or (
+        os.path.join(REF_DEFAULT, "zeno", "include") if REF_DEFAULT else None)
+    if not zeno_inc or not os.path.isdir(zeno_inc):
+        pytest.skip("zeno headers not given (ZENO_INCLUDE or ZENO_REFERENCE)")
     root = os.path.dirname(HERE)
     cxx = shutil.which("g++") or "g++"
     r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-DZSMPM_WITH_ZENO", "-I", zeno_inc,
@@ -77,3 +79,34 @@ def test_node_file_compiles_against_zeno_headers():
                         os.path.join(root, "zeno_gb300", "nodes", "MPMNodes.cpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+# ConfigConstitutiveModel's meaning, not only its sockets: the "params" dict
+# (Generation.cu:32,53-58) is read where the reference reads it.
+MPM_FCR, MPM_NHK, MPM_STVK, MPM_EOS = 0, 1, 2, 3
+MPM_PLASTIC_NONE, MPM_PLASTIC_NADP = 0, 1
+
+
+def test_config_model_reads_friction_angle_from_params(zsmpm_mod):
+    m, vol = zsmpm_mod.config_model("stvk", "nadp", E=1e5, nu=0.3, dx=1.0 / 256, ppc=8.0,
+                                    params={"friction_angle": 30.0})
+    assert m["plasticity"] == MPM_PLASTIC_NADP and m["type"] == MPM_STVK
+    assert m["friction_angle_deg"] == 30.0
+    assert vol == np.float32((1.0 / 256) ** 3 / 8.0)
+    # no params: the reference default of 35 degrees (Generation.cu:70)
+    m, _ = zsmpm_mod.config_model("fcr", "nadp", E=1e5, nu=0.3)
+    assert m["friction_angle_deg"] == 35.0 and m["type"] == MPM_STVK
+
+
+def test_config_model_params_of_other_models(zsmpm_mod):
+    # the fluid extension takes its bulk modulus and exponent from params
+    m, _ = zsmpm_mod.config_model("eos", "none", params={"bulk": 2e4, "gamma": 5.0})
+    assert m["type"] == MPM_EOS and m["bulk"] == 2e4 and m["gamma"] == 5.0
+    m, _ = zsmpm_mod.config_model("nhk", "none", E=5e4, nu=0.3, params={"friction_angle": 20.0})
+    assert m["type"] == MPM_NHK and m["plasticity"] == MPM_PLASTIC_NONE
+    assert m["E"] == 5e4 and m["nu"] == np.float32(0.3)
+
+
+def test_config_model_rejects_unknown_model(zsmpm_mod):
+    with pytest.raises(RuntimeError, match="unrecognized"):
+        zsmpm_mod.config_model("bogus")

@@ -276,16 +276,22 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
     if (sd.boundary.type < MPM_BC_NONE || sd.boundary.type > MPM_BC_SEPARATE ||
         sd.boundary.thickness < 0)
       return fail(MPM_ERR_INVALID, "bad boundary");
+    // each factor and each partial product is bounded before the next
+    // multiplication, so the directory size cannot wrap around
     long long nd = 1;
     for (int k = 0; k < 3; ++k) {
       if (sd.block_dims[k] < 3) return fail(MPM_ERR_INVALID, "block_dims must be >= 3");
+      if (sd.block_lo[k] < -kMaxBlockCoord || sd.block_lo[k] > kMaxBlockCoord - sd.block_dims[k])
+        return fail(MPM_ERR_INVALID, "block_lo + block_dims outside +-2^27 blocks");
       nd *= sd.block_dims[k];
+      if (nd >= kMaxDirBlocks)
+        return fail(MPM_ERR_INVALID, "block directory larger than 2^25 blocks");
     }
     sp[s] = scene_from(sd);
     sp[s].dir_off = (int)std::min<long long>(ndir, 1ll << 30);
     ndir += nd;
+    if (ndir >= kMaxDirBlocks) return fail(MPM_ERR_INVALID, "block directory larger than 2^25 blocks");
   }
-  if (ndir >= (1ll << 25)) return fail(MPM_ERR_INVALID, "block directory larger than 2^25 blocks");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
     return fail(MPM_ERR_NO_DEVICE, "no CUDA device");

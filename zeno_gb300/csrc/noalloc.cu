@@ -14,6 +14,9 @@
 // the device address of the array with cudaGetSymbolAddress -- host code
 // cannot use the symbol itself, which names a host-side stand-in -- and
 // caches it per device.  Make that first call before any stream capture.
+// The cached address belongs to the device's primary context: after
+// cudaDeviceReset (or any teardown of that context) it is stale, so a process
+// that resets a device must not call this entry point on it again.
 //
 // Every call shares the one array and leaves its contents behind; each call
 // clears the parts that must start at zero.  Calls that overlap on the GPU
@@ -131,14 +134,18 @@ extern "C" int32_t mpm_partition_noalloc(const float *x_planes, int64_t n, float
   if (n > kNoAllocMaxParticles)
     return fail(MPM_ERR_CAPACITY, "mpm_partition_noalloc takes at most " +
                                       std::to_string(kNoAllocMaxParticles) + " particles");
+  // each factor and each partial product is bounded before the next
+  // multiplication, so the directory size cannot wrap around
   long long ndir = 1;
   for (int k = 0; k < 3; ++k) {
     if (block_dims[k] < 3) return fail(MPM_ERR_INVALID, "block_dims must be >= 3");
+    if (block_lo[k] < -kMaxBlockCoord || block_lo[k] > kMaxBlockCoord - block_dims[k])
+      return fail(MPM_ERR_INVALID, "block_lo + block_dims outside +-2^27 blocks");
     ndir *= block_dims[k];
+    if (ndir > kNoAllocMaxBlocks)
+      return fail(MPM_ERR_CAPACITY, "mpm_partition_noalloc takes a block directory of at most " +
+                                        std::to_string(kNoAllocMaxBlocks) + " blocks");
   }
-  if (ndir > kNoAllocMaxBlocks)
-    return fail(MPM_ERR_CAPACITY, "mpm_partition_noalloc takes a block directory of at most " +
-                                      std::to_string(kNoAllocMaxBlocks) + " blocks");
   DeviceScratch sc;
   int32_t rc = scratch_for_current_device(sc);
   if (rc) return rc;

@@ -70,6 +70,13 @@ enum : int {
   ST_MATERIAL = 64  // a material id of an asynchronous upload out of range
 };
 
+// block coordinates (and so node indices, 4 per block) stay inside +-2^27
+// blocks, which keeps every node index of a domain an int32
+constexpr int kMaxBlockCoord = 1 << 27;
+// directory entries of one context (all scenes); key = (entry << 6) | cell
+// must stay an int32
+constexpr long long kMaxDirBlocks = 1ll << 25;
+
 constexpr int kMaxMaterials = 256;
 constexpr int kMaxScenes = 4096;
 constexpr int kScanTile = 512;        // directory entries per scan tile

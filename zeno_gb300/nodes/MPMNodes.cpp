@@ -21,6 +21,7 @@
 #ifdef ZSMPM_WITH_ZENO
 // inside zeno: the real node API (projects/CuLagrange/CMakeLists.txt adds
 // this file to the zeno target)
+#include <zeno/types/DictObject.h>
 #include <zeno/types/NumericObject.h>
 #include <zeno/types/PrimitiveObject.h>
 #include <zeno/types/StringObject.h>
@@ -112,6 +113,17 @@ struct ZenoConstitutiveModel : IObject {
   mpm_material mat{};
   float dx = 0.1f, volume = 0.0f, density = 1000.0f;
 };
+
+// The material and particle volume a ZSModel object carries (false: the
+// object is not a ZSModel); lets a host inspect what ConfigConstitutiveModel
+// made of its inputs.
+bool zsmodel_material(const zany &obj, mpm_material *mat, float *volume) {
+  auto m = std::dynamic_pointer_cast<ZenoConstitutiveModel>(obj);
+  if (!m) return false;
+  if (mat) *mat = m->mat;
+  if (volume) *volume = m->volume;
+  return true;
+}
 
 // ToZSParticles output (Structures.hpp:134-531)
 struct ZenoParticles : IObject {
@@ -365,13 +377,22 @@ struct ConfigConstitutiveModel : INode {
     m.E = get_input2<float>("E");
     m.nu = get_input2<float>("nu");
     m.density = out->density;
+    // the "params" dict (Generation.cu:32,53-58): optional numbers by key,
+    // read where the reference reads them; the equation-of-state fluid (an
+    // extension of this backend) takes its bulk modulus and exponent there too
+    auto params = has_input("params") ? get_input<DictObject>("params") : std::make_shared<DictObject>();
+    auto get_arg = [&params](const char *tag, float defl) {
+      auto it = params->lut.find(tag);
+      if (it == params->lut.end()) return defl;
+      auto num = std::dynamic_pointer_cast<NumericObject>(it->second);
+      if (!num)
+        throw std::runtime_error(std::string("ConfigConstitutiveModel: params[\"") + tag +
+                                 "\"] is not a number");
+      return num->get<float>();
+    };
     m.friction_angle_deg = 35.0f;  // reference default (Generation.cu:70)
-    m.bulk = 1e4f;
-    m.gamma = 7.0f;
-    if (has_input<NumericObject>("friction_angle"))
-      m.friction_angle_deg = get_input<NumericObject>("friction_angle")->get<float>();
-    if (has_input<NumericObject>("bulk")) m.bulk = get_input<NumericObject>("bulk")->get<float>();
-    if (has_input<NumericObject>("gamma")) m.gamma = get_input<NumericObject>("gamma")->get<float>();
+    m.bulk = get_arg("bulk", 1e4f);
+    m.gamma = get_arg("gamma", 7.0f);
     const std::string type = get_input2<std::string>("type");
     if (type == "fcr")
       m.type = MPM_FCR;
@@ -389,6 +410,7 @@ struct ConfigConstitutiveModel : INode {
     if (plastic == "nadp") {
       m.type = MPM_STVK;  // plasticity runs on StvkWithHencky (Generation.cu:66-70)
       m.plasticity = MPM_PLASTIC_NADP;
+      m.friction_angle_deg = get_arg("friction_angle", 35.0f);  // Generation.cu:69-70
     } else if (plastic == "none") {
       m.plasticity = MPM_PLASTIC_NONE;
     } else {

@@ -14,6 +14,10 @@
 
 #include "zeno_api.hpp"
 
+namespace zeno {
+bool zsmodel_material(const zany &obj, mpm_material *mat, float *volume);
+}
+
 namespace {
 
 std::string esc(const std::string &s) {
@@ -71,6 +75,48 @@ int32_t zsn_descriptors_json(char *buf, int64_t cap) {
   return copy_out(os.str(), buf, cap);
 }
 
+// One ConfigConstitutiveModel node (dx, ppc, density, type, aniso,
+// plasticity, E, nu and a "params" dict given as "key=value;key=value")
+// applied through the graph; returns the material and particle volume its
+// ZSModel carries, or -1 with the node's error text in err.
+int32_t zsn_config_model(float dx, float ppc, float density, const char *type, const char *aniso,
+                         const char *plasticity, float E, float nu, const char *params,
+                         mpm_material *out, float *out_volume, char *err, int64_t err_cap) {
+  using namespace zeno;
+  try {
+    Graph g;
+    auto num = [](float v) { return std::make_shared<NumericObject>(v); };
+    auto str = [](const char *v) { return std::make_shared<StringObject>(v); };
+    g.addNode("ConfigConstitutiveModel", "model");
+    g.setNodeInput("model", "dx", num(dx));
+    g.setNodeInput("model", "ppc", num(ppc));
+    g.setNodeInput("model", "density", num(density));
+    g.setNodeInput("model", "type", str(type));
+    g.setNodeInput("model", "aniso", str(aniso));
+    g.setNodeInput("model", "plasticity", str(plasticity));
+    g.setNodeInput("model", "E", num(E));
+    g.setNodeInput("model", "nu", num(nu));
+    if (params && params[0]) {
+      auto dict = std::make_shared<DictObject>();
+      std::istringstream ps(params);
+      std::string item;
+      while (std::getline(ps, item, ';')) {
+        const size_t eq = item.find('=');
+        if (eq == std::string::npos) continue;
+        dict->lut[item.substr(0, eq)] = num(std::stof(item.substr(eq + 1)));
+      }
+      g.setNodeInput("model", "params", dict);
+    }
+    g.applyNodes({"model"});
+    if (!zsmodel_material(g.getNodeOutput("model", "ZSModel"), out, out_volume))
+      throw std::runtime_error("ConfigConstitutiveModel did not output a ZSModel");
+    return 0;
+  } catch (const std::exception &e) {
+    copy_out(e.what(), err, err_cap);
+    return -1;
+  }
+}
+
 // Runs `substeps` substeps of one particle set through the node graph
 // (fused = 0: the reference's node sequence per substep; fused = 1: one
 // ZSMPMSubstep node) and returns x, v (n x 3) and the last MaxVelSqr.
@@ -86,7 +132,7 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       int64_t tracker_n, const float *tracker_x, float *tracker_out_x,
                       float *tracker_out_v, const char *write_path, const char *bending_type,
                       float bending_stiffness, const char *attr_name, int32_t attr_dim,
-                      float *attr_out) {
+                      float *attr_out, const char *model_params) {
   using namespace zeno;
   try {
     Graph g;
@@ -112,6 +158,19 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
     g.setNodeInput("model", "plasticity", str(plasticity));
     g.setNodeInput("model", "E", num(E));
     g.setNodeInput("model", "nu", num(nu));
+    // ConfigConstitutiveModel "params": "key=value;key=value" as a DictObject
+    // of NumericObjects, the way a zeno graph feeds that socket
+    if (model_params && model_params[0]) {
+      auto dict = std::make_shared<DictObject>();
+      std::istringstream ps(model_params);
+      std::string item;
+      while (std::getline(ps, item, ';')) {
+        const size_t eq = item.find('=');
+        if (eq == std::string::npos) continue;
+        dict->lut[item.substr(0, eq)] = num(std::stof(item.substr(eq + 1)));
+      }
+      g.setNodeInput("model", "params", dict);
+    }
     g.addNode("ToZSParticles", "pars");
     g.bindNodeInput("pars", "ZSModel", "model", "ZSModel");
     g.setNodeInput("pars", "prim", prim);

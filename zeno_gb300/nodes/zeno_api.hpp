@@ -2,7 +2,8 @@
 // written against, so the node wrappers compile and run headless without
 // the rest of zeno:
 //   IObject / zany                 zeno/include/zeno/core/IObject.h:89
-//   NumericObject, PrimitiveObject zeno/include/zeno/types/*.h
+//   NumericObject, DictObject,
+//   PrimitiveObject                zeno/include/zeno/types/*.h
 //   INode (get_input, get_input2, has_input, set_output, get_param)
 //                                  zeno/include/zeno/core/INode.h:23-127
 //   Descriptor + ZENDEFNODE        zeno/include/zeno/core/Descriptor.h, defNode.h:16-34
@@ -52,6 +53,12 @@ struct NumericObject : IObject {
     }
   }
   template <class T> void set(T v) { value = v; }
+};
+
+// DictObject: named objects (zeno/include/zeno/types/DictObject.h:11-31);
+// ConfigConstitutiveModel's "params" holds NumericObjects by key
+struct DictObject : IObject {
+  std::map<std::string, zany> lut;
 };
 
 struct StringObject : IObject {

@@ -653,8 +653,13 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_int32, C.c_float, C.c_float, C.c_int32, P, P, P,
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
                                 C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P,
-                                C.c_char_p, C.c_char_p, C.c_float, C.c_char_p, C.c_int32, P]
+                                C.c_char_p, C.c_char_p, C.c_float, C.c_char_p, C.c_int32, P,
+                                C.c_char_p]
     L.zsn_run_graph.restype = C.c_int32
+    L.zsn_config_model.argtypes = [C.c_float, C.c_float, C.c_float, C.c_char_p, C.c_char_p,
+                                   C.c_char_p, C.c_float, C.c_float, C.c_char_p,
+                                   C.POINTER(Material), P, C.c_char_p, C.c_int64]
+    L.zsn_config_model.restype = C.c_int32
     _nodes = L
     return L
 
@@ -672,10 +677,27 @@ def node_descriptors() -> dict:
         cap = 2 * n
 
 
+def config_model(type="fcr", plasticity="none", aniso="none", E=1e4, nu=0.4, dx=0.1, ppc=8.0,
+                 density=1000.0, params=None):
+    """Apply one ConfigConstitutiveModel node (params: its "params" dict,
+    {key: number}); returns (mpm_material fields as a dict, particle volume).
+    Runs on the host only: the node makes no device call."""
+    L = load_nodes()
+    mat = Material()
+    vol = np.zeros(1, np.float32)
+    err = C.create_string_buffer(1024)
+    ptxt = ";".join(f"{k}={float(v)!r}" for k, v in (params or {}).items()).encode()
+    rc = L.zsn_config_model(dx, ppc, density, type.encode(), aniso.encode(), plasticity.encode(),
+                            E, nu, ptxt, C.byref(mat), _p(vol), err, 1024)
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return {k: getattr(mat, k) for k, _ in Material._fields_}, float(vol[0])
+
+
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
                    fused=False, levelset=None, transfer="apic", cloth=None, trackers=None,
-                   write_path=None, bending=None, attr=None):
+                   write_path=None, bending=None, attr=None, params=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -692,7 +714,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     and WriteZSParticles to this .geo file.  bending: (type, stiffness) of a
     ConstructBendingSprings on the cloth, fed to the ZSBending inputs.  attr:
     (name, width) of an UpdatePrimitiveAttrFromZSParticles after the
-    substeps; the attribute's values are appended to the return value."""
+    substeps; the attribute's values are appended to the return value.
+    params: ConfigConstitutiveModel's "params" dict ({key: number}), e.g.
+    {"friction_angle": 30.0} for Drucker-Prager sand."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -740,7 +764,8 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
                          bending[0].encode() if bending else None,
                          float(bending[1]) if bending else 0.0,
                          attr[0].encode() if attr else None, int(attr[1]) if attr else 0,
-                         _p(aout))
+                         _p(aout),
+                         ";".join(f"{k}={float(v)!r}" for k, v in (params or {}).items()).encode())
     if rc != 0:
         raise RuntimeError(err.value.decode())
     out = (ox, ov, float(vmax[0]))
