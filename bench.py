@@ -583,6 +583,44 @@ def sand_form(zsmpm, dev: int, steps: int = 128, ckpt: int = 8):
             "checkpoint_bytes": sim.peak_checkpoint_bytes, "plain_status": st["status"]}
 
 
+def diff_profile(kind: str, dev: int):
+    """One forward + backward of a differentiable rollout, for profiling:
+    'fwd_bwd' is the 65,536-particle fixed-corotated rollout (64 substeps,
+    checkpoint every 16); 'sand' is the sand column cut to 128 x 32 x 64 cells
+    (2,097,152 particles, dx = 1/512), 16 substeps, recompute every 8.  One
+    untimed pass, then one timed pass; prints one JSON line."""
+    import torch
+    from zeno_gb300 import diff, scenes
+    if kind == "sand":
+        scene, parts = scenes.sand_column(cells=(128, 32, 64))
+        v0 = scenes.sand_velocity(parts.n)
+        E = np.full(parts.n, float(scene.materials[0].E))
+        steps, ckpt = 16, 8
+    else:
+        scene, parts = scenes.diff_scene()
+        E = parts.mu.astype(np.float64) * 2.0 * (1.0 + scene.materials[0].nu)
+        v0 = scenes.diff_velocity(parts.n)
+        steps, ckpt = 64, 16
+    sim = diff.Rollout(scene, parts, steps, ckpt, device=dev)
+
+    def fwd_bwd():
+        v = torch.tensor(v0, dtype=torch.float32, device="cuda", requires_grad=True)
+        e = torch.tensor(E, dtype=torch.float64, device="cuda", requires_grad=True)
+        diff.com_loss(sim.rollout(v, e), (0.7, 0.5, 0.5)).backward()
+        return v.grad
+
+    fwd_bwd()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = fwd_bwd()
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0)
+    print(json.dumps({"diff_profile": kind, "particles": parts.n, "substeps": steps,
+                      "ckpt": ckpt, "ms_fwd_bwd": ms,
+                      "grad_finite": bool(torch.isfinite(g).all())}))
+    return 0
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
@@ -926,7 +964,13 @@ def main():
                     help="device timing only (no clock sampling, e2e or CPU legs): for ncu")
     ap.add_argument("--transfer", default="apic", choices=["apic", "flip", "aflip"],
                     help="grid transfer of the --quick run (profiling the FLIP kernels)")
+    ap.add_argument("--diff-profile", default=None, choices=["fwd_bwd", "sand"],
+                    help="run one forward + backward of a differentiable rollout only: for ncu")
     args = ap.parse_args()
+    if args.diff_profile:
+        import torch
+        torch.cuda.set_device(0)
+        return diff_profile(args.diff_profile, 0)
     if args.transfer != "apic" and not args.quick:
         ap.error("--transfer applies to --quick runs; the headline is the APIC substep")
     if args.warmup < 3:

@@ -16,13 +16,21 @@ pytestmark = pytest.mark.gpu
 TARGET = np.array([0.7, 0.5, 0.5])
 
 
+def _directions(n, k):
+    """k-th direction of the directional checks: dv (n x 3) for v0 and
+    relative factors rE in [0.5, 1.5] for E, from independent seeds."""
+    base = [[1.0, 0.5, -0.3], [-0.4, 1.0, 0.6], [0.7, -0.8, 1.0]][k % 3]
+    dv = np.tile([base], (n, 1)) + 0.5 * S.normal(5 + 10 * k, 0, n * 3).reshape(-1, 3)
+    rE = 0.5 + S.uniform(6 + 10 * k, 0, n)
+    return dv, rE
+
+
 def _problem(cells=(16, 8, 8)):
     scene, parts = S.diff_scene(cells=cells)
     nu = scene.materials[0].nu
     E = parts.mu.astype(np.float64) * 2.0 * (1.0 + nu)
     v0 = S.diff_velocity(parts.n)
-    dv = np.tile([[1.0, 0.5, -0.3]], (parts.n, 1)) + 0.5 * S.normal(5, 0, parts.n * 3).reshape(-1, 3)
-    rE = 0.5 + S.uniform(6, 0, parts.n)
+    dv, rE = _directions(parts.n, 0)
     return scene, parts, E, v0, dv, rE
 
 
@@ -56,8 +64,11 @@ def _oracle_loss(oracle_mod, scene, parts, v0, E, steps):
     return float(((out.x.mean(axis=0) - TARGET) ** 2).sum())
 
 
-def test_gradients_against_fp32_finite_differences(zsmpm_mod):
-    scene, parts, E, v0, dv, rE = _problem()
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_gradients_against_fp32_finite_differences(zsmpm_mod, k):
+    """Three independent directions of v0 and of E."""
+    scene, parts, E, v0, _, _ = _problem()
+    dv, rE = _directions(parts.n, k)
     steps = 64
     sim, L, gv, gE = _gpu_grads(scene, parts, E, v0, steps, 16)
     h = 1e-3
@@ -70,8 +81,12 @@ def test_gradients_against_fp32_finite_differences(zsmpm_mod):
     assert abs(ad_E - fd_E) <= 5e-2 * abs(fd_E) + 1e-12, (ad_E, fd_E)
 
 
-def test_gradients_against_fp64_reference(zsmpm_mod, oracle_mod):
-    scene, parts, E, v0, dv, rE = _problem()
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_gradients_against_fp64_reference(zsmpm_mod, oracle_mod, k):
+    """Three independent directions of v0 and of E against central
+    differences of the FP64 oracle."""
+    scene, parts, E, v0, _, _ = _problem()
+    dv, rE = _directions(parts.n, k)
     steps = 64
     _, L, gv, gE = _gpu_grads(scene, parts, E, v0, steps, 16)
     h = 1e-6
@@ -83,6 +98,52 @@ def test_gradients_against_fp64_reference(zsmpm_mod, oracle_mod):
              _oracle_loss(oracle_mod, scene, parts, v0, E * (1 - h * rE), steps)) / (2 * h)
     ad_E = float((gE * E * rE).sum())
     assert abs(ad_E - ref_E) <= 1e-2 * abs(ref_E) + 1e-12, (ad_E, ref_E)
+
+
+def _entries(n, count=16):
+    """(particle, component) entries spread over the particle index range."""
+    idx = np.linspace(0, n - 1, count).round().astype(int)
+    return idx, np.arange(count) % 3
+
+
+def test_per_entry_gradients_against_fp64_reference(zsmpm_mod, oracle_mod):
+    """The gradient entry by entry: 16 (particle, component) entries of v0
+    and the E of 16 particles, each against a central difference of the FP64
+    oracle on that single entry (v0: h = 3e-4 absolute; E: h = 1e-4
+    relative; at these steps the FP64 differences agree with steps 3x
+    larger and smaller to ~1e-5).  Tolerance per entry: 1e-3 of the entry
+    for v0, 1e-2 for E (entries below 10 % of the largest sampled one are
+    held to the same bound relative to that 10 % floor)."""
+    scene, parts, E, v0, _, _ = _problem()
+    steps = 64
+    _, _, gv, gE = _gpu_grads(scene, parts, E, v0, steps, 16)
+    idx, comp = _entries(parts.n)
+    ref_v = []
+    h = 3e-4
+    for i, c in zip(idx, comp):
+        vp, vm = v0.copy(), v0.copy()
+        vp[i, c] += h
+        vm[i, c] -= h
+        ref_v.append((_oracle_loss(oracle_mod, scene, parts, vp, E, steps) -
+                      _oracle_loss(oracle_mod, scene, parts, vm, E, steps)) / (2 * h))
+    ref_v = np.array(ref_v)
+    ad_v = gv[idx, comp]
+    floor_v = 0.1 * np.abs(ref_v).max()
+    err_v = np.abs(ad_v - ref_v) / np.maximum(np.abs(ref_v), floor_v)
+    assert err_v.max() <= 1e-3, (err_v, ad_v, ref_v)
+    ref_E = []
+    h = 1e-4
+    for i in idx:
+        Ep, Em = E.copy(), E.copy()
+        Ep[i] *= 1 + h
+        Em[i] *= 1 - h
+        ref_E.append((_oracle_loss(oracle_mod, scene, parts, v0, Ep, steps) -
+                      _oracle_loss(oracle_mod, scene, parts, v0, Em, steps)) / (2 * h * E[i]))
+    ref_E = np.array(ref_E)
+    ad_E = gE[idx]
+    floor_E = 0.1 * np.abs(ref_E).max()
+    err_E = np.abs(ad_E - ref_E) / np.maximum(np.abs(ref_E), floor_E)
+    assert err_E.max() <= 1e-2, (err_E, ad_E, ref_E)
 
 
 def test_checkpoint_interval_does_not_change_gradients(zsmpm_mod):

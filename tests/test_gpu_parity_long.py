@@ -81,7 +81,7 @@ def test_batched_workload_16_scenes_200_substeps(zsmpm_mod, oracle_mod):
     for the workload's 200 substeps; every scene against the oracle."""
     counts = S.batched_counts()
     order = np.argsort(counts, kind="stable")
-    pick = sorted(set(int(order[i]) for i in np.linspace(0, len(order) - 1, 16).round()))
+    pick = sorted(set(int(order[int(i)]) for i in np.linspace(0, len(order) - 1, 16).round()))
     pairs = [S.batched_scene(i, int(counts[i])) for i in pick]
     assert min(p.n for _, p in pairs) == counts.min() and max(p.n for _, p in pairs) == counts.max()
     scenes, mats, parts, offs = zsmpm_mod.concat_scenes(pairs)
