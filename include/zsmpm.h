@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define ZSMPM_ABI_VERSION 1
+#define ZSMPM_ABI_VERSION 2
 
 typedef enum mpm_status {
   MPM_OK = 0,
@@ -114,7 +114,7 @@ typedef struct mpm_collider_desc {
  * [block_lo, block_lo + block_dims) on each axis; particles must stay at
  * least one block inside it. */
 typedef struct mpm_ctx_desc {
-  int32_t device;          /* CUDA device ordinal */
+  int32_t device;          /* CUDA device ordinal (-1: the calling thread's current device) */
   float dx;                /* MakeZSGrid "dx" */
   int32_t block_lo[3];
   int32_t block_dims[3];
@@ -348,25 +348,48 @@ enum {
 int32_t mpm_substep_timed(mpm_ctx *ctx, float dt, float *stage_ms, int32_t n_stages);
 
 /* ---- differentiable form (no counterpart in the reference) ----
- * State / adjoint planes: 25 device float planes of n particles each, in
- * upload order: x (3), v (3), C (9), F (9), J (1). */
-#define MPM_STATE_PLANES 25
-/* keep = 1: G2P writes every particle back to its own slot, so the particle
- * store keeps the upload order and saved states / adjoints share it
- * (required by the calls below). */
-int32_t mpm_set_order_mode(mpm_ctx *ctx, int32_t keep_upload_order);
-/* copy the current state to / from caller device memory (checkpoints) */
+ * A state is MPM_STATE_PLANES device planes of n floats each, one entry per
+ * storage slot: x (3), v (3), C (9), F (9), J (1), m, vol, mu, lam, then the
+ * material id and the upload index as int32 bit patterns.  The substep keeps
+ * the particle store sorted by block (each substep writes the particles at
+ * their sorted positions), so the slots of consecutive states are in
+ * different orders; the upload-index plane says which particle a slot holds.
+ * A state whose upload-index plane is 0..n-1 is in upload order.  An adjoint
+ * is MPM_ADJ_PLANES planes (x, v, C, F, J) in the slot order of its state. */
+#define MPM_STATE_PLANES 31
+#define MPM_ADJ_PLANES 25
+/* on = 1: per-particle mu / lam (from the state planes), the grid buffers of
+ * the adjoint; required by the calls below.  APIC transfer, no cloth. */
+int32_t mpm_set_differentiable(mpm_ctx *ctx, int32_t on);
+/* copy the current state to / from caller device memory (checkpoints); a
+ * load replaces the particles (n stays the uploaded count) */
 int32_t mpm_state_save(mpm_ctx *ctx, float *dst_planes);
 int32_t mpm_state_load(mpm_ctx *ctx, const float *src_planes);
 /* Adjoint of the substep that advances the current state n with dt: given
- * adj_next, the adjoint planes of state n+1, writes adj_prev, the adjoint
- * planes of state n, and adds the gradients with respect to every
- * particle's mu and lam to grad_mu / grad_lam (n floats each, device).  The
- * state is not advanced.  Fixed-corotated, Neo-Hookean and StVK-Hencky
- * materials, the last with or without the Drucker-Prager projection (sand);
- * not the equation-of-state fluid (MPM_ERR_INVALID). */
+ * adj_next, the adjoint of state n+1 (slot order of state n+1), writes
+ * adj_prev, the adjoint of state n (slot order of state n), and adds the
+ * gradients with respect to every particle's mu and lam to grad_mu /
+ * grad_lam (n floats each, device, by upload index).  The state is not
+ * advanced.  Fixed-corotated, Neo-Hookean and StVK-Hencky materials, the last
+ * with or without the Drucker-Prager projection (sand); not the
+ * equation-of-state fluid (MPM_ERR_INVALID). */
 int32_t mpm_adjoint_substep(mpm_ctx *ctx, float dt, const float *adj_next, float *adj_prev,
                             float *grad_mu, float *grad_lam);
+/* Forward of a rollout with checkpoints, in one call: loads state0, runs
+ * n_substeps substeps of dt, saving the state before substep k * every into
+ * ckpts + k * MPM_STATE_PLANES * n (k = 0 .. ceil(n_substeps / every) - 1)
+ * and the final state into final_state (all device memory). */
+int32_t mpm_rollout_forward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
+                            const float *state0, float *ckpts, float *final_state);
+/* Backward of that rollout, in one call: adj holds the adjoint of the final
+ * state; the segments run last to first, each recomputed from its checkpoint
+ * into seg_states (every x MPM_STATE_PLANES x n floats) and then taken back
+ * through mpm_adjoint_substep, so that adj ends as the adjoint of state0
+ * (adj_tmp: MPM_ADJ_PLANES x n floats of scratch) and grad_mu / grad_lam
+ * (by upload index) gain the gradients of every substep. */
+int32_t mpm_rollout_backward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
+                             const float *ckpts, float *seg_states, float *adj, float *adj_tmp,
+                             float *grad_mu, float *grad_lam);
 
 /* Launch shape of the persistent kernels, chosen by the autotuner
  * (zeno_gb300/autotune.py); 0 fields take the defaults (occupancy maximum for
@@ -382,9 +405,31 @@ typedef struct mpm_launch_config {
 int32_t mpm_set_launch_config(mpm_ctx *ctx, const mpm_launch_config *cfg);
 int32_t mpm_get_launch_config(mpm_ctx *ctx, mpm_launch_config *cfg);
 
-/* Wait for the context's stream; returns the device status word. */
+/* Wait for the context's stream; returns the device status word.  With a
+ * growing directory (mpm_set_auto_regrow) a particle that left the directory
+ * is not an error: the directory grows and the halted substeps run again
+ * before this returns. */
 int32_t mpm_sync(mpm_ctx *ctx);
 int32_t mpm_get_stats(mpm_ctx *ctx, mpm_stats *out);
+
+/* Growing block directory, the counterpart of zpc's hashed block table that
+ * grows as particles occupy new blocks (projects/CUDA/Structures.hpp:535,
+ * zs::bht<int,3,int,16>; inserts at MPMPipeline.cu:75-84).  The dense
+ * directory covers a box of blocks fixed at creation; with this switched on
+ * (one-scene contexts only), a particle, cloth vertex or tracker that leaves
+ * it halts the substeps queued behind it on the device (the state stays the
+ * one after the last complete substep), and the next synchronising call
+ * (mpm_sync, mpm_get_stats, a download, any call that reads or changes the
+ * particles) recentres and enlarges the directory around the particles -- the
+ * box of their blocks plus a quarter of its extent, at least 2 blocks, on
+ * every side, up to 2^25 blocks -- reallocates it (and the grid-sized buffers
+ * if the new box needs more grid blocks), and runs the halted substeps again.
+ * Each enqueued substep then also launches one single-thread gate kernel.
+ * Off: such a particle is MPM_ERR_OUT_OF_DOMAIN. */
+int32_t mpm_set_auto_regrow(mpm_ctx *ctx, int32_t on);
+/* The directory box (in 4^3 blocks) and how many times it has grown. */
+int32_t mpm_get_domain(mpm_ctx *ctx, int32_t block_lo[3], int32_t block_dims[3],
+                       int32_t *n_regrows);
 
 /* Inspection of the last partition (bit-exact tests): sorted directory
  * index and particle count of every non-empty particle block, the particle

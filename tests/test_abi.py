@@ -25,7 +25,7 @@ def test_library_exports_every_symbol(zsmpm_mod):
 
 
 def test_abi_version(zsmpm_mod):
-    assert zsmpm_mod.load().mpm_abi_version() == 1
+    assert zsmpm_mod.load().mpm_abi_version() == 2
 
 
 def test_create_fails_cleanly_without_gb300(zsmpm_mod):

@@ -108,7 +108,7 @@ def test_cloth_rejects_differentiable_form(zsmpm_mod):
         ctx.upload(_empty())
         ctx.add_cloth(_sheet())
         with pytest.raises(zsmpm_mod.MPMError, match="cloth"):
-            ctx.set_order_mode(True)
+            ctx.set_differentiable(True)
 
 
 @pytest.mark.parametrize("fused", [False, True])

@@ -168,4 +168,4 @@ def test_differentiable_form_rejects_flip(zsmpm_mod):
     scene, parts = _thrown(tr=S.TRANSFER_FLIP)
     with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
         with pytest.raises(zsmpm_mod.MPMError, match="APIC"):
-            ctx.set_order_mode(True)
+            ctx.set_differentiable(True)

@@ -20,8 +20,10 @@
 //                   nodes: v-bar = m sum W mv-bar, A-bar = sum W mv-bar (x_i - x_p)^T,
 //                   C-bar = m A-bar, tau-bar = -dt Dinv vol A-bar through the
 //                   stress adjoint, x-bar through the weights and (x_i - x_p)
-// The particles stay in upload order in the differentiable mode, so every
-// state and adjoint array shares one indexing.
+// Every state is in its own slot order (the forward sorts the store by block
+// each substep): a particle at slot p of state n sits at its sorted position
+// sp of state n+1, so the G2P adjoint reads the next adjoint at sp and
+// writes this one at p; the mu / lam gradients go by upload index.
 #include <cuda_runtime.h>
 
 #include "binning.cuh"
@@ -87,19 +89,23 @@ __global__ void __launch_bounds__(kP2GThreads)
       const int nc = min(kP2GChunk, cnt - c0);
       __syncthreads();
       for (int j = tid; j < nc; j += kP2GThreads) {
-        const int p = d.perm[start + c0 + j];
+        // the particle's slot p in this state and its slot sp in the next
+        // (the forward G2P writes it at its sorted position)
+        const int sp = start + c0 + j;
+        const int p = d.perm[sp];
+        const int id = iin[iidx(IC_ID, p)];
         float x[3], F[9], xb[3], vb[3], Cb[9], Fb[9];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           x[k] = pin[pidx((CH_X + k), p)];
-          xb[k] = an[(AJ_X + k) * n + p];
-          vb[k] = an[(AJ_V + k) * n + p] + dt * xb[k];
+          xb[k] = an[(AJ_X + k) * n + sp];
+          vb[k] = an[(AJ_V + k) * n + sp] + dt * xb[k];
         }
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
           F[k] = pin[pidx((CH_F + k), p)];
-          Fb[k] = an[(AJ_F + k) * n + p];
-          Cb[k] = an[(AJ_C + k) * n + p];
+          Fb[k] = an[(AJ_F + k) * n + sp];
+          Cb[k] = an[(AJ_C + k) * n + sp];
         }
         const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
                        s2 = stencil1(x[2], inv_dx);
@@ -150,8 +156,8 @@ __global__ void __launch_bounds__(kP2GThreads)
           const float lam = lame ? pin[pidx(CH_LAM, p)] : mp.lam;
           float mub = 0.f, lamb = 0.f;
           dp_projection_vjp(mu, lam, mp.alpha, Ft, Fb, mub, lamb);
-          gmu[p] += mub;
-          glam[p] += lamb;
+          gmu[id] += mub;
+          glam[id] += lamb;
         }
         // C'b += dt F'b F^T
 #pragma unroll
@@ -439,8 +445,9 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
         ap[(AJ_F + k) * n + p] = Fb[k];
       }
       ap[AJ_J * n + p] = 0.0f;
-      gmu[p] += mub;
-      glam[p] += lamb;
+      const int id = iin[iidx(IC_ID, p)];
+      gmu[id] += mub;
+      glam[id] += lamb;
     }
     __syncthreads();
   }

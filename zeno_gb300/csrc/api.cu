@@ -72,6 +72,15 @@ struct mpm_ctx {
   cudaStream_t frame_stream = nullptr;
   cudaEvent_t frame_ready = nullptr, frame_done = nullptr;
   bool frame_pending = false;
+  // growing directory (mpm_set_auto_regrow): the fused substeps queued since
+  // the last synchronisation, as (dt, count) batches, and the device's
+  // started-substep count at that synchronisation
+  bool auto_regrow = false;
+  std::vector<std::pair<float, int32_t>> pending;
+  int64_t pending_total = 0;
+  int64_t started_base = 0;
+  int32_t regrows = 0;
+  int32_t max_grid_blocks_req = 0;  // as given at creation (0: the default rule)
 };
 
 namespace {
@@ -179,6 +188,9 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   mark(MPM_STAGE_SCAN);
   if (cloth) launch_cloth_mark(c->d, c->stream);  // the cloth's grid blocks
   if (trackers) launch_tracker_mark(c->d, c->stream);
+  // a growing directory: this substep and the queued ones halt if a
+  // particle, cloth vertex or tracker left the directory
+  if (c->auto_regrow) launch_substep_gate(c->d, c->stream);
   launch_scan(c->d, c->stream);
   mark(MPM_STAGE_SCATTER);
   launch_scatter(c->d, c->stream);
@@ -228,6 +240,133 @@ int32_t prepare_partition(mpm_ctx *c) {
     c->needs_full_clear = false;
     c->binned = false;
   }
+  return MPM_OK;
+}
+
+void drop_graphs(mpm_ctx *c) {
+  for (int k = 0; k < 2; ++k)
+    if (c->graph[k]) {
+      cudaGraphExecDestroy(c->graph[k]);
+      c->graph[k] = nullptr;
+    }
+}
+
+// replays of one synchronisation after which the directory has grown
+constexpr int kMaxRegrowRounds = 8;
+
+}  // namespace
+extern "C" int32_t mpm_sync(mpm_ctx *c);
+namespace {
+
+// With a growing directory, the calls that read or change the particle state
+// first let the queued substeps finish (growing the directory and replaying
+// them if a particle left it), so that they see the state after all of them.
+int32_t settle(mpm_ctx *c) {
+  if (!c->auto_regrow || c->pending_total == 0) return MPM_OK;
+  return mpm_sync(c);
+}
+
+// frees a buffer of the context and forgets it
+void dfree(mpm_ctx *c, void *p) {
+  if (!p) return;
+  auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
+  if (it != c->allocs.end()) c->allocs.erase(it);
+  cudaFree(p);
+}
+
+template <class T> int32_t drealloc(mpm_ctx *c, T **p, size_t count) {
+  dfree(c, *p);
+  *p = nullptr;
+  return dalloc(c, p, count);
+}
+
+// ordered bits (k_bbox) -> float
+float from_ordered_bits(unsigned u) {
+  const unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  float f;
+  std::memcpy(&f, &b, sizeof(f));
+  return f;
+}
+
+// Grows the directory of a one-scene context around its current particles
+// (and cloth vertices, trackers): the box of their blocks plus a margin of a
+// quarter of its extent (at least 2 blocks) on every side.  The directory
+// and, if the new box allows more grid blocks than the context holds, the
+// grid-sized buffers are reallocated; the counters, graphs and partition
+// start afresh, and the next substep bins the current positions.
+int32_t regrow(mpm_ctx *c) {
+  DevPtrs &d = c->d;
+  if (c->scenes.size() != 1) return fail(MPM_ERR_OUT_OF_DOMAIN, "a particle left the block directory");
+  const unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+  ZS_CUDA(cudaMemcpyAsync(d.cnt->bbox, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+  launch_bbox(d, c->cur, c->stream);
+  ZS_CUDA(cudaMemcpyAsync(c->h_cnt, d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  SceneParams &S = c->scenes[0];
+  int lo[3], dims[3];
+  long long ndir = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (c->h_cnt->bbox[a] > c->h_cnt->bbox[3 + a]) {  // nothing to place
+      lo[a] = S.block_lo[a];
+      dims[a] = S.block_dims[a];
+    } else {
+      const double xl = from_ordered_bits(c->h_cnt->bbox[a]);
+      const double xh = from_ordered_bits(c->h_cnt->bbox[3 + a]);
+      const double bl = std::floor(std::floor(xl * S.inv_dx - 0.5) / 4.0);
+      const double bh = std::floor(std::floor(xh * S.inv_dx - 0.5) / 4.0);
+      const double ext = bh - bl + 1.0, margin = std::max(2.0, std::floor(ext / 4.0));
+      const double l = bl - margin, dm = ext + 2.0 * margin;
+      if (l < -kMaxBlockCoord || l + dm > kMaxBlockCoord || dm > (double)kMaxDirBlocks)
+        return fail(MPM_ERR_OUT_OF_DOMAIN, "particles spread beyond the largest block directory");
+      lo[a] = (int)l;
+      dims[a] = std::max(3, (int)dm);
+    }
+    ndir *= dims[a];
+    if (ndir >= kMaxDirBlocks)
+      return fail(MPM_ERR_OUT_OF_DOMAIN,
+                  "particles spread beyond the largest block directory (2^25 blocks)");
+  }
+  int32_t rc;
+  const int ntiles = (int)((ndir + kScanTile - 1) / kScanTile);
+  if ((rc = drealloc(c, &d.dir_count, ndir)) || (rc = drealloc(c, &d.dir_fill, ndir)) ||
+      (rc = drealloc(c, &d.dir_gb, ndir)) || (rc = drealloc(c, &d.dir_bk, ndir)) ||
+      (rc = drealloc(c, &d.dir_flag, ndir)) || (rc = drealloc(c, &d.tile_sums, (size_t)3 * ntiles)))
+    return rc;
+  long long capg = c->max_grid_blocks_req > 0 ? c->max_grid_blocks_req
+                                               : std::max<long long>(16384, d.cap / 4);
+  capg = std::min<long long>(capg, ndir);
+  if (capg > d.cap_gblocks) {
+    if ((rc = drealloc(c, &d.ptile, (size_t)capg * kTileNodes)) ||
+        (rc = drealloc(c, &d.gb_dir, capg)) || (rc = drealloc(c, &d.bk_dir, capg)) ||
+        (rc = drealloc(c, &d.bk_start, capg)) || (rc = drealloc(c, &d.bk_count, capg)) ||
+        (rc = drealloc(c, &d.grid, (size_t)capg * 64)) || (rc = drealloc(c, &d.near_gb, capg)))
+      return rc;
+    if (d.grid2 && (rc = drealloc(c, &d.grid2, (size_t)capg * 64))) return rc;
+    if (d.ptile2 && (rc = drealloc(c, &d.ptile2, (size_t)capg * kTileNodes))) return rc;
+    if (d.ptile_adj && (rc = drealloc(c, &d.ptile_adj, (size_t)capg * kTileNodes))) return rc;
+    d.cap_gblocks = (int)capg;
+  }
+  ZS_CUDA(cudaMemsetAsync(d.dir_count, 0, ndir * sizeof(int32_t), c->stream));
+  ZS_CUDA(cudaMemsetAsync(d.dir_fill, 0, ndir * sizeof(int32_t), c->stream));
+  ZS_CUDA(cudaMemsetAsync(d.dir_gb, 0xff, ndir * sizeof(int32_t), c->stream));
+  ZS_CUDA(cudaMemsetAsync(d.dir_bk, 0xff, ndir * sizeof(int32_t), c->stream));
+  ZS_CUDA(cudaMemsetAsync(d.dir_flag, 0, ndir, c->stream));
+  ZS_CUDA(cudaMemsetAsync(d.cnt, 0, sizeof(Counters), c->stream));
+  for (int a = 0; a < 3; ++a) {
+    S.block_lo[a] = lo[a];
+    S.block_dims[a] = dims[a];
+  }
+  S.dir_off = 0;
+  d.ndir = ndir;
+  d.ntiles = ntiles;
+  c->prm_dirty = true;
+  if ((rc = push_params(c))) return rc;
+  drop_graphs(c);
+  c->started_base = 0;
+  c->needs_full_clear = false;
+  c->binned = false;
+  c->partition_valid = false;
+  c->regrows += 1;
   return MPM_OK;
 }
 
@@ -295,6 +434,8 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
     return fail(MPM_ERR_NO_DEVICE, "no CUDA device");
+  if (device == -1 && cudaGetDevice(&device) != cudaSuccess)
+    return fail(MPM_ERR_CUDA, "cudaGetDevice");
   if (device < 0 || device >= ndev) return fail(MPM_ERR_INVALID, "bad device ordinal");
   int major = 0, minor = 0, sms = 0;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
@@ -320,6 +461,7 @@ int32_t create_context(int32_t device, const mpm_scene_desc *scenes, int32_t n_s
   long long capg = max_grid_blocks > 0 ? max_grid_blocks : std::max<long long>(16384, cap / 4);
   capg = std::min<long long>(capg, ndir);
   DevPtrs &d = c->d;
+  c->max_grid_blocks_req = max_grid_blocks;
   d.cap = cap;
   d.ndir = ndir;
   d.cap_gblocks = (int)capg;
@@ -438,6 +580,7 @@ int32_t mpm_set_stream(mpm_ctx *c, void *stream) {
 int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (!mats || n <= 0 || n > kMaxMaterials)
     return fail(MPM_ERR_INVALID, "need 1.." + std::to_string(kMaxMaterials) + " materials");
   std::vector<MatParams> h(kMaxMaterials);
@@ -520,13 +663,7 @@ static void ypr_rotation(const float ypr_deg[3], float R[9]) {
 }
 
 // the captured substep graphs contain the collider pass or not
-static void drop_graphs(mpm_ctx *c) {
-  for (int k = 0; k < 2; ++k)
-    if (c->graph[k]) {
-      cudaGraphExecDestroy(c->graph[k]);
-      c->graph[k] = nullptr;
-    }
-}
+
 
 int32_t mpm_add_collider(mpm_ctx *c, const mpm_collider_desc *desc, int32_t *id) {
   int32_t rc = check(c);
@@ -701,8 +838,13 @@ int32_t upload_impl(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, const f
     ZS_CUDA(cudaMemsetAsync(c->d.beta, 0, (size_t)n * sizeof(float), c->stream));
     ZS_CUDA(cudaMemsetAsync(c->d.vms, 0, (size_t)n * sizeof(float), c->stream));
   }
-  // a fresh store: clear the status word and the whole directory
+  // a fresh store: clear the status word, the substep gate and the whole
+  // directory; substeps queued before the upload no longer matter
   ZS_CUDA(cudaMemsetAsync(&c->d.cnt->status, 0, sizeof(int), c->stream));
+  ZS_CUDA(cudaMemsetAsync(&c->d.cnt->halt, 0, 2 * sizeof(int), c->stream));
+  c->pending.clear();
+  c->pending_total = 0;
+  c->started_base = 0;
   c->needs_full_clear = true;
   c->partition_valid = false;
   c->binned = false;
@@ -753,6 +895,7 @@ int32_t mpm_batch_upload(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, co
 int32_t mpm_particles_set_lame(mpm_ctx *c, const float *mu, const float *lam) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (!mu || !lam) return fail(MPM_ERR_INVALID, "mu and lam are required");
   const long long n = c->prm.n;
   if (n == 0) return MPM_OK;
@@ -773,6 +916,7 @@ int32_t mpm_particles_set_lame(mpm_ctx *c, const float *mu, const float *lam) {
 int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *F, float *J) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   const long long n = c->prm.n;
   float *st = c->d.pbuf[1 - c->cur];
   // only the requested channels are gathered into upload order
@@ -798,6 +942,7 @@ int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *
 int32_t mpm_particles_get_attr(mpm_ctx *c, const char *name, float *values) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
   const std::string a(name);
   const long long n = c->prm.n;
@@ -836,6 +981,7 @@ int32_t mpm_particles_get_attr(mpm_ctx *c, const char *name, float *values) {
 int32_t mpm_particles_set_attr(mpm_ctx *c, const char *name, const float *values) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (!name || !values) return fail(MPM_ERR_INVALID, "null argument");
   if (std::string(name) == "cloth_beta") {  // the cloth's vertices (n_verts values)
     if (c->d.cloth.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
@@ -861,7 +1007,7 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
     return fail(MPM_ERR_INVALID, "a cloth needs vertices and triangles");
   if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "a cloth needs a single-scene context");
   if (c->d.cloth.n_verts > 0) return fail(MPM_ERR_STATE, "one cloth per context");
-  if (c->d.keep_order) return fail(MPM_ERR_INVALID, "the differentiable form takes no cloth");
+  if (c->d.differentiable) return fail(MPM_ERR_INVALID, "the differentiable form takes no cloth");
   if (desc->model != MPM_FCR && desc->model != MPM_NHK && desc->model != MPM_STVK)
     return fail(MPM_ERR_INVALID, "cloth model must be fixed-corotated, Neo-Hookean or StVK-Hencky");
   if (desc->kind != MPM_MESH_SURFACE && desc->kind != MPM_MESH_CURVE)
@@ -1155,6 +1301,7 @@ int32_t mpm_cloth_download(mpm_ctx *c, float *vx, float *vv, float *vC, float *e
                            float *eC, float *eF, float *ed) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   const ClothDev &cl = c->d.cloth;
   if (cl.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
   auto get = [&](float *h, const float *dsrc, long long count) -> int32_t {
@@ -1196,6 +1343,7 @@ int32_t mpm_trackers_create(mpm_ctx *c, int64_t n, const float *x, const float *
 int32_t mpm_trackers_download(mpm_ctx *c, float *x, float *v) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   const long long n = c->d.n_trackers;
   if (n == 0) return fail(MPM_ERR_STATE, "no trackers in this context");
   if (x) ZS_CUDA(cudaMemcpyAsync(x, c->d.tx, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
@@ -1207,6 +1355,7 @@ int32_t mpm_trackers_download(mpm_ctx *c, float *x, float *v) {
 int32_t mpm_compute_von_mises(mpm_ctx *c, int32_t by_log1p) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (c->prm.n == 0) return MPM_OK;
   if ((rc = push_params(c))) return rc;
   launch_von_mises(c->d, c->cur, by_log1p ? 1 : 0, c->stream);
@@ -1225,6 +1374,7 @@ int32_t mpm_frame_wait(mpm_ctx *c) {
 int32_t mpm_frame_begin(mpm_ctx *c, float *x, float *v) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if ((rc = mpm_frame_wait(c))) return rc;  // the snapshot buffer is free again
   const long long n = c->prm.n;
   if (n == 0) return MPM_OK;
@@ -1252,9 +1402,10 @@ int32_t mpm_frame_begin(mpm_ctx *c, float *x, float *v) {
 int32_t mpm_set_transfer(mpm_ctx *c, int32_t scheme) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (scheme < MPM_TRANSFER_APIC || scheme > MPM_TRANSFER_AFLIP)
     return fail(MPM_ERR_INVALID, "unknown transfer scheme");
-  if (scheme != MPM_TRANSFER_APIC && c->d.keep_order)
+  if (scheme != MPM_TRANSFER_APIC && c->d.differentiable)
     return fail(MPM_ERR_INVALID, "the differentiable form takes the APIC transfer only");
   if (scheme == c->d.transfer) return MPM_OK;
   DevPtrs &d = c->d;
@@ -1281,6 +1432,7 @@ int32_t mpm_set_transfer(mpm_ctx *c, int32_t scheme) {
 int32_t mpm_compute_particle_beta(mpm_ctx *c, float dt, int32_t collider) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (collider < -1 || collider >= (int32_t)c->colliders.size())
     return fail(MPM_ERR_INVALID, "collider id out of range");
   if ((rc = push_params(c))) return rc;
@@ -1295,10 +1447,23 @@ int32_t mpm_partition(mpm_ctx *c) {
   int32_t rc = check(c);
   if (rc) return rc;
   set_auto_step(c, 0);  // the stage path moves colliders only on request
+  if ((rc = settle(c))) return rc;
   if ((rc = push_params(c)) || (rc = prepare_partition(c))) return rc;
   enqueue_bin_if_needed(c);
   if (c->d.cloth.n_verts > 0) launch_cloth_mark(c->d, c->stream);
   if (c->d.n_trackers > 0) launch_tracker_mark(c->d, c->stream);
+  if (c->auto_regrow) {  // a growing directory: grow it before sorting
+    ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
+                            c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    const int b = c->h_cnt->status;
+    if ((b & ST_OUT_OF_DOMAIN) && !(b & (ST_NAN | ST_CAPACITY | ST_MATERIAL))) {
+      if ((rc = regrow(c)) || (rc = push_params(c))) return rc;
+      enqueue_bin_if_needed(c);
+      if (c->d.cloth.n_verts > 0) launch_cloth_mark(c->d, c->stream);
+      if (c->d.n_trackers > 0) launch_tracker_mark(c->d, c->stream);
+    }
+  }
   enqueue_sort(c);
   if ((rc = launch_check("partition"))) return rc;
   c->partition_valid = true;
@@ -1418,6 +1583,10 @@ int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
   }
   c->partition_valid = false;
   c->substeps += n_substeps;
+  if (c->auto_regrow && n_substeps > 0) {
+    c->pending.emplace_back(dt, n_substeps);
+    c->pending_total += n_substeps;
+  }
   return MPM_OK;
 }
 
@@ -1480,29 +1649,34 @@ int32_t mpm_get_launch_config(mpm_ctx *c, mpm_launch_config *cfg) {
   return MPM_OK;
 }
 
-int32_t mpm_set_order_mode(mpm_ctx *c, int32_t keep) {
+int32_t mpm_set_differentiable(mpm_ctx *c, int32_t on) {
   int32_t rc = check(c);
   if (rc) return rc;
-  if (keep && c->d.transfer != MPM_TRANSFER_APIC)
+  if ((rc = settle(c))) return rc;
+  if (on && c->d.transfer != MPM_TRANSFER_APIC)
     return fail(MPM_ERR_INVALID, "the differentiable form takes the APIC transfer only");
-  if (keep && c->d.cloth.n_verts > 0)
+  if (on && c->d.cloth.n_verts > 0)
     return fail(MPM_ERR_INVALID, "the differentiable form takes no cloth");
-  if (keep && !c->d.ptile_adj && (rc = dalloc(c, &c->d.ptile_adj, (size_t)c->d.cap_gblocks * kTileNodes)))
+  if (on && !c->d.ptile_adj &&
+      (rc = dalloc(c, &c->d.ptile_adj, (size_t)c->d.cap_gblocks * kTileNodes)))
     return rc;
-  ZS_CUDA(cudaStreamSynchronize(c->stream));
-  c->d.keep_order = keep ? 1 : 0;
-  for (int k = 0; k < 2; ++k)  // the graphs hold the old G2P output indexing
-    if (c->graph[k]) {
-      cudaGraphExecDestroy(c->graph[k]);
-      c->graph[k] = nullptr;
-    }
+  if (on && !c->prm.has_lame) {  // the states carry per-particle mu / lam
+    launch_lame_from_materials(c->d, c->cur, c->stream);
+    if ((rc = launch_check("per-particle Lame parameters"))) return rc;
+    c->prm.has_lame = 1;
+    c->prm_dirty = true;
+    if ((rc = push_params(c))) return rc;
+  }
+  c->d.differentiable = on ? 1 : 0;
+  drop_graphs(c);
   return MPM_OK;
 }
 
 int32_t mpm_state_save(mpm_ctx *c, float *dst) {
   int32_t rc = check(c);
   if (rc) return rc;
-  if (!c->d.keep_order) return fail(MPM_ERR_STATE, "state copies need mpm_set_order_mode(ctx, 1)");
+  if ((rc = settle(c))) return rc;
+  if (!c->d.differentiable) return fail(MPM_ERR_STATE, "state copies need mpm_set_differentiable(ctx, 1)");
   if (!dst) return fail(MPM_ERR_INVALID, "null destination");
   const size_t n = (size_t)c->prm.n;
   if (n == 0) return MPM_OK;
@@ -1513,7 +1687,8 @@ int32_t mpm_state_save(mpm_ctx *c, float *dst) {
 int32_t mpm_state_load(mpm_ctx *c, const float *src) {
   int32_t rc = check(c);
   if (rc) return rc;
-  if (!c->d.keep_order) return fail(MPM_ERR_STATE, "state copies need mpm_set_order_mode(ctx, 1)");
+  if ((rc = settle(c))) return rc;
+  if (!c->d.differentiable) return fail(MPM_ERR_STATE, "state copies need mpm_set_differentiable(ctx, 1)");
   if (!src) return fail(MPM_ERR_INVALID, "null source");
   const size_t n = (size_t)c->prm.n;
   if (n == 0) return MPM_OK;
@@ -1531,7 +1706,8 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
                             float *grad_mu, float *grad_lam) {
   int32_t rc = check(c);
   if (rc) return rc;
-  if (!c->d.keep_order) return fail(MPM_ERR_STATE, "the adjoint needs mpm_set_order_mode(ctx, 1)");
+  if ((rc = settle(c))) return rc;
+  if (!c->d.differentiable) return fail(MPM_ERR_STATE, "the adjoint needs mpm_set_differentiable(ctx, 1)");
   if (!adj_next || !adj_prev || !grad_mu || !grad_lam)
     return fail(MPM_ERR_INVALID, "null adjoint buffer");
   if (!c->differentiable)
@@ -1557,16 +1733,125 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
   return MPM_OK;
 }
 
+int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
+                            const float *state0, float *ckpts, float *final_state) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (n_substeps < 0 || every <= 0 || !state0 || !final_state || (n_substeps > 0 && !ckpts))
+    return fail(MPM_ERR_INVALID, "invalid rollout arguments");
+  const size_t plane = (size_t)MPM_STATE_PLANES * (size_t)c->prm.n;
+  if ((rc = mpm_state_load(c, state0))) return rc;
+  for (int32_t s = 0; s < n_substeps; ++s) {
+    if (s % every == 0 && (rc = mpm_state_save(c, ckpts + (size_t)(s / every) * plane))) return rc;
+    if ((rc = mpm_substep(c, dt, 1))) return rc;
+  }
+  return mpm_state_save(c, final_state);
+}
+
+int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
+                             const float *ckpts, float *seg_states, float *adj, float *adj_tmp,
+                             float *grad_mu, float *grad_lam) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (n_substeps < 0 || every <= 0 || (n_substeps > 0 && (!ckpts || !seg_states)) || !adj ||
+      !adj_tmp || !grad_mu || !grad_lam)
+    return fail(MPM_ERR_INVALID, "invalid rollout arguments");
+  const size_t n = (size_t)c->prm.n;
+  const size_t plane = (size_t)MPM_STATE_PLANES * n;
+  float *a = adj, *b = adj_tmp;  // adjoint of the next state, of this one
+  const int32_t n_seg = (n_substeps + every - 1) / every;
+  for (int32_t seg = n_seg - 1; seg >= 0; --seg) {
+    const int32_t s0 = seg * every, s1 = std::min(s0 + every, n_substeps);
+    // recompute the segment from its checkpoint, keeping its states
+    if ((rc = mpm_state_load(c, ckpts + (size_t)seg * plane))) return rc;
+    for (int32_t s = s0; s < s1; ++s) {
+      if ((rc = mpm_state_save(c, seg_states + (size_t)(s - s0) * plane))) return rc;
+      if (s + 1 < s1 && (rc = mpm_substep(c, dt, 1))) return rc;
+    }
+    // adjoint substeps, last to first
+    for (int32_t s = s1 - 1; s >= s0; --s) {
+      if ((rc = mpm_state_load(c, seg_states + (size_t)(s - s0) * plane))) return rc;
+      if ((rc = mpm_adjoint_substep(c, dt, a, b, grad_mu, grad_lam))) return rc;
+      std::swap(a, b);
+    }
+  }
+  if (a != adj)
+    ZS_CUDA(cudaMemcpyAsync(adj, a, (size_t)MPM_ADJ_PLANES * n * sizeof(float),
+                            cudaMemcpyDeviceToDevice, c->stream));
+  return MPM_OK;
+}
+
 int32_t mpm_sync(mpm_ctx *c) {
   int32_t rc = check(c);
   if (rc) return rc;
   ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
                           c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
+  // a growing directory: a particle left it, and no worse error came with it
+  for (int round = 0; c->auto_regrow && round < kMaxRegrowRounds; ++round) {
+    const int b = c->h_cnt->status;
+    if (!(b & ST_OUT_OF_DOMAIN) || (b & (ST_NAN | ST_CAPACITY | ST_MATERIAL))) break;
+    // the gate let `started` of the queued substeps run; the state after the
+    // last of them is complete (the halted ones changed nothing)
+    const int64_t started = (int64_t)c->h_cnt->n_started - c->started_base;
+    const int64_t halted = std::max<int64_t>(0, c->pending_total - started);
+    if (halted & 1) c->cur = 1 - c->cur;
+    c->substeps -= halted;
+    std::vector<std::pair<float, int32_t>> replay;
+    int64_t need = halted;
+    for (auto it = c->pending.rbegin(); it != c->pending.rend() && need > 0; ++it) {
+      const int32_t k = (int32_t)std::min<int64_t>(need, it->second);
+      replay.emplace_back(it->first, k);
+      need -= k;
+    }
+    std::reverse(replay.begin(), replay.end());
+    c->pending.clear();
+    c->pending_total = 0;
+    if ((rc = regrow(c))) return rc;
+    for (const auto &r : replay)
+      if ((rc = mpm_substep(c, r.first, r.second))) return rc;
+    ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
+                            c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  c->pending.clear();
+  c->pending_total = 0;
+  c->started_base = c->h_cnt->n_started;
   const int bits = c->h_cnt->status;
   if (bits & (ST_CAPACITY | ST_OUT_OF_DOMAIN)) c->needs_full_clear = true;
   const int32_t st = map_status(bits);
   if (st != MPM_OK) return fail(st, status_text(st));
+  return MPM_OK;
+}
+
+int32_t mpm_set_auto_regrow(mpm_ctx *c, int32_t on) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (on && c->scenes.size() != 1)
+    return fail(MPM_ERR_INVALID, "a growing directory needs a one-scene context");
+  if ((rc = settle(c))) return rc;
+  if ((on != 0) != c->auto_regrow) {
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    ZS_CUDA(cudaMemsetAsync(&c->d.cnt->halt, 0, 2 * sizeof(int), c->stream));
+    c->auto_regrow = on != 0;
+    c->pending.clear();
+    c->pending_total = 0;
+    c->started_base = 0;
+    drop_graphs(c);  // the graphs gain or lose the substep gate
+  }
+  return MPM_OK;
+}
+
+int32_t mpm_get_domain(mpm_ctx *c, int32_t block_lo[3], int32_t block_dims[3],
+                       int32_t *n_regrows) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = settle(c))) return rc;
+  for (int a = 0; a < 3; ++a) {
+    if (block_lo) block_lo[a] = c->scenes[0].block_lo[a];
+    if (block_dims) block_dims[a] = c->scenes[0].block_dims[a];
+  }
+  if (n_regrows) *n_regrows = c->regrows;
   return MPM_OK;
 }
 

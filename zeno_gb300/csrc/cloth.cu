@@ -150,6 +150,7 @@ __device__ __forceinline__ void matmul3(const float (&A)[9], const float (&B)[9]
 // the blocks of the cloth's vertices and elements (and their neighbours)
 // join the next partition's grid blocks
 __global__ void k_cloth_mark(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const long long n = cl.n_verts + cl.n_eles;
@@ -167,6 +168,7 @@ __global__ void k_cloth_mark(DevPtrs d) {
 
 // element P2G (type i on the grid, type ii impulses on the vertices)
 __global__ void k_cloth_p2g_elements(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const float dt = d.prm->dt, dx = S.dx, inv_dx = S.inv_dx;
@@ -315,6 +317,7 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
 
 // vertex P2G: mass, momentum and the impulse of its elements
 __global__ void k_cloth_p2g_verts(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const float dx = S.dx, inv_dx = S.inv_dx;
@@ -363,6 +366,7 @@ __global__ void k_cloth_p2g_verts(DevPtrs d) {
 // grids); adding it to the vertex's impulse, which the vertex P2G scatters
 // the same way, gives the same sums.
 __global__ void k_cloth_bending(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const float dt = d.prm->dt, t2 = cl.thickness * cl.thickness;
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < cl.n_springs;
@@ -491,6 +495,7 @@ __device__ __forceinline__ void curve_g2p(const DevPtrs &d, const ClothDev &cl, 
 }
 
 __global__ void k_cloth_g2p_verts(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const float dt = d.prm->dt;
@@ -518,6 +523,7 @@ __global__ void k_cloth_g2p_verts(DevPtrs d) {
 
 // element G2P and the surface return mapping (after the vertices moved)
 __global__ void k_cloth_g2p_elements(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const float dt = d.prm->dt;
@@ -663,6 +669,7 @@ __global__ void k_cloth_beta(DevPtrs d, float dt, int collider) {
 
 // tracker points (ToTrackerParticles): their blocks join the partition
 __global__ void k_tracker_mark(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const SceneParams &S = d.scn[0];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.n_trackers;
        i += (long long)gridDim.x * blockDim.x) {
@@ -679,6 +686,7 @@ __global__ void k_tracker_mark(DevPtrs d) {
 // tracker G2P (Transfer.cu:1259-1285): v = sum W v_i of the grid's "v"
 // channel (also on FLIP grids), x += v dt
 __global__ void k_tracker_g2p(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   const SceneParams &S = d.scn[0];
   const float dt = d.prm->dt, inv_dx = S.inv_dx;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < d.n_trackers;

@@ -88,6 +88,7 @@ template <bool kAffine> struct FLayout {
 template <bool kAffine>
 __global__ void __launch_bounds__(kFThreads, 3)
     k_p2g_flip(DevPtrs d, const float *__restrict__ pin) {
+  if (ZSMPM_HALTED(d)) return;
   using RC = FRaw<kAffine>;
   using L = FLayout<kAffine>;
   extern __shared__ __align__(16) unsigned char fsm[];
@@ -438,6 +439,7 @@ __device__ __forceinline__ void flip_update_node(const SceneParams &S, float dt,
 }
 
 __global__ void __launch_bounds__(64 * kFGatherBlocks) k_grid_gather_flip(DevPtrs d, int mode) {
+  if (ZSMPM_HALTED(d)) return;
   __shared__ int sbk[kFGatherBlocks][8];
   __shared__ int sorg[kFGatherBlocks][4];
   const SimParams &P = *d.prm;
@@ -508,6 +510,7 @@ __global__ void __launch_bounds__(64 * kFGatherBlocks) k_grid_gather_flip(DevPtr
 
 // the stage path's UpdateZSGrid / walls on a gathered FLIP grid
 __global__ void k_grid_update_flip(DevPtrs d, int mode) {
+  if (ZSMPM_HALTED(d)) return;
   const SimParams &P = *d.prm;
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
   float vmax = 0.0f;
@@ -560,6 +563,7 @@ template <bool kAffine, bool kFuseRM, bool kFuseBin>
 __global__ void __launch_bounds__(kFG2PThreads, 4)
     k_g2p_flip(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
                float *__restrict__ pout, int32_t *__restrict__ iout) {
+  if (ZSMPM_HALTED(d)) return;
   constexpr int NT = kFG2PThreads;
   using GC = FG2PCh<kAffine>;
   extern __shared__ __align__(16) unsigned char fg_smem[];
@@ -804,7 +808,7 @@ __global__ void __launch_bounds__(kFG2PThreads, 4)
 #pragma unroll
       for (int k = 0; k < 9; ++k) finite = finite && isfinite(F[k]);
       if (!finite) atomicOr(&d.cnt->status, ST_NAN);
-      const int so = d.keep_order ? p : s;
+      const int so = s;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         pout[pidx((CH_X + k), so)] = x[k];

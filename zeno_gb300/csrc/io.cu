@@ -83,18 +83,37 @@ __global__ void k_set_lame(float *__restrict__ pb, const int32_t *__restrict__ i
   }
 }
 
-// state planes [MPM_STATE_PLANES][n] (x v C F J of every slot) <-> the
-// first channels of the tiled store: dst != null saves, src != null loads
-__global__ void k_state_copy(float *__restrict__ pb, float *__restrict__ dst,
-                             const float *__restrict__ src, long long n) {
+__global__ void k_lame_from_materials(const DevPtrs d, float *__restrict__ pb,
+                                      const int32_t *__restrict__ ib) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < d.prm->n;
+       s += (long long)gridDim.x * blockDim.x) {
+    const MatParams mp = d.mats[min(max(ib[iidx(IC_MAT, s)], 0), kMaxMaterials - 1)];
+    pb[pidx(CH_MU, s)] = mp.mu;
+    pb[pidx(CH_LAM, s)] = mp.lam;
+  }
+}
+
+// state planes [MPM_STATE_PLANES][n] of every slot <-> the tiled store:
+// x v C F J m vol mu lam are the store's float channels 0..28, then the
+// material id and the upload index (int32 bits); dst != null saves,
+// src != null loads
+static_assert(MPM_STATE_PLANES == CH_LAM + 1 + NICH && CH_S == CH_LAM + 1,
+              "state planes: float channels up to lam, then the int channels");
+__global__ void k_state_copy(float *__restrict__ pb, int32_t *__restrict__ ib,
+                             float *__restrict__ dst, const float *__restrict__ src, long long n) {
+  constexpr int NF = CH_LAM + 1;
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n;
        s += (long long)gridDim.x * blockDim.x) {
+    if (dst) {
 #pragma unroll
-    for (int k = 0; k < MPM_STATE_PLANES; ++k) {
-      if (dst)
-        dst[k * n + s] = pb[pidx(k, s)];
-      else
-        pb[pidx(k, s)] = src[k * n + s];
+      for (int k = 0; k < NF; ++k) dst[k * n + s] = pb[pidx(k, s)];
+      dst[(NF + IC_MAT) * n + s] = __int_as_float(ib[iidx(IC_MAT, s)]);
+      dst[(NF + IC_ID) * n + s] = __int_as_float(ib[iidx(IC_ID, s)]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NF; ++k) pb[pidx(k, s)] = src[k * n + s];
+      ib[iidx(IC_MAT, s)] = __float_as_int(src[(NF + IC_MAT) * n + s]);
+      ib[iidx(IC_ID, s)] = __float_as_int(src[(NF + IC_ID) * n + s]);
     }
   }
 }
@@ -128,7 +147,7 @@ void launch_check_materials(const DevPtrs &d, const int32_t *mat, long long n, i
 void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, long long n,
                        cudaStream_t s) {
   if (n <= 0) return;
-  k_state_copy<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], dst, src, n);
+  k_state_copy<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], dst, src, n);
 }
 
 void launch_egest_channel(const DevPtrs &d, int cur, int ch, float *dst, long long n,
@@ -141,6 +160,10 @@ void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *la
                      cudaStream_t s) {
   if (n <= 0) return;
   k_set_lame<<<d.num_sms * 8, 256, 0, s>>>(d.pbuf[cur], d.ibuf[cur], d.cap, mu, lam, n);
+}
+
+void launch_lame_from_materials(const DevPtrs &d, int cur, cudaStream_t s) {
+  k_lame_from_materials<<<d.num_sms * 8, 256, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
 }
 
 void launch_ingest(const DevPtrs &d, int cur, IngestSrc src, long long b0, long long b1,

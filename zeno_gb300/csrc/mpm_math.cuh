@@ -471,22 +471,27 @@ __device__ __forceinline__ void nhk_vjp(float mu, float lam, const float (&F)[9]
 //   D_ij = (t_i - t_j) / (b_i - b_j),  Jt_ik = dt_i / db_k,
 // and F-bar += 2 B-bar F.  The divided differences are written as functions
 // of u = (b_i - b_j) / b_j; for near-equal eigenvalues (|u| < 1e-3, where the
-// FP32 difference of the closed forms cancels) they come from FP64 series.
+// FP32 difference of the closed forms cancels) they come from their Taylor
+// series in u.  The series are evaluated in FP32: u is an FP32 number, the
+// truncation error after the u^3 term is below |u|^4 / 4 < 3e-13, and the
+// Horner steps round to a few ulp of the O(1) result, so FP64 arithmetic
+// would not change the rounded value (GB300's FP64 rate is a small fraction
+// of its FP32 rate, and nearly every particle of a sand column at rest takes
+// this branch).
 
-// log1p(u) / u
+// log1p(u) / u = 1 - u/2 + u^2/3 - u^3/4 + ...
 __device__ __forceinline__ float log1p_over(float u) {
-  if (fabsf(u) < 1e-3f) {
-    const double x = u;
-    return (float)(1.0 - x * (0.5 - x * (1.0 / 3.0 - x * 0.25)));
-  }
+  if (fabsf(u) < 1e-3f) return fmaf(-u, fmaf(-u, fmaf(-u, 0.25f, 1.0f / 3.0f), 0.5f), 1.0f);
   return log1pf(u) / u;
 }
 
 // ((1 + u)^a - 1) / u = expm1(a log1p(u)) / u
+//   = a (1 + u (a-1)/2 + u^2 (a-1)(a-2)/6 + u^3 (a-1)(a-2)(a-3)/24 + ...)
 __device__ __forceinline__ float pow1p_m1_over(float a, float u) {
   if (fabsf(u) < 1e-3f) {
-    const double x = u, y = a;
-    return (float)(y * (1.0 + x * ((y - 1.0) * 0.5 + x * (y - 1.0) * (y - 2.0) / 6.0)));
+    const float c1 = (a - 1.0f) * 0.5f, c2 = c1 * (a - 2.0f) * (1.0f / 3.0f),
+                c3 = c2 * (a - 3.0f) * 0.25f;
+    return a * fmaf(u, fmaf(u, fmaf(u, c3, c2), c1), 1.0f);
   }
   return expm1f(a * log1pf(u)) / u;
 }

@@ -78,6 +78,7 @@ __global__ void k_noalloc_clear(unsigned char *base, long long ndir) {
     c->status = 0;
     c->max_vel_sqr_bits = 0u;
     c->n_binned = 0;
+    c->halt = 0;
   }
 }
 

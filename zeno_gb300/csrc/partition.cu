@@ -75,6 +75,15 @@ __global__ void k_bin(DevPtrs d, const float *__restrict__ pin) {
 // Pass 1 of the directory scan: per tile sums of (grid block flag, particle
 // count, non-empty flag).
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
+  // a particle left the directory (binned with key -1): the partition of
+  // these positions is incomplete, so this and the queued stages stop here
+  // and the state stays the last complete one (with a growing directory the
+  // host then grows it and replays them; otherwise the status is the error)
+  if (d.cnt->status & ST_OUT_OF_DOMAIN) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.cnt->halt = 1;
+    return;
+  }
   const long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanPerThread;
   int f = 0, c = 0, e = 0;
 #pragma unroll
@@ -112,6 +121,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevPtrs d) {
 // Every entry of the tile is rewritten: grid block index or -1, particle
 // block index or -1, count and flag back to 0 for the next binning.
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   __shared__ int red[3][kScanThreads / 32];
   __shared__ int tile_prefix[3];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -241,6 +251,7 @@ constexpr int kScatterPerCta = kScatterThreads * kScatterPer;
 constexpr int kScatterSlots = 64;
 
 __global__ void __launch_bounds__(kScatterThreads) k_scatter(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   __shared__ int tkey[kScatterSlots], tcount[kScatterSlots], tbase[kScatterSlots];
   const long long n = d.prm->n;
   const int tid = threadIdx.x;
@@ -327,6 +338,7 @@ __device__ __forceinline__ void warp_exclusive_scan64(const int *in, int *out) {
 }
 
 __global__ void __launch_bounds__(kSortThreads) k_bucket_sort(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
   __shared__ __align__(16) int sbuf[2 * kSortCap];
   int *sp = sbuf, *op = sbuf + kSortCap;
   __shared__ unsigned char sc[kSortCap], oc[kSortCap];
@@ -448,6 +460,59 @@ __global__ void k_grid_clear(DevPtrs d) {
     d.grid[i] = z;
 }
 
+// The gate of one fused substep: a particle that left the directory (bit
+// set by the previous substep's binning) halts this and every later queued
+// substep; otherwise the substep is counted as started.
+__global__ void k_substep_gate(DevPtrs d) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Counters *c = d.cnt;
+  if (c->status & ST_OUT_OF_DOMAIN) c->halt = 1;
+  if (!c->halt) c->n_started += 1;
+}
+
+// float -> unsigned with the order of the floats (for atomicMin / atomicMax)
+__device__ __forceinline__ unsigned ordered_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_bbox(DevPtrs d, const float *__restrict__ pin) {
+  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  auto take = [&](float x0, float x1, float x2) {
+    const float x[3] = {x0, x1, x2};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (!isfinite(x[a])) continue;
+      const unsigned b = ordered_bits(x[a]);
+      lo[a] = min(lo[a], b);
+      hi[a] = max(hi[a], b);
+    }
+  };
+  for (long long i = t0; i < d.prm->n; i += stride)
+    take(pin[pidx(CH_X, i)], pin[pidx(CH_X + 1, i)], pin[pidx(CH_X + 2, i)]);
+  for (long long i = t0; i < d.cloth.n_verts; i += stride)
+    take(d.cloth.vx[3 * i], d.cloth.vx[3 * i + 1], d.cloth.vx[3 * i + 2]);
+  for (long long i = t0; i < d.n_trackers; i += stride)
+    take(d.tx[3 * i], d.tx[3 * i + 1], d.tx[3 * i + 2]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[a] = min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+      hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&d.cnt->bbox[a], lo[a]);
+      atomicMax(&d.cnt->bbox[3 + a], hi[a]);
+    }
+  }
+}
+
 inline int grid_for(const DevPtrs &d, int per_sm) { return d.num_sms * per_sm; }
 
 }  // namespace
@@ -478,6 +543,13 @@ void launch_bucket_sort(const DevPtrs &d, cudaStream_t s) {
 
 void launch_grid_clear(const DevPtrs &d, cudaStream_t s) {
   k_grid_clear<<<grid_for(d, 8), 256, 0, s>>>(d);
+}
+
+void launch_substep_gate(const DevPtrs &d, cudaStream_t s) { k_substep_gate<<<1, 32, 0, s>>>(d); }
+
+// the caller sets bbox to (all ones) x 3, (zeros) x 3 first
+void launch_bbox(const DevPtrs &d, int cur, cudaStream_t s) {
+  k_bbox<<<grid_for(d, 4), 256, 0, s>>>(d, d.pbuf[cur]);
 }
 
 }  // namespace zsmpm

@@ -88,6 +88,7 @@ constexpr int RC_X = 0, RC_V = 3, RC_C = 6, RC_S = 15, RC_M = 21, RC_KEY = 22;
 
 __global__ void __launch_bounds__(kColThreads, 4) k_p2g(DevPtrs d, const float *__restrict__ pin,
                                                      const int32_t *__restrict__ iin) {
+  if (ZSMPM_HALTED(d)) return;
   extern __shared__ __align__(16) unsigned char p2g_smem[];
   float(*raw)[kColChunk] = reinterpret_cast<float(*)[kColChunk]>(p2g_smem);
   float4(*spd)[kColChunk] = reinterpret_cast<float4(*)[kColChunk]>(p2g_smem + kColOffSpd);
@@ -349,6 +350,7 @@ __device__ __forceinline__ void update_node_at(const DevPtrs &d, int scene, cons
 constexpr int kGatherBlocks = 4;
 
 __global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, int mode) {
+  if (ZSMPM_HALTED(d)) return;
   __shared__ int sbk[kGatherBlocks][8];
   __shared__ int sorg[kGatherBlocks][4];  // node origin, scene
   const SimParams &P = *d.prm;
@@ -446,6 +448,7 @@ __device__ __forceinline__ void update_node_at(const DevPtrs &d, int scene, cons
 }
 
 __global__ void k_grid_update(DevPtrs d, int mode) {
+  if (ZSMPM_HALTED(d)) return;
   const SimParams &P = *d.prm;
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
   float vmax = 0.0f;
@@ -490,6 +493,7 @@ template <bool kFuseRM, bool kFuseBin, int NT>
 __global__ void __launch_bounds__(NT, 768 / NT)
     k_g2p(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
           float *__restrict__ pout, int32_t *__restrict__ iout) {
+  if (ZSMPM_HALTED(d)) return;
   extern __shared__ __align__(16) unsigned char g2p_smem[];
   float4(*gsm)[kNodes] = reinterpret_cast<float4(*)[kNodes]>(g2p_smem);
   float(*psm)[kG2PCh][NT] =
@@ -710,9 +714,8 @@ __global__ void __launch_bounds__(NT, 768 / NT)
 #pragma unroll
       for (int k = 0; k < 9; ++k) finite = finite && isfinite(F[k]);
       if (!finite) atomicOr(&d.cnt->status, ST_NAN);
-      // next buffer: sorted position s, or the particle's own slot p in the
-      // differentiable mode (every state then shares the upload order)
-      const int so = d.keep_order ? p : s;
+      // next buffer: the particle's sorted position
+      const int so = s;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         pout[pidx((CH_X + k), so)] = x[k];
@@ -879,6 +882,7 @@ void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
 // between gather and boundary): every block, skipped by the warp unless its
 // node box meets the world box of a collider.
 __global__ void k_apply_colliders(DevPtrs d, int id, int listed) {
+  if (ZSMPM_HALTED(d)) return;
   const int nc = d.prm->n_colliders;
   const int k0 = id < 0 ? 0 : id, k1 = id < 0 ? nc : min(id + 1, nc);
   const int ng = listed ? min(d.cnt->n_near, d.cap_gblocks) : min(d.cnt->n_gblocks, d.cap_gblocks);

@@ -97,8 +97,18 @@ struct Counters {
   int n_binned;
   int bad_material;  // set by the upload check of material ids
   int n_near;        // grid blocks the fused substep's gather found near a collider
-  int pad;
+  // growing directory: the substep gate sets `halt` when a particle left the
+  // directory, and every kernel of the queued substeps then does nothing;
+  // `n_started` counts the substeps the gate let through
+  int halt;
+  int n_started;
+  unsigned bbox[6];  // ordered-bits min x, y, z, max x, y, z of the positions
 };
+
+// Every kernel of the fused substep starts with this test: the substeps
+// queued behind one whose particles left the directory leave the state as
+// it is, so that the context can grow its directory and replay them.
+#define ZSMPM_HALTED(d) ((d).cnt->halt != 0)
 
 // Device-resident parameters; the host updates them with one small copy
 // when they change, so captured graphs read the current values.
@@ -229,7 +239,7 @@ struct DevPtrs {
   // ToTrackerParticles: points advected by the grid velocity, no P2G
   long long n_trackers;
   float *tx, *tv;
-  int keep_order;     // differentiable mode: G2P writes each particle to its own slot
+  int differentiable;  // mpm_set_differentiable: adjoint buffers allocated
   int planar_x;       // pbuf[0] holds positions as 3 planes of `cap` floats (binning only)
   int32_t *tile_sums;
   int ntiles;
@@ -276,6 +286,11 @@ void launch_scatter(const DevPtrs &d, cudaStream_t s);
 void launch_bucket_sort(const DevPtrs &d, cudaStream_t s);
 void launch_grid_clear(const DevPtrs &d, cudaStream_t s);
 void launch_full_dir_clear(const DevPtrs &d, cudaStream_t s);
+// first kernel of every fused substep of a context that grows its directory
+void launch_substep_gate(const DevPtrs &d, cudaStream_t s);
+// bounding box of the particle positions (and cloth vertices, trackers) of
+// buffer `cur` into Counters::bbox
+void launch_bbox(const DevPtrs &d, int cur, cudaStream_t s);
 
 // transfer.cu
 // fills the persistent grid sizes of DevPtrs from the occupancy of each kernel
@@ -325,6 +340,8 @@ void launch_state_copy(const DevPtrs &d, int cur, float *dst, const float *src, 
                        cudaStream_t s);
 void launch_set_lame(const DevPtrs &d, int cur, const float *mu, const float *lam, long long n,
                      cudaStream_t s);
+// every particle's mu / lam channels from its material
+void launch_lame_from_materials(const DevPtrs &d, int cur, cudaStream_t s);
 // writes AoS x(3) v(3) C(9) F(9) J(1) planes-of-arrays in upload order into dst
 struct EgestDst {
   float *x, *v, *C, *F, *J;

@@ -1,18 +1,25 @@
 """Differentiable MLS-MPM rollouts.
 
 `Rollout(scene, particles, n_substeps, ckpt_every)` wraps a context in the
-upload-order mode and exposes `rollout(v0, E) -> x_final` as a
+differentiable mode and exposes `rollout(v0, E) -> x_final` as a
 `torch.autograd.Function`:
 
-* forward: loads the initial state (positions of the scene, v0, C = 0, F = I)
-  with per-particle Young's moduli E (nu of the material), runs n_substeps
-  substeps and saves the state every `ckpt_every` substeps (device buffers
-  owned by torch);
-* backward: walks the segments in reverse; each segment is recomputed from its
-  checkpoint (its states kept), then the hand-written adjoint substep
-  (mpm_adjoint_substep: G2P, grid update + boundary, P2G and the stress)
-  runs backwards through it.  Memory: one checkpoint per segment plus one
-  segment of states.
+* forward: builds the initial state on the device (positions of the scene,
+  v0, C = 0, F = I, per-particle mu / lam from Young's moduli E and the
+  material's nu) and runs the whole rollout in one C-ABI call
+  (mpm_rollout_forward), which keeps the state every `ckpt_every` substeps
+  in device buffers owned by torch;
+* backward: one C-ABI call (mpm_rollout_backward) walks the segments in
+  reverse; each segment is recomputed from its checkpoint (its states kept)
+  and the hand-written adjoint substep (G2P, grid update + boundary, P2G and
+  the stress) runs backwards through it.  Memory: one checkpoint per segment
+  plus one segment of states, 31 planes of n floats each.
+
+The substep keeps the particle store sorted by block, so every state (and
+its adjoint) is in its own slot order; the state's upload-index plane maps
+slots to particles.  The initial state is in upload order, so the adjoint of
+v0 comes out in upload order; the gradients of mu and lam accumulate by
+upload index.
 
 Gradients are returned for v0 (n x 3) and E (n); other initial data are
 constants.  Fixed-corotated, Neo-Hookean and StVK-Hencky materials, the last
@@ -25,8 +32,10 @@ import torch
 
 from . import zsmpm
 
-PLANES = 25  # x 3, v 3, C 9, F 9, J 1
+PLANES = zsmpm.STATE_PLANES  # x 3, v 3, C 9, F 9, J, m, vol, mu, lam, material, upload index
+ADJ = zsmpm.ADJ_PLANES       # x 3, v 3, C 9, F 9, J
 X, V, Cc, Fc, J = slice(0, 3), slice(3, 6), slice(6, 15), slice(15, 24), 24
+M, VOL, MU, LAM, MAT, ID = 25, 26, 27, 28, 29, 30
 
 
 class Rollout:
@@ -39,24 +48,27 @@ class Rollout:
         self.dt = float(scene.dt)
         self.n_substeps = int(n_substeps)
         self.ckpt_every = max(1, int(ckpt_every))
+        self.n_ckpt = (self.n_substeps + self.ckpt_every - 1) // self.ckpt_every
         self.nu = float(scene.materials[0].nu)
         self.dev = torch.device("cuda", device)
         self.stream = torch.cuda.Stream(device=self.dev)
         self.ctx = zsmpm.Context(scene, max_particles=parts.n, device=device,
                                  max_grid_blocks=max_grid_blocks)
         self.ctx.set_stream(self.stream.cuda_stream)
-        self.ctx.set_order_mode(True)
-        p = parts.copy()
-        mu, lam = self.lame(np.full(self.n, scene.materials[0].E))
-        p.mu = mu.astype(np.float32)
-        p.lam = lam.astype(np.float32)
-        self.ctx.upload(p)
-        s0 = torch.zeros(PLANES, self.n, dtype=torch.float32, device=self.dev)
+        self.ctx.upload(parts)
+        self.ctx.set_differentiable(True)
+        n = self.n
+        s0 = torch.zeros(PLANES, n, dtype=torch.float32, device=self.dev)
         s0[X] = torch.from_numpy(np.ascontiguousarray(parts.x.T)).to(self.dev)
         s0[Fc] = torch.eye(3, device=self.dev).reshape(9, 1)
         s0[J] = 1.0
+        s0[M] = torch.from_numpy(np.ascontiguousarray(parts.m, np.float32)).to(self.dev)
+        s0[VOL] = torch.from_numpy(np.ascontiguousarray(parts.vol, np.float32)).to(self.dev)
+        s0[MAT] = torch.from_numpy(np.ascontiguousarray(parts.mat, np.int32)).to(
+            self.dev).view(torch.float32)
+        s0[ID] = torch.arange(n, dtype=torch.int32, device=self.dev).view(torch.float32)
         self.state0 = s0
-        self.peak_checkpoint_bytes = 0
+        self.peak_checkpoint_bytes = (self.n_ckpt + self.ckpt_every + 1) * PLANES * n * 4
 
     def lame(self, E):
         nu = self.nu
@@ -66,13 +78,6 @@ class Rollout:
         nu = self.nu
         return 1.0 / (2.0 * (1.0 + nu)), nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
 
-    def _set_E(self, E: torch.Tensor):
-        mu, lam = self.lame(E.detach().double().cpu().numpy())
-        self.ctx.set_lame(mu, lam)
-
-    def _new_state(self):
-        return torch.empty(PLANES, self.n, dtype=torch.float32, device=self.dev)
-
     def rollout(self, v0: torch.Tensor, E: torch.Tensor) -> torch.Tensor:
         return _RolloutFn.apply(v0, E, self)
 
@@ -80,60 +85,47 @@ class Rollout:
 class _RolloutFn(torch.autograd.Function):
     @staticmethod
     def forward(fctx, v0, E, sim: Rollout):
+        n = sim.n
+        sim.stream.wait_stream(torch.cuda.current_stream())  # v0, E are ready
         with torch.cuda.stream(sim.stream):
-            sim._set_E(E)
             state = sim.state0.clone()
             state[V] = v0.detach().to(sim.dev, torch.float32).T
-            sim.stream.synchronize()
-            sim.ctx.state_load(state.data_ptr())
-            ckpts = []
-            for s in range(sim.n_substeps):
-                if s % sim.ckpt_every == 0:
-                    buf = sim._new_state()
-                    sim.ctx.state_save(buf.data_ptr())
-                    ckpts.append(buf)
-                sim.ctx.substep(sim.dt, 1)
-            final = sim._new_state()
-            sim.ctx.state_save(final.data_ptr())
-            sim.ctx.sync()
-        sim.peak_checkpoint_bytes = (len(ckpts) + sim.ckpt_every) * PLANES * sim.n * 4
+            mu, lam = sim.lame(E.detach().to(sim.dev, torch.float64))
+            state[MU] = mu.float()
+            state[LAM] = lam.float()
+            ckpts = torch.empty(max(sim.n_ckpt, 1), PLANES, n, dtype=torch.float32,
+                                device=sim.dev)
+            final = torch.empty(PLANES, n, dtype=torch.float32, device=sim.dev)
+            sim.ctx.rollout_forward(sim.dt, sim.n_substeps, sim.ckpt_every, state.data_ptr(),
+                                    ckpts.data_ptr(), final.data_ptr())
+            # the final state's slots back into upload order
+            ids = final[ID].view(torch.int32).long()
+            x = torch.empty(n, 3, dtype=torch.float32, device=sim.dev)
+            x[ids] = final[X].T
+        torch.cuda.current_stream().wait_stream(sim.stream)
         fctx.sim = sim
         fctx.ckpts = ckpts
+        fctx.ids = ids
         fctx.E = E.detach()
-        return final[X].T.contiguous()
+        return x
 
     @staticmethod
     def backward(fctx, gx):
         sim: Rollout = fctx.sim
-        n, k, T = sim.n, sim.ckpt_every, sim.n_substeps
+        n, k = sim.n, sim.ckpt_every
+        sim.stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(sim.stream):
-            adj = torch.zeros(PLANES, n, dtype=torch.float32, device=sim.dev)
-            adj[X] = gx.detach().to(sim.dev, torch.float32).T
-            nxt = torch.empty_like(adj)
+            adj = torch.zeros(ADJ, n, dtype=torch.float32, device=sim.dev)
+            adj[X] = gx.detach().to(sim.dev, torch.float32)[fctx.ids].T  # final slot order
+            tmp = torch.empty_like(adj)
             gmu = torch.zeros(n, dtype=torch.float32, device=sim.dev)
             glam = torch.zeros(n, dtype=torch.float32, device=sim.dev)
-            sim._set_E(fctx.E)
-            sim.stream.synchronize()
-            n_seg = len(fctx.ckpts)
-            states = [sim._new_state() for _ in range(k)]
-            for seg in reversed(range(n_seg)):
-                s0 = seg * k
-                s1 = min(s0 + k, T)
-                # recompute the segment from its checkpoint
-                sim.ctx.state_load(fctx.ckpts[seg].data_ptr())
-                for s in range(s0, s1):
-                    sim.ctx.state_save(states[s - s0].data_ptr())
-                    if s + 1 < s1:
-                        sim.ctx.substep(sim.dt, 1)
-                # adjoint substeps, last to first
-                for s in reversed(range(s0, s1)):
-                    sim.ctx.state_load(states[s - s0].data_ptr())
-                    sim.ctx.adjoint_substep(sim.dt, adj.data_ptr(), nxt.data_ptr(),
-                                            gmu.data_ptr(), glam.data_ptr())
-                    adj, nxt = nxt, adj
-            sim.ctx.sync()
+            seg = torch.empty(k, PLANES, n, dtype=torch.float32, device=sim.dev)
+            sim.ctx.rollout_backward(sim.dt, sim.n_substeps, k, fctx.ckpts.data_ptr(),
+                                     seg.data_ptr(), adj.data_ptr(), tmp.data_ptr(),
+                                     gmu.data_ptr(), glam.data_ptr())
             dmu, dlam = sim.dlame_dE()
-            gv0 = adj[V].T.contiguous()
+            gv0 = adj[V].T.contiguous()  # state 0 is in upload order
             gE = gmu.double() * dmu + glam.double() * dlam
         torch.cuda.current_stream().wait_stream(sim.stream)
         return gv0, gE.to(fctx.E.dtype), None

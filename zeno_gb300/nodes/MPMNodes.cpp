@@ -227,9 +227,11 @@ int32_t transfer_of(const ZenoGrid &g) {
   return MPM_TRANSFER_APIC;
 }
 
-// A device context for a particle set / mesh: the directory covers
-// [lo, hi] (the optional domain inputs), else the bounding box of `pos`
-// grown by its own extent (at least 32 cells) on every side.
+// A device context for a particle set / mesh on the current CUDA device: the
+// directory covers [lo, hi] (the optional domain inputs), else the bounding
+// box of `pos` plus 8 cells on every side, and grows (recentred on the
+// particles) whenever one leaves it, as the reference's hashed block table
+// takes new blocks (Structures.hpp:535).
 std::shared_ptr<MpmContext> make_context(const ZenoConstitutiveModel &model,
                                          const std::vector<vec3f> &pos, const float *lo_in,
                                          const float *hi_in, int64_t max_particles) {
@@ -253,13 +255,12 @@ std::shared_ptr<MpmContext> make_context(const ZenoConstitutiveModel &model,
     if (pos.empty())
       for (int d = 0; d < 3; ++d) lo[d] = hi[d] = 0.0f;
     for (int d = 0; d < 3; ++d) {
-      const float grow = std::max(hi[d] - lo[d], 32.0f * dx);
-      lo[d] -= grow;
-      hi[d] += grow;
+      lo[d] -= 8.0f * dx;
+      hi[d] += 8.0f * dx;
     }
   }
   mpm_ctx_desc desc{};
-  desc.device = 0;
+  desc.device = -1;  // the calling thread's current CUDA device
   desc.dx = dx;
   for (int d = 0; d < 3; ++d) {
     const int b0 = (int)std::floor(lo[d] / dx / 4.0f) - 1;
@@ -272,6 +273,7 @@ std::shared_ptr<MpmContext> make_context(const ZenoConstitutiveModel &model,
   ctx->dx = dx;
   check(mpm_ctx_create(&desc, &ctx->h), "mpm_ctx_create");
   check(mpm_set_materials(ctx->h, &model.mat, 1), "mpm_set_materials");
+  check(mpm_set_auto_regrow(ctx->h, 1), "mpm_set_auto_regrow");
   return ctx;
 }
 

@@ -83,11 +83,15 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_g2p", "mpm_return_mapping",
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
-           "mpm_get_launch_config", "mpm_set_order_mode", "mpm_state_save", "mpm_state_load",
-           "mpm_adjoint_substep", "mpm_add_collider", "mpm_clear_colliders",
-           "mpm_step_colliders"]
+           "mpm_get_launch_config", "mpm_set_differentiable", "mpm_state_save",
+           "mpm_state_load", "mpm_adjoint_substep", "mpm_rollout_forward", "mpm_rollout_backward", "mpm_add_collider", "mpm_clear_colliders",
+           "mpm_step_colliders", "mpm_set_auto_regrow", "mpm_get_domain"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
+# differentiable form (include/zsmpm.h): state planes x 3, v 3, C 9, F 9, J,
+# m, vol, mu, lam, material id, upload index; adjoint planes x v C F J
+STATE_PLANES = 31
+ADJ_PLANES = 25
 
 _lib = None
 
@@ -152,7 +156,11 @@ def load(path: str = LIB_PATH):
         "mpm_partition_noalloc": ([P, i64, f32, P, P, P, P, P, i64, P, P], i32),
         "mpm_set_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
         "mpm_get_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
-        "mpm_set_order_mode": ([P, i32], i32),
+        "mpm_set_differentiable": ([P, i32], i32),
+        "mpm_rollout_forward": ([P, f32, i32, i32, P, P, P], i32),
+        "mpm_rollout_backward": ([P, f32, i32, i32, P, P, P, P, P, P], i32),
+        "mpm_set_auto_regrow": ([P, i32], i32),
+        "mpm_get_domain": ([P, P, P, P], i32),
         "mpm_state_save": ([P, P], i32),
         "mpm_state_load": ([P, P], i32),
         "mpm_adjoint_substep": ([P, f32, P, P, P, P], i32),
@@ -332,7 +340,8 @@ class Context:
 
     @property
     def dir_size(self) -> int:
-        return int(np.prod(self.scene.block_dims))
+        _, dims, _ = self.domain()  # the directory may have grown
+        return int(np.prod(dims))
 
     def _check(self, rc: int, where: str):
         if rc != MPM_OK:
@@ -502,9 +511,36 @@ class Context:
     def sync(self):
         self._check(self._L.mpm_sync(self.h), "mpm_sync")
 
-    # differentiable form: device pointers (ints), 25 planes of n floats
-    def set_order_mode(self, keep: bool):
-        self._check(self._L.mpm_set_order_mode(self.h, 1 if keep else 0), "mpm_set_order_mode")
+    # growing directory
+    def set_auto_regrow(self, on: bool = True):
+        self._check(self._L.mpm_set_auto_regrow(self.h, 1 if on else 0), "mpm_set_auto_regrow")
+
+    def domain(self):
+        """(block_lo, block_dims, n_regrows) of the directory."""
+        lo = (C.c_int32 * 3)()
+        dims = (C.c_int32 * 3)()
+        nr = C.c_int32(0)
+        self._check(self._L.mpm_get_domain(self.h, lo, dims, C.byref(nr)), "mpm_get_domain")
+        return tuple(lo), tuple(dims), nr.value
+
+    # differentiable form: device pointers (ints); a state is STATE_PLANES
+    # planes of n floats in the store's slot order, an adjoint ADJ_PLANES
+    def set_differentiable(self, on: bool = True):
+        self._check(self._L.mpm_set_differentiable(self.h, 1 if on else 0),
+                    "mpm_set_differentiable")
+
+    def rollout_forward(self, dt, n_substeps: int, every: int, state0: int, ckpts: int,
+                        final: int):
+        self._check(self._L.mpm_rollout_forward(self.h, dt, int(n_substeps), int(every),
+                                                C.c_void_p(state0), C.c_void_p(ckpts),
+                                                C.c_void_p(final)), "mpm_rollout_forward")
+
+    def rollout_backward(self, dt, n_substeps: int, every: int, ckpts: int, seg_states: int,
+                         adj: int, adj_tmp: int, grad_mu: int, grad_lam: int):
+        self._check(self._L.mpm_rollout_backward(
+            self.h, dt, int(n_substeps), int(every), C.c_void_p(ckpts), C.c_void_p(seg_states),
+            C.c_void_p(adj), C.c_void_p(adj_tmp), C.c_void_p(grad_mu), C.c_void_p(grad_lam)),
+            "mpm_rollout_backward")
 
     def state_save(self, dst_ptr: int):
         self._check(self._L.mpm_state_save(self.h, C.c_void_p(dst_ptr)), "mpm_state_save")
