@@ -166,8 +166,10 @@ def test_forward_matches_plain_substeps(zsmpm_mod):
                         torch.tensor(E, device="cuda")).cpu().numpy()
     p = parts.copy()
     p.v = v0.astype(np.float32)
-    mu, lam = S.lame(E, scene.materials[0].nu)
-    p.mu, p.lam = mu.astype(np.float32), lam.astype(np.float32)
+    # the rollout's own mu, lam (torch divides by a scalar through its
+    # reciprocal, so numpy's quotients can differ by an ulp)
+    mu, lam = sim.lame(torch.tensor(E, device="cuda"))
+    p.mu, p.lam = mu.float().cpu().numpy(), lam.float().cpu().numpy()
     with zsmpm_mod.Context(scene, max_particles=p.n) as ctx:
         ctx.upload(p)
         ctx.substep(scene.dt, 20)

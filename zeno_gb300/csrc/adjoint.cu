@@ -8,11 +8,12 @@
 //         x' = x + dt v',  F' = (I + dt C') F
 // Given the adjoints (x', v', C', F')-bar of the next state, the three
 // kernels here produce the adjoints of this state and of mu, lam:
-//   k_g2p_adjoint   per particle block: recomputes G2P, takes F'b back through
-//                   the Drucker-Prager projection (sand), forms
+//   k_g2p_adjoint_particles  per particle: recomputes G2P's C', takes F'b back
+//                   through the Drucker-Prager projection (sand), forms
 //                   Cb = C'b + dt F'b F^T, vb = v'b + dt x'b, F-bar = (I + dt C')^T F'b,
-//                   x-bar through the weights, and scatters the node adjoint
-//                   v_i-bar += W (vb + Dinv Cb (x_i - x_p)) into tiles
+//                   x-bar through the weights (stencil moments), and writes
+//                   the record of its node adjoint W (vb + Dinv Cb (x_i - x_p))
+//   k_g2p_adjoint_scatter    per particle block: the records into tiles
 //                   (tile_scatter: deterministic, no atomics)
 //   k_grid_adjoint  per node: the tiles' sum, the boundary's transpose, then
 //                   mv_i-bar = v-bar / m_i, m_i-bar = -v-bar . mv_i / m_i^2
@@ -26,6 +27,7 @@
 // writes this one at p; the mu / lam gradients go by upload index.
 #include <cuda_runtime.h>
 
+#include "adj_moments.cuh"
 #include "binning.cuh"
 #include "colliders.cuh"
 #include "mpm_math.cuh"
@@ -50,26 +52,32 @@ __device__ __forceinline__ int gb_of(const DevPtrs &d, const SceneParams &S, int
   return d.dir_gb[dir + ((t >> 2) * dy + ((t >> 1) & 1)) * dz + (t & 1)];
 }
 
-// 216 node float4 staged after the tile smem, at a 16-byte boundary
-constexpr int kAdjSgOffset = (kP2GSmem + 15) & ~15;
-constexpr int kAdjSmem = kAdjSgOffset + kNodes * 16;
-static_assert(kAdjSgOffset % 16 == 0, "float4 staging must be 16-byte aligned");
+// Scatter records of the G2P adjoint, one per particle at its sorted
+// position: b (3), A (9, row-major), f (3) as in tile_stage, then the cell
+// (int32 bits): the node adjoint of stencil node o is W (b + A o dx).
+constexpr int kAdjRec = 16;
 
-__global__ void __launch_bounds__(kP2GThreads)
-    k_g2p_adjoint(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
-                  const float *__restrict__ an, float *__restrict__ ap, float *__restrict__ gmu,
-                  float *__restrict__ glam, long long n) {
-  extern __shared__ __align__(16) unsigned char adj_smem[];
-  const TileSmem ts = tile_smem(adj_smem);
-  float4 *sg = reinterpret_cast<float4 *>(adj_smem + kAdjSgOffset);
+// Per-particle part of the G2P adjoint.  A CTA takes particle blocks
+// (grid-stride over the partition), stages the block's 216 node velocities,
+// and gives one particle to each thread: the node sums it needs are stencil
+// moments (adj_moments), the forward C' among them; then the Drucker-Prager
+// projection's adjoint (sand), Cb, F-bar, x-bar, and the scatter record.
+constexpr int kAdjPThreads = 128;
+
+__global__ void __launch_bounds__(kAdjPThreads, 4)
+    k_g2p_adjoint_particles(DevPtrs d, const float *__restrict__ pin,
+                            const int32_t *__restrict__ iin, const float *__restrict__ an,
+                            float *__restrict__ ap, float *__restrict__ gmu,
+                            float *__restrict__ glam, float *__restrict__ rec, long long n) {
+  __shared__ float4 sg[kNodes];
   __shared__ int sgb[8];
   const SimParams &P = *d.prm;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const int tid = threadIdx.x;
   const bool lame = P.has_lame != 0;
+  const long long cap = d.cap;
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    tile_zero(ts);
     const int dir = d.bk_dir[b];
     const SceneParams &S = d.scn[scene_of_dir(d, dir)];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
@@ -77,154 +85,171 @@ __global__ void __launch_bounds__(kP2GThreads)
     int K[3];
     origin_of(S, dir - S.dir_off, K);
     __syncthreads();
-    for (int nd = tid; nd < kNodes; nd += kP2GThreads) {
+    for (int nd = tid; nd < kNodes; nd += kAdjPThreads) {
       const int lx = nd / 36, ly = (nd / 6) % 6, lz = nd % 6;
       const int gb = sgb[((lx >> 2) << 2) | ((ly >> 2) << 1) | (lz >> 2)];
       const int cell = ((lx & 3) << 4) | ((ly & 3) << 2) | (lz & 3);
       sg[nd] = gb >= 0 ? d.grid[(long long)gb * 64 + cell] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    __syncthreads();
+    const int start = d.bk_start[b];
+    const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
+    for (int j = tid; j < cnt; j += kAdjPThreads) {
+      // the particle's slot p in this state and its slot sp in the next
+      // (the forward G2P writes it at its sorted position)
+      const int sp = start + j;
+      const int p = d.perm[sp];
+      const int id = iin[iidx(IC_ID, p)];
+      float x[3], F[9], xb[3], vb[3], Cb[9], Fb[9];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        x[k] = pin[pidx((CH_X + k), p)];
+        xb[k] = an[(AJ_X + k) * n + sp];
+        vb[k] = an[(AJ_V + k) * n + sp] + dt * xb[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        F[k] = pin[pidx((CH_F + k), p)];
+        Fb[k] = an[(AJ_F + k) * n + sp];
+        Cb[k] = an[(AJ_C + k) * n + sp];
+      }
+      const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
+                     s2 = stencil1(x[2], inv_dx);
+      const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
+      const bool inside = (unsigned)l0 <= 3u && (unsigned)l1 <= 3u && (unsigned)l2 <= 3u;
+      if (!inside) atomicOr(&d.cnt->status, ST_STENCIL);
+      AdjMoments M;
+      const AxisFactors A0 = axis_factors(s0, dx, inv_dx), A1 = axis_factors(s1, dx, inv_dx),
+                        A2 = axis_factors(s2, dx, inv_dx);
+      if (inside) {
+        adj_moments<false>(sg, l0, l1, l2, A0, A1, A2, M);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          M.W[c] = 0.f;
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            M.X[a][c] = M.D[a][c] = 0.f;
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb) M.DX[a][bb][c] = 0.f;
+          }
+        }
+      }
+      // forward C' (times 1/Dinv) of this substep: Cn[c][b] = sum W g_c xx_b
+      float Cn[9];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) Cn[c * 3 + bb] = M.X[bb][c];
+      // Drucker-Prager return mapping: F'b is the adjoint of the projected
+      // F; take it back to the trial F = (I + dt C') F
+      const MatParams mp = d.mats[min(max(iin[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
+      if (mp.type != MPM_EOS && mp.plastic == MPM_PLASTIC_NADP) {
+        float Ft[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            Ft[r * 3 + c] = F[r * 3 + c] + dt * Dinv *
+                                               (Cn[r * 3 + 0] * F[0 * 3 + c] +
+                                                Cn[r * 3 + 1] * F[1 * 3 + c] +
+                                                Cn[r * 3 + 2] * F[2 * 3 + c]);
+        const float mu = lame ? pin[pidx(CH_MU, p)] : mp.mu;
+        const float lam = lame ? pin[pidx(CH_LAM, p)] : mp.lam;
+        float mub = 0.f, lamb = 0.f;
+        dp_projection_vjp(mu, lam, mp.alpha, Ft, Fb, mub, lamb);
+        gmu[id] += mub;
+        glam[id] += lamb;
+      }
+      // C'b += dt F'b F^T
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          Cb[r * 3 + c] += dt * (Fb[r * 3] * F[c * 3] + Fb[r * 3 + 1] * F[c * 3 + 1] +
+                                 Fb[r * 3 + 2] * F[c * 3 + 2]);
+      // x-bar through the weights: with s_n = g_n . vb + Dinv g_n . (Cb xx_n),
+      //   gx_a = sum dW_a s_n - Dinv sum W (Cb^T g_n)_a
+      //        = vb . D[a] + Dinv sum_bc Cb_cb DX[a][b][c] - Dinv sum_c Cb_ca W[c]
+      float gx[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        float t = 0.f, u = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          t = fmaf(vb[c], M.D[a][c], t);
+          u = fmaf(-Cb[c * 3 + a], M.W[c], u);
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb) u = fmaf(Cb[c * 3 + bb], M.DX[a][bb][c], u);
+        }
+        gx[a] = fmaf(Dinv, u, t);
+      }
+      // F-bar = (I + dt C')^T F'b
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          ap[(AJ_F + r * 3 + c) * n + p] =
+              Fb[r * 3 + c] + dt * Dinv *
+                                  (Cn[0 * 3 + r] * Fb[0 * 3 + c] + Cn[1 * 3 + r] * Fb[1 * 3 + c] +
+                                   Cn[2 * 3 + r] * Fb[2 * 3 + c]);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) ap[(AJ_X + k) * n + p] = xb[k] + gx[k];
+      // the scatter record of W (vb + Dinv Cb (x_i - x_p)): b = vb - dx A f, A = Dinv Cb
+      const float f[3] = {s0.f, s1.f, s2.f};
+      float A[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) A[k] = inside ? Dinv * Cb[k] : 0.0f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        rec[a * cap + sp] = inside ? vb[a] - dx * (A[a * 3] * f[0] + A[a * 3 + 1] * f[1] +
+                                                   A[a * 3 + 2] * f[2])
+                                   : 0.0f;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) rec[(3 + k) * cap + sp] = A[k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) rec[(12 + k) * cap + sp] = f[k];
+      rec[15 * cap + sp] = __int_as_float(d.pkey[p] & 63);
+    }
+    __syncthreads();  // sg reused by the next block
+  }
+}
+
+// Scatter part of the G2P adjoint: per particle block, its records (read
+// in sorted order) into the block's tile of node adjoints (tile_scatter:
+// deterministic, no atomics).
+__global__ void __launch_bounds__(kP2GThreads)
+    k_g2p_adjoint_scatter(DevPtrs d, const float *__restrict__ rec) {
+  extern __shared__ __align__(16) unsigned char adj_smem[];
+  const TileSmem ts = tile_smem(adj_smem);
+  const SimParams &P = *d.prm;
+  const int nb = d.cnt->n_buckets;
+  const int tid = threadIdx.x;
+  const long long cap = d.cap;
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    tile_zero(ts);
+    const int dir = d.bk_dir[b];
+    const SceneParams &S = d.scn[scene_of_dir(d, dir)];
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
     for (int c0 = 0; c0 < cnt; c0 += kP2GChunk) {
       const int nc = min(kP2GChunk, cnt - c0);
       __syncthreads();
       for (int j = tid; j < nc; j += kP2GThreads) {
-        // the particle's slot p in this state and its slot sp in the next
-        // (the forward G2P writes it at its sorted position)
-        const int sp = start + c0 + j;
-        const int p = d.perm[sp];
-        const int id = iin[iidx(IC_ID, p)];
-        float x[3], F[9], xb[3], vb[3], Cb[9], Fb[9];
+        const long long sp = start + c0 + j;
+        float bv[3], A[9], f[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          x[k] = pin[pidx((CH_X + k), p)];
-          xb[k] = an[(AJ_X + k) * n + sp];
-          vb[k] = an[(AJ_V + k) * n + sp] + dt * xb[k];
-        }
+        for (int k = 0; k < 3; ++k) bv[k] = rec[k * cap + sp];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          F[k] = pin[pidx((CH_F + k), p)];
-          Fb[k] = an[(AJ_F + k) * n + sp];
-          Cb[k] = an[(AJ_C + k) * n + sp];
-        }
-        const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
-                       s2 = stencil1(x[2], inv_dx);
-        const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
-        float dw0[3], dw1[3], dw2[3];
-        stencil_dw(s0.f, dw0);
-        stencil_dw(s1.f, dw1);
-        stencil_dw(s2.f, dw2);
-        float Cn[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        float gx[3] = {0.f, 0.f, 0.f};
-        const bool inside = (unsigned)l0 <= 3u && (unsigned)l1 <= 3u && (unsigned)l2 <= 3u;
-        if (!inside) atomicOr(&d.cnt->status, ST_STENCIL);
-        // forward C' (times 1/Dinv) of this substep
-        if (inside) {
+        for (int k = 0; k < 9; ++k) A[k] = rec[(3 + k) * cap + sp];
 #pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int jj = 0; jj < 3; ++jj)
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                const float4 g4 = sg[((l0 + i) * 6 + (l1 + jj)) * 6 + (l2 + kk)];
-                const float g[3] = {g4.y, g4.z, g4.w};
-                const float W = s0.w[i] * s1.w[jj] * s2.w[kk];
-                const float xx[3] = {((float)i - s0.f) * dx, ((float)jj - s1.f) * dx,
-                                     ((float)kk - s2.f) * dx};
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                  Cn[a * 3 + 0] += W * g[a] * xx[0];
-                  Cn[a * 3 + 1] += W * g[a] * xx[1];
-                  Cn[a * 3 + 2] += W * g[a] * xx[2];
-                }
-              }
-        }
-        // Drucker-Prager return mapping: F'b is the adjoint of the projected
-        // F; take it back to the trial F = (I + dt C') F
-        const MatParams mp = d.mats[min(max(iin[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
-        if (mp.type != MPM_EOS && mp.plastic == MPM_PLASTIC_NADP) {
-          float Ft[9];
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-              Ft[r * 3 + c] = F[r * 3 + c] + dt * Dinv *
-                                                 (Cn[r * 3 + 0] * F[0 * 3 + c] +
-                                                  Cn[r * 3 + 1] * F[1 * 3 + c] +
-                                                  Cn[r * 3 + 2] * F[2 * 3 + c]);
-          const float mu = lame ? pin[pidx(CH_MU, p)] : mp.mu;
-          const float lam = lame ? pin[pidx(CH_LAM, p)] : mp.lam;
-          float mub = 0.f, lamb = 0.f;
-          dp_projection_vjp(mu, lam, mp.alpha, Ft, Fb, mub, lamb);
-          gmu[id] += mub;
-          glam[id] += lamb;
-        }
-        // C'b += dt F'b F^T
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            Cb[r * 3 + c] += dt * (Fb[r * 3] * F[c * 3] + Fb[r * 3 + 1] * F[c * 3 + 1] +
-                                   Fb[r * 3 + 2] * F[c * 3 + 2]);
-        if (inside) {
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int jj = 0; jj < 3; ++jj)
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                const float4 g4 = sg[((l0 + i) * 6 + (l1 + jj)) * 6 + (l2 + kk)];
-                const float g[3] = {g4.y, g4.z, g4.w};
-                const float W = s0.w[i] * s1.w[jj] * s2.w[kk];
-                const float dW[3] = {dw0[i] * s1.w[jj] * s2.w[kk] * inv_dx,
-                                     s0.w[i] * dw1[jj] * s2.w[kk] * inv_dx,
-                                     s0.w[i] * s1.w[jj] * dw2[kk] * inv_dx};
-                const float xx[3] = {((float)i - s0.f) * dx, ((float)jj - s1.f) * dx,
-                                     ((float)kk - s2.f) * dx};
-                float Cx[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-                  Cx[a] = Cb[a * 3] * xx[0] + Cb[a * 3 + 1] * xx[1] + Cb[a * 3 + 2] * xx[2];
-                const float s = g[0] * vb[0] + g[1] * vb[1] + g[2] * vb[2] +
-                                Dinv * (g[0] * Cx[0] + g[1] * Cx[1] + g[2] * Cx[2]);
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                  // x-bar via dW and via (x_i - x_p)
-                  const float CTg = Cb[0 * 3 + a] * g[0] + Cb[1 * 3 + a] * g[1] + Cb[2 * 3 + a] * g[2];
-                  gx[a] += dW[a] * s - Dinv * W * CTg;
-                }
-              }
-        }
-        // F-bar = (I + dt C')^T F'b
-        float Fbn[9];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            Fbn[r * 3 + c] = Fb[r * 3 + c] + dt * Dinv *
-                                                 (Cn[0 * 3 + r] * Fb[0 * 3 + c] +
-                                                  Cn[1 * 3 + r] * Fb[1 * 3 + c] +
-                                                  Cn[2 * 3 + r] * Fb[2 * 3 + c]);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) ap[(AJ_X + k) * n + p] = xb[k] + gx[k];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) ap[(AJ_F + k) * n + p] = Fbn[k];
-        // node scatter of W (vb + Dinv Cb (x_i - x_p)): b = vb - dx A f, A = Dinv Cb
-        float A[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) A[k] = inside ? Dinv * Cb[k] : 0.0f;
-        const float f[3] = {s0.f, s1.f, s2.f};
-        float bv[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-          bv[a] = inside ? vb[a] - dx * (A[a * 3] * f[0] + A[a * 3 + 1] * f[1] + A[a * 3 + 2] * f[2])
-                         : 0.0f;
-        tile_stage(ts, j, 0.0f, bv, A, f, d.pkey[p] & 63);
+        for (int k = 0; k < 3; ++k) f[k] = rec[(12 + k) * cap + sp];
+        tile_stage(ts, j, 0.0f, bv, A, f, __float_as_int(rec[15 * cap + sp]));
       }
       __syncthreads();
       tile_cell_ranges(ts, nc);
       __syncthreads();
-      tile_scatter(ts, dx);
+      tile_scatter(ts, S.dx);
     }
     __syncthreads();
     tile_store(ts, d.ptile_adj + (long long)b * kTileNodes);
@@ -321,7 +346,7 @@ __global__ void k_grid_adjoint(DevPtrs d) {
 
 constexpr int kP2GAdjThreads = 128;
 
-__global__ void __launch_bounds__(kP2GAdjThreads)
+__global__ void __launch_bounds__(kP2GAdjThreads, 4)
     k_p2g_adjoint(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
                   float *__restrict__ ap, float *__restrict__ gmu, float *__restrict__ glam,
                   long long n) {
@@ -379,46 +404,37 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
       const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx),
                      s2 = stencil1(x[2], inv_dx);
       const int l0 = s0.base - K[0], l1 = s1.base - K[1], l2 = s2.base - K[2];
-      float dw0[3], dw1[3], dw2[3];
-      stencil_dw(s0.f, dw0);
-      stencil_dw(s1.f, dw1);
-      stencil_dw(s2.f, dw2);
       float vbar[3] = {0.f, 0.f, 0.f}, Ab[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
       float gx[3] = {0.f, 0.f, 0.f};
       if ((unsigned)l0 > 3u || (unsigned)l1 > 3u || (unsigned)l2 > 3u) {
         atomicOr(&d.cnt->status, ST_STENCIL);
       } else {
+        // node sums as stencil moments of (m-bar, mv-bar): with
+        //   u_n = m-bar_n m + mv-bar_n . (m v + A xx_n),
+        // v-bar_a = sum W mv-bar_a, A-bar_ab = sum W mv-bar_a xx_b and
+        // x-bar_a = sum dW_a u_n - sum W (A^T mv-bar_n)_a
+        AdjMoments M;
+        const AxisFactors A0 = axis_factors(s0, dx, inv_dx), A1 = axis_factors(s1, dx, inv_dx),
+                          A2 = axis_factors(s2, dx, inv_dx);
+        adj_moments<true>(sg, l0, l1, l2, A0, A1, A2, M);
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+        for (int a = 0; a < 3; ++a) {
+          vbar[a] = M.W[a];
 #pragma unroll
-          for (int jj = 0; jj < 3; ++jj)
+          for (int bb = 0; bb < 3; ++bb) Ab[a * 3 + bb] = M.X[bb][a];
+        }
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const float4 g4 = sg[((l0 + i) * 6 + (l1 + jj)) * 6 + (l2 + q)];
-              const float mb = g4.x, gb3[3] = {g4.y, g4.z, g4.w};
-              const float W = s0.w[i] * s1.w[jj] * s2.w[q];
-              const float dW[3] = {dw0[i] * s1.w[jj] * s2.w[q] * inv_dx,
-                                   s0.w[i] * dw1[jj] * s2.w[q] * inv_dx,
-                                   s0.w[i] * s1.w[jj] * dw2[q] * inv_dx};
-              const float xx[3] = {((float)i - s0.f) * dx, ((float)jj - s1.f) * dx,
-                                   ((float)q - s2.f) * dx};
-              float u = mb * mass;  // d(m_i)/dW m-bar + mv-bar . (m v + A xx)
+        for (int a = 0; a < 3; ++a) {
+          float t = mass * M.Dm[a];
 #pragma unroll
-              for (int a = 0; a < 3; ++a) {
-                const float val = mass * v[a] + A[a * 3] * xx[0] + A[a * 3 + 1] * xx[1] +
-                                  A[a * 3 + 2] * xx[2];
-                u += gb3[a] * val;
-                vbar[a] += W * gb3[a];
-                Ab[a * 3 + 0] += W * gb3[a] * xx[0];
-                Ab[a * 3 + 1] += W * gb3[a] * xx[1];
-                Ab[a * 3 + 2] += W * gb3[a] * xx[2];
-              }
+          for (int c = 0; c < 3; ++c) {
+            t = fmaf(mass * v[c], M.D[a][c], t);
+            t = fmaf(-A[c * 3 + a], M.W[c], t);
 #pragma unroll
-              for (int a = 0; a < 3; ++a) {
-                const float ATg = A[0 * 3 + a] * gb3[0] + A[1 * 3 + a] * gb3[1] + A[2 * 3 + a] * gb3[2];
-                gx[a] += dW[a] * u - W * ATg;
-              }
-            }
+            for (int bb = 0; bb < 3; ++bb) t = fmaf(A[c * 3 + bb], M.DX[a][bb][c], t);
+          }
+          gx[a] = t;
+        }
       }
       // tau-bar = -dt Dinv vol A-bar; stress adjoint
       float tb[9], Fb[9];
@@ -457,9 +473,11 @@ __global__ void __launch_bounds__(kP2GAdjThreads)
 
 void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, float *gmu,
                         float *glam, long long n, cudaStream_t s) {
-  cudaFuncSetAttribute(k_g2p_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, kAdjSmem);
-  k_g2p_adjoint<<<d.num_sms * 2, kP2GThreads, kAdjSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur], an,
-                                                            ap, gmu, glam, n);
+  k_g2p_adjoint_particles<<<d.num_sms * 4, kAdjPThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur], an,
+                                                                ap, gmu, glam, d.adj_rec, n);
+  cudaFuncSetAttribute(k_g2p_adjoint_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kP2GSmem);
+  k_g2p_adjoint_scatter<<<d.num_sms * 4, kP2GThreads, kP2GSmem, s>>>(d, d.adj_rec);
 }
 
 void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s) {

@@ -1660,6 +1660,7 @@ int32_t mpm_set_differentiable(mpm_ctx *c, int32_t on) {
   if (on && !c->d.ptile_adj &&
       (rc = dalloc(c, &c->d.ptile_adj, (size_t)c->d.cap_gblocks * kTileNodes)))
     return rc;
+  if (on && !c->d.adj_rec && (rc = dalloc(c, &c->d.adj_rec, (size_t)16 * c->d.cap))) return rc;
   if (on && !c->prm.has_lame) {  // the states carry per-particle mu / lam
     launch_lame_from_materials(c->d, c->cur, c->stream);
     if ((rc = launch_check("per-particle Lame parameters"))) return rc;

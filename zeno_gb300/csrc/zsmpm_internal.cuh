@@ -232,6 +232,7 @@ struct DevPtrs {
                       // (ComputeParticleBeta; 0 at upload), outside the
                       // double-buffered store so that APIC substeps keep it
   float4 *ptile_adj;  // the same for the G2P adjoint (differentiable mode)
+  float *adj_rec;     // G2P adjoint scatter records, 16 planes of `cap` (differentiable mode)
   ColliderDev *colliders;  // kMaxColliders entries (device)
   int32_t *near_gb;        // cap_gblocks entries: the grid blocks near a collider
   float *vms;              // ComputeVonMises per particle, by upload index (0 at upload)
