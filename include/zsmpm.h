@@ -375,18 +375,26 @@ int32_t mpm_state_load(mpm_ctx *ctx, const float *src_planes);
  * equation-of-state fluid (MPM_ERR_INVALID). */
 int32_t mpm_adjoint_substep(mpm_ctx *ctx, float dt, const float *adj_next, float *adj_prev,
                             float *grad_mu, float *grad_lam);
-/* Forward of a rollout with checkpoints, in one call: loads state0, runs
- * n_substeps substeps of dt, saving the state before substep k * every into
- * ckpts + k * MPM_STATE_PLANES * n (k = 0 .. ceil(n_substeps / every) - 1)
- * and the final state into final_state (all device memory). */
+/* Size of one rollout snapshot: the whole particle store of a state as the
+ * substep keeps it (tiled channels, the stored stress included), opaque to
+ * the caller: 37 x (n rounded up to a multiple of 32) floats. */
+int32_t mpm_snapshot_floats(mpm_ctx *ctx, int64_t *floats);
+/* Forward of a rollout with checkpoints, in one call: loads state0 (state
+ * planes), runs n_substeps substeps of dt, saving a snapshot of the state
+ * before substep k * every into ckpts + k * mpm_snapshot_floats (k = 0 ..
+ * ceil(n_substeps / every) - 1), and the final state into final_state
+ * (state planes); all device memory. */
 int32_t mpm_rollout_forward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
                             const float *state0, float *ckpts, float *final_state);
 /* Backward of that rollout, in one call: adj holds the adjoint of the final
  * state; the segments run last to first, each recomputed from its checkpoint
- * into seg_states (every x MPM_STATE_PLANES x n floats) and then taken back
- * through mpm_adjoint_substep, so that adj ends as the adjoint of state0
- * (adj_tmp: MPM_ADJ_PLANES x n floats of scratch) and grad_mu / grad_lam
- * (by upload index) gain the gradients of every substep. */
+ * (each substep writing the next state straight into its snapshot in
+ * seg_states, `every` snapshots) and then taken back through the adjoint
+ * substep on each snapshot in place, so that adj ends as the adjoint of
+ * state0 (adj_tmp: MPM_ADJ_PLANES x n floats of scratch) and grad_mu /
+ * grad_lam (by upload index) gain the gradients of every substep.  The
+ * context's own particle store is left unspecified: load a state before
+ * stepping it again. */
 int32_t mpm_rollout_backward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
                              const float *ckpts, float *seg_states, float *adj, float *adj_tmp,
                              float *grad_mu, float *grad_lam);

@@ -1734,16 +1734,84 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
   return MPM_OK;
 }
 
+int32_t mpm_snapshot_floats(mpm_ctx *c, int64_t *floats) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!floats) return fail(MPM_ERR_INVALID, "null argument");
+  *floats = tiled_elems(c->prm.n, NCH) + tiled_elems(c->prm.n, NICH);
+  return MPM_OK;
+}
+
+namespace {
+
+// A snapshot buffer as a particle store: the tiled float channels, then the
+// tiled int channels of n particles (128-byte aligned: whole tiles).
+struct SnapStore {
+  float *f;
+  int32_t *i;
+};
+SnapStore snap_store(const mpm_ctx *c, float *base) {
+  return SnapStore{base, reinterpret_cast<int32_t *>(base + tiled_elems(c->prm.n, NCH))};
+}
+
+int32_t snapshot_copy(mpm_ctx *c, SnapStore dst, const float *src_f, const int32_t *src_i) {
+  const long long n = c->prm.n;
+  ZS_CUDA(cudaMemcpyAsync(dst.f, src_f, (size_t)tiled_elems(n, NCH) * sizeof(float),
+                          cudaMemcpyDeviceToDevice, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(dst.i, src_i, (size_t)tiled_elems(n, NICH) * sizeof(int32_t),
+                          cudaMemcpyDeviceToDevice, c->stream));
+  return MPM_OK;
+}
+
+// Runs the kernels with the particle store pair (a -> b) in place of the
+// context's own buffers: store 0 = a, store 1 = b, current 0.
+struct StoreSwap {
+  mpm_ctx *c;
+  float *pb[2];
+  int32_t *ib[2];
+  int cur;
+  explicit StoreSwap(mpm_ctx *ctx) : c(ctx), cur(ctx->cur) {
+    for (int k = 0; k < 2; ++k) {
+      pb[k] = c->d.pbuf[k];
+      ib[k] = c->d.ibuf[k];
+    }
+  }
+  void use(SnapStore a, SnapStore b) {
+    c->d.pbuf[0] = a.f;
+    c->d.ibuf[0] = a.i;
+    c->d.pbuf[1] = b.f;
+    c->d.ibuf[1] = b.i;
+    c->cur = 0;
+  }
+  ~StoreSwap() {
+    for (int k = 0; k < 2; ++k) {
+      c->d.pbuf[k] = pb[k];
+      c->d.ibuf[k] = ib[k];
+    }
+    c->cur = cur;
+    // the context's own store no longer matches the directory's counts
+    c->needs_full_clear = true;
+    c->binned = false;
+    c->partition_valid = false;
+  }
+};
+
+}  // namespace
+
 int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
                             const float *state0, float *ckpts, float *final_state) {
   int32_t rc = check(c);
   if (rc) return rc;
   if (n_substeps < 0 || every <= 0 || !state0 || !final_state || (n_substeps > 0 && !ckpts))
     return fail(MPM_ERR_INVALID, "invalid rollout arguments");
-  const size_t plane = (size_t)MPM_STATE_PLANES * (size_t)c->prm.n;
+  const long long n = c->prm.n;
+  const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));
   if ((rc = mpm_state_load(c, state0))) return rc;
   for (int32_t s = 0; s < n_substeps; ++s) {
-    if (s % every == 0 && (rc = mpm_state_save(c, ckpts + (size_t)(s / every) * plane))) return rc;
+    if (s % every == 0 &&
+        (rc = snapshot_copy(c, snap_store(c, ckpts + (size_t)(s / every) * snap), c->d.pbuf[c->cur],
+                            c->d.ibuf[c->cur])))
+      return rc;
     if ((rc = mpm_substep(c, dt, 1))) return rc;
   }
   return mpm_state_save(c, final_state);
@@ -1754,25 +1822,61 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
                              float *grad_mu, float *grad_lam) {
   int32_t rc = check(c);
   if (rc) return rc;
+  if ((rc = settle(c))) return rc;
   if (n_substeps < 0 || every <= 0 || (n_substeps > 0 && (!ckpts || !seg_states)) || !adj ||
       !adj_tmp || !grad_mu || !grad_lam)
     return fail(MPM_ERR_INVALID, "invalid rollout arguments");
-  const size_t n = (size_t)c->prm.n;
-  const size_t plane = (size_t)MPM_STATE_PLANES * n;
+  if (!c->d.differentiable) return fail(MPM_ERR_STATE, "the adjoint needs mpm_set_differentiable(ctx, 1)");
+  if (!c->differentiable)
+    return fail(MPM_ERR_INVALID,
+                "the adjoint covers fixed-corotated, Neo-Hookean and StVK-Hencky (with or without "
+                "the Drucker-Prager projection) materials, not the equation-of-state fluid");
+  for (const ColliderDev &cd : c->colliders)
+    if (cd.db[0] != 0.0f || cd.db[1] != 0.0f || cd.db[2] != 0.0f || cd.ds != 0.0f)
+      return fail(MPM_ERR_INVALID, "the adjoint takes static colliders only");
+  const long long n = c->prm.n;
+  const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));
   float *a = adj, *b = adj_tmp;  // adjoint of the next state, of this one
   const int32_t n_seg = (n_substeps + every - 1) / every;
+  StoreSwap swap(c);
+  if ((rc = set_dt(c, dt))) return rc;
   for (int32_t seg = n_seg - 1; seg >= 0; --seg) {
     const int32_t s0 = seg * every, s1 = std::min(s0 + every, n_substeps);
-    // recompute the segment from its checkpoint, keeping its states
-    if ((rc = mpm_state_load(c, ckpts + (size_t)seg * plane))) return rc;
-    for (int32_t s = s0; s < s1; ++s) {
-      if ((rc = mpm_state_save(c, seg_states + (size_t)(s - s0) * plane))) return rc;
-      if (s + 1 < s1 && (rc = mpm_substep(c, dt, 1))) return rc;
+    // the segment's states: its checkpoint, then the recomputed ones, each
+    // substep reading one snapshot and writing the next (no copies)
+    auto state = [&](int32_t s) {
+      return s == s0 ? snap_store(c, const_cast<float *>(ckpts) + (size_t)seg * snap)
+                     : snap_store(c, seg_states + (size_t)(s - s0) * snap);
+    };
+    set_auto_step(c, 1);
+    if ((rc = push_params(c))) return rc;
+    c->needs_full_clear = true;
+    c->binned = false;
+    for (int32_t s = s0; s + 1 < s1; ++s) {
+      swap.use(state(s), state(s + 1));
+      if ((rc = prepare_partition(c))) return rc;
+      enqueue_bin_if_needed(c);
+      enqueue_substep(c, 0);  // bins the new positions: the next one needs no binning
+      if ((rc = launch_check("rollout recompute"))) return rc;
     }
-    // adjoint substeps, last to first
+    // adjoint substeps, last to first, each on its own snapshot
+    set_auto_step(c, 0);
+    if ((rc = push_params(c))) return rc;
+    const long long nn = c->prm.n;
     for (int32_t s = s1 - 1; s >= s0; --s) {
-      if ((rc = mpm_state_load(c, seg_states + (size_t)(s - s0) * plane))) return rc;
-      if ((rc = mpm_adjoint_substep(c, dt, a, b, grad_mu, grad_lam))) return rc;
+      swap.use(state(s), state(s));
+      c->needs_full_clear = true;  // the counts described another state
+      c->binned = false;
+      if ((rc = prepare_partition(c))) return rc;
+      enqueue_bin_if_needed(c);
+      enqueue_sort(c);
+      launch_p2g(c->d, 0, c->stream);
+      launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
+      if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
+      launch_g2p_adjoint(c->d, 0, a, b, grad_mu, grad_lam, nn, c->stream);
+      launch_grid_adjoint(c->d, c->stream);
+      launch_p2g_adjoint(c->d, 0, b, grad_mu, grad_lam, nn, c->stream);
+      if ((rc = launch_check("rollout adjoint"))) return rc;
       std::swap(a, b);
     }
   }

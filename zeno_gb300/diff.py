@@ -7,13 +7,15 @@ differentiable mode and exposes `rollout(v0, E) -> x_final` as a
 * forward: builds the initial state on the device (positions of the scene,
   v0, C = 0, F = I, per-particle mu / lam from Young's moduli E and the
   material's nu) and runs the whole rollout in one C-ABI call
-  (mpm_rollout_forward), which keeps the state every `ckpt_every` substeps
-  in device buffers owned by torch;
+  (mpm_rollout_forward), which keeps a snapshot of the particle store every
+  `ckpt_every` substeps in device buffers owned by torch;
 * backward: one C-ABI call (mpm_rollout_backward) walks the segments in
-  reverse; each segment is recomputed from its checkpoint (its states kept)
-  and the hand-written adjoint substep (G2P, grid update + boundary, P2G and
-  the stress) runs backwards through it.  Memory: one checkpoint per segment
-  plus one segment of states, 31 planes of n floats each.
+  reverse; each segment is recomputed from its checkpoint (each substep
+  writing the next state straight into a snapshot buffer) and the
+  hand-written adjoint substep (G2P, grid update + boundary, P2G and the
+  stress) runs backwards through the snapshots in place.  Memory: one
+  snapshot per segment plus one segment of snapshots, 37 floats per particle
+  each.
 
 The substep keeps the particle store sorted by block, so every state (and
 its adjoint) is in its own slot order; the state's upload-index plane maps
@@ -68,7 +70,8 @@ class Rollout:
             self.dev).view(torch.float32)
         s0[ID] = torch.arange(n, dtype=torch.int32, device=self.dev).view(torch.float32)
         self.state0 = s0
-        self.peak_checkpoint_bytes = (self.n_ckpt + self.ckpt_every + 1) * PLANES * n * 4
+        self.snap = self.ctx.snapshot_floats()  # floats of one store snapshot
+        self.peak_checkpoint_bytes = (self.n_ckpt + self.ckpt_every) * self.snap * 4
 
     def lame(self, E):
         nu = self.nu
@@ -93,7 +96,7 @@ class _RolloutFn(torch.autograd.Function):
             mu, lam = sim.lame(E.detach().to(sim.dev, torch.float64))
             state[MU] = mu.float()
             state[LAM] = lam.float()
-            ckpts = torch.empty(max(sim.n_ckpt, 1), PLANES, n, dtype=torch.float32,
+            ckpts = torch.empty(max(sim.n_ckpt, 1), sim.snap, dtype=torch.float32,
                                 device=sim.dev)
             final = torch.empty(PLANES, n, dtype=torch.float32, device=sim.dev)
             sim.ctx.rollout_forward(sim.dt, sim.n_substeps, sim.ckpt_every, state.data_ptr(),
@@ -120,7 +123,7 @@ class _RolloutFn(torch.autograd.Function):
             tmp = torch.empty_like(adj)
             gmu = torch.zeros(n, dtype=torch.float32, device=sim.dev)
             glam = torch.zeros(n, dtype=torch.float32, device=sim.dev)
-            seg = torch.empty(k, PLANES, n, dtype=torch.float32, device=sim.dev)
+            seg = torch.empty(k, sim.snap, dtype=torch.float32, device=sim.dev)
             sim.ctx.rollout_backward(sim.dt, sim.n_substeps, k, fctx.ckpts.data_ptr(),
                                      seg.data_ptr(), adj.data_ptr(), tmp.data_ptr(),
                                      gmu.data_ptr(), glam.data_ptr())

@@ -84,7 +84,7 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_substep", "mpm_substep_timed", "mpm_sync", "mpm_get_stats", "mpm_partition_download",
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_differentiable", "mpm_state_save",
-           "mpm_state_load", "mpm_adjoint_substep", "mpm_rollout_forward", "mpm_rollout_backward", "mpm_add_collider", "mpm_clear_colliders",
+           "mpm_state_load", "mpm_adjoint_substep", "mpm_rollout_forward", "mpm_rollout_backward", "mpm_snapshot_floats", "mpm_add_collider", "mpm_clear_colliders",
            "mpm_step_colliders", "mpm_set_auto_regrow", "mpm_get_domain"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
@@ -158,6 +158,7 @@ def load(path: str = LIB_PATH):
         "mpm_get_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
         "mpm_set_differentiable": ([P, i32], i32),
         "mpm_rollout_forward": ([P, f32, i32, i32, P, P, P], i32),
+        "mpm_snapshot_floats": ([P, P], i32),
         "mpm_rollout_backward": ([P, f32, i32, i32, P, P, P, P, P, P], i32),
         "mpm_set_auto_regrow": ([P, i32], i32),
         "mpm_get_domain": ([P, P, P, P], i32),
@@ -528,6 +529,11 @@ class Context:
     def set_differentiable(self, on: bool = True):
         self._check(self._L.mpm_set_differentiable(self.h, 1 if on else 0),
                     "mpm_set_differentiable")
+
+    def snapshot_floats(self) -> int:
+        v = C.c_int64(0)
+        self._check(self._L.mpm_snapshot_floats(self.h, C.byref(v)), "mpm_snapshot_floats")
+        return v.value
 
     def rollout_forward(self, dt, n_substeps: int, every: int, state0: int, ckpts: int,
                         final: int):
