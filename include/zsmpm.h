@@ -409,7 +409,18 @@ typedef struct mpm_launch_config {
   int32_t sort_ctas_per_sm;
   int32_t stream_ctas_per_sm; /* binning, scatter, grid gather */
   int32_t g2p_threads;        /* 128 or 256 */
+  int32_t p2g_shape;          /* MPM_P2G_* tile shape of the P2G column scatter */
+  int32_t gather_blocks;      /* grid blocks per CTA of the grid gather: 2, 4 or 8 (0: 4) */
 } mpm_launch_config;
+/* P2G tile shapes: threads per CTA and particles per chunk (the 16 cell
+ * columns of a block are scattered by 9-lane slots, three per warp) */
+enum {
+  MPM_P2G_192x128 = 0, /* default: one cell layer per chunk at 8 particles per cell */
+  MPM_P2G_192x192 = 1,
+  MPM_P2G_192x96 = 2,
+  MPM_P2G_256x128 = 3,
+  MPM_P2G_256x256 = 4
+};
 int32_t mpm_set_launch_config(mpm_ctx *ctx, const mpm_launch_config *cfg);
 int32_t mpm_get_launch_config(mpm_ctx *ctx, mpm_launch_config *cfg);
 

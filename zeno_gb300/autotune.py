@@ -1,7 +1,8 @@
 """Autotuner of the substep's launch shapes.
 
-The persistent kernels take their grid size (CTAs per SM) and, for G2P, the
-block size at run time (mpm_set_launch_config).  The tuner runs a coordinate
+The persistent kernels take their grid size (CTAs per SM), the G2P block
+size, the P2G tile shape (threads per CTA, particles per chunk) and the grid
+gather's blocks per CTA at run time (mpm_set_launch_config).  The tuner runs a coordinate
 search on the caller's own scene: each knob is varied in turn with the others
 held, and judged by the device time of the stages it drives (measured with
 CUDA events between the same kernels, mpm_substep_timed), so one knob's noise
@@ -22,9 +23,14 @@ KNOBS = {
     # knob: (candidates, stages whose time it drives)
     "g2p_threads": ([128, 256], ("g2p",)),
     "g2p_ctas_per_sm": ([0, 2, 3, 4, 6], ("g2p",)),
+    # P2G tile shape (threads per CTA x particles per chunk, MPM_P2G_*):
+    # 192x128, 192x192, 192x96, 256x128, 256x256
+    "p2g_shape": ([0, 1, 2, 3, 4], ("p2g",)),
     "p2g_ctas_per_sm": ([0, 1, 2, 3], ("p2g",)),
     "sort_ctas_per_sm": ([4, 8, 16], ("sort",)),
     "stream_ctas_per_sm": ([4, 8, 16], ("scatter", "grid_update")),
+    # grid blocks per CTA of the grid gather
+    "gather_blocks": ([2, 4, 8], ("grid_update",)),
 }
 
 

@@ -1622,11 +1622,15 @@ int32_t mpm_set_launch_config(mpm_ctx *c, const mpm_launch_config *cfg) {
   if (!cfg || cfg->p2g_ctas_per_sm < 0 || cfg->g2p_ctas_per_sm < 0 || cfg->sort_ctas_per_sm < 0 ||
       cfg->stream_ctas_per_sm < 0 || cfg->p2g_ctas_per_sm > 64 || cfg->g2p_ctas_per_sm > 64 ||
       cfg->sort_ctas_per_sm > 64 || cfg->stream_ctas_per_sm > 64 ||
-      (cfg->g2p_threads != 0 && cfg->g2p_threads != 128 && cfg->g2p_threads != 256))
+      (cfg->g2p_threads != 0 && cfg->g2p_threads != 128 && cfg->g2p_threads != 256) ||
+      cfg->p2g_shape < MPM_P2G_192x128 || cfg->p2g_shape > MPM_P2G_256x256 ||
+      (cfg->gather_blocks != 0 && cfg->gather_blocks != 2 && cfg->gather_blocks != 4 &&
+       cfg->gather_blocks != 8))
     return fail(MPM_ERR_INVALID, "bad launch configuration");
   ZS_CUDA(cudaStreamSynchronize(c->stream));
-  c->d.launch = LaunchConfig{cfg->p2g_ctas_per_sm, cfg->g2p_ctas_per_sm, cfg->sort_ctas_per_sm,
-                             cfg->stream_ctas_per_sm, cfg->g2p_threads};
+  c->d.launch = LaunchConfig{cfg->p2g_ctas_per_sm,    cfg->g2p_ctas_per_sm, cfg->sort_ctas_per_sm,
+                             cfg->stream_ctas_per_sm, cfg->g2p_threads,     cfg->p2g_shape,
+                             cfg->gather_blocks};
   configure_launches(c->d);
   for (int k = 0; k < 2; ++k)  // the captured graphs hold the old shapes
     if (c->graph[k]) {
@@ -1646,6 +1650,8 @@ int32_t mpm_get_launch_config(mpm_ctx *c, mpm_launch_config *cfg) {
   cfg->sort_ctas_per_sm = d.grid_sort / d.num_sms;
   cfg->stream_ctas_per_sm = d.grid_stream / d.num_sms;
   cfg->g2p_threads = d.g2p_threads;
+  cfg->p2g_shape = d.launch.p2g_shape;
+  cfg->gather_blocks = d.launch.gather_blocks == 0 ? 4 : d.launch.gather_blocks;
   return MPM_OK;
 }
 

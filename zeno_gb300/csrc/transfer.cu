@@ -59,43 +59,49 @@ namespace {
 // block at the nominal 8 particles per cell (16 cells x 8), so the 16
 // columns scatter equal shares before the chunk's barrier (a chunk of 192,
 // one and a half layers, gave half the columns twice the work: 7 % slower).
-constexpr int kColThreads = 192;
-constexpr int kColChunk = 128;
 constexpr int kColRaw = 23;            // x3 v3 C9 S6 m key
 constexpr int kColRecs = 16 * 9 * 6;  // float4 records: (column, oi oj, z)
 constexpr int kColMeta = 64;           // blocks per CTA whose metadata is staged
-// shared memory: raw[23][chunk] floats; spd[4][chunk] float4 (b0 b1 a00 a10),
-// (a01 a11 a02 a12), (b2 m a20 a21), (a22 wz0 wz1 wz2), laid out so that
-// the pairs the scatter combines with packed FP32x2 instructions are the
-// halves of one float4; sw[chunk][6] wx0..2 wy0..2; the records; the
-// chunk's cells; block metadata
-constexpr int kColOffSpd = kColRaw * kColChunk * 4;
-constexpr int kColOffW = kColOffSpd + 4 * kColChunk * 16;
-constexpr int kColOffRec = kColOffW + kColChunk * 6 * 4;
-constexpr int kColOffCell = kColOffRec + kColRecs * 16;
-constexpr int kColOffMeta = kColOffCell + ((kColChunk + 15) & ~15);
 // per-block launch metadata staged in shared memory (32 bytes)
 struct ColMeta {
   int start, cnt, dir, scene;
   int K[3];  // node index of the block's first node
   int pad;
 };
-constexpr int kColSmem = kColOffMeta + kColMeta * (int)sizeof(ColMeta);
-static_assert(kColOffSpd % 16 == 0 && kColOffRec % 16 == 0 && kColOffMeta % 16 == 0,
-              "float4 / int4 regions must be 16-byte aligned");
+// Shared-memory layout of k_p2g<NT, CH> (NT threads, chunks of CH <= NT
+// particles): raw[23][CH] floats; spd[4][CH] float4 (b0 b1 a00 a10),
+// (a01 a11 a02 a12), (b2 m a20 a21), (a22 wz0 wz1 wz2), laid out so that
+// the pairs the scatter combines with packed FP32x2 instructions are the
+// halves of one float4; sw[CH][6] wx0..2 wy0..2; the records; the chunk's
+// cells; block metadata
+template <int NT, int CH>
+struct ColLayout {
+  static_assert(CH <= NT && NT % 32 == 0 && NT >= 192, "a chunk is at most one particle per "
+                "thread, and 16 columns need 6 warps of three 9-lane slots");
+  static constexpr int off_spd = kColRaw * CH * 4;
+  static constexpr int off_w = off_spd + 4 * CH * 16;
+  static constexpr int off_rec = off_w + CH * 6 * 4;
+  static constexpr int off_cell = off_rec + kColRecs * 16;
+  static constexpr int off_meta = off_cell + ((CH + 15) & ~15);
+  static constexpr int smem = off_meta + kColMeta * (int)sizeof(ColMeta);
+  static_assert(off_spd % 16 == 0 && off_rec % 16 == 0 && off_meta % 16 == 0,
+                "float4 / int4 regions must be 16-byte aligned");
+};
 // raw channel slots
 constexpr int RC_X = 0, RC_V = 3, RC_C = 6, RC_S = 15, RC_M = 21, RC_KEY = 22;
 
-__global__ void __launch_bounds__(kColThreads, 4) k_p2g(DevPtrs d, const float *__restrict__ pin,
+template <int kColThreads, int kColChunk>
+__global__ void __launch_bounds__(kColThreads, kColThreads == 192 ? 4 : 3) k_p2g(DevPtrs d, const float *__restrict__ pin,
                                                      const int32_t *__restrict__ iin) {
+  using Lay = ColLayout<kColThreads, kColChunk>;
   if (ZSMPM_HALTED(d)) return;
   extern __shared__ __align__(16) unsigned char p2g_smem[];
   float(*raw)[kColChunk] = reinterpret_cast<float(*)[kColChunk]>(p2g_smem);
-  float4(*spd)[kColChunk] = reinterpret_cast<float4(*)[kColChunk]>(p2g_smem + kColOffSpd);
-  float(*sw)[6] = reinterpret_cast<float(*)[6]>(p2g_smem + kColOffW);
-  float4 *rec = reinterpret_cast<float4 *>(p2g_smem + kColOffRec);
-  unsigned char *scell = p2g_smem + kColOffCell;
-  ColMeta *meta = reinterpret_cast<ColMeta *>(p2g_smem + kColOffMeta);
+  float4(*spd)[kColChunk] = reinterpret_cast<float4(*)[kColChunk]>(p2g_smem + Lay::off_spd);
+  float(*sw)[6] = reinterpret_cast<float(*)[6]>(p2g_smem + Lay::off_w);
+  float4 *rec = reinterpret_cast<float4 *>(p2g_smem + Lay::off_rec);
+  unsigned char *scell = p2g_smem + Lay::off_cell;
+  ColMeta *meta = reinterpret_cast<ColMeta *>(p2g_smem + Lay::off_meta);
   const SimParams &P = *d.prm;
   const long long n = P.n;
   const float dt = P.dt;
@@ -343,12 +349,12 @@ __device__ __forceinline__ void update_node_at(const DevPtrs &d, int scene, cons
                                                float dt, int mode, const int (&I)[3], float4 &g,
                                                float &vmax);
 
-// One 64-thread group per grid block, 4 blocks per CTA: the group fetches its
+// One 64-thread group per grid block, kGatherBlocks (2, 4 or 8) blocks per
+// CTA, a launch knob: the group fetches its
 // block's scene, node origin and the (particle block) tiles of the 8 blocks
 // whose tiles can cover it once into shared memory; each thread then sums
 // its node's <= 8 tile entries and applies the update.
-constexpr int kGatherBlocks = 4;
-
+template <int kGatherBlocks>
 __global__ void __launch_bounds__(64 * kGatherBlocks) k_grid_gather(DevPtrs d, int mode) {
   if (ZSMPM_HALTED(d)) return;
   __shared__ int sbk[kGatherBlocks][8];
@@ -849,11 +855,27 @@ template <int NT> int g2p_occupancy() {
   return b > 0 ? b : 1;
 }
 
-void configure_launches(DevPtrs &d) {
+// the P2G tile shapes the launch knobs can pick: (threads, chunk)
+template <int NT, int CH> int p2g_occupancy() {
+  constexpr int smem = ColLayout<NT, CH>::smem;
+  cudaFuncSetAttribute(k_p2g<NT, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int a = 0;
-  cudaFuncSetAttribute(k_p2g, cudaFuncAttributeMaxDynamicSharedMemorySize, kColSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g, kColThreads, kColSmem);
-  a = a > 0 ? a : 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<NT, CH>, NT, smem);
+  return a > 0 ? a : 1;
+}
+
+int p2g_shape_occupancy(int shape) {
+  switch (shape) {
+    case 1: return p2g_occupancy<192, 192>();
+    case 2: return p2g_occupancy<192, 96>();
+    case 3: return p2g_occupancy<256, 128>();
+    case 4: return p2g_occupancy<256, 256>();
+    default: return p2g_occupancy<192, 128>();
+  }
+}
+
+void configure_launches(DevPtrs &d) {
+  const int a = p2g_shape_occupancy(d.launch.p2g_shape);
   const LaunchConfig &L = d.launch;
   const int gt = L.g2p_threads == 256 ? 256 : 128;
   const int g = gt == 256 ? g2p_occupancy<256>() : g2p_occupancy<128>();
@@ -864,14 +886,28 @@ void configure_launches(DevPtrs &d) {
   d.g2p_threads = gt;
 }
 
+template <int NT, int CH> void launch_p2g_shape(const DevPtrs &d, int cur, cudaStream_t s) {
+  k_p2g<NT, CH><<<d.grid_p2g, NT, ColLayout<NT, CH>::smem, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+}
+
 void launch_p2g(const DevPtrs &d, int cur, cudaStream_t s) {
   if (d.transfer != MPM_TRANSFER_APIC) return launch_p2g_flip(d, cur, s);
-  k_p2g<<<d.grid_p2g, kColThreads, kColSmem, s>>>(d, d.pbuf[cur], d.ibuf[cur]);
+  switch (d.launch.p2g_shape) {
+    case 1: return launch_p2g_shape<192, 192>(d, cur, s);
+    case 2: return launch_p2g_shape<192, 96>(d, cur, s);
+    case 3: return launch_p2g_shape<256, 128>(d, cur, s);
+    case 4: return launch_p2g_shape<256, 256>(d, cur, s);
+    default: return launch_p2g_shape<192, 128>(d, cur, s);
+  }
 }
 
 void launch_grid_gather(const DevPtrs &d, int mode, cudaStream_t s) {
   if (d.transfer != MPM_TRANSFER_APIC) return launch_grid_gather_flip(d, mode, s);
-  k_grid_gather<<<d.grid_stream, 64 * kGatherBlocks, 0, s>>>(d, mode);
+  switch (d.launch.gather_blocks) {
+    case 2: k_grid_gather<2><<<d.grid_stream * 2, 128, 0, s>>>(d, mode); return;
+    case 8: k_grid_gather<8><<<(d.grid_stream + 1) / 2, 512, 0, s>>>(d, mode); return;
+    default: k_grid_gather<4><<<d.grid_stream, 256, 0, s>>>(d, mode); return;
+  }
 }
 
 // ApplyBoundaryOnZSGrid with level sets: collider `id` (-1: every collider,

@@ -209,6 +209,8 @@ struct SceneParams {
 // autotuner through mpm_set_launch_config.
 struct LaunchConfig {
   int p2g_ctas_per_sm, g2p_ctas_per_sm, sort_ctas_per_sm, stream_ctas_per_sm, g2p_threads;
+  int p2g_shape;      // MPM_P2G_* tile shape (threads, chunk)
+  int gather_blocks;  // grid blocks per CTA of the grid gather: 2, 4 or 8 (0: 4)
 };
 
 struct DevPtrs {

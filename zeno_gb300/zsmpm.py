@@ -61,7 +61,8 @@ class ColliderDesc(C.Structure):
 class LaunchConfig(C.Structure):
     _fields_ = [("p2g_ctas_per_sm", C.c_int32), ("g2p_ctas_per_sm", C.c_int32),
                 ("sort_ctas_per_sm", C.c_int32), ("stream_ctas_per_sm", C.c_int32),
-                ("g2p_threads", C.c_int32)]
+                ("g2p_threads", C.c_int32), ("p2g_shape", C.c_int32),
+                ("gather_blocks", C.c_int32)]
 
 
 class Stats(C.Structure):
