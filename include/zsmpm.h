@@ -49,25 +49,39 @@ typedef enum mpm_status {
   MPM_ERR_STATE = 9          /* call out of order (e.g. p2g before partition) */
 } mpm_status;
 
-/* elastic models: ConfigConstitutiveModel "type" (Generation.cu:40-51), plus
- * the equation-of-state fluid, which the reference nodes do not expose. */
-enum { MPM_FCR = 0, MPM_NHK = 1, MPM_STVK = 2, MPM_EOS = 3 };
-/* plasticity: ConfigConstitutiveModel "plasticity" (Generation.cu:66-84) */
-enum { MPM_PLASTIC_NONE = 0, MPM_PLASTIC_NADP = 1 };
+/* elastic models: ConfigConstitutiveModel "type" (Generation.cu:40-51:
+ * fcr, nhk, stvk, snhk), plus the equation-of-state fluid, which the
+ * reference nodes do not expose. */
+enum { MPM_FCR = 0, MPM_NHK = 1, MPM_STVK = 2, MPM_EOS = 3, MPM_SNHK = 4 };
+/* plasticity: ConfigConstitutiveModel "plasticity" (Generation.cu:66-84):
+ * non-associative Drucker-Prager (sand), von Mises, Cam-Clay; each runs on
+ * the StVK-Hencky model.  A Cam-Clay particle keeps its hardening state
+ * log(Jp) in the J channel (upload it there; the reference starts it at
+ * -0.04, Generation.cpp:987). */
+enum {
+  MPM_PLASTIC_NONE = 0,
+  MPM_PLASTIC_NADP = 1,
+  MPM_PLASTIC_NAVM = 2,
+  MPM_PLASTIC_NACC = 3
+};
 /* collider types: ToZSBoundary "type" (Generation.cu:1601-1611) */
 enum { MPM_BC_NONE = 0, MPM_BC_STICKY = 1, MPM_BC_SLIP = 2, MPM_BC_SEPARATE = 3 };
 /* grid transfer schemes: MakeZSGrid "transfer" (Generation.cu:1493-1504) */
 enum { MPM_TRANSFER_APIC = 0, MPM_TRANSFER_FLIP = 1, MPM_TRANSFER_AFLIP = 2 };
 
 /* Material of ConfigConstitutiveModel (Generation.cu:18-103): E, nu ->
- * Lame parameters; Drucker-Prager friction angle in degrees; bulk modulus
- * and exponent of the equation-of-state fluid. */
+ * Lame parameters; friction angle in degrees (Drucker-Prager, Cam-Clay);
+ * bulk modulus and exponent of the equation-of-state fluid; von Mises yield
+ * stress; Cam-Clay cohesion beta and hardening xi (the "params" keys
+ * friction_angle, yield_stress, beta, xi of Generation.cu:69-82). */
 typedef struct mpm_material {
   int32_t type;
   int32_t plasticity;
   float E, nu, density;
   float friction_angle_deg;
   float bulk, gamma;
+  float yield_stress;
+  float cc_beta, cc_xi;
 } mpm_material;
 
 /* Analytic box collider standing in for ToZSBoundary's level set

@@ -40,6 +40,7 @@ namespace {
 
 template <class R> struct Params {
   R mu, lam, alpha, bulk, gamma;
+  R yield, ccM, ccbeta, ccxi;
   int type, plastic;
 };
 
@@ -57,6 +58,11 @@ template <class R> Params<R> material_params(const orc_material &m) {
   p.alpha = std::sqrt(R(2) / R(3)) * R(2) * s / (R(3) - s);
   p.bulk = R(m.bulk);
   p.gamma = R(m.gamma);
+  p.yield = R(m.yield_stress);
+  // Cam-Clay critical-state slope: the Mohr-Coulomb compression match
+  p.ccM = R(6) * s / (R(3) - s);
+  p.ccbeta = R(m.cc_beta);
+  p.ccxi = R(m.cc_xi);
   p.type = m.type;
   p.plastic = m.plasticity;
   return p;
@@ -162,6 +168,18 @@ bool kirchhoff(const Params<R> &p, const R *F, R J, R *tau) {
   }
   R B[9];
   mul_ABt(F, F, B);
+  if (p.type == ORC_SNHK) {
+    // stable Neo-Hookean, invariant form (Smith, de Goes & Kim 2018):
+    // Psi = mu/2 (I_C - 3) - mu (J - 1) + lam/2 (J - 1)^2,
+    // P = mu F + (lam (J - 1) - mu) J F^-T, tau = mu B + (lam (J - 1) - mu) J I
+    const R Jf = det3(F);
+    for (int i = 0; i < 9; ++i) tau[i] = p.mu * B[i];
+    const R diag = (p.lam * (Jf - R(1)) - p.mu) * Jf;
+    tau[0] += diag;
+    tau[4] += diag;
+    tau[8] += diag;
+    return std::isfinite(tau[0]);
+  }
   if (p.type == ORC_NHK) {
     const R Jf = det3(F);
     if (!(Jf > R(0))) return false;
@@ -235,6 +253,80 @@ template <class R> int project_dp(const Params<R> &p, R *F) {
   }
   R ratio[3], Mr[9], Fn[9];
   for (int k = 0; k < 3; ++k) ratio[k] = sig_new[k] / sig[k];
+  qdqt(Q, ratio, Mr);
+  mul_AB(Mr, F, Fn);
+  for (int i = 0; i < 9; ++i) F[i] = Fn[i];
+  return 1;
+}
+
+// Von Mises and Cam-Clay return mappings in Hencky strain space (the navm /
+// nacc options of ConfigConstitutiveModel, Generation.cu:71-82, applied by
+// ZSReturnMapping, MPMPipeline.cu:958-971).  With F = U S V^T and the log
+// stretches e = ln S, a rule moves e to e' and F <- U exp(e') V^T =
+// U (exp(e')/S) U^T F.  On h = e - tr(e)/3:
+//   von Mises (Jiang et al. 2016, "The Material Point Method for Simulating
+//     Continuum Materials", SIGGRAPH course, sec. 8.2): if
+//     dg = |h| - yield / (2 mu) > 0, e' = e - dg h / |h|;
+//   Cam-Clay (Gaume et al. 2018, "Dynamic anticrack propagation in snow",
+//     Nat. Commun. 9:3047, Methods): p = -kappa tr(e) (kappa = lam + 2mu/3),
+//     q = sqrt(3/2) 2mu |h|, p0 = kappa sinh(xi max(-log Jp, 0)); states past
+//     the caps go to (p0, 0) / (-beta p0, 0); outside the ellipse
+//     q^2 (1 + 2 beta) + M^2 (p + beta p0)(p - p0) = 0 they move along the
+//     line to its centre ((1 - beta) p0 / 2, 0) onto it; e' keeps the
+//     direction of h with |h'| = q' / (sqrt(3/2) 2mu) and tr(e') = -p'/kappa;
+//     log Jp += tr(e) - tr(e').
+template <class R> int project_hencky(const Params<R> &p, R *F, R &logJp) {
+  R B[9], w[3], Q[9];
+  mul_ABt(F, F, B);
+  sym_eig3(B, w, Q, kSweeps);
+  R sig[3], e[3];
+  for (int k = 0; k < 3; ++k) {
+    sig[k] = std::sqrt(std::max(w[k], R(0)));
+    if (!(sig[k] > R(0))) return -1;
+    e[k] = std::log(sig[k]);
+  }
+  const R tr = e[0] + e[1] + e[2];
+  R h[3];
+  for (int k = 0; k < 3; ++k) h[k] = e[k] - tr / R(3);
+  const R nrm = std::sqrt(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
+  R hs = R(1), trn = tr;
+  bool projected = false;
+  if (p.plastic == ORC_PLASTIC_NAVM) {
+    const R dg = nrm - p.yield / (R(2) * p.mu);
+    if (dg > R(0)) {
+      hs = R(1) - dg / nrm;
+      projected = true;
+    }
+  } else {
+    const R kappa = p.lam + R(2) * p.mu / R(3);
+    const R p0 = kappa * std::sinh(p.ccxi * std::max(-logJp, R(0)));
+    const R beta = p.ccbeta, M = p.ccM;
+    const R pr = -kappa * tr, q = std::sqrt(R(1.5)) * R(2) * p.mu * nrm;
+    R pn = pr, qn = q;
+    if (pr > p0) {
+      pn = p0;
+      qn = R(0);
+      projected = true;
+    } else if (pr < -beta * p0) {
+      pn = -beta * p0;
+      qn = R(0);
+      projected = true;
+    } else if (q * q * (R(1) + R(2) * beta) + M * M * (pr + beta * p0) * (pr - p0) > R(0)) {
+      const R pc = R(0.5) * (R(1) - beta) * p0, a = R(0.5) * (R(1) + beta) * p0, dp = pr - pc;
+      const R t = M * a / std::sqrt(q * q * (R(1) + R(2) * beta) + M * M * dp * dp);
+      pn = pc + t * dp;
+      qn = t * q;
+      projected = true;
+    }
+    if (projected) {
+      trn = -pn / kappa;
+      hs = q > R(0) ? qn / q : R(0);
+      logJp += tr - trn;
+    }
+  }
+  if (!projected) return 0;
+  R ratio[3], Mr[9], Fn[9];
+  for (int k = 0; k < 3; ++k) ratio[k] = std::exp(hs * h[k] + trn / R(3)) / sig[k];
   qdqt(Q, ratio, Mr);
   mul_AB(Mr, F, Fn);
   for (int i = 0; i < 9; ++i) F[i] = Fn[i];
@@ -1243,15 +1335,17 @@ template <class R> struct Sim {
         for (int i = 0; i < 9; ++i) A[i] = dt * Cn[i] + ((i % 4 == 0) ? R(1) : R(0));
         mul_AB(A, Fp, Fn);
         for (int i = 0; i < 9; ++i) Fp[i] = Fn[i];
-        if (mp.plastic == ORC_PLASTIC_NADP) {
-          Params<R> pp = mp;
-          if (mu && lam) {
-            pp.mu = mu[p];
-            pp.lam = lam[p];
-          }
-          if (project_dp(pp, Fp) < 0) bad |= 1;
+        Params<R> pp = mp;
+        if (mu && lam) {
+          pp.mu = mu[p];
+          pp.lam = lam[p];
         }
-        J[p] = det3(Fp);
+        if (mp.plastic == ORC_PLASTIC_NADP) {
+          if (project_dp(pp, Fp) < 0) bad |= 1;
+        } else if (mp.plastic == ORC_PLASTIC_NAVM || mp.plastic == ORC_PLASTIC_NACC) {
+          if (project_hencky(pp, Fp, J[p]) < 0) bad |= 1;  // J holds log(Jp) for Cam-Clay
+        }
+        if (mp.plastic != ORC_PLASTIC_NACC) J[p] = det3(Fp);
       }
       for (int i = 0; i < 9; ++i)
         if (!std::isfinite(Fp[i])) bad |= 1;
@@ -1468,6 +1562,15 @@ int32_t orc_kirchhoff(const orc_material *mat, const double *F, double J, double
 int32_t orc_project_dp(const orc_material *mat, double *F) {
   const Params<double> p = material_params<double>(*mat);
   return project_dp<double>(p, F);
+}
+
+int32_t orc_project_hencky(const orc_material *mat, double *F, double *logJp) {
+  const Params<double> p = material_params<double>(*mat);
+  if (p.plastic != ORC_PLASTIC_NAVM && p.plastic != ORC_PLASTIC_NACC) return -2;
+  double lj = logJp ? *logJp : 0.0;
+  const int r = project_hencky<double>(p, F, lj);
+  if (logJp) *logJp = lj;
+  return r;
 }
 
 // ToZSCloth (Generation.cpp:489-688): per triangle, area A (double), vol =

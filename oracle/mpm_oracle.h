@@ -37,8 +37,8 @@
 extern "C" {
 #endif
 
-enum { ORC_FCR = 0, ORC_NHK = 1, ORC_STVK = 2, ORC_EOS = 3 };
-enum { ORC_PLASTIC_NONE = 0, ORC_PLASTIC_NADP = 1 };
+enum { ORC_FCR = 0, ORC_NHK = 1, ORC_STVK = 2, ORC_EOS = 3, ORC_SNHK = 4 };
+enum { ORC_PLASTIC_NONE = 0, ORC_PLASTIC_NADP = 1, ORC_PLASTIC_NAVM = 2, ORC_PLASTIC_NACC = 3 };
 enum { ORC_BC_NONE = 0, ORC_BC_STICKY = 1, ORC_BC_SLIP = 2, ORC_BC_SEPARATE = 3 };
 /* MakeZSGrid "transfer" (Generation.cu:1493-1504) */
 enum { ORC_TRANSFER_APIC = 0, ORC_TRANSFER_FLIP = 1, ORC_TRANSFER_AFLIP = 2 };
@@ -52,11 +52,13 @@ enum {
 };
 
 typedef struct orc_material {
-  int32_t type;        /* ORC_FCR / ORC_NHK / ORC_STVK / ORC_EOS */
-  int32_t plasticity;  /* ORC_PLASTIC_NONE / ORC_PLASTIC_NADP */
+  int32_t type;        /* ORC_FCR / ORC_NHK / ORC_STVK / ORC_EOS / ORC_SNHK */
+  int32_t plasticity;  /* ORC_PLASTIC_NONE / _NADP / _NAVM / _NACC */
   float E, nu, density;
-  float friction_angle_deg; /* Drucker-Prager friction angle */
+  float friction_angle_deg; /* Drucker-Prager / Cam-Clay friction angle */
   float bulk, gamma;        /* equation-of-state fluid */
+  float yield_stress;       /* von Mises */
+  float cc_beta, cc_xi;     /* Cam-Clay cohesion and hardening; log(Jp) in J */
 } orc_material;
 
 /* Level-set collider (MakeZSLevelSet + ToZSBoundary, Generation.cu:1521-1647;
@@ -207,6 +209,10 @@ int32_t orc_kirchhoff(const orc_material *mat, const double *F, double J,
 
 /* Drucker-Prager return mapping of F in place; returns 1 if projected. */
 int32_t orc_project_dp(const orc_material *mat, double *F);
+/* Von Mises / Cam-Clay return mapping of F (and Cam-Clay's log(Jp)) in
+ * place; returns 1 if projected, 0 if inside, -1 degenerate, -2 if the
+ * material has neither. */
+int32_t orc_project_hencky(const orc_material *mat, double *F, double *logJp);
 
 /* ToZSCloth's set-up of the vertex and element arrays of `out` (allocated
  * by the caller for n_verts / n_tris) from a mesh: positions x, optional

@@ -22,7 +22,8 @@ LIB_PATH = os.path.join(HERE, "libzsmpm_oracle.so")
 class OrcMaterial(C.Structure):
     _fields_ = [("type", C.c_int32), ("plasticity", C.c_int32), ("E", C.c_float),
                 ("nu", C.c_float), ("density", C.c_float), ("friction_angle_deg", C.c_float),
-                ("bulk", C.c_float), ("gamma", C.c_float)]
+                ("bulk", C.c_float), ("gamma", C.c_float), ("yield_stress", C.c_float),
+                ("cc_beta", C.c_float), ("cc_xi", C.c_float)]
 
 
 class OrcCollider(C.Structure):
@@ -112,6 +113,8 @@ def lib():
         L.orc_kirchhoff.restype = C.c_int32
         L.orc_project_dp.argtypes = [C.POINTER(OrcMaterial), P]
         L.orc_project_dp.restype = C.c_int32
+        L.orc_project_hencky.argtypes = [C.POINTER(OrcMaterial), P, P]
+        L.orc_project_hencky.restype = C.c_int32
         L.orc_max_threads.restype = C.c_int32
         _lib = L
     return _lib
@@ -124,7 +127,8 @@ def _ptr(a):
 def make_material(m) -> OrcMaterial:
     return OrcMaterial(int(m.type), int(m.plasticity), float(m.E), float(m.nu),
                        float(m.density), float(m.friction_angle_deg), float(m.bulk),
-                       float(m.gamma))
+                       float(m.gamma), float(getattr(m, "yield_stress", 1e5)),
+                       float(getattr(m, "cc_beta", 2.0)), float(getattr(m, "cc_xi", 1.0)))
 
 
 class _SceneHolder:
@@ -406,6 +410,15 @@ def project_dp(material, F: np.ndarray):
     m = make_material(material)
     rc = lib().orc_project_dp(C.byref(m), _ptr(F))
     return rc, F.reshape(3, 3)
+
+
+def project_hencky(material, F: np.ndarray, logJp: float = 0.0):
+    """Von Mises / Cam-Clay return mapping of F: (status, F', log(Jp)')."""
+    F = np.array(F, dtype=np.float64, copy=True).reshape(9)
+    lj = np.array([logJp], dtype=np.float64)
+    m = make_material(material)
+    rc = lib().orc_project_hencky(C.byref(m), _ptr(F), _ptr(lj))
+    return rc, F.reshape(3, 3), float(lj[0])
 
 
 def max_threads() -> int:

@@ -586,12 +586,16 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
   std::vector<MatParams> h(kMaxMaterials);
   for (int i = 0; i < n; ++i) {
     const mpm_material &m = mats[i];
-    if (m.type < MPM_FCR || m.type > MPM_EOS) return fail(MPM_ERR_INVALID, "unknown material type");
-    if (m.plasticity != MPM_PLASTIC_NONE && m.plasticity != MPM_PLASTIC_NADP)
+    if (m.type < MPM_FCR || m.type > MPM_SNHK) return fail(MPM_ERR_INVALID, "unknown material type");
+    if (m.plasticity < MPM_PLASTIC_NONE || m.plasticity > MPM_PLASTIC_NACC)
       return fail(MPM_ERR_INVALID, "unknown plasticity");
-    if (m.plasticity == MPM_PLASTIC_NADP && m.type != MPM_STVK)
+    if (m.plasticity != MPM_PLASTIC_NONE && m.type != MPM_STVK)
       return fail(MPM_ERR_INVALID,
-                  "nadp plasticity runs on the StVK-Hencky model (Generation.cu:66-70)");
+                  "plasticity runs on the StVK-Hencky model (Generation.cu:66-84)");
+    if (m.plasticity == MPM_PLASTIC_NAVM && !(m.yield_stress > 0.0f))
+      return fail(MPM_ERR_INVALID, "von Mises plasticity needs a positive yield stress");
+    if (m.plasticity == MPM_PLASTIC_NACC && !(m.cc_beta >= 0.0f && m.cc_xi >= 0.0f))
+      return fail(MPM_ERR_INVALID, "Cam-Clay needs beta >= 0 and xi >= 0");
     MatParams &p = h[i];
     p.type = m.type;
     p.plastic = m.plasticity;
@@ -603,6 +607,13 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
     p.alpha = (float)(std::sqrt(2.0 / 3.0) * 2.0 * s / (3.0 - s));
     p.bulk = m.bulk;
     p.gamma = m.gamma;
+    p.yield = m.yield_stress;
+    // Cam-Clay critical-state slope from the friction angle (the
+    // Mohr-Coulomb compression match M = 6 sin(phi) / (3 - sin(phi)))
+    p.cc_M = (float)(6.0 * s / (3.0 - s));
+    p.cc_beta = m.cc_beta;
+    p.cc_xi = m.cc_xi;
+    p.pad = 0.0f;
   }
   ZS_CUDA(cudaMemcpyAsync(c->d.mats, h.data(), sizeof(MatParams) * kMaxMaterials,
                           cudaMemcpyHostToDevice, c->stream));
@@ -612,7 +623,9 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
   // without the Drucker-Prager projection); not for the equation-of-state fluid
   c->differentiable = true;
   for (int i = 0; i < n; ++i)
-    if (mats[i].type == MPM_EOS) c->differentiable = false;
+    if (mats[i].type == MPM_EOS || mats[i].type == MPM_SNHK ||
+        mats[i].plasticity == MPM_PLASTIC_NAVM || mats[i].plasticity == MPM_PLASTIC_NACC)
+      c->differentiable = false;
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
   if (c->prm.n > 0) {  // stored stresses follow the new parameters
@@ -1720,7 +1733,8 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
   if (!c->differentiable)
     return fail(MPM_ERR_INVALID,
                 "the adjoint covers fixed-corotated, Neo-Hookean and StVK-Hencky (with or without "
-                "the Drucker-Prager projection) materials, not the equation-of-state fluid");
+                "the Drucker-Prager projection) materials, not the equation-of-state fluid, the "
+                "stable Neo-Hookean model or von Mises / Cam-Clay plasticity");
   for (const ColliderDev &cd : c->colliders)
     if (cd.db[0] != 0.0f || cd.db[1] != 0.0f || cd.db[2] != 0.0f || cd.ds != 0.0f)
       return fail(MPM_ERR_INVALID, "the adjoint takes static colliders only");
@@ -1836,7 +1850,8 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
   if (!c->differentiable)
     return fail(MPM_ERR_INVALID,
                 "the adjoint covers fixed-corotated, Neo-Hookean and StVK-Hencky (with or without "
-                "the Drucker-Prager projection) materials, not the equation-of-state fluid");
+                "the Drucker-Prager projection) materials, not the equation-of-state fluid, the "
+                "stable Neo-Hookean model or von Mises / Cam-Clay plasticity");
   for (const ColliderDev &cd : c->colliders)
     if (cd.db[0] != 0.0f || cd.db[1] != 0.0f || cd.db[2] != 0.0f || cd.ds != 0.0f)
       return fail(MPM_ERR_INVALID, "the adjoint takes static colliders only");

@@ -793,14 +793,15 @@ __global__ void __launch_bounds__(kFG2PThreads, 4)
           for (int c = 0; c < 3; ++c)
             F[r * 3 + c] = Fo[r * 3 + c] + dt * (X[r * 3 + 0] * Fo[c] + X[r * 3 + 1] * Fo[3 + c] +
                                                  X[r * 3 + 2] * Fo[6 + c]);
-        if (kFuseRM && mp.plastic == MPM_PLASTIC_NADP) {
-          ok_state = project_dp(mu, lam, mp.alpha, F, tau) >= 0;
+        float jch = q[GC::J][tid];  // log(Jp) of a Cam-Clay particle
+        if (kFuseRM && mp.plastic != MPM_PLASTIC_NONE) {
+          ok_state = return_mapping(mp, mu, lam, F, jch, tau) >= 0;
           if (!kAffine && lame)  // the stress of the projected F with the material's mu, lam
             ok_state = kirchhoff(mp.type, mu_s, lam_s, mp.bulk, mp.gamma, F, 1.0f, tau) && ok_state;
         } else {
           ok_state = kirchhoff(mp.type, mu_s, lam_s, mp.bulk, mp.gamma, F, 1.0f, tau);
         }
-        J = det3(F);
+        J = mp.plastic == MPM_PLASTIC_NACC ? jch : det3(F);
       }
       if (!ok_state) atomicOr(&d.cnt->status, ST_NAN);
       const float vol = q[GC::VOL][tid];

@@ -204,6 +204,16 @@ __device__ __forceinline__ bool kirchhoff(int type, float mu, float lam, float b
                mu * E.yz};
     return J > 0.0f;
   }
+  if (type == MPM_SNHK) {
+    // stable Neo-Hookean (Smith, de Goes & Kim 2018, "Stable Neo-Hookean
+    // Flesh Simulation"), invariant form Psi = mu/2 (I_C - 3) - mu (J - 1)
+    // + lam/2 (J - 1)^2: tau = mu (B - I) + (lam (J - 1) J - mu (J - 1)) I,
+    // defined through inversion
+    const float diag = Jm1 * (lam * J - mu);
+    tau = Sym3{mu * E.xx + diag, mu * E.yy + diag, mu * E.zz + diag, mu * E.xy, mu * E.xz,
+               mu * E.yz};
+    return true;
+  }
   if (type == MPM_FCR && J > 0.0f) {
     fcr_tau_invariant(mu, lam, E, Jm1, tau);
     return true;
@@ -296,6 +306,103 @@ __device__ __forceinline__ int project_dp(float mu, float lam, float alpha, floa
 #pragma unroll
   for (int i = 0; i < 9; ++i) F[i] = Fn[i];
   return 1;
+}
+
+// Return mapping in Hencky strain space for the von Mises and Cam-Clay
+// models (ZSReturnMapping, MPMPipeline.cu:953-972, navm / nacc): with
+// B = F F^T = U diag(b) U^T and the log stretches e_i = ln(b_i) / 2, a rule
+// moves e to e' on the yield surface; F <- U diag(exp(e' - e)) U^T F, and tau
+// is the StVK-Hencky stress of e'.  Rules, on h = e - tr(e)/3 and tr(e):
+//  von Mises (the Hencky-strain projection of Jiang et al. 2016, "The
+//    Material Point Method for Simulating Continuum Materials", SIGGRAPH
+//    course, sec. 8.2): with dg = |h| - yield / (2 mu) > 0, e' = e - dg h / |h|;
+//  Cam-Clay (Gaume et al. 2018, "Dynamic anticrack propagation in snow",
+//    Nat. Commun. 9:3047, Methods): pressure p = -kappa tr(e), kappa = lam +
+//    2mu/3, deviatoric q = sqrt(3/2) 2mu |h|, yield surface
+//    q^2 (1 + 2 beta) + M^2 (p + beta p0)(p - p0) <= 0 with
+//    p0 = kappa sinh(xi max(-log Jp, 0)); beyond the caps p > p0 or
+//    p < -beta p0 the state goes to (p0, 0) or (-beta p0, 0), otherwise outside
+//    the ellipse it moves toward the ellipse's centre ((1 - beta) p0 / 2, 0)
+//    onto the surface (a non-associative return); log Jp gains the plastic
+//    volume change tr(e) - tr(e').
+// Returns -1 on a degenerate F, 1 if projected, 0 if inside the yield surface.
+__device__ __forceinline__ int project_hencky(const MatParams &mp, float mu, float lam,
+                                              float (&F)[9], float &logJp, Sym3 &tau) {
+  Sym3 E;
+  float Jm1;
+  strain_of(F, E, Jm1);
+  float w[3], Q[9];
+  sym_eig3(E, w, Q);
+  if (!(w[0] > -1.0f && w[1] > -1.0f && w[2] > -1.0f)) {
+    tau = Sym3{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    return -1;
+  }
+  const float e[3] = {0.5f * log1pf(w[0]), 0.5f * log1pf(w[1]), 0.5f * log1pf(w[2])};
+  const float tr = e[0] + e[1] + e[2];
+  const float h[3] = {e[0] - tr / 3.0f, e[1] - tr / 3.0f, e[2] - tr / 3.0f};
+  const float nrm = sqrtf(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
+  float hs = 1.0f, trn = tr;  // e' = hs h + trn / 3
+  bool projected = false;
+  if (mp.plastic == MPM_PLASTIC_NAVM) {
+    const float dg = nrm - mp.yield / (2.0f * mu);
+    if (dg > 0.0f) {
+      hs = 1.0f - dg / nrm;
+      projected = true;
+    }
+  } else {  // Cam-Clay
+    const float kappa = lam + 2.0f * mu / 3.0f;
+    const float p0 = kappa * sinhf(mp.cc_xi * fmaxf(-logJp, 0.0f));
+    const float beta = mp.cc_beta, M = mp.cc_M;
+    const float p = -kappa * tr, q = 1.2247448713915890f * 2.0f * mu * nrm;  // sqrt(3/2)
+    float pn = p, qn = q;
+    if (p > p0) {
+      pn = p0;
+      qn = 0.0f;
+      projected = true;
+    } else if (p < -beta * p0) {
+      pn = -beta * p0;
+      qn = 0.0f;
+      projected = true;
+    } else if (q * q * (1.0f + 2.0f * beta) + M * M * (p + beta * p0) * (p - p0) > 0.0f) {
+      const float pc = 0.5f * (1.0f - beta) * p0, a = 0.5f * (1.0f + beta) * p0, dp = p - pc;
+      const float t = M * a * rsqrtf(q * q * (1.0f + 2.0f * beta) + M * M * dp * dp);
+      pn = pc + t * dp;
+      qn = t * q;
+      projected = true;
+    }
+    if (projected) {
+      trn = -pn / kappa;
+      hs = q > 0.0f ? qn / q : 0.0f;
+      logJp += tr - trn;
+    }
+  }
+  float en[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) en[k] = hs * h[k] + trn / 3.0f;
+  const float trp = en[0] + en[1] + en[2];
+  tau = qdqt(Q, 2.0f * mu * en[0] + lam * trp, 2.0f * mu * en[1] + lam * trp,
+             2.0f * mu * en[2] + lam * trp);
+  if (!projected) return 0;
+  const Sym3 Mr = qdqt(Q, expm1f(en[0] - e[0]), expm1f(en[1] - e[1]), expm1f(en[2] - e[2]));
+  float Fn[9];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    Fn[0 * 3 + j] = F[0 * 3 + j] + Mr.xx * F[j] + Mr.xy * F[3 + j] + Mr.xz * F[6 + j];
+    Fn[1 * 3 + j] = F[1 * 3 + j] + Mr.xy * F[j] + Mr.yy * F[3 + j] + Mr.yz * F[6 + j];
+    Fn[2 * 3 + j] = F[2 * 3 + j] + Mr.xz * F[j] + Mr.yz * F[3 + j] + Mr.zz * F[6 + j];
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) F[i] = Fn[i];
+  return 1;
+}
+
+// The return mapping of a plastic material (ZSReturnMapping) and the stress
+// of the result: Drucker-Prager, von Mises or Cam-Clay; `jch` is the J
+// channel, which holds log(Jp) for Cam-Clay.
+__device__ __forceinline__ int return_mapping(const MatParams &mp, float mu, float lam,
+                                              float (&F)[9], float &jch, Sym3 &tau) {
+  if (mp.plastic == MPM_PLASTIC_NADP) return project_dp(mu, lam, mp.alpha, F, tau);
+  return project_hencky(mp, mu, lam, F, jch, tau);
 }
 
 __device__ __forceinline__ float det3(const float (&F)[9]) {

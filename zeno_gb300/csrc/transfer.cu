@@ -708,11 +708,12 @@ __global__ void __launch_bounds__(NT, 768 / NT)
           for (int c = 0; c < 3; ++c)
             F[r * 3 + c] = Fo[r * 3 + c] + dt * (Cn[r * 3 + 0] * Fo[c] + Cn[r * 3 + 1] * Fo[3 + c] +
                                                  Cn[r * 3 + 2] * Fo[6 + c]);
-        if (kFuseRM && mp.plastic == MPM_PLASTIC_NADP)
-          ok_state = project_dp(mu, lam, mp.alpha, F, tau) >= 0;
+        float jch = q[GC_J][tid];  // log(Jp) of a Cam-Clay particle
+        if (kFuseRM && mp.plastic != MPM_PLASTIC_NONE)
+          ok_state = return_mapping(mp, mu, lam, F, jch, tau) >= 0;
         else
           ok_state = kirchhoff(mp.type, mu, lam, mp.bulk, mp.gamma, F, 1.0f, tau);
-        J = det3(F);
+        J = mp.plastic == MPM_PLASTIC_NACC ? jch : det3(F);
       }
       if (!ok_state) atomicOr(&d.cnt->status, ST_NAN);
       const float vol = q[GC_VOL][tid];
@@ -785,7 +786,7 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     const MatParams mp = d.mats[min(max(ibuf[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
-    if (mp.type == MPM_EOS || mp.plastic != MPM_PLASTIC_NADP) continue;
+    if (mp.type == MPM_EOS || mp.plastic == MPM_PLASTIC_NONE) continue;
     float F[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) F[k] = pbuf[pidx((CH_F + k), p)];
@@ -795,12 +796,13 @@ __global__ void k_return_mapping(DevPtrs d, float *__restrict__ pbuf,
       lam = pbuf[pidx(CH_LAM, p)];
     }
     Sym3 tau;
-    const int r = project_dp(mu, lam, mp.alpha, F, tau);
+    float jch = pbuf[pidx(CH_J, p)];  // log(Jp) of a Cam-Clay particle
+    const int r = return_mapping(mp, mu, lam, F, jch, tau);
     if (r < 0) atomicOr(&d.cnt->status, ST_NAN);
     if (r > 0) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) pbuf[pidx((CH_F + k), p)] = F[k];
-      pbuf[pidx(CH_J, p)] = det3(F);
+      pbuf[pidx(CH_J, p)] = mp.plastic == MPM_PLASTIC_NACC ? jch : det3(F);
       // the FLIP P2G takes the material's Lame parameters (Transfer.cu:897-907)
       if (lame && d.transfer == MPM_TRANSFER_FLIP &&
           !kirchhoff(mp.type, mp.mu, mp.lam, mp.bulk, mp.gamma, F, 1.0f, tau))

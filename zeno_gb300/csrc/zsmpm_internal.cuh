@@ -86,7 +86,9 @@ constexpr int kTileNodes = 216;       // 6^3 nodes of one particle block's stenc
 
 struct MatParams {
   int type, plastic;
-  float mu, lam, alpha, bulk, gamma, pad;
+  float mu, lam, alpha, bulk, gamma;
+  float yield;                    // von Mises yield stress
+  float cc_M, cc_beta, cc_xi, pad;  // Cam-Clay slope, cohesion, hardening
 };
 
 struct Counters {

@@ -395,6 +395,9 @@ struct ConfigConstitutiveModel : INode {
     m.friction_angle_deg = 35.0f;  // reference default (Generation.cu:70)
     m.bulk = get_arg("bulk", 1e4f);
     m.gamma = get_arg("gamma", 7.0f);
+    m.yield_stress = 1e5f;
+    m.cc_beta = 2.0f;
+    m.cc_xi = 1.0f;
     const std::string type = get_input2<std::string>("type");
     if (type == "fcr")
       m.type = MPM_FCR;
@@ -402,17 +405,31 @@ struct ConfigConstitutiveModel : INode {
       m.type = MPM_NHK;
     else if (type == "stvk")
       m.type = MPM_STVK;
+    else if (type == "snhk")
+      m.type = MPM_SNHK;
     else if (type == "eos")
       m.type = MPM_EOS;
     else
       throw std::runtime_error("unrecognized (isotropic) elastic model [" + type + "]");
     if (get_input2<std::string>("aniso") != "none")
       throw std::runtime_error("anisotropic models are not supported by this MPM backend");
+    // plasticity runs on StvkWithHencky (Generation.cu:66-82), with its
+    // parameters from "params" and the reference's defaults
     const std::string plastic = get_input2<std::string>("plasticity");
     if (plastic == "nadp") {
-      m.type = MPM_STVK;  // plasticity runs on StvkWithHencky (Generation.cu:66-70)
+      m.type = MPM_STVK;
       m.plasticity = MPM_PLASTIC_NADP;
       m.friction_angle_deg = get_arg("friction_angle", 35.0f);  // Generation.cu:69-70
+    } else if (plastic == "navm") {
+      m.type = MPM_STVK;
+      m.plasticity = MPM_PLASTIC_NAVM;
+      m.yield_stress = get_arg("yield_stress", 1e5f);  // Generation.cu:73-75
+    } else if (plastic == "nacc") {
+      m.type = MPM_STVK;
+      m.plasticity = MPM_PLASTIC_NACC;
+      m.friction_angle_deg = get_arg("friction_angle", 35.0f);  // Generation.cu:77-82
+      m.cc_beta = get_arg("beta", 2.0f);
+      m.cc_xi = get_arg("xi", 1.0f);
     } else if (plastic == "none") {
       m.plasticity = MPM_PLASTIC_NONE;
     } else {
@@ -608,8 +625,13 @@ struct ToZSParticles : INode {
     if (auto *vel = prim_access::vel(*prim, false); vel && (int64_t)vel->size() == n)
       for (int64_t i = 0; i < n; ++i)
         for (int d = 0; d < 3; ++d) v[3 * i + d] = (*vel)[i][d];
-    check(mpm_particles_upload(ctx->h, n, x.data(), v.data(), nullptr, nullptr, nullptr, m.data(),
-                               vol.data(), nullptr, nullptr, nullptr),
+    // Cam-Clay particles start hardened at log(Jp) = -0.04, carried in the J
+    // channel (Generation.cpp:987)
+    std::vector<float> J;
+    if (model->mat.plasticity == MPM_PLASTIC_NACC) J.assign(n, -0.04f);
+    check(mpm_particles_upload(ctx->h, n, x.data(), v.data(), nullptr, nullptr,
+                               J.empty() ? nullptr : J.data(), m.data(), vol.data(), nullptr,
+                               nullptr, nullptr),
           "mpm_particles_upload");
     out->ctx = ctx;
     set_output("ZSParticles", out);

@@ -19,8 +19,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 # material types and plasticity flags (same numbering as include/zsmpm.h)
-FCR, NHK, STVK, EOS = 0, 1, 2, 3
-PLASTIC_NONE, PLASTIC_NADP = 0, 1
+FCR, NHK, STVK, EOS, SNHK = 0, 1, 2, 3, 4
+PLASTIC_NONE, PLASTIC_NADP, PLASTIC_NAVM, PLASTIC_NACC = 0, 1, 2, 3
 BC_NONE, BC_STICKY, BC_SLIP, BC_SEPARATE = 0, 1, 2, 3
 # MakeZSGrid "transfer": APIC, FLIP (PIC/FLIP blend 0.99), affine FLIP
 TRANSFER_APIC, TRANSFER_FLIP, TRANSFER_AFLIP = 0, 1, 2
@@ -63,6 +63,11 @@ class Material:
     friction_angle_deg: float = 35.0
     bulk: float = 1e4
     gamma: float = 7.0
+    # von Mises yield stress; Cam-Clay cohesion and hardening (the
+    # reference's defaults, Generation.cu:74,78-79)
+    yield_stress: float = 1e5
+    cc_beta: float = 2.0
+    cc_xi: float = 1.0
 
 
 @dataclass

@@ -37,7 +37,8 @@ class CtxDesc(C.Structure):
 class Material(C.Structure):
     _fields_ = [("type", C.c_int32), ("plasticity", C.c_int32), ("E", C.c_float),
                 ("nu", C.c_float), ("density", C.c_float), ("friction_angle_deg", C.c_float),
-                ("bulk", C.c_float), ("gamma", C.c_float)]
+                ("bulk", C.c_float), ("gamma", C.c_float), ("yield_stress", C.c_float),
+                ("cc_beta", C.c_float), ("cc_xi", C.c_float)]
 
 
 class Boundary(C.Structure):
@@ -371,7 +372,11 @@ class Context:
         arr = (Material * len(mats))(*[Material(int(m.type), int(m.plasticity), float(m.E),
                                                 float(m.nu), float(m.density),
                                                 float(m.friction_angle_deg), float(m.bulk),
-                                                float(m.gamma)) for m in mats])
+                                                float(m.gamma),
+                                                float(getattr(m, "yield_stress", 1e5)),
+                                                float(getattr(m, "cc_beta", 2.0)),
+                                                float(getattr(m, "cc_xi", 1.0)))
+                                       for m in mats])
         self._check(self._L.mpm_set_materials(self.h, arr, len(mats)), "mpm_set_materials")
 
     def set_boundary(self, bc_type, thickness, lo, hi):
