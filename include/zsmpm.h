@@ -422,7 +422,7 @@ typedef struct mpm_launch_config {
   int32_t g2p_ctas_per_sm;
   int32_t sort_ctas_per_sm;
   int32_t stream_ctas_per_sm; /* binning, scatter, grid gather */
-  int32_t g2p_threads;        /* 128 or 256 */
+  int32_t g2p_threads;        /* 128 (0: 128) */
   int32_t p2g_shape;          /* MPM_P2G_* tile shape of the P2G column scatter */
   int32_t gather_blocks;      /* grid blocks per CTA of the grid gather: 2, 4 or 8 (0: 4) */
 } mpm_launch_config;

@@ -182,7 +182,7 @@ def test_launch_shapes_do_not_change_results(zsmpm_mod):
     """Every launch configuration the autotuner may pick gives the same bits."""
     scene, parts = S.multi_material(dx=1.0 / 128, region_cells=(32, 16, 16))
     outs = []
-    for cfg in ({}, {"g2p_threads": 256, "g2p_ctas_per_sm": 2, "p2g_ctas_per_sm": 1},
+    for cfg in ({}, {"g2p_ctas_per_sm": 2, "p2g_ctas_per_sm": 1},
                 {"sort_ctas_per_sm": 16, "stream_ctas_per_sm": 4, "g2p_ctas_per_sm": 3},
                 {"p2g_shape": 1, "gather_blocks": 2}, {"p2g_shape": 2, "gather_blocks": 8},
                 {"p2g_shape": 3}, {"p2g_shape": 4, "p2g_ctas_per_sm": 2}):

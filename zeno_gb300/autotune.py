@@ -21,7 +21,6 @@ import numpy as np
 
 KNOBS = {
     # knob: (candidates, stages whose time it drives)
-    "g2p_threads": ([128, 256], ("g2p",)),
     "g2p_ctas_per_sm": ([0, 2, 3, 4, 6], ("g2p",)),
     # P2G tile shape (threads per CTA x particles per chunk, MPM_P2G_*):
     # 192x128, 192x192, 192x96, 256x128, 256x256
@@ -70,7 +69,6 @@ def tune(ctx, dt: float, state=None, reps: int = 5, use_cache: bool = True) -> d
         return cache[key]
     saved = None if state is not None else ctx.download()
     cfg = {k: 0 for k in KNOBS}
-    cfg["g2p_threads"] = 128
     timings = {}
     for knob, (cands, stages) in KNOBS.items():
         best, best_t = cfg[knob], None

@@ -619,6 +619,13 @@ int32_t mpm_set_materials(mpm_ctx *c, const mpm_material *mats, int32_t n) {
                           cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   c->n_materials = n;
+  int hencky = 0;
+  for (int i = 0; i < n; ++i)
+    hencky |= mats[i].plasticity == MPM_PLASTIC_NAVM || mats[i].plasticity == MPM_PLASTIC_NACC;
+  if (hencky != c->d.hencky) {
+    c->d.hencky = hencky;
+    drop_graphs(c);  // the graphs hold the G2P variant
+  }
   // adjoints exist for the elastic models and for sand (StVK-Hencky with or
   // without the Drucker-Prager projection); not for the equation-of-state fluid
   c->differentiable = true;
@@ -1635,7 +1642,7 @@ int32_t mpm_set_launch_config(mpm_ctx *c, const mpm_launch_config *cfg) {
   if (!cfg || cfg->p2g_ctas_per_sm < 0 || cfg->g2p_ctas_per_sm < 0 || cfg->sort_ctas_per_sm < 0 ||
       cfg->stream_ctas_per_sm < 0 || cfg->p2g_ctas_per_sm > 64 || cfg->g2p_ctas_per_sm > 64 ||
       cfg->sort_ctas_per_sm > 64 || cfg->stream_ctas_per_sm > 64 ||
-      (cfg->g2p_threads != 0 && cfg->g2p_threads != 128 && cfg->g2p_threads != 256) ||
+      (cfg->g2p_threads != 0 && cfg->g2p_threads != 128) ||
       cfg->p2g_shape < MPM_P2G_192x128 || cfg->p2g_shape > MPM_P2G_256x256 ||
       (cfg->gather_blocks != 0 && cfg->gather_blocks != 2 && cfg->gather_blocks != 4 &&
        cfg->gather_blocks != 8))

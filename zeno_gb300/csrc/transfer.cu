@@ -495,7 +495,10 @@ constexpr int g2p_smem_bytes() {
 // i+1's block (216 float4) and chunk i+1's particle channels are in flight
 // as cp.async copies into the other half of double-buffered shared memory,
 // and the permutation entries of chunk i+2 are loading into registers.
-template <bool kFuseRM, bool kFuseBin, int NT>
+// kHencky: the von Mises / Cam-Clay return mappings are compiled in (only for
+// contexts whose materials use them: their extra registers would otherwise
+// make every G2P spill)
+template <bool kFuseRM, bool kFuseBin, int NT, bool kHencky>
 __global__ void __launch_bounds__(NT, 768 / NT)
     k_g2p(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
           float *__restrict__ pout, int32_t *__restrict__ iout) {
@@ -709,8 +712,10 @@ __global__ void __launch_bounds__(NT, 768 / NT)
             F[r * 3 + c] = Fo[r * 3 + c] + dt * (Cn[r * 3 + 0] * Fo[c] + Cn[r * 3 + 1] * Fo[3 + c] +
                                                  Cn[r * 3 + 2] * Fo[6 + c]);
         float jch = q[GC_J][tid];  // log(Jp) of a Cam-Clay particle
-        if (kFuseRM && mp.plastic != MPM_PLASTIC_NONE)
-          ok_state = return_mapping(mp, mu, lam, F, jch, tau) >= 0;
+        if (kFuseRM && mp.plastic == MPM_PLASTIC_NADP)
+          ok_state = project_dp(mu, lam, mp.alpha, F, tau) >= 0;
+        else if (kHencky && kFuseRM && mp.plastic != MPM_PLASTIC_NONE)
+          ok_state = project_hencky(mp, mu, lam, F, jch, tau) >= 0;
         else
           ok_state = kirchhoff(mp.type, mu, lam, mp.bulk, mp.gamma, F, 1.0f, tau);
         J = mp.plastic == MPM_PLASTIC_NACC ? jch : det3(F);
@@ -846,14 +851,21 @@ __global__ void k_stress(DevPtrs d, float *__restrict__ pbuf, const int32_t *__r
 
 }  // namespace
 
-template <int NT> int g2p_occupancy() {
+int g2p_occupancy() {
+  constexpr int NT = 128;
   constexpr int smem = g2p_smem_bytes<NT>();
-  cudaFuncSetAttribute(k_g2p<true, true, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_g2p<true, false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  cudaFuncSetAttribute(k_g2p<false, false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_g2p<true, true, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       smem);
+  cudaFuncSetAttribute(k_g2p<true, false, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       smem);
+  cudaFuncSetAttribute(k_g2p<false, false, NT, false>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaFuncSetAttribute(k_g2p<true, true, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       smem);
+  cudaFuncSetAttribute(k_g2p<true, false, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        smem);
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true, NT>, NT, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p<true, true, NT, false>, NT, smem);
   return b > 0 ? b : 1;
 }
 
@@ -879,8 +891,8 @@ int p2g_shape_occupancy(int shape) {
 void configure_launches(DevPtrs &d) {
   const int a = p2g_shape_occupancy(d.launch.p2g_shape);
   const LaunchConfig &L = d.launch;
-  const int gt = L.g2p_threads == 256 ? 256 : 128;
-  const int g = gt == 256 ? g2p_occupancy<256>() : g2p_occupancy<128>();
+  const int gt = 128;
+  const int g = g2p_occupancy();
   d.grid_p2g = d.num_sms * (L.p2g_ctas_per_sm > 0 ? std::min(L.p2g_ctas_per_sm, a) : a);
   d.grid_g2p = d.num_sms * (L.g2p_ctas_per_sm > 0 ? std::min(L.g2p_ctas_per_sm, g) : g);
   d.grid_sort = d.num_sms * (L.sort_ctas_per_sm > 0 ? L.sort_ctas_per_sm : 8);
@@ -991,26 +1003,25 @@ void launch_grid_update(const DevPtrs &d, int mode, cudaStream_t s) {
   k_grid_update<<<d.num_sms * 8, 256, 0, s>>>(d, mode);
 }
 
-template <int NT>
-void launch_g2p_nt(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
+void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
+  if (d.transfer != MPM_TRANSFER_APIC) return launch_g2p_flip(d, cur, fuse_rm, fuse_bin, s);
+  constexpr int NT = 128;
   const int grid = d.grid_g2p;
   constexpr int smem = g2p_smem_bytes<NT>();
   float *pi = d.pbuf[cur], *po = d.pbuf[1 - cur];
   int32_t *ii = d.ibuf[cur], *io = d.ibuf[1 - cur];
-  if (fuse_rm && fuse_bin)
-    k_g2p<true, true, NT><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
-  else if (fuse_rm)
-    k_g2p<true, false, NT><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
-  else
-    k_g2p<false, false, NT><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
-}
-
-void launch_g2p(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
-  if (d.transfer != MPM_TRANSFER_APIC) return launch_g2p_flip(d, cur, fuse_rm, fuse_bin, s);
-  if (d.g2p_threads == 256)
-    launch_g2p_nt<256>(d, cur, fuse_rm, fuse_bin, s);
-  else
-    launch_g2p_nt<128>(d, cur, fuse_rm, fuse_bin, s);
+  if (fuse_rm && d.hencky) {
+    if (fuse_bin)
+      k_g2p<true, true, NT, true><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
+    else
+      k_g2p<true, false, NT, true><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
+  } else if (fuse_rm && fuse_bin) {
+    k_g2p<true, true, NT, false><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
+  } else if (fuse_rm) {
+    k_g2p<true, false, NT, false><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
+  } else {
+    k_g2p<false, false, NT, false><<<grid, NT, smem, s>>>(d, pi, ii, po, io);
+  }
 }
 
 void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s) {

@@ -257,6 +257,7 @@ struct DevPtrs {
   int grid_p2g, grid_g2p;  // persistent grids: SMs x resident CTAs per SM
   int grid_sort, grid_stream, g2p_threads;
   int transfer;                      // MPM_TRANSFER_* (host copy of SimParams::transfer)
+  int hencky;  // some material uses the von Mises / Cam-Clay return mapping
   int grid_p2g_flip, grid_g2p_flip;  // persistent grids of the FLIP transfer kernels
   LaunchConfig launch;
 };
