@@ -326,7 +326,7 @@ __device__ __forceinline__ int project_dp(float mu, float lam, float alpha, floa
 //    onto the surface (a non-associative return); log Jp gains the plastic
 //    volume change tr(e) - tr(e').
 // Returns -1 on a degenerate F, 1 if projected, 0 if inside the yield surface.
-__device__ __noinline__ int project_hencky(const MatParams &mp, float mu, float lam,
+static __device__ __noinline__ int project_hencky(const MatParams &mp, float mu, float lam,
                                            float (&F)[9], float &logJp, Sym3 &tau) {
   Sym3 E;
   float Jm1;
