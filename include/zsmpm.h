@@ -460,6 +460,26 @@ int32_t mpm_get_stats(mpm_ctx *ctx, mpm_stats *out);
  * Each enqueued substep then also launches one single-thread gate kernel.
  * Off: such a particle is MPM_ERR_OUT_OF_DOMAIN. */
 int32_t mpm_set_auto_regrow(mpm_ctx *ctx, int32_t on);
+/* The fused substep as ONE persistent kernel: a cooperative launch of as
+ * many CTAs as the SMs hold runs the partition (directory scan, placement,
+ * in-block sort), P2G, the grid gather and update with walls and level-set
+ * colliders, and G2P with the return mapping, stress and binning, with a
+ * grid-wide barrier between the stages -- one launch (plus a 4-byte reset of
+ * the barrier counter) per substep instead of seven, captured in the
+ * context's graph like them.  Results equal those of the stage kernels to
+ * rounding (the G2P and P2G use one fixed tile shape).  Applies to APIC
+ * contexts without cloth or trackers; others keep the stage kernels.
+ * barrier_limit: spins (of about 100 ns) a CTA waits at a barrier before it
+ * gives up: the substep then ends early and the status is MPM_ERR_TIMEOUT
+ * (the state is that of an incomplete substep).  Returns MPM_ERR_INVALID if
+ * the device cannot launch the kernel cooperatively. */
+#define MPM_BARRIER_LIMIT_DEFAULT (1ull << 24)
+int32_t mpm_set_persistent(mpm_ctx *ctx, int32_t on, uint64_t barrier_limit);
+/* Self-test of the bounded barrier: one CTA per SM waits at a barrier that
+ * nothing completes, for barrier_limit spins each; *timed_out is 1 when every
+ * wait gave up and reported it (the context's status word is left as it
+ * was). */
+int32_t mpm_barrier_selftest(mpm_ctx *ctx, uint64_t barrier_limit, int32_t *timed_out);
 /* The directory box (in 4^3 blocks) and how many times it has grown. */
 int32_t mpm_get_domain(mpm_ctx *ctx, int32_t block_lo[3], int32_t block_dims[3],
                        int32_t *n_regrows);

@@ -81,6 +81,8 @@ struct mpm_ctx {
   int64_t started_base = 0;
   int32_t regrows = 0;
   int32_t max_grid_blocks_req = 0;  // as given at creation (0: the default rule)
+  // mpm_set_persistent: the fused substep as one cooperative kernel
+  bool persistent = false;
 };
 
 namespace {
@@ -176,6 +178,12 @@ void enqueue_sort(mpm_ctx *c) {
   c->binned = false;
 }
 
+// mpm_set_persistent applies: the fused substep is one cooperative kernel
+bool uses_persistent(const mpm_ctx *c) {
+  return c->persistent && c->d.cloth.n_verts == 0 && c->d.n_trackers == 0 &&
+         c->d.transfer == MPM_TRANSFER_APIC;
+}
+
 // One substep of the fused path; the counts of the current positions must be
 // binned already, and the G2P epilogue bins the new positions, so a graph of
 // this sequence can be replayed back to back.  With `ev` set, event i is
@@ -186,6 +194,12 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   };
   const bool cloth = c->d.cloth.n_verts > 0, trackers = c->d.n_trackers > 0;
   mark(MPM_STAGE_SCAN);
+  if (uses_persistent(c)) {
+    if (c->auto_regrow) launch_substep_gate(c->d, c->stream);
+    launch_substep_persistent(c->d, cur, !c->colliders.empty(), c->stream);
+    for (int i = MPM_STAGE_SCATTER; i <= MPM_NUM_STAGES; ++i) mark(i);
+    return;
+  }
   if (cloth) launch_cloth_mark(c->d, c->stream);  // the cloth's grid blocks
   if (trackers) launch_tracker_mark(c->d, c->stream);
   // a growing directory: this substep and the queued ones halt if a
@@ -1625,10 +1639,30 @@ int32_t mpm_substep_timed(mpm_ctx *c, float dt, float *stage_ms, int32_t n_stage
   enqueue_substep(c, c->cur, c->events);
   if ((rc = launch_check("timed substep"))) return rc;
   ZS_CUDA(cudaEventSynchronize(c->events[MPM_NUM_STAGES]));
-  for (int i = 0; i < MPM_NUM_STAGES; ++i) {
-    float ms = 0.0f;
-    ZS_CUDA(cudaEventElapsedTime(&ms, c->events[i], c->events[i + 1]));
-    stage_ms[i] = ms;
+  if (uses_persistent(c)) {
+    // one kernel: its stages from the times it noted at each barrier (the
+    // launch itself counted to the scan)
+    float bin = 0.0f, all = 0.0f;
+    ZS_CUDA(cudaEventElapsedTime(&bin, c->events[MPM_STAGE_BIN], c->events[MPM_STAGE_SCAN]));
+    ZS_CUDA(cudaEventElapsedTime(&all, c->events[MPM_STAGE_SCAN], c->events[MPM_NUM_STAGES]));
+    ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
+                            c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    const unsigned long long *t = c->h_cnt->stage_t;
+    auto ms = [&](int a, int b) { return (float)((double)(t[b] - t[a]) * 1e-6); };
+    stage_ms[MPM_STAGE_BIN] = bin;
+    stage_ms[MPM_STAGE_SCATTER] = ms(2, 3);
+    stage_ms[MPM_STAGE_SORT] = ms(3, 4);
+    stage_ms[MPM_STAGE_P2G] = ms(4, 5);
+    stage_ms[MPM_STAGE_GRID_UPDATE] = ms(5, 6);
+    stage_ms[MPM_STAGE_G2P] = ms(6, 7);
+    stage_ms[MPM_STAGE_SCAN] = all - ms(2, 7);
+  } else {
+    for (int i = 0; i < MPM_NUM_STAGES; ++i) {
+      float ms = 0.0f;
+      ZS_CUDA(cudaEventElapsedTime(&ms, c->events[i], c->events[i + 1]));
+      stage_ms[i] = ms;
+    }
   }
   c->cur = 1 - c->cur;
   c->partition_valid = false;
@@ -1923,7 +1957,7 @@ int32_t mpm_sync(mpm_ctx *c) {
   // a growing directory: a particle left it, and no worse error came with it
   for (int round = 0; c->auto_regrow && round < kMaxRegrowRounds; ++round) {
     const int b = c->h_cnt->status;
-    if (!(b & ST_OUT_OF_DOMAIN) || (b & (ST_NAN | ST_CAPACITY | ST_MATERIAL))) break;
+    if (!(b & ST_OUT_OF_DOMAIN) || (b & (ST_NAN | ST_CAPACITY | ST_MATERIAL | ST_TIMEOUT))) break;
     // the gate let `started` of the queued substeps run; the state after the
     // last of them is complete (the halted ones changed nothing)
     const int64_t started = (int64_t)c->h_cnt->n_started - c->started_base;
@@ -1972,6 +2006,45 @@ int32_t mpm_set_auto_regrow(mpm_ctx *c, int32_t on) {
     c->started_base = 0;
     drop_graphs(c);  // the graphs gain or lose the substep gate
   }
+  return MPM_OK;
+}
+
+int32_t mpm_set_persistent(mpm_ctx *c, int32_t on, uint64_t barrier_limit) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = settle(c))) return rc;
+  if (on) {
+    int coop = 0;
+    ZS_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
+    if (!coop || persistent_grid(c->d) <= 0)
+      return fail(MPM_ERR_INVALID, "the device cannot run the persistent substep kernel");
+  }
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->persistent = on != 0;
+  c->prm.barrier_limit = barrier_limit;
+  c->prm_dirty = true;
+  drop_graphs(c);
+  return MPM_OK;
+}
+
+int32_t mpm_barrier_selftest(mpm_ctx *c, uint64_t barrier_limit, int32_t *timed_out) {
+  if (!timed_out) return fail(MPM_ERR_INVALID, "null output");
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = settle(c))) return rc;
+  ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  const Counters keep = *c->h_cnt;
+  cudaError_t e = launch_barrier_selftest(c->d, barrier_limit, c->stream);
+  if (e != cudaSuccess)
+    return fail(MPM_ERR_CUDA, std::string("barrier self-test: ") + cudaGetErrorString(e));
+  ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  *timed_out = (c->h_cnt->status & ST_TIMEOUT) != 0 && c->h_cnt->halt != 0;
+  // the context's counters (status word, halt flag) as they were
+  ZS_CUDA(cudaMemcpyAsync(c->d.cnt, &keep, sizeof(Counters), cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  *c->h_cnt = keep;
   return MPM_OK;
 }
 

@@ -105,6 +105,12 @@ struct Counters {
   int halt;
   int n_started;
   unsigned bbox[6];  // ordered-bits min x, y, z, max x, y, z of the positions
+  // grid-wide barrier of the persistent substep kernel: arrivals and the
+  // generation the last arrival publishes; CTAs done with the last stage
+  unsigned bar_count, bar_done, bar_gen, pad;
+  // global timer (ns) when the last persistent substep started and when it
+  // passed each of its stage barriers (the last entry: every CTA done)
+  unsigned long long stage_t[8];
 };
 
 // Every kernel of the fused substep starts with this test: the substeps
@@ -121,6 +127,9 @@ struct SimParams {
   int auto_step;    // the fused substep advances the colliders by dt
   int transfer;     // MPM_TRANSFER_* (MakeZSGrid "transfer")
   long long n;      // particles of all scenes
+  // spins a CTA of the persistent substep waits at a grid barrier before it
+  // gives up (ST_TIMEOUT); about 100 ns each
+  unsigned long long barrier_limit;
 };
 
 // Level-set collider (MakeZSLevelSet + ToZSBoundary): dense signed distance
@@ -297,6 +306,16 @@ void launch_substep_gate(const DevPtrs &d, cudaStream_t s);
 // bounding box of the particle positions (and cloth vertices, trackers) of
 // buffer `cur` into Counters::bbox
 void launch_bbox(const DevPtrs &d, int cur, cudaStream_t s);
+
+// persistent.cu: the whole fused substep (APIC; `colliders`: level-set
+// colliders on the listed blocks) as one cooperative kernel, its barrier
+// counter reset on the stream first; CTAs it launches with, 0 if the device
+// cannot run it
+int persistent_grid(const DevPtrs &d);
+cudaError_t launch_substep_persistent(const DevPtrs &d, int cur, bool colliders, cudaStream_t s);
+// a grid barrier that nothing completes, with `limit` spins: every CTA gives
+// up and sets ST_TIMEOUT (the self-test of the bounded wait)
+cudaError_t launch_barrier_selftest(const DevPtrs &d, unsigned long long limit, cudaStream_t s);
 
 // transfer.cu
 // fills the persistent grid sizes of DevPtrs from the occupancy of each kernel

@@ -87,7 +87,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_grid_download", "mpm_partition_noalloc", "mpm_set_launch_config",
            "mpm_get_launch_config", "mpm_set_differentiable", "mpm_state_save",
            "mpm_state_load", "mpm_adjoint_substep", "mpm_rollout_forward", "mpm_rollout_backward", "mpm_snapshot_floats", "mpm_add_collider", "mpm_clear_colliders",
-           "mpm_step_colliders", "mpm_set_auto_regrow", "mpm_get_domain"]
+           "mpm_step_colliders", "mpm_set_auto_regrow", "mpm_get_domain",
+           "mpm_set_persistent", "mpm_barrier_selftest"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 # differentiable form (include/zsmpm.h): state planes x 3, v 3, C 9, F 9, J,
@@ -164,6 +165,8 @@ def load(path: str = LIB_PATH):
         "mpm_rollout_backward": ([P, f32, i32, i32, P, P, P, P, P, P], i32),
         "mpm_set_auto_regrow": ([P, i32], i32),
         "mpm_get_domain": ([P, P, P, P], i32),
+        "mpm_set_persistent": ([P, i32, C.c_uint64], i32),
+        "mpm_barrier_selftest": ([P, C.c_uint64, P], i32),
         "mpm_state_save": ([P, P], i32),
         "mpm_state_load": ([P, P], i32),
         "mpm_adjoint_substep": ([P, f32, P, P, P, P], i32),
@@ -521,6 +524,20 @@ class Context:
     # growing directory
     def set_auto_regrow(self, on: bool = True):
         self._check(self._L.mpm_set_auto_regrow(self.h, 1 if on else 0), "mpm_set_auto_regrow")
+
+    # one persistent kernel per substep (include/zsmpm.h: mpm_set_persistent)
+    BARRIER_LIMIT_DEFAULT = 1 << 24
+
+    def set_persistent(self, on: bool = True, barrier_limit: int = BARRIER_LIMIT_DEFAULT):
+        self._check(self._L.mpm_set_persistent(self.h, 1 if on else 0, int(barrier_limit)),
+                    "mpm_set_persistent")
+
+    def barrier_selftest(self, barrier_limit: int = 1000) -> bool:
+        """True when waits at a barrier nothing completes gave up and said so."""
+        t = C.c_int32(0)
+        self._check(self._L.mpm_barrier_selftest(self.h, int(barrier_limit), C.byref(t)),
+                    "mpm_barrier_selftest")
+        return bool(t.value)
 
     def domain(self):
         """(block_lo, block_dims, n_regrows) of the directory."""
