@@ -209,7 +209,9 @@ __global__ void __launch_bounds__(kAdjPThreads, 4)
       for (int k = 0; k < 9; ++k) rec[(3 + k) * cap + sp] = A[k];
 #pragma unroll
       for (int k = 0; k < 3; ++k) rec[(12 + k) * cap + sp] = f[k];
-      rec[15 * cap + sp] = __int_as_float(d.pkey[p] & 63);
+      // the cell of the particle's key, from its position as the binning
+      // forms it (the key store itself holds the next state's keys by now)
+      rec[15 * cap + sp] = __int_as_float(sort_cell(s0.base & 3, s1.base & 3, s2.base & 3));
     }
     __syncthreads();  // sg reused by the next block
   }

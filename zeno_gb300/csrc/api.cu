@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -83,6 +84,12 @@ struct mpm_ctx {
   int32_t max_grid_blocks_req = 0;  // as given at creation (0: the default rule)
   // mpm_set_persistent: the fused substep as one cooperative kernel
   bool persistent = false;
+  // differentiable rollout: the partition and grid of each recomputed
+  // substep of a segment, kept for its adjoint (PartSet below), `pset_cap`
+  // blocks each; n_gblocks, n_buckets of each (device, 2 per set)
+  std::vector<zsmpm::PartSet> psets;
+  int pset_cap = 0;
+  int32_t *pset_cnt = nullptr;
 };
 
 namespace {
@@ -373,6 +380,7 @@ int32_t regrow(mpm_ctx *c) {
   S.dir_off = 0;
   d.ndir = ndir;
   d.ntiles = ntiles;
+  d.grid_persist = persistent_grid(d);
   c->prm_dirty = true;
   if ((rc = push_params(c))) return rc;
   drop_graphs(c);
@@ -1857,6 +1865,79 @@ struct StoreSwap {
   }
 };
 
+void free_psets(mpm_ctx *c) {
+  for (PartSet &p : c->psets) {
+    for (void *q : {(void *)p.perm, (void *)p.dir_gb, (void *)p.dir_bk, (void *)p.gb_dir,
+                    (void *)p.bk_dir, (void *)p.bk_start, (void *)p.bk_count, (void *)p.grid,
+                    (void *)p.ptile})
+      dfree(c, q);
+  }
+  c->psets.clear();
+  dfree(c, c->pset_cnt);
+  c->pset_cnt = nullptr;
+  c->pset_cap = 0;
+}
+
+// `count` partition sets of `capb` blocks each; false (none kept) when the
+// device has not room for them with a margin, so that the rollout takes the
+// path that partitions each adjoint substep again.
+bool ensure_psets(mpm_ctx *c, int count, int capb) {
+  if ((int)c->psets.size() >= count && c->pset_cap >= capb) return true;
+  free_psets(c);
+  const DevPtrs &d = c->d;
+  const size_t per = (size_t)d.cap * 4 + (size_t)d.ndir * 8 + (size_t)capb * 16 +
+                     (size_t)capb * (64 + kTileNodes) * sizeof(float4);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return false;
+  const size_t margin = std::max<size_t>(total_b / 16, (size_t)2 << 30);
+  if (per * count + margin > free_b) return false;
+  bool ok = dalloc(c, &c->pset_cnt, 2 * (size_t)count) == MPM_OK;
+  for (int k = 0; ok && k < count; ++k) {
+    PartSet p{};
+    ok = dalloc(c, &p.perm, (size_t)d.cap) == MPM_OK && dalloc(c, &p.dir_gb, (size_t)d.ndir) == MPM_OK &&
+         dalloc(c, &p.dir_bk, (size_t)d.ndir) == MPM_OK && dalloc(c, &p.gb_dir, (size_t)capb) == MPM_OK &&
+         dalloc(c, &p.bk_dir, (size_t)capb) == MPM_OK && dalloc(c, &p.bk_start, (size_t)capb) == MPM_OK &&
+         dalloc(c, &p.bk_count, (size_t)capb) == MPM_OK &&
+         dalloc(c, &p.grid, (size_t)capb * 64) == MPM_OK &&
+         dalloc(c, &p.ptile, (size_t)capb * kTileNodes) == MPM_OK;
+    c->psets.push_back(p);  // freed with the others if incomplete
+  }
+  if (!ok) {
+    free_psets(c);
+    cudaGetLastError();  // the failed allocation is not this call's error
+    return false;
+  }
+  c->pset_cap = capb;
+  return true;
+}
+
+// Runs the kernels with partition set k in place of the context's own
+// partition and grid buffers (and its capacity in blocks).
+struct PartSwap {
+  mpm_ctx *c;
+  PartSet own;
+  int cap;
+  explicit PartSwap(mpm_ctx *ctx) : c(ctx), cap(ctx->d.cap_gblocks) {
+    const DevPtrs &d = c->d;
+    own = PartSet{d.perm, d.dir_gb, d.dir_bk, d.gb_dir, d.bk_dir, d.bk_start, d.bk_count,
+                  d.grid, d.ptile};
+  }
+  void set(const PartSet &p, int capb) {
+    DevPtrs &d = c->d;
+    d.perm = p.perm;
+    d.dir_gb = p.dir_gb;
+    d.dir_bk = p.dir_bk;
+    d.gb_dir = p.gb_dir;
+    d.bk_dir = p.bk_dir;
+    d.bk_start = p.bk_start;
+    d.bk_count = p.bk_count;
+    d.grid = p.grid;
+    d.ptile = p.ptile;
+    d.cap_gblocks = capb;
+  }
+  ~PartSwap() { set(own, cap); }
+};
+
 }  // namespace
 
 int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
@@ -1868,6 +1949,8 @@ int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t ev
   const long long n = c->prm.n;
   const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));
   if ((rc = mpm_state_load(c, state0))) return rc;
+  // the block counts of these partitions size the backward's kept ones
+  ZS_CUDA(cudaMemsetAsync(&c->d.cnt->max_gblocks, 0, 2 * sizeof(int), c->stream));
   for (int32_t s = 0; s < n_substeps; ++s) {
     if (s % every == 0 &&
         (rc = snapshot_copy(c, snap_store(c, ckpts + (size_t)(s / every) * snap), c->d.pbuf[c->cur],
@@ -1900,7 +1983,20 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
   const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));
   float *a = adj, *b = adj_tmp;  // adjoint of the next state, of this one
   const int32_t n_seg = (n_substeps + every - 1) / every;
+  // Each recomputed substep partitions its state and gathers its grid into
+  // a set of its own, which its adjoint then reads instead of partitioning
+  // and scattering again (sized by the forward rollout's block counts; the
+  // same substeps recomputed bit for bit ask for the same counts).
+  ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  const int seen = std::max(c->h_cnt->max_gblocks, c->h_cnt->max_buckets);
+  const int capb =
+      seen > 0 ? std::min(c->d.cap_gblocks, seen + std::max(64, seen / 64)) : c->d.cap_gblocks;
+  const bool keep = n_substeps > 0 && ensure_psets(c, std::min(every, n_substeps), capb);
+  static_assert(offsetof(Counters, n_buckets) == offsetof(Counters, n_gblocks) + sizeof(int),
+                "n_gblocks, n_buckets adjacent");
   StoreSwap swap(c);
+  PartSwap pswap(c);
   if ((rc = set_dt(c, dt))) return rc;
   for (int32_t seg = n_seg - 1; seg >= 0; --seg) {
     const int32_t s0 = seg * every, s1 = std::min(s0 + every, n_substeps);
@@ -1916,9 +2012,13 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
     c->binned = false;
     for (int32_t s = s0; s + 1 < s1; ++s) {
       swap.use(state(s), state(s + 1));
+      if (keep) pswap.set(c->psets[s - s0], c->pset_cap);
       if ((rc = prepare_partition(c))) return rc;
       enqueue_bin_if_needed(c);
       enqueue_substep(c, 0);  // bins the new positions: the next one needs no binning
+      if (keep)
+        ZS_CUDA(cudaMemcpyAsync(c->pset_cnt + 2 * (s - s0), &c->d.cnt->n_gblocks, 2 * sizeof(int),
+                                cudaMemcpyDeviceToDevice, c->stream));
       if ((rc = launch_check("rollout recompute"))) return rc;
     }
     // adjoint substeps, last to first, each on its own snapshot
@@ -1927,14 +2027,20 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
     const long long nn = c->prm.n;
     for (int32_t s = s1 - 1; s >= s0; --s) {
       swap.use(state(s), state(s));
-      c->needs_full_clear = true;  // the counts described another state
-      c->binned = false;
-      if ((rc = prepare_partition(c))) return rc;
-      enqueue_bin_if_needed(c);
-      enqueue_sort(c);
-      launch_p2g(c->d, 0, c->stream);
-      launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
-      if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
+      if (keep) pswap.set(c->psets[s - s0], c->pset_cap);
+      if (keep && s + 1 < s1) {  // kept by the recompute
+        ZS_CUDA(cudaMemcpyAsync(&c->d.cnt->n_gblocks, c->pset_cnt + 2 * (s - s0), 2 * sizeof(int),
+                                cudaMemcpyDeviceToDevice, c->stream));
+      } else {  // the segment's last substep (not recomputed), or no sets
+        c->needs_full_clear = true;  // the counts described another state
+        c->binned = false;
+        if ((rc = prepare_partition(c))) return rc;
+        enqueue_bin_if_needed(c);
+        enqueue_sort(c);
+        launch_p2g(c->d, 0, c->stream);
+        launch_grid_gather(c->d, 3, c->stream);  // grid velocities of this substep
+        if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
+      }
       launch_g2p_adjoint(c->d, 0, a, b, grad_mu, grad_lam, nn, c->stream);
       launch_grid_adjoint(c->d, c->stream);
       launch_p2g_adjoint(c->d, 0, b, grad_mu, grad_lam, nn, c->stream);
@@ -2016,7 +2122,7 @@ int32_t mpm_set_persistent(mpm_ctx *c, int32_t on, uint64_t barrier_limit) {
   if (on) {
     int coop = 0;
     ZS_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device));
-    if (!coop || persistent_grid(c->d) <= 0)
+    if (!coop || c->d.grid_persist <= 0)
       return fail(MPM_ERR_INVALID, "the device cannot run the persistent substep kernel");
   }
   ZS_CUDA(cudaStreamSynchronize(c->stream));

@@ -179,6 +179,8 @@ __device__ __forceinline__ void stage_scan_apply(const DevPtrs &d, int bid, int 
       d.cnt->n_gblocks = min(gpos, cap);
       d.cnt->n_buckets = min(bpos, cap);
       d.cnt->n_binned = ppos;
+      atomicMax(&d.cnt->max_gblocks, gpos);
+      atomicMax(&d.cnt->max_buckets, bpos);
       if (gpos > cap) atomicOr(&d.cnt->status, ST_CAPACITY);
     }
     __syncthreads();  // shared entries reused by the next tile

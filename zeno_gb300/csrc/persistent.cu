@@ -162,16 +162,21 @@ cudaError_t launch(const DevPtrs &d, int cur, int grid, cudaStream_t s) {
 
 }  // namespace
 
+// Fewer CTAs make each barrier cheaper (one arrival each); a small
+// context's stages have little work to spread: a CTA per 256 particle
+// slots of capacity (and per directory scan tile), at least one per SM.
 int persistent_grid(const DevPtrs &d) {
   int occ = occupancy<false, false>();
   occ = std::min(occ, occupancy<false, true>());
   occ = std::min(occ, occupancy<true, false>());
   occ = std::min(occ, occupancy<true, true>());
-  return occ > 0 ? occ * d.num_sms : 0;
+  if (occ <= 0) return 0;
+  const long long want = std::max<long long>((d.cap + 255) / 256, d.ntiles);
+  return (int)std::min<long long>(std::max<long long>(want, d.num_sms), (long long)occ * d.num_sms);
 }
 
 cudaError_t launch_substep_persistent(const DevPtrs &d, int cur, bool col, cudaStream_t s) {
-  const int grid = persistent_grid(d);
+  const int grid = d.grid_persist;
   if (grid <= 0) return cudaErrorCooperativeLaunchTooLarge;
   // the arrival counts (a launch that timed out may have left them set)
   static_assert(offsetof(Counters, bar_done) == offsetof(Counters, bar_count) + sizeof(unsigned),

@@ -206,6 +206,7 @@ void configure_launches(DevPtrs &d) {
   d.grid_sort = d.num_sms * (L.sort_ctas_per_sm > 0 ? L.sort_ctas_per_sm : 8);
   d.grid_stream = d.num_sms * (L.stream_ctas_per_sm > 0 ? L.stream_ctas_per_sm : 8);
   d.g2p_threads = gt;
+  d.grid_persist = persistent_grid(d);
 }
 
 template <int NT, int CH> void launch_p2g_shape(const DevPtrs &d, int cur, cudaStream_t s) {

@@ -105,6 +105,9 @@ struct Counters {
   int halt;
   int n_started;
   unsigned bbox[6];  // ordered-bits min x, y, z, max x, y, z of the positions
+  // the most grid / particle blocks a partition asked for since the last
+  // reset (the differentiable rollout sizes its per-substep partitions by it)
+  int max_gblocks, max_buckets;
   // grid-wide barrier of the persistent substep kernel: arrivals and the
   // generation the last arrival publishes; CTAs done with the last stage
   unsigned bar_count, bar_done, bar_gen, pad;
@@ -268,7 +271,16 @@ struct DevPtrs {
   int transfer;                      // MPM_TRANSFER_* (host copy of SimParams::transfer)
   int hencky;  // some material uses the von Mises / Cam-Clay return mapping
   int grid_p2g_flip, grid_g2p_flip;  // persistent grids of the FLIP transfer kernels
+  int grid_persist;  // CTAs of the persistent substep kernel (0: it cannot run)
   LaunchConfig launch;
+};
+
+// The partition and grid of one substep (the buffers a partition, P2G and
+// the grid gather write and the adjoint kernels read), for a differentiable
+// rollout that keeps them per substep instead of partitioning again.
+struct PartSet {
+  int32_t *perm, *dir_gb, *dir_bk, *gb_dir, *bk_dir, *bk_start, *bk_count;
+  float4 *grid, *ptile;
 };
 
 // flip.cu: the FLIP / AFLIP transfers (the launch_* functions of transfer.cu
@@ -309,8 +321,9 @@ void launch_bbox(const DevPtrs &d, int cur, cudaStream_t s);
 
 // persistent.cu: the whole fused substep (APIC; `colliders`: level-set
 // colliders on the listed blocks) as one cooperative kernel, its barrier
-// counter reset on the stream first; CTAs it launches with, 0 if the device
-// cannot run it
+// counter reset on the stream first, with d.grid_persist CTAs: the CTAs
+// the context's capacity needs, between one and all the CTAs the SMs hold at
+// once (0 if the device cannot run it)
 int persistent_grid(const DevPtrs &d);
 cudaError_t launch_substep_persistent(const DevPtrs &d, int cur, bool colliders, cudaStream_t s);
 // a grid barrier that nothing completes, with `limit` spins: every CTA gives
