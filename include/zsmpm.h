@@ -397,18 +397,25 @@ int32_t mpm_snapshot_floats(mpm_ctx *ctx, int64_t *floats);
  * planes), runs n_substeps substeps of dt, saving a snapshot of the state
  * before substep k * every into ckpts + k * mpm_snapshot_floats (k = 0 ..
  * ceil(n_substeps / every) - 1), and the final state into final_state
- * (state planes); all device memory. */
+ * (state planes); all device memory.  seg_states (optional, `every`
+ * snapshots, the backward's scratch): the substeps of the last segment then
+ * keep their states there and their partitions and grids in the context, so
+ * that the backward that follows with the same arguments takes that segment
+ * back without recomputing it (when the device has room for the partitions;
+ * otherwise it recomputes it). */
 int32_t mpm_rollout_forward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
-                            const float *state0, float *ckpts, float *final_state);
+                            const float *state0, float *ckpts, float *seg_states,
+                            float *final_state);
 /* Backward of that rollout, in one call: adj holds the adjoint of the final
  * state; the segments run last to first, each recomputed from its checkpoint
  * (each substep writing the next state straight into its snapshot in
- * seg_states, `every` snapshots) and then taken back through the adjoint
- * substep on each snapshot in place, so that adj ends as the adjoint of
- * state0 (adj_tmp: MPM_ADJ_PLANES x n floats of scratch) and grad_mu /
- * grad_lam (by upload index) gain the gradients of every substep.  The
- * context's own particle store is left unspecified: load a state before
- * stepping it again. */
+ * seg_states, `every` snapshots, and its partition and grid into a set the
+ * context keeps per substep of a segment, when the device has room) and then
+ * taken back through the adjoint substep on each snapshot in place, so that
+ * adj ends as the adjoint of state0 (adj_tmp: MPM_ADJ_PLANES x n floats of
+ * scratch) and grad_mu / grad_lam (by upload index) gain the gradients of
+ * every substep.  The context's own particle store is left unspecified: load
+ * a state before stepping it again. */
 int32_t mpm_rollout_backward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
                              const float *ckpts, float *seg_states, float *adj, float *adj_tmp,
                              float *grad_mu, float *grad_lam);

@@ -27,6 +27,8 @@
 // writes this one at p; the mu / lam gradients go by upload index.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "adj_moments.cuh"
 #include "binning.cuh"
 #include "colliders.cuh"
@@ -68,7 +70,8 @@ __global__ void __launch_bounds__(kAdjPThreads, 4)
     k_g2p_adjoint_particles(DevPtrs d, const float *__restrict__ pin,
                             const int32_t *__restrict__ iin, const float *__restrict__ an,
                             float *__restrict__ ap, float *__restrict__ gmu,
-                            float *__restrict__ glam, float *__restrict__ rec, long long n) {
+                            float *__restrict__ glam, float *__restrict__ rec, long long n,
+                            int kc) {
   __shared__ float4 sg[kNodes];
   __shared__ int sgb[8];
   const SimParams &P = *d.prm;
@@ -77,7 +80,10 @@ __global__ void __launch_bounds__(kAdjPThreads, 4)
   const int tid = threadIdx.x;
   const bool lame = P.has_lame != 0;
   const long long cap = d.cap;
-  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+  // work item w: chunk w % kc of particle block w / kc (kc CTAs share a
+  // block when the scene has few blocks)
+  for (int w = blockIdx.x; w < nb * kc; w += gridDim.x) {
+    const int b = w / kc, chunk = w - b * kc;
     const int dir = d.bk_dir[b];
     const SceneParams &S = d.scn[scene_of_dir(d, dir)];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
@@ -94,7 +100,7 @@ __global__ void __launch_bounds__(kAdjPThreads, 4)
     __syncthreads();
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
-    for (int j = tid; j < cnt; j += kAdjPThreads) {
+    for (int j = chunk * kAdjPThreads + tid; j < cnt; j += kc * kAdjPThreads) {
       // the particle's slot p in this state and its slot sp in the next
       // (the forward G2P writes it at its sorted position)
       const int sp = start + j;
@@ -351,14 +357,15 @@ constexpr int kP2GAdjThreads = 128;
 __global__ void __launch_bounds__(kP2GAdjThreads, 4)
     k_p2g_adjoint(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
                   float *__restrict__ ap, float *__restrict__ gmu, float *__restrict__ glam,
-                  long long n) {
+                  long long n, int kc) {
   __shared__ float4 sg[kNodes];
   __shared__ int sgb[8];
   const SimParams &P = *d.prm;
   const float dt = P.dt;
   const int nb = d.cnt->n_buckets;
   const bool lame = P.has_lame != 0;
-  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+  for (int w = blockIdx.x; w < nb * kc; w += gridDim.x) {  // chunk w % kc of block w / kc
+    const int b = w / kc, chunk = w - b * kc;
     const int dir = d.bk_dir[b];
     const SceneParams &S = d.scn[scene_of_dir(d, dir)];
     const float dx = S.dx, inv_dx = S.inv_dx, Dinv = S.Dinv;
@@ -375,7 +382,8 @@ __global__ void __launch_bounds__(kP2GAdjThreads, 4)
     __syncthreads();
     const int start = d.bk_start[b];
     const int cnt = (int)max(0ll, min((long long)d.bk_count[b], P.n - start));
-    for (int s = start + threadIdx.x; s < start + cnt; s += kP2GAdjThreads) {
+    for (int s = start + chunk * kP2GAdjThreads + threadIdx.x; s < start + cnt;
+         s += kc * kP2GAdjThreads) {
       const int p = d.perm[s];
       const MatParams mp = d.mats[min(max(iin[iidx(IC_MAT, p)], 0), kMaxMaterials - 1)];
       float x[3], v[3], C[9], F[9], Sv[6];
@@ -471,12 +479,20 @@ __global__ void __launch_bounds__(kP2GAdjThreads, 4)
   }
 }
 
+// CTAs per particle block of the per-particle adjoint kernels: a scene of
+// few blocks (about 400 particles each) spreads each block over several CTAs
+// so that the launch's CTAs all have work; the results do not depend on it.
+int adjoint_chunks(const DevPtrs &d, long long n) {
+  const long long want = (long long)d.num_sms * 4 * 384;
+  return (int)std::min<long long>(8, std::max<long long>(1, (want + n - 1) / std::max(n, 1ll)));
+}
+
 }  // namespace
 
 void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, float *gmu,
                         float *glam, long long n, cudaStream_t s) {
-  k_g2p_adjoint_particles<<<d.num_sms * 4, kAdjPThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur], an,
-                                                                ap, gmu, glam, d.adj_rec, n);
+  k_g2p_adjoint_particles<<<d.num_sms * 4, kAdjPThreads, 0, s>>>(
+      d, d.pbuf[cur], d.ibuf[cur], an, ap, gmu, glam, d.adj_rec, n, adjoint_chunks(d, n));
   cudaFuncSetAttribute(k_g2p_adjoint_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kP2GSmem);
   k_g2p_adjoint_scatter<<<d.num_sms * 4, kP2GThreads, kP2GSmem, s>>>(d, d.adj_rec);
@@ -489,7 +505,7 @@ void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s) {
 void launch_p2g_adjoint(const DevPtrs &d, int cur, float *ap, float *gmu, float *glam, long long n,
                         cudaStream_t s) {
   k_p2g_adjoint<<<d.num_sms * 4, kP2GAdjThreads, 0, s>>>(d, d.pbuf[cur], d.ibuf[cur], ap, gmu,
-                                                        glam, n);
+                                                        glam, n, adjoint_chunks(d, n));
 }
 
 }  // namespace zsmpm

@@ -90,6 +90,15 @@ struct mpm_ctx {
   std::vector<zsmpm::PartSet> psets;
   int pset_cap = 0;
   int32_t *pset_cnt = nullptr;
+  // the last segment of the latest rollout forward, kept in seg_states and
+  // psets for the backward with the same arguments
+  struct {
+    bool valid = false;
+    float dt = 0.0f;
+    int32_t n = 0, every = 0;
+    const float *ckpts = nullptr;
+    const float *seg = nullptr;
+  } tail;
 };
 
 namespace {
@@ -1941,22 +1950,97 @@ struct PartSwap {
 }  // namespace
 
 int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
-                            const float *state0, float *ckpts, float *final_state) {
+                            const float *state0, float *ckpts, float *seg_states,
+                            float *final_state) {
   int32_t rc = check(c);
   if (rc) return rc;
   if (n_substeps < 0 || every <= 0 || !state0 || !final_state || (n_substeps > 0 && !ckpts))
     return fail(MPM_ERR_INVALID, "invalid rollout arguments");
+  c->tail.valid = false;
   const long long n = c->prm.n;
   const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));
   if ((rc = mpm_state_load(c, state0))) return rc;
   // the block counts of these partitions size the backward's kept ones
   ZS_CUDA(cudaMemsetAsync(&c->d.cnt->max_gblocks, 0, 2 * sizeof(int), c->stream));
-  for (int32_t s = 0; s < n_substeps; ++s) {
+  const int32_t n_seg = (n_substeps + every - 1) / every;
+  const int32_t s_tail = n_substeps > 0 ? (n_seg - 1) * every : 0;
+  const bool want_tail = seg_states && n_substeps > 0 && c->differentiable;
+  for (int32_t s = 0; s < (want_tail ? s_tail : n_substeps); ++s) {
     if (s % every == 0 &&
         (rc = snapshot_copy(c, snap_store(c, ckpts + (size_t)(s / every) * snap), c->d.pbuf[c->cur],
                             c->d.ibuf[c->cur])))
       return rc;
     if ((rc = mpm_substep(c, dt, 1))) return rc;
+  }
+  // The last segment through kept snapshots and partitions, sized by the
+  // block counts so far with room to double (a segment that outgrows them
+  // is run again the plain way).
+  bool tail = false;
+  Counters before{};
+  if (want_tail) {
+    if ((rc = mpm_sync(c))) return rc;
+    before = *c->h_cnt;
+    const int seen = std::max(c->h_cnt->max_gblocks, c->h_cnt->max_buckets);
+    const int capb = seen > 0 ? std::min(c->d.cap_gblocks, std::max(2 * seen, seen + 4096))
+                              : c->d.cap_gblocks;
+    tail = ensure_psets(c, std::min(every, n_substeps), capb);
+  }
+  if (tail) {
+    SnapStore ck = snap_store(c, ckpts + (size_t)(n_seg - 1) * snap);
+    if ((rc = snapshot_copy(c, ck, c->d.pbuf[c->cur], c->d.ibuf[c->cur]))) return rc;
+    // state s of the segment: its checkpoint, then seg_states slots 1 ..;
+    // the final state into slot 0 (the backward's recompute never uses it)
+    auto state = [&](int32_t s) {
+      return s == s_tail ? ck
+                         : snap_store(c, seg_states + (s == n_substeps ? 0 : (size_t)(s - s_tail) * snap));
+    };
+    {
+      StoreSwap swap(c);
+      PartSwap pswap(c);
+      set_auto_step(c, 1);
+      if ((rc = set_dt(c, dt)) || (rc = push_params(c))) return rc;
+      for (int32_t s = s_tail; s < n_substeps; ++s) {
+        swap.use(state(s), state(s + 1));
+        pswap.set(c->psets[s - s_tail], c->pset_cap);
+        if ((rc = prepare_partition(c))) return rc;
+        enqueue_bin_if_needed(c);
+        enqueue_substep(c, 0);
+        ZS_CUDA(cudaMemcpyAsync(c->pset_cnt + 2 * (s - s_tail), &c->d.cnt->n_gblocks,
+                                2 * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+        if ((rc = launch_check("rollout forward"))) return rc;
+      }
+    }
+    ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+    ZS_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->h_cnt->status & ST_CAPACITY) {
+      // more blocks than the kept sets hold: the segment again, the plain
+      // way, from the counters as they were before it
+      ZS_CUDA(cudaMemcpyAsync(c->d.cnt, &before, sizeof(Counters), cudaMemcpyHostToDevice,
+                              c->stream));
+      ZS_CUDA(cudaMemcpyAsync(c->d.pbuf[c->cur], ck.f, (size_t)tiled_elems(n, NCH) * sizeof(float),
+                              cudaMemcpyDeviceToDevice, c->stream));
+      ZS_CUDA(cudaMemcpyAsync(c->d.ibuf[c->cur], ck.i,
+                              (size_t)tiled_elems(n, NICH) * sizeof(int32_t),
+                              cudaMemcpyDeviceToDevice, c->stream));
+      ZS_CUDA(cudaStreamSynchronize(c->stream));
+      free_psets(c);
+      for (int32_t s = s_tail; s < n_substeps; ++s)
+        if ((rc = mpm_substep(c, dt, 1))) return rc;
+      return mpm_state_save(c, final_state);
+    }
+    // the final state back into the context's own store
+    SnapStore fin = state(n_substeps);
+    ZS_CUDA(cudaMemcpyAsync(c->d.pbuf[c->cur], fin.f, (size_t)tiled_elems(n, NCH) * sizeof(float),
+                            cudaMemcpyDeviceToDevice, c->stream));
+    ZS_CUDA(cudaMemcpyAsync(c->d.ibuf[c->cur], fin.i, (size_t)tiled_elems(n, NICH) * sizeof(int32_t),
+                            cudaMemcpyDeviceToDevice, c->stream));
+    c->substeps += n_substeps - s_tail;
+    c->tail.valid = true;
+    c->tail.dt = dt;
+    c->tail.n = n_substeps;
+    c->tail.every = every;
+    c->tail.ckpts = ckpts;
+    c->tail.seg = seg_states;
   }
   return mpm_state_save(c, final_state);
 }
@@ -1992,7 +2076,14 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
   const int seen = std::max(c->h_cnt->max_gblocks, c->h_cnt->max_buckets);
   const int capb =
       seen > 0 ? std::min(c->d.cap_gblocks, seen + std::max(64, seen / 64)) : c->d.cap_gblocks;
-  const bool keep = n_substeps > 0 && ensure_psets(c, std::min(every, n_substeps), capb);
+  // the forward with these arguments kept its last segment (states in
+  // seg_states, partitions in the sets): no recompute for that one
+  const bool tail_kept = c->tail.valid && c->tail.dt == dt && c->tail.n == n_substeps &&
+                         c->tail.every == every && c->tail.ckpts == ckpts &&
+                         c->tail.seg == seg_states && (int)c->psets.size() >= std::min(every, n_substeps);
+  c->tail.valid = false;  // the recompute of the other segments overwrites it
+  const bool keep =
+      n_substeps > 0 && (tail_kept || ensure_psets(c, std::min(every, n_substeps), capb));
   static_assert(offsetof(Counters, n_buckets) == offsetof(Counters, n_gblocks) + sizeof(int),
                 "n_gblocks, n_buckets adjacent");
   StoreSwap swap(c);
@@ -2006,11 +2097,12 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
       return s == s0 ? snap_store(c, const_cast<float *>(ckpts) + (size_t)seg * snap)
                      : snap_store(c, seg_states + (size_t)(s - s0) * snap);
     };
+    const bool kept = tail_kept && seg == n_seg - 1;  // states and sets from the forward
     set_auto_step(c, 1);
     if ((rc = push_params(c))) return rc;
     c->needs_full_clear = true;
     c->binned = false;
-    for (int32_t s = s0; s + 1 < s1; ++s) {
+    for (int32_t s = s0; !kept && s + 1 < s1; ++s) {
       swap.use(state(s), state(s + 1));
       if (keep) pswap.set(c->psets[s - s0], c->pset_cap);
       if ((rc = prepare_partition(c))) return rc;
@@ -2028,7 +2120,7 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
     for (int32_t s = s1 - 1; s >= s0; --s) {
       swap.use(state(s), state(s));
       if (keep) pswap.set(c->psets[s - s0], c->pset_cap);
-      if (keep && s + 1 < s1) {  // kept by the recompute
+      if (keep && (s + 1 < s1 || kept)) {  // kept by the recompute (or the forward)
         ZS_CUDA(cudaMemcpyAsync(&c->d.cnt->n_gblocks, c->pset_cnt + 2 * (s - s0), 2 * sizeof(int),
                                 cudaMemcpyDeviceToDevice, c->stream));
       } else {  // the segment's last substep (not recomputed), or no sets

@@ -8,14 +8,16 @@ differentiable mode and exposes `rollout(v0, E) -> x_final` as a
   v0, C = 0, F = I, per-particle mu / lam from Young's moduli E and the
   material's nu) and runs the whole rollout in one C-ABI call
   (mpm_rollout_forward), which keeps a snapshot of the particle store every
-  `ckpt_every` substeps in device buffers owned by torch;
+  `ckpt_every` substeps in device buffers owned by torch, and the last
+  segment's states in the backward's segment buffer;
 * backward: one C-ABI call (mpm_rollout_backward) walks the segments in
-  reverse; each segment is recomputed from its checkpoint (each substep
-  writing the next state straight into a snapshot buffer) and the
-  hand-written adjoint substep (G2P, grid update + boundary, P2G and the
-  stress) runs backwards through the snapshots in place.  Memory: one
-  snapshot per segment plus one segment of snapshots, 37 floats per particle
-  each.
+  reverse; each segment but the last is recomputed from its checkpoint
+  (each substep writing the next state straight into a snapshot buffer, and
+  its partition and grid into a set the context keeps) and the hand-written
+  adjoint substep (G2P, grid update + boundary, P2G and the stress) runs
+  backwards through the snapshots in place.  Memory: one snapshot per
+  segment plus one segment of snapshots, 37 floats per particle each, plus
+  one partition and grid per substep of a segment.
 
 The substep keeps the particle store sorted by block, so every state (and
 its adjoint) is in its own slot order; the state's upload-index plane maps
@@ -99,8 +101,11 @@ class _RolloutFn(torch.autograd.Function):
             ckpts = torch.empty(max(sim.n_ckpt, 1), sim.snap, dtype=torch.float32,
                                 device=sim.dev)
             final = torch.empty(PLANES, n, dtype=torch.float32, device=sim.dev)
+            # the backward's segment scratch, already holding the last
+            # segment's states when the backward comes
+            seg = torch.empty(sim.ckpt_every, sim.snap, dtype=torch.float32, device=sim.dev)
             sim.ctx.rollout_forward(sim.dt, sim.n_substeps, sim.ckpt_every, state.data_ptr(),
-                                    ckpts.data_ptr(), final.data_ptr())
+                                    ckpts.data_ptr(), final.data_ptr(), seg.data_ptr())
             # the final state's slots back into upload order
             ids = final[ID].view(torch.int32).long()
             x = torch.empty(n, 3, dtype=torch.float32, device=sim.dev)
@@ -108,6 +113,7 @@ class _RolloutFn(torch.autograd.Function):
         torch.cuda.current_stream().wait_stream(sim.stream)
         fctx.sim = sim
         fctx.ckpts = ckpts
+        fctx.seg = seg
         fctx.ids = ids
         fctx.E = E.detach()
         return x
@@ -123,7 +129,7 @@ class _RolloutFn(torch.autograd.Function):
             tmp = torch.empty_like(adj)
             gmu = torch.zeros(n, dtype=torch.float32, device=sim.dev)
             glam = torch.zeros(n, dtype=torch.float32, device=sim.dev)
-            seg = torch.empty(k, sim.snap, dtype=torch.float32, device=sim.dev)
+            seg = fctx.seg
             sim.ctx.rollout_backward(sim.dt, sim.n_substeps, k, fctx.ckpts.data_ptr(),
                                      seg.data_ptr(), adj.data_ptr(), tmp.data_ptr(),
                                      gmu.data_ptr(), glam.data_ptr())

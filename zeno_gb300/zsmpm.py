@@ -160,7 +160,7 @@ def load(path: str = LIB_PATH):
         "mpm_set_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
         "mpm_get_launch_config": ([P, C.POINTER(LaunchConfig)], i32),
         "mpm_set_differentiable": ([P, i32], i32),
-        "mpm_rollout_forward": ([P, f32, i32, i32, P, P, P], i32),
+        "mpm_rollout_forward": ([P, f32, i32, i32, P, P, P, P], i32),
         "mpm_snapshot_floats": ([P, P], i32),
         "mpm_rollout_backward": ([P, f32, i32, i32, P, P, P, P, P, P], i32),
         "mpm_set_auto_regrow": ([P, i32], i32),
@@ -559,9 +559,12 @@ class Context:
         return v.value
 
     def rollout_forward(self, dt, n_substeps: int, every: int, state0: int, ckpts: int,
-                        final: int):
+                        final: int, seg_states: int = 0):
+        """seg_states (0: none): the backward's scratch, which then receives
+        the last segment's states so that the backward skips recomputing it."""
         self._check(self._L.mpm_rollout_forward(self.h, dt, int(n_substeps), int(every),
                                                 C.c_void_p(state0), C.c_void_p(ckpts),
+                                                C.c_void_p(seg_states or None),
                                                 C.c_void_p(final)), "mpm_rollout_forward")
 
     def rollout_backward(self, dt, n_substeps: int, every: int, ckpts: int, seg_states: int,
