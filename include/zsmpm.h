@@ -191,6 +191,36 @@ int32_t mpm_set_gravity(mpm_ctx *ctx, float gx, float gy, float gz);
  * b += db/dt dt, s += ds/dt dt). */
 #define MPM_MAX_COLLIDERS 16
 int32_t mpm_add_collider(mpm_ctx *ctx, const mpm_collider_desc *desc, int32_t *id);
+/* Boundary grid (MakeZSGrid transfer="boundary", Generation.cu:1490-1506)
+ * of a one-scene context: ZSBoundaryPrimitiveToZSGrid (Transfer.cu:1532-1623)
+ * scatters the points with the linear kernel -- m += W m_p, m v += W m_p v_p
+ * and, for the n_eles triangle rows after the n_verts vertex rows,
+ * m nrm += W m_p nrm_p -- and UpdateZSGrid's boundary branch
+ * (MPMPipeline.cu:899-911) sets v = m v / m, nrm = unit(m nrm) (a node no
+ * triangle reached keeps a zero normal where the reference divides by zero).
+ * Every substep then applies it as ApplyGridBoundaryOnZSGrid
+ * (Boundary.cu:18-69) with `type` (MPM_BC_STICKY / SLIP / SEPARATE) to each
+ * grid node of non-zero mass whose boundary node has non-zero mass, after
+ * the walls and the level-set colliders.  Host arrays: x, v (NULL: zero),
+ * nrm (n_verts + n_eles) x 3, m n_verts + n_eles.  The points do not move;
+ * set them again to move the boundary.  The adjoint and the persistent
+ * substep kernel take no boundary grid (the substep keeps its kernels). */
+int32_t mpm_set_grid_boundary(mpm_ctx *ctx, int32_t type, int64_t n_verts, int64_t n_eles,
+                              const float *x, const float *v, const float *m, const float *nrm);
+int32_t mpm_clear_grid_boundary(mpm_ctx *ctx);
+/* ApplyGridBoundaryOnZSGrid alone, for node graphs (after mpm_grid_update) */
+int32_t mpm_apply_grid_boundary(mpm_ctx *ctx);
+/* ToBoundaryParticles (Generation.cpp:1154-1460, without sprayed points):
+ * host-side conversion of a triangle mesh (n_verts positions, velocities or
+ * NULL, n_tris index triples) into boundary points, the vertices first, then
+ * one point per triangle.  Vertex: m = the sum over its triangles of a third
+ * of the triangle's area in units of dx^2, v its velocity, nrm the unit sum
+ * of its triangles' normals.  Triangle: m its area in dx^2, x and v the
+ * means of its vertices', nrm = unit(unit(p1 - p0) x unit(p2 - p0)).
+ * Outputs hold n_verts + n_tris rows (x, v, nrm 3 floats each). */
+int32_t mpm_boundary_points_from_mesh(int64_t n_verts, const float *pos, const float *vel,
+                                      int64_t n_tris, const int32_t *tris, float dx, float *x,
+                                      float *v, float *m, float *nrm);
 int32_t mpm_clear_colliders(mpm_ctx *ctx);
 /* id: the collider from mpm_add_collider, or -1 for every collider */
 int32_t mpm_step_colliders(mpm_ctx *ctx, int32_t id, float dt);

@@ -26,11 +26,13 @@
 #include "mpm_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <limits>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -499,6 +501,80 @@ template <class R> struct Sim {
   std::vector<R> grid;
   R max_vel_sqr = 0;
 
+  // Boundary grid nodes by node index (ZSBoundaryPrimitiveToZSGrid,
+  // Transfer.cu:1532-1623, then UpdateZSGrid's boundary branch,
+  // MPMPipeline.cu:899-911); the boundary points do not move.
+  struct BNode {
+    R m, v[3], n[3];
+  };
+  std::unordered_map<int64_t, BNode> bgrid;
+  static int64_t node_key(const int32_t *I) {
+    return ((int64_t(I[0]) + (1 << 20)) << 42) | ((int64_t(I[1]) + (1 << 20)) << 21) |
+           (int64_t(I[2]) + (1 << 20));
+  }
+  void build_grid_boundary() {
+    const orc_grid_boundary *gb = sc.grid_boundary;
+    if (!gb) return;
+    const float inv_dx = 1.0f / sc.dx;
+    std::unordered_map<int64_t, std::array<R, 7>> acc;
+    const int64_t np = gb->n_verts + gb->n_eles;
+    for (int64_t p = 0; p < np; ++p) {
+      // linear kernel: nodes base, base + 1 per axis, base = floor(x / dx)
+      int32_t base[3];
+      R w[3][2];
+      for (int d = 0; d < 3; ++d) {
+        const float c = gb->x[3 * p + d] * inv_dx;
+        base[d] = int32_t(std::floor(c));
+        const R f = R(c) - R(base[d]);
+        w[d][0] = R(1) - f;
+        w[d][1] = f;
+      }
+      const R m = R(gb->m[p]);
+      const bool with_n = p >= gb->n_verts;
+      for (int o = 0; o < 8; ++o) {
+        const int32_t I[3] = {base[0] + (o >> 2), base[1] + ((o >> 1) & 1), base[2] + (o & 1)};
+        const R W = w[0][o >> 2] * w[1][(o >> 1) & 1] * w[2][o & 1];
+        auto &a = acc.try_emplace(node_key(I), std::array<R, 7>{}).first->second;
+        a[0] += W * m;
+        for (int d = 0; d < 3; ++d) a[1 + d] += W * m * R(gb->v[3 * p + d]);
+        if (with_n)
+          for (int d = 0; d < 3; ++d) a[4 + d] += W * m * R(gb->nrm[3 * p + d]);
+      }
+    }
+    for (const auto &kv : acc) {
+      const auto &a = kv.second;
+      BNode b{};
+      b.m = a[0];
+      if (a[0] != R(0)) {
+        for (int d = 0; d < 3; ++d) b.v[d] = a[1 + d] / a[0];
+        // unit(nrm / m); a node no triangle reached keeps a zero normal
+        const R nn = std::sqrt(a[4] * a[4] + a[5] * a[5] + a[6] * a[6]);
+        if (nn > R(0))
+          for (int d = 0; d < 3; ++d) b.n[d] = a[4 + d] / nn;
+      }
+      bgrid.emplace(kv.first, b);
+    }
+  }
+
+  // ApplyGridBoundaryOnZSGrid (Boundary.cu:18-69) on the velocity of the
+  // node at index I (a node of non-zero mass)
+  void apply_grid_boundary(const int32_t *I, R *vel) const {
+    if (bgrid.empty()) return;
+    const auto it = bgrid.find(node_key(I));
+    if (it == bgrid.end() || it->second.m == R(0)) return;
+    const BNode &b = it->second;
+    if (sc.grid_boundary->type == ORC_BC_STICKY) {
+      for (int d = 0; d < 3; ++d) vel[d] = b.v[d];
+      return;
+    }
+    R u[3];
+    for (int d = 0; d < 3; ++d) u[d] = vel[d] - b.v[d];
+    const R proj = b.n[0] * u[0] + b.n[1] * u[1] + b.n[2] * u[2];
+    if (sc.grid_boundary->type == ORC_BC_SLIP || (sc.grid_boundary->type == ORC_BC_SEPARATE && proj < 0))
+      for (int d = 0; d < 3; ++d) u[d] -= proj * b.n[d];
+    for (int d = 0; d < 3; ++d) vel[d] = u[d] + b.v[d];
+  }
+
   Sim(const orc_scene &s, int nt) : sc(s), nthreads(nt) {
     for (int d = 0; d < 3; ++d) {
       dir.lo[d] = s.block_lo[d];
@@ -513,6 +589,7 @@ template <class R> struct Sim {
       c.s = R(c.c->scale);
       cols.push_back(c);
     }
+    build_grid_boundary();
   }
 
   // R = Ry(yaw) Rx(pitch) Rz(roll), angles in degrees
@@ -1248,6 +1325,7 @@ template <class R> struct Sim {
           vmax = std::max(vmax, vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
           apply_bc(I, vel);
           apply_colliders(I, vel);
+          apply_grid_boundary(I, vel);
           for (int d = 0; d < 3; ++d) nd[1 + d] = vel[d];
         } else {
           // MPMPipeline.cu:882-893: v = mv / m; vstar = vstar / m + v + g dt;
@@ -1260,6 +1338,7 @@ template <class R> struct Sim {
           vmax = std::max(vmax, vs[0] * vs[0] + vs[1] * vs[1] + vs[2] * vs[2]);
           apply_bc(I, vs);
           apply_colliders(I, vs);
+          apply_grid_boundary(I, vs);
           for (int d = 0; d < 3; ++d) {
             nd[1 + d] = vel[d];
             nd[4 + d] = vs[d];
@@ -1742,6 +1821,67 @@ int32_t orc_curve_init_f64(int64_t n_verts, const float *x, const float *v, int6
   }
   out->n_verts = n_verts;
   out->n_eles = n_segs;
+  return ORC_OK;
+}
+
+int32_t orc_boundary_points_from_mesh(int64_t n_verts, const float *pos, const float *vel,
+                                      int64_t n_tris, const int32_t *tris, float dx,
+                                      double *x, double *v, double *m, double *nrm) {
+  if (n_verts < 0 || n_tris < 0 || !pos || (n_tris > 0 && !tris) || !(dx > 0) || !x || !v || !m ||
+      !nrm)
+    return ORC_ERR_INVALID;
+  for (int64_t t = 0; t < 3 * n_tris; ++t)
+    if (tris[t] < 0 || tris[t] >= n_verts) return ORC_ERR_INVALID;
+  auto unit = [](double *a) {
+    const double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (l > 0)
+      for (int d = 0; d < 3; ++d) a[d] /= l;
+  };
+  for (int64_t i = 0; i < n_verts; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      x[3 * i + d] = pos[3 * i + d];
+      v[3 * i + d] = vel ? vel[3 * i + d] : 0.0;
+      nrm[3 * i + d] = 0.0;
+    }
+    m[i] = 0.0;
+  }
+  for (int64_t t = 0; t < n_tris; ++t) {
+    const int32_t *tr = tris + 3 * t;
+    double p[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int d = 0; d < 3; ++d) p[k][d] = pos[3 * tr[k] + d];
+    double a[3], b[3];
+    for (int d = 0; d < 3; ++d) {
+      a[d] = (p[1][d] - p[0][d]) / dx;
+      b[d] = (p[2][d] - p[0][d]) / dx;
+    }
+    const double cr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                          a[0] * b[1] - a[1] * b[0]};
+    const double area = 0.5 * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    double e1[3], e2[3];
+    for (int d = 0; d < 3; ++d) {
+      e1[d] = p[1][d] - p[0][d];
+      e2[d] = p[2][d] - p[0][d];
+    }
+    unit(e1);
+    unit(e2);
+    double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                   e1[0] * e2[1] - e1[1] * e2[0]};
+    unit(n);
+    const int64_t r = n_verts + t;
+    m[r] = area;
+    for (int d = 0; d < 3; ++d) {
+      x[3 * r + d] = (p[0][d] + p[1][d] + p[2][d]) / 3.0;
+      v[3 * r + d] = vel ? (double(vel[3 * tr[0] + d]) + vel[3 * tr[1] + d] + vel[3 * tr[2] + d]) / 3.0
+                         : 0.0;
+      nrm[3 * r + d] = n[d];
+    }
+    for (int k = 0; k < 3; ++k) {
+      m[tr[k]] += area / 3.0;
+      for (int d = 0; d < 3; ++d) nrm[3 * tr[k] + d] += n[d];
+    }
+  }
+  for (int64_t i = 0; i < n_verts; ++i) unit(nrm + 3 * i);
   return ORC_OK;
 }
 

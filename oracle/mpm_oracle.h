@@ -119,6 +119,23 @@ typedef struct orc_trackers {
   double *x, *v; /* n x 3, in/out */
 } orc_trackers;
 
+/* Boundary grid (MakeZSGrid transfer="boundary", Generation.cu:1490-1506)
+ * filled from boundary points by ZSBoundaryPrimitiveToZSGrid
+ * (Transfer.cu:1532-1623: linear kernel, m += W m_p, mv += W m_p v_p, and for
+ * the element rows m nrm += W m_p nrm_p), normalised by UpdateZSGrid's
+ * boundary branch (MPMPipeline.cu:899-911: v = mv / m, nrm = unit(nrm / m)),
+ * and applied to the velocity of every grid node whose mass is non-zero in
+ * both grids by ApplyGridBoundaryOnZSGrid (Boundary.cu:18-69), after the
+ * walls and the level-set colliders.  Rows 0 .. n_verts-1 are the mesh's
+ * vertices (no normal), the n_eles rows after them its triangles. */
+typedef struct orc_grid_boundary {
+  int32_t type; /* ORC_BC_STICKY / SLIP / SEPARATE */
+  int64_t n_verts, n_eles;
+  const float *x, *v; /* (n_verts + n_eles) x 3 */
+  const float *m;     /* n_verts + n_eles */
+  const float *nrm;   /* (n_verts + n_eles) x 3; read for the element rows */
+} orc_grid_boundary;
+
 typedef struct orc_scene {
   float dx;
   float gravity[3];
@@ -136,6 +153,7 @@ typedef struct orc_scene {
   int32_t transfer;          /* ORC_TRANSFER_* */
   orc_cloth *cloth;          /* NULL, or one cloth stepped with the particles (FP64 only) */
   orc_trackers *trackers;    /* NULL, or tracker points (FP64 only) */
+  const orc_grid_boundary *grid_boundary; /* NULL, or the boundary grid's points */
 } orc_scene;
 
 typedef struct orc_stats {
@@ -230,6 +248,18 @@ int32_t orc_curve_init_f64(int64_t n_verts, const float *x, const float *v, int6
                            orc_cloth *out);
 
 int32_t orc_max_threads(void);
+
+/* ToBoundaryParticles (Generation.cpp:1154-1460) without sprayed points: a
+ * triangle mesh (n_verts positions, velocities or NULL, n_tris index
+ * triples) to boundary points, the vertices first, then one point per
+ * triangle.  Vertex: m = the sum over its triangles of a third of the
+ * triangle's area in units of dx^2, v its velocity, nrm the unit sum of its
+ * triangles' normals.  Triangle: m its area in dx^2, x and v the means of its
+ * vertices', nrm = unit(unit(p1 - p0) x unit(p2 - p0)).  Outputs hold
+ * n_verts + n_tris rows. */
+int32_t orc_boundary_points_from_mesh(int64_t n_verts, const float *pos, const float *vel,
+                                      int64_t n_tris, const int32_t *tris, float dx,
+                                      double *x, double *v, double *m, double *nrm);
 
 #ifdef __cplusplus
 }

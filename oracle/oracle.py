@@ -53,6 +53,11 @@ class OrcTrackers(C.Structure):
     _fields_ = [("n", C.c_int64), ("x", C.c_void_p), ("v", C.c_void_p)]
 
 
+class OrcGridBoundary(C.Structure):
+    _fields_ = [("type", C.c_int32), ("n_verts", C.c_int64), ("n_eles", C.c_int64),
+                ("x", C.c_void_p), ("v", C.c_void_p), ("m", C.c_void_p), ("nrm", C.c_void_p)]
+
+
 class OrcScene(C.Structure):
     _fields_ = [("dx", C.c_float), ("gravity", C.c_float * 3), ("block_lo", C.c_int32 * 3),
                 ("block_dims", C.c_int32 * 3), ("bc_type", C.c_int32),
@@ -60,7 +65,8 @@ class OrcScene(C.Structure):
                 ("n_materials", C.c_int32), ("materials", C.POINTER(OrcMaterial)),
                 ("n_colliders", C.c_int32), ("colliders", C.POINTER(OrcCollider)),
                 ("collider_autostep", C.c_int32), ("transfer", C.c_int32),
-                ("cloth", C.POINTER(OrcCloth)), ("trackers", C.POINTER(OrcTrackers))]
+                ("cloth", C.POINTER(OrcCloth)), ("trackers", C.POINTER(OrcTrackers)),
+                ("grid_boundary", C.POINTER(OrcGridBoundary))]
 
 
 class OrcStats(C.Structure):
@@ -116,6 +122,9 @@ def lib():
         L.orc_project_hencky.argtypes = [C.POINTER(OrcMaterial), P, P]
         L.orc_project_hencky.restype = C.c_int32
         L.orc_max_threads.restype = C.c_int32
+        L.orc_boundary_points_from_mesh.argtypes = [C.c_int64, P, P, C.c_int64, P, C.c_float,
+                                                    P, P, P, P]
+        L.orc_boundary_points_from_mesh.restype = C.c_int32
         _lib = L
     return _lib
 
@@ -161,7 +170,13 @@ class _SceneHolder:
                           (C.c_int32 * 3)(*scene.bc_lo), (C.c_int32 * 3)(*scene.bc_hi),
                           len(scene.materials), C.cast(mats, C.POINTER(OrcMaterial)),
                           len(cols), C.cast(carr, C.POINTER(OrcCollider)), 1,
-                          int(getattr(scene, "transfer", 0)), None, None)
+                          int(getattr(scene, "transfer", 0)), None, None, None)
+        gbd = getattr(scene, "grid_boundary", None)
+        if gbd is not None:
+            self.gbd = OrcGridBoundary(int(gbd.type), int(gbd.n_verts),
+                                       int(len(gbd.m) - gbd.n_verts), arr(gbd.x), arr(gbd.v),
+                                       arr(gbd.m), arr(gbd.nrm))
+            self.s.grid_boundary = C.pointer(self.gbd)
 
     def attach_cloth(self, cl: "OrcCloth"):
         self.cloth = cl
@@ -423,3 +438,24 @@ def project_hencky(material, F: np.ndarray, logJp: float = 0.0):
 
 def max_threads() -> int:
     return int(lib().orc_max_threads())
+
+
+def boundary_points_from_mesh(pos: np.ndarray, tris: np.ndarray, dx: float,
+                              vel: np.ndarray | None = None) -> dict:
+    """ToBoundaryParticles (no sprayed points) in FP64: rows of the mesh's
+    vertices, then of its triangles: x, v, m, nrm."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+    tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    nv, nt = pos.shape[0], tris.shape[0]
+    velp = None
+    if vel is not None:
+        vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+        velp = _ptr(vel)
+    out = {k: np.zeros((nv + nt, 3) if k != "m" else nv + nt, np.float64)
+           for k in ("x", "v", "m", "nrm")}
+    rc = lib().orc_boundary_points_from_mesh(nv, _ptr(pos), velp, nt, _ptr(tris), C.c_float(dx),
+                                             _ptr(out["x"]), _ptr(out["v"]), _ptr(out["m"]),
+                                             _ptr(out["nrm"]))
+    if rc != 0:
+        raise RuntimeError(f"oracle boundary points failed with status {rc}")
+    return out

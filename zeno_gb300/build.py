@@ -22,7 +22,7 @@ NODES_LIB = os.path.join(PKG, "libzsmpm_nodes.so")
 NODES = os.path.join(PKG, "nodes")
 NODE_SOURCES = ["MPMNodes.cpp", "nodes_capi.cpp"]
 
-SOURCES = ["partition.cu", "transfer.cu", "flip.cu", "cloth.cu", "adjoint.cu", "io.cu", "output.cu", "api.cu", "noalloc.cu", "persistent.cu"]
+SOURCES = ["partition.cu", "transfer.cu", "flip.cu", "cloth.cu", "adjoint.cu", "io.cu", "output.cu", "api.cu", "noalloc.cu", "persistent.cu", "boundary_grid.cu"]
 HEADERS = ["zsmpm_internal.cuh", "mpm_math.cuh", "binning.cuh", "tile_scatter.cuh", "cp_async.cuh",
            "adj_moments.cuh", "partition_stages.cuh", "transfer_stages.cuh",
            "colliders.cuh", "blocks.cuh"]

@@ -84,6 +84,10 @@ struct mpm_ctx {
   int32_t max_grid_blocks_req = 0;  // as given at creation (0: the default rule)
   // mpm_set_persistent: the fused substep as one cooperative kernel
   bool persistent = false;
+  // boundary grid (mpm_set_grid_boundary): its points as given (the grid is
+  // built again when the directory grows)
+  std::vector<float> bnd_pts;  // x 3, v 3, m, nrm 3 per point
+  int64_t bnd_n = 0, bnd_n_verts = 0;
   // differentiable rollout: the partition and grid of each recomputed
   // substep of a segment, kept for its adjoint (PartSet below), `pset_cap`
   // blocks each; n_gblocks, n_buckets of each (device, 2 per set)
@@ -197,7 +201,7 @@ void enqueue_sort(mpm_ctx *c) {
 // mpm_set_persistent applies: the fused substep is one cooperative kernel
 bool uses_persistent(const mpm_ctx *c) {
   return c->persistent && c->d.cloth.n_verts == 0 && c->d.n_trackers == 0 &&
-         c->d.transfer == MPM_TRANSFER_APIC;
+         c->d.transfer == MPM_TRANSFER_APIC && !c->d.bnd_map;
 }
 
 // One substep of the fused path; the counts of the current positions must be
@@ -238,6 +242,7 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
     launch_grid_gather(c->d, 3, c->stream);
     if (!c->colliders.empty()) launch_apply_colliders_listed(c->d, c->stream);
   }
+  launch_apply_grid_boundary(c->d, c->stream);  // a boundary grid, if set
   mark(MPM_STAGE_G2P);
   launch_g2p(c->d, cur, 1, 1, c->stream);
   if (cloth) launch_cloth_g2p(c->d, c->stream);
@@ -324,6 +329,8 @@ float from_ordered_bits(unsigned u) {
 // and, if the new box allows more grid blocks than the context holds, the
 // grid-sized buffers are reallocated; the counters, graphs and partition
 // start afresh, and the next substep bins the current positions.
+int32_t build_grid_boundary(mpm_ctx *c);
+
 int32_t regrow(mpm_ctx *c) {
   DevPtrs &d = c->d;
   if (c->scenes.size() != 1) return fail(MPM_ERR_OUT_OF_DOMAIN, "a particle left the block directory");
@@ -398,6 +405,11 @@ int32_t regrow(mpm_ctx *c) {
   c->binned = false;
   c->partition_valid = false;
   c->regrows += 1;
+  if (c->bnd_n > 0) {  // the boundary grid on the new directory
+    dfree(c, d.bnd_map);
+    d.bnd_map = nullptr;
+    if ((rc = build_grid_boundary(c))) return rc;
+  }
   return MPM_OK;
 }
 
@@ -786,6 +798,163 @@ int32_t mpm_clear_colliders(mpm_ctx *c) {
   c->collider_allocs.clear();
   if (!c->colliders.empty()) drop_graphs(c);
   c->colliders.clear();
+  return MPM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Builds the boundary grid from the context's boundary points (a sync: the
+// number of boundary blocks sizes it).
+int32_t build_grid_boundary(mpm_ctx *c) {
+  DevPtrs &d = c->d;
+  const int64_t n = c->bnd_n;
+  float *pts = nullptr;
+  int32_t *cnt = nullptr;
+  double *acc = nullptr;
+  int32_t rc = MPM_OK, nb = 0;
+  auto done = [&](int32_t r) {
+    cudaStreamSynchronize(c->stream);
+    dfree(c, pts);
+    dfree(c, cnt);
+    dfree(c, acc);
+    return r;
+  };
+  ZS_CUDA(cudaStreamSynchronize(c->stream));  // no kernel still reads the old grid
+  dfree(c, d.bnd_grid);
+  d.bnd_grid = nullptr;
+  if (!d.bnd_map && (rc = dalloc(c, &d.bnd_map, (size_t)d.ndir))) return rc;
+  ZS_CUDA(cudaMemsetAsync(d.bnd_map, 0xff, (size_t)d.ndir * sizeof(int32_t), c->stream));  // -1
+  if ((rc = dalloc(c, &pts, (size_t)n * 10)) || (rc = dalloc(c, &cnt, 1))) return done(rc);
+  ZS_CUDA(cudaMemcpyAsync(pts, c->bnd_pts.data(), (size_t)n * 10 * sizeof(float),
+                          cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t), c->stream));
+  const SceneParams &S = c->scenes[0];
+  float *x = pts, *v = pts + 3 * n, *m = pts + 6 * n, *nrm = pts + 7 * n;
+  launch_bnd_mark(d, S, x, n, c->stream);
+  launch_bnd_index(d, cnt, c->stream);
+  ZS_CUDA(cudaMemcpyAsync(&nb, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  if ((rc = dalloc(c, &d.bnd_grid, (size_t)std::max(nb, 1) * 128)) ||
+      (rc = dalloc(c, &acc, (size_t)std::max(nb, 1) * 64 * 7)))
+    return done(rc);
+  ZS_CUDA(cudaMemsetAsync(acc, 0, (size_t)std::max(nb, 1) * 64 * 7 * sizeof(double), c->stream));
+  launch_bnd_accumulate(d, S, x, v, m, nrm, c->bnd_n_verts, n, acc, c->stream);
+  launch_bnd_finalize(d, acc, nb, c->stream);
+  if ((rc = launch_check("boundary grid"))) return done(rc);
+  return done(MPM_OK);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mpm_set_grid_boundary(mpm_ctx *c, int32_t type, int64_t n_verts, int64_t n_eles,
+                              const float *x, const float *v, const float *m, const float *nrm) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "a boundary grid needs a one-scene context");
+  if (type != MPM_BC_STICKY && type != MPM_BC_SLIP && type != MPM_BC_SEPARATE)
+    return fail(MPM_ERR_INVALID, "boundary grid type must be sticky, slip or separate");
+  const int64_t n = n_verts + n_eles;
+  if (n_verts < 0 || n_eles < 0 || n == 0 || !x || !m || (n_eles > 0 && !nrm))
+    return fail(MPM_ERR_INVALID, "invalid boundary points");
+  if ((rc = settle(c))) return rc;
+  std::vector<float> pts((size_t)n * 10, 0.0f);
+  for (int64_t p = 0; p < n; ++p) {
+    for (int a = 0; a < 3; ++a) {
+      pts[3 * p + a] = x[3 * p + a];
+      pts[3 * n + 3 * p + a] = v ? v[3 * p + a] : 0.0f;
+      pts[7 * n + 3 * p + a] = (p >= n_verts) ? nrm[3 * p + a] : 0.0f;
+    }
+    pts[6 * n + p] = m[p];
+  }
+  c->bnd_pts.swap(pts);
+  c->bnd_n = n;
+  c->bnd_n_verts = n_verts;
+  if (!c->d.bnd_map) drop_graphs(c);  // the graphs gain the boundary pass
+  c->d.bnd_type = type;
+  if ((rc = build_grid_boundary(c))) return rc;
+  drop_graphs(c);  // the new grid's address
+  return MPM_OK;
+}
+
+int32_t mpm_clear_grid_boundary(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = settle(c))) return rc;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  dfree(c, c->d.bnd_map);
+  dfree(c, c->d.bnd_grid);
+  if (c->d.bnd_map) drop_graphs(c);
+  c->d.bnd_map = nullptr;
+  c->d.bnd_grid = nullptr;
+  c->bnd_pts.clear();
+  c->bnd_n = c->bnd_n_verts = 0;
+  return MPM_OK;
+}
+
+int32_t mpm_apply_grid_boundary(mpm_ctx *c) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!c->d.bnd_map) return fail(MPM_ERR_STATE, "no boundary grid (mpm_set_grid_boundary)");
+  if (!c->partition_valid) return fail(MPM_ERR_STATE, "call mpm_partition first");
+  launch_apply_grid_boundary(c->d, c->stream);
+  return launch_check("apply grid boundary");
+}
+
+int32_t mpm_boundary_points_from_mesh(int64_t n_verts, const float *pos, const float *vel,
+                                      int64_t n_tris, const int32_t *tris, float dx, float *x,
+                                      float *v, float *m, float *nrm) {
+  if (n_verts < 0 || n_tris < 0 || !pos || (n_tris > 0 && !tris) || !(dx > 0.0f) || !x || !v ||
+      !m || !nrm)
+    return fail(MPM_ERR_INVALID, "invalid mesh");
+  for (int64_t t = 0; t < 3 * n_tris; ++t)
+    if (tris[t] < 0 || tris[t] >= n_verts) return fail(MPM_ERR_INVALID, "triangle index out of range");
+  auto unit = [](float *a) {
+    const float l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (l > 0.0f)
+      for (int k = 0; k < 3; ++k) a[k] /= l;
+  };
+  for (int64_t i = 0; i < n_verts; ++i) {
+    for (int k = 0; k < 3; ++k) {
+      x[3 * i + k] = pos[3 * i + k];
+      v[3 * i + k] = vel ? vel[3 * i + k] : 0.0f;
+      nrm[3 * i + k] = 0.0f;
+    }
+    m[i] = 0.0f;
+  }
+  for (int64_t t = 0; t < n_tris; ++t) {
+    const int32_t *tr = tris + 3 * t;
+    const float *p0 = pos + 3 * tr[0], *p1 = pos + 3 * tr[1], *p2 = pos + 3 * tr[2];
+    float a[3], b[3], e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+      e1[k] = p1[k] - p0[k];
+      e2[k] = p2[k] - p0[k];
+      a[k] = e1[k] / dx;
+      b[k] = e2[k] / dx;
+    }
+    const float cr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const float area = 0.5f * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    unit(e1);
+    unit(e2);
+    float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                  e1[0] * e2[1] - e1[1] * e2[0]};
+    unit(n);
+    const int64_t r = n_verts + t;
+    m[r] = area;
+    for (int k = 0; k < 3; ++k) {
+      x[3 * r + k] = (p0[k] + p1[k] + p2[k]) / 3.0f;
+      v[3 * r + k] = vel ? (vel[3 * tr[0] + k] + vel[3 * tr[1] + k] + vel[3 * tr[2] + k]) / 3.0f : 0.0f;
+      nrm[3 * r + k] = n[k];
+    }
+    for (int j = 0; j < 3; ++j) {
+      m[tr[j]] += area / 3.0f;
+      for (int k = 0; k < 3; ++k) nrm[3 * tr[j] + k] += n[k];
+    }
+  }
+  for (int64_t i = 0; i < n_verts; ++i) unit(nrm + 3 * i);
   return MPM_OK;
 }
 
@@ -1786,6 +1955,7 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
   if (!c->d.differentiable) return fail(MPM_ERR_STATE, "the adjoint needs mpm_set_differentiable(ctx, 1)");
+  if (c->d.bnd_map) return fail(MPM_ERR_INVALID, "the adjoint takes no boundary grid");
   if (!adj_next || !adj_prev || !grad_mu || !grad_lam)
     return fail(MPM_ERR_INVALID, "null adjoint buffer");
   if (!c->differentiable)
@@ -2063,6 +2233,7 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
   for (const ColliderDev &cd : c->colliders)
     if (cd.db[0] != 0.0f || cd.db[1] != 0.0f || cd.db[2] != 0.0f || cd.ds != 0.0f)
       return fail(MPM_ERR_INVALID, "the adjoint takes static colliders only");
+  if (c->d.bnd_map) return fail(MPM_ERR_INVALID, "the adjoint takes no boundary grid");
   const long long n = c->prm.n;
   const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));
   float *a = adj, *b = adj_tmp;  // adjoint of the next state, of this one

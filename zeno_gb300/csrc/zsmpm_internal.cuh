@@ -272,6 +272,11 @@ struct DevPtrs {
   int hencky;  // some material uses the von Mises / Cam-Clay return mapping
   int grid_p2g_flip, grid_g2p_flip;  // persistent grids of the FLIP transfer kernels
   int grid_persist;  // CTAs of the persistent substep kernel (0: it cannot run)
+  // boundary grid (mpm_set_grid_boundary; null: none): per directory entry
+  // its boundary block or -1, per boundary node (m, v) then (nrm, 0)
+  int32_t *bnd_map;
+  float4 *bnd_grid;
+  int bnd_type;  // MPM_BC_STICKY / SLIP / SEPARATE
   LaunchConfig launch;
 };
 
@@ -351,6 +356,22 @@ void launch_return_mapping(const DevPtrs &d, int cur, cudaStream_t s);
 // vol * Kirchhoff stress of every particle from its current F (or J)
 // slots [b0, b1) (b1 < 0: every particle)
 void launch_stress(const DevPtrs &d, int cur, cudaStream_t s, long long b0 = 0, long long b1 = -1);
+
+// boundary_grid.cu: the boundary grid of one-scene context from boundary
+// points (x, v, m, nrm device arrays, the vertex rows first): mark the
+// directory entries whose blocks the points' linear stencils touch (bnd_map
+// -1 everywhere before), number them (count in *n_blocks), then, with
+// accumulators of 7 doubles per node zeroed, add the points and normalise
+// into d.bnd_grid.
+void launch_bnd_mark(const DevPtrs &d, const SceneParams &S, const float *x, long long n,
+                     cudaStream_t s);
+void launch_bnd_index(const DevPtrs &d, int32_t *n_blocks, cudaStream_t s);
+void launch_bnd_accumulate(const DevPtrs &d, const SceneParams &S, const float *x, const float *v,
+                           const float *m, const float *nrm, long long n_verts, long long n,
+                           double *acc, cudaStream_t s);
+void launch_bnd_finalize(const DevPtrs &d, const double *acc, int n_blocks, cudaStream_t s);
+// ApplyGridBoundaryOnZSGrid on the active grid nodes
+void launch_apply_grid_boundary(const DevPtrs &d, cudaStream_t s);
 
 // api.cu: the text mpm_last_error() returns on this thread
 void set_last_error(const std::string &msg);

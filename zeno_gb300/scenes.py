@@ -169,6 +169,37 @@ def cloth_sheet(center, size: float, n: int, jitter: float = 0.0, seed: int = 0,
 
 
 @dataclass
+class GridBoundary:
+    """Points of a boundary grid (ToBoundaryParticles rows: the mesh's
+    vertices, then one per triangle; x, v, nrm (n, 3) and m (n,), float32)
+    and the type ApplyGridBoundaryOnZSGrid applies (BC_STICKY / SLIP /
+    SEPARATE)."""
+    type: int
+    x: np.ndarray
+    v: np.ndarray
+    m: np.ndarray
+    nrm: np.ndarray
+    n_verts: int
+
+
+def ramp_mesh(center, size: float, n: int, slope_deg: float = 0.0):
+    """A square of size x size in the x-z plane, tilted by slope_deg about the
+    z axis, centred at `center`: (n + 1)^2 vertices, 2 n^2 triangles whose
+    normals point up."""
+    u = np.linspace(-0.5 * size, 0.5 * size, n + 1)
+    gx, gz = np.meshgrid(u, u, indexing="ij")
+    t = np.radians(slope_deg)
+    x = np.stack([gx.ravel() * np.cos(t), gx.ravel() * np.sin(t), gz.ravel()], 1)
+    x = x + np.asarray(center, np.float64)
+    tris = []
+    for i in range(n):
+        for j in range(n):
+            a, b, c, d = i * (n + 1) + j, (i + 1) * (n + 1) + j, i * (n + 1) + j + 1, (i + 1) * (n + 1) + j + 1
+            tris += [(a, d, b), (a, c, d)]
+    return x.astype(np.float32), np.array(tris, np.int32)
+
+
+@dataclass
 class Scene:
     """Grid, boundary and material description of one MPM scene."""
     dx: float
@@ -183,6 +214,7 @@ class Scene:
     dt: float = 1e-4
     colliders: list = field(default_factory=list)
     transfer: int = TRANSFER_APIC
+    grid_boundary: "GridBoundary | None" = None
 
     @staticmethod
     def unit_box(dx: float, **kw) -> "Scene":

@@ -88,7 +88,8 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_get_launch_config", "mpm_set_differentiable", "mpm_state_save",
            "mpm_state_load", "mpm_adjoint_substep", "mpm_rollout_forward", "mpm_rollout_backward", "mpm_snapshot_floats", "mpm_add_collider", "mpm_clear_colliders",
            "mpm_step_colliders", "mpm_set_auto_regrow", "mpm_get_domain",
-           "mpm_set_persistent", "mpm_barrier_selftest"]
+           "mpm_set_persistent", "mpm_barrier_selftest", "mpm_set_grid_boundary",
+           "mpm_clear_grid_boundary", "mpm_apply_grid_boundary", "mpm_boundary_points_from_mesh"]
 
 STAGES = ["bin", "scan", "scatter", "sort", "p2g", "grid_update", "g2p"]
 # differentiable form (include/zsmpm.h): state planes x 3, v 3, C 9, F 9, J,
@@ -166,6 +167,10 @@ def load(path: str = LIB_PATH):
         "mpm_set_auto_regrow": ([P, i32], i32),
         "mpm_get_domain": ([P, P, P, P], i32),
         "mpm_set_persistent": ([P, i32, C.c_uint64], i32),
+        "mpm_set_grid_boundary": ([P, i32, C.c_int64, C.c_int64, P, P, P, P], i32),
+        "mpm_clear_grid_boundary": ([P], i32),
+        "mpm_apply_grid_boundary": ([P], i32),
+        "mpm_boundary_points_from_mesh": ([C.c_int64, P, P, C.c_int64, P, f32, P, P, P, P], i32),
         "mpm_barrier_selftest": ([P, C.c_uint64, P], i32),
         "mpm_state_save": ([P, P], i32),
         "mpm_state_load": ([P, P], i32),
@@ -198,6 +203,33 @@ class ClothDesc(C.Structure):
                 ("kind", C.c_int32)]
 
 
+def boundary_points_from_mesh(pos, tris, dx: float, vel=None) -> dict:
+    """ToBoundaryParticles (host code of the library, no GPU): rows of the
+    mesh's vertices, then one per triangle: x, v, m, nrm (float32)."""
+    L = load()
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+    tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    nv, nt = pos.shape[0], tris.shape[0]
+    if vel is not None:
+        vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+    out = {k: np.zeros((nv + nt, 3) if k != "m" else nv + nt, np.float32)
+           for k in ("x", "v", "m", "nrm")}
+    rc = L.mpm_boundary_points_from_mesh(nv, _p(pos), _p(vel) if vel is not None else None, nt,
+                                         _p(tris), float(dx), _p(out["x"]), _p(out["v"]),
+                                         _p(out["m"]), _p(out["nrm"]))
+    if rc != 0:
+        raise MPMError(rc, "mpm_boundary_points_from_mesh", L.mpm_last_error().decode())
+    return out
+
+
+def mesh_grid_boundary(pos, tris, dx: float, type: int, vel=None):
+    """A scenes.GridBoundary of a triangle mesh (ToBoundaryParticles)."""
+    from .scenes import GridBoundary
+    o = boundary_points_from_mesh(pos, tris, dx, vel)
+    return GridBoundary(type=int(type), x=o["x"], v=o["v"], m=o["m"], nrm=o["nrm"],
+                        n_verts=int(np.asarray(pos).reshape(-1, 3).shape[0]))
+
+
 class Context:
     """One MPM scene on one GPU (ZSGrid + ZSPartition + ZSParticles)."""
 
@@ -219,6 +251,8 @@ class Context:
             self.add_collider(c)
         if getattr(scene, "transfer", 0):
             self.set_transfer(scene.transfer)
+        if getattr(scene, "grid_boundary", None) is not None:
+            self.set_grid_boundary(scene.grid_boundary)
 
     def set_transfer(self, scheme: int):
         """MakeZSGrid "transfer": scenes.TRANSFER_APIC / FLIP / AFLIP."""
@@ -337,6 +371,21 @@ class Context:
 
     def clear_colliders(self):
         self._check(self._L.mpm_clear_colliders(self.h), "mpm_clear_colliders")
+
+    def set_grid_boundary(self, gb):
+        """mpm_set_grid_boundary for a scenes.GridBoundary."""
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+        x, v, m, nrm = f(gb.x), f(gb.v), f(gb.m), f(gb.nrm)
+        n = m.shape[0]
+        self._check(self._L.mpm_set_grid_boundary(self.h, int(gb.type), int(gb.n_verts),
+                                                  int(n - gb.n_verts), _p(x), _p(v), _p(m),
+                                                  _p(nrm)), "mpm_set_grid_boundary")
+
+    def clear_grid_boundary(self):
+        self._check(self._L.mpm_clear_grid_boundary(self.h), "mpm_clear_grid_boundary")
+
+    def apply_grid_boundary(self):
+        self._check(self._L.mpm_apply_grid_boundary(self.h), "mpm_apply_grid_boundary")
 
     def step_colliders(self, dt: float, collider: int = -1):
         """StepZSBoundary: b += db/dt dt, s += ds/dt dt (stage path), for one
