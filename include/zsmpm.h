@@ -351,7 +351,10 @@ int32_t mpm_set_transfer(mpm_ctx *ctx, int32_t scheme);
 /* ComputeParticleBeta (Boundary.cu:172-516) on the current particles: with
  * collider = -1 beta = 0.5 where det F > 1 (J for the equation-of-state
  * fluid), else 0; with a collider id, first beta = 0 for particles that at
- * x + dt v are inside that collider and move into it. */
+ * x + dt v are inside that collider and move into it; with -2, first beta = 0
+ * for particles whose linear stencil at x + dt v has a boundary-grid node
+ * (mpm_set_grid_boundary) of non-zero mass with (v - v_b) . nrm_b < 0
+ * (Boundary.cu:172-222; particles only, not a cloth). */
 int32_t mpm_compute_particle_beta(mpm_ctx *ctx, float dt, int32_t collider);
 
 /* Stage entry points (one reference node each). */

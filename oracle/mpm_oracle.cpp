@@ -1581,10 +1581,33 @@ int32_t orc_von_mises_f64(const orc_scene *scene, int64_t n, const double *F, co
 int32_t orc_particle_beta_f64(const orc_scene *scene, int64_t n, const double *x, const double *v,
                               const double *F, const double *J, const int32_t *mat, double dt,
                               int32_t collider, double *beta) {
-  if (!scene || n < 0 || !beta || collider >= scene->n_colliders) return ORC_ERR_INVALID;
+  if (!scene || n < 0 || !beta || collider >= scene->n_colliders || collider < -2 ||
+      (collider == -2 && !scene->grid_boundary))
+    return ORC_ERR_INVALID;
   Sim<double> sim(*scene, 1);
   for (int64_t p = 0; p < n; ++p) {
     if (mat[p] < 0 || mat[p] >= scene->n_materials) return ORC_ERR_INVALID;
+    if (collider == -2) {
+      // the boundary grid (Boundary.cu:172-222): at x + dt v, a node of the
+      // linear stencil with boundary mass where (v - v_b) . nrm_b < 0
+      const float inv_dx = 1.0f / scene->dx;
+      int32_t base[3];
+      for (int a = 0; a < 3; ++a)
+        base[a] = int32_t(std::floor(float(x[3 * p + a] + dt * v[3 * p + a]) * inv_dx));
+      bool in = false;
+      for (int o = 0; o < 8 && !in; ++o) {
+        const int32_t I[3] = {base[0] + (o >> 2), base[1] + ((o >> 1) & 1), base[2] + (o & 1)};
+        const auto it = sim.bgrid.find(sim.node_key(I));
+        if (it == sim.bgrid.end() || it->second.m == 0) continue;
+        const auto &b = it->second;
+        in = (v[3 * p] - b.v[0]) * b.n[0] + (v[3 * p + 1] - b.v[1]) * b.n[1] +
+                 (v[3 * p + 2] - b.v[2]) * b.n[2] < 0;
+      }
+      if (in) {
+        beta[p] = 0;
+        continue;
+      }
+    }
     if (collider >= 0) {
       double pos[3], nrm[3], vo[3];
       for (int a = 0; a < 3; ++a) pos[a] = x[3 * p + a] + dt * v[3 * p + a];

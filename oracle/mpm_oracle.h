@@ -202,7 +202,9 @@ int32_t orc_run_f32(const orc_scene *scene, int64_t n, float *x, float *v,
  * collider < 0 the criterion of the node without a boundary (beta = 0.5 where
  * det F > 1, else 0; J for the equation-of-state fluid); with the index of
  * one of the scene's colliders, first the level-set test at x + dt v
- * (beta = 0 where the particle moves into the collider). */
+ * (beta = 0 where the particle moves into the collider); with -2, first the
+ * test against the scene's boundary grid: beta = 0 where a node of the
+ * linear stencil at x + dt v has boundary mass and (v - v_b) . nrm_b < 0. */
 /* ComputeVonMises (Generation.cu:1873-1920) in double: for the StVK-Hencky
  * particles vms = sqrt(sum_d (c_d - c_{d+1})^2 / 2) of the principal Cauchy
  * stresses c_i = (2 mu e_i + lam sum e) / J, e_i = ln s_i (s the singular

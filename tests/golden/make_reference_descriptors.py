@@ -27,7 +27,8 @@ NODES = ["ConfigConstitutiveModel", "ToZSParticles", "MakeZSPartition", "MakeZSG
          "ConstructBendingSprings", "RetrievePrimitiveFromZSParticles",
          "ExtractPrimitiveFromZSParticles", "UpdatePrimitiveAttributesFromZSParticles",
          "UpdatePrimitiveAttrFromZSParticles",
-         "ToTrackerParticles"]
+         "ToTrackerParticles", "ToBoundaryParticles", "ZSBoundaryPrimitiveToZSGrid",
+         "ApplyGridBoundaryOnZSGrid"]
 
 
 def parse_braces(s, i):

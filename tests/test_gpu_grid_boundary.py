@@ -111,9 +111,9 @@ def test_boundary_grid_follows_a_growing_directory(zsmpm_mod, oracle_mod):
     built again on it, and the run equals the oracle's on the full box."""
     scene, parts = _ramp_scene(zsmpm_mod, S.BC_SLIP)
     base = np.floor(parts.x.astype(np.float64) / scene.dx - 0.5).astype(int) // 4
-    lo = base.min(axis=0) - 2
+    lo = base.min(axis=0) - 1  # the particles' blocks and the one ring the binning needs
     tight = dataclasses.replace(scene, block_lo=tuple(int(a) for a in lo),
-                                block_dims=tuple(int(a) for a in base.max(axis=0) - lo + 3))
+                                block_dims=tuple(int(a) for a in base.max(axis=0) - lo + 2))
     steps = 250
     out, dom = _gpu(zsmpm_mod, tight, parts, steps, regrow=True)
     assert dom[2] >= 1

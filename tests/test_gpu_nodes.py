@@ -1,5 +1,7 @@
 """A zeno graph of the MPM nodes, run headless on the GPU through the C++
 node layer, against the oracle and against the fused ZSMPMSubstep node."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -144,3 +146,25 @@ def test_node_graph_sand_friction_angle_from_params(zsmpm_mod, oracle_mod):
     assert rel_l2(x, ref.x) < 1e-4 and rel_l2(v, ref.v) < 1e-4
     ref35, _ = oracle_mod.run(*sand(35.0), steps, "f64")
     assert rel_l2(v, ref35.v) > 1e-2
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_node_graph_boundary_grid_matches_oracle(zsmpm_mod, oracle_mod, fused):
+    """ToBoundaryParticles -> MakeZSGrid "boundary" -> ZSPartitionForZSParticles
+    -> ZSGridFromZSPartition -> ZSBoundaryPrimitiveToZSGrid -> UpdateZSGrid,
+    applied by ApplyGridBoundaryOnZSGrid (slip) after the walls every substep
+    (fused: ZSMPMSubstep's BoundaryZSGrid), against the oracle."""
+    scene, parts = S.jelly_cube(cells=8)
+    parts.v[:] = np.array([0.3, -3.0, 0.0], np.float32)
+    pos, tris = S.ramp_mesh((0.42, 0.30, 0.42), 0.5, 20, slope_deg=15.0)
+    steps = 150
+    x, v, _ = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", E=5e4, nu=0.3,
+                                       substeps=steps, bc="sticky", thickness=3, fused=fused,
+                                       boundary_mesh=(pos, tris, None, "slip"))
+    scene.grid_boundary = zsmpm_mod.mesh_grid_boundary(pos, tris, scene.dx, S.BC_SLIP)
+    ref, st = oracle_mod.run(scene, parts, steps, "f64")
+    assert st["status"] == 0
+    assert rel_l2(x, ref.x) < 1e-4 and rel_l2(v, ref.v) < 1e-4
+    free = dataclasses.replace(scene, grid_boundary=None)
+    nob, _ = oracle_mod.run(free, parts, steps, "f64")
+    assert rel_l2(ref.v, nob.v) > 1e-2  # the boundary acted

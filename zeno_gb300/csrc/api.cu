@@ -1653,8 +1653,12 @@ int32_t mpm_compute_particle_beta(mpm_ctx *c, float dt, int32_t collider) {
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
-  if (collider < -1 || collider >= (int32_t)c->colliders.size())
+  if (collider < -2 || collider >= (int32_t)c->colliders.size())
     return fail(MPM_ERR_INVALID, "collider id out of range");
+  if (collider == -2 && !c->d.bnd_map)
+    return fail(MPM_ERR_STATE, "no boundary grid (mpm_set_grid_boundary)");
+  if (collider == -2 && c->d.cloth.n_verts > 0)
+    return fail(MPM_ERR_INVALID, "the boundary-grid beta of a cloth is not implemented");
   if ((rc = push_params(c))) return rc;
   if (c->prm.n > 0) launch_particle_beta(c->d, c->cur, dt, collider, c->stream);
   // a triangle cloth's vertices (curves keep beta 0, as in the reference)

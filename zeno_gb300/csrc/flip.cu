@@ -853,7 +853,8 @@ __global__ void __launch_bounds__(kFG2PThreads, 4)
 }
 
 // ComputeParticleBeta (Boundary.cu:172-516) on the current store: the
-// level-set form (determine_beta_sdf, :285-315) first -- at x + dt v, a
+// boundary-grid form (collider -2, :172-222) or the level-set form
+// (determine_beta_sdf, :285-315) first -- at x + dt v, a
 // particle inside the collider moving into it, (v - v_obj) . n < 0, gets
 // beta 0 -- then the volume criterion beta = 0.5 where J > Jp_critical = 1
 // (J = det F, or the fluid's J), else 0.  beta is stored by upload index.
@@ -870,6 +871,37 @@ __global__ void k_particle_beta(DevPtrs d, const float *__restrict__ pb,
     for (int a = 0; a < 3; ++a) {
       v[a] = pb[pidx((CH_V + a), p)];
       x[a] = pb[pidx((CH_X + a), p)] + dt * v[a];
+    }
+    if (collider == -2) {
+      // the boundary grid (Boundary.cu:172-222): a node of the linear
+      // stencil at x + dt v with boundary mass where (v - v_b) . nrm_b < 0
+      const SceneParams &S = d.scn[0];
+      int base[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) base[a] = __float2int_rd(__fmul_rn(x[a], S.inv_dx));
+      bool in = false;
+      for (int o = 0; o < 8 && !in; ++o) {
+        const int I[3] = {base[0] + (o >> 2), base[1] + ((o >> 1) & 1), base[2] + (o & 1)};
+        int c[3];
+        bool inside = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          c[a] = (I[a] >> 2) - S.block_lo[a];
+          inside = inside && c[a] >= 0 && c[a] < S.block_dims[a];
+        }
+        if (!inside) continue;
+        const int bb = d.bnd_map[S.dir_off + ((long long)c[0] * S.block_dims[1] + c[1]) * S.block_dims[2] + c[2]];
+        if (bb < 0) continue;
+        const int cell = ((I[0] & 3) << 4) | ((I[1] & 3) << 2) | (I[2] & 3);
+        const float4 bmv = d.bnd_grid[2 * ((long long)bb * 64 + cell)];
+        if (bmv.x == 0.0f) continue;
+        const float4 bn = d.bnd_grid[2 * ((long long)bb * 64 + cell) + 1];
+        in = (v[0] - bmv.y) * bn.x + (v[1] - bmv.z) * bn.y + (v[2] - bmv.w) * bn.z < 0.0f;
+      }
+      if (in) {
+        d.beta[id] = 0.0f;
+        continue;
+      }
     }
     if (collider >= 0) {
       float nrm[3], vo[3];

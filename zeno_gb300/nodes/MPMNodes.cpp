@@ -103,6 +103,10 @@ void check(int32_t rc, const char *what) {
 struct MpmContext {
   mpm_ctx *h = nullptr;
   float dx = 0.0f;
+  // the boundary points (a ToBoundaryParticles object) and type of the
+  // boundary grid set in this context
+  const void *bnd_src = nullptr;
+  int32_t bnd_type = 0;
   ~MpmContext() {
     if (h) mpm_ctx_destroy(h);
   }
@@ -149,12 +153,19 @@ struct ZenoParticles : IObject {
   std::shared_ptr<ZenoConstitutiveModel> model;
   int64_t n = 0;
   int category = 0;
+  // ToBoundaryParticles: points of a boundary mesh (the vertices, then one
+  // per triangle) for a boundary grid, kept on the host
+  bool boundary = false;
+  float bdx = 0.0f;
+  int64_t b_verts = 0, b_n = 0;
+  std::vector<float> bx, bv, bm, bnrm;
 };
 
 // MakeZSPartition output (Structures.hpp:533-586)
 struct ZenoPartition : IObject {
   std::shared_ptr<MpmContext> ctx;
   bool rebuilt = false;
+  std::shared_ptr<ZenoParticles> bnd;  // the partition of boundary points
 };
 
 // MakeZSGrid output (Structures.hpp:588-623)
@@ -163,6 +174,7 @@ struct ZenoGrid : IObject {
   std::string transferScheme = "apic";
   std::shared_ptr<MpmContext> ctx;
   std::shared_ptr<ZenoPartition> partition;
+  std::shared_ptr<ZenoParticles> bnd;  // transfer "boundary": the points it holds
 };
 
 // MakeZSLevelSet output (Structures.hpp: ZenoLevelSet): here a dense grid of
@@ -662,10 +674,7 @@ struct MakeZSGrid : INode {
     grid->dx = get_input2<float>("dx");
     grid->transferScheme = get_input2<std::string>("transfer");
     const std::string &ts = grid->transferScheme;
-    if (ts == "boundary")
-      throw std::runtime_error("boundary grids (transfer [boundary]) are not implemented by this "
-                               "backend");
-    if (ts != "apic" && ts != "flip" && ts != "aflip")
+    if (ts != "apic" && ts != "flip" && ts != "aflip" && ts != "boundary")
       throw std::runtime_error("unrecognized transfer scheme [" + ts + "]");
     set_output("ZSGrid", grid);
   }
@@ -685,6 +694,15 @@ struct ZSPartitionForZSParticles : INode {
     auto table = get_input<ZenoPartition>("ZSPartition");
     auto grid = get_input<ZenoGrid>("ZSGrid");
     auto pars = get_input<ZenoParticles>("ZSParticles");
+    if (pars->boundary) {  // boundary points: their grid is built where it is applied
+      if (grid->transferScheme != "boundary")
+        throw std::runtime_error("boundary particles partition a grid of transfer [boundary]");
+      table->bnd = pars;
+      grid->bnd = pars;
+      table->rebuilt = true;
+      set_output("ZSPartition", table);
+      return;
+    }
     ensure_cloth_ctx(*pars);
     const std::string strategy = get_param<std::string>("strategy");
     if (strategy != "force" && strategy != "cache")
@@ -736,6 +754,11 @@ struct ZSGridFromZSPartition : INode {
   void apply() override {
     auto table = get_input<ZenoPartition>("ZSPartition");
     auto grid = get_input<ZenoGrid>("ZSGrid");
+    if (grid->transferScheme == "boundary") {  // cleared when its points are scattered
+      grid->partition = table;
+      set_output("ZSGrid", grid);
+      return;
+    }
     auto ctx = bound_ctx(table, "ZSGridFromZSPartition");
     grid->ctx = ctx;
     grid->partition = table;
@@ -774,6 +797,13 @@ struct UpdateZSGrid : INode {
   void apply() override {
     auto table = get_input<ZenoPartition>("ZSPartition");
     auto grid = get_input<ZenoGrid>("ZSGrid");
+    if (grid->transferScheme == "boundary") {
+      // v = mv / m and nrm = unit(nrm / m) (MPMPipeline.cu:899-911) are part
+      // of building the boundary grid in the context that applies it
+      set_output("ZSGrid", grid);
+      set_output("MaxVelSqr", std::make_shared<NumericObject>(0.0f));
+      return;
+    }
     auto ctx = bound_ctx(table, "UpdateZSGrid");
     float acc[3] = {0.0f, get_input2<float>("gravity"), 0.0f};
     if (has_input("Accel")) {
@@ -988,6 +1018,120 @@ ZENDEFNODE(ApplyBoundaryOnZSGrid, {
                                       {"MPM"},
                                   });
 
+/// ToBoundaryParticles (Generation.cpp:1154-1482): a triangle mesh to
+/// boundary points -- its vertices (mass a third of their triangles' area in
+/// dx^2, the primitive's "vel" or zero) and one point per triangle (its area,
+/// centroid, mean velocity and unit normal).  Sprayed points (prim_tris) are
+/// not supported.
+struct ToBoundaryParticles : INode {
+  void apply() override {
+    auto prim = get_input<PrimitiveObject>("prim");
+    if (has_input("prim_tris"))
+      throw std::runtime_error("ToBoundaryParticles: sprayed particles (prim_tris) are not "
+                               "implemented by this backend");
+    const auto &pos = prim_access::pos(*prim);
+    const auto &tris = prim_access::tris(*prim);
+    if (tris.empty()) throw std::runtime_error("boundary primitive is not a surface mesh!");
+    const float dx = get_input2<float>("dx");
+    auto out = std::make_shared<ZenoParticles>();
+    out->prim = prim;
+    out->boundary = true;
+    out->bdx = dx;
+    const int64_t nv = (int64_t)pos.size(), nt = (int64_t)tris.size();
+    std::vector<float> p(3 * nv), vel;
+    std::vector<int32_t> t(3 * nt);
+    for (int64_t i = 0; i < nv; ++i)
+      for (int d = 0; d < 3; ++d) p[3 * i + d] = pos[i][d];
+    for (int64_t i = 0; i < nt; ++i)
+      for (int d = 0; d < 3; ++d) t[3 * i + d] = tris[i][d];
+    if (auto *v = prim_access::vel(*prim, false); v && (int64_t)v->size() == nv) {
+      vel.resize(3 * nv);
+      for (int64_t i = 0; i < nv; ++i)
+        for (int d = 0; d < 3; ++d) vel[3 * i + d] = (*v)[i][d];
+    }
+    out->b_verts = nv;
+    out->b_n = nv + nt;
+    out->bx.resize(3 * out->b_n);
+    out->bv.resize(3 * out->b_n);
+    out->bnrm.resize(3 * out->b_n);
+    out->bm.resize(out->b_n);
+    check(mpm_boundary_points_from_mesh(nv, p.data(), vel.empty() ? nullptr : vel.data(), nt,
+                                        t.data(), dx, out->bx.data(), out->bv.data(),
+                                        out->bm.data(), out->bnrm.data()),
+          "mpm_boundary_points_from_mesh");
+    set_output("ZSParticles", out);
+  }
+};
+ZENDEFNODE(ToBoundaryParticles, {
+                                    {"prim", "prim_tris", {"float", "dx", "0.1"}},
+                                    {"ZSParticles"},
+                                    {},
+                                    {"MPM"},
+                                });
+
+/// ZSBoundaryPrimitiveToZSGrid (Transfer.cu:1532-1623): the boundary points
+/// into a grid of transfer "boundary" (scattered, with the linear kernel, in
+/// the context of the particles the grid is applied to)
+struct ZSBoundaryPrimitiveToZSGrid : INode {
+  void apply() override {
+    auto pars = get_input<ZenoParticles>("ZSParticles");
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    (void)get_input<ZenoPartition>("ZSPartition");
+    if (grid->transferScheme != "boundary") throw std::runtime_error("grid is not of boundary type!");
+    if (!pars->boundary)
+      throw std::runtime_error("boundary primitive does not have normal channel!");
+    grid->bnd = pars;
+    set_output("ZSGrid", grid);
+  }
+};
+ZENDEFNODE(ZSBoundaryPrimitiveToZSGrid, {
+                                            {"ZSParticles", "ZSPartition", "ZSGrid"},
+                                            {"ZSGrid"},
+                                            {},
+                                            {"MPM"},
+                                        });
+
+/// ApplyGridBoundaryOnZSGrid (Boundary.cu:18-69): the boundary grid's
+/// velocity on every node of the grid whose mass, and whose boundary node's
+/// mass, is non-zero -- sticky, slip or separate along the boundary normal.
+/// The boundary grid is built in the particles' context the first time (and
+/// again when its points or the type change).
+struct ApplyGridBoundaryOnZSGrid : INode {
+  void apply() override {
+    auto grid = get_input<ZenoGrid>("ZSGrid");
+    auto table = get_input<ZenoPartition>("ZSPartition");
+    auto bg = get_input<ZenoGrid>("BoundaryZSGrid");
+    (void)get_input<ZenoPartition>("BoundaryZSPartition");
+    if (bg->transferScheme != "boundary")
+      throw std::runtime_error("boundary grid is not of boundary type!");
+    if (!bg->bnd)
+      throw std::runtime_error("ApplyGridBoundaryOnZSGrid: the boundary grid holds no points "
+                               "(run ZSBoundaryPrimitiveToZSGrid first)");
+    auto ctx = bound_ctx(table, "ApplyGridBoundaryOnZSGrid");
+    const std::string ts = get_param<std::string>("type");
+    const int32_t type = ts == "sticky" ? MPM_BC_STICKY : (ts == "slip" ? MPM_BC_SLIP : MPM_BC_SEPARATE);
+    const ZenoParticles &b = *bg->bnd;
+    if (std::fabs(b.bdx - ctx->dx) > 1e-6f * ctx->dx)
+      throw std::runtime_error("the boundary particles' dx differs from the grid's");
+    if (ctx->bnd_src != (const void *)&b || ctx->bnd_type != type) {
+      check(mpm_set_grid_boundary(ctx->h, type, b.b_verts, b.b_n - b.b_verts, b.bx.data(),
+                                  b.bv.data(), b.bm.data(), b.bnrm.data()),
+            "mpm_set_grid_boundary");
+      ctx->bnd_src = &b;
+      ctx->bnd_type = type;
+    }
+    check(mpm_apply_grid_boundary(ctx->h), "mpm_apply_grid_boundary");
+    set_output("ZSGrid", grid);
+  }
+};
+ZENDEFNODE(ApplyGridBoundaryOnZSGrid, {
+                                          {"ZSPartition", "ZSGrid", "BoundaryZSPartition",
+                                           "BoundaryZSGrid"},
+                                          {"ZSGrid"},
+                                          {{"enum sticky slip separate", "type", "sticky"}},
+                                          {"MPM"},
+                                      });
+
 /// StepZSBoundary (Generation.cu:1662-1685): b += db/dt dt, s += ds/dt dt,
 /// on the boundary and, once attached, on its collider in the context
 struct StepZSBoundary : INode {
@@ -1071,15 +1215,28 @@ ZENDEFNODE(WriteZSParticles, {
 /// update.  With a level-set ZSBoundary, particles that at x + dt v are
 /// inside it and move into it get 0; otherwise 0.5 where det F > 1, else 0.
 /// A ZSBoundary of box walls (no level set) gives the volume criterion only;
-/// boundary grids (transfer "boundary") are not implemented.
+/// a boundary grid (transfer "boundary") the test against its nodes at
+/// x + dt v (Boundary.cu:172-222).
 struct ComputeParticleBeta : INode {
   void apply() override {
     auto pars = get_input<ZenoParticles>("ZSParticles");
     auto ctx = pars->ctx;
     int32_t collider = -1;
-    if (has_input<ZenoGrid>("ZSBoundary(Grid)"))
-      throw std::runtime_error("ComputeParticleBeta: boundary grids are not implemented; pass a "
-                               "level-set ZSBoundary");
+    if (has_input<ZenoGrid>("ZSBoundary(Grid)")) {  // a boundary grid
+      auto bg = get_input<ZenoGrid>("ZSBoundary(Grid)");
+      if (bg->transferScheme != "boundary" || !bg->bnd)
+        throw std::runtime_error("ComputeParticleBeta: the ZSGrid is not a filled boundary grid");
+      const ZenoParticles &b = *bg->bnd;
+      if (ctx->bnd_src != (const void *)&b) {  // built as ApplyGridBoundaryOnZSGrid would
+        const int32_t type = ctx->bnd_src ? ctx->bnd_type : MPM_BC_STICKY;
+        check(mpm_set_grid_boundary(ctx->h, type, b.b_verts, b.b_n - b.b_verts, b.bx.data(),
+                                    b.bv.data(), b.bm.data(), b.bnrm.data()),
+              "mpm_set_grid_boundary");
+        ctx->bnd_src = &b;
+        ctx->bnd_type = type;
+      }
+      collider = -2;
+    }
     if (has_input<ZenoBoundary>("ZSBoundary(Grid)")) {
       auto b = get_input<ZenoBoundary>("ZSBoundary(Grid)");
       if (b->ls) {
@@ -1470,6 +1627,22 @@ struct ZSMPMSubstep : INode {
     if (has_input<ZenoParticles>("ZSBending"))
       attach_bending(ctx, *get_input<ZenoParticles>("ZSBending"));
     // the transfer scheme of a MakeZSGrid (default APIC)
+    if (has_input<ZenoGrid>("BoundaryZSGrid")) {  // a boundary grid, every substep
+      auto bg = get_input<ZenoGrid>("BoundaryZSGrid");
+      if (bg->transferScheme != "boundary" || !bg->bnd)
+        throw std::runtime_error("ZSMPMSubstep: BoundaryZSGrid is not a filled boundary grid");
+      const std::string ts = get_input2<std::string>("boundary_type");
+      const int32_t type =
+          ts == "sticky" ? MPM_BC_STICKY : (ts == "slip" ? MPM_BC_SLIP : MPM_BC_SEPARATE);
+      const ZenoParticles &b = *bg->bnd;
+      if (ctx->bnd_src != (const void *)&b || ctx->bnd_type != type) {
+        check(mpm_set_grid_boundary(ctx->h, type, b.b_verts, b.b_n - b.b_verts, b.bx.data(),
+                                    b.bv.data(), b.bm.data(), b.bnrm.data()),
+              "mpm_set_grid_boundary");
+        ctx->bnd_src = &b;
+        ctx->bnd_type = type;
+      }
+    }
     if (has_input<ZenoGrid>("ZSGrid"))
       check(mpm_set_transfer(ctx->h, transfer_of(*get_input<ZenoGrid>("ZSGrid"))),
             "mpm_set_transfer");
@@ -1489,6 +1662,8 @@ ZENDEFNODE(ZSMPMSubstep, {
                               "ZSCloth",
                               "ZSTrackers",
                               "ZSBending",
+                              "BoundaryZSGrid",
+                              {"enum sticky slip separate", "boundary_type", "sticky"},
                               "dt",
                               {"float", "gravity", "-9.8"},
                               "Accel",

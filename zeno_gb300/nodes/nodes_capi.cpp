@@ -132,7 +132,9 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       int64_t tracker_n, const float *tracker_x, float *tracker_out_x,
                       float *tracker_out_v, const char *write_path, const char *bending_type,
                       float bending_stiffness, const char *attr_name, int32_t attr_dim,
-                      float *attr_out, const char *model_params) {
+                      float *attr_out, const char *model_params, int64_t bmesh_nv,
+                      const float *bmesh_x, const float *bmesh_v, int64_t bmesh_nt,
+                      const int32_t *bmesh_tris, const char *bgrid_type) {
   using namespace zeno;
   try {
     Graph g;
@@ -255,6 +257,51 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       g.setNodeInput("trk", "prim", tprim);
       g.markOnce("trk");
     }
+    // optional boundary grid: a triangle mesh through ToBoundaryParticles,
+    // its own partition and grid of transfer "boundary" and
+    // ZSBoundaryPrimitiveToZSGrid, applied with bgrid_type after the walls
+    // (and the collider)
+    std::shared_ptr<PrimitiveObject> bprim;
+    const bool bgrid = bmesh_nv > 0 && bmesh_x && bmesh_nt > 0 && bmesh_tris && bgrid_type;
+    if (bgrid) {
+      bprim = std::make_shared<PrimitiveObject>();
+      auto &bp = bprim->verts();
+      bp.resize(bmesh_nv);
+      auto &bv = bprim->attrs3["vel"];
+      bv.resize(bmesh_nv);
+      for (int64_t i = 0; i < bmesh_nv; ++i)
+        for (int d = 0; d < 3; ++d) {
+          bp[i][d] = bmesh_x[3 * i + d];
+          bv[i][d] = bmesh_v ? bmesh_v[3 * i + d] : 0.0f;
+        }
+      bprim->tris.resize(bmesh_nt);
+      for (int64_t i = 0; i < bmesh_nt; ++i)
+        for (int d = 0; d < 3; ++d) bprim->tris[i][d] = bmesh_tris[3 * i + d];
+      g.addNode("ToBoundaryParticles", "bpars");
+      g.setNodeInput("bpars", "prim", bprim);
+      g.setNodeInput("bpars", "dx", num(dx));
+      g.addNode("MakeZSPartition", "btable");
+      g.addNode("MakeZSGrid", "bgrid0");
+      g.setNodeInput("bgrid0", "dx", num(dx));
+      g.setNodeInput("bgrid0", "transfer", str("boundary"));
+      g.addNode("ZSPartitionForZSParticles", "bpart");
+      g.bindNodeInput("bpart", "ZSPartition", "btable", "ZSPartition");
+      g.bindNodeInput("bpart", "ZSGrid", "bgrid0", "ZSGrid");
+      g.bindNodeInput("bpart", "ZSParticles", "bpars", "ZSParticles");
+      g.addNode("ZSGridFromZSPartition", "bclear");
+      g.bindNodeInput("bclear", "ZSPartition", "bpart", "ZSPartition");
+      g.bindNodeInput("bclear", "ZSGrid", "bgrid0", "ZSGrid");
+      g.addNode("ZSBoundaryPrimitiveToZSGrid", "bp2g");
+      g.bindNodeInput("bp2g", "ZSParticles", "bpars", "ZSParticles");
+      g.bindNodeInput("bp2g", "ZSPartition", "bpart", "ZSPartition");
+      g.bindNodeInput("bp2g", "ZSGrid", "bclear", "ZSGrid");
+      g.addNode("UpdateZSGrid", "bupd");
+      g.bindNodeInput("bupd", "ZSPartition", "bpart", "ZSPartition");
+      g.bindNodeInput("bupd", "ZSGrid", "bp2g", "ZSGrid");
+      g.setNodeInput("bupd", "dt", num(dt));
+      for (const char *id : {"bpars", "btable", "bgrid0", "bpart", "bclear", "bp2g", "bupd"})
+        g.markOnce(id);
+    }
     auto dtobj = num(dt);
     std::string last;
     if (fused) {
@@ -266,6 +313,10 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       if (cloth) g.bindNodeInput("step", "ZSCloth", "cloth", "ZSParticles");
       if (trackers) g.bindNodeInput("step", "ZSTrackers", "trk", "ZSParticles");
       if (bending) g.bindNodeInput("step", "ZSBending", "bend", "ZSSpringPrim");
+      if (bgrid) {
+        g.bindNodeInput("step", "BoundaryZSGrid", "bupd", "ZSGrid");
+        g.setNodeInput("step", "boundary_type", str(bgrid_type));
+      }
       g.setNodeInput("step", "dt", dtobj);
       g.setNodeInput("step", "gravity", num(gravity));
       g.setNodeInput("step", "substeps", inum(substeps));
@@ -309,6 +360,15 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
         g.bindNodeInput("bc2", "ZSGrid", "bc", "ZSGrid");
         g.bindNodeInput("bc2", "ZSBoundary", "stepb", "ZSBoundary");
         grid_src = "bc2";
+      }
+      if (bgrid) {
+        g.addNode("ApplyGridBoundaryOnZSGrid", "gbc");
+        g.bindNodeInput("gbc", "ZSPartition", "expand", "ZSPartition");
+        g.bindNodeInput("gbc", "ZSGrid", grid_src, "ZSGrid");
+        g.bindNodeInput("gbc", "BoundaryZSPartition", "bpart", "ZSPartition");
+        g.bindNodeInput("gbc", "BoundaryZSGrid", "bupd", "ZSGrid");
+        g.setNodeInput("gbc", "type:", str(bgrid_type));
+        grid_src = "gbc";
       }
       g.addNode("ZSGridToZSParticle", "g2p");
       g.bindNodeInput("g2p", "ZSGrid", grid_src, "ZSGrid");

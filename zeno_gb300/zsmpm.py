@@ -771,7 +771,7 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
                                 C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P,
                                 C.c_char_p, C.c_char_p, C.c_float, C.c_char_p, C.c_int32, P,
-                                C.c_char_p]
+                                C.c_char_p, C.c_int64, P, P, C.c_int64, P, C.c_char_p]
     L.zsn_run_graph.restype = C.c_int32
     L.zsn_config_model.argtypes = [C.c_float, C.c_float, C.c_float, C.c_char_p, C.c_char_p,
                                    C.c_char_p, C.c_float, C.c_float, C.c_char_p,
@@ -814,7 +814,7 @@ def config_model(type="fcr", plasticity="none", aniso="none", E=1e4, nu=0.4, dx=
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
                    fused=False, levelset=None, transfer="apic", cloth=None, trackers=None,
-                   write_path=None, bending=None, attr=None, params=None):
+                   write_path=None, bending=None, attr=None, params=None, boundary_mesh=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -833,7 +833,12 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     (name, width) of an UpdatePrimitiveAttrFromZSParticles after the
     substeps; the attribute's values are appended to the return value.
     params: ConfigConstitutiveModel's "params" dict ({key: number}), e.g.
-    {"friction_angle": 30.0} for Drucker-Prager sand."""
+    {"friction_angle": 30.0} for Drucker-Prager sand.  boundary_mesh:
+    optional (pos, tris, vel or None, type) of a triangle mesh made a boundary
+    grid (ToBoundaryParticles, MakeZSGrid "boundary",
+    ZSBoundaryPrimitiveToZSGrid) and applied after the walls and the collider
+    -- by ApplyGridBoundaryOnZSGrid in the stage graph, as ZSMPMSubstep's
+    BoundaryZSGrid in the fused one."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -869,6 +874,13 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
         tk["x"] = np.ascontiguousarray(trackers, dtype=np.float32).reshape(-1, 3)
         tk["ox"] = np.zeros_like(tk["x"])
         tk["ov"] = np.zeros_like(tk["x"])
+    bm = {}
+    if boundary_mesh is not None:
+        bm["x"] = np.ascontiguousarray(boundary_mesh[0], dtype=np.float32).reshape(-1, 3)
+        bm["t"] = np.ascontiguousarray(boundary_mesh[1], dtype=np.int32).reshape(-1, 3)
+        bm["v"] = (None if boundary_mesh[2] is None else
+                   np.ascontiguousarray(boundary_mesh[2], dtype=np.float32).reshape(-1, 3))
+        bm["type"] = boundary_mesh[3].encode()
     rc = L.zsn_run_graph(1 if fused else 0, n, _p(x), _p(v), dx, type.encode(),
                          plasticity.encode(), E, nu, density, ppc, bc.encode(), thickness, dt,
                          gravity, substeps, _p(ox), _p(ov), _p(vmax), err, 1024, shape,
@@ -882,7 +894,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
                          float(bending[1]) if bending else 0.0,
                          attr[0].encode() if attr else None, int(attr[1]) if attr else 0,
                          _p(aout),
-                         ";".join(f"{k}={float(v)!r}" for k, v in (params or {}).items()).encode())
+                         ";".join(f"{k}={float(v)!r}" for k, v in (params or {}).items()).encode(),
+                         bm["x"].shape[0] if bm else 0, _p(bm.get("x")), _p(bm.get("v")),
+                         bm["t"].shape[0] if bm else 0, _p(bm.get("t")), bm.get("type"))
     if rc != 0:
         raise RuntimeError(err.value.decode())
     out = (ox, ov, float(vmax[0]))
