@@ -116,3 +116,32 @@ def test_node_graph_trackers(zsmpm_mod, oracle_mod, fused):
     assert st["status"] == 0
     assert rel_l2(tx, ref["tx"]) < 1e-6 and rel_l2(tv, ref["tv"]) < 1e-4
     assert rel_l2(x, p.x) < 1e-6 and rel_l2(v, p.v) < 1e-4
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_node_graph_tet_mesh_moves_like_trackers(zsmpm_mod, fused):
+    """A tetrahedral mesh through ToZSParticles (category 3): the reference's
+    transfers scatter nothing of it and move its vertices with the grid, so
+    its vertices follow exactly the path of the same points as trackers."""
+    scene, parts = S.jelly_cube(cells=8)
+    parts.v = np.tile(np.array([0.3, -0.5, 0.1], np.float32), (parts.n, 1))
+    g = np.linspace(0.37, 0.47, 5)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    # five tetrahedra per cube of the 4^3 lattice
+    tets = []
+    idx = lambda i, j, k: (i * 5 + j) * 5 + k
+    for i in range(4):
+        for j in range(4):
+            for k in range(4):
+                c = [idx(i + a, j + b, k + cc) for a in (0, 1) for b in (0, 1) for cc in (0, 1)]
+                tets += [(c[0], c[1], c[2], c[4]), (c[3], c[1], c[2], c[7]), (c[5], c[1], c[4], c[7]),
+                         (c[6], c[2], c[4], c[7]), (c[1], c[2], c[4], c[7])]
+    steps = 20
+    kw = dict(substeps=steps, bc="sticky", thickness=3, fused=fused, trackers=pts)
+    a = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", E=5e4, nu=0.3, **kw)
+    b = zsmpm_mod.run_node_graph(parts.x, parts.v, scene.dx, "fcr", E=5e4, nu=0.3,
+                                 tracker_tets=np.asarray(tets, np.int32), **kw)
+    for u, w in zip(a, b):
+        if isinstance(u, np.ndarray):
+            np.testing.assert_array_equal(u, w)
+    assert np.abs(b[3] - pts).max() > 1e-3  # the vertices moved

@@ -41,6 +41,7 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
 }
 inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris.values; }
 inline const std::vector<vec2i> &lines(PrimitiveObject &p) { return p.lines.values; }
+inline const std::vector<vec4i> &quads(PrimitiveObject &p) { return p.quads.values; }
 // float / vec3f attribute `k` of the vertices (tris: of the triangles),
 // created when absent, sized to the element count
 template <class T> std::vector<T> &attr(PrimitiveObject &p, bool tris, const std::string &k) {
@@ -73,6 +74,7 @@ inline const std::vector<float> *float_attr(PrimitiveObject &p, const std::strin
 }
 inline const std::vector<vec3i> &tris(PrimitiveObject &p) { return p.tris; }
 inline const std::vector<vec2i> &lines(PrimitiveObject &p) { return p.lines; }
+inline const std::vector<vec4i> &quads(PrimitiveObject &p) { return p.quads; }
 template <class T> std::vector<T> &attr(PrimitiveObject &p, bool tris, const std::string &k) {
   const size_t n = tris ? p.tris.size() : p.size();
   std::vector<T> *a;
@@ -320,7 +322,9 @@ void attach_cloth(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &cl) {
 // ToTrackerParticles points join the particles' context once; the
 // primitive's "pos" ("vel" when present) seeds them
 void attach_trackers(const std::shared_ptr<MpmContext> &ctx, ZenoParticles &tk) {
-  if (!tk.tracker) throw std::runtime_error("ZSTrackers: the input is not a ToTrackerParticles output");
+  if (!tk.tracker)
+    throw std::runtime_error("ZSTrackers: the input is not a ToTrackerParticles output or a "
+                             "tetrahedral ToZSParticles mesh");
   if (tk.tracker_ctx.lock() == ctx) return;
   if (tk.tracker_ctx.lock())
     throw std::runtime_error("ZSTrackers: the trackers belong to another context");
@@ -596,15 +600,27 @@ struct ToZSParticles : INode {
         hi[d] = b[d];
       }
     }
+    if (out->category != 0 && !prim_access::quads(*prim).empty()) {
+      // a tetrahedral mesh (Generation.cpp:740-741, 780-797): the reference's
+      // transfers scatter nothing of it (ZSParticleToZSGrid takes surfaces and
+      // curves only, Transfer.cu:1016-1036) and move its vertices with the
+      // grid velocity (Transfer.cu:1287-1372); here its vertices are tracker
+      // points, stepped through the ZSTrackers input of the particles whose
+      // grid moves them
+      out->tracker = true;
+      out->category = 3;  // ZenoParticles::tet
+      out->n = n;
+      set_output("ZSParticles", out);
+      return;
+    }
     if (out->category != 0) {
       // a mesh (Generation.cpp:738-749): triangles become a surface (cloth),
       // segments a curve (hair), with the defaults of Generation.cpp:695-699
-      // (k = 800, gamma = fa = dc = 0); tetrahedra are not implemented
+      // (k = 800, gamma = fa = dc = 0)
       const bool tri = !prim_access::tris(*prim).empty(), seg = !prim_access::lines(*prim).empty();
       if (!tri && !seg)
         throw std::runtime_error("ToZSParticles: category " + std::to_string(out->category) +
-                                 " needs a triangle or segment mesh (tetrahedra are not "
-                                 "implemented by this backend)");
+                                 " needs a tetrahedron, triangle or segment mesh");
       const int type = model->mat.type;
       if (type != MPM_FCR && type != MPM_NHK && type != MPM_STVK)
         throw std::runtime_error("ToZSParticles: a surface takes fcr, nhk or stvk");

@@ -134,7 +134,8 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
                       float bending_stiffness, const char *attr_name, int32_t attr_dim,
                       float *attr_out, const char *model_params, int64_t bmesh_nv,
                       const float *bmesh_x, const float *bmesh_v, int64_t bmesh_nt,
-                      const int32_t *bmesh_tris, const char *bgrid_type) {
+                      const int32_t *bmesh_tris, const char *bgrid_type, int64_t tracker_nq,
+                      const int32_t *tracker_quads) {
   using namespace zeno;
   try {
     Graph g;
@@ -253,7 +254,16 @@ int32_t zsn_run_graph(int32_t fused, int64_t n, const float *pos, const float *v
       tp.resize(tracker_n);
       for (int64_t i = 0; i < tracker_n; ++i)
         for (int d = 0; d < 3; ++d) tp[i][d] = tracker_x[3 * i + d];
-      g.addNode("ToTrackerParticles", "trk");
+      if (tracker_quads && tracker_nq > 0) {  // a tetrahedral mesh's vertices
+        tprim->quads.resize(tracker_nq);
+        for (int64_t i = 0; i < tracker_nq; ++i)
+          for (int d = 0; d < 4; ++d) tprim->quads[i][d] = tracker_quads[4 * i + d];
+        g.addNode("ToZSParticles", "trk");
+        g.bindNodeInput("trk", "ZSModel", "model", "ZSModel");
+        g.setNodeInput("trk", "category", inum(3));
+      } else {
+        g.addNode("ToTrackerParticles", "trk");
+      }
       g.setNodeInput("trk", "prim", tprim);
       g.markOnce("trk");
     }

@@ -31,6 +31,7 @@ namespace zeno {
 using vec3f = std::array<float, 3>;
 using vec3i = std::array<int, 3>;
 using vec2i = std::array<int, 2>;
+using vec4i = std::array<int, 4>;
 
 struct IObject {
   virtual ~IObject() = default;
@@ -74,6 +75,7 @@ struct PrimitiveObject : IObject {
   std::map<std::string, std::vector<float>> attrs1;
   std::vector<vec3i> tris;  // triangle vertex indices
   std::vector<vec2i> lines; // segment vertex indices
+  std::vector<vec4i> quads; // tetrahedron vertex indices
   std::map<std::string, std::vector<vec3f>> tri_attrs3;  // per-triangle attributes
   std::map<std::string, std::vector<float>> tri_attrs1;
   std::vector<vec3f> &verts() { return attrs3["pos"]; }

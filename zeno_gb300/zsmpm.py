@@ -771,7 +771,8 @@ def load_nodes(path: str = NODES_LIB_PATH):
                                 C.c_char_p, C.c_int64, C.c_char_p, P, C.c_char_p, C.c_char_p,
                                 C.c_int64, P, P, C.c_int64, P, P, P, P, C.c_int64, P, P, P,
                                 C.c_char_p, C.c_char_p, C.c_float, C.c_char_p, C.c_int32, P,
-                                C.c_char_p, C.c_int64, P, P, C.c_int64, P, C.c_char_p]
+                                C.c_char_p, C.c_int64, P, P, C.c_int64, P, C.c_char_p,
+                                C.c_int64, P]
     L.zsn_run_graph.restype = C.c_int32
     L.zsn_config_model.argtypes = [C.c_float, C.c_float, C.c_float, C.c_char_p, C.c_char_p,
                                    C.c_char_p, C.c_float, C.c_float, C.c_char_p,
@@ -814,7 +815,8 @@ def config_model(type="fcr", plasticity="none", aniso="none", E=1e4, nu=0.4, dx=
 def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, density=1000.0,
                    ppc=8.0, bc="sticky", thickness=3, dt=1e-4, gravity=-9.8, substeps=1,
                    fused=False, levelset=None, transfer="apic", cloth=None, trackers=None,
-                   write_path=None, bending=None, attr=None, params=None, boundary_mesh=None):
+                   write_path=None, bending=None, attr=None, params=None, boundary_mesh=None,
+                   tracker_tets=None):
     """Run the zeno MPM substep graph headless through the C++ node layer.
     levelset: optional dict for a MakeZSLevelSet -> ToZSBoundary collider
     applied after the walls -- in the stage graph through StepZSBoundary and a
@@ -838,7 +840,9 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
     grid (ToBoundaryParticles, MakeZSGrid "boundary",
     ZSBoundaryPrimitiveToZSGrid) and applied after the walls and the collider
     -- by ApplyGridBoundaryOnZSGrid in the stage graph, as ZSMPMSubstep's
-    BoundaryZSGrid in the fused one."""
+    BoundaryZSGrid in the fused one.  tracker_tets: optional (m, 4) tetrahedra
+    over the tracker points: they then enter as a tetrahedral mesh through
+    ToZSParticles (category 3) instead of ToTrackerParticles."""
     L = load_nodes()
     x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 3)
     v = np.ascontiguousarray(v, dtype=np.float32).reshape(-1, 3)
@@ -874,6 +878,7 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
         tk["x"] = np.ascontiguousarray(trackers, dtype=np.float32).reshape(-1, 3)
         tk["ox"] = np.zeros_like(tk["x"])
         tk["ov"] = np.zeros_like(tk["x"])
+    tq = None if tracker_tets is None else np.ascontiguousarray(tracker_tets, np.int32).reshape(-1, 4)
     bm = {}
     if boundary_mesh is not None:
         bm["x"] = np.ascontiguousarray(boundary_mesh[0], dtype=np.float32).reshape(-1, 3)
@@ -896,7 +901,8 @@ def run_node_graph(x, v, dx, type="fcr", plasticity="none", E=1e4, nu=0.4, densi
                          _p(aout),
                          ";".join(f"{k}={float(v)!r}" for k, v in (params or {}).items()).encode(),
                          bm["x"].shape[0] if bm else 0, _p(bm.get("x")), _p(bm.get("v")),
-                         bm["t"].shape[0] if bm else 0, _p(bm.get("t")), bm.get("type"))
+                         bm["t"].shape[0] if bm else 0, _p(bm.get("t")), bm.get("type"),
+                         tq.shape[0] if tq is not None else 0, _p(tq))
     if rc != 0:
         raise RuntimeError(err.value.decode())
     out = (ox, ov, float(vmax[0]))
