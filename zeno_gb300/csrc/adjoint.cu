@@ -493,9 +493,12 @@ void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, f
                         float *glam, long long n, cudaStream_t s) {
   k_g2p_adjoint_particles<<<d.num_sms * 4, kAdjPThreads, 0, s>>>(
       d, d.pbuf[cur], d.ibuf[cur], an, ap, gmu, glam, d.adj_rec, n, adjoint_chunks(d, n));
+  k_g2p_adjoint_scatter<<<d.num_sms * 4, kP2GThreads, kP2GSmem, s>>>(d, d.adj_rec);
+}
+
+void configure_adjoint() {
   cudaFuncSetAttribute(k_g2p_adjoint_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        kP2GSmem);
-  k_g2p_adjoint_scatter<<<d.num_sms * 4, kP2GThreads, kP2GSmem, s>>>(d, d.adj_rec);
 }
 
 void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s) {

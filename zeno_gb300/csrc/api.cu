@@ -2264,34 +2264,33 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
   StoreSwap swap(c);
   PartSwap pswap(c);
   if ((rc = set_dt(c, dt))) return rc;
-  for (int32_t seg = n_seg - 1; seg >= 0; --seg) {
-    const int32_t s0 = seg * every, s1 = std::min(s0 + every, n_substeps);
+  // the colliders are static here, so stepping them is the identity: one
+  // parameter set for the whole walk (no upload inside a segment)
+  set_auto_step(c, 1);
+  if ((rc = push_params(c))) return rc;
+  const long long nn = c->prm.n;
+  // One segment: recompute its states from `ck` (its checkpoint), then take
+  // them back through the adjoint substeps, last to first.
+  auto segment = [&](int32_t s0, int32_t s1, SnapStore ck, bool kept) -> int32_t {
     // the segment's states: its checkpoint, then the recomputed ones, each
     // substep reading one snapshot and writing the next (no copies)
     auto state = [&](int32_t s) {
-      return s == s0 ? snap_store(c, const_cast<float *>(ckpts) + (size_t)seg * snap)
-                     : snap_store(c, seg_states + (size_t)(s - s0) * snap);
+      return s == s0 ? ck : snap_store(c, seg_states + (size_t)(s - s0) * snap);
     };
-    const bool kept = tail_kept && seg == n_seg - 1;  // states and sets from the forward
-    set_auto_step(c, 1);
-    if ((rc = push_params(c))) return rc;
+    int32_t r;
     c->needs_full_clear = true;
     c->binned = false;
     for (int32_t s = s0; !kept && s + 1 < s1; ++s) {
       swap.use(state(s), state(s + 1));
       if (keep) pswap.set(c->psets[s - s0], c->pset_cap);
-      if ((rc = prepare_partition(c))) return rc;
+      if ((r = prepare_partition(c))) return r;
       enqueue_bin_if_needed(c);
       enqueue_substep(c, 0);  // bins the new positions: the next one needs no binning
       if (keep)
         ZS_CUDA(cudaMemcpyAsync(c->pset_cnt + 2 * (s - s0), &c->d.cnt->n_gblocks, 2 * sizeof(int),
                                 cudaMemcpyDeviceToDevice, c->stream));
-      if ((rc = launch_check("rollout recompute"))) return rc;
+      if ((r = launch_check("rollout recompute"))) return r;
     }
-    // adjoint substeps, last to first, each on its own snapshot
-    set_auto_step(c, 0);
-    if ((rc = push_params(c))) return rc;
-    const long long nn = c->prm.n;
     for (int32_t s = s1 - 1; s >= s0; --s) {
       swap.use(state(s), state(s));
       if (keep) pswap.set(c->psets[s - s0], c->pset_cap);
@@ -2301,7 +2300,7 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
       } else {  // the segment's last substep (not recomputed), or no sets
         c->needs_full_clear = true;  // the counts described another state
         c->binned = false;
-        if ((rc = prepare_partition(c))) return rc;
+        if ((r = prepare_partition(c))) return r;
         enqueue_bin_if_needed(c);
         enqueue_sort(c);
         launch_p2g(c->d, 0, c->stream);
@@ -2311,9 +2310,59 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
       launch_g2p_adjoint(c->d, 0, a, b, grad_mu, grad_lam, nn, c->stream);
       launch_grid_adjoint(c->d, c->stream);
       launch_p2g_adjoint(c->d, 0, b, grad_mu, grad_lam, nn, c->stream);
-      if ((rc = launch_check("rollout adjoint"))) return rc;
+      if ((r = launch_check("rollout adjoint"))) return r;
       std::swap(a, b);
     }
+    return MPM_OK;
+  };
+  // Full segments of an even length all launch the same operations on the
+  // same buffers (the kept partition sets, the segment states; the adjoint
+  // pair swapped an even number of times) once each one's checkpoint is
+  // copied into slot 0 of seg_states, which no recompute writes: for scenes
+  // of up to 4M particles the first is captured as a CUDA graph and the rest
+  // replay it, without the per-launch gaps.
+  cudaGraphExec_t seg_graph = nullptr;
+  struct GraphGuard {
+    cudaGraphExec_t *g;
+    ~GraphGuard() {
+      if (*g) cudaGraphExecDestroy(*g);
+    }
+  } graph_guard{&seg_graph};
+  bool graph_failed = false;
+  for (int32_t seg = n_seg - 1; seg >= 0; --seg) {
+    const int32_t s0 = seg * every, s1 = std::min(s0 + every, n_substeps);
+    const bool kept = tail_kept && seg == n_seg - 1;  // states and sets from the forward
+    const SnapStore ck = snap_store(c, const_cast<float *>(ckpts) + (size_t)seg * snap);
+    // (large scenes gain nothing from it: their kernels dwarf the launches,
+    // and the checkpoint copy would cost more)
+    const bool replay = keep && !kept && s1 - s0 == every && every % 2 == 0 && every > 1 &&
+                        nn <= (1ll << 22) && graphs_enabled() && !graph_failed;
+    if (!replay) {
+      if ((rc = segment(s0, s1, ck, kept))) return rc;
+      continue;
+    }
+    const SnapStore slot0 = snap_store(c, seg_states);
+    ZS_CUDA(cudaMemcpyAsync(slot0.f, ck.f, snap * sizeof(float), cudaMemcpyDeviceToDevice,
+                            c->stream));
+    if (!seg_graph) {
+      cudaGraph_t g = nullptr;
+      float *a0 = a, *b0 = b;
+      ZS_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      const int32_t r = segment(s0, s1, slot0, false);
+      cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+      if (r == MPM_OK && e == cudaSuccess) e = cudaGraphInstantiate(&seg_graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      a = a0;  // the captured segment has not run yet
+      b = b0;
+      if (r != MPM_OK || e != cudaSuccess) {  // run it (and the rest) without a graph
+        seg_graph = nullptr;
+        graph_failed = true;
+        cudaGetLastError();
+        if ((rc = segment(s0, s1, slot0, false))) return rc;
+        continue;
+      }
+    }
+    ZS_CUDA(cudaGraphLaunch(seg_graph, c->stream));
   }
   if (a != adj)
     ZS_CUDA(cudaMemcpyAsync(adj, a, (size_t)MPM_ADJ_PLANES * n * sizeof(float),

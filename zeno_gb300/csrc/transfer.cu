@@ -207,6 +207,7 @@ void configure_launches(DevPtrs &d) {
   d.grid_stream = d.num_sms * (L.stream_ctas_per_sm > 0 ? L.stream_ctas_per_sm : 8);
   d.g2p_threads = gt;
   d.grid_persist = persistent_grid(d);
+  configure_adjoint();
 }
 
 template <int NT, int CH> void launch_p2g_shape(const DevPtrs &d, int cur, cudaStream_t s) {

@@ -381,6 +381,9 @@ void set_last_error(const std::string &msg);
 void launch_g2p_adjoint(const DevPtrs &d, int cur, const float *an, float *ap, float *gmu,
                         float *glam, long long n, cudaStream_t s);
 void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s);
+// the adjoint kernels' launch attributes on the current device (once per
+// context, outside any stream capture)
+void configure_adjoint();
 void launch_p2g_adjoint(const DevPtrs &d, int cur, float *ap, float *gmu, float *glam, long long n,
                         cudaStream_t s);
 
