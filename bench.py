@@ -197,6 +197,18 @@ def batched_form(zsmpm, steps: int, dev: int):
     ms_b = e0.elapsed_time(e1)
     ctx.sync()
     st = ctx.stats()
+    # the same batch with one persistent cooperative kernel per substep
+    ctx.set_persistent(True)
+    ctx.substep(dt, 5)
+    ctx.sync()
+    e0.record(stream)
+    ctx.substep(dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_pk = e0.elapsed_time(e1)
+    ctx.sync()
+    pk_status = ctx.stats()["status"]
+    ctx.set_persistent(False)
     # sample for the parity check of the cpu_baseline leg: scenes 0-7 after
     # 20 substeps of the batch
     check_steps = 20
@@ -232,6 +244,8 @@ def batched_form(zsmpm, steps: int, dev: int):
             "plain_sequential": n * steps / (ms_p * 1e-3),
             "speedup_over_plain": ms_p / ms_b,
             "kernel_launches_per_step": KERNELS_PER_SUBSTEP,
+            "persistent": {"value": n * steps / (ms_pk * 1e-3), "ms_per_step": ms_pk / steps,
+                           "status": pk_status, "kernel_launches_per_step": 1},
             "launch_config": tuned["config"],
             "note": "plain_sequential: the same scenes, one plain context each, default launch "
                     "shapes; batched: autotuned launch shapes",
@@ -928,6 +942,8 @@ def run_gpu(args):
         tchk = forms.get(name, {}).pop("_check", None)
         if tchk:
             checks[name] = tchk
+    if "batched" in forms:  # particle-substeps/s against the plain path's
+        forms["batched"]["vs_plain_path"] = forms["batched"]["value"] / value
     bchk = forms.get("batched", {}).pop("_check", None)
     if bchk:
         for k, (sc, pt, gx, gv) in enumerate(bchk["scenes"]):
