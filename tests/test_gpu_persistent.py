@@ -128,3 +128,33 @@ def test_zero_barrier_limit_times_out(zsmpm_mod):
         out = ctx.download(("x",))
     ref = _run(zsmpm_mod, scene, parts, 3, False)
     assert rel_l2(out["x"], ref["x"]) <= 1e-6
+
+
+def test_batched_scenes(zsmpm_mod, oracle_mod):
+    """A batch of independent scenes (own dx, directory, walls; an empty
+    scene and a one-particle scene among them) through the persistent kernel:
+    each scene against the stage kernels and the oracle."""
+    from .test_gpu_batched import _mixed_scenes
+    pairs = _mixed_scenes()
+    scns, mats, parts, offs = zsmpm_mod.concat_scenes(pairs)
+    dt = pairs[0][0].dt
+    outs = []
+    for persistent in (True, False):
+        with zsmpm_mod.BatchContext(scns, mats, max_particles=parts.n) as ctx:
+            if persistent:
+                ctx.set_persistent(True)
+            ctx.upload_batch(parts, offs)
+            ctx.substep(dt, 30)
+            ctx.sync()
+            assert ctx.stats()["status"] == 0
+            outs.append(ctx.download())
+    per, stg = outs
+    for k, (scene, p) in enumerate(pairs):
+        if p.n == 0:
+            continue
+        sl = slice(offs[k], offs[k + 1])
+        for ch in ("x", "v", "F"):
+            assert rel_l2(per[ch][sl], stg[ch][sl]) <= 1e-5, (k, ch)
+        if p.n >= 1000:
+            ref, _ = oracle_mod.run(scene, p, 30, "f64")
+            assert rel_l2(per["x"][sl], ref.x) <= 1e-4 and rel_l2(per["v"][sl], ref.v) <= 1e-4
