@@ -98,8 +98,37 @@ def test_stage_path_matches_fused(zsmpm_mod):
     mesh = _sheet()
     _, fused, _, _ = _gpu(zsmpm_mod, scene, _empty(), mesh, 20)
     _, staged, _, _ = _gpu(zsmpm_mod, scene, _empty(), mesh, 20, staged=True)
-    # float atomics: the summation order differs from run to run
-    assert rel_l2(staged["vx"], fused["vx"]) < 1e-6 and rel_l2(staged["vv"], fused["vv"]) < 1e-4
+    for k in ("vx", "vv", "eF"):
+        np.testing.assert_array_equal(staged[k], fused[k], err_msg=k)
+
+
+@pytest.mark.parametrize("tr", [S.TRANSFER_APIC, S.TRANSFER_AFLIP])
+def test_cloth_is_bit_reproducible(zsmpm_mod, tr):
+    """The cloth's P2G sums every node in a fixed order (its points
+    partitioned and sorted, tiles summed per node, impulses per vertex in
+    slot order; no float atomics): repeated runs and other launch shapes give
+    the same bits, with a jelly block and bending springs in the same grid."""
+    scene, parts = S.jelly_cube(cells=10)
+    scene.transfer = tr
+    mesh = S.cloth_sheet((0.475, 0.55, 0.475), 0.35, 14, jitter=0.2, seed=3, E=2e4, nu=0.3,
+                         density=300.0, gamma=50.0, k=800.0, fa=30.0, dc=0.02)
+    mesh.v = np.tile(np.array([0.0, -1.5, 0.0], np.float32), (mesh.x.shape[0], 1))
+    outs = []
+    for cfg in ({}, {}, {"sort_ctas_per_sm": 16, "stream_ctas_per_sm": 3, "p2g_shape": 4}):
+        with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+            ctx.set_launch_config(cfg)
+            ctx.upload(parts)
+            ctx.add_cloth(mesh)
+            ctx.add_cloth_bending(50.0, "vertex")
+            ctx.substep(scene.dt, 60)
+            ctx.sync()
+            assert ctx.stats()["status"] == 0
+            outs.append((ctx.cloth_download(), ctx.download(("x", "v"))))
+    for cl, mpm in outs[1:]:
+        for k in ("vx", "vv", "eF", "ed"):
+            np.testing.assert_array_equal(cl[k], outs[0][0][k], err_msg=k)
+        for k in ("x", "v"):
+            np.testing.assert_array_equal(mpm[k], outs[0][1][k], err_msg=k)
 
 
 def test_cloth_rejects_differentiable_form(zsmpm_mod):

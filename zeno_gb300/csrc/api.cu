@@ -1220,6 +1220,92 @@ int32_t mpm_particles_set_attr(mpm_ctx *c, const char *name, const float *values
   return MPM_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The per-vertex contribution slots of a cloth's impulses: element corners
+// (3 e + corner, the first `per` corners) in element order, then spring ends
+// (3 n_eles + 2 s + end) in spring order.
+int32_t upload_cloth_slots(mpm_ctx *c, ClothDev &cl, const std::vector<int32_t> &inds, int per,
+                           const std::vector<int32_t> &springs) {
+  const long long nv = cl.n_verts, ne = cl.n_eles, ns = (long long)springs.size() / 2;
+  std::vector<int32_t> ptr(nv + 1, 0), list;
+  for (long long e = 0; e < ne; ++e)
+    for (int k = 0; k < per; ++k) ++ptr[inds[3 * e + k] + 1];
+  for (long long s = 0; s < 2 * ns; ++s) ++ptr[springs[s] + 1];
+  for (long long v = 0; v < nv; ++v) ptr[v + 1] += ptr[v];
+  list.resize(ptr[nv]);
+  std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (long long e = 0; e < ne; ++e)
+    for (int k = 0; k < per; ++k) list[fill[inds[3 * e + k]]++] = (int32_t)(3 * e + k);
+  for (long long s = 0; s < 2 * ns; ++s) list[fill[springs[s]]++] = (int32_t)(3 * ne + s);
+  dfree(c, cl.vptr);
+  dfree(c, cl.vlist);
+  dfree(c, cl.cimp);
+  cl.vptr = cl.vlist = nullptr;
+  cl.cimp = nullptr;
+  int32_t rc;
+  if ((rc = dalloc(c, &cl.vptr, (size_t)nv + 1)) || (rc = dalloc(c, &cl.vlist, list.size())) ||
+      (rc = dalloc(c, &cl.cimp, (size_t)(3 * ne + 2 * ns))))
+    return rc;
+  ZS_CUDA(cudaMemcpyAsync(cl.vptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                          c->stream));
+  if (!list.empty())
+    ZS_CUDA(cudaMemcpyAsync(cl.vlist, list.data(), list.size() * sizeof(int32_t),
+                            cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));  // the host vectors go away
+  return MPM_OK;
+}
+
+// The arrays of the cloth's deterministic P2G: records, slots, and the
+// partition of its points into blocks of their own, with room for eight
+// times the blocks the mesh occupies at creation (more is a capacity
+// error of the context).
+int32_t alloc_cloth_p2g(mpm_ctx *c, ClothDev &cl, const std::vector<int32_t> &inds, int per,
+                        const std::vector<float> &vx, const std::vector<float> &ex) {
+  const DevPtrs &d = c->d;
+  const SceneParams &S = c->scenes[0];
+  const long long np = cl.n_verts + cl.n_eles;
+  std::unordered_map<long long, int> blocks;
+  auto add = [&](const float *x) {
+    long long k = 0;
+    for (int a = 0; a < 3; ++a) {
+      const int b = (int)std::floor(x[a] * S.inv_dx - 0.5f) >> 2;
+      k = k * (1ll << 21) + (b + (1 << 20));
+    }
+    blocks.emplace(k, 0);
+  };
+  for (long long i = 0; i < cl.n_verts; ++i) add(&vx[3 * i]);
+  for (long long e = 0; e < cl.n_eles; ++e) add(&ex[3 * e]);
+  const long long capb = std::min<long long>({d.ndir, np, std::max<long long>(8 * (long long)blocks.size(), 1024)});
+  cl.cap_cblocks = (int)capb;
+  int32_t rc;
+  if ((rc = dalloc(c, &cl.crec, (size_t)np * kClothRec)) || (rc = dalloc(c, &cl.ckey, (size_t)np)) ||
+      (rc = dalloc(c, &cl.cperm, (size_t)np)) || (rc = dalloc(c, &cl.cperm_tmp, (size_t)np)) ||
+      (rc = dalloc(c, &cl.cinv, (size_t)np)) || (rc = dalloc(c, &cl.cdir_count, (size_t)d.ndir)) ||
+      (rc = dalloc(c, &cl.cdir_fill, (size_t)d.ndir)) || (rc = dalloc(c, &cl.cdir_gb, (size_t)d.ndir)) ||
+      (rc = dalloc(c, &cl.cdir_bk, (size_t)d.ndir)) || (rc = dalloc(c, &cl.cdir_flag, (size_t)d.ndir)) ||
+      (rc = dalloc(c, &cl.cgb_dir, (size_t)capb)) || (rc = dalloc(c, &cl.cbk_dir, (size_t)capb)) ||
+      (rc = dalloc(c, &cl.cbk_start, (size_t)capb)) || (rc = dalloc(c, &cl.cbk_count, (size_t)capb)) ||
+      (rc = dalloc(c, &cl.ctile_sums, (size_t)3 * d.ntiles)) ||
+      (rc = dalloc(c, &cl.ctile, (size_t)capb * kTileNodes)) ||
+      (rc = dalloc(c, &cl.ctile2, (size_t)capb * kTileNodes)) || (rc = dalloc(c, &cl.ccnt, 1)) ||
+      (rc = dalloc(c, &cl.cprm, 1)))
+    return rc;
+  ZS_CUDA(cudaMemsetAsync(cl.cdir_count, 0, (size_t)d.ndir * sizeof(int32_t), c->stream));
+  ZS_CUDA(cudaMemsetAsync(cl.cdir_flag, 0, (size_t)d.ndir, c->stream));
+  ZS_CUDA(cudaMemsetAsync(cl.ccnt, 0, sizeof(Counters), c->stream));
+  SimParams cp{};
+  cp.n = np;  // and no collider stepping: auto_step = 0
+  ZS_CUDA(cudaMemcpyAsync(cl.cprm, &cp, sizeof(SimParams), cudaMemcpyHostToDevice, c->stream));
+  return upload_cloth_slots(c, cl, inds, per, {});
+}
+
+}  // namespace
+
+extern "C" {
+
 int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
   int32_t rc = check(c);
   if (rc) return rc;
@@ -1400,6 +1486,7 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   nc.n_verts = nv;
   nc.n_eles = ne;
+  if ((rc = alloc_cloth_p2g(c, nc, inds, curve ? 2 : 3, vx, ex))) return rc;
   nc.kind = desc->kind;
   nc.model = curve ? MPM_STVK : desc->model;  // curves: StVK-Hencky (Generation.cpp:761-769)
   nc.gamma = desc->stiffness_shear;
@@ -1513,6 +1600,8 @@ int32_t mpm_cloth_add_bending(mpm_ctx *c, int32_t type, float stiffness, float t
   ZS_CUDA(cudaMemcpy(cl.srl, srl.data(), srl.size() * 4, cudaMemcpyHostToDevice));
   cl.thickness = thickness;
   cl.n_springs = ns;
+  // the springs' impulse slots join their vertices' lists
+  if ((rc = upload_cloth_slots(c, cl, inds, 3, sv))) return rc;
   drop_graphs(c);  // the substep gains the springs' kernel
   return MPM_OK;
 }

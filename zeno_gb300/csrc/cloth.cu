@@ -32,11 +32,6 @@
 namespace zsmpm {
 namespace {
 
-struct V3 {
-  float x, y, z;
-};
-__device__ __forceinline__ V3 ld3(const float *p) { return V3{p[0], p[1], p[2]}; }
-
 // grid node index of node I of scene 0, or -1 outside the grid blocks
 __device__ __forceinline__ long long node_of(const DevPtrs &d, const SceneParams &S, int i0, int i1,
                                              int i2) {
@@ -166,13 +161,15 @@ __global__ void k_cloth_mark(DevPtrs d) {
   }
 }
 
-// element P2G (type i on the grid, type ii impulses on the vertices)
-__global__ void k_cloth_p2g_elements(DevPtrs d) {
+// Element P2G, first part: the element's stress, its scatter record (type i:
+// mass, momentum and the normal-direction force on its 27 nodes) at its
+// sorted position, and its type (ii) impulses on its vertices, one
+// contribution slot each (no atomics).
+__global__ void k_cloth_elements(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
-  const SceneParams &S = d.scn[0];
-  const float dt = d.prm->dt, dx = S.dx, inv_dx = S.inv_dx;
-  const bool flip_style = d.transfer != MPM_TRANSFER_APIC, affine = d.transfer != MPM_TRANSFER_FLIP;
+  const float dt = d.prm->dt;
+  const bool affine = d.transfer != MPM_TRANSFER_FLIP;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cl.n_eles;
        e += (long long)gridDim.x * blockDim.x) {
     float F[9], dm[9], Q[9], R[9];
@@ -243,52 +240,33 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) P[i] += T[i];
     const float mass = cl.em[e], vol = cl.evol[e];
-    const V3 ve = ld3(cl.ev + 3 * e);
-    float C[9];
+    const int r = cl.cinv[cl.n_verts + e];
+    if (r >= 0) {  // (a point outside the directory has no record; the status says so)
+      float *rec = cl.crec + (long long)r * kClothRec;
+      const float kf = -vol * dt;
+      const float dc1[3] = {dm[1], dm[4], dm[7]}, dc2[3] = {dm[2], dm[5], dm[8]};
 #pragma unroll
-    for (int i = 0; i < 9; ++i) C[i] = affine ? cl.eC[9 * e + i] : 0.0f;
-    const float x[3] = {cl.ex[3 * e], cl.ex[3 * e + 1], cl.ex[3 * e + 2]};
-    const Stencil1 s0 = stencil1(x[0], inv_dx), s1 = stencil1(x[1], inv_dx), s2 = stencil1(x[2], inv_dx);
-    const float kf = -vol * dt;
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
-        for (int k = 0; k < 3; ++k) {
-          const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
-          if (idx < 0) {
-            atomicOr(&d.cnt->status, ST_STENCIL);
-            continue;
-          }
-          const float W = s0.w[i] * s1.w[j] * s2.w[k];
-          const float gw[3] = {wgrad(s0, i) * s1.w[j] * s2.w[k] * inv_dx,
-                               s0.w[i] * wgrad(s1, j) * s2.w[k] * inv_dx,
-                               s0.w[i] * s1.w[j] * wgrad(s2, k) * inv_dx};
-          // surface: P_c3 (grad W . d_c3); curve: P_c23 (d_c23^T grad W); times -vol dt
-          const float s2f = (gw[0] * dm[2] + gw[1] * dm[5] + gw[2] * dm[8]) * kf;
-          const float s1f = curve ? (gw[0] * dm[1] + gw[1] * dm[4] + gw[2] * dm[7]) * kf : 0.0f;
-          const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
-          const float vn[3] = {ve.x, ve.y, ve.z};
-          float mom[3], fo[3];
+      for (int a = 0; a < 3; ++a) {
+        rec[a] = cl.ex[3 * e + a];
+        rec[4 + a] = mass * cl.ev[3 * e + a];
+        rec[25 + a] = 0.0f;
 #pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const float Cx = C[a * 3 + 0] * xi[0] + C[a * 3 + 1] * xi[1] + C[a * 3 + 2] * xi[2];
-            fo[a] = P[a * 3 + 1] * s1f + P[a * 3 + 2] * s2f;
-            mom[a] = W * mass * (vn[a] + Cx) + (flip_style ? 0.0f : fo[a]);
-          }
-          float4 *g4 = d.grid + idx;
-          atomicAdd(g4, make_float4(W * mass, mom[0], mom[1], mom[2]));  // one 16-byte atomic
-          if (flip_style) {
-            float4 *h4 = d.grid2 + idx;
-            atomicAdd(h4, make_float4(fo[0], fo[1], fo[2], 0.0f));
-          }
+        for (int c = 0; c < 3; ++c) {
+          rec[7 + a * 3 + c] = affine ? mass * cl.eC[9 * e + a * 3 + c] : 0.0f;
+          // surface: P_c3 (grad W . d_c3); curve: P_c2 (grad W . d_c2) too
+          rec[16 + a * 3 + c] =
+              kf * ((curve ? P[a * 3 + 1] * dc1[c] : 0.0f) + P[a * 3 + 2] * dc2[c]);
         }
+      }
+      rec[3] = mass;
+    }
+    float4 *ci = cl.cimp + 3 * e;
     if (curve) {  // type (ii): +-vol dt P_c0 DmInv00 on the two vertices
-      const int t0 = cl.inds[3 * e], t1 = cl.inds[3 * e + 1];
       const float di = cl.eDmInv[9 * e];
-      if (t0 < 0 || t0 >= cl.n_verts || t1 < 0 || t1 >= cl.n_verts) continue;
       const float4 f = make_float4(vol * dt * P[0] * di, vol * dt * P[3] * di,
                                    vol * dt * P[6] * di, 0.0f);
-      atomicAdd(imp4(cl, t0), f);
-      atomicAdd(imp4(cl, t1), make_float4(-f.x, -f.y, -f.z, 0.0f));
+      ci[0] = f;
+      ci[1] = make_float4(-f.x, -f.y, -f.z, 0.0f);
       continue;
     }
     // type (ii): impulses from the in-plane columns of P through DmInv rows
@@ -296,8 +274,6 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
     const float r1[2] = {cl.eDmInv[9 * e + 3], cl.eDmInv[9 * e + 4]};
 #pragma unroll
     for (int vi = 0; vi < 3; ++vi) {
-      const int t = cl.inds[3 * e + vi];
-      if (t < 0 || t >= cl.n_verts) continue;
       float Dr0, Dr1, coeff;
       if (vi == 0) {
         Dr0 = r0[0] + r1[0];
@@ -308,63 +284,66 @@ __global__ void k_cloth_p2g_elements(DevPtrs d) {
         Dr1 = vi == 1 ? r0[1] : r1[1];
         coeff = -vol * dt;
       }
-      atomicAdd(imp4(cl, t), make_float4(coeff * (P[0] * Dr0 + P[1] * Dr1),
-                                         coeff * (P[3] * Dr0 + P[4] * Dr1),
-                                         coeff * (P[6] * Dr0 + P[7] * Dr1), 0.0f));
+      ci[vi] = make_float4(coeff * (P[0] * Dr0 + P[1] * Dr1), coeff * (P[3] * Dr0 + P[4] * Dr1),
+                           coeff * (P[6] * Dr0 + P[7] * Dr1), 0.0f);
     }
   }
 }
 
-// vertex P2G: mass, momentum and the impulse of its elements
-__global__ void k_cloth_p2g_verts(DevPtrs d) {
+// Vertex impulses: the contribution slots of each vertex (its elements in
+// index order, then its springs) summed in that fixed order.
+__global__ void k_cloth_vertex_impulses(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
-  const SceneParams &S = d.scn[0];
-  const float dx = S.dx, inv_dx = S.inv_dx;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < cl.n_verts;
+       v += (long long)gridDim.x * blockDim.x) {
+    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = cl.vptr[v]; j < cl.vptr[v + 1]; ++j) {
+      const float4 c = cl.cimp[cl.vlist[j]];
+      sum.x += c.x;
+      sum.y += c.y;
+      sum.z += c.z;
+    }
+    *imp4(cl, v) = sum;
+  }
+}
+
+// Vertex P2G records: mass, momentum m (v + C (x_i - x_p)) and the impulse
+// (in the momentum, or in vstar on FLIP-style grids).
+__global__ void k_cloth_vertex_records(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
+  const ClothDev &cl = d.cloth;
   const bool flip_style = d.transfer != MPM_TRANSFER_APIC, affine = d.transfer != MPM_TRANSFER_FLIP;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < cl.n_verts;
        p += (long long)gridDim.x * blockDim.x) {
+    const int r = cl.cinv[p];
+    if (r < 0) continue;
+    float *rec = cl.crec + (long long)r * kClothRec;
     const float mass = cl.vm[p];
-    const float vp[3] = {cl.vv[3 * p], cl.vv[3 * p + 1], cl.vv[3 * p + 2]};
-    const float4 im4 = *imp4(cl, p);
-    const float im[3] = {im4.x, im4.y, im4.z};
-    float C[9];
+    const float4 im = *imp4(cl, p);
+    const float imv[3] = {im.x, im.y, im.z};
 #pragma unroll
-    for (int i = 0; i < 9; ++i) C[i] = affine ? cl.vC[9 * p + i] : 0.0f;
-    const Stencil1 s0 = stencil1(cl.vx[3 * p], inv_dx), s1 = stencil1(cl.vx[3 * p + 1], inv_dx),
-                   s2 = stencil1(cl.vx[3 * p + 2], inv_dx);
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
-        for (int k = 0; k < 3; ++k) {
-          const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
-          if (idx < 0) {
-            atomicOr(&d.cnt->status, ST_STENCIL);
-            continue;
-          }
-          const float W = s0.w[i] * s1.w[j] * s2.w[k];
-          const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
-          float mom[3];
+    for (int a = 0; a < 3; ++a) {
+      rec[a] = cl.vx[3 * p + a];
+      rec[4 + a] = mass * cl.vv[3 * p + a] + (flip_style ? 0.0f : imv[a]);
+      rec[25 + a] = flip_style ? imv[a] : 0.0f;
 #pragma unroll
-          for (int a = 0; a < 3; ++a) {
-            const float Cx = C[a * 3 + 0] * xi[0] + C[a * 3 + 1] * xi[1] + C[a * 3 + 2] * xi[2];
-            mom[a] = flip_style ? W * mass * (vp[a] + Cx) : W * (mass * (vp[a] + Cx) + im[a]);
-          }
-          float4 *g4 = d.grid + idx;
-          atomicAdd(g4, make_float4(W * mass, mom[0], mom[1], mom[2]));  // one 16-byte atomic
-          if (flip_style) {
-            float4 *h4 = d.grid2 + idx;
-            atomicAdd(h4, make_float4(W * im[0], W * im[1], W * im[2], 0.0f));
-          }
-        }
+      for (int c = 0; c < 3; ++c) {
+        rec[7 + a * 3 + c] = affine ? mass * cl.vC[9 * p + a * 3 + c] : 0.0f;
+        rec[16 + a * 3 + c] = 0.0f;
+      }
+    }
+    rec[3] = mass;
   }
 }
 
 // vertex bending springs (p2g_vert_bending_force, Transfer.cu:357-400): a
 // spring shorter than its rest length pushes its two vertices apart with
-// impulses -+ t^2 len k (1 - len / rl) dt along x1 - x0.  The reference
-// scatters each with its vertex's weights into the grid's "v" (vstar on FLIP
-// grids); adding it to the vertex's impulse, which the vertex P2G scatters
-// the same way, gives the same sums.
+// impulses -+ t^2 len k (1 - len / rl) dt along x1 - x0, into the spring's
+// two contribution slots.  The reference scatters each with its vertex's
+// weights into the grid's "v" (vstar on FLIP grids); adding it to the
+// vertex's impulse, which the vertex P2G scatters the same way, gives the
+// same sums.
 __global__ void k_cloth_bending(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
@@ -376,10 +355,202 @@ __global__ void k_cloth_bending(DevPtrs d) {
                          cl.vx[3 * a1 + 2] - cl.vx[3 * a0 + 2]};
     const float len = sqrtf(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
     const float rl = cl.srl[s];
-    if (!(len < rl) || len == 0.0f) continue;
+    float4 *ci = cl.cimp + 3 * cl.n_eles + 2 * s;
+    if (!(len < rl) || len == 0.0f) {
+      ci[0] = ci[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
     const float c = t2 * len * cl.sk[s] * (1.0f - len / rl) * dt / len;
-    atomicAdd(imp4(cl, a0), make_float4(-c * dv[0], -c * dv[1], -c * dv[2], 0.0f));
-    atomicAdd(imp4(cl, a1), make_float4(c * dv[0], c * dv[1], c * dv[2], 0.0f));
+    ci[0] = make_float4(-c * dv[0], -c * dv[1], -c * dv[2], 0.0f);
+    ci[1] = make_float4(c * dv[0], c * dv[1], c * dv[2], 0.0f);
+  }
+}
+
+// The cloth's points into the blocks of their own partition: key (block,
+// cell) per point, warp-aggregated counts per block (no grid blocks).
+__global__ void k_cloth_bin(DevPtrs d, DevPtrs dc) {
+  if (ZSMPM_HALTED(d)) return;
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const long long np = cl.n_verts + cl.n_eles;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < np; base += stride) {
+    const long long i = base + threadIdx.x;
+    int key = -1;
+    if (i < np) {
+      const float *x = i < cl.n_verts ? cl.vx + 3 * i : cl.ex + 3 * (i - cl.n_verts);
+      key = bin_key(S, x[0], x[1], x[2], &d.cnt->status);
+      cl.ckey[i] = key;
+    }
+    const int dd = key >> 6;  // -1 for none
+    const unsigned peers = __match_any_sync(0xffffffffu, dd);
+    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+      atomicAdd(&dc.dir_count[dd], __popc(peers));
+  }
+}
+
+// more cloth blocks than the cloth's block capacity: a capacity error of the
+// context (the points of the blocks left out would be lost)
+__global__ void k_cloth_status(DevPtrs d) {
+  if (threadIdx.x != 0) return;
+  if (d.cloth.ccnt->status & ST_CAPACITY) atomicOr(&d.cnt->status, ST_CAPACITY);
+  d.cloth.ccnt->status = 0;
+}
+
+// sorted position of every binned point (-1 before: not binned)
+__global__ void k_cloth_inverse(DevPtrs d) {
+  const ClothDev &cl = d.cloth;
+  const long long nb = min((long long)cl.ccnt->n_binned, cl.n_verts + cl.n_eles);
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nb;
+       s += (long long)gridDim.x * blockDim.x)
+    cl.cinv[cl.cperm[s]] = (int)s;
+}
+
+// One CTA per cloth block: each of the 216 threads owns a node of the
+// block's 6^3 tile and sums, in a fixed order (the 27 cells around the
+// node, then the points of each cell in sorted order), the record of every
+// point whose quadratic stencil covers it.
+constexpr int kClothTileThreads = 224;
+__global__ void __launch_bounds__(kClothTileThreads) k_cloth_tiles(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const float dx = S.dx, inv_dx = S.inv_dx;
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
+  __shared__ int ccount[64], cstart[65];
+  const int nb = min(cl.ccnt->n_buckets, cl.cap_cblocks);
+  const long long np = cl.n_verts + cl.n_eles;
+  const int t = threadIdx.x;
+  const int I = t / 36, J = (t / 6) % 6, Kz = t % 6;
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+    const int start = cl.cbk_start[b];
+    const int cnt = (int)max(0ll, min((long long)cl.cbk_count[b], np - start));
+    if (t < 64) ccount[t] = 0;
+    __syncthreads();
+    for (int j = t; j < cnt; j += kClothTileThreads)
+      atomicAdd(&ccount[cl.ckey[cl.cperm[start + j]] & 63], 1);
+    __syncthreads();
+    if (t < 32) {  // exclusive scan of the 64 cell counts (two per lane)
+      const int a = ccount[2 * t], c = ccount[2 * t + 1];
+      int sum = a + c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, sum, o);
+        if (t >= o) sum += u;
+      }
+      cstart[2 * t] = sum - a - c;
+      cstart[2 * t + 1] = sum - c;
+      if (t == 31) cstart[64] = sum;
+    }
+    __syncthreads();
+    if (t < kTileNodes) {
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f), h = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int cx = max(0, I - 2); cx <= min(3, I); ++cx)
+        for (int cy = max(0, J - 2); cy <= min(3, J); ++cy)
+          for (int cz = max(0, Kz - 2); cz <= min(3, Kz); ++cz) {
+            const int cell = sort_cell(cx, cy, cz);
+            const int o[3] = {I - cx, J - cy, Kz - cz};
+            for (int q = cstart[cell]; q < cstart[cell + 1]; ++q) {
+              const float4 *r4 = reinterpret_cast<const float4 *>(cl.crec + (long long)(start + q) * kClothRec);
+              const float4 x_m = r4[0], b_a0 = r4[1], a1 = r4[2], a2 = r4[3], q0 = r4[4],
+                           q1 = r4[5], q2 = r4[6];
+              // record: x0 x1 x2 m | b0 b1 b2 A00 | A01 A02 A10 A11 | A12 A20 A21 A22 |
+              //         Q00 Q01 Q02 Q10 | Q11 Q12 Q20 Q21 | Q22 b20 b21 b22
+              const Stencil1 s0 = stencil1(x_m.x, inv_dx), s1 = stencil1(x_m.y, inv_dx),
+                             s2 = stencil1(x_m.z, inv_dx);
+              const float w0 = s0.w[o[0]], w1 = s1.w[o[1]], w2 = s2.w[o[2]];
+              const float W = w0 * w1 * w2;
+              const float gw[3] = {wgrad(s0, o[0]) * w1 * w2 * inv_dx, w0 * wgrad(s1, o[1]) * w2 * inv_dx,
+                                   w0 * w1 * wgrad(s2, o[2]) * inv_dx};
+              const float xi[3] = {((float)o[0] - s0.f) * dx, ((float)o[1] - s1.f) * dx,
+                                   ((float)o[2] - s2.f) * dx};
+              const float bv[3] = {b_a0.x, b_a0.y, b_a0.z};
+              const float A[9] = {b_a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
+              const float Q[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+              const float b2[3] = {q2.y, q2.z, q2.w};
+              float mom[3], fo[3];
+#pragma unroll
+              for (int a = 0; a < 3; ++a) {
+                mom[a] = W * (bv[a] + A[a * 3] * xi[0] + A[a * 3 + 1] * xi[1] + A[a * 3 + 2] * xi[2]);
+                fo[a] = Q[a * 3] * gw[0] + Q[a * 3 + 1] * gw[1] + Q[a * 3 + 2] * gw[2];
+              }
+              g.x += W * x_m.w;
+              if (flip_style) {
+                g.y += mom[0];
+                g.z += mom[1];
+                g.w += mom[2];
+                h.x += fo[0] + W * b2[0];
+                h.y += fo[1] + W * b2[1];
+                h.z += fo[2] + W * b2[2];
+              } else {
+                g.y += mom[0] + fo[0];
+                g.z += mom[1] + fo[1];
+                g.w += mom[2] + fo[2];
+              }
+            }
+          }
+      cl.ctile[(long long)b * kTileNodes + t] = g;
+      if (flip_style) cl.ctile2[(long long)b * kTileNodes + t] = h;
+    }
+    __syncthreads();  // counts reused by the next block
+  }
+}
+
+// The cloth tiles into the grid the particle tiles were gathered into: per
+// active node the <= 8 tiles covering it, in the fixed order of the
+// particle gather.
+__global__ void k_cloth_grid_add(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
+  const ClothDev &cl = d.cloth;
+  const SceneParams &S = d.scn[0];
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
+  const int dy = S.block_dims[1], dz = S.block_dims[2];
+  const long long nn = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nn;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
+    const int gdir = d.gb_dir[gb];
+    const int ldir = gdir - S.dir_off;
+    const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
+    const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f), h = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool any = false;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
+      if ((o0 && (l0 >= 2 || c0 < 1)) || (o1 && (l1 >= 2 || c1 < 1)) || (o2 && (l2 >= 2 || c2 < 1)))
+        continue;
+      const int bk = cl.cdir_bk[gdir - (o0 * dy + o1) * dz - o2];
+      if (bk < 0 || bk >= cl.cap_cblocks) continue;
+      const long long ti =
+          (long long)bk * kTileNodes + ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2);
+      const float4 t = cl.ctile[ti];
+      g.x += t.x;
+      g.y += t.y;
+      g.z += t.z;
+      g.w += t.w;
+      if (flip_style) {
+        const float4 u = cl.ctile2[ti];
+        h.x += u.x;
+        h.y += u.y;
+        h.z += u.z;
+      }
+      any = true;
+    }
+    if (!any) continue;
+    float4 a = d.grid[idx];
+    a.x += g.x;
+    a.y += g.y;
+    a.z += g.z;
+    a.w += g.w;
+    d.grid[idx] = a;
+    if (flip_style) {
+      float4 u = d.grid2[idx];
+      u.x += h.x;
+      u.y += h.y;
+      u.z += h.z;
+      d.grid2[idx] = u;
+    }
   }
 }
 
@@ -736,11 +907,46 @@ void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
   k_cloth_mark<<<d.num_sms * 4, 256, 0, s>>>(d);
 }
 
+// The cloth's P2G into the grid that holds the particles' sums: its points'
+// own partition (the partition's scan, placement and sort on the cloth's
+// arrays), the element stresses, records and impulse slots, the per-vertex
+// impulse sums and records, the tiles, and the tiles into the grid.  No
+// float atomics: the result does not depend on the order threads run in.
 void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
-  cudaMemsetAsync(d.cloth.imp, 0, (size_t)d.cloth.n_verts * 4 * sizeof(float), s);
-  if (d.cloth.n_springs > 0) k_cloth_bending<<<d.num_sms * 4, 128, 0, s>>>(d);
-  k_cloth_p2g_elements<<<d.num_sms * 4, 128, 0, s>>>(d);
-  k_cloth_p2g_verts<<<d.num_sms * 4, 128, 0, s>>>(d);
+  const ClothDev &cl = d.cloth;
+  const long long np = cl.n_verts + cl.n_eles;
+  DevPtrs dc = d;
+  dc.pkey = cl.ckey;
+  dc.perm = cl.cperm;
+  dc.perm_tmp = cl.cperm_tmp;
+  dc.dir_count = cl.cdir_count;
+  dc.dir_fill = cl.cdir_fill;
+  dc.dir_flag = cl.cdir_flag;
+  dc.dir_gb = cl.cdir_gb;
+  dc.dir_bk = cl.cdir_bk;
+  dc.gb_dir = cl.cgb_dir;
+  dc.bk_dir = cl.cbk_dir;
+  dc.bk_start = cl.cbk_start;
+  dc.bk_count = cl.cbk_count;
+  dc.cap_gblocks = cl.cap_cblocks;
+  dc.tile_sums = cl.ctile_sums;
+  dc.cnt = cl.ccnt;
+  dc.prm = cl.cprm;
+  dc.cap = np;
+  const int g = d.num_sms * 4;
+  k_cloth_bin<<<g, 256, 0, s>>>(d, dc);
+  launch_scan(dc, s);
+  launch_scatter(dc, s);
+  launch_bucket_sort(dc, s);
+  k_cloth_status<<<1, 32, 0, s>>>(d);
+  cudaMemsetAsync(cl.cinv, 0xff, (size_t)np * sizeof(int32_t), s);  // -1: no record
+  k_cloth_inverse<<<g, 256, 0, s>>>(d);
+  if (cl.n_springs > 0) k_cloth_bending<<<g, 128, 0, s>>>(d);
+  k_cloth_elements<<<g, 128, 0, s>>>(d);
+  k_cloth_vertex_impulses<<<g, 128, 0, s>>>(d);
+  k_cloth_vertex_records<<<g, 128, 0, s>>>(d);
+  k_cloth_tiles<<<d.num_sms * 8, kClothTileThreads, 0, s>>>(d);
+  k_cloth_grid_add<<<d.num_sms * 8, 256, 0, s>>>(d);
 }
 
 void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s) {

@@ -203,7 +203,31 @@ struct ClothDev {
   int32_t *sv;
   float *sk, *srl;
   float thickness;
+  // Deterministic P2G.  The cloth's points (the vertices, then the
+  // elements) are partitioned into 4^3 blocks of their own each substep
+  // (keys, permutation and block lists below, through the partition's own
+  // scan, placement and sort); each point writes one scatter record at its
+  // sorted position, and each node of a block's 6^3 tile sums the records
+  // of the cells around it in a fixed order.  The element and spring
+  // impulses on the vertices are written per contribution slot (3 per
+  // element, 2 per spring) and summed per vertex in the fixed order of the
+  // vertex's slot list.
+  float *crec;                    // kClothRec floats per point, at its sorted position
+  float4 *cimp;                   // impulse contributions
+  int32_t *vptr, *vlist;          // per vertex: its contribution slots
+  int32_t *ckey, *cperm, *cperm_tmp, *cinv;  // key per point, sorted order and its inverse
+  int32_t *cdir_count, *cdir_fill, *cdir_gb, *cdir_bk, *cgb_dir, *ctile_sums;
+  uint8_t *cdir_flag;             // stays zero: the points make no grid blocks here
+  int32_t *cbk_dir, *cbk_start, *cbk_count;
+  int cap_cblocks;
+  float4 *ctile, *ctile2;         // per cloth block: its 216 node sums (ctile2: FLIP-style vstar)
+  Counters *ccnt;
+  SimParams *cprm;                // n = the number of points, no collider stepping
 };
+// floats of a cloth point's scatter record: x, m, b, A, Q, b2 -- the node
+// receives W m, W (b + A (x_i - x_p)) and Q grad W (momentum, or vstar on
+// FLIP-style grids), and W b2 in vstar
+constexpr int kClothRec = 28;
 
 // One scene of a context: its grid spacing, its slice of the concatenated
 // block directory, its boundary and gravity.  A context holds one scene
