@@ -1283,7 +1283,7 @@ int32_t alloc_cloth_p2g(mpm_ctx *c, ClothDev &cl, const std::vector<int32_t> &in
   int32_t rc;
   if ((rc = dalloc(c, &cl.crec, (size_t)np * kClothRec)) || (rc = dalloc(c, &cl.ckey, (size_t)np)) ||
       (rc = dalloc(c, &cl.cperm, (size_t)np)) || (rc = dalloc(c, &cl.cperm_tmp, (size_t)np)) ||
-      (rc = dalloc(c, &cl.cinv, (size_t)np)) || (rc = dalloc(c, &cl.cdir_count, (size_t)d.ndir)) ||
+      (rc = dalloc(c, &cl.cdir_count, (size_t)d.ndir)) ||
       (rc = dalloc(c, &cl.cdir_fill, (size_t)d.ndir)) || (rc = dalloc(c, &cl.cdir_gb, (size_t)d.ndir)) ||
       (rc = dalloc(c, &cl.cdir_bk, (size_t)d.ndir)) || (rc = dalloc(c, &cl.cdir_flag, (size_t)d.ndir)) ||
       (rc = dalloc(c, &cl.cgb_dir, (size_t)capb)) || (rc = dalloc(c, &cl.cbk_dir, (size_t)capb)) ||
@@ -1474,7 +1474,7 @@ int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
     return MPM_OK;
   };
   if ((rc = up(&nc.vx, vx)) || (rc = up(&nc.vv, vv)) || (rc = up(&nc.vC, vC)) || (rc = up(&nc.vm, vm)) ||
-      (rc = up(&nc.imp, std::vector<float>(4 * nv, 0.0f))) || (rc = up(&nc.ex, ex)) ||
+      (rc = up(&nc.ex, ex)) ||
       (rc = up(&nc.ev, ev)) || (rc = up(&nc.eC, eC)) || (rc = up(&nc.eF, eF)) || (rc = up(&nc.ed, ed)) ||
       (rc = up(&nc.eDmInv, eDi)) || (rc = up(&nc.em, em)) || (rc = up(&nc.evol, evol)) ||
       (rc = up(&nc.emu, emu)) || (rc = up(&nc.elam, elam)) ||

@@ -45,11 +45,6 @@ __device__ __forceinline__ long long node_of(const DevPtrs &d, const SceneParams
   return (long long)gb * 64 + (((i0 & 3) << 4) | ((i1 & 3) << 2) | (i2 & 3));
 }
 
-// a vertex's impulse sum (x, y, z, unused): one 16-byte atomic per update
-__device__ __forceinline__ float4 *imp4(const ClothDev &cl, long long v) {
-  return reinterpret_cast<float4 *>(cl.imp) + v;
-}
-
 // w' of the quadratic B-spline with respect to the particle position (cells)
 __device__ __forceinline__ float wgrad(const Stencil1 &s, int o) {
   return o == 0 ? s.f - 1.5f : (o == 1 ? -2.0f * (s.f - 1.0f) : s.f - 0.5f);
@@ -162,9 +157,9 @@ __global__ void k_cloth_mark(DevPtrs d) {
 }
 
 // Element P2G, first part: the element's stress, its scatter record (type i:
-// mass, momentum and the normal-direction force on its 27 nodes) at its
-// sorted position, and its type (ii) impulses on its vertices, one
-// contribution slot each (no atomics).
+// mass, momentum and the normal-direction force on its 27 nodes), and its
+// type (ii) impulses on its vertices, one contribution slot each (no
+// atomics).
 __global__ void k_cloth_elements(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
@@ -240,9 +235,8 @@ __global__ void k_cloth_elements(DevPtrs d) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) P[i] += T[i];
     const float mass = cl.em[e], vol = cl.evol[e];
-    const int r = cl.cinv[cl.n_verts + e];
-    if (r >= 0) {  // (a point outside the directory has no record; the status says so)
-      float *rec = cl.crec + (long long)r * kClothRec;
+    {
+      float *rec = cl.crec + (cl.n_verts + e) * kClothRec;
       const float kf = -vol * dt;
       const float dc1[3] = {dm[1], dm[4], dm[7]}, dc2[3] = {dm[2], dm[5], dm[8]};
 #pragma unroll
@@ -290,38 +284,25 @@ __global__ void k_cloth_elements(DevPtrs d) {
   }
 }
 
-// Vertex impulses: the contribution slots of each vertex (its elements in
-// index order, then its springs) summed in that fixed order.
-__global__ void k_cloth_vertex_impulses(DevPtrs d) {
-  if (ZSMPM_HALTED(d)) return;
-  const ClothDev &cl = d.cloth;
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < cl.n_verts;
-       v += (long long)gridDim.x * blockDim.x) {
-    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int j = cl.vptr[v]; j < cl.vptr[v + 1]; ++j) {
-      const float4 c = cl.cimp[cl.vlist[j]];
-      sum.x += c.x;
-      sum.y += c.y;
-      sum.z += c.z;
-    }
-    *imp4(cl, v) = sum;
-  }
-}
-
-// Vertex P2G records: mass, momentum m (v + C (x_i - x_p)) and the impulse
-// (in the momentum, or in vstar on FLIP-style grids).
+// Vertex P2G records: the vertex's impulse (its contribution slots -- its
+// elements in index order, then its springs -- summed in that order), mass,
+// momentum m (v + C (x_i - x_p)) and the impulse (in the momentum, or in
+// vstar on FLIP-style grids).
 __global__ void k_cloth_vertex_records(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const bool flip_style = d.transfer != MPM_TRANSFER_APIC, affine = d.transfer != MPM_TRANSFER_FLIP;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < cl.n_verts;
        p += (long long)gridDim.x * blockDim.x) {
-    const int r = cl.cinv[p];
-    if (r < 0) continue;
-    float *rec = cl.crec + (long long)r * kClothRec;
+    float imv[3] = {0.f, 0.f, 0.f};
+    for (int j = cl.vptr[p]; j < cl.vptr[p + 1]; ++j) {
+      const float4 c = cl.cimp[cl.vlist[j]];
+      imv[0] += c.x;
+      imv[1] += c.y;
+      imv[2] += c.z;
+    }
+    float *rec = cl.crec + p * kClothRec;
     const float mass = cl.vm[p];
-    const float4 im = *imp4(cl, p);
-    const float imv[3] = {im.x, im.y, im.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       rec[a] = cl.vx[3 * p + a];
@@ -397,31 +378,27 @@ __global__ void k_cloth_status(DevPtrs d) {
   d.cloth.ccnt->status = 0;
 }
 
-// sorted position of every binned point (-1 before: not binned)
-__global__ void k_cloth_inverse(DevPtrs d) {
-  const ClothDev &cl = d.cloth;
-  const long long nb = min((long long)cl.ccnt->n_binned, cl.n_verts + cl.n_eles);
-  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nb;
-       s += (long long)gridDim.x * blockDim.x)
-    cl.cinv[cl.cperm[s]] = (int)s;
-}
-
-// One CTA per cloth block: each of the 216 threads owns a node of the
-// block's 6^3 tile and sums, in a fixed order (the 27 cells around the
-// node, then the points of each cell in sorted order), the record of every
-// point whose quadratic stencil covers it.
-constexpr int kClothTileThreads = 224;
+// One CTA per cloth block, in two passes over shared memory.  First, for
+// each non-empty cell of the block and each of the 27 stencil offsets, the
+// sum over the cell's points in sorted order of their contributions to the
+// node at that offset (a work item is a cell and the offsets (o0, o1, *):
+// nine items per cell, each reading the cell's records once); then each of
+// the tile's 216 nodes adds the sums of the non-empty cells around it in a
+// fixed order.
+constexpr int kClothTileThreads = 192;
+constexpr int kClothCh = 7;  // m, momentum (3), vstar (3)
+constexpr int kClothTileSmem = 64 * 27 * kClothCh * (int)sizeof(float);
 __global__ void __launch_bounds__(kClothTileThreads) k_cloth_tiles(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
+  extern __shared__ float csum[];  // [64 cells][27 offsets][kClothCh]
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const float dx = S.dx, inv_dx = S.inv_dx;
   const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
-  __shared__ int ccount[64], cstart[65];
+  __shared__ int ccount[64], cstart[65], cells[64], n_cells;
   const int nb = min(cl.ccnt->n_buckets, cl.cap_cblocks);
   const long long np = cl.n_verts + cl.n_eles;
   const int t = threadIdx.x;
-  const int I = t / 36, J = (t / 6) % 6, Kz = t % 6;
   for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const int start = cl.cbk_start[b];
     const int cnt = (int)max(0ll, min((long long)cl.cbk_count[b], np - start));
@@ -430,7 +407,8 @@ __global__ void __launch_bounds__(kClothTileThreads) k_cloth_tiles(DevPtrs d) {
     for (int j = t; j < cnt; j += kClothTileThreads)
       atomicAdd(&ccount[cl.ckey[cl.cperm[start + j]] & 63], 1);
     __syncthreads();
-    if (t < 32) {  // exclusive scan of the 64 cell counts (two per lane)
+    if (t < 32) {  // exclusive scan of the 64 cell counts (two per lane), and
+                   // the list of the non-empty cells in cell order
       const int a = ccount[2 * t], c = ccount[2 * t + 1];
       int sum = a + c;
 #pragma unroll
@@ -441,58 +419,94 @@ __global__ void __launch_bounds__(kClothTileThreads) k_cloth_tiles(DevPtrs d) {
       cstart[2 * t] = sum - a - c;
       cstart[2 * t + 1] = sum - c;
       if (t == 31) cstart[64] = sum;
+      const int ne = (a > 0) + (c > 0);
+      int incl = ne;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (t >= o) incl += u;
+      }
+      int pos = incl - ne;
+      if (a > 0) cells[pos++] = 2 * t;
+      if (c > 0) cells[pos] = 2 * t + 1;
+      if (t == 31) n_cells = incl;
     }
     __syncthreads();
-    if (t < kTileNodes) {
+    // pass 1
+    for (int w = t; w < n_cells * 9; w += kClothTileThreads) {
+      const int cell = cells[w / 9], o0 = (w % 9) / 3, o1 = w % 3;
+      float acc[3][kClothCh];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int h = 0; h < kClothCh; ++h) acc[k][h] = 0.0f;
+      for (int q = cstart[cell]; q < cstart[cell + 1]; ++q) {
+        const float4 *r4 =
+            reinterpret_cast<const float4 *>(cl.crec + (long long)cl.cperm[start + q] * kClothRec);
+        const float4 x_m = r4[0], b_a0 = r4[1], a1 = r4[2], a2 = r4[3], q0 = r4[4], q1 = r4[5],
+                     q2 = r4[6];
+        // record: x0 x1 x2 m | b0 b1 b2 A00 | A01 A02 A10 A11 | A12 A20 A21 A22 |
+        //         Q00 Q01 Q02 Q10 | Q11 Q12 Q20 Q21 | Q22 b20 b21 b22
+        const Stencil1 s0 = stencil1(x_m.x, inv_dx), s1 = stencil1(x_m.y, inv_dx),
+                       s2 = stencil1(x_m.z, inv_dx);
+        const float bv[3] = {b_a0.x, b_a0.y, b_a0.z};
+        const float A[9] = {b_a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
+        const float Q[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+        const float b2[3] = {q2.y, q2.z, q2.w};
+        const float w01 = s0.w[o0] * s1.w[o1];
+        const float g0 = wgrad(s0, o0) * s1.w[o1] * inv_dx, g1 = s0.w[o0] * wgrad(s1, o1) * inv_dx;
+        const float xi0 = ((float)o0 - s0.f) * dx, xi1 = ((float)o1 - s1.f) * dx;
+#pragma unroll
+        for (int o2 = 0; o2 < 3; ++o2) {
+          const float w2 = s2.w[o2];
+          const float W = w01 * w2;
+          const float gw[3] = {g0 * w2, g1 * w2, w01 * wgrad(s2, o2) * inv_dx};
+          const float xi[3] = {xi0, xi1, ((float)o2 - s2.f) * dx};
+          float *a = acc[o2];
+          a[0] += W * x_m.w;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float mom = W * (bv[c] + A[c * 3] * xi[0] + A[c * 3 + 1] * xi[1] + A[c * 3 + 2] * xi[2]);
+            const float fo = Q[c * 3] * gw[0] + Q[c * 3 + 1] * gw[1] + Q[c * 3 + 2] * gw[2];
+            if (flip_style) {
+              a[1 + c] += mom;
+              a[4 + c] += fo + W * b2[c];
+            } else {
+              a[1 + c] += mom + fo;
+            }
+          }
+        }
+      }
+      float *dst = csum + (cell * 27 + o0 * 9 + o1 * 3) * kClothCh;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int h = 0; h < kClothCh; ++h) dst[k * kClothCh + h] = acc[k][h];
+    }
+    __syncthreads();
+    // pass 2: each node adds the sums of the non-empty cells around it, in order
+    for (int nd = t; nd < kTileNodes; nd += kClothTileThreads) {
+      const int I = nd / 36, J = (nd / 6) % 6, Kz = nd % 6;
       float4 g = make_float4(0.f, 0.f, 0.f, 0.f), h = make_float4(0.f, 0.f, 0.f, 0.f);
       for (int cx = max(0, I - 2); cx <= min(3, I); ++cx)
         for (int cy = max(0, J - 2); cy <= min(3, J); ++cy)
           for (int cz = max(0, Kz - 2); cz <= min(3, Kz); ++cz) {
             const int cell = sort_cell(cx, cy, cz);
-            const int o[3] = {I - cx, J - cy, Kz - cz};
-            for (int q = cstart[cell]; q < cstart[cell + 1]; ++q) {
-              const float4 *r4 = reinterpret_cast<const float4 *>(cl.crec + (long long)(start + q) * kClothRec);
-              const float4 x_m = r4[0], b_a0 = r4[1], a1 = r4[2], a2 = r4[3], q0 = r4[4],
-                           q1 = r4[5], q2 = r4[6];
-              // record: x0 x1 x2 m | b0 b1 b2 A00 | A01 A02 A10 A11 | A12 A20 A21 A22 |
-              //         Q00 Q01 Q02 Q10 | Q11 Q12 Q20 Q21 | Q22 b20 b21 b22
-              const Stencil1 s0 = stencil1(x_m.x, inv_dx), s1 = stencil1(x_m.y, inv_dx),
-                             s2 = stencil1(x_m.z, inv_dx);
-              const float w0 = s0.w[o[0]], w1 = s1.w[o[1]], w2 = s2.w[o[2]];
-              const float W = w0 * w1 * w2;
-              const float gw[3] = {wgrad(s0, o[0]) * w1 * w2 * inv_dx, w0 * wgrad(s1, o[1]) * w2 * inv_dx,
-                                   w0 * w1 * wgrad(s2, o[2]) * inv_dx};
-              const float xi[3] = {((float)o[0] - s0.f) * dx, ((float)o[1] - s1.f) * dx,
-                                   ((float)o[2] - s2.f) * dx};
-              const float bv[3] = {b_a0.x, b_a0.y, b_a0.z};
-              const float A[9] = {b_a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
-              const float Q[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
-              const float b2[3] = {q2.y, q2.z, q2.w};
-              float mom[3], fo[3];
-#pragma unroll
-              for (int a = 0; a < 3; ++a) {
-                mom[a] = W * (bv[a] + A[a * 3] * xi[0] + A[a * 3 + 1] * xi[1] + A[a * 3 + 2] * xi[2]);
-                fo[a] = Q[a * 3] * gw[0] + Q[a * 3 + 1] * gw[1] + Q[a * 3 + 2] * gw[2];
-              }
-              g.x += W * x_m.w;
-              if (flip_style) {
-                g.y += mom[0];
-                g.z += mom[1];
-                g.w += mom[2];
-                h.x += fo[0] + W * b2[0];
-                h.y += fo[1] + W * b2[1];
-                h.z += fo[2] + W * b2[2];
-              } else {
-                g.y += mom[0] + fo[0];
-                g.z += mom[1] + fo[1];
-                g.w += mom[2] + fo[2];
-              }
-            }
+            if (ccount[cell] == 0) continue;
+            const float *src =
+                csum + (cell * 27 + (I - cx) * 9 + (J - cy) * 3 + (Kz - cz)) * kClothCh;
+            g.x += src[0];
+            g.y += src[1];
+            g.z += src[2];
+            g.w += src[3];
+            h.x += src[4];
+            h.y += src[5];
+            h.z += src[6];
           }
-      cl.ctile[(long long)b * kTileNodes + t] = g;
-      if (flip_style) cl.ctile2[(long long)b * kTileNodes + t] = h;
+      cl.ctile[(long long)b * kTileNodes + nd] = g;
+      if (flip_style) cl.ctile2[(long long)b * kTileNodes + nd] = h;
     }
-    __syncthreads();  // counts reused by the next block
+    __syncthreads();  // counts, cells and sums reused by the next block
   }
 }
 
@@ -903,14 +917,18 @@ void launch_cloth_beta(const DevPtrs &d, float dt, int collider, cudaStream_t s)
   k_cloth_beta<<<d.num_sms * 4, 128, 0, s>>>(d, dt, collider);
 }
 
+void configure_cloth() {
+  cudaFuncSetAttribute(k_cloth_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, kClothTileSmem);
+}
+
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
   k_cloth_mark<<<d.num_sms * 4, 256, 0, s>>>(d);
 }
 
 // The cloth's P2G into the grid that holds the particles' sums: its points'
 // own partition (the partition's scan, placement and sort on the cloth's
-// arrays), the element stresses, records and impulse slots, the per-vertex
-// impulse sums and records, the tiles, and the tiles into the grid.  No
+// arrays), the element stresses, records and impulse slots, the vertex
+// records with their impulse sums, the tiles, and the tiles into the grid.  No
 // float atomics: the result does not depend on the order threads run in.
 void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
   const ClothDev &cl = d.cloth;
@@ -939,13 +957,10 @@ void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
   launch_scatter(dc, s);
   launch_bucket_sort(dc, s);
   k_cloth_status<<<1, 32, 0, s>>>(d);
-  cudaMemsetAsync(cl.cinv, 0xff, (size_t)np * sizeof(int32_t), s);  // -1: no record
-  k_cloth_inverse<<<g, 256, 0, s>>>(d);
   if (cl.n_springs > 0) k_cloth_bending<<<g, 128, 0, s>>>(d);
   k_cloth_elements<<<g, 128, 0, s>>>(d);
-  k_cloth_vertex_impulses<<<g, 128, 0, s>>>(d);
   k_cloth_vertex_records<<<g, 128, 0, s>>>(d);
-  k_cloth_tiles<<<d.num_sms * 8, kClothTileThreads, 0, s>>>(d);
+  k_cloth_tiles<<<d.num_sms * 4, kClothTileThreads, kClothTileSmem, s>>>(d);
   k_cloth_grid_add<<<d.num_sms * 8, 256, 0, s>>>(d);
 }
 

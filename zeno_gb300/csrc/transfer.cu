@@ -208,6 +208,7 @@ void configure_launches(DevPtrs &d) {
   d.g2p_threads = gt;
   d.grid_persist = persistent_grid(d);
   configure_adjoint();
+  configure_cloth();
 }
 
 template <int NT, int CH> void launch_p2g_shape(const DevPtrs &d, int cur, cudaStream_t s) {

@@ -192,7 +192,6 @@ struct ClothDev {
   int model;                 // MPM_FCR / MPM_NHK / MPM_STVK (curves: MPM_STVK)
   float gamma, k, fc, dc;    // shear stiffness, normal stiffness, tan(fa / pi), damping
   float *vx, *vv, *vC, *vm;
-  float *imp;  // per vertex (x, y, z, unused): the impulse sums of a P2G
   float *vbeta;     // ComputeParticleBeta per vertex (FLIP-style position update)
   int32_t *vowner;  // scratch of the beta pass: the last element of each vertex
   float *ex, *ev, *eC, *eF, *ed, *eDmInv, *em, *evol, *emu, *elam;
@@ -206,16 +205,16 @@ struct ClothDev {
   // Deterministic P2G.  The cloth's points (the vertices, then the
   // elements) are partitioned into 4^3 blocks of their own each substep
   // (keys, permutation and block lists below, through the partition's own
-  // scan, placement and sort); each point writes one scatter record at its
-  // sorted position, and each node of a block's 6^3 tile sums the records
-  // of the cells around it in a fixed order.  The element and spring
+  // scan, placement and sort); each point writes one scatter record, and
+  // the nodes of a block's 6^3 tile take the records of the cells around
+  // them in a fixed order (cells, then points in sorted order).  The element and spring
   // impulses on the vertices are written per contribution slot (3 per
   // element, 2 per spring) and summed per vertex in the fixed order of the
   // vertex's slot list.
-  float *crec;                    // kClothRec floats per point, at its sorted position
+  float *crec;                    // kClothRec floats per point
   float4 *cimp;                   // impulse contributions
   int32_t *vptr, *vlist;          // per vertex: its contribution slots
-  int32_t *ckey, *cperm, *cperm_tmp, *cinv;  // key per point, sorted order and its inverse
+  int32_t *ckey, *cperm, *cperm_tmp;  // key per point, sorted order
   int32_t *cdir_count, *cdir_fill, *cdir_gb, *cdir_bk, *cgb_dir, *ctile_sums;
   uint8_t *cdir_flag;             // stays zero: the points make no grid blocks here
   int32_t *cbk_dir, *cbk_start, *cbk_count;
@@ -408,6 +407,8 @@ void launch_grid_adjoint(const DevPtrs &d, cudaStream_t s);
 // the adjoint kernels' launch attributes on the current device (once per
 // context, outside any stream capture)
 void configure_adjoint();
+// cloth.cu: the same for the cloth's tile kernel
+void configure_cloth();
 void launch_p2g_adjoint(const DevPtrs &d, int cur, float *ap, float *gmu, float *glam, long long n,
                         cudaStream_t s);
 
