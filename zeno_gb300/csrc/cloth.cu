@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include "binning.cuh"
+#include "cp_async.cuh"
 #include "colliders.cuh"
 #include "mpm_math.cuh"
 #include "zsmpm_internal.cuh"
@@ -156,6 +157,24 @@ __global__ void k_cloth_mark(DevPtrs d) {
   }
 }
 
+// a point's scatter record at its sorted position, as seven 16-byte stores
+__device__ __forceinline__ void store_record(const ClothDev &cl, int pos, const float (&r)[kClothRec]) {
+  float4 *dst = reinterpret_cast<float4 *>(cl.crec) + (long long)pos * (kClothRec / 4);
+#pragma unroll
+  for (int k = 0; k < kClothRec / 4; ++k)
+    dst[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+}
+
+// each binned point's sorted position (the inverse of the permutation)
+__global__ void k_cloth_inverse(DevPtrs d) {
+  if (ZSMPM_HALTED(d)) return;
+  const ClothDev &cl = d.cloth;
+  const long long nb = min((long long)cl.ccnt->n_binned, cl.n_verts + cl.n_eles);
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nb;
+       s += (long long)gridDim.x * blockDim.x)
+    cl.cperm_tmp[cl.cperm[s]] = (int)s;
+}
+
 // Element P2G, first part: the element's stress, its scatter record (type i:
 // mass, momentum and the normal-direction force on its 27 nodes), and its
 // type (ii) impulses on its vertices, one contribution slot each (no
@@ -235,24 +254,25 @@ __global__ void k_cloth_elements(DevPtrs d) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) P[i] += T[i];
     const float mass = cl.em[e], vol = cl.evol[e];
-    {
-      float *rec = cl.crec + (cl.n_verts + e) * kClothRec;
+    if (cl.ckey[cl.n_verts + e] >= 0) {  // a binned point: its record at its sorted position
       const float kf = -vol * dt;
       const float dc1[3] = {dm[1], dm[4], dm[7]}, dc2[3] = {dm[2], dm[5], dm[8]};
+      float r[kClothRec];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        rec[a] = cl.ex[3 * e + a];
-        rec[4 + a] = mass * cl.ev[3 * e + a];
-        rec[25 + a] = 0.0f;
+        r[a] = cl.ex[3 * e + a];
+        r[4 + a] = mass * cl.ev[3 * e + a];
+        r[25 + a] = 0.0f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          rec[7 + a * 3 + c] = affine ? mass * cl.eC[9 * e + a * 3 + c] : 0.0f;
+          r[7 + a * 3 + c] = affine ? mass * cl.eC[9 * e + a * 3 + c] : 0.0f;
           // surface: P_c3 (grad W . d_c3); curve: P_c2 (grad W . d_c2) too
-          rec[16 + a * 3 + c] =
+          r[16 + a * 3 + c] =
               kf * ((curve ? P[a * 3 + 1] * dc1[c] : 0.0f) + P[a * 3 + 2] * dc2[c]);
         }
       }
-      rec[3] = mass;
+      r[3] = mass;
+      store_record(cl, cl.cperm_tmp[cl.n_verts + e], r);
     }
     float4 *ci = cl.cimp + 3 * e;
     if (curve) {  // type (ii): +-vol dt P_c0 DmInv00 on the two vertices
@@ -294,27 +314,39 @@ __global__ void k_cloth_vertex_records(DevPtrs d) {
   const bool flip_style = d.transfer != MPM_TRANSFER_APIC, affine = d.transfer != MPM_TRANSFER_FLIP;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < cl.n_verts;
        p += (long long)gridDim.x * blockDim.x) {
+    if (cl.ckey[p] < 0) continue;  // not binned: no record
     float imv[3] = {0.f, 0.f, 0.f};
-    for (int j = cl.vptr[p]; j < cl.vptr[p + 1]; ++j) {
-      const float4 c = cl.cimp[cl.vlist[j]];
-      imv[0] += c.x;
-      imv[1] += c.y;
-      imv[2] += c.z;
+    const int je = cl.vptr[p + 1];
+    for (int j = cl.vptr[p]; j < je; j += 4) {  // four slots' loads in flight, summed in order
+      int sl[4];
+      float4 c[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) sl[u] = j + u < je ? cl.vlist[j + u] : -1;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) c[u] = sl[u] >= 0 ? cl.cimp[sl[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (sl[u] >= 0) {
+          imv[0] += c[u].x;
+          imv[1] += c[u].y;
+          imv[2] += c[u].z;
+        }
     }
-    float *rec = cl.crec + p * kClothRec;
     const float mass = cl.vm[p];
+    float r[kClothRec];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      rec[a] = cl.vx[3 * p + a];
-      rec[4 + a] = mass * cl.vv[3 * p + a] + (flip_style ? 0.0f : imv[a]);
-      rec[25 + a] = flip_style ? imv[a] : 0.0f;
+      r[a] = cl.vx[3 * p + a];
+      r[4 + a] = mass * cl.vv[3 * p + a] + (flip_style ? 0.0f : imv[a]);
+      r[25 + a] = flip_style ? imv[a] : 0.0f;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        rec[7 + a * 3 + c] = affine ? mass * cl.vC[9 * p + a * 3 + c] : 0.0f;
-        rec[16 + a * 3 + c] = 0.0f;
+        r[7 + a * 3 + c] = affine ? mass * cl.vC[9 * p + a * 3 + c] : 0.0f;
+        r[16 + a * 3 + c] = 0.0f;
       }
     }
-    rec[3] = mass;
+    r[3] = mass;
+    store_record(cl, cl.cperm_tmp[p], r);
   }
 }
 
@@ -374,41 +406,105 @@ __global__ void k_cloth_bin(DevPtrs d, DevPtrs dc) {
 // context (the points of the blocks left out would be lost)
 __global__ void k_cloth_status(DevPtrs d) {
   if (threadIdx.x != 0) return;
-  if (d.cloth.ccnt->status & ST_CAPACITY) atomicOr(&d.cnt->status, ST_CAPACITY);
-  d.cloth.ccnt->status = 0;
+  Counters *cc = d.cloth.ccnt;
+  if ((cc->status & ST_CAPACITY) || cc->max_buckets > d.cloth.cap_cblocks)
+    atomicOr(&d.cnt->status, ST_CAPACITY);
+  cc->status = 0;
+  cc->max_buckets = 0;
 }
 
-// One CTA per cloth block, in two passes over shared memory.  First, for
-// each non-empty cell of the block and each of the 27 stencil offsets, the
-// sum over the cell's points in sorted order of their contributions to the
-// node at that offset (a work item is a cell and the offsets (o0, o1, *):
-// nine items per cell, each reading the cell's records once); then each of
-// the tile's 216 nodes adds the sums of the non-empty cells around it in a
-// fixed order.
+// One CTA per cloth block at a time, in two passes over shared memory.
+// First, for each non-empty cell of the block and each of the 27 stencil
+// offsets, the sum over the cell's points in sorted order of their
+// contributions to the node at that offset (a work item is a cell and the
+// offsets (o0, o1, *): nine items per cell, each reading the cell's records
+// once); then each of the tile's 216 nodes adds the sums of the non-empty
+// cells around it in cell order.  The records lie in sorted order, so a
+// block's records are one contiguous run: they are staged in shared memory
+// in chunks of kClothStage points with cp.async, the next chunk (of this
+// block or the CTA's next one) in flight while the current one computes.  A
+// cell that spans two chunks carries its sums over in shared memory, which
+// adds in the same order as one pass would.  kFlip: the grids take vstar
+// (FLIP-style transfers), seven sums per node instead of four.
 constexpr int kClothTileThreads = 192;
-constexpr int kClothCh = 7;  // m, momentum (3), vstar (3)
-constexpr int kClothTileSmem = 64 * 27 * kClothCh * (int)sizeof(float);
-__global__ void __launch_bounds__(kClothTileThreads) k_cloth_tiles(DevPtrs d) {
+constexpr int kClothStage = 192;
+constexpr int kClothStageF4 = kClothStage * (kClothRec / 4);
+__host__ __device__ constexpr int cloth_tile_smem(bool flip) {
+  return (2 * kClothStageF4 * 4 + 64 * 27 * (flip ? 7 : 4)) * (int)sizeof(float);
+}
+
+// the quadratic B-spline weight of node o (0, 1, 2) at fractional offset f
+// (cells from the stencil's base) as a (f - b)^2 + c, and its derivative
+// e (f - b); stencil1 and wgrad give the same values
+struct SplineRow {
+  float a, b, c, e;
+};
+__device__ __forceinline__ SplineRow spline_row(int o) {
+  return o == 1 ? SplineRow{-1.0f, 1.0f, 0.75f, -2.0f}
+                : SplineRow{0.5f, o == 0 ? 1.5f : 0.5f, 0.0f, 1.0f};
+}
+
+template <bool kFlip>
+__global__ void __launch_bounds__(kClothTileThreads, 3) k_cloth_tiles(DevPtrs d) {
+  constexpr int ch = kFlip ? 7 : 4;  // m, momentum (3)[, vstar (3)]
   if (ZSMPM_HALTED(d)) return;
-  extern __shared__ float csum[];  // [64 cells][27 offsets][kClothCh]
+  // two staging buffers of [kClothStage][7] float4, then the sums [64][27][ch]
+  extern __shared__ float4 csmem[];
+  float *csum = reinterpret_cast<float *>(csmem + 2 * kClothStageF4);
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const float dx = S.dx, inv_dx = S.inv_dx;
-  const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
-  __shared__ int ccount[64], cstart[65], cells[64], n_cells;
+  __shared__ int ccount[64], cstart[65], cells[64], n_cells, carry_cell, last_cell;
+  __shared__ unsigned long long cmask;  // the block's non-empty cells so far
   const int nb = min(cl.ccnt->n_buckets, cl.cap_cblocks);
   const long long np = cl.n_verts + cl.n_eles;
   const int t = threadIdx.x;
-  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    const int start = cl.cbk_start[b];
-    const int cnt = (int)max(0ll, min((long long)cl.cbk_count[b], np - start));
+  const float4 *crec4 = reinterpret_cast<const float4 *>(cl.crec);
+  auto block_range = [&](int bb, int &st, int &n) {
+    st = cl.cbk_start[bb];
+    n = (int)max(0ll, min((long long)cl.cbk_count[bb], np - st));
+  };
+  auto issue = [&](float4 *buf, int first, int len) {
+    const float4 *src = crec4 + (long long)first * (kClothRec / 4);
+    for (int j = t; j < len * (kClothRec / 4); j += kClothTileThreads) cp_async16(buf + j, src + j);
+  };
+  int b = blockIdx.x, c0 = 0, start = 0, cnt = 0;
+  if (b < nb) {
+    block_range(b, start, cnt);
+    issue(csmem, start, min(kClothStage, cnt));
+  }
+  cp_async_commit();
+  for (int it = 0; b < nb; ++it) {
+    // the next chunk: of this block, or of the CTA's next block
+    int nbk = b, nc0 = c0 + kClothStage, nstart = start, ncnt = cnt;
+    if (nc0 >= cnt) {
+      nbk = b + gridDim.x;
+      nc0 = 0;
+      if (nbk < nb) block_range(nbk, nstart, ncnt);
+    }
+    if (nbk < nb) issue(csmem + ((it + 1) & 1) * kClothStageF4, nstart + nc0, min(kClothStage, ncnt - nc0));
+    cp_async_commit();
+    float4 *rec = csmem + (it & 1) * kClothStageF4;
+    const int len = min(kClothStage, cnt - c0);
     if (t < 64) ccount[t] = 0;
+    cp_async_wait<1>();  // this chunk's copies (the next chunk's may be pending)
     __syncthreads();
-    for (int j = t; j < cnt; j += kClothTileThreads)
-      atomicAdd(&ccount[cl.ckey[cl.cperm[start + j]] & 63], 1);
+    // the chunk's cell counts, from its points' positions (the key's cell);
+    // each position becomes its offset from the stencil base (in cells)
+    for (int r = t; r < len; r += kClothTileThreads) {
+      float4 x = rec[r * (kClothRec / 4)];
+      const int b0 = particle_base(x.x, inv_dx), b1 = particle_base(x.y, inv_dx),
+                b2 = particle_base(x.z, inv_dx);
+      atomicAdd(&ccount[sort_cell(b0 & 3, b1 & 3, b2 & 3)], 1);
+      x.x = __fsub_rn(__fmul_rn(x.x, inv_dx), (float)b0);
+      x.y = __fsub_rn(__fmul_rn(x.y, inv_dx), (float)b1);
+      x.z = __fsub_rn(__fmul_rn(x.z, inv_dx), (float)b2);
+      rec[r * (kClothRec / 4)] = x;
+    }
     __syncthreads();
-    if (t < 32) {  // exclusive scan of the 64 cell counts (two per lane), and
-                   // the list of the non-empty cells in cell order
+    if (t < 32) {  // exclusive scan of the 64 cell counts (two per lane), the
+                   // list of the chunk's non-empty cells in cell order, the
+                   // cell continued from the block's previous chunk
       const int a = ccount[2 * t], c = ccount[2 * t + 1];
       int sum = a + c;
 #pragma unroll
@@ -429,85 +525,108 @@ __global__ void __launch_bounds__(kClothTileThreads) k_cloth_tiles(DevPtrs d) {
       int pos = incl - ne;
       if (a > 0) cells[pos++] = 2 * t;
       if (c > 0) cells[pos] = 2 * t + 1;
-      if (t == 31) n_cells = incl;
+      const unsigned lo = __ballot_sync(0xffffffffu, a > 0), hi = __ballot_sync(0xffffffffu, c > 0);
+      __syncwarp();
+      if (t == 31) {
+        unsigned long long bits = 0;
+        for (int k = 0; k < 32; ++k)
+          bits |= (unsigned long long)((lo >> k) & 1u) << (2 * k) |
+                  (unsigned long long)((hi >> k) & 1u) << (2 * k + 1);
+        n_cells = incl;
+        carry_cell = c0 > 0 ? last_cell : -1;
+        cmask = c0 > 0 ? (cmask | bits) : bits;
+        if (incl > 0) last_cell = cells[incl - 1];
+      }
     }
     __syncthreads();
-    // pass 1
+    // pass 1 over the chunk's cells
     for (int w = t; w < n_cells * 9; w += kClothTileThreads) {
       const int cell = cells[w / 9], o0 = (w % 9) / 3, o1 = w % 3;
-      float acc[3][kClothCh];
+      float *dst = csum + (cell * 27 + o0 * 9 + o1 * 3) * ch;
+      const bool carry = cell == carry_cell;  // begun in the block's previous chunk
+      float acc[3][ch];
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int h = 0; h < kClothCh; ++h) acc[k][h] = 0.0f;
+        for (int h = 0; h < ch; ++h) acc[k][h] = carry ? dst[k * ch + h] : 0.0f;
+      const SplineRow r0 = spline_row(o0), r1 = spline_row(o1);
+      const float e0 = r0.e * inv_dx, e1 = r1.e * inv_dx, od0 = (float)o0, od1 = (float)o1;
       for (int q = cstart[cell]; q < cstart[cell + 1]; ++q) {
-        const float4 *r4 =
-            reinterpret_cast<const float4 *>(cl.crec + (long long)cl.cperm[start + q] * kClothRec);
-        const float4 x_m = r4[0], b_a0 = r4[1], a1 = r4[2], a2 = r4[3], q0 = r4[4], q1 = r4[5],
-                     q2 = r4[6];
-        // record: x0 x1 x2 m | b0 b1 b2 A00 | A01 A02 A10 A11 | A12 A20 A21 A22 |
+        const float4 *r4 = rec + q * (kClothRec / 4);
+        // record: f0 f1 f2 m | b0 b1 b2 A00 | A01 A02 A10 A11 | A12 A20 A21 A22 |
         //         Q00 Q01 Q02 Q10 | Q11 Q12 Q20 Q21 | Q22 b20 b21 b22
-        const Stencil1 s0 = stencil1(x_m.x, inv_dx), s1 = stencil1(x_m.y, inv_dx),
-                       s2 = stencil1(x_m.z, inv_dx);
+        const float4 f_m = r4[0], b_a0 = r4[1], a1 = r4[2], a2 = r4[3], q0 = r4[4], q1 = r4[5],
+                     q2 = r4[6];
         const float bv[3] = {b_a0.x, b_a0.y, b_a0.z};
         const float A[9] = {b_a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
         const float Q[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
-        const float b2[3] = {q2.y, q2.z, q2.w};
-        const float w01 = s0.w[o0] * s1.w[o1];
-        const float g0 = wgrad(s0, o0) * s1.w[o1] * inv_dx, g1 = s0.w[o0] * wgrad(s1, o1) * inv_dx;
-        const float xi0 = ((float)o0 - s0.f) * dx, xi1 = ((float)o1 - s1.f) * dx;
+        const float t0 = f_m.x - r0.b, t1 = f_m.y - r1.b;
+        const float w0 = r0.a * t0 * t0 + r0.c, w1 = r1.a * t1 * t1 + r1.c;
+        const float w01 = w0 * w1;
+        const float g0 = e0 * t0 * w1, g1 = w0 * e1 * t1;
+        const float xi0 = (od0 - f_m.x) * dx, xi1 = (od1 - f_m.y) * dx;
+        const float f2 = f_m.z;
 #pragma unroll
         for (int o2 = 0; o2 < 3; ++o2) {
-          const float w2 = s2.w[o2];
+          const SplineRow r2 = spline_row(o2);
+          const float t2 = f2 - r2.b;
+          const float w2 = r2.a * t2 * t2 + r2.c;
           const float W = w01 * w2;
-          const float gw[3] = {g0 * w2, g1 * w2, w01 * wgrad(s2, o2) * inv_dx};
-          const float xi[3] = {xi0, xi1, ((float)o2 - s2.f) * dx};
+          const float gw[3] = {g0 * w2, g1 * w2, w01 * (r2.e * inv_dx) * t2};
+          const float xi[3] = {xi0, xi1, ((float)o2 - f2) * dx};
           float *a = acc[o2];
-          a[0] += W * x_m.w;
+          a[0] += W * f_m.w;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const float mom = W * (bv[c] + A[c * 3] * xi[0] + A[c * 3 + 1] * xi[1] + A[c * 3 + 2] * xi[2]);
+            const float mom =
+                W * (bv[c] + A[c * 3] * xi[0] + A[c * 3 + 1] * xi[1] + A[c * 3 + 2] * xi[2]);
             const float fo = Q[c * 3] * gw[0] + Q[c * 3 + 1] * gw[1] + Q[c * 3 + 2] * gw[2];
-            if (flip_style) {
+            if constexpr (kFlip) {
+              const float b2v = c == 0 ? q2.y : (c == 1 ? q2.z : q2.w);
               a[1 + c] += mom;
-              a[4 + c] += fo + W * b2[c];
+              a[4 + c] += fo + W * b2v;
             } else {
               a[1 + c] += mom + fo;
             }
           }
         }
       }
-      float *dst = csum + (cell * 27 + o0 * 9 + o1 * 3) * kClothCh;
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int h = 0; h < kClothCh; ++h) dst[k * kClothCh + h] = acc[k][h];
+        for (int h = 0; h < ch; ++h) dst[k * ch + h] = acc[k][h];
     }
-    __syncthreads();
-    // pass 2: each node adds the sums of the non-empty cells around it, in order
-    for (int nd = t; nd < kTileNodes; nd += kClothTileThreads) {
-      const int I = nd / 36, J = (nd / 6) % 6, Kz = nd % 6;
-      float4 g = make_float4(0.f, 0.f, 0.f, 0.f), h = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int cx = max(0, I - 2); cx <= min(3, I); ++cx)
-        for (int cy = max(0, J - 2); cy <= min(3, J); ++cy)
-          for (int cz = max(0, Kz - 2); cz <= min(3, Kz); ++cz) {
-            const int cell = sort_cell(cx, cy, cz);
-            if (ccount[cell] == 0) continue;
-            const float *src =
-                csum + (cell * 27 + (I - cx) * 9 + (J - cy) * 3 + (Kz - cz)) * kClothCh;
-            g.x += src[0];
-            g.y += src[1];
-            g.z += src[2];
-            g.w += src[3];
-            h.x += src[4];
-            h.y += src[5];
-            h.z += src[6];
-          }
-      cl.ctile[(long long)b * kTileNodes + nd] = g;
-      if (flip_style) cl.ctile2[(long long)b * kTileNodes + nd] = h;
+    if (c0 + kClothStage >= cnt) {  // the block's last chunk
+      __syncthreads();
+      // pass 2: each node adds the sums of the non-empty cells around it,
+      // in cell order
+      const unsigned long long mask = cmask;
+      for (int nd = t; nd < kTileNodes; nd += kClothTileThreads) {
+        const int I = nd / 36, J = (nd / 6) % 6, Kz = nd % 6;
+        float g[ch];
+#pragma unroll
+        for (int h = 0; h < ch; ++h) g[h] = 0.0f;
+        for (unsigned long long m = mask; m; m &= m - 1) {
+          const int cell = __ffsll((long long)m) - 1;
+          const unsigned o0 = (unsigned)(I - ((cell >> 2) & 3)), o1 = (unsigned)(J - (cell & 3)),
+                         o2 = (unsigned)(Kz - (cell >> 4));
+          if (o0 > 2u || o1 > 2u || o2 > 2u) continue;
+          const float *src = csum + (cell * 27 + o0 * 9 + o1 * 3 + o2) * ch;
+#pragma unroll
+          for (int h = 0; h < ch; ++h) g[h] += src[h];
+        }
+        cl.ctile[(long long)b * kTileNodes + nd] = make_float4(g[0], g[1], g[2], g[3]);
+        if constexpr (kFlip)
+          cl.ctile2[(long long)b * kTileNodes + nd] = make_float4(g[4], g[5], g[6], 0.0f);
+      }
     }
-    __syncthreads();  // counts, cells and sums reused by the next block
+    __syncthreads();  // the chunk's buffer, counts and sums are read no more
+    b = nbk;
+    c0 = nc0;
+    start = nstart;
+    cnt = ncnt;
   }
+  cp_async_wait<0>();
 }
 
 // The cloth tiles into the grid the particle tiles were gathered into: per
@@ -579,14 +698,42 @@ __device__ __forceinline__ void cloth_gather(const DevPtrs &d, const SceneParams
   for (int a = 0; a < 3; ++a) vel[a] = vs[a] = 0.0f;
 #pragma unroll
   for (int i = 0; i < 9; ++i) Cn[i] = 0.0f;
+  // the grid blocks of the (up to) 2 x 2 x 2 blocks the stencil touches,
+  // looked up first, so that the 27 node loads below are all in flight
+  const int l0 = s0.base & 3, l1 = s1.base & 3, l2 = s2.base & 3;
+  const int bb0 = (s0.base >> 2) - S.block_lo[0], bb1 = (s1.base >> 2) - S.block_lo[1],
+            bb2 = (s2.base >> 2) - S.block_lo[2];
+  const int dy = S.block_dims[1], dz = S.block_dims[2];
+  int gbk[8];
+#pragma unroll
+  for (int o = 0; o < 8; ++o) {
+    const int a0 = o >> 2, a1 = (o >> 1) & 1, a2 = o & 1;
+    const int c0 = bb0 + a0, c1 = bb1 + a1, c2 = bb2 + a2;
+    int gb = -1;
+    if ((!a0 || l0 >= 2) && (!a1 || l1 >= 2) && (!a2 || l2 >= 2) &&
+        (unsigned)c0 < (unsigned)S.block_dims[0] && (unsigned)c1 < (unsigned)dy &&
+        (unsigned)c2 < (unsigned)dz) {
+      gb = d.dir_gb[S.dir_off + (c0 * dy + c1) * dz + c2];
+      if (gb >= d.cap_gblocks) gb = -1;
+    }
+    gbk[o] = gb;
+  }
+#pragma unroll
   for (int i = 0; i < 3; ++i)
+#pragma unroll
     for (int j = 0; j < 3; ++j)
+#pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const long long idx = node_of(d, S, s0.base + i, s1.base + j, s2.base + k);
-        if (idx < 0) {
+        const int n0 = l0 + i, n1 = l1 + j, n2 = l2 + k;
+        const int h0 = n0 >> 2, h1 = n1 >> 2, h2 = n2 >> 2;
+        // (selects, not a runtime index: the lookups stay in registers)
+        const int gb = h0 ? (h1 ? (h2 ? gbk[7] : gbk[6]) : (h2 ? gbk[5] : gbk[4]))
+                          : (h1 ? (h2 ? gbk[3] : gbk[2]) : (h2 ? gbk[1] : gbk[0]));
+        if (gb < 0) {
           atomicOr(&d.cnt->status, ST_STENCIL);
           continue;
         }
+        const long long idx = (long long)gb * 64 + (((n0 & 3) << 4) | ((n1 & 3) << 2) | (n2 & 3));
         const float W = s0.w[i] * s1.w[j] * s2.w[k];
         const float xi[3] = {((float)i - s0.f) * dx, ((float)j - s1.f) * dx, ((float)k - s2.f) * dx};
         const float4 g = d.grid[idx];
@@ -918,7 +1065,10 @@ void launch_cloth_beta(const DevPtrs &d, float dt, int collider, cudaStream_t s)
 }
 
 void configure_cloth() {
-  cudaFuncSetAttribute(k_cloth_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, kClothTileSmem);
+  cudaFuncSetAttribute(k_cloth_tiles<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       cloth_tile_smem(false));
+  cudaFuncSetAttribute(k_cloth_tiles<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       cloth_tile_smem(true));
 }
 
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
@@ -958,9 +1108,14 @@ void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
   launch_bucket_sort(dc, s);
   k_cloth_status<<<1, 32, 0, s>>>(d);
   if (cl.n_springs > 0) k_cloth_bending<<<g, 128, 0, s>>>(d);
+  k_cloth_inverse<<<g, 256, 0, s>>>(d);
   k_cloth_elements<<<g, 128, 0, s>>>(d);
   k_cloth_vertex_records<<<g, 128, 0, s>>>(d);
-  k_cloth_tiles<<<d.num_sms * 4, kClothTileThreads, kClothTileSmem, s>>>(d);
+  const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
+  if (flip_style)
+    k_cloth_tiles<true><<<d.num_sms * 2, kClothTileThreads, cloth_tile_smem(true), s>>>(d);
+  else
+    k_cloth_tiles<false><<<d.num_sms * 3, kClothTileThreads, cloth_tile_smem(false), s>>>(d);
   k_cloth_grid_add<<<d.num_sms * 8, 256, 0, s>>>(d);
 }
 

@@ -211,10 +211,12 @@ struct ClothDev {
   // impulses on the vertices are written per contribution slot (3 per
   // element, 2 per spring) and summed per vertex in the fixed order of the
   // vertex's slot list.
-  float *crec;                    // kClothRec floats per point
+  float *crec;                    // kClothRec floats per point, in sorted order
   float4 *cimp;                   // impulse contributions
   int32_t *vptr, *vlist;          // per vertex: its contribution slots
-  int32_t *ckey, *cperm, *cperm_tmp;  // key per point, sorted order
+  // key per point, sorted order; cperm_tmp is the sort's scratch, then the
+  // inverse permutation (each point's sorted position, where its record goes)
+  int32_t *ckey, *cperm, *cperm_tmp;
   int32_t *cdir_count, *cdir_fill, *cdir_gb, *cdir_bk, *cgb_dir, *ctile_sums;
   uint8_t *cdir_flag;             // stays zero: the points make no grid blocks here
   int32_t *cbk_dir, *cbk_start, *cbk_count;
