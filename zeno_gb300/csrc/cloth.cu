@@ -24,6 +24,8 @@
 // (MPMPipeline.cu:1012-1093).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "binning.cuh"
 #include "cp_async.cuh"
 #include "colliders.cuh"
@@ -426,7 +428,7 @@ __global__ void k_cloth_status(DevPtrs d) {
 // cell that spans two chunks carries its sums over in shared memory, which
 // adds in the same order as one pass would.  kFlip: the grids take vstar
 // (FLIP-style transfers), seven sums per node instead of four.
-constexpr int kClothTileThreads = 192;
+constexpr int kClothTileThreads = 224;  // the 216 nodes of pass 2 in one round
 constexpr int kClothStage = 192;
 constexpr int kClothStageF4 = kClothStage * (kClothRec / 4);
 __host__ __device__ constexpr int cloth_tile_smem(bool flip) {
@@ -550,7 +552,7 @@ __global__ void __launch_bounds__(kClothTileThreads, 3) k_cloth_tiles(DevPtrs d)
 #pragma unroll
         for (int h = 0; h < ch; ++h) acc[k][h] = carry ? dst[k * ch + h] : 0.0f;
       const SplineRow r0 = spline_row(o0), r1 = spline_row(o1);
-      const float e0 = r0.e * inv_dx, e1 = r1.e * inv_dx, od0 = (float)o0, od1 = (float)o1;
+      const float e0 = r0.e * inv_dx, e1 = r1.e * inv_dx, od0 = (float)o0 * dx, od1 = (float)o1 * dx;
       for (int q = cstart[cell]; q < cstart[cell + 1]; ++q) {
         const float4 *r4 = rec + q * (kClothRec / 4);
         // record: f0 f1 f2 m | b0 b1 b2 A00 | A01 A02 A10 A11 | A12 A20 A21 A22 |
@@ -563,24 +565,30 @@ __global__ void __launch_bounds__(kClothTileThreads, 3) k_cloth_tiles(DevPtrs d)
         const float t0 = f_m.x - r0.b, t1 = f_m.y - r1.b;
         const float w0 = r0.a * t0 * t0 + r0.c, w1 = r1.a * t1 * t1 + r1.c;
         const float w01 = w0 * w1;
-        const float g0 = e0 * t0 * w1, g1 = w0 * e1 * t1;
-        const float xi0 = (od0 - f_m.x) * dx, xi1 = (od1 - f_m.y) * dx;
-        const float f2 = f_m.z;
+        const float g0 = e0 * t0 * w1, g1 = w0 * e1 * t1;  // d(w0 w1)/dx0, d(w0 w1)/dx1
+        const float xi0 = od0 - f_m.x * dx, xi1 = od1 - f_m.y * dx, f2 = f_m.z, f2dx = f2 * dx;
+        // the parts of the node's momentum and force that do not depend on o2:
+        // b + A (xi0, xi1, 0), and Q (g0, g1, 0) and Q_c2 w01 per row
+        float mb[3], qg[3], qz[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          mb[c] = bv[c] + A[c * 3] * xi0 + A[c * 3 + 1] * xi1;
+          qg[c] = Q[c * 3] * g0 + Q[c * 3 + 1] * g1;
+          qz[c] = Q[c * 3 + 2] * w01 * inv_dx;
+        }
 #pragma unroll
         for (int o2 = 0; o2 < 3; ++o2) {
           const SplineRow r2 = spline_row(o2);
           const float t2 = f2 - r2.b;
-          const float w2 = r2.a * t2 * t2 + r2.c;
-          const float W = w01 * w2;
-          const float gw[3] = {g0 * w2, g1 * w2, w01 * (r2.e * inv_dx) * t2};
-          const float xi[3] = {xi0, xi1, ((float)o2 - f2) * dx};
+          const float w2 = r2.a * t2 * t2 + r2.c, d2 = r2.e * t2;
+          const float W = w01 * w2, xi2 = (float)o2 * dx - f2dx;
           float *a = acc[o2];
           a[0] += W * f_m.w;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const float mom =
-                W * (bv[c] + A[c * 3] * xi[0] + A[c * 3 + 1] * xi[1] + A[c * 3 + 2] * xi[2]);
-            const float fo = Q[c * 3] * gw[0] + Q[c * 3 + 1] * gw[1] + Q[c * 3 + 2] * gw[2];
+            // W (b + A xi) and Q grad W, grad W = (g0 w2, g1 w2, w01 d2 / dx)
+            const float mom = W * (mb[c] + A[c * 3 + 2] * xi2);
+            const float fo = qg[c] * w2 + qz[c] * d2;
             if constexpr (kFlip) {
               const float b2v = c == 0 ? q2.y : (c == 1 ? q2.z : q2.w);
               a[1 + c] += mom;
@@ -603,14 +611,27 @@ __global__ void __launch_bounds__(kClothTileThreads, 3) k_cloth_tiles(DevPtrs d)
       const unsigned long long mask = cmask;
       for (int nd = t; nd < kTileNodes; nd += kClothTileThreads) {
         const int I = nd / 36, J = (nd / 6) % 6, Kz = nd % 6;
+        // the cells (bit (l2 << 4) | (l0 << 2) | l1) whose stencil covers the
+        // node: l0 in [I - 2, I], l1 in [J - 2, J], l2 in [Kz - 2, Kz]
+        auto span = [](int hi) {  // bits lo..hi of 0..3, lo = hi - 2
+          const int h = min(hi, 3), l = max(hi - 2, 0);
+          return ((2u << h) - 1u) & ~((1u << l) - 1u);
+        };
+        const unsigned s0 = span(I), s1 = span(J), s2 = span(Kz);
+        unsigned long long sel0 = 0, sel2 = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if ((s0 >> k) & 1u) sel0 |= 0xFull << (4 * k);
+          if ((s2 >> k) & 1u) sel2 |= 0xFFFFull << (16 * k);
+        }
+        const unsigned long long cand =
+            mask & (sel0 * 0x0001000100010001ull) & ((unsigned long long)s1 * 0x1111111111111111ull) & sel2;
         float g[ch];
 #pragma unroll
         for (int h = 0; h < ch; ++h) g[h] = 0.0f;
-        for (unsigned long long m = mask; m; m &= m - 1) {
+        for (unsigned long long m = cand; m; m &= m - 1) {
           const int cell = __ffsll((long long)m) - 1;
-          const unsigned o0 = (unsigned)(I - ((cell >> 2) & 3)), o1 = (unsigned)(J - (cell & 3)),
-                         o2 = (unsigned)(Kz - (cell >> 4));
-          if (o0 > 2u || o1 > 2u || o2 > 2u) continue;
+          const int o0 = I - ((cell >> 2) & 3), o1 = J - (cell & 3), o2 = Kz - (cell >> 4);
           const float *src = csum + (cell * 27 + o0 * 9 + o1 * 3 + o2) * ch;
 #pragma unroll
           for (int h = 0; h < ch; ++h) g[h] += src[h];
@@ -1119,9 +1140,14 @@ void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
   k_cloth_grid_add<<<d.num_sms * 8, 256, 0, s>>>(d);
 }
 
+// one point per thread up to 8 CTAs per SM: the gathers are latency-bound
+static int cloth_g2p_grid(const DevPtrs &d, long long n) {
+  return (int)std::max(1ll, std::min<long long>((n + 127) / 128, 8ll * d.num_sms));
+}
+
 void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s) {
-  k_cloth_g2p_verts<<<d.num_sms * 4, 128, 0, s>>>(d);
-  k_cloth_g2p_elements<<<d.num_sms * 4, 128, 0, s>>>(d);
+  k_cloth_g2p_verts<<<cloth_g2p_grid(d, d.cloth.n_verts), 128, 0, s>>>(d);
+  k_cloth_g2p_elements<<<cloth_g2p_grid(d, d.cloth.n_eles), 128, 0, s>>>(d);
 }
 
 }  // namespace zsmpm
