@@ -188,12 +188,25 @@ __global__ void k_cloth_elements(DevPtrs d) {
   const bool affine = d.transfer != MPM_TRANSFER_FLIP;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cl.n_eles;
        e += (long long)gridDim.x * blockDim.x) {
-    float F[9], dm[9], Q[9], R[9];
+    // every load first, ahead of the stores (which the compiler may not
+    // move them past), so that they are in flight together
+    float F[9], dm[9], Q[9], R[9], xe[3], ve[3], Ce[9], Di[4];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
       F[i] = cl.eF[9 * e + i];
       dm[i] = cl.ed[9 * e + i];
+      Ce[i] = affine ? cl.eC[9 * e + i] : 0.0f;
     }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      xe[a] = cl.ex[3 * e + a];
+      ve[a] = cl.ev[3 * e + a];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Di[i] = cl.eDmInv[9 * e + (i < 2 ? i : i + 1)];  // 0 1 3 4
+    const float mass = cl.em[e], vol = cl.evol[e];
+    const int key = cl.ckey[cl.n_verts + e];
+    const int pos = key >= 0 ? cl.cperm_tmp[cl.n_verts + e] : 0;
     gram_schmidt(F, Q, R);
     const bool curve = cl.kind == MPM_MESH_CURVE;
     const float g = cl.gamma;
@@ -255,30 +268,29 @@ __global__ void k_cloth_elements(DevPtrs d) {
     matmul3(QA, Rt, T);
 #pragma unroll
     for (int i = 0; i < 9; ++i) P[i] += T[i];
-    const float mass = cl.em[e], vol = cl.evol[e];
-    if (cl.ckey[cl.n_verts + e] >= 0) {  // a binned point: its record at its sorted position
+    if (key >= 0) {  // a binned point: its record at its sorted position
       const float kf = -vol * dt;
       const float dc1[3] = {dm[1], dm[4], dm[7]}, dc2[3] = {dm[2], dm[5], dm[8]};
       float r[kClothRec];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        r[a] = cl.ex[3 * e + a];
-        r[4 + a] = mass * cl.ev[3 * e + a];
+        r[a] = xe[a];
+        r[4 + a] = mass * ve[a];
         r[25 + a] = 0.0f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          r[7 + a * 3 + c] = affine ? mass * cl.eC[9 * e + a * 3 + c] : 0.0f;
+          r[7 + a * 3 + c] = mass * Ce[a * 3 + c];
           // surface: P_c3 (grad W . d_c3); curve: P_c2 (grad W . d_c2) too
           r[16 + a * 3 + c] =
               kf * ((curve ? P[a * 3 + 1] * dc1[c] : 0.0f) + P[a * 3 + 2] * dc2[c]);
         }
       }
       r[3] = mass;
-      store_record(cl, cl.cperm_tmp[cl.n_verts + e], r);
+      store_record(cl, pos, r);
     }
     float4 *ci = cl.cimp + 3 * e;
     if (curve) {  // type (ii): +-vol dt P_c0 DmInv00 on the two vertices
-      const float di = cl.eDmInv[9 * e];
+      const float di = Di[0];
       const float4 f = make_float4(vol * dt * P[0] * di, vol * dt * P[3] * di,
                                    vol * dt * P[6] * di, 0.0f);
       ci[0] = f;
@@ -286,8 +298,8 @@ __global__ void k_cloth_elements(DevPtrs d) {
       continue;
     }
     // type (ii): impulses from the in-plane columns of P through DmInv rows
-    const float r0[2] = {cl.eDmInv[9 * e + 0], cl.eDmInv[9 * e + 1]};
-    const float r1[2] = {cl.eDmInv[9 * e + 3], cl.eDmInv[9 * e + 4]};
+    const float r0[2] = {Di[0], Di[1]};
+    const float r1[2] = {Di[2], Di[3]};
 #pragma unroll
     for (int vi = 0; vi < 3; ++vi) {
       float Dr0, Dr1, coeff;
@@ -651,59 +663,75 @@ __global__ void __launch_bounds__(kClothTileThreads, 3) k_cloth_tiles(DevPtrs d)
 }
 
 // The cloth tiles into the grid the particle tiles were gathered into: per
-// active node the <= 8 tiles covering it, in the fixed order of the
-// particle gather.
+// active node the <= 8 tiles covering it (the tiles of its block and of the
+// blocks before it along each axis), in a fixed order.  A warp takes a grid
+// block (two nodes per lane) and skips it when no cloth block covers it.
 __global__ void k_cloth_grid_add(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
   const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
   const int dy = S.block_dims[1], dz = S.block_dims[2];
-  const long long nn = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nn;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int gb = (int)(idx >> 6), cell = (int)(idx & 63);
+  const int lane = threadIdx.x & 31;
+  const int ngb = min(d.cnt->n_gblocks, d.cap_gblocks);
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < ngb; gb += warps) {
     const int gdir = d.gb_dir[gb];
     const int ldir = gdir - S.dir_off;
     const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
-    const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
-    float4 g = make_float4(0.f, 0.f, 0.f, 0.f), h = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool any = false;
-#pragma unroll
-    for (int o = 0; o < 8; ++o) {
-      const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
-      if ((o0 && (l0 >= 2 || c0 < 1)) || (o1 && (l1 >= 2 || c1 < 1)) || (o2 && (l2 >= 2 || c2 < 1)))
-        continue;
-      const int bk = cl.cdir_bk[gdir - (o0 * dy + o1) * dz - o2];
-      if (bk < 0 || bk >= cl.cap_cblocks) continue;
-      const long long ti =
-          (long long)bk * kTileNodes + ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2);
-      const float4 t = cl.ctile[ti];
-      g.x += t.x;
-      g.y += t.y;
-      g.z += t.z;
-      g.w += t.w;
-      if (flip_style) {
-        const float4 u = cl.ctile2[ti];
-        h.x += u.x;
-        h.y += u.y;
-        h.z += u.z;
+    // the cloth block of each source (o0, o1, o2): this block minus o
+    int bk = -1;
+    if (lane < 8) {
+      const int o0 = lane >> 2, o1 = (lane >> 1) & 1, o2 = lane & 1;
+      if (c0 >= o0 && c1 >= o1 && c2 >= o2) {
+        bk = cl.cdir_bk[gdir - (o0 * dy + o1) * dz - o2];
+        if (bk >= cl.cap_cblocks) bk = -1;
       }
-      any = true;
     }
-    if (!any) continue;
-    float4 a = d.grid[idx];
-    a.x += g.x;
-    a.y += g.y;
-    a.z += g.z;
-    a.w += g.w;
-    d.grid[idx] = a;
-    if (flip_style) {
-      float4 u = d.grid2[idx];
-      u.x += h.x;
-      u.y += h.y;
-      u.z += h.z;
-      d.grid2[idx] = u;
+    if (!__any_sync(0xffffffffu, bk >= 0)) continue;
+    int src[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) src[o] = __shfl_sync(0xffffffffu, bk, o);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int cell = lane + 32 * h;
+      const long long idx = (long long)gb * 64 + cell;
+      const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f), u2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      bool any = false;
+#pragma unroll
+      for (int o = 0; o < 8; ++o) {
+        const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
+        if ((o0 && l0 >= 2) || (o1 && l1 >= 2) || (o2 && l2 >= 2) || src[o] < 0) continue;
+        const long long ti =
+            (long long)src[o] * kTileNodes + ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2);
+        const float4 t = cl.ctile[ti];
+        g.x += t.x;
+        g.y += t.y;
+        g.z += t.z;
+        g.w += t.w;
+        if (flip_style) {
+          const float4 u = cl.ctile2[ti];
+          u2.x += u.x;
+          u2.y += u.y;
+          u2.z += u.z;
+        }
+        any = true;
+      }
+      if (!any) continue;
+      float4 a = d.grid[idx];
+      a.x += g.x;
+      a.y += g.y;
+      a.z += g.z;
+      a.w += g.w;
+      d.grid[idx] = a;
+      if (flip_style) {
+        float4 u = d.grid2[idx];
+        u.x += u2.x;
+        u.y += u2.y;
+        u.z += u2.z;
+        d.grid2[idx] = u;
+      }
     }
   }
 }
