@@ -597,6 +597,37 @@ def sand_form(zsmpm, dev: int, steps: int = 128, ckpt: int = 8):
             "checkpoint_bytes": sim.peak_checkpoint_bytes, "plain_status": st["status"]}
 
 
+def profile_case(kind: str, dev: int):
+    """A few substeps of a small case for an ncu capture (no timing):
+    'persistent_262k' is the four-material scene at 1/8 scale (262,144
+    particles, dx = 1/128) stepped 8 times by the persistent kernel; 'cloth'
+    is the 2,097,152-particle four-material scene with the 148,225-vertex
+    cloth sheet of the cloth form, stepped 4 times.  Prints the context's
+    counters as one JSON line."""
+    from zeno_gb300 import zsmpm, scenes
+    if kind == "persistent_262k":
+        scene, parts = scenes.multi_material(dx=1.0 / 128, region_cells=(32, 16, 16))
+        steps = 8
+    else:
+        scene, parts = make_workload()
+        steps = 4
+    with zsmpm.Context(scene, max_particles=parts.n, device=dev) as ctx:
+        if kind == "persistent_262k":
+            ctx.set_persistent(True, barrier_limit=1 << 20)
+        ctx.upload(parts)
+        if kind == "cloth":
+            mesh = scenes.cloth_sheet((0.5, 0.45, 0.5), 0.8, 384, E=5e4, nu=0.3, density=300.0,
+                                      gamma=100.0, k=800.0, fa=30.0, dc=0.02)
+            mesh.v = np.tile(np.array([0.0, -1.0, 0.0], np.float32), (mesh.x.shape[0], 1))
+            ctx.add_cloth(mesh)
+        for _ in range(steps):
+            ctx.substep(scene.dt, 1)
+        ctx.sync()
+        st = ctx.stats()
+    print(json.dumps({"profile_case": kind, "status": st["status"], "substeps": st["substeps"]}))
+    return 0 if st["status"] == 0 else 1
+
+
 def diff_profile(kind: str, dev: int):
     """One forward + backward of a differentiable rollout, for profiling:
     'fwd_bwd' is the 65,536-particle fixed-corotated rollout (64 substeps,
@@ -1011,7 +1042,11 @@ def main():
                     help="grid transfer of the --quick run (profiling the FLIP kernels)")
     ap.add_argument("--diff-profile", default=None, choices=["fwd_bwd", "sand"],
                     help="run one forward + backward of a differentiable rollout only: for ncu")
+    ap.add_argument("--profile-case", default=None, choices=["persistent_262k", "cloth"],
+                    help="run a few substeps of a small case only: for ncu")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args.profile_case, 0)
     if args.diff_profile:
         import torch
         torch.cuda.set_device(0)
