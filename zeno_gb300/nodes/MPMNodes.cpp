@@ -577,8 +577,8 @@ ZENDEFNODE(ToTrackerParticles, {
 
 /// ToZSParticles (Generation.cpp:690-1145): m = vol * density, F = I, C = 0.
 /// The device context is sized for the primitive: its block directory spans
-/// the optional domain_min / domain_max inputs, else the bounding box grown
-/// by its own extent (at least 8 blocks) on every side.
+/// the optional domain_min / domain_max inputs, else the bounding box plus 8
+/// cells on every side, and grows whenever a particle leaves it.
 struct ToZSParticles : INode {
   void apply() override {
     auto model = get_input<ZenoConstitutiveModel>("ZSModel");
