@@ -258,6 +258,12 @@ int32_t mpm_cloth_create(mpm_ctx *ctx, const mpm_cloth_desc *desc);
  * (n_verts x 9); elements x, v (n_tris x 3), C, F, d (n_tris x 9, row-major) */
 int32_t mpm_cloth_download(mpm_ctx *ctx, float *vx, float *vv, float *vC, float *ex, float *ev,
                            float *eC, float *eF, float *ed);
+/* the inverse of mpm_cloth_download (NULL keeps an array): the cloth's state
+ * from a checkpoint, in the same layout.  The mesh, masses, rest shapes and
+ * springs stay as created. */
+int32_t mpm_cloth_upload(mpm_ctx *ctx, const float *vx, const float *vv, const float *vC,
+                         const float *ex, const float *ev, const float *eC, const float *eF,
+                         const float *ed);
 /* ConstructBendingSprings (Generation.cu:563-1001) on the context's triangle
  * cloth, from its current state.  MPM_BENDING_VERTEX: one spring between the
  * two vertices opposite each interior (consistently oriented) edge, k = E /

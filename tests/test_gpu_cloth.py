@@ -270,6 +270,39 @@ def test_node_graph_bending(zsmpm_mod, oracle_mod, fused):
     assert rel_l2(x, p.x) < 1e-6 and rel_l2(v, p.v) < 1e-4
 
 
+def test_cloth_beta_of_normal_stretch(zsmpm_mod, oracle_mod):
+    """ComputeParticleBeta's stretch branch: a sheet whose elements are
+    stretched by 1.1 along their normals (d3 and F = d Dm^-1 restored from a
+    checkpoint through mpm_cloth_upload) gives every vertex beta 0.2, as the
+    oracle does; the same state unstretched-by-0.9 gives 0."""
+    scene = S.Scene.unit_box(1.0 / 64, bc_type=S.BC_STICKY, materials=[S.Material()])
+    scene.transfer = S.TRANSFER_AFLIP
+    mesh = _sheet()
+    state = oracle_mod.cloth_init(mesh, scene.dx)
+    Dinv = state["eDmInv"].reshape(-1, 3, 3)
+    with zsmpm_mod.Context(scene, max_particles=1) as ctx:
+        ctx.upload(_empty())
+        ctx.add_cloth(mesh)
+        init = ctx.cloth_download()
+        for scale, want in ((1.1, 0.2), (0.9, 0.0)):
+            d = init["ed"].astype(np.float64).reshape(-1, 3, 3).copy()
+            d[:, :, 2] *= scale
+            F = d @ Dinv
+            ctx.cloth_upload({"ed": d.reshape(-1, 9), "eF": F.reshape(-1, 9)})
+            back = ctx.cloth_download()
+            np.testing.assert_array_equal(back["ed"], d.reshape(-1, 9).astype(np.float32))
+            ctx.compute_particle_beta(scene.dt, -1)
+            beta = ctx.cloth_beta()
+            ref_state = dict(state)
+            for k in ("vx", "vv", "vC", "ex", "ev", "eC"):
+                ref_state[k] = np.asarray(init[k], np.float64).reshape(state[k].shape)
+            ref_state["ed"] = np.asarray(back["ed"], np.float64).reshape(state["ed"].shape)
+            ref_state["eF"] = np.asarray(back["eF"], np.float64).reshape(state["eF"].shape)
+            ref = oracle_mod.cloth_beta(scene, ref_state, scene.dt, -1)
+            np.testing.assert_array_equal(beta, np.full_like(beta, np.float32(want)))
+            np.testing.assert_array_equal(beta, ref.astype(np.float32))
+
+
 @pytest.mark.parametrize("with_collider", [False, True])
 def test_cloth_beta_matches_oracle(zsmpm_mod, oracle_mod, with_collider):
     """ComputeParticleBeta on a deformed sheet (vertex beta 0.2 / 0 from its

@@ -1627,6 +1627,30 @@ int32_t mpm_cloth_download(mpm_ctx *c, float *vx, float *vv, float *vC, float *e
   return MPM_OK;
 }
 
+int32_t mpm_cloth_upload(mpm_ctx *c, const float *vx, const float *vv, const float *vC,
+                         const float *ex, const float *ev, const float *eC, const float *eF,
+                         const float *ed) {
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if ((rc = settle(c))) return rc;
+  const ClothDev &cl = c->d.cloth;
+  if (cl.n_verts == 0) return fail(MPM_ERR_STATE, "no cloth in this context");
+  auto put = [&](float *dst, const float *h, long long count) -> int32_t {
+    if (!h) return MPM_OK;
+    ZS_CUDA(cudaMemcpyAsync(dst, h, count * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    return MPM_OK;
+  };
+  const long long nv = cl.n_verts, ne = cl.n_eles;
+  if ((rc = put(cl.vx, vx, 3 * nv)) || (rc = put(cl.vv, vv, 3 * nv)) ||
+      (rc = put(cl.vC, vC, 9 * nv)) || (rc = put(cl.ex, ex, 3 * ne)) ||
+      (rc = put(cl.ev, ev, 3 * ne)) || (rc = put(cl.eC, eC, 9 * ne)) ||
+      (rc = put(cl.eF, eF, 9 * ne)) || (rc = put(cl.ed, ed, 9 * ne)))
+    return rc;
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->partition_valid = false;  // the cloth's points moved
+  return MPM_OK;
+}
+
 int32_t mpm_trackers_create(mpm_ctx *c, int64_t n, const float *x, const float *v) {
   int32_t rc = check(c);
   if (rc) return rc;

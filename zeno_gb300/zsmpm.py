@@ -80,6 +80,7 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
            "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
            "mpm_frame_begin", "mpm_frame_wait", "mpm_cloth_create", "mpm_cloth_download",
+           "mpm_cloth_upload",
            "mpm_cloth_add_bending",
            "mpm_trackers_create", "mpm_trackers_download",
            "mpm_g2p", "mpm_return_mapping",
@@ -146,6 +147,7 @@ def load(path: str = LIB_PATH):
         "mpm_cloth_add_bending": ([P, i32, C.c_float, C.c_float, P], i32),
         "mpm_trackers_download": ([P, P, P], i32),
         "mpm_cloth_download": ([P] + [P] * 8, i32),
+        "mpm_cloth_upload": ([P] + [P] * 8, i32),
         "mpm_frame_begin": ([P, P, P], i32),
         "mpm_frame_wait": ([P], i32),
         "mpm_apply_collider": ([P, i32], i32),
@@ -335,6 +337,15 @@ class Context:
                                                          ("vx", "vv", "vC", "ex", "ev", "eC",
                                                           "eF", "ed")]), "mpm_cloth_download")
         return out
+
+    def cloth_upload(self, state: dict):
+        """The inverse of cloth_download: arrays given by key (vx, vv, vC,
+        ex, ev, eC, eF, ed) replace the cloth's, the others stay."""
+        nv, ne = self._cloth_n
+        shapes = {"vx": (nv, 3), "vv": (nv, 3), "vC": (nv, 9), "ex": (ne, 3), "ev": (ne, 3),
+                  "eC": (ne, 9), "eF": (ne, 9), "ed": (ne, 9)}
+        arrs = [None if state.get(k) is None else _f32(state[k], shapes[k]) for k in shapes]
+        self._check(self._L.mpm_cloth_upload(self.h, *[_p(a) for a in arrs]), "mpm_cloth_upload")
 
     def compute_von_mises(self, by_log1p: bool = True):
         """ComputeVonMises; the result is the attribute "vms"."""
