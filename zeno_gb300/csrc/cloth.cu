@@ -167,8 +167,18 @@ __device__ __forceinline__ void store_record(const ClothDev &cl, int pos, const 
     dst[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
 }
 
-// each binned point's sorted position (the inverse of the permutation)
+// each binned point's sorted position (the inverse of the permutation); and
+// (one thread) more cloth blocks than the cloth's block capacity -- the
+// points of the blocks left out would be lost -- as a capacity error of the
+// context, the cloth partition's counters cleared for the next substep
 __global__ void k_cloth_inverse(DevPtrs d) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    Counters *cc = d.cloth.ccnt;
+    if ((cc->status & ST_CAPACITY) || cc->max_buckets > d.cloth.cap_cblocks)
+      atomicOr(&d.cnt->status, ST_CAPACITY);
+    cc->status = 0;
+    cc->max_buckets = 0;
+  }
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const long long nb = min((long long)cl.ccnt->n_binned, cl.n_verts + cl.n_eles);
@@ -416,16 +426,6 @@ __global__ void k_cloth_bin(DevPtrs d, DevPtrs dc) {
   }
 }
 
-// more cloth blocks than the cloth's block capacity: a capacity error of the
-// context (the points of the blocks left out would be lost)
-__global__ void k_cloth_status(DevPtrs d) {
-  if (threadIdx.x != 0) return;
-  Counters *cc = d.cloth.ccnt;
-  if ((cc->status & ST_CAPACITY) || cc->max_buckets > d.cloth.cap_cblocks)
-    atomicOr(&d.cnt->status, ST_CAPACITY);
-  cc->status = 0;
-  cc->max_buckets = 0;
-}
 
 // One CTA per cloth block at a time, in two passes over shared memory.
 // First, for each non-empty cell of the block and each of the 27 stencil
@@ -1155,9 +1155,8 @@ void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
   launch_scan(dc, s);
   launch_scatter(dc, s);
   launch_bucket_sort(dc, s);
-  k_cloth_status<<<1, 32, 0, s>>>(d);
-  if (cl.n_springs > 0) k_cloth_bending<<<g, 128, 0, s>>>(d);
   k_cloth_inverse<<<g, 256, 0, s>>>(d);
+  if (cl.n_springs > 0) k_cloth_bending<<<g, 128, 0, s>>>(d);
   k_cloth_elements<<<g, 128, 0, s>>>(d);
   k_cloth_vertex_records<<<g, 128, 0, s>>>(d);
   const bool flip_style = d.transfer != MPM_TRANSFER_APIC;
