@@ -441,7 +441,10 @@ int32_t mpm_snapshot_floats(mpm_ctx *ctx, int64_t *floats);
  * keep their states there and their partitions and grids in the context, so
  * that the backward that follows with the same arguments takes that segment
  * back without recomputing it (when the device has room for the partitions;
- * otherwise it recomputes it). */
+ * otherwise it recomputes it).  A context with a growing directory
+ * (mpm_set_auto_regrow) is refused with MPM_ERR_INVALID, here and in the
+ * backward: the backward recomputes from checkpoints that a moved directory
+ * may not cover. */
 int32_t mpm_rollout_forward(mpm_ctx *ctx, float dt, int32_t n_substeps, int32_t every,
                             const float *state0, float *ckpts, float *seg_states,
                             float *final_state);

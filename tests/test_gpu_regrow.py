@@ -81,6 +81,53 @@ def test_growth_replays_only_the_halted_substeps(zsmpm_mod):
         np.testing.assert_array_equal(grown[k], ref[k], err_msg=k)
 
 
+def test_growth_with_a_cloth(zsmpm_mod):
+    """A cloth sheet riding a thrown block out of the starting directory: the
+    cloth's own partition arrays follow the grown directory, and block and
+    cloth end as on a directory that never grew (bit for bit)."""
+    scene, parts = _thrown_block(v=(6.0, 0.0, 0.0))
+    tight = _tight(scene, parts)
+    mesh = S.cloth_sheet((0.185, 0.455, 0.765), 0.1, 8, model=S.FCR, E=3e4, nu=0.3,
+                         density=500.0, gamma=100.0, k=800.0, fa=30.0, dc=0.05)
+    mesh.v = np.tile(np.array([6.0, 0.0, 0.0], np.float32), (mesh.x.shape[0], 1))
+    outs = []
+    for sc, grow in ((tight, True), (scene, False)):
+        with zsmpm_mod.Context(sc, max_particles=parts.n) as ctx:
+            ctx.set_auto_regrow(grow)
+            ctx.upload(parts)
+            ctx.add_cloth(mesh)
+            for _ in range(6):
+                ctx.substep(scene.dt, 50)
+            ctx.sync()
+            assert ctx.stats()["status"] == 0
+            out = ctx.download(("x", "v", "F"))
+            out.update({"c" + k: v for k, v in ctx.cloth_download().items()})
+            if grow:
+                assert ctx.domain()[2] >= 1
+            outs.append(out)
+    assert outs[0]["cvx"][:, 0].mean() - mesh.x[:, 0].mean() > 0.1
+    for k in outs[1]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+
+
+def test_rollouts_need_a_fixed_directory(zsmpm_mod):
+    """The backward recomputes from checkpoints that a moved directory may
+    not cover: a rollout on a growing directory is refused."""
+    torch = pytest.importorskip("torch")
+    scene, parts = _thrown_block()
+    with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+        ctx.upload(parts)
+        ctx.set_differentiable(True)
+        ctx.set_auto_regrow(True)
+        snap = ctx.snapshot_floats()
+        st = torch.zeros(zsmpm_mod.STATE_PLANES * parts.n, dtype=torch.float32, device="cuda")
+        ck = torch.zeros(snap, dtype=torch.float32, device="cuda")
+        fin = torch.zeros_like(st)
+        ctx.state_save(st.data_ptr())
+        with pytest.raises(zsmpm_mod.MPMError, match="fixed block directory"):
+            ctx.rollout_forward(scene.dt, 4, 4, st.data_ptr(), ck.data_ptr(), fin.data_ptr())
+
+
 def test_without_growth_leaving_the_directory_is_an_error(zsmpm_mod):
     scene, parts = _thrown_block()
     tight = _tight(scene, parts)

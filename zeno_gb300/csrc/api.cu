@@ -331,6 +331,20 @@ float from_ordered_bits(unsigned u) {
 // start afresh, and the next substep bins the current positions.
 int32_t build_grid_boundary(mpm_ctx *c);
 
+// frees a rollout's kept partition sets (PartSet)
+void drop_psets(mpm_ctx *c) {
+  for (PartSet &p : c->psets) {
+    for (void *q : {(void *)p.perm, (void *)p.dir_gb, (void *)p.dir_bk, (void *)p.gb_dir,
+                    (void *)p.bk_dir, (void *)p.bk_start, (void *)p.bk_count, (void *)p.grid,
+                    (void *)p.ptile})
+      dfree(c, q);
+  }
+  c->psets.clear();
+  dfree(c, c->pset_cnt);
+  c->pset_cnt = nullptr;
+  c->pset_cap = 0;
+}
+
 int32_t regrow(mpm_ctx *c) {
   DevPtrs &d = c->d;
   if (c->scenes.size() != 1) return fail(MPM_ERR_OUT_OF_DOMAIN, "a particle left the block directory");
@@ -389,6 +403,17 @@ int32_t regrow(mpm_ctx *c) {
   ZS_CUDA(cudaMemsetAsync(d.dir_bk, 0xff, ndir * sizeof(int32_t), c->stream));
   ZS_CUDA(cudaMemsetAsync(d.dir_flag, 0, ndir, c->stream));
   ZS_CUDA(cudaMemsetAsync(d.cnt, 0, sizeof(Counters), c->stream));
+  ClothDev &cl = d.cloth;
+  if (cl.n_verts > 0) {  // the cloth's own partition runs on the same directory
+    if ((rc = drealloc(c, &cl.cdir_count, ndir)) || (rc = drealloc(c, &cl.cdir_fill, ndir)) ||
+        (rc = drealloc(c, &cl.cdir_gb, ndir)) || (rc = drealloc(c, &cl.cdir_bk, ndir)) ||
+        (rc = drealloc(c, &cl.cdir_flag, ndir)) ||
+        (rc = drealloc(c, &cl.ctile_sums, (size_t)3 * ntiles)))
+      return rc;
+    ZS_CUDA(cudaMemsetAsync(cl.cdir_count, 0, ndir * sizeof(int32_t), c->stream));
+    ZS_CUDA(cudaMemsetAsync(cl.cdir_flag, 0, ndir, c->stream));
+    ZS_CUDA(cudaMemsetAsync(cl.ccnt, 0, sizeof(Counters), c->stream));
+  }
   for (int a = 0; a < 3; ++a) {
     S.block_lo[a] = lo[a];
     S.block_dims[a] = dims[a];
@@ -405,6 +430,9 @@ int32_t regrow(mpm_ctx *c) {
   c->binned = false;
   c->partition_valid = false;
   c->regrows += 1;
+  // a rollout's kept partition sets index the old directory
+  drop_psets(c);
+  c->tail.valid = false;
   if (c->bnd_n > 0) {  // the boundary grid on the new directory
     dfree(c, d.bnd_map);
     d.bnd_map = nullptr;
@@ -2072,6 +2100,8 @@ int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
   if (!c->d.differentiable) return fail(MPM_ERR_STATE, "the adjoint needs mpm_set_differentiable(ctx, 1)");
+  if (c->auto_regrow)
+    return fail(MPM_ERR_INVALID, "a rollout needs a fixed block directory (mpm_set_auto_regrow(ctx, 0))");
   if (c->d.bnd_map) return fail(MPM_ERR_INVALID, "the adjoint takes no boundary grid");
   if (!adj_next || !adj_prev || !grad_mu || !grad_lam)
     return fail(MPM_ERR_INVALID, "null adjoint buffer");
@@ -2161,18 +2191,7 @@ struct StoreSwap {
   }
 };
 
-void free_psets(mpm_ctx *c) {
-  for (PartSet &p : c->psets) {
-    for (void *q : {(void *)p.perm, (void *)p.dir_gb, (void *)p.dir_bk, (void *)p.gb_dir,
-                    (void *)p.bk_dir, (void *)p.bk_start, (void *)p.bk_count, (void *)p.grid,
-                    (void *)p.ptile})
-      dfree(c, q);
-  }
-  c->psets.clear();
-  dfree(c, c->pset_cnt);
-  c->pset_cnt = nullptr;
-  c->pset_cap = 0;
-}
+void free_psets(mpm_ctx *c) { drop_psets(c); }
 
 // `count` partition sets of `capb` blocks each; false (none kept) when the
 // device has not room for them with a margin, so that the rollout takes the
@@ -2243,6 +2262,10 @@ int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t ev
   if (rc) return rc;
   if (n_substeps < 0 || every <= 0 || !state0 || !final_state || (n_substeps > 0 && !ckpts))
     return fail(MPM_ERR_INVALID, "invalid rollout arguments");
+  if (c->auto_regrow)
+    return fail(MPM_ERR_INVALID, "a rollout needs a fixed block directory: the backward recomputes "
+                                 "from checkpoints that a moved directory may not cover "
+                                 "(mpm_set_auto_regrow(ctx, 0))");
   c->tail.valid = false;
   const long long n = c->prm.n;
   const size_t snap = (size_t)(tiled_elems(n, NCH) + tiled_elems(n, NICH));

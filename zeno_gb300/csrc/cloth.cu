@@ -406,6 +406,9 @@ __global__ void k_cloth_bending(DevPtrs d) {
 // The cloth's points into the blocks of their own partition: key (block,
 // cell) per point, warp-aggregated counts per block (no grid blocks).
 __global__ void k_cloth_bin(DevPtrs d, DevPtrs dc) {
+  // the cloth's partition stages (their own counters) stop with the context:
+  // run on stale keys, they would place points at stale block offsets
+  if (blockIdx.x == 0 && threadIdx.x == 0) dc.cnt->halt = d.cnt->halt;
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
   const SceneParams &S = d.scn[0];
