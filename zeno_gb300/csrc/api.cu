@@ -53,6 +53,7 @@ struct mpm_ctx {
   bool prm_dirty = true;
   int cur = 0;
   bool partition_valid = false;
+  long long cloth_capb_want = 0;  // the cloth's block capacity before the directory's bound
   bool needs_full_clear = false;
   bool binned = false;  // directory counts describe the current positions
   int64_t substeps = 0;
@@ -413,6 +414,16 @@ int32_t regrow(mpm_ctx *c) {
     ZS_CUDA(cudaMemsetAsync(cl.cdir_count, 0, ndir * sizeof(int32_t), c->stream));
     ZS_CUDA(cudaMemsetAsync(cl.cdir_flag, 0, ndir, c->stream));
     ZS_CUDA(cudaMemsetAsync(cl.ccnt, 0, sizeof(Counters), c->stream));
+    const long long capb =
+        std::min<long long>({ndir, cl.n_verts + cl.n_eles, c->cloth_capb_want});
+    if (capb > cl.cap_cblocks) {  // the old directory bounded the cloth's blocks
+      if ((rc = drealloc(c, &cl.cgb_dir, capb)) || (rc = drealloc(c, &cl.cbk_dir, capb)) ||
+          (rc = drealloc(c, &cl.cbk_start, capb)) || (rc = drealloc(c, &cl.cbk_count, capb)) ||
+          (rc = drealloc(c, &cl.ctile, (size_t)capb * kTileNodes)) ||
+          (rc = drealloc(c, &cl.ctile2, (size_t)capb * kTileNodes)))
+        return rc;
+      cl.cap_cblocks = (int)capb;
+    }
   }
   for (int a = 0; a < 3; ++a) {
     S.block_lo[a] = lo[a];
@@ -1306,7 +1317,10 @@ int32_t alloc_cloth_p2g(mpm_ctx *c, ClothDev &cl, const std::vector<int32_t> &in
   };
   for (long long i = 0; i < cl.n_verts; ++i) add(&vx[3 * i]);
   for (long long e = 0; e < cl.n_eles; ++e) add(&ex[3 * e]);
-  const long long capb = std::min<long long>({d.ndir, np, std::max<long long>(8 * (long long)blocks.size(), 1024)});
+  // room for the cloth to spread over 8x its blocks; a grown directory
+  // raises the directory's share of the bound (regrow)
+  c->cloth_capb_want = std::max<long long>(8 * (long long)blocks.size(), 1024);
+  const long long capb = std::min<long long>({d.ndir, np, c->cloth_capb_want});
   cl.cap_cblocks = (int)capb;
   int32_t rc;
   if ((rc = dalloc(c, &cl.crec, (size_t)np * kClothRec)) || (rc = dalloc(c, &cl.ckey, (size_t)np)) ||
