@@ -25,7 +25,7 @@ NODE_SOURCES = ["MPMNodes.cpp", "nodes_capi.cpp"]
 SOURCES = ["partition.cu", "transfer.cu", "flip.cu", "cloth.cu", "adjoint.cu", "io.cu", "output.cu", "api.cu", "noalloc.cu", "persistent.cu", "boundary_grid.cu"]
 HEADERS = ["zsmpm_internal.cuh", "mpm_math.cuh", "binning.cuh", "tile_scatter.cuh", "cp_async.cuh",
            "adj_moments.cuh", "partition_stages.cuh", "transfer_stages.cuh",
-           "colliders.cuh", "blocks.cuh"]
+           "colliders.cuh", "blocks.cuh", "cloth_grid.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]

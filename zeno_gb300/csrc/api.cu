@@ -18,6 +18,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "cloth_grid.cuh"
 #include "zsmpm_internal.cuh"
 
 using namespace zsmpm;
@@ -234,10 +235,10 @@ void enqueue_substep(mpm_ctx *c, int cur, cudaEvent_t *ev = nullptr) {
   mark(MPM_STAGE_P2G);
   launch_p2g(c->d, cur, c->stream);
   mark(MPM_STAGE_GRID_UPDATE);
-  if (cloth) {  // particle sums, the cloth's scatter, then the update
+  if (cloth) {  // particle sums, the cloth's scatter, then its tiles and the update
     launch_grid_gather(c->d, 0, c->stream);
-    launch_cloth_p2g(c->d, c->stream);
-    launch_grid_update(c->d, 3, c->stream);
+    launch_cloth_p2g(c->d, false, c->stream);
+    launch_grid_update(c->d, 3 | kGridAddCloth, c->stream);
     if (!c->colliders.empty()) launch_apply_colliders(c->d, -1, c->stream);
   } else {
     launch_grid_gather(c->d, 3, c->stream);
@@ -1864,7 +1865,7 @@ int32_t mpm_p2g(mpm_ctx *c, float dt) {
   if ((rc = set_dt(c, dt))) return rc;
   launch_p2g(c->d, c->cur, c->stream);
   launch_grid_gather(c->d, 0, c->stream);  // grid = m, mv as after the reference P2G
-  if (c->d.cloth.n_verts > 0) launch_cloth_p2g(c->d, c->stream);
+  if (c->d.cloth.n_verts > 0) launch_cloth_p2g(c->d, true, c->stream);
   return launch_check("p2g");
 }
 

@@ -27,6 +27,7 @@
 #include <algorithm>
 
 #include "binning.cuh"
+#include "cloth_grid.cuh"
 #include "cp_async.cuh"
 #include "colliders.cuh"
 #include "mpm_math.cuh"
@@ -665,10 +666,10 @@ __global__ void __launch_bounds__(kClothTileThreads, 3) k_cloth_tiles(DevPtrs d)
   cp_async_wait<0>();
 }
 
-// The cloth tiles into the grid the particle tiles were gathered into: per
-// active node the <= 8 tiles covering it (the tiles of its block and of the
-// blocks before it along each axis), in a fixed order.  A warp takes a grid
-// block (two nodes per lane) and skips it when no cloth block covers it.
+// The cloth tiles into the grid the particle tiles were gathered into (the
+// stage path; the whole substep adds them in its grid update): a warp takes
+// a grid block (two nodes per lane) and skips it when no cloth block covers
+// it.
 __global__ void k_cloth_grid_add(DevPtrs d) {
   if (ZSMPM_HALTED(d)) return;
   const ClothDev &cl = d.cloth;
@@ -681,60 +682,18 @@ __global__ void k_cloth_grid_add(DevPtrs d) {
   for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < ngb; gb += warps) {
     const int gdir = d.gb_dir[gb];
     const int ldir = gdir - S.dir_off;
-    const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
-    // the cloth block of each source (o0, o1, o2): this block minus o
-    int bk = -1;
-    if (lane < 8) {
-      const int o0 = lane >> 2, o1 = (lane >> 1) & 1, o2 = lane & 1;
-      if (c0 >= o0 && c1 >= o1 && c2 >= o2) {
-        bk = cl.cdir_bk[gdir - (o0 * dy + o1) * dz - o2];
-        if (bk >= cl.cap_cblocks) bk = -1;
-      }
-    }
+    const int bk = cloth_source(cl, S, gdir, ldir / (dz * dy), (ldir / dz) % dy, ldir % dz, lane);
     if (!__any_sync(0xffffffffu, bk >= 0)) continue;
     int src[8];
 #pragma unroll
     for (int o = 0; o < 8; ++o) src[o] = __shfl_sync(0xffffffffu, bk, o);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int cell = lane + 32 * h;
-      const long long idx = (long long)gb * 64 + cell;
-      const int l0 = cell >> 4, l1 = (cell >> 2) & 3, l2 = cell & 3;
-      float4 g = make_float4(0.f, 0.f, 0.f, 0.f), u2 = make_float4(0.f, 0.f, 0.f, 0.f);
-      bool any = false;
-#pragma unroll
-      for (int o = 0; o < 8; ++o) {
-        const int o0 = o >> 2, o1 = (o >> 1) & 1, o2 = o & 1;
-        if ((o0 && l0 >= 2) || (o1 && l1 >= 2) || (o2 && l2 >= 2) || src[o] < 0) continue;
-        const long long ti =
-            (long long)src[o] * kTileNodes + ((l0 + 4 * o0) * 6 + (l1 + 4 * o1)) * 6 + (l2 + 4 * o2);
-        const float4 t = cl.ctile[ti];
-        g.x += t.x;
-        g.y += t.y;
-        g.z += t.z;
-        g.w += t.w;
-        if (flip_style) {
-          const float4 u = cl.ctile2[ti];
-          u2.x += u.x;
-          u2.y += u.y;
-          u2.z += u.z;
-        }
-        any = true;
-      }
-      if (!any) continue;
-      float4 a = d.grid[idx];
-      a.x += g.x;
-      a.y += g.y;
-      a.z += g.z;
-      a.w += g.w;
-      d.grid[idx] = a;
-      if (flip_style) {
-        float4 u = d.grid2[idx];
-        u.x += u2.x;
-        u.y += u2.y;
-        u.z += u2.z;
-        d.grid2[idx] = u;
-      }
+      const long long idx = (long long)gb * 64 + lane + 32 * h;
+      float4 g = d.grid[idx], u = flip_style ? d.grid2[idx] : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!add_cloth_tiles(cl, src, lane + 32 * h, flip_style, g, u)) continue;
+      d.grid[idx] = g;
+      if (flip_style) d.grid2[idx] = u;
     }
   }
 }
@@ -1130,9 +1089,11 @@ void launch_cloth_mark(const DevPtrs &d, cudaStream_t s) {
 // The cloth's P2G into the grid that holds the particles' sums: its points'
 // own partition (the partition's scan, placement and sort on the cloth's
 // arrays), the element stresses, records and impulse slots, the vertex
-// records with their impulse sums, the tiles, and the tiles into the grid.  No
-// float atomics: the result does not depend on the order threads run in.
-void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
+// records with their impulse sums, the tiles, and (add_to_grid; otherwise
+// the grid update adds them, mode bit kGridAddCloth) the tiles into the
+// grid.  No float atomics: the result does not depend on the order threads
+// run in.
+void launch_cloth_p2g(const DevPtrs &d, bool add_to_grid, cudaStream_t s) {
   const ClothDev &cl = d.cloth;
   const long long np = cl.n_verts + cl.n_eles;
   DevPtrs dc = d;
@@ -1167,7 +1128,7 @@ void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s) {
     k_cloth_tiles<true><<<d.num_sms * 2, kClothTileThreads, cloth_tile_smem(true), s>>>(d);
   else
     k_cloth_tiles<false><<<d.num_sms * 3, kClothTileThreads, cloth_tile_smem(false), s>>>(d);
-  k_cloth_grid_add<<<d.num_sms * 8, 256, 0, s>>>(d);
+  if (add_to_grid) k_cloth_grid_add<<<d.num_sms * 8, 256, 0, s>>>(d);
 }
 
 // one point per thread up to 8 CTAs per SM: the gathers are latency-bound

@@ -23,6 +23,7 @@
 
 #include "binning.cuh"
 #include "blocks.cuh"
+#include "cloth_grid.cuh"
 #include "colliders.cuh"
 #include "cp_async.cuh"
 #include "mpm_math.cuh"
@@ -514,22 +515,57 @@ __global__ void k_grid_update_flip(DevPtrs d, int mode) {
   const SimParams &P = *d.prm;
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
   float vmax = 0.0f;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-       idx += (long long)gridDim.x * blockDim.x) {
-    float4 g = d.grid[idx];
-    if (g.x == 0.0f) continue;
-    float4 h = d.grid2[idx];
-    const int gdir = d.gb_dir[idx >> 6];
-    const int sc = scene_of_dir(d, gdir);
-    const SceneParams &S = d.scn[sc];
-    const int dz = S.block_dims[2], dy = S.block_dims[1];
-    const int ldir = gdir - S.dir_off, cell = (int)(idx & 63);
-    const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
-                      (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
-                      ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
-    flip_update_node(S, P.dt, mode, I, g, h, vmax);
-    d.grid[idx] = g;
-    d.grid2[idx] = h;
+  if (mode & kGridAddCloth) {
+    // the cloth's tiles first (one context, one scene): a warp per grid
+    // block, two nodes per lane
+    const SceneParams &S = d.scn[0];
+    const int dy = S.block_dims[1], dz = S.block_dims[2], lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < (int)(n >> 6);
+         gb += warps) {
+      const int gdir = d.gb_dir[gb], ldir = gdir - S.dir_off;
+      const int c0 = ldir / (dz * dy), c1 = (ldir / dz) % dy, c2 = ldir % dz;
+      const int bk = cloth_source(d.cloth, S, gdir, c0, c1, c2, lane);
+      const bool covered = __any_sync(0xffffffffu, bk >= 0);
+      int src[8];
+#pragma unroll
+      for (int o = 0; o < 8; ++o) src[o] = __shfl_sync(0xffffffffu, bk, o);
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int cell = lane + 32 * hh;
+        const long long idx = (long long)gb * 64 + cell;
+        float4 g = d.grid[idx], h = d.grid2[idx];
+        const bool added = covered && add_cloth_tiles(d.cloth, src, cell, true, g, h);
+        if (g.x != 0.0f) {
+          const int I[3] = {(c0 + S.block_lo[0]) * 4 + (cell >> 4),
+                            (c1 + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
+                            (c2 + S.block_lo[2]) * 4 + (cell & 3)};
+          flip_update_node(S, P.dt, mode, I, g, h, vmax);
+        }
+        if (g.x != 0.0f || added) {
+          d.grid[idx] = g;
+          d.grid2[idx] = h;
+        }
+      }
+    }
+  } else {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+      float4 g = d.grid[idx];
+      if (g.x == 0.0f) continue;
+      float4 h = d.grid2[idx];
+      const int gdir = d.gb_dir[idx >> 6];
+      const int sc = scene_of_dir(d, gdir);
+      const SceneParams &S = d.scn[sc];
+      const int dz = S.block_dims[2], dy = S.block_dims[1];
+      const int ldir = gdir - S.dir_off, cell = (int)(idx & 63);
+      const int I[3] = {((ldir / (dz * dy)) + S.block_lo[0]) * 4 + (cell >> 4),
+                        (((ldir / dz) % dy) + S.block_lo[1]) * 4 + ((cell >> 2) & 3),
+                        ((ldir % dz) + S.block_lo[2]) * 4 + (cell & 3)};
+      flip_update_node(S, P.dt, mode, I, g, h, vmax);
+      d.grid[idx] = g;
+      d.grid2[idx] = h;
+    }
   }
   if (mode & 1) {
 #pragma unroll

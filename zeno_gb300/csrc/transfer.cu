@@ -24,6 +24,7 @@
 
 #include "binning.cuh"
 #include "blocks.cuh"
+#include "cloth_grid.cuh"
 #include "colliders.cuh"
 #include "cp_async.cuh"
 #include "mpm_math.cuh"
@@ -61,15 +62,42 @@ __global__ void k_grid_update(DevPtrs d, int mode) {
   const SimParams &P = *d.prm;
   const long long n = (long long)min(d.cnt->n_gblocks, d.cap_gblocks) * 64;
   float vmax = 0.0f;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-       idx += (long long)gridDim.x * blockDim.x) {
-    float4 g = d.grid[idx];
-    if (g.x == 0.0f) continue;
-    const int gdir = d.gb_dir[idx >> 6];
-    const int sc = scene_of_dir(d, gdir);
-    const SceneParams &S = d.scn[sc];
-    update_node(d, sc, S, P.dt, mode, gdir - S.dir_off, (int)(idx & 63), g, vmax);
-    d.grid[idx] = g;
+  if (mode & kGridAddCloth) {
+    // the cloth's tiles first (one context, one scene): a warp per grid
+    // block, two nodes per lane
+    const SceneParams &S = d.scn[0];
+    const int dy = S.block_dims[1], dz = S.block_dims[2], lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int gb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); gb < (int)(n >> 6);
+         gb += warps) {
+      const int gdir = d.gb_dir[gb], ldir = gdir - S.dir_off;
+      const int bk =
+          cloth_source(d.cloth, S, gdir, ldir / (dz * dy), (ldir / dz) % dy, ldir % dz, lane);
+      const bool covered = __any_sync(0xffffffffu, bk >= 0);
+      int src[8];
+#pragma unroll
+      for (int o = 0; o < 8; ++o) src[o] = __shfl_sync(0xffffffffu, bk, o);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int cell = lane + 32 * h;
+        const long long idx = (long long)gb * 64 + cell;
+        float4 g = d.grid[idx], unused;
+        const bool added = covered && add_cloth_tiles(d.cloth, src, cell, false, g, unused);
+        if (g.x != 0.0f) update_node(d, 0, S, P.dt, mode, ldir, cell, g, vmax);
+        if (g.x != 0.0f || added) d.grid[idx] = g;
+      }
+    }
+  } else {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+      float4 g = d.grid[idx];
+      if (g.x == 0.0f) continue;
+      const int gdir = d.gb_dir[idx >> 6];
+      const int sc = scene_of_dir(d, gdir);
+      const SceneParams &S = d.scn[sc];
+      update_node(d, sc, S, P.dt, mode, gdir - S.dir_off, (int)(idx & 63), g, vmax);
+      d.grid[idx] = g;
+    }
   }
   if (mode & 1) {
 #pragma unroll

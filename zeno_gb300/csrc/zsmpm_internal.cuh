@@ -325,7 +325,8 @@ void launch_particle_beta(const DevPtrs &d, int cur, float dt, int collider, cud
 
 // cloth.cu
 void launch_cloth_mark(const DevPtrs &d, cudaStream_t s);
-void launch_cloth_p2g(const DevPtrs &d, cudaStream_t s);
+// add_to_grid false: the tiles are left for the grid update (mode bit 4)
+void launch_cloth_p2g(const DevPtrs &d, bool add_to_grid, cudaStream_t s);
 void launch_cloth_g2p(const DevPtrs &d, cudaStream_t s);
 // ComputeParticleBeta on the cloth's vertices (triangle meshes)
 void launch_cloth_beta(const DevPtrs &d, float dt, int collider, cudaStream_t s);
