@@ -595,7 +595,10 @@ template <bool kAffine> constexpr int fg2p_smem_bytes() {
          kG2PMetaFlip * (int)sizeof(G2PMeta);
 }
 
-template <bool kAffine, bool kFuseRM, bool kFuseBin>
+// kHencky: the von Mises / Cam-Clay return mappings are compiled in (only
+// for contexts whose materials use them; Drucker-Prager alone keeps the
+// register count down)
+template <bool kAffine, bool kFuseRM, bool kFuseBin, bool kHencky>
 __global__ void __launch_bounds__(kFG2PThreads, 4)
     k_g2p_flip(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
                float *__restrict__ pout, int32_t *__restrict__ iout) {
@@ -830,8 +833,10 @@ __global__ void __launch_bounds__(kFG2PThreads, 4)
             F[r * 3 + c] = Fo[r * 3 + c] + dt * (X[r * 3 + 0] * Fo[c] + X[r * 3 + 1] * Fo[3 + c] +
                                                  X[r * 3 + 2] * Fo[6 + c]);
         float jch = q[GC::J][tid];  // log(Jp) of a Cam-Clay particle
-        if (kFuseRM && mp.plastic != MPM_PLASTIC_NONE) {
-          ok_state = return_mapping(mp, mu, lam, F, jch, tau) >= 0;
+        if (kFuseRM && mp.plastic != MPM_PLASTIC_NONE &&
+            (kHencky || mp.plastic == MPM_PLASTIC_NADP)) {
+          ok_state = (kHencky ? return_mapping(mp, mu, lam, F, jch, tau)
+                              : project_dp(mu, lam, mp.alpha, F, tau)) >= 0;
           if (!kAffine && lame)  // the stress of the projected F with the material's mu, lam
             ok_state = kirchhoff(mp.type, mu_s, lam_s, mp.bulk, mp.gamma, F, 1.0f, tau) && ok_state;
         } else {
@@ -974,10 +979,15 @@ template <class K> static int occupancy(K kernel, int threads, int smem) {
 void configure_flip_launches(DevPtrs &d) {
   const int a = std::min(occupancy(k_p2g_flip<true>, kFThreads, FLayout<true>::bytes),
                          occupancy(k_p2g_flip<false>, kFThreads, FLayout<false>::bytes));
-  int g = occupancy(k_g2p_flip<true, true, true>, kFG2PThreads, fg2p_smem_bytes<true>());
-  g = std::min(g, occupancy(k_g2p_flip<false, true, true>, kFG2PThreads, fg2p_smem_bytes<false>()));
-  occupancy(k_g2p_flip<true, false, false>, kFG2PThreads, fg2p_smem_bytes<true>());
-  occupancy(k_g2p_flip<false, false, false>, kFG2PThreads, fg2p_smem_bytes<false>());
+  int g = occupancy(k_g2p_flip<true, true, true, false>, kFG2PThreads, fg2p_smem_bytes<true>());
+  g = std::min(g, occupancy(k_g2p_flip<false, true, true, false>, kFG2PThreads,
+                            fg2p_smem_bytes<false>()));
+  g = std::min(g, occupancy(k_g2p_flip<true, true, true, true>, kFG2PThreads,
+                            fg2p_smem_bytes<true>()));
+  g = std::min(g, occupancy(k_g2p_flip<false, true, true, true>, kFG2PThreads,
+                            fg2p_smem_bytes<false>()));
+  occupancy(k_g2p_flip<true, false, false, false>, kFG2PThreads, fg2p_smem_bytes<true>());
+  occupancy(k_g2p_flip<false, false, false, false>, kFG2PThreads, fg2p_smem_bytes<false>());
   d.grid_p2g_flip = d.num_sms * a;
   d.grid_g2p_flip = d.num_sms * g;
 }
@@ -1003,16 +1013,20 @@ void launch_g2p_flip(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaS
   const int grid = d.grid_g2p_flip;
   if (d.transfer == MPM_TRANSFER_AFLIP) {
     constexpr int smem = fg2p_smem_bytes<true>();
-    if (fuse_rm && fuse_bin)
-      k_g2p_flip<true, true, true><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
+    if (fuse_rm && fuse_bin && d.hencky)
+      k_g2p_flip<true, true, true, true><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
+    else if (fuse_rm && fuse_bin)
+      k_g2p_flip<true, true, true, false><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
     else
-      k_g2p_flip<true, false, false><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
+      k_g2p_flip<true, false, false, false><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
   } else {
     constexpr int smem = fg2p_smem_bytes<false>();
-    if (fuse_rm && fuse_bin)
-      k_g2p_flip<false, true, true><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
+    if (fuse_rm && fuse_bin && d.hencky)
+      k_g2p_flip<false, true, true, true><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
+    else if (fuse_rm && fuse_bin)
+      k_g2p_flip<false, true, true, false><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
     else
-      k_g2p_flip<false, false, false><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
+      k_g2p_flip<false, false, false, false><<<grid, kFG2PThreads, smem, s>>>(d, pi, ii, po, io);
   }
 }
 
