@@ -797,11 +797,16 @@ def run_gpu(args):
     sampler = ClockSampler(dev)
     if not args.quick:
         sampler.start()
-        # keep the GPU busy ~0.4 s so the sampler sees the loaded clock
+        # keep the GPU busy ~0.4 s so the sampler sees the loaded clock,
+        # then start the timed substeps from the uploaded state again (the
+        # workload's substeps from its initial state, after the warm-up)
         t_busy = time.perf_counter()
         while time.perf_counter() - t_busy < 0.4:
             ctx.substep(dt, 20)
             ctx.sync()
+        ctx.upload(parts)
+        ctx.substep(dt, max(args.warmup, 3))
+        ctx.sync()
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
