@@ -10,8 +10,11 @@
 //    force P_c3 (grad W . d_c3)(-vol dt) and the element's mass and momentum
 //    on its 27 nodes (type i), the in-plane force as impulses on its three
 //    vertices (type ii); then per vertex its mass, momentum and impulse.
-//    FLIP grids take the forces in vstar.  Float atomics into the grid the
-//    particle tiles were gathered into (grid update after this);
+//    FLIP grids take the forces in vstar.  No float atomics: the cloth's
+//    points are partitioned into blocks of their own, each point writes a
+//    scatter record, each cloth block's node tile sums its records in a
+//    fixed order, and the tiles join the grid the particle tiles were
+//    gathered into (in the grid update of the whole substep);
 //  * G2P (Transfer.cu:1287-1445): vertices as damped APIC (C = skew + (1 -
 //    dc) sym; or the FLIP-style blend), then elements: damped C, centroid
 //    and mean velocity of their vertices, d1 = p1 - p0, d2 = p2 - p0, d3 +=
