@@ -8,6 +8,7 @@
 // refreshes with one copy before launching, so a captured graph stays valid
 // when dt changes (SubstepDt, zeno/src/nodes/ControlNodes.cpp:251-320).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -22,6 +23,17 @@
 #include "zsmpm_internal.cuh"
 
 using namespace zsmpm;
+
+// An NVTX range around a C-ABI call: the call's name on a profiler's
+// timeline (NVTX v3 is header-only; with no tool attached a push is a check
+// of one function pointer).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+#define ZS_RANGE(name) NvtxRange zs_nvtx_range_(name)
 
 namespace {
 
@@ -892,6 +904,7 @@ extern "C" {
 
 int32_t mpm_set_grid_boundary(mpm_ctx *c, int32_t type, int64_t n_verts, int64_t n_eles,
                               const float *x, const float *v, const float *m, const float *nrm) {
+  ZS_RANGE("mpm_set_grid_boundary");
   int32_t rc = check(c);
   if (rc) return rc;
   if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "a boundary grid needs a one-scene context");
@@ -1134,6 +1147,7 @@ int32_t mpm_particles_upload(mpm_ctx *c, int64_t n, const float *x, const float 
                              const float *C, const float *F, const float *J, const float *m,
                              const float *vol, const int32_t *mat, const float *mu,
                              const float *lam) {
+  ZS_RANGE("mpm_particles_upload");
   return upload_impl(c, nullptr, n, x, v, C, F, J, m, vol, mat, mu, lam);
 }
 
@@ -1141,6 +1155,7 @@ int32_t mpm_particles_upload_async(mpm_ctx *c, int64_t n, const float *x, const 
                                    const float *C, const float *F, const float *J,
                                    const float *m, const float *vol, const int32_t *mat,
                                    const float *mu, const float *lam) {
+  ZS_RANGE("mpm_particles_upload_async");
   return upload_impl(c, nullptr, n, x, v, C, F, J, m, vol, mat, mu, lam, true);
 }
 
@@ -1148,6 +1163,7 @@ int32_t mpm_batch_upload(mpm_ctx *c, const int64_t *scene_offsets, int64_t n, co
                          const float *v, const float *C, const float *F, const float *J,
                          const float *m, const float *vol, const int32_t *mat, const float *mu,
                          const float *lam) {
+  ZS_RANGE("mpm_batch_upload");
   if (!scene_offsets) return fail(MPM_ERR_INVALID, "scene offsets are required");
   return upload_impl(c, scene_offsets, n, x, v, C, F, J, m, vol, mat, mu, lam);
 }
@@ -1174,6 +1190,7 @@ int32_t mpm_particles_set_lame(mpm_ctx *c, const float *mu, const float *lam) {
 }
 
 int32_t mpm_particles_download(mpm_ctx *c, float *x, float *v, float *C, float *F, float *J) {
+  ZS_RANGE("mpm_particles_download");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -1350,6 +1367,7 @@ int32_t alloc_cloth_p2g(mpm_ctx *c, ClothDev &cl, const std::vector<int32_t> &in
 extern "C" {
 
 int32_t mpm_cloth_create(mpm_ctx *c, const mpm_cloth_desc *desc) {
+  ZS_RANGE("mpm_cloth_create");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!desc || desc->n_verts <= 0 || desc->n_tris <= 0 || !desc->x || !desc->tris)
@@ -1651,6 +1669,7 @@ int32_t mpm_cloth_add_bending(mpm_ctx *c, int32_t type, float stiffness, float t
 
 int32_t mpm_cloth_download(mpm_ctx *c, float *vx, float *vv, float *vC, float *ex, float *ev,
                            float *eC, float *eF, float *ed) {
+  ZS_RANGE("mpm_cloth_download");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -1673,6 +1692,7 @@ int32_t mpm_cloth_download(mpm_ctx *c, float *vx, float *vv, float *vC, float *e
 int32_t mpm_cloth_upload(mpm_ctx *c, const float *vx, const float *vv, const float *vC,
                          const float *ex, const float *ev, const float *eC, const float *eF,
                          const float *ed) {
+  ZS_RANGE("mpm_cloth_upload");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -1748,6 +1768,7 @@ int32_t mpm_frame_wait(mpm_ctx *c) {
 }
 
 int32_t mpm_frame_begin(mpm_ctx *c, float *x, float *v) {
+  ZS_RANGE("mpm_frame_begin");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -1806,6 +1827,7 @@ int32_t mpm_set_transfer(mpm_ctx *c, int32_t scheme) {
 }
 
 int32_t mpm_compute_particle_beta(mpm_ctx *c, float dt, int32_t collider) {
+  ZS_RANGE("mpm_compute_particle_beta");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -1824,6 +1846,7 @@ int32_t mpm_compute_particle_beta(mpm_ctx *c, float dt, int32_t collider) {
 }
 
 int32_t mpm_partition(mpm_ctx *c) {
+  ZS_RANGE("mpm_partition");
   int32_t rc = check(c);
   if (rc) return rc;
   set_auto_step(c, 0);  // the stage path moves colliders only on request
@@ -1851,6 +1874,7 @@ int32_t mpm_partition(mpm_ctx *c) {
 }
 
 int32_t mpm_grid_clear(mpm_ctx *c) {
+  ZS_RANGE("mpm_grid_clear");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "grid clear needs a partition");
@@ -1859,6 +1883,7 @@ int32_t mpm_grid_clear(mpm_ctx *c) {
 }
 
 int32_t mpm_p2g(mpm_ctx *c, float dt) {
+  ZS_RANGE("mpm_p2g");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "p2g needs a partition of the current positions");
@@ -1870,6 +1895,7 @@ int32_t mpm_p2g(mpm_ctx *c, float dt) {
 }
 
 int32_t mpm_grid_update(mpm_ctx *c, float dt, float *max_vel_sqr) {
+  ZS_RANGE("mpm_grid_update");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "grid update needs a partition");
@@ -1889,6 +1915,7 @@ int32_t mpm_grid_update(mpm_ctx *c, float dt, float *max_vel_sqr) {
 }
 
 int32_t mpm_apply_boundary(mpm_ctx *c) {
+  ZS_RANGE("mpm_apply_boundary");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "boundary needs a partition");
@@ -1899,6 +1926,7 @@ int32_t mpm_apply_boundary(mpm_ctx *c) {
 }
 
 int32_t mpm_apply_walls(mpm_ctx *c) {
+  ZS_RANGE("mpm_apply_walls");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "boundary needs a partition");
@@ -1908,6 +1936,7 @@ int32_t mpm_apply_walls(mpm_ctx *c) {
 }
 
 int32_t mpm_apply_collider(mpm_ctx *c, int32_t id) {
+  ZS_RANGE("mpm_apply_collider");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "collider needs a partition");
@@ -1920,6 +1949,7 @@ int32_t mpm_apply_collider(mpm_ctx *c, int32_t id) {
 }
 
 int32_t mpm_g2p(mpm_ctx *c, float dt) {
+  ZS_RANGE("mpm_g2p");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!c->partition_valid) return fail(MPM_ERR_STATE, "g2p needs the partition used by p2g");
@@ -1936,6 +1966,7 @@ int32_t mpm_g2p(mpm_ctx *c, float dt) {
 }
 
 int32_t mpm_return_mapping(mpm_ctx *c) {
+  ZS_RANGE("mpm_return_mapping");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = push_params(c))) return rc;
@@ -1944,6 +1975,7 @@ int32_t mpm_return_mapping(mpm_ctx *c) {
 }
 
 int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
+  ZS_RANGE("mpm_substep");
   int32_t rc = check(c);
   if (rc) return rc;
   if (n_substeps < 0) return fail(MPM_ERR_INVALID, "negative substep count");
@@ -1971,6 +2003,7 @@ int32_t mpm_substep(mpm_ctx *c, float dt, int32_t n_substeps) {
 }
 
 int32_t mpm_substep_timed(mpm_ctx *c, float dt, float *stage_ms, int32_t n_stages) {
+  ZS_RANGE("mpm_substep_timed");
   int32_t rc = check(c);
   if (rc) return rc;
   if (!stage_ms || n_stages < MPM_NUM_STAGES)
@@ -2080,6 +2113,7 @@ int32_t mpm_set_differentiable(mpm_ctx *c, int32_t on) {
 }
 
 int32_t mpm_state_save(mpm_ctx *c, float *dst) {
+  ZS_RANGE("mpm_state_save");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -2092,6 +2126,7 @@ int32_t mpm_state_save(mpm_ctx *c, float *dst) {
 }
 
 int32_t mpm_state_load(mpm_ctx *c, const float *src) {
+  ZS_RANGE("mpm_state_load");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -2111,6 +2146,7 @@ int32_t mpm_state_load(mpm_ctx *c, const float *src) {
 
 int32_t mpm_adjoint_substep(mpm_ctx *c, float dt, const float *adj_next, float *adj_prev,
                             float *grad_mu, float *grad_lam) {
+  ZS_RANGE("mpm_adjoint_substep");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -2273,6 +2309,7 @@ struct PartSwap {
 int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
                             const float *state0, float *ckpts, float *seg_states,
                             float *final_state) {
+  ZS_RANGE("mpm_rollout_forward");
   int32_t rc = check(c);
   if (rc) return rc;
   if (n_substeps < 0 || every <= 0 || !state0 || !final_state || (n_substeps > 0 && !ckpts))
@@ -2373,6 +2410,7 @@ int32_t mpm_rollout_forward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t ev
 int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t every,
                              const float *ckpts, float *seg_states, float *adj, float *adj_tmp,
                              float *grad_mu, float *grad_lam) {
+  ZS_RANGE("mpm_rollout_backward");
   int32_t rc = check(c);
   if (rc) return rc;
   if ((rc = settle(c))) return rc;
@@ -2522,6 +2560,7 @@ int32_t mpm_rollout_backward(mpm_ctx *c, float dt, int32_t n_substeps, int32_t e
 }
 
 int32_t mpm_sync(mpm_ctx *c) {
+  ZS_RANGE("mpm_sync");
   int32_t rc = check(c);
   if (rc) return rc;
   ZS_CUDA(cudaMemcpyAsync(c->h_cnt, c->d.cnt, sizeof(Counters), cudaMemcpyDeviceToHost,
