@@ -281,6 +281,21 @@ enum { MPM_BENDING_VERTEX = 0, MPM_BENDING_ELEMENT = 1, MPM_BENDING_ANGLE = 2 };
 int32_t mpm_cloth_add_bending(mpm_ctx *ctx, int32_t type, float stiffness, float thickness,
                               int64_t *n_out);
 
+/* Checkpoint / resume (a binary, versioned file): the solver state of a
+ * one-scene context -- the particle store in its slot order with the upload
+ * ids, the per-particle beta, the level-set colliders' current poses, the
+ * cloth's and the trackers' state, the substep count -- written to `path`,
+ * and read back into a context made with the same scene, materials,
+ * colliders, cloth mesh and trackers, which then steps exactly as the
+ * uninterrupted run; it then holds the checkpoint's particle count (read
+ * it with mpm_get_stats before a download) (frame caches of the reference: GlobalComm::toDisk,
+ * zeno/src/extra/GlobalComm.cpp:37,277; the reference keeps no solver state).
+ * Read fails with MPM_ERR_INVALID for another format version, a file of
+ * another scene (dx, transfer, collider count, cloth or tracker sizes) or
+ * more particles than the context holds. */
+int32_t mpm_checkpoint_write(mpm_ctx *ctx, const char *path);
+int32_t mpm_checkpoint_read(mpm_ctx *ctx, const char *path);
+
 /* ToTrackerParticles (Generation.cu:105-170): n points (x, optional v,
  * n x 3) that join the partition and are advected in every substep's G2P by
  * the grid velocity (Transfer.cu:1259-1285; the grid's transferred "v" also

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstddef>
 #include <cstdlib>
 #include <cstring>
@@ -2657,6 +2658,208 @@ int32_t mpm_barrier_selftest(mpm_ctx *c, uint64_t barrier_limit, int32_t *timed_
   ZS_CUDA(cudaMemcpyAsync(c->d.cnt, &keep, sizeof(Counters), cudaMemcpyHostToDevice, c->stream));
   ZS_CUDA(cudaStreamSynchronize(c->stream));
   *c->h_cnt = keep;
+  return MPM_OK;
+}
+
+// Checkpoint files: a fixed header, then the blocks in the order written
+// below, each a plain little-endian array.  The particle store goes in its
+// slot order with the upload ids, so a resumed run steps exactly as the
+// uninterrupted one.
+struct CkptHeader {
+  char magic[8];  // "ZSMPMCK1"
+  uint32_t version, nch, nich;
+  int32_t transfer, has_lame, n_colliders;
+  int64_t n, substeps, store_floats, store_ints;
+  float dx;
+  int32_t reserved;
+  int64_t cloth_verts, cloth_eles, trackers;
+};
+constexpr uint32_t kCkptVersion = 1;
+constexpr int kCkptColliderFloats = 10;  // b[3], s, lo[3], hi[3]: the current pose
+
+int32_t mpm_checkpoint_write(mpm_ctx *c, const char *path) {
+  ZS_RANGE("mpm_checkpoint_write");
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!path) return fail(MPM_ERR_INVALID, "null path");
+  if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "checkpoints take a one-scene context");
+  if ((rc = settle(c))) return rc;
+  const DevPtrs &d = c->d;
+  const ClothDev &cl = d.cloth;
+  CkptHeader h{};
+  std::memcpy(h.magic, "ZSMPMCK1", 8);
+  h.version = kCkptVersion;
+  h.nch = NCH;
+  h.nich = NICH;
+  h.transfer = d.transfer;
+  h.has_lame = c->prm.has_lame;
+  h.n_colliders = c->prm.n_colliders;
+  h.n = c->prm.n;
+  h.substeps = c->substeps;
+  h.store_floats = tiled_elems(h.n, NCH);
+  h.store_ints = tiled_elems(h.n, NICH);
+  h.dx = c->scenes[0].dx;
+  h.cloth_verts = cl.n_verts;
+  h.cloth_eles = cl.n_eles;
+  h.trackers = d.n_trackers;
+  std::vector<float> store((size_t)h.store_floats), beta((size_t)h.n);
+  std::vector<int32_t> istore((size_t)h.store_ints);
+  std::vector<ColliderDev> col((size_t)h.n_colliders);
+  ZS_CUDA(cudaMemcpyAsync(store.data(), d.pbuf[c->cur], store.size() * sizeof(float),
+                          cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(istore.data(), d.ibuf[c->cur], istore.size() * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(beta.data(), d.beta, beta.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                          c->stream));
+  if (h.n_colliders > 0)
+    ZS_CUDA(cudaMemcpyAsync(col.data(), d.colliders, col.size() * sizeof(ColliderDev),
+                            cudaMemcpyDeviceToHost, c->stream));
+  // the cloth (vx vv vC ex ev eC eF ed, vertex beta) and the trackers (x, v)
+  const long long nv = cl.n_verts, ne = cl.n_eles, nt = d.n_trackers;
+  std::vector<std::pair<const float *, long long>> extra;
+  if (nv > 0)
+    extra = {{cl.vx, 3 * nv}, {cl.vv, 3 * nv}, {cl.vC, 9 * nv}, {cl.ex, 3 * ne}, {cl.ev, 3 * ne},
+             {cl.eC, 9 * ne}, {cl.eF, 9 * ne}, {cl.ed, 9 * ne}, {cl.vbeta, nv}};
+  if (nt > 0) {
+    extra.push_back({d.tx, 3 * nt});
+    extra.push_back({d.tv, 3 * nt});
+  }
+  std::vector<std::vector<float>> ex(extra.size());
+  for (size_t k = 0; k < extra.size(); ++k) {
+    ex[k].resize((size_t)extra[k].second);
+    ZS_CUDA(cudaMemcpyAsync(ex[k].data(), extra[k].first, ex[k].size() * sizeof(float),
+                            cudaMemcpyDeviceToHost, c->stream));
+  }
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<float> poses((size_t)h.n_colliders * kCkptColliderFloats);
+  for (int k = 0; k < h.n_colliders; ++k) {
+    float *q = &poses[(size_t)k * kCkptColliderFloats];
+    for (int a = 0; a < 3; ++a) {
+      q[a] = col[k].b[a];
+      q[4 + a] = col[k].lo[a];
+      q[7 + a] = col[k].hi[a];
+    }
+    q[3] = col[k].s;
+  }
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(MPM_ERR_INVALID, std::string("cannot open ") + path + " for writing");
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+            std::fwrite(store.data(), sizeof(float), store.size(), f) == store.size() &&
+            std::fwrite(istore.data(), sizeof(int32_t), istore.size(), f) == istore.size() &&
+            std::fwrite(beta.data(), sizeof(float), beta.size(), f) == beta.size() &&
+            std::fwrite(poses.data(), sizeof(float), poses.size(), f) == poses.size();
+  for (size_t k = 0; ok && k < ex.size(); ++k)
+    ok = std::fwrite(ex[k].data(), sizeof(float), ex[k].size(), f) == ex[k].size();
+  ok = std::fclose(f) == 0 && ok;
+  if (!ok) return fail(MPM_ERR_INVALID, std::string("writing ") + path + " failed");
+  return MPM_OK;
+}
+
+int32_t mpm_checkpoint_read(mpm_ctx *c, const char *path) {
+  ZS_RANGE("mpm_checkpoint_read");
+  int32_t rc = check(c);
+  if (rc) return rc;
+  if (!path) return fail(MPM_ERR_INVALID, "null path");
+  if (c->scenes.size() != 1) return fail(MPM_ERR_INVALID, "checkpoints take a one-scene context");
+  if ((rc = settle(c))) return rc;
+  DevPtrs &d = c->d;
+  ClothDev &cl = d.cloth;
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(MPM_ERR_INVALID, std::string("cannot open ") + path);
+  struct Closer {
+    FILE *f;
+    ~Closer() { std::fclose(f); }
+  } closer{f};
+  CkptHeader h{};
+  if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, "ZSMPMCK1", 8) != 0)
+    return fail(MPM_ERR_INVALID, std::string(path) + " is not a checkpoint of this library");
+  if (h.version != kCkptVersion || h.nch != (uint32_t)NCH || h.nich != (uint32_t)NICH)
+    return fail(MPM_ERR_INVALID, "the checkpoint's format version or store layout differs");
+  if (h.n < 0 || h.n > d.cap || h.store_floats != tiled_elems(h.n, NCH) ||
+      h.store_ints != tiled_elems(h.n, NICH))
+    return fail(MPM_ERR_INVALID, "the checkpoint's particles do not fit this context");
+  if (h.dx != c->scenes[0].dx || h.transfer != d.transfer || h.n_colliders != c->prm.n_colliders ||
+      h.cloth_verts != cl.n_verts || h.cloth_eles != cl.n_eles || h.trackers != d.n_trackers)
+    return fail(MPM_ERR_INVALID, "the checkpoint was written by a context with another scene "
+                                 "(dx, transfer, colliders, cloth or trackers)");
+  std::vector<float> store((size_t)h.store_floats), beta((size_t)h.n),
+      poses((size_t)h.n_colliders * kCkptColliderFloats);
+  std::vector<int32_t> istore((size_t)h.store_ints);
+  bool ok = std::fread(store.data(), sizeof(float), store.size(), f) == store.size() &&
+            std::fread(istore.data(), sizeof(int32_t), istore.size(), f) == istore.size() &&
+            std::fread(beta.data(), sizeof(float), beta.size(), f) == beta.size() &&
+            std::fread(poses.data(), sizeof(float), poses.size(), f) == poses.size();
+  const long long nv = cl.n_verts, ne = cl.n_eles, nt = d.n_trackers;
+  std::vector<std::pair<float *, long long>> extra;
+  if (nv > 0)
+    extra = {{cl.vx, 3 * nv}, {cl.vv, 3 * nv}, {cl.vC, 9 * nv}, {cl.ex, 3 * ne}, {cl.ev, 3 * ne},
+             {cl.eC, 9 * ne}, {cl.eF, 9 * ne}, {cl.ed, 9 * ne}, {cl.vbeta, nv}};
+  if (nt > 0) {
+    extra.push_back({d.tx, 3 * nt});
+    extra.push_back({d.tv, 3 * nt});
+  }
+  std::vector<std::vector<float>> ex(extra.size());
+  for (size_t k = 0; ok && k < extra.size(); ++k) {
+    ex[k].resize((size_t)extra[k].second);
+    ok = std::fread(ex[k].data(), sizeof(float), ex[k].size(), f) == ex[k].size();
+  }
+  if (!ok) return fail(MPM_ERR_INVALID, std::string(path) + " is truncated");
+  // the ids index per-particle arrays and the materials the parameter table:
+  // a file that breaks either is refused before anything reaches the device
+  std::vector<char> seen((size_t)h.n, 0);
+  for (long long p = 0; p < h.n; ++p) {
+    const int32_t id = istore[(size_t)iidx(IC_ID, p)], mat = istore[(size_t)iidx(IC_MAT, p)];
+    if (id < 0 || id >= h.n || seen[(size_t)id] || mat < 0 || mat >= c->n_materials)
+      return fail(MPM_ERR_INVALID, std::string(path) + " holds invalid particle ids or materials");
+    seen[(size_t)id] = 1;
+  }
+  // the colliders' current poses into their device entries (the samples and
+  // the rates stay the context's own)
+  std::vector<ColliderDev> col((size_t)h.n_colliders);
+  if (h.n_colliders > 0) {
+    ZS_CUDA(cudaMemcpy(col.data(), d.colliders, col.size() * sizeof(ColliderDev),
+                       cudaMemcpyDeviceToHost));
+    for (int k = 0; k < h.n_colliders; ++k) {
+      const float *q = &poses[(size_t)k * kCkptColliderFloats];
+      for (int a = 0; a < 3; ++a) {
+        col[k].b[a] = q[a];
+        col[k].lo[a] = q[4 + a];
+        col[k].hi[a] = q[7 + a];
+      }
+      col[k].s = q[3];
+    }
+  }
+  ZS_CUDA(cudaMemcpyAsync(d.pbuf[c->cur], store.data(), store.size() * sizeof(float),
+                          cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(d.ibuf[c->cur], istore.data(), istore.size() * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaMemcpyAsync(d.beta, beta.data(), beta.size() * sizeof(float), cudaMemcpyHostToDevice,
+                          c->stream));
+  if (h.n_colliders > 0)
+    ZS_CUDA(cudaMemcpyAsync(d.colliders, col.data(), col.size() * sizeof(ColliderDev),
+                            cudaMemcpyHostToDevice, c->stream));
+  for (size_t k = 0; k < ex.size(); ++k)
+    ZS_CUDA(cudaMemcpyAsync(extra[k].first, ex[k].data(), ex[k].size() * sizeof(float),
+                            cudaMemcpyHostToDevice, c->stream));
+  ZS_CUDA(cudaMemsetAsync(d.vms, 0, (size_t)std::max<long long>(h.n, 1) * sizeof(float),
+                          c->stream));
+  // a fresh store, as after an upload: status word, substep gate, directory
+  ZS_CUDA(cudaMemsetAsync(&d.cnt->status, 0, sizeof(int), c->stream));
+  ZS_CUDA(cudaMemsetAsync(&d.cnt->halt, 0, 2 * sizeof(int), c->stream));
+  ZS_CUDA(cudaStreamSynchronize(c->stream));
+  c->prm.n = h.n;
+  c->prm.has_lame = h.has_lame;
+  c->scenes[0].p_off = 0;
+  c->prm_dirty = true;
+  if ((rc = push_params(c))) return rc;
+  c->pending.clear();
+  c->pending_total = 0;
+  c->started_base = 0;
+  c->substeps = h.substeps;
+  c->needs_full_clear = true;  // the directory counts described the old positions
+  c->binned = false;
+  c->partition_valid = false;
+  drop_graphs(c);
   return MPM_OK;
 }
 

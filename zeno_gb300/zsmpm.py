@@ -80,7 +80,7 @@ EXPORTS = ["mpm_abi_version", "mpm_last_error", "mpm_ctx_create", "mpm_ctx_destr
            "mpm_apply_collider", "mpm_set_transfer", "mpm_compute_particle_beta",
            "mpm_particles_get_attr", "mpm_particles_set_attr", "mpm_compute_von_mises",
            "mpm_frame_begin", "mpm_frame_wait", "mpm_cloth_create", "mpm_cloth_download",
-           "mpm_cloth_upload",
+           "mpm_cloth_upload", "mpm_checkpoint_write", "mpm_checkpoint_read",
            "mpm_cloth_add_bending",
            "mpm_trackers_create", "mpm_trackers_download",
            "mpm_g2p", "mpm_return_mapping",
@@ -148,6 +148,8 @@ def load(path: str = LIB_PATH):
         "mpm_trackers_download": ([P, P, P], i32),
         "mpm_cloth_download": ([P] + [P] * 8, i32),
         "mpm_cloth_upload": ([P] + [P] * 8, i32),
+        "mpm_checkpoint_write": ([P, C.c_char_p], i32),
+        "mpm_checkpoint_read": ([P, C.c_char_p], i32),
         "mpm_frame_begin": ([P, P, P], i32),
         "mpm_frame_wait": ([P], i32),
         "mpm_apply_collider": ([P, i32], i32),
@@ -337,6 +339,16 @@ class Context:
                                                          ("vx", "vv", "vC", "ex", "ev", "eC",
                                                           "eF", "ed")]), "mpm_cloth_download")
         return out
+
+    def checkpoint_write(self, path: str):
+        """The solver state to a file (mpm_checkpoint_write)."""
+        self._check(self._L.mpm_checkpoint_write(self.h, os.fsencode(path)),
+                    "mpm_checkpoint_write")
+
+    def checkpoint_read(self, path: str):
+        """The solver state from a file of a context with the same scene."""
+        self._check(self._L.mpm_checkpoint_read(self.h, os.fsencode(path)), "mpm_checkpoint_read")
+        self.n = self.stats()["n_particles"]  # the checkpoint's particles
 
     def cloth_upload(self, state: dict):
         """The inverse of cloth_download: arrays given by key (vx, vv, vC,
