@@ -140,6 +140,27 @@ def test_cloth_rejects_differentiable_form(zsmpm_mod):
             ctx.set_differentiable(True)
 
 
+def test_cloth_block_capacity_is_reported(zsmpm_mod):
+    """A cloth whose points spread over more blocks than its own partition
+    holds (its starting blocks x 8, at least 1,024): the substep ends with a
+    capacity error instead of losing the points of the blocks left out."""
+    scene = S.Scene.unit_box(1.0 / 64, materials=[S.Material()])
+    mesh = _sheet(n=40)
+    nv, ne = mesh.x.shape[0], mesh.tris.shape[0]
+    # one vertex per interior block of the 16^3-block directory
+    i = np.arange(nv)
+    blocks = np.stack([1 + i % 14, 1 + (i // 14) % 14, 1 + i // 196], axis=1)
+    vx = ((blocks + 0.5) * 4.0 * scene.dx).astype(np.float32)
+    ex = vx[mesh.tris].mean(axis=1).astype(np.float32)
+    with zsmpm_mod.Context(scene, max_particles=1) as ctx:
+        ctx.upload(_empty())
+        ctx.add_cloth(mesh)
+        ctx.cloth_upload({"vx": vx, "ex": ex, "vv": np.zeros((nv, 3)), "ev": np.zeros((ne, 3))})
+        ctx.substep(scene.dt, 1)
+        with pytest.raises(zsmpm_mod.MPMError, match="capacity"):
+            ctx.sync()
+
+
 @pytest.mark.parametrize("fused", [False, True])
 def test_node_graph_cloth(zsmpm_mod, oracle_mod, fused):
     """ConfigConstitutiveModel -> ToZSParticles + ToZSCloth, stepped by the
