@@ -597,6 +597,38 @@ def sand_form(zsmpm, dev: int, steps: int = 128, ckpt: int = 8):
             "checkpoint_bytes": sim.peak_checkpoint_bytes, "plain_status": st["status"]}
 
 
+def parity_long(n_substeps: int, dev: int):
+    """The plain 2,097,152-particle workload against the FP64 oracle over its
+    own length: relative L2 of positions and velocities at 1, 10, 100, ...
+    and n_substeps substeps (the error's growth).  Prints one JSON line."""
+    from oracle import oracle
+    from zeno_gb300 import zsmpm
+    oracle.build()
+    scene, parts = make_workload()
+    ks = [k for k in (1, 10, 100, 1000, 10000) if k < n_substeps] + [n_substeps]
+    xs, vs, done = [], [], 0
+    with zsmpm.Context(scene, max_particles=parts.n, device=dev) as ctx:
+        ctx.upload(parts)
+        for k in ks:
+            ctx.substep(scene.dt, k - done)
+            done = k
+            o = ctx.download(("x", "v"))
+            xs.append(o["x"])
+            vs.append(o["v"])
+        st = ctx.stats()
+    growth, ref, done = [], parts, 0
+    t0 = time.perf_counter()
+    for k, x_k, v_k in zip(ks, xs, vs):
+        ref, ost = oracle.run(scene, ref, k - done, "f64")
+        done = k
+        growth.append({"substeps": k, "rel_l2_x": rel_l2(x_k, ref.x), "rel_l2_v": rel_l2(v_k, ref.v),
+                       "oracle_status": ost["status"]})
+    print(json.dumps({"parity_long": WORKLOAD, "particles": parts.n, "reference": "FP64 oracle",
+                      "gpu_status": st["status"], "growth": growth,
+                      "oracle_s": time.perf_counter() - t0}))
+    return 0 if st["status"] == 0 and all(g["oracle_status"] == 0 for g in growth) else 1
+
+
 def profile_case(kind: str, dev: int):
     """A few substeps of a small case for an ncu capture (no timing):
     'persistent_262k' is the four-material scene at 1/8 scale (262,144
@@ -1049,9 +1081,13 @@ def main():
                     help="run one forward + backward of a differentiable rollout only: for ncu")
     ap.add_argument("--profile-case", default=None, choices=["persistent_262k", "cloth"],
                     help="run a few substeps of a small case only: for ncu")
+    ap.add_argument("--parity-long", type=int, default=0, metavar="N",
+                    help="only compare N substeps of the workload with the FP64 oracle")
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args.profile_case, 0)
+    if args.parity_long > 0:
+        return parity_long(args.parity_long, 0)
     if args.diff_profile:
         import torch
         torch.cuda.set_device(0)
