@@ -629,6 +629,53 @@ def parity_long(n_substeps: int, dev: int):
     return 0 if st["status"] == 0 and all(g["oracle_status"] == 0 for g in growth) else 1
 
 
+def parity_config(cfg: int, dev: int):
+    """Config 3 (the 256-scene batched workload, every scene, 200 substeps) or
+    config 5's forward (the 16,777,216-particle sand column thrown at the
+    floor, 128 substeps) against the FP64 oracle at its own size and length.
+    Prints one JSON line."""
+    from oracle import oracle
+    from zeno_gb300 import scenes, zsmpm
+    oracle.build()
+    if cfg == 3:
+        pairs = scenes.batched_workload()
+        scns, mats, parts, offs = zsmpm.concat_scenes(pairs)
+        steps, dt = 200, pairs[0][0].dt
+        with zsmpm.BatchContext(scns, mats, max_particles=parts.n, device=dev) as ctx:
+            ctx.upload_batch(parts, offs)
+            ctx.substep(dt, steps)
+            ctx.sync()
+            st = ctx.stats()
+            out = ctx.download()
+        cases = [(sc, p, slice(offs[k], offs[k + 1])) for k, (sc, p) in enumerate(pairs) if p.n]
+    else:
+        scene, parts = scenes.sand_column()
+        parts.v = scenes.sand_velocity(parts.n).astype(np.float32)
+        steps = 128
+        with zsmpm.Context(scene, max_particles=parts.n, device=dev,
+                           max_grid_blocks=max(65536, parts.n // 128)) as ctx:
+            ctx.upload(parts)
+            ctx.substep(scene.dt, steps)
+            ctx.sync()
+            st = ctx.stats()
+            out = ctx.download(("x", "v"))
+        cases = [(scene, parts, slice(0, parts.n))]
+    t0 = time.perf_counter()
+    ex, ev, bad = [], [], 0
+    for sc, p, sl in cases:
+        ref, ost = oracle.run(sc, p, steps, "f64")
+        ex.append(rel_l2(out["x"][sl], ref.x))
+        ev.append(rel_l2(out["v"][sl], ref.v))
+        bad += ost["status"] != 0
+    print(json.dumps({"parity_config": cfg, "substeps": steps, "cases": len(cases),
+                      "particles": int(parts.n), "reference": "FP64 oracle",
+                      "gpu_status": st["status"], "oracle_failures": bad,
+                      "max_rel_l2_x": max(ex), "max_rel_l2_v": max(ev),
+                      "median_rel_l2_x": float(np.median(ex)), "median_rel_l2_v": float(np.median(ev)),
+                      "oracle_s": time.perf_counter() - t0}))
+    return 0 if st["status"] == 0 and bad == 0 else 1
+
+
 def profile_case(kind: str, dev: int):
     """A few substeps of a small case for an ncu capture (no timing):
     'persistent_262k' is the four-material scene at 1/8 scale (262,144
@@ -1083,7 +1130,12 @@ def main():
                     help="run a few substeps of a small case only: for ncu")
     ap.add_argument("--parity-long", type=int, default=0, metavar="N",
                     help="only compare N substeps of the workload with the FP64 oracle")
+    ap.add_argument("--parity-config", type=int, default=0, choices=[3, 5],
+                    help="only compare config 3 (batched) or config 5's forward (sand) with "
+                         "the FP64 oracle at their own sizes and lengths")
     args = ap.parse_args()
+    if args.parity_config:
+        return parity_config(args.parity_config, 0)
     if args.profile_case:
         return profile_case(args.profile_case, 0)
     if args.parity_long > 0:
