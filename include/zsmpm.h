@@ -292,7 +292,9 @@ int32_t mpm_cloth_add_bending(mpm_ctx *ctx, int32_t type, float stiffness, float
  * zeno/src/extra/GlobalComm.cpp:37,277; the reference keeps no solver state).
  * Read fails with MPM_ERR_INVALID for another format version, a file of
  * another scene (dx, transfer, collider count, cloth or tracker sizes) or
- * more particles than the context holds. */
+ * more particles than the context holds.  The block directory is not part of
+ * the state (the physics does not depend on it): the reading context's must
+ * cover the particles, or grow (mpm_set_auto_regrow). */
 int32_t mpm_checkpoint_write(mpm_ctx *ctx, const char *path);
 int32_t mpm_checkpoint_read(mpm_ctx *ctx, const char *path);
 
