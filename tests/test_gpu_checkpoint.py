@@ -110,3 +110,31 @@ def test_foreign_or_broken_files_are_refused(zsmpm_mod, tmp_path):
     with zsmpm_mod.Context(scene, max_particles=parts.n // 2) as small:
         with pytest.raises(zsmpm_mod.MPMError, match="do not fit"):
             small.checkpoint_read(path)
+
+
+def test_resume_into_a_growing_directory(zsmpm_mod, tmp_path):
+    """A block thrown out of its starting directory: the checkpoint is taken
+    after the directory grew; a fresh context with the starting directory
+    and growth on resumes it (growing at its first substep) and ends as the
+    uninterrupted run."""
+    from .test_gpu_regrow import _thrown_block, _tight
+    scene, parts = _thrown_block(v=(6.0, 0.0, 0.0))
+    tight = _tight(scene, parts)
+    path = str(tmp_path / "grown.ckpt")
+    with zsmpm_mod.Context(tight, max_particles=parts.n) as a:
+        a.set_auto_regrow(True)
+        a.upload(parts)
+        a.substep(scene.dt, 200)
+        a.checkpoint_write(path)
+        assert a.domain()[2] >= 1
+        a.substep(scene.dt, 100)
+        a.sync()
+        ref = a.download(KEYS)
+    with zsmpm_mod.Context(tight, max_particles=parts.n) as b:
+        b.set_auto_regrow(True)
+        b.checkpoint_read(path)
+        b.substep(scene.dt, 100)
+        b.sync()
+        assert b.stats()["status"] == 0 and b.stats()["substeps"] == 300
+        out = b.download(KEYS)
+    _compare(out, ref)
