@@ -1,7 +1,8 @@
 """Device-side failure detection without faulting the GPU.
 
 Bad inputs are made on the host (a particle outside the block directory, a
-NaN position, a grid capacity that is too small); the kernels turn each into
+NaN position of a particle, a cloth vertex or a tracker, a grid capacity that
+is too small); the kernels turn each into
 a status bit, the C ABI returns the matching error code, and the same
 context keeps working after a fresh upload.
 """
@@ -48,6 +49,36 @@ def test_nan_position(zsmpm_mod):
         ctx.upload(parts)
         ctx.substep(scene.dt, 3)
         ctx.sync()
+
+
+def test_nan_in_cloth_and_trackers(zsmpm_mod):
+    """A non-finite cloth vertex (restored from a state with one NaN) or
+    tracker point: the substep reports MPM_ERR_NAN; with the cloth's state
+    and the particles replaced, the same context steps again."""
+    scene, parts = _scene()
+    mesh = S.cloth_sheet((0.5, 0.62, 0.5), 0.2, 8, model=S.FCR, E=3e4, nu=0.3, density=500.0,
+                         gamma=100.0, k=800.0, fa=30.0, dc=0.05)
+    with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+        ctx.upload(parts)
+        ctx.add_cloth(mesh)
+        good = ctx.cloth_download()
+        vx = good["vx"].copy()
+        vx[5, 0] = np.nan
+        ctx.cloth_upload({"vx": vx})
+        ctx.substep(scene.dt, 1)
+        _expect(zsmpm_mod, ctx, 6, ctx.sync)
+        ctx.cloth_upload(good)
+        ctx.upload(parts)
+        ctx.substep(scene.dt, 3)
+        ctx.sync()
+        assert np.isfinite(ctx.cloth_download()["vx"]).all()
+    pts = parts.x[::50].copy()
+    pts[2, 2] = np.nan
+    with zsmpm_mod.Context(scene, max_particles=parts.n) as ctx:
+        ctx.upload(parts)
+        ctx.add_trackers(pts)
+        ctx.substep(scene.dt, 1)
+        _expect(zsmpm_mod, ctx, 6, ctx.sync)
 
 
 def test_grid_capacity(zsmpm_mod):
