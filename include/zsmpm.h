@@ -286,7 +286,7 @@ int32_t mpm_cloth_add_bending(mpm_ctx *ctx, int32_t type, float stiffness, float
  * ids, the per-particle beta, the level-set colliders' current poses, the
  * cloth's and the trackers' state, the substep count -- written to `path`,
  * and read back into a context made with the same scene, materials,
- * colliders, cloth mesh and trackers, which then steps exactly as the
+ * colliders, boundary grid, cloth mesh and trackers, which then steps exactly as the
  * uninterrupted run; it then holds the checkpoint's particle count (read
  * it with mpm_get_stats before a download) (frame caches of the reference: GlobalComm::toDisk,
  * zeno/src/extra/GlobalComm.cpp:37,277; the reference keeps no solver state).
