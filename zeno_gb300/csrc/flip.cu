@@ -598,8 +598,9 @@ template <bool kAffine> constexpr int fg2p_smem_bytes() {
 // kHencky: the von Mises / Cam-Clay return mappings are compiled in (only
 // for contexts whose materials use them; Drucker-Prager alone keeps the
 // register count down)
+// CTAs per SM: AFLIP fits 5 (96 registers); FLIP's staged C holds it at 4
 template <bool kAffine, bool kFuseRM, bool kFuseBin, bool kHencky>
-__global__ void __launch_bounds__(kFG2PThreads, 4)
+__global__ void __launch_bounds__(kFG2PThreads, kAffine ? 5 : 4)
     k_g2p_flip(DevPtrs d, const float *__restrict__ pin, const int32_t *__restrict__ iin,
                float *__restrict__ pout, int32_t *__restrict__ iout) {
   if (ZSMPM_HALTED(d)) return;
@@ -979,17 +980,20 @@ template <class K> static int occupancy(K kernel, int threads, int smem) {
 void configure_flip_launches(DevPtrs &d) {
   const int a = std::min(occupancy(k_p2g_flip<true>, kFThreads, FLayout<true>::bytes),
                          occupancy(k_p2g_flip<false>, kFThreads, FLayout<false>::bytes));
-  int g = occupancy(k_g2p_flip<true, true, true, false>, kFG2PThreads, fg2p_smem_bytes<true>());
-  g = std::min(g, occupancy(k_g2p_flip<false, true, true, false>, kFG2PThreads,
-                            fg2p_smem_bytes<false>()));
-  g = std::min(g, occupancy(k_g2p_flip<true, true, true, true>, kFG2PThreads,
-                            fg2p_smem_bytes<true>()));
-  g = std::min(g, occupancy(k_g2p_flip<false, true, true, true>, kFG2PThreads,
-                            fg2p_smem_bytes<false>()));
-  occupancy(k_g2p_flip<true, false, false, false>, kFG2PThreads, fg2p_smem_bytes<true>());
-  occupancy(k_g2p_flip<false, false, false, false>, kFG2PThreads, fg2p_smem_bytes<false>());
+  // the G2P grids: as many CTAs as every instance of the transfer holds
+  int ga = occupancy(k_g2p_flip<true, true, true, false>, kFG2PThreads, fg2p_smem_bytes<true>());
+  ga = std::min(ga, occupancy(k_g2p_flip<true, true, true, true>, kFG2PThreads,
+                              fg2p_smem_bytes<true>()));
+  ga = std::min(ga, occupancy(k_g2p_flip<true, false, false, false>, kFG2PThreads,
+                              fg2p_smem_bytes<true>()));
+  int gf = occupancy(k_g2p_flip<false, true, true, false>, kFG2PThreads, fg2p_smem_bytes<false>());
+  gf = std::min(gf, occupancy(k_g2p_flip<false, true, true, true>, kFG2PThreads,
+                              fg2p_smem_bytes<false>()));
+  gf = std::min(gf, occupancy(k_g2p_flip<false, false, false, false>, kFG2PThreads,
+                              fg2p_smem_bytes<false>()));
   d.grid_p2g_flip = d.num_sms * a;
-  d.grid_g2p_flip = d.num_sms * g;
+  d.grid_g2p_flip = d.num_sms * gf;
+  d.grid_g2p_aflip = d.num_sms * ga;
 }
 
 void launch_p2g_flip(const DevPtrs &d, int cur, cudaStream_t s) {
@@ -1010,7 +1014,7 @@ void launch_grid_update_flip(const DevPtrs &d, int mode, cudaStream_t s) {
 void launch_g2p_flip(const DevPtrs &d, int cur, int fuse_rm, int fuse_bin, cudaStream_t s) {
   float *pi = d.pbuf[cur], *po = d.pbuf[1 - cur];
   int32_t *ii = d.ibuf[cur], *io = d.ibuf[1 - cur];
-  const int grid = d.grid_g2p_flip;
+  const int grid = d.transfer == MPM_TRANSFER_AFLIP ? d.grid_g2p_aflip : d.grid_g2p_flip;
   if (d.transfer == MPM_TRANSFER_AFLIP) {
     constexpr int smem = fg2p_smem_bytes<true>();
     if (fuse_rm && fuse_bin && d.hencky)
