@@ -86,8 +86,10 @@ template <bool kAffine> struct FLayout {
   static_assert(rec4 % 16 == 0 && meta % 16 == 0, "float4 regions must be 16-byte aligned");
 };
 
+// CTAs per SM: FLIP fits 4 at 80 registers; AFLIP's affine records would
+// spill there, so it keeps 3
 template <bool kAffine>
-__global__ void __launch_bounds__(kFThreads, 3)
+__global__ void __launch_bounds__(kFThreads, kAffine ? 3 : 4)
     k_p2g_flip(DevPtrs d, const float *__restrict__ pin) {
   if (ZSMPM_HALTED(d)) return;
   using RC = FRaw<kAffine>;
@@ -978,8 +980,8 @@ template <class K> static int occupancy(K kernel, int threads, int smem) {
 }
 
 void configure_flip_launches(DevPtrs &d) {
-  const int a = std::min(occupancy(k_p2g_flip<true>, kFThreads, FLayout<true>::bytes),
-                         occupancy(k_p2g_flip<false>, kFThreads, FLayout<false>::bytes));
+  const int pa = occupancy(k_p2g_flip<true>, kFThreads, FLayout<true>::bytes),
+            pf = occupancy(k_p2g_flip<false>, kFThreads, FLayout<false>::bytes);
   // the G2P grids: as many CTAs as every instance of the transfer holds
   int ga = occupancy(k_g2p_flip<true, true, true, false>, kFG2PThreads, fg2p_smem_bytes<true>());
   ga = std::min(ga, occupancy(k_g2p_flip<true, true, true, true>, kFG2PThreads,
@@ -991,14 +993,15 @@ void configure_flip_launches(DevPtrs &d) {
                               fg2p_smem_bytes<false>()));
   gf = std::min(gf, occupancy(k_g2p_flip<false, false, false, false>, kFG2PThreads,
                               fg2p_smem_bytes<false>()));
-  d.grid_p2g_flip = d.num_sms * a;
+  d.grid_p2g_flip = d.num_sms * pf;
+  d.grid_p2g_aflip = d.num_sms * pa;
   d.grid_g2p_flip = d.num_sms * gf;
   d.grid_g2p_aflip = d.num_sms * ga;
 }
 
 void launch_p2g_flip(const DevPtrs &d, int cur, cudaStream_t s) {
   if (d.transfer == MPM_TRANSFER_AFLIP)
-    k_p2g_flip<true><<<d.grid_p2g_flip, kFThreads, FLayout<true>::bytes, s>>>(d, d.pbuf[cur]);
+    k_p2g_flip<true><<<d.grid_p2g_aflip, kFThreads, FLayout<true>::bytes, s>>>(d, d.pbuf[cur]);
   else
     k_p2g_flip<false><<<d.grid_p2g_flip, kFThreads, FLayout<false>::bytes, s>>>(d, d.pbuf[cur]);
 }

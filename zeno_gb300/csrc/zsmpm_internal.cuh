@@ -295,7 +295,8 @@ struct DevPtrs {
   int grid_sort, grid_stream, g2p_threads;
   int transfer;                      // MPM_TRANSFER_* (host copy of SimParams::transfer)
   int hencky;  // some material uses the von Mises / Cam-Clay return mapping
-  int grid_p2g_flip, grid_g2p_flip, grid_g2p_aflip;  // persistent grids of the FLIP kernels
+  // persistent grids of the FLIP and AFLIP transfer kernels
+  int grid_p2g_flip, grid_p2g_aflip, grid_g2p_flip, grid_g2p_aflip;
   int grid_persist;  // CTAs of the persistent substep kernel (0: it cannot run)
   // boundary grid (mpm_set_grid_boundary; null: none): per directory entry
   // its boundary block or -1, per boundary node (m, v) then (nrm, 0)
